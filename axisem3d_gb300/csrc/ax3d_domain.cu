@@ -1,0 +1,769 @@
+// ax3d_domain.cu -- host runtime behind include/ax3d.h: the GB300 Domain.
+//
+// Mirrors the reference's Domain (SOLVER/src/core/domain/Domain.h:20-125): it owns the
+// points, elements, source terms, source-time function and receivers, and runs the
+// Newmark::solve loop body (SOLVER/src/core/newmark/Newmark.cpp:47-93) on one CUDA
+// stream.  Set-up data arrive as structure-of-arrays host buffers, are validated and
+// packed once in ax3d_finalize (the counterpart of Mesh::release), and stay resident in
+// HBM for the whole run.  There is no CPU fallback: a failed CUDA call is an error.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/ax3d.h"
+#include "ax3d_kernels.cuh"
+
+namespace {
+
+thread_local std::string g_err;
+
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+#define CK(call)                                                                                 \
+    do {                                                                                         \
+        cudaError_t e_ = (call);                                                                 \
+        if (e_ != cudaSuccess)                                                                   \
+            throw Error(AX3D_ERR_CUDA, std::string(#call) + " || " + cudaGetErrorString(e_)); \
+    } while (0)
+
+template <typename T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    void alloc(size_t count) {
+        free();
+        n = count;
+        if (count) CK(cudaMalloc(&p, count * sizeof(T)));
+    }
+    void upload(const std::vector<T> &v, cudaStream_t s) {
+        alloc(v.size());
+        if (n) CK(cudaMemcpyAsync(p, v.data(), n * sizeof(T), cudaMemcpyHostToDevice, s));
+    }
+    void zero(cudaStream_t s) {
+        if (n) CK(cudaMemsetAsync(p, 0, n * sizeof(T), s));
+    }
+    void free() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    ~DevBuf() { free(); }
+};
+
+int n_moduli(int mat) {
+    switch (mat) {
+        case AX3D_MAT_ISO: return 2;
+        case AX3D_MAT_TISO: return 5;
+        case AX3D_MAT_ANISO: return 21;
+        case AX3D_MAT_ACOUSTIC: return 1;
+    }
+    throw Error(AX3D_ERR_ARG, "ax3d_add_elements || unknown material");
+}
+
+}  // namespace
+
+struct ax3d_domain {
+    // ---------------- configuration ----------------
+    int device = 0;
+    double dt = 0.;
+    float g_gll[25], g_glj[25];
+    ax3d::SLS sls{};
+    int kahan = 0;
+    int stab_interval = 0;
+    cudaStream_t stream = nullptr;
+    bool finalized = false;
+    int tstep = 1;
+
+    // ---------------- host staging ----------------
+    std::vector<int32_t> p_nr;
+    std::vector<int8_t> p_kind;
+    std::vector<uint8_t> p_axial, p_fsurf;
+    std::vector<int32_t> p_mslen, p_mflen, p_sflen;
+    std::vector<int64_t> p_msofs, p_mfofs, p_sfofs;
+    std::vector<float> p_ms, p_mf, p_sfn, p_sfni;
+
+    std::vector<int32_t> e_pts, e_flags, e_nr;
+    std::vector<float> e_geo, e_trig;
+    std::vector<int64_t> e_mofs, e_aofs;
+    std::vector<float> e_mod, e_attm;
+
+    std::vector<int32_t> s_elem, s_nord;
+    std::vector<int64_t> s_ofs;
+    std::vector<float> s_force;  // complex interleaved
+    std::vector<float> stf;
+
+    std::vector<int32_t> r_elem;
+    std::vector<float> r_phi, r_w;
+
+    // ---------------- device ----------------
+    DevBuf<int32_t> d_pnr, d_mslen, d_mflen, d_sflen, d_sg_ptr, d_fg_ptr, d_srow, d_frow;
+    DevBuf<int8_t> d_pkind;
+    DevBuf<uint8_t> d_paxial, d_pfsurf;
+    DevBuf<int64_t> d_sofs, d_fofs, d_msofs, d_mfofs, d_sfofs, d_sg_ref, d_fg_ref;
+    DevBuf<float> d_ms, d_mf, d_sfn, d_sfni;
+    DevBuf<int32_t> d_epts, d_eflags, d_enr;
+    DevBuf<float> d_geo, d_trig, d_mod, d_attm, d_mem;
+    DevBuf<int64_t> d_mofs, d_aofs, d_memofs, d_efofs, d_twofs;
+    DevBuf<float2> d_ef, d_tw;
+    DevBuf<float2> d_su, d_sv, d_sa, d_ss, d_sku, d_skv, d_fu, d_fv, d_fa, d_fs, d_fku, d_fkv;
+    DevBuf<int2> d_items_s, d_items_f;
+    std::vector<ax3d::PhysBucket> buckets_s, buckets_f;
+    std::vector<DevBuf<int32_t>> bucket_lists;
+    DevBuf<int32_t> d_pts3d, d_sf3d;
+    int n_pts3d = 0, n_sf3d = 0;
+    DevBuf<int32_t> d_selem, d_snord;
+    DevBuf<int64_t> d_sofs_src;
+    DevBuf<float2> d_sforce;
+    DevBuf<float> d_stf;
+    DevBuf<int32_t> d_relem;
+    DevBuf<float> d_rphi, d_rw, d_seis;
+    int seis_cap = 0;
+    DevBuf<int32_t> d_flag;
+
+    ax3d::ElemTable T{};
+    ax3d::PointTable P{};
+    ax3d::Fields F{};
+    int64_t nsolid = 0, nfluid = 0;  // complex sizes
+    int nitems_s = 0, nitems_f = 0;
+
+    ~ax3d_domain() {
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    // ================================================================
+    void add_points(int n, const int32_t *nr, const int8_t *kind, const uint8_t *axial,
+                    const uint8_t *fsurf, const int32_t *msl, const float *ms, const int32_t *mfl,
+                    const float *mf, const int32_t *sfl, const float *sfn, const float *sfni) {
+        if (finalized) throw Error(AX3D_ERR_STATE, "ax3d_add_points || domain already finalized");
+        if (n < 0 || !nr || !kind || !axial || !msl || !mfl)
+            throw Error(AX3D_ERR_ARG, "ax3d_add_points || null argument");
+        int64_t om = 0, of = 0, osf = 0;
+        for (int i = 0; i < n; i++) {
+            const int r = nr[i], k = kind[i];
+            if (r < 1) throw Error(AX3D_ERR_ARG, "ax3d_add_points || nr must be >= 1");
+            if (k < 0 || k > 2) throw Error(AX3D_ERR_ARG, "ax3d_add_points || bad point kind");
+            const bool hasS = k != AX3D_POINT_FLUID, hasF = k != AX3D_POINT_SOLID;
+            const int ls = msl[i], lf = mfl[i], lsf = sfl ? sfl[i] : 0;
+            if (hasS ? !(ls == 1 || ls == r) : ls != 0)
+                throw Error(AX3D_ERR_ARG, "ax3d_add_points || solid mass length must be 1 or nr");
+            if (hasF ? !(lf == 1 || lf == r) : lf != 0)
+                throw Error(AX3D_ERR_ARG, "ax3d_add_points || fluid mass length must be 1 or nr");
+            if (k == AX3D_POINT_SOLID_FLUID ? !(lsf == 1 || lsf == r) : lsf != 0)
+                throw Error(AX3D_ERR_ARG, "ax3d_add_points || coupling length must be 1 or nr");
+            p_nr.push_back(r);
+            p_kind.push_back((int8_t)k);
+            p_axial.push_back(axial[i] ? 1 : 0);
+            p_fsurf.push_back(fsurf && fsurf[i] ? 1 : 0);
+            p_mslen.push_back(ls);
+            p_msofs.push_back((int64_t)p_ms.size());
+            if (ls) p_ms.insert(p_ms.end(), ms + om, ms + om + ls);
+            om += ls;
+            p_mflen.push_back(lf);
+            p_mfofs.push_back((int64_t)p_mf.size());
+            if (lf) p_mf.insert(p_mf.end(), mf + of, mf + of + lf);
+            of += lf;
+            p_sflen.push_back(lsf);
+            p_sfofs.push_back((int64_t)p_sfn.size() / 3);
+            if (lsf) {
+                p_sfn.insert(p_sfn.end(), sfn + osf * 3, sfn + (osf + lsf) * 3);
+                p_sfni.insert(p_sfni.end(), sfni + osf * 3, sfni + (osf + lsf) * 3);
+            }
+            osf += lsf;
+        }
+    }
+
+    void add_elements(int n, const int32_t *pts, const int8_t *mat, const uint8_t *axial,
+                      const uint8_t *in3d, const float *geo, const float *trig, const int64_t *mofs,
+                      const float *mod, const int8_t *att, const int64_t *aofs, const float *attm) {
+        if (finalized) throw Error(AX3D_ERR_STATE, "ax3d_add_elements || domain already finalized");
+        if (n < 0 || !pts || !mat || !axial || !in3d || !geo || !mofs || !mod)
+            throw Error(AX3D_ERR_ARG, "ax3d_add_elements || null argument");
+        const int npts = (int)p_nr.size();
+        for (int e = 0; e < n; e++) {
+            int nr = -1;
+            bool any_solid = false, any_fluid = false;
+            for (int l = 0; l < 25; l++) {
+                const int p = pts[(int64_t)e * 25 + l];
+                if (p < 0 || p >= npts) throw Error(AX3D_ERR_ARG, "ax3d_add_elements || point index out of range");
+                nr = std::max(nr, p_nr[p]);  // Element.cpp:13-18
+                any_solid |= p_kind[p] != AX3D_POINT_FLUID;
+                any_fluid |= p_kind[p] != AX3D_POINT_SOLID;
+                e_pts.push_back(p);
+            }
+            const int m = mat[e];
+            const int km = n_moduli(m);
+            const bool fluid = m == AX3D_MAT_ACOUSTIC;
+            for (int l = 0; l < 25; l++) {
+                const int p = pts[(int64_t)e * 25 + l];
+                if (fluid && p_kind[p] == AX3D_POINT_SOLID)
+                    throw Error(AX3D_ERR_ARG, "ax3d_add_elements || fluid element on a solid-only point");
+                if (!fluid && p_kind[p] == AX3D_POINT_FLUID)
+                    throw Error(AX3D_ERR_ARG, "ax3d_add_elements || solid element on a fluid-only point");
+            }
+            const int a = (fluid || !att) ? 0 : att[e];
+            if (a < 0 || a > 2) throw Error(AX3D_ERR_ARG, "ax3d_add_elements || bad attenuation kind");
+            if (a && sls.nsls <= 0) throw Error(AX3D_ERR_ARG, "ax3d_add_elements || attenuation without SLS");
+            if ((m == AX3D_MAT_TISO || m == AX3D_MAT_ANISO) && !trig)
+                throw Error(AX3D_ERR_ARG, "ax3d_add_elements || TISO/ANISO need theta tables");
+            const bool e3d = in3d[e] != 0;
+            int flags = (axial[e] ? ax3d::EF_AXIAL : 0) | (e3d ? ax3d::EF_IN3D : 0) |
+                        (fluid ? ax3d::EF_FLUID : 0) | (m << 4) | (a << 8);
+            e_flags.push_back(flags);
+            e_nr.push_back(nr);
+            e_geo.insert(e_geo.end(), geo + (int64_t)e * 125, geo + (int64_t)e * 125 + 125);
+            if (trig)
+                e_trig.insert(e_trig.end(), trig + (int64_t)e * 100, trig + (int64_t)e * 100 + 100);
+            else
+                e_trig.insert(e_trig.end(), 100, 0.f);
+            const int64_t mlen = (int64_t)km * 25 * (e3d ? nr : 1);
+            e_mofs.push_back((int64_t)e_mod.size());
+            e_mod.insert(e_mod.end(), mod + mofs[e], mod + mofs[e] + mlen);
+            const int npa = a == AX3D_ATT_CG4 ? 4 : 25;
+            const int64_t alen = a ? 2LL * npa * (e3d ? nr : 1) : 0;
+            if (a && (!aofs || !attm)) throw Error(AX3D_ERR_ARG, "ax3d_add_elements || attenuation moduli missing");
+            e_aofs.push_back((int64_t)e_attm.size());
+            if (alen) e_attm.insert(e_attm.end(), attm + aofs[e], attm + aofs[e] + alen);
+        }
+    }
+
+    // ================================================================
+    void finalize() {
+        if (finalized) throw Error(AX3D_ERR_STATE, "ax3d_finalize || already finalized");
+        CK(cudaSetDevice(device));
+        CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        ax3d::init_kernel_attributes();
+        ax3d::set_g_matrices(g_gll, g_glj, stream);
+        const int np = (int)p_nr.size(), ne = (int)e_nr.size();
+        // point field offsets and row maps
+        std::vector<int64_t> sofs(np, -1), fofs(np, -1);
+        std::vector<int32_t> srow, frow;
+        for (int p = 0; p < np; p++) {
+            const int na = p_nr[p] / 2 + 1;
+            if (p_kind[p] != AX3D_POINT_FLUID) {
+                sofs[p] = nsolid;
+                nsolid += (int64_t)na * 3;
+                srow.insert(srow.end(), na, p);
+            }
+            if (p_kind[p] != AX3D_POINT_SOLID) {
+                fofs[p] = nfluid;
+                nfluid += na;
+                frow.insert(frow.end(), na, p);
+            }
+        }
+        // element force buffer, memory variables, gather lists, work items, buckets
+        std::vector<int64_t> efofs(ne), memofs(ne);
+        int64_t efsize = 0, memsize = 0;
+        std::vector<std::vector<int64_t>> sref(np), fref(np);
+        std::vector<int2> items_s, items_f;
+        std::map<int, std::vector<int32_t>> phys_s, phys_f;  // keyed by bucket id
+        int nr_max = 1;
+        for (int e = 0; e < ne; e++) {
+            const int nr = e_nr[e], n = nr / 2 + 1, flags = e_flags[e];
+            nr_max = std::max(nr_max, nr);
+            const bool fluid = flags & ax3d::EF_FLUID, e3d = flags & ax3d::EF_IN3D;
+            const int nc = fluid ? 1 : 3;
+            efofs[e] = efsize;
+            for (int l = 0; l < 25; l++) {
+                const int p = e_pts[(int64_t)e * 25 + l];
+                (fluid ? fref : sref)[p].push_back(efsize + (int64_t)l * n * nc);
+            }
+            efsize += (int64_t)25 * n * nc;
+            const int a = ax3d::ef_att(flags), npa = a == AX3D_ATT_CG4 ? 4 : 25;
+            memofs[e] = memsize;
+            if (a) memsize += (int64_t)(sls.nsls + 1) * 6 * npa * (e3d ? nr : 2 * n);
+            if (e3d) {
+                // geometric buckets of nr so shared memory is sized per bucket
+                int b = (int)std::floor(std::log((double)nr) / std::log(1.15));
+                (fluid ? phys_f : phys_s)[b].push_back(e);
+            } else {
+                for (int al = 0; al < n; al++) (fluid ? items_f : items_s).push_back(make_int2(e, al));
+            }
+        }
+        std::vector<int32_t> sg_ptr(np + 1, 0), fg_ptr(np + 1, 0);
+        std::vector<int64_t> sg_ref, fg_ref;
+        for (int p = 0; p < np; p++) {
+            sg_ptr[p + 1] = sg_ptr[p] + (int32_t)sref[p].size();
+            fg_ptr[p + 1] = fg_ptr[p] + (int32_t)fref[p].size();
+            sg_ref.insert(sg_ref.end(), sref[p].begin(), sref[p].end());
+            fg_ref.insert(fg_ref.end(), fref[p].begin(), fref[p].end());
+        }
+        // twiddle tables (cos, sin)(2 pi m / nr) in FP64, for every nr used by 3D elements
+        std::vector<int64_t> twofs(nr_max + 1, 0);
+        std::vector<float2> tw;
+        std::vector<char> used(nr_max + 1, 0);
+        for (int e = 0; e < ne; e++)
+            if (e_flags[e] & ax3d::EF_IN3D) used[e_nr[e]] = 1;
+        for (int r = 1; r <= nr_max; r++) {
+            if (!used[r]) continue;
+            twofs[r] = (int64_t)tw.size();
+            for (int m = 0; m < r; m++) {
+                const double th = 2.0 * M_PI * (double)m / (double)r;
+                tw.push_back(make_float2((float)std::cos(th), (float)std::sin(th)));
+            }
+        }
+        if (tw.empty()) tw.push_back(make_float2(1.f, 0.f));
+        // 3D points (Mass3D) and 3D couplings
+        std::vector<int32_t> pts3d, sf3d;
+        for (int p = 0; p < np; p++) {
+            if ((p_mslen[p] > 1) || (p_mflen[p] > 1)) pts3d.push_back(p);
+            if (p_sflen[p] > 1) sf3d.push_back(p);
+        }
+        // sources
+        for (size_t s = 0; s < s_elem.size(); s++)
+            if (e_flags[s_elem[s]] & ax3d::EF_FLUID)
+                throw Error(AX3D_ERR_ARG, "ax3d_add_source || source in a fluid element");
+
+        cudaStream_t st = stream;
+        d_pnr.upload(p_nr, st);
+        d_pkind.upload(p_kind, st);
+        d_paxial.upload(p_axial, st);
+        d_pfsurf.upload(p_fsurf, st);
+        d_sofs.upload(sofs, st);
+        d_fofs.upload(fofs, st);
+        d_mslen.upload(p_mslen, st);
+        d_msofs.upload(p_msofs, st);
+        d_ms.upload(p_ms.empty() ? std::vector<float>{0.f} : p_ms, st);
+        d_mflen.upload(p_mflen, st);
+        d_mfofs.upload(p_mfofs, st);
+        d_mf.upload(p_mf.empty() ? std::vector<float>{0.f} : p_mf, st);
+        d_sflen.upload(p_sflen, st);
+        d_sfofs.upload(p_sfofs, st);
+        d_sfn.upload(p_sfn.empty() ? std::vector<float>{0.f} : p_sfn, st);
+        d_sfni.upload(p_sfni.empty() ? std::vector<float>{0.f} : p_sfni, st);
+        d_sg_ptr.upload(sg_ptr, st);
+        d_fg_ptr.upload(fg_ptr, st);
+        d_sg_ref.upload(sg_ref.empty() ? std::vector<int64_t>{0} : sg_ref, st);
+        d_fg_ref.upload(fg_ref.empty() ? std::vector<int64_t>{0} : fg_ref, st);
+        d_srow.upload(srow.empty() ? std::vector<int32_t>{0} : srow, st);
+        d_frow.upload(frow.empty() ? std::vector<int32_t>{0} : frow, st);
+        d_epts.upload(e_pts, st);
+        d_eflags.upload(e_flags, st);
+        d_enr.upload(e_nr, st);
+        d_geo.upload(e_geo, st);
+        d_trig.upload(e_trig, st);
+        d_mofs.upload(e_mofs, st);
+        d_mod.upload(e_mod.empty() ? std::vector<float>{0.f} : e_mod, st);
+        d_aofs.upload(e_aofs, st);
+        d_attm.upload(e_attm.empty() ? std::vector<float>{0.f} : e_attm, st);
+        d_memofs.upload(memofs, st);
+        d_mem.alloc(std::max<int64_t>(memsize, 1));
+        d_mem.zero(st);
+        d_efofs.upload(efofs, st);
+        d_ef.alloc(std::max<int64_t>(efsize, 1));
+        d_ef.zero(st);
+        d_tw.upload(tw, st);
+        d_twofs.upload(twofs, st);
+        for (auto *b : {&d_su, &d_sv, &d_sa, &d_ss}) {
+            b->alloc(std::max<int64_t>(nsolid, 1));
+            b->zero(st);
+        }
+        for (auto *b : {&d_fu, &d_fv, &d_fa, &d_fs}) {
+            b->alloc(std::max<int64_t>(nfluid, 1));
+            b->zero(st);
+        }
+        if (kahan) {
+            for (auto *b : {&d_sku, &d_skv}) { b->alloc(std::max<int64_t>(nsolid, 1)); b->zero(st); }
+            for (auto *b : {&d_fku, &d_fkv}) { b->alloc(std::max<int64_t>(nfluid, 1)); b->zero(st); }
+        }
+        d_items_s.upload(items_s, st);
+        d_items_f.upload(items_f, st);
+        nitems_s = (int)items_s.size();
+        nitems_f = (int)items_f.size();
+        bucket_lists.resize(phys_s.size() + phys_f.size());
+        size_t bi = 0;
+        for (int fl = 0; fl < 2; fl++) {
+            auto &src = fl ? phys_f : phys_s;
+            auto &dst = fl ? buckets_f : buckets_s;
+            for (auto &kv : src) {
+                ax3d::PhysBucket b;
+                b.count = (int)kv.second.size();
+                for (int e : kv.second) b.nr_max = std::max(b.nr_max, e_nr[e]);
+                const int nc = fl ? 3 : 6;
+                b.npts_chunk = ax3d::phys_points_per_chunk(b.nr_max, nc);
+                if (b.npts_chunk <= 0)
+                    throw Error(AX3D_ERR_UNSUPPORTED, "ax3d_finalize || nr too large for the physical-space kernel");
+                b.smem = ax3d::phys_smem_bytes(b.nr_max, nc, b.npts_chunk);
+                bucket_lists[bi].upload(kv.second, st);
+                b.elems = bucket_lists[bi].p;
+                bi++;
+                dst.push_back(b);
+            }
+        }
+        n_pts3d = (int)pts3d.size();
+        n_sf3d = (int)sf3d.size();
+        d_pts3d.upload(pts3d.empty() ? std::vector<int32_t>{0} : pts3d, st);
+        d_sf3d.upload(sf3d.empty() ? std::vector<int32_t>{0} : sf3d, st);
+        // sources, stf, receivers
+        d_selem.upload(s_elem.empty() ? std::vector<int32_t>{0} : s_elem, st);
+        d_snord.upload(s_nord.empty() ? std::vector<int32_t>{0} : s_nord, st);
+        d_sofs_src.upload(s_ofs.empty() ? std::vector<int64_t>{0} : s_ofs, st);
+        {
+            std::vector<float2> f(s_force.size() / 2);
+            for (size_t i = 0; i < f.size(); i++) f[i] = make_float2(s_force[2 * i], s_force[2 * i + 1]);
+            d_sforce.upload(f.empty() ? std::vector<float2>{make_float2(0.f, 0.f)} : f, st);
+        }
+        d_stf.upload(stf.empty() ? std::vector<float>{0.f} : stf, st);
+        d_relem.upload(r_elem.empty() ? std::vector<int32_t>{0} : r_elem, st);
+        d_rphi.upload(r_phi.empty() ? std::vector<float>{0.f} : r_phi, st);
+        d_rw.upload(r_w.empty() ? std::vector<float>{0.f} : r_w, st);
+        seis_cap = std::max<int>((int)stf.size(), 1);
+        d_seis.alloc((size_t)seis_cap * std::max<size_t>(r_elem.size(), 1) * 3);
+        d_seis.zero(st);
+        d_flag.alloc(1);
+        d_flag.zero(st);
+
+        P.n = np;
+        P.nr = d_pnr.p;
+        P.kind = d_pkind.p;
+        P.axial = d_paxial.p;
+        P.fsurf = d_pfsurf.p;
+        P.sofs = d_sofs.p;
+        P.fofs = d_fofs.p;
+        P.mslen = d_mslen.p;
+        P.msofs = d_msofs.p;
+        P.ms = d_ms.p;
+        P.mflen = d_mflen.p;
+        P.mfofs = d_mfofs.p;
+        P.mf = d_mf.p;
+        P.sflen = d_sflen.p;
+        P.sfofs = d_sfofs.p;
+        P.sfn = d_sfn.p;
+        P.sfni = d_sfni.p;
+        P.sg_ptr = d_sg_ptr.p;
+        P.sg_ref = d_sg_ref.p;
+        P.fg_ptr = d_fg_ptr.p;
+        P.fg_ref = d_fg_ref.p;
+        P.nsrows = nsolid / 3;
+        P.nfrows = nfluid;
+        P.srow_pt = d_srow.p;
+        P.frow_pt = d_frow.p;
+        T.pts = d_epts.p;
+        T.flags = d_eflags.p;
+        T.nr = d_enr.p;
+        T.geo = d_geo.p;
+        T.trig = d_trig.p;
+        T.mofs = d_mofs.p;
+        T.moduli = d_mod.p;
+        T.aofs = d_aofs.p;
+        T.attm = d_attm.p;
+        T.memofs = d_memofs.p;
+        T.mem = d_mem.p;
+        T.efofs = d_efofs.p;
+        T.ef = d_ef.p;
+        T.twtab = d_tw.p;
+        T.twofs = d_twofs.p;
+        F.su = d_su.p; F.sv = d_sv.p; F.sa = d_sa.p; F.ss = d_ss.p; F.sku = d_sku.p; F.skv = d_skv.p;
+        F.fu = d_fu.p; F.fv = d_fv.p; F.fa = d_fa.p; F.fs = d_fs.p; F.fku = d_fku.p; F.fkv = d_fkv.p;
+        CK(cudaStreamSynchronize(st));
+        finalized = true;
+        tstep = 1;
+    }
+
+    void need_final() const {
+        if (!finalized) throw Error(AX3D_ERR_STATE, "ax3d || domain not finalized");
+    }
+
+    // ================= Domain loop bodies =================
+    void update_newmark() {
+        const double half_dt = 0.5 * dt, half_dt_dt = half_dt * dt;
+        ax3d::launch_newmark(P, F, (float)dt, (float)half_dt, (float)half_dt_dt, kahan, d_pts3d.p, n_pts3d,
+                             stream);
+    }
+    void apply_source(int t) {
+        if (s_elem.empty()) return;
+        if (t < 0 || t >= (int)stf.size()) throw Error(AX3D_ERR_ARG, "ax3d_apply_source || step out of range");
+        ax3d::launch_source(P, T, F, d_selem.p, d_snord.p, d_sofs_src.p, d_sforce.p, (int)s_elem.size(),
+                            d_stf.p, t, stream);
+    }
+    void compute_stiff() {
+        ax3d::launch_elem_fourier_solid(T, P, F.su, d_items_s.p, nitems_s, sls, stream);
+        ax3d::launch_elem_fourier_fluid(T, P, F.fu, d_items_f.p, nitems_f, stream);
+        for (auto &b : buckets_s) ax3d::launch_elem_phys_solid(T, P, F.su, b, sls, stream);
+        for (auto &b : buckets_f) ax3d::launch_elem_phys_fluid(T, P, F.fu, b, stream);
+        ax3d::launch_gather(P, T, F, stream);
+    }
+    void couple() { ax3d::launch_couple(P, F, d_sf3d.p, n_sf3d, stream); }
+    void record(int t) {
+        if (r_elem.empty()) return;
+        if (t < 0) throw Error(AX3D_ERR_ARG, "ax3d_record || negative step");
+        if (t >= seis_cap) grow_seis(t + 1);
+        ax3d::launch_record(P, T, F.su, d_relem.p, d_rphi.p, d_rw.p, (int)r_elem.size(),
+                            d_seis.p + (size_t)t * r_elem.size() * 3, stream);
+    }
+    void grow_seis(int need) {
+        int cap = std::max(need, seis_cap * 2);
+        DevBuf<float> nb;
+        nb.alloc((size_t)cap * r_elem.size() * 3);
+        nb.zero(stream);
+        CK(cudaMemcpyAsync(nb.p, d_seis.p, (size_t)seis_cap * r_elem.size() * 3 * sizeof(float),
+                           cudaMemcpyDeviceToDevice, stream));
+        CK(cudaStreamSynchronize(stream));
+        std::swap(nb.p, d_seis.p);
+        std::swap(nb.n, d_seis.n);
+        seis_cap = cap;
+    }
+    int step(int nsteps) {
+        need_final();
+        for (int s = 0; s < nsteps; s++) {
+            update_newmark();
+            if (!s_elem.empty()) apply_source(tstep - 1);
+            compute_stiff();
+            couple();
+            record(tstep - 1);
+            if (stab_interval > 0 && tstep % stab_interval == 0)
+                ax3d::launch_stability(F.su, nsolid, F.fu, nfluid, d_flag.p, stream);
+            tstep++;
+        }
+        CK(cudaGetLastError());
+        int32_t flag = 0;
+        CK(cudaMemcpyAsync(&flag, d_flag.p, sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        if (flag) throw Error(AX3D_ERR_UNSTABLE, "Domain::checkStability || Simulation blew up.");
+        return AX3D_OK;
+    }
+
+    float2 *field(int which, int phase) {
+        if (phase == AX3D_PHASE_SOLID) {
+            switch (which) {
+                case AX3D_FIELD_DISPL: return F.su;
+                case AX3D_FIELD_VELOC: return F.sv;
+                case AX3D_FIELD_ACCEL: return F.sa;
+                case AX3D_FIELD_STIFF: return F.ss;
+            }
+        } else if (phase == AX3D_PHASE_FLUID) {
+            switch (which) {
+                case AX3D_FIELD_DISPL: return F.fu;
+                case AX3D_FIELD_VELOC: return F.fv;
+                case AX3D_FIELD_ACCEL: return F.fa;
+                case AX3D_FIELD_STIFF: return F.fs;
+            }
+        }
+        throw Error(AX3D_ERR_ARG, "ax3d_get_field || bad field or phase");
+    }
+    int64_t fsize(int phase) const { return phase == AX3D_PHASE_SOLID ? nsolid : nfluid; }
+
+    void reset() {
+        need_final();
+        for (auto *b : {&d_su, &d_sv, &d_sa, &d_ss, &d_fu, &d_fv, &d_fa, &d_fs, &d_ef}) b->zero(stream);
+        if (kahan)
+            for (auto *b : {&d_sku, &d_skv, &d_fku, &d_fkv}) b->zero(stream);
+        d_mem.zero(stream);
+        d_seis.zero(stream);
+        d_flag.zero(stream);
+        CK(cudaStreamSynchronize(stream));
+        tstep = 1;
+    }
+};
+
+// ================================================================ C ABI
+namespace {
+template <typename F>
+int guard(F f) {
+    try {
+        f();
+        return AX3D_OK;
+    } catch (const Error &e) {
+        g_err = e.what();
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        g_err = "ax3d || out of host memory";
+        return AX3D_ERR_NOMEM;
+    } catch (const std::exception &e) {
+        g_err = e.what();
+        return AX3D_ERR_ARG;
+    }
+}
+}  // namespace
+
+extern "C" {
+
+int ax3d_create(const ax3d_config *cfg, ax3d_domain **out) {
+    return guard([&] {
+        if (!cfg || !out) throw Error(AX3D_ERR_ARG, "ax3d_create || null argument");
+        if (cfg->npol != 4) throw Error(AX3D_ERR_UNSUPPORTED, "ax3d_create || only nPol = 4 is built");
+        if (!(cfg->dt > 0.)) throw Error(AX3D_ERR_ARG, "ax3d_create || dt must be positive");
+        if (!cfg->g_gll || !cfg->g_glj) throw Error(AX3D_ERR_ARG, "ax3d_create || G matrices missing");
+        if (cfg->nsls < 0 || cfg->nsls > 8) throw Error(AX3D_ERR_ARG, "ax3d_create || nsls must be in [0, 8]");
+        int ndev = 0;
+        CK(cudaGetDeviceCount(&ndev));
+        if (cfg->device < 0 || cfg->device >= ndev) throw Error(AX3D_ERR_ARG, "ax3d_create || bad device");
+        auto *d = new ax3d_domain();
+        d->device = cfg->device;
+        d->dt = cfg->dt;
+        for (int i = 0; i < 25; i++) {
+            d->g_gll[i] = (float)cfg->g_gll[i];
+            d->g_glj[i] = (float)cfg->g_glj[i];
+        }
+        d->sls.nsls = cfg->nsls;
+        for (int i = 0; i < cfg->nsls; i++) {
+            d->sls.a[i] = (float)cfg->att_alpha[i];
+            d->sls.b[i] = (float)cfg->att_beta[i];
+            d->sls.g[i] = (float)cfg->att_gamma[i];
+        }
+        d->sls.do_kappa = cfg->att_do_kappa != 0;
+        d->kahan = cfg->kahan != 0;
+        d->stab_interval = cfg->stability_interval;
+        *out = d;
+    });
+}
+
+int ax3d_add_points(ax3d_domain *d, int32_t n, const int32_t *nr, const int8_t *kind, const uint8_t *axial,
+                    const uint8_t *fluid_surface, const int32_t *mass_solid_len, const float *mass_solid_inv,
+                    const int32_t *mass_fluid_len, const float *mass_fluid_inv, const int32_t *sf_len,
+                    const float *sf_normal, const float *sf_normal_invmf, int32_t *first) {
+    return guard([&] {
+        if (!d) throw Error(AX3D_ERR_ARG, "ax3d_add_points || null domain");
+        int32_t f0 = (int32_t)d->p_nr.size();
+        d->add_points(n, nr, kind, axial, fluid_surface, mass_solid_len, mass_solid_inv, mass_fluid_len,
+                      mass_fluid_inv, sf_len, sf_normal, sf_normal_invmf);
+        if (first) *first = f0;
+    });
+}
+
+int ax3d_add_elements(ax3d_domain *d, int32_t n, const int32_t *points, const int8_t *material,
+                      const uint8_t *axial, const uint8_t *in_3d, const float *geometry, const float *trig,
+                      const int64_t *moduli_ofs, const float *moduli, const int8_t *att, const int64_t *att_ofs,
+                      const float *att_moduli, int32_t *first) {
+    return guard([&] {
+        if (!d) throw Error(AX3D_ERR_ARG, "ax3d_add_elements || null domain");
+        int32_t f0 = (int32_t)d->e_nr.size();
+        d->add_elements(n, points, material, axial, in_3d, geometry, trig, moduli_ofs, moduli, att, att_ofs,
+                        att_moduli);
+        if (first) *first = f0;
+    });
+}
+
+int ax3d_add_source(ax3d_domain *d, int32_t elem, int32_t norders, const float *force) {
+    return guard([&] {
+        if (!d || !force) throw Error(AX3D_ERR_ARG, "ax3d_add_source || null argument");
+        if (d->finalized) throw Error(AX3D_ERR_STATE, "ax3d_add_source || domain already finalized");
+        if (elem < 0 || elem >= (int)d->e_nr.size()) throw Error(AX3D_ERR_ARG, "ax3d_add_source || element out of range");
+        if (norders < 1) throw Error(AX3D_ERR_ARG, "ax3d_add_source || norders must be >= 1");
+        d->s_elem.push_back(elem);
+        d->s_nord.push_back(norders);
+        d->s_ofs.push_back((int64_t)d->s_force.size() / 2);
+        d->s_force.insert(d->s_force.end(), force, force + (size_t)25 * norders * 3 * 2);
+    });
+}
+
+int ax3d_set_stf(ax3d_domain *d, int32_t nsteps, const float *stf) {
+    return guard([&] {
+        if (!d || (nsteps > 0 && !stf) || nsteps < 0) throw Error(AX3D_ERR_ARG, "ax3d_set_stf || bad argument");
+        if (d->finalized) throw Error(AX3D_ERR_STATE, "ax3d_set_stf || domain already finalized");
+        d->stf.assign(stf, stf + nsteps);
+    });
+}
+
+int ax3d_add_receivers(ax3d_domain *d, int32_t n, const int32_t *elem, const float *phi, const float *weights) {
+    return guard([&] {
+        if (!d || n < 0 || (n && (!elem || !phi || !weights))) throw Error(AX3D_ERR_ARG, "ax3d_add_receivers || bad argument");
+        if (d->finalized) throw Error(AX3D_ERR_STATE, "ax3d_add_receivers || domain already finalized");
+        for (int i = 0; i < n; i++) {
+            if (elem[i] < 0 || elem[i] >= (int)d->e_nr.size())
+                throw Error(AX3D_ERR_ARG, "ax3d_add_receivers || element out of range");
+            if (d->e_flags[elem[i]] & ax3d::EF_FLUID)
+                throw Error(AX3D_ERR_ARG, "ax3d_add_receivers || receiver in a fluid element");
+        }
+        d->r_elem.insert(d->r_elem.end(), elem, elem + n);
+        d->r_phi.insert(d->r_phi.end(), phi, phi + n);
+        d->r_w.insert(d->r_w.end(), weights, weights + (size_t)n * 25);
+    });
+}
+
+int ax3d_finalize(ax3d_domain *d) {
+    return guard([&] {
+        if (!d) throw Error(AX3D_ERR_ARG, "ax3d_finalize || null domain");
+        d->finalize();
+    });
+}
+
+int64_t ax3d_field_size(const ax3d_domain *d, int32_t phase) { return d ? d->fsize(phase) : -1; }
+
+int ax3d_get_field(ax3d_domain *d, int32_t which, int32_t phase, float *out) {
+    return guard([&] {
+        if (!d || !out) throw Error(AX3D_ERR_ARG, "ax3d_get_field || null argument");
+        d->need_final();
+        float2 *src = d->field(which, phase);
+        CK(cudaMemcpyAsync(out, src, d->fsize(phase) * sizeof(float2), cudaMemcpyDeviceToHost, d->stream));
+        CK(cudaStreamSynchronize(d->stream));
+    });
+}
+
+int ax3d_set_field(ax3d_domain *d, int32_t which, int32_t phase, const float *in) {
+    return guard([&] {
+        if (!d || !in) throw Error(AX3D_ERR_ARG, "ax3d_set_field || null argument");
+        d->need_final();
+        float2 *dst = d->field(which, phase);
+        CK(cudaMemcpyAsync(dst, in, d->fsize(phase) * sizeof(float2), cudaMemcpyHostToDevice, d->stream));
+        CK(cudaStreamSynchronize(d->stream));
+    });
+}
+
+#define AX3D_SIMPLE(name, body)                  \
+    int name {                                   \
+        return guard([&] {                       \
+            if (!d) throw Error(AX3D_ERR_ARG, #name " || null domain"); \
+            d->need_final();                     \
+            body;                                \
+            CK(cudaGetLastError());              \
+            CK(cudaStreamSynchronize(d->stream)); \
+        });                                      \
+    }
+
+AX3D_SIMPLE(ax3d_update_newmark(ax3d_domain *d), d->update_newmark())
+AX3D_SIMPLE(ax3d_apply_source(ax3d_domain *d, int32_t tstep), d->apply_source(tstep))
+AX3D_SIMPLE(ax3d_compute_stiff(ax3d_domain *d), d->compute_stiff())
+AX3D_SIMPLE(ax3d_couple_solid_fluid(ax3d_domain *d), d->couple())
+AX3D_SIMPLE(ax3d_record(ax3d_domain *d, int32_t tstep), d->record(tstep))
+
+int ax3d_step(ax3d_domain *d, int32_t nsteps) {
+    return guard([&] {
+        if (!d || nsteps < 0) throw Error(AX3D_ERR_ARG, "ax3d_step || bad argument");
+        d->step(nsteps);
+    });
+}
+
+int ax3d_read_seismograms(ax3d_domain *d, int32_t first, int32_t nsteps, float *out) {
+    return guard([&] {
+        if (!d || !out || first < 0 || nsteps < 0) throw Error(AX3D_ERR_ARG, "ax3d_read_seismograms || bad argument");
+        d->need_final();
+        if (first + nsteps > d->seis_cap) throw Error(AX3D_ERR_ARG, "ax3d_read_seismograms || steps not recorded");
+        const size_t row = d->r_elem.size() * 3;
+        CK(cudaMemcpyAsync(out, d->d_seis.p + (size_t)first * row, (size_t)nsteps * row * sizeof(float),
+                           cudaMemcpyDeviceToHost, d->stream));
+        CK(cudaStreamSynchronize(d->stream));
+    });
+}
+
+int ax3d_reset(ax3d_domain *d) {
+    return guard([&] {
+        if (!d) throw Error(AX3D_ERR_ARG, "ax3d_reset || null domain");
+        d->reset();
+    });
+}
+
+int32_t ax3d_current_step(const ax3d_domain *d) { return d ? d->tstep : -1; }
+
+int ax3d_destroy(ax3d_domain *d) {
+    delete d;
+    return AX3D_OK;
+}
+
+size_t ax3d_last_error(char *buf, size_t len) {
+    if (buf && len) {
+        size_t n = std::min(len - 1, g_err.size());
+        std::memcpy(buf, g_err.data(), n);
+        buf[n] = 0;
+    }
+    return g_err.size();
+}
+
+}  // extern "C"

@@ -1,0 +1,183 @@
+/*
+ * ax3d.h -- C-ABI of the GB300 time-stepping path for AxiSEM3D (nPol = 4).
+ *
+ * The reference has no FFI for this path: it sits behind C++ virtual
+ * interfaces that Mesh::release populates (SOLVER/src/core/domain/Domain.h:31-40,
+ * SOLVER/src/core/element/Element.h:20, SOLVER/src/core/point/Point.h:17-51) and
+ * is driven by Newmark::solve (SOLVER/src/core/newmark/Newmark.cpp:47-93).  Each
+ * entry point below names the reference interface it replaces.  All calls take
+ * plain host pointers and sizes; nothing here exposes CUDA or torch types.
+ *
+ * Data model (host FP32 unless stated; "complex" = two interleaved floats):
+ *   point p      : nr_p azimuthal samples, Nu_p = nr_p / 2 Fourier orders stored
+ *                  as (Nu_p + 1) complex values per component.  Solid fields are
+ *                  laid out per point as [alpha][3] complex (s, phi, z); fluid
+ *                  fields as [alpha] complex.  Points are concatenated in the
+ *                  order they were added.
+ *   element e    : 25 GLL points, row-major (ipol * 5 + jpol).  nr_e is the
+ *                  maximum nr of its points (SOLVER/src/core/element/Element.cpp:13-18).
+ *
+ * Errors: every function returns AX3D_OK (0) or an AX3D_ERR_* code; the text
+ * of the last error on the calling thread is returned by ax3d_last_error.
+ * The reference throws std::runtime_error("Class::method || msg") and aborts
+ * (SOLVER/src/axisem.cpp:193-204); here the same conditions return a code.
+ */
+#ifndef AX3D_H
+#define AX3D_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AX3D_NPOL 4
+#define AX3D_NPE 25
+
+enum {
+    AX3D_OK = 0,
+    AX3D_ERR_ARG = 1,        /* invalid argument or size */
+    AX3D_ERR_STATE = 2,      /* call out of order (e.g. step before finalize) */
+    AX3D_ERR_CUDA = 3,       /* CUDA runtime error */
+    AX3D_ERR_UNSTABLE = 4,   /* non-finite displacement (Domain::checkStability) */
+    AX3D_ERR_NOMEM = 5,
+    AX3D_ERR_UNSUPPORTED = 6,
+    AX3D_ERR_TIMEOUT = 7     /* a bounded device wait gave up */
+};
+
+/* point kinds (GLLPoint::release, SOLVER/src/preloop/mesh/GLLPoint.cpp:48-128) */
+enum { AX3D_POINT_SOLID = 0, AX3D_POINT_FLUID = 1, AX3D_POINT_SOLID_FLUID = 2 };
+
+/* element materials (Material::createElastic / createAcoustic,
+   SOLVER/src/preloop/physics/material/Material.cpp:257-519) */
+enum {
+    AX3D_MAT_ISO = 0,      /* 2 moduli: lambda (=F), mu (=L)                       */
+    AX3D_MAT_TISO = 1,     /* 5 moduli: A, C, F, L, N (Love)                        */
+    AX3D_MAT_ANISO = 2,    /* 21 moduli: C11..C16, C22..C26, C33..C36, C44..C46, C55, C56, C66 */
+    AX3D_MAT_ACOUSTIC = 3  /* 1 modulus: K = integral factor / rho (fluid element)  */
+};
+
+/* attenuation (AttBuilder::createAttenuation1D/3D,
+   SOLVER/src/preloop/physics/attenuation/AttBuilder.cpp:17-129) */
+enum { AX3D_ATT_NONE = 0, AX3D_ATT_FULL = 1, AX3D_ATT_CG4 = 2 };
+
+/* which field for get/set */
+enum { AX3D_FIELD_DISPL = 0, AX3D_FIELD_VELOC = 1, AX3D_FIELD_ACCEL = 2, AX3D_FIELD_STIFF = 3 };
+enum { AX3D_PHASE_SOLID = 0, AX3D_PHASE_FLUID = 1 };
+
+typedef struct ax3d_config {
+    int32_t npol;                 /* must be 4 (SOLVER/src/global.h:26-33) */
+    double dt;                    /* time step, cast to float in the update like Newmark */
+    const double *g_gll;          /* [25] G(i,j) = l_i'(xi_j), GLL nodes, row-major     */
+    const double *g_glj;          /* [25] the same on GLJ(0,1) nodes (axial xi)         */
+    int32_t nsls;                 /* number of standard linear solids, 0 = elastic      */
+    const double *att_alpha;      /* [nsls] SLS factors (AttAxiSEM::computeAttFactors)  */
+    const double *att_beta;       /* [nsls]                                             */
+    const double *att_gamma;      /* [nsls]                                             */
+    int32_t att_do_kappa;         /* ATTENUATION_QKAPPA                                 */
+    int32_t kahan;                /* 1: compensated sums in the Newmark update          */
+    int32_t stability_interval;   /* steps between non-finite checks, <= 0: never       */
+    int32_t device;               /* CUDA device ordinal (ignored by the CPU oracle)    */
+} ax3d_config;
+
+typedef struct ax3d_domain ax3d_domain;
+
+/* Creates an empty domain.  Replaces `new Domain` + SpectralConstants/Gradient
+   static set-up (SOLVER/src/axisem.cpp:40-60, Gradient::setGMat Gradient.cpp:324-329). */
+int ax3d_create(const ax3d_config *cfg, ax3d_domain **out);
+
+/* Bulk Domain::addPoint (Domain.h:31-40) of typed points as GLLPoint::release builds them
+   (GLLPoint.cpp:48-128).  Per point: nr, kind (AX3D_POINT_*), axial, fluid_surface
+   (fluid point on the free surface, FluidPoint.cpp:25-28).
+   Inverse masses: mass_*_len[p] is 0 (no such phase), 1 (Mass1D) or nr (Mass3D); the
+   values are concatenated in mass_*_inv.  Solid-fluid coupling (kind == SOLID_FLUID):
+   sf_len[p] is 1 (SFCoupling1D) or nr (SFCoupling3D); sf_normal holds the unassembled
+   normal [len][3] and sf_normal_invmf the assembled normal / fluid mass [len][3]
+   (SFCoupling1D uses components 0 and 2 of row 0).  Returns the index of the first
+   point in *first. */
+int ax3d_add_points(ax3d_domain *d, int32_t n, const int32_t *nr, const int8_t *kind,
+                    const uint8_t *axial, const uint8_t *fluid_surface,
+                    const int32_t *mass_solid_len, const float *mass_solid_inv,
+                    const int32_t *mass_fluid_len, const float *mass_fluid_inv,
+                    const int32_t *sf_len, const float *sf_normal,
+                    const float *sf_normal_invmf, int32_t *first);
+
+/* Bulk Domain::addElement of SolidElement / FluidElement as Quad::release builds them
+   (SOLVER/src/preloop/mesh/Quad.cpp:378-420).
+   points   [n][25] point indices (ipol * 5 + jpol)
+   material AX3D_MAT_*; in_3d = 1 for physical-space (3D) material, 0 for Fourier-space (1D)
+   geometry [n][5][25]: dsdxii, dsdeta, dzdxii, dzdeta, inv_s (Quad::createGraident,
+            Quad.cpp:509-525), cast from FP64
+   trig     [n][4][25]: sin(theta), cos(theta), sin(2 theta), cos(2 theta) of the GLL
+            points (CrdTransTIsoSolid.cpp:7-12); read for TISO and ANISO only; may be NULL
+            when no element needs it
+   moduli   concatenated, moduli_ofs[e] floats into it: 1D [k][25]; 3D [k][nr_e][25]
+   att      AX3D_ATT_*; att_moduli concatenated, att_ofs[e] floats into it:
+            1D FULL [2][25] (dkappa, dmu); 1D CG4 [2][4]; 3D FULL [2][nr_e][25];
+            3D CG4 [2][nr_e][4].  CG4 points are (1,1), (1,3), (3,1), (3,3).
+   Returns the index of the first element in *first. */
+int ax3d_add_elements(ax3d_domain *d, int32_t n, const int32_t *points,
+                      const int8_t *material, const uint8_t *axial, const uint8_t *in_3d,
+                      const float *geometry, const float *trig,
+                      const int64_t *moduli_ofs, const float *moduli,
+                      const int8_t *att, const int64_t *att_ofs, const float *att_moduli,
+                      int32_t *first);
+
+/* Domain::addSourceTerm of a SourceTerm (SourceTerm.cpp:13-27): force [25][norders][3]
+   complex, truncated per point to Nu_p + 1 orders like the SourceTerm constructor. */
+int ax3d_add_source(ax3d_domain *d, int32_t elem, int32_t norders, const float *force);
+
+/* Domain::setSTF (SourceTimeFunction.h:11-24): one factor per time step. */
+int ax3d_set_stf(ax3d_domain *d, int32_t nsteps, const float *stf);
+
+/* Receivers (PointwiseRecorder, SOLVER/src/core/output/pointwise/PointwiseRecorder.cpp:62-144):
+   element index, azimuth phi and Lagrange weights [n][25] (Receiver::computeInterpFact).
+   Each step records (s, phi, z) displacement via Element::computeGroundMotion. */
+int ax3d_add_receivers(ax3d_domain *d, int32_t n, const int32_t *elem, const float *phi,
+                       const float *weights);
+
+/* Ends set-up (Mesh::release + Domain::initializeRecorders): checks sizes, builds the
+   gather lists and element buckets, uploads everything. */
+int ax3d_finalize(ax3d_domain *d);
+
+/* Number of complex values in the solid or fluid field arrays. */
+int64_t ax3d_field_size(const ax3d_domain *d, int32_t phase);
+
+/* Copy a whole field (all points, concatenated) to / from the host. */
+int ax3d_get_field(ax3d_domain *d, int32_t which, int32_t phase, float *out);
+int ax3d_set_field(ax3d_domain *d, int32_t which, int32_t phase, const float *in);
+
+/* The Domain loop bodies, one call each (Domain.cpp:82-191), for fine-grained parity. */
+int ax3d_update_newmark(ax3d_domain *d);                /* Domain::updateNewmark      */
+int ax3d_apply_source(ax3d_domain *d, int32_t tstep);   /* Domain::applySource(tstep) */
+int ax3d_compute_stiff(ax3d_domain *d);                 /* Domain::computeStiff       */
+int ax3d_couple_solid_fluid(ax3d_domain *d);            /* Domain::coupleSolidFluid   */
+int ax3d_record(ax3d_domain *d, int32_t tstep);         /* Domain::record(tstep, t)   */
+
+/* nsteps iterations of Newmark::solve's loop body (Newmark.cpp:47-93) starting at the
+   internal step counter: update, source, stiffness, solid-fluid coupling, record,
+   stability check every stability_interval steps.  Returns AX3D_ERR_UNSTABLE if a
+   non-finite displacement was found. */
+int ax3d_step(ax3d_domain *d, int32_t nsteps);
+
+/* Recorded (s, phi, z) displacement [nsteps][nrec][3] for steps first..first+nsteps-1. */
+int ax3d_read_seismograms(ax3d_domain *d, int32_t first, int32_t nsteps, float *out);
+
+/* Zero every field and memory variable (Domain::resetZero, Domain.cpp:67-74); the
+   internal step counter restarts at 1. */
+int ax3d_reset(ax3d_domain *d);
+
+/* Current internal step counter (next step to run, 1-based like Newmark::solve). */
+int32_t ax3d_current_step(const ax3d_domain *d);
+
+int ax3d_destroy(ax3d_domain *d);
+
+/* Text of the last error on this thread (always NUL terminated); returns its length. */
+size_t ax3d_last_error(char *buf, size_t len);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* AX3D_H */

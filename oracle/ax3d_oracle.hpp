@@ -1,0 +1,922 @@
+// ax3d_oracle.hpp -- CPU oracle of the AxiSEM3D time-stepping hot path.
+//
+// TEST INFRASTRUCTURE ONLY.  This file is the checker for the CUDA path: only the
+// tests, __graft_entry__.smoke() and the cpu_baseline leg of bench.py may load it.
+// The product library never links or calls it.
+//
+// It restates, without Eigen and FFTW, the reference's per-step arithmetic on the
+// same packed data model as include/ax3d.h, templated on Real (float = the
+// reference's default build, SOLVER/src/global.h:12-18; double = the FP64 oracle).
+// Each block cites the reference file:line it follows (paths relative to the
+// reference repository).  The FFT is an exact DFT accumulated in double and rounded
+// to Real, with FFTW's conventions: C2R unnormalised and reading only the real part
+// of order 0, R2C scaled by 1/nr (SOLVER/src/core/fftw/SolverFFTW_N6.cpp:45-53).
+#pragma once
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <complex>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace axo {
+
+constexpr int nPol = 4;
+constexpr int nP = 5;    // nPntEdge
+constexpr int nPE = 25;  // nPntElem
+
+template <typename Real>
+struct Oracle {
+    using C = std::complex<Real>;
+
+    // ---------------- configuration ----------------
+    double dt = 0.;
+    Real G_gll[nP][nP], G_glj[nP][nP];  // G(i,j) = l_i'(xi_j)
+    int nsls = 0;
+    std::vector<Real> att_a, att_b, att_g;
+    bool doKappa = false;
+    bool kahan = false;
+    int stab_interval = 0;
+
+    // ---------------- points ----------------
+    struct Point {
+        int nr, nu;
+        int kind;           // 0 solid, 1 fluid, 2 solid+fluid
+        bool axial, fsurf;
+        int64_t sofs = -1;  // complex offset into solid fields ([alpha][3])
+        int64_t fofs = -1;  // complex offset into fluid fields ([alpha])
+        std::vector<Real> ims, imf;     // inverse mass, size 1 or nr
+        std::vector<Real> sfn, sfni;    // [len][3]
+    };
+    std::vector<Point> pts;
+    std::vector<C> su, sv, sa, ss;   // solid displ, veloc, accel, stiff
+    std::vector<C> fu, fv, fa, fs;   // fluid
+    std::vector<C> sku, skv, fku, fkv;  // Kahan compensations
+
+    // ---------------- elements ----------------
+    struct Elem {
+        int pts[nPE];
+        int mat;         // AX3D_MAT_*
+        bool axial, in3d, fluid, tiso;
+        int nr, nu, nyq;
+        Real geo[5][nPE];
+        Real trig[4][nPE];
+        std::vector<Real> mod;   // 1D [k][25], 3D [k][nr][25]
+        int att;                 // 0 none, 1 full, 2 cg4
+        std::vector<Real> attm;  // dkappa, dmu
+        std::vector<C> mem1;     // 1D state: (nsls+1) * (nu+1) * 6 * npa (last block = stressR)
+        std::vector<Real> mem3;  // 3D state: (nsls+1) * nr * 6 * npa
+    };
+    std::vector<Elem> elems;
+
+    struct Source {
+        int elem;
+        int nord;
+        std::vector<C> force;  // [25][nord][3]
+    };
+    std::vector<Source> srcs;
+    std::vector<Real> stf;
+
+    struct Rec {
+        int elem;
+        Real phi;
+        Real w[nPE];
+    };
+    std::vector<Rec> recs;
+    std::vector<Real> seis;  // [step][nrec][3]
+
+    bool finalized = false;
+    int tstep = 1;  // next step (1-based)
+
+    // ================= set-up =================
+    void config(double dt_, const double *ggll, const double *gglj, int nsls_, const double *a,
+                const double *b, const double *g, bool dk, bool kh, int stab) {
+        dt = dt_;
+        for (int i = 0; i < nP; i++)
+            for (int j = 0; j < nP; j++) {
+                G_gll[i][j] = (Real)ggll[i * nP + j];
+                G_glj[i][j] = (Real)gglj[i * nP + j];
+            }
+        nsls = nsls_;
+        att_a.assign(nsls, 0);
+        att_b.assign(nsls, 0);
+        att_g.assign(nsls, 0);
+        for (int i = 0; i < nsls; i++) {
+            att_a[i] = (Real)a[i];
+            att_b[i] = (Real)b[i];
+            att_g[i] = (Real)g[i];
+        }
+        doKappa = dk;
+        kahan = kh;
+        stab_interval = stab;
+    }
+
+    void add_points(int n, const int32_t *nr, const int8_t *kind, const uint8_t *axial,
+                    const uint8_t *fsurf, const int32_t *msl, const float *ms, const int32_t *mfl,
+                    const float *mf, const int32_t *sfl, const float *sfn, const float *sfni) {
+        int64_t om = 0, of = 0, osf = 0;
+        for (int i = 0; i < n; i++) {
+            Point p;
+            p.nr = nr[i];
+            if (p.nr < 1) throw std::runtime_error("Point || nr must be >= 1");
+            p.nu = p.nr / 2;
+            p.kind = kind[i];
+            p.axial = axial[i] != 0;
+            p.fsurf = fsurf ? fsurf[i] != 0 : false;
+            int ls = msl[i], lf = mfl[i];
+            bool hasS = p.kind != 1, hasF = p.kind != 0;
+            if (hasS && !(ls == 1 || ls == p.nr)) throw std::runtime_error("Point || bad solid mass length");
+            if (hasF && !(lf == 1 || lf == p.nr)) throw std::runtime_error("Point || bad fluid mass length");
+            if (hasS) p.ims.assign(ms + om, ms + om + ls);
+            om += ls;
+            if (hasF) p.imf.assign(mf + of, mf + of + lf);
+            of += lf;
+            int lsf = sfl ? sfl[i] : 0;
+            if (p.kind == 2) {
+                if (!(lsf == 1 || lsf == p.nr)) throw std::runtime_error("Point || bad coupling length");
+                p.sfn.assign(sfn + osf * 3, sfn + (osf + lsf) * 3);
+                p.sfni.assign(sfni + osf * 3, sfni + (osf + lsf) * 3);
+            }
+            osf += lsf;
+            pts.push_back(p);
+        }
+    }
+
+    static int n_moduli(int mat) {
+        switch (mat) {
+            case 0: return 2;
+            case 1: return 5;
+            case 2: return 21;
+            case 3: return 1;
+        }
+        throw std::runtime_error("Element || bad material");
+    }
+
+    void add_elements(int n, const int32_t *ep, const int8_t *mat, const uint8_t *axial,
+                      const uint8_t *in3d, const float *geo, const float *trig,
+                      const int64_t *mofs, const float *mod, const int8_t *att,
+                      const int64_t *aofs, const float *attm) {
+        for (int e = 0; e < n; e++) {
+            Elem el;
+            el.nr = -1;
+            for (int i = 0; i < nPE; i++) {
+                el.pts[i] = ep[e * nPE + i];
+                if (el.pts[i] < 0 || el.pts[i] >= (int)pts.size())
+                    throw std::runtime_error("Element || point index out of range");
+                el.nr = std::max(el.nr, pts[el.pts[i]].nr);  // Element.cpp:13-18
+            }
+            el.nu = el.nr / 2;
+            el.nyq = (el.nr % 2 == 0);
+            el.mat = mat[e];
+            el.fluid = el.mat == 3;
+            el.axial = axial[e] != 0;
+            el.in3d = in3d[e] != 0;
+            el.tiso = (el.mat == 1 || el.mat == 2);  // needTIso (SolidElement.cpp:21-24)
+            for (int k = 0; k < 5; k++)
+                for (int i = 0; i < nPE; i++) el.geo[k][i] = geo[(int64_t)e * 125 + k * 25 + i];
+            for (int k = 0; k < 4; k++)
+                for (int i = 0; i < nPE; i++)
+                    el.trig[k][i] = (el.tiso && trig) ? trig[(int64_t)e * 100 + k * 25 + i] : Real(0);
+            if (el.tiso && !trig) throw std::runtime_error("Element || trig needed");
+            int km = n_moduli(el.mat);
+            int64_t len = (int64_t)km * nPE * (el.in3d ? el.nr : 1);
+            el.mod.assign(mod + mofs[e], mod + mofs[e] + len);
+            el.att = el.fluid ? 0 : att[e];
+            if (el.att && nsls <= 0) throw std::runtime_error("Element || attenuation without SLS");
+            int npa = el.att == 2 ? 4 : nPE;
+            if (el.att) {
+                int64_t alen = 2LL * npa * (el.in3d ? el.nr : 1);
+                el.attm.assign(attm + aofs[e], attm + aofs[e] + alen);
+                if (el.in3d)
+                    el.mem3.assign((size_t)(nsls + 1) * el.nr * 6 * npa, Real(0));
+                else
+                    el.mem1.assign((size_t)(nsls + 1) * (el.nu + 1) * 6 * npa, C(0));
+            }
+            elems.push_back(std::move(el));
+        }
+    }
+
+    void finalize() {
+        int64_t so = 0, fo = 0;
+        for (auto &p : pts) {
+            if (p.kind != 1) { p.sofs = so; so += (int64_t)(p.nu + 1) * 3; }
+            if (p.kind != 0) { p.fofs = fo; fo += (p.nu + 1); }
+        }
+        su.assign(so, C(0)); sv = sa = ss = sku = skv = su;
+        fu.assign(fo, C(0)); fv = fa = fs = fku = fkv = fu;
+        for (auto &e : elems)
+            for (int i = 0; i < nPE; i++) {
+                const Point &p = pts[e.pts[i]];
+                if (e.fluid && p.kind == 0) throw std::runtime_error("Element || fluid element on solid point");
+                if (!e.fluid && p.kind == 1) throw std::runtime_error("Element || solid element on fluid point");
+            }
+        for (auto &s : srcs)
+            if (elems[s.elem].fluid) throw std::runtime_error("Source || source in fluid element");
+        finalized = true;
+    }
+
+    void reset() {
+        for (auto *v : {&su, &sv, &sa, &ss, &sku, &skv, &fu, &fv, &fa, &fs, &fku, &fkv})
+            std::fill(v->begin(), v->end(), C(0));
+        for (auto &e : elems) {
+            std::fill(e.mem1.begin(), e.mem1.end(), C(0));
+            std::fill(e.mem3.begin(), e.mem3.end(), Real(0));
+        }
+        tstep = 1;
+        seis.clear();
+    }
+
+    // ================= FFT (FFTW conventions) =================
+    // C2R: x_k = Re X_0 + 2 sum_{a=1}^{Nu'} Re(X_a e^{+2 pi i k a / nr}), Nu' = Nu - nyquist;
+    // the Nyquist order enters with weight 1 (zero wherever the reference uses it).
+    static void c2r(const C *X, int nr, Real *x, int stride_in = 1) {
+        int nu = nr / 2;
+        for (int k = 0; k < nr; k++) {
+            double acc = (double)X[0].real();
+            for (int a = 1; a <= nu; a++) {
+                double th = 2. * M_PI * (double)((int64_t)k * a % nr) / nr;
+                double w = (nr % 2 == 0 && a == nu) ? 1. : 2.;
+                const C &v = X[(size_t)a * stride_in];
+                acc += w * ((double)v.real() * std::cos(th) - (double)v.imag() * std::sin(th));
+            }
+            x[k] = (Real)acc;
+        }
+    }
+    // R2C scaled by 1/nr: X_a = (1/nr) sum_k x_k e^{-2 pi i k a / nr}, a = 0..Nu.
+    static void r2c(const Real *x, int nr, C *X, int stride_out = 1) {
+        int nu = nr / 2;
+        for (int a = 0; a <= nu; a++) {
+            double re = 0., im = 0.;
+            for (int k = 0; k < nr; k++) {
+                double th = 2. * M_PI * (double)((int64_t)k * a % nr) / nr;
+                re += (double)x[k] * std::cos(th);
+                im -= (double)x[k] * std::sin(th);
+            }
+            X[(size_t)a * stride_out] = C((Real)(re / nr), (Real)(im / nr));
+        }
+    }
+
+    // ================= Gradient (SOLVER/src/core/element/grad/Gradient.cpp) =================
+    // u[c][i*5+j]; G_xi = GLJ on axial elements (Gradient.cpp:15-23), G_eta = GLL.
+    // computeGrad6 (Gradient.cpp:206-265), written once for every order; at alpha = 0 it
+    // reduces to the "hardcode for alpha = 0" branch (only real parts are meaningful).
+    void grad6(const Elem &e, int alpha, const C u[3][nPE], C eps[6][nPE]) const {
+        const Real(*Gx)[nP] = e.axial ? G_glj : G_gll;
+        const Real(*Ge)[nP] = G_gll;
+        const Real *dsdxii = e.geo[0], *dsdeta = e.geo[1], *dzdxii = e.geo[2], *dzdeta = e.geo[3],
+                   *inv_s = e.geo[4];
+        C ia(0, (Real)alpha);
+        C GU[3][nPE], UG[3][nPE], v[3][nPE];
+        for (int c = 0; c < 3; c++)
+            for (int i = 0; i < nP; i++)
+                for (int j = 0; j < nP; j++) {
+                    C gu(0), ug(0);
+                    for (int k = 0; k < nP; k++) {
+                        gu += Gx[k][i] * u[c][k * nP + j];  // (G_xi^T u)(i,j)
+                        ug += u[c][i * nP + k] * Ge[k][j];  // (u G_eta)(i,j)
+                    }
+                    GU[c][i * nP + j] = gu;
+                    UG[c][i * nP + j] = ug;
+                }
+        for (int p = 0; p < nPE; p++) {
+            v[0][p] = u[0][p] + ia * u[1][p];
+            v[1][p] = ia * u[0][p] - u[1][p];
+            v[2][p] = ia * u[2][p];
+        }
+        for (int p = 0; p < nPE; p++) {
+            eps[0][p] = dzdeta[p] * GU[0][p] + dzdxii[p] * UG[0][p];
+            eps[1][p] = inv_s[p] * v[0][p];
+            eps[2][p] = dsdeta[p] * GU[2][p] + dsdxii[p] * UG[2][p];
+            eps[3][p] = dsdeta[p] * GU[1][p] + dsdxii[p] * UG[1][p] + inv_s[p] * v[2][p];
+            eps[4][p] = dsdeta[p] * GU[0][p] + dsdxii[p] * UG[0][p] + dzdeta[p] * GU[2][p] +
+                        dzdxii[p] * UG[2][p];
+            eps[5][p] = dzdeta[p] * GU[1][p] + dzdxii[p] * UG[1][p] + inv_s[p] * v[1][p];
+        }
+        if (e.axial) {  // Gradient.cpp:245-253 (and 221-224 for alpha = 0)
+            for (int j = 0; j < nP; j++) {
+                C g0(0), g1(0), g2(0);
+                for (int k = 0; k < nP; k++) {
+                    g0 += Gx[k][0] * v[0][k * nP + j];
+                    g1 += Gx[k][0] * v[1][k * nP + j];
+                    g2 += Gx[k][0] * v[2][k * nP + j];
+                }
+                eps[1][j] += dzdeta[j] * g0;
+                eps[5][j] += dzdeta[j] * g1;
+                eps[3][j] += dzdeta[j] * g2;
+            }
+            if (alpha == 1) {
+                for (int j = 0; j < nP; j++) {
+                    C h0(0), h1(0);
+                    for (int k = 0; k < nP; k++) {
+                        h0 += v[0][k] * Ge[k][j];
+                        h1 += v[1][k] * Ge[k][j];
+                    }
+                    eps[1][j] += dzdxii[j] * h0;
+                    eps[5][j] += dzdxii[j] * h1;
+                }
+            }
+        }
+    }
+
+    // computeQuad6 (Gradient.cpp:267-317).
+    void quad6(const Elem &e, int beta, const C sig[6][nPE], C f[3][nPE]) const {
+        const Real(*Gx)[nP] = e.axial ? G_glj : G_gll;
+        const Real(*Ge)[nP] = G_gll;
+        const Real *dsdxii = e.geo[0], *dsdeta = e.geo[1], *dzdxii = e.geo[2], *dzdeta = e.geo[3],
+                   *inv_s = e.geo[4];
+        C ib(0, -(Real)beta);
+        C g[3][nPE], X[3][nPE], Y[3][nPE];
+        for (int p = 0; p < nPE; p++) {
+            g[0][p] = sig[1][p] + ib * sig[5][p];
+            g[1][p] = ib * sig[1][p] - sig[5][p];
+            g[2][p] = ib * sig[3][p];
+            X[0][p] = dzdeta[p] * sig[0][p] + dsdeta[p] * sig[4][p];
+            X[1][p] = dzdeta[p] * sig[5][p] + dsdeta[p] * sig[3][p];
+            X[2][p] = dzdeta[p] * sig[4][p] + dsdeta[p] * sig[2][p];
+            Y[0][p] = dzdxii[p] * sig[0][p] + dsdxii[p] * sig[4][p];
+            Y[1][p] = dzdxii[p] * sig[5][p] + dsdxii[p] * sig[3][p];
+            Y[2][p] = dzdxii[p] * sig[4][p] + dsdxii[p] * sig[2][p];
+        }
+        for (int c = 0; c < 3; c++)
+            for (int i = 0; i < nP; i++)
+                for (int j = 0; j < nP; j++) {
+                    C a(0), b(0);
+                    for (int k = 0; k < nP; k++) {
+                        a += Gx[i][k] * X[c][k * nP + j];  // (G_xi X)(i,j)
+                        b += Y[c][i * nP + k] * Ge[j][k];  // (Y G_eta^T)(i,j)
+                    }
+                    f[c][i * nP + j] = a + b + inv_s[i * nP + j] * g[c][i * nP + j];
+                }
+        if (e.axial) {
+            for (int c = 0; c < 3; c++)
+                for (int i = 0; i < nP; i++)
+                    for (int j = 0; j < nP; j++) f[c][i * nP + j] += Gx[i][0] * (dzdeta[j] * g[c][j]);
+            if (beta == 1) {
+                for (int c = 0; c < 2; c++)
+                    for (int j = 0; j < nP; j++) {
+                        C acc(0);
+                        for (int k = 0; k < nP; k++) acc += (dzdxii[k] * g[c][k]) * Ge[j][k];
+                        f[c][j] += acc;
+                    }
+            }
+        }
+    }
+
+    // computeGrad / computeQuad, scalar potential (Gradient.cpp:26-82).
+    void grad1(const Elem &e, int alpha, const C u[nPE], C eps[3][nPE]) const {
+        const Real(*Gx)[nP] = e.axial ? G_glj : G_gll;
+        const Real(*Ge)[nP] = G_gll;
+        const Real *dsdxii = e.geo[0], *dsdeta = e.geo[1], *dzdxii = e.geo[2], *dzdeta = e.geo[3],
+                   *inv_s = e.geo[4];
+        C ia(0, (Real)alpha);
+        C GU[nPE], UG[nPE], v[nPE];
+        for (int i = 0; i < nP; i++)
+            for (int j = 0; j < nP; j++) {
+                C gu(0), ug(0);
+                for (int k = 0; k < nP; k++) {
+                    gu += Gx[k][i] * u[k * nP + j];
+                    ug += u[i * nP + k] * Ge[k][j];
+                }
+                GU[i * nP + j] = gu;
+                UG[i * nP + j] = ug;
+            }
+        for (int p = 0; p < nPE; p++) {
+            v[p] = ia * u[p];
+            eps[0][p] = dzdeta[p] * GU[p] + dzdxii[p] * UG[p];
+            eps[1][p] = inv_s[p] * v[p];
+            eps[2][p] = dsdeta[p] * GU[p] + dsdxii[p] * UG[p];
+        }
+        if (e.axial && alpha > 0) {
+            for (int j = 0; j < nP; j++) {
+                C g0(0);
+                for (int k = 0; k < nP; k++) g0 += Gx[k][0] * v[k * nP + j];
+                eps[1][j] += dzdeta[j] * g0;
+            }
+        }
+    }
+
+    void quad1(const Elem &e, int beta, const C sig[3][nPE], C f[nPE]) const {
+        const Real(*Gx)[nP] = e.axial ? G_glj : G_gll;
+        const Real(*Ge)[nP] = G_gll;
+        const Real *dsdxii = e.geo[0], *dsdeta = e.geo[1], *dzdxii = e.geo[2], *dzdeta = e.geo[3],
+                   *inv_s = e.geo[4];
+        C ib(0, -(Real)beta);
+        C g[nPE], X[nPE], Y[nPE];
+        for (int p = 0; p < nPE; p++) {
+            g[p] = ib * sig[1][p];
+            X[p] = dzdeta[p] * sig[0][p] + dsdeta[p] * sig[2][p];
+            Y[p] = dzdxii[p] * sig[0][p] + dsdxii[p] * sig[2][p];
+        }
+        for (int i = 0; i < nP; i++)
+            for (int j = 0; j < nP; j++) {
+                C a(0), b(0);
+                for (int k = 0; k < nP; k++) {
+                    a += Gx[i][k] * X[k * nP + j];
+                    b += Y[i * nP + k] * Ge[j][k];
+                }
+                f[i * nP + j] = a + b + inv_s[i * nP + j] * g[i * nP + j];
+            }
+        if (e.axial && beta > 0)
+            for (int i = 0; i < nP; i++)
+                for (int j = 0; j < nP; j++) f[i * nP + j] += Gx[i][0] * (dzdeta[j] * g[j]);
+    }
+
+    // ================= CrdTransTIsoSolid (CrdTransTIsoSolid.cpp:14-42) =================
+    template <typename T>
+    void spz_rtz(const Elem &e, T *ua[6], int p) const {
+        Real s1 = e.trig[0][p], c1 = e.trig[1][p], s2 = e.trig[2][p], c2 = e.trig[3][p];
+        T sum02 = *ua[0] + *ua[2];
+        T dif02 = *ua[0] - *ua[2];
+        T u3 = *ua[3];
+        *ua[0] = Real(0.5) * (sum02 + c2 * dif02 - s2 * *ua[4]);
+        *ua[2] = sum02 - *ua[0];
+        *ua[4] = c2 * *ua[4] + s2 * dif02;
+        *ua[3] = c1 * u3 + s1 * *ua[5];
+        *ua[5] = c1 * *ua[5] - s1 * u3;
+    }
+    template <typename T>
+    void rtz_spz(const Elem &e, T *ua[6], int p) const {
+        Real s1 = e.trig[0][p], c1 = e.trig[1][p], s2 = e.trig[2][p], c2 = e.trig[3][p];
+        T sum02 = *ua[0] + *ua[2];
+        T dif02 = (*ua[0] - *ua[2]) * Real(0.5);
+        T u3 = *ua[3];
+        *ua[0] = Real(0.5) * sum02 + c2 * dif02 + s2 * *ua[4];
+        *ua[2] = sum02 - *ua[0];
+        *ua[4] = c2 * *ua[4] - s2 * dif02;
+        *ua[3] = c1 * u3 - s1 * *ua[5];
+        *ua[5] = c1 * *ua[5] + s1 * u3;
+    }
+
+    // ================= elastic strain -> stress, one GLL point / sample =================
+    // Isotropic1D.cpp:9-26 / Isotropic3D.cpp:10-28; TransverselyIsotropic1D.cpp:9-27 /
+    // TransverselyIsotropic3D.cpp:10-28; Anisotropic1D.cpp:9-54 / Anisotropic3D.cpp:10-54.
+    // m(k) returns modulus k at this point (and sample).
+    template <typename T, typename M>
+    static void elastic(int mat, const T eps[6], T sig[6], M m) {
+        if (mat == 0) {
+            Real lam = m(0), mu = m(1), mu2 = Real(2) * mu;
+            T sii = lam * (eps[0] + eps[1] + eps[2]);
+            sig[0] = sii + mu2 * eps[0];
+            sig[1] = sii + mu2 * eps[1];
+            sig[2] = sii + mu2 * eps[2];
+            sig[3] = mu * eps[3];
+            sig[4] = mu * eps[4];
+            sig[5] = mu * eps[5];
+        } else if (mat == 1) {
+            Real A = m(0), Cc = m(1), F = m(2), L = m(3), N = m(4), N2 = Real(2) * N;
+            T e01 = eps[0] + eps[1];
+            T temp = A * e01 + F * eps[2];
+            sig[0] = temp - N2 * eps[1];
+            sig[1] = temp - N2 * eps[0];
+            sig[2] = Cc * eps[2] + F * e01;
+            sig[3] = L * eps[3];
+            sig[4] = L * eps[4];
+            sig[5] = N * eps[5];
+        } else {
+            // index of C_ij (i <= j) in the 21-vector
+            auto idx = [](int i, int j) {
+                if (i > j) std::swap(i, j);
+                return i * 6 - i * (i - 1) / 2 + (j - i);
+            };
+            for (int i = 0; i < 6; i++) {
+                T acc = m(idx(i, 0)) * eps[0];
+                for (int j = 1; j < 6; j++) acc = acc + m(idx(i, j)) * eps[j];
+                sig[i] = acc;
+            }
+        }
+    }
+
+    // ================= SLS (Attenuation1D_Full.cpp:16-74, _CG4.cpp:17-82,
+    //                        Attenuation3D_Full.cpp:16-50, _CG4.cpp:16-62) =================
+    // One attenuated point: R[l][c] memory variables, SR[c] stressR, strain e, moduli dk, dmu.
+    // applyToStress (sig -= sum R) must be done by the caller before update.
+    template <typename T>
+    void sls_update(T *R, T *SR, int stride_l, int stride_c, const T e[6], Real dk, Real dmu) const {
+        // R <- a R + b SR
+        for (int l = 0; l < nsls; l++)
+            for (int c = 0; c < 6; c++) {
+                T &r = R[l * stride_l + c * stride_c];
+                r = att_a[l] * r + att_b[l] * SR[c * stride_c];
+            }
+        Real third = (Real)(1.0 / 3.0);
+        Real dk3 = Real(3) * dk, dmu2 = Real(2) * dmu;
+        T e3 = (e[0] + e[1] + e[2]) * third;
+        T s[6];
+        if (doKappa) {
+            T sii3 = dk3 * e3;
+            s[0] = sii3 + dmu2 * (e[0] - e3);
+            s[1] = sii3 + dmu2 * (e[1] - e3);
+            s[2] = sii3 + dmu2 * (e[2] - e3);
+        } else {
+            s[0] = dmu2 * (e[0] - e3);
+            s[1] = dmu2 * (e[1] - e3);
+            s[2] = -(s[0] + s[1]);
+        }
+        s[3] = dmu * e[3];
+        s[4] = dmu * e[4];
+        s[5] = dmu * e[5];
+        for (int c = 0; c < 6; c++) SR[c * stride_c] = s[c];
+        for (int l = 0; l < nsls; l++)
+            for (int c = 0; c < 6; c++) R[l * stride_l + c * stride_c] += att_g[l] * s[c];
+    }
+
+    static int cg4_index(int p) {  // CG4 points (1,1), (1,3), (3,1), (3,3)
+        switch (p) {
+            case 6: return 0;
+            case 8: return 1;
+            case 16: return 2;
+            case 18: return 3;
+        }
+        return -1;
+    }
+
+    // ================= element stiffness =================
+    // scatterDisplToElement (SolidPoint.cpp:175-195): orders above a point's Nu and its
+    // Nyquist order read as zero.
+    C solid_u_elem(const std::vector<C> &fld, const Point &p, int alpha, int c) const {
+        int lim = p.nu - (p.nr % 2 == 0);
+        if (alpha > lim) return C(0);
+        return fld[p.sofs + (int64_t)alpha * 3 + c];
+    }
+    C fluid_u_elem(const std::vector<C> &fld, const Point &p, int alpha) const {
+        int lim = p.nu - (p.nr % 2 == 0);
+        if (alpha > lim) return C(0);
+        return fld[p.fofs + alpha];
+    }
+
+    // SolidElement::computeStiff + displToStiff (SolidElement.cpp:43-65, 404-443), no PRT.
+    // Returns the element force K u as [alpha][3][25].
+    void solid_stiff(Elem &e, const std::vector<C> &u, std::vector<C> &force) {
+        const int n = e.nu + 1;
+        const int lim = e.nu - e.nyq;  // orders handled by grad/quad; Nyquist masked
+        std::vector<std::array<std::array<C, nPE>, 6>> strain(n), stress(n);
+        for (int a = 0; a < n; a++) {
+            C ua[3][nPE];
+            for (int p = 0; p < nPE; p++)
+                for (int c = 0; c < 3; c++) ua[c][p] = solid_u_elem(u, pts[e.pts[p]], a, c);
+            C eps[6][nPE];
+            if (a <= lim) {
+                grad6(e, a, ua, eps);
+            } else {
+                for (int c = 0; c < 6; c++)
+                    for (int p = 0; p < nPE; p++) eps[c][p] = C(0);
+            }
+            if (e.tiso)
+                for (int p = 0; p < nPE; p++) {
+                    C *pp[6] = {&eps[0][p], &eps[1][p], &eps[2][p], &eps[3][p], &eps[4][p], &eps[5][p]};
+                    spz_rtz(e, pp, p);
+                }
+            for (int c = 0; c < 6; c++)
+                for (int p = 0; p < nPE; p++) strain[a][c][p] = eps[c][p];
+        }
+        const int npa = e.att == 2 ? 4 : nPE;
+        if (!e.in3d) {
+            // Fourier space (1D material)
+            for (int a = 0; a < n; a++)
+                for (int p = 0; p < nPE; p++) {
+                    C eps[6], sig[6];
+                    for (int c = 0; c < 6; c++) eps[c] = strain[a][c][p];
+                    const Real *md = e.mod.data();
+                    elastic(e.mat, eps, sig, [&](int k) { return md[k * nPE + p]; });
+                    for (int c = 0; c < 6; c++) stress[a][c][p] = sig[c];
+                }
+            if (e.att) {
+                // applyToStress, then updateMemoryVariables with the (rotated) strain
+                const int64_t sl = (int64_t)n * 6 * npa;  // stride between SLS blocks
+                for (int a = 0; a < n; a++)
+                    for (int p = 0; p < nPE; p++) {
+                        int q = e.att == 2 ? cg4_index(p) : p;
+                        if (q < 0) continue;
+                        C *R = &e.mem1[(int64_t)a * 6 * npa + q];
+                        C *SR = R + (int64_t)nsls * sl;
+                        for (int l = 0; l < nsls; l++)
+                            for (int c = 0; c < 6; c++) stress[a][c][p] -= R[l * sl + c * npa];
+                        C eps[6];
+                        for (int c = 0; c < 6; c++) eps[c] = strain[a][c][p];
+                        Real dk = e.attm[q], dm = e.attm[npa + q];
+                        sls_update(R, SR, (int)sl, npa, eps, dk, dm);
+                    }
+            }
+        } else {
+            // physical space (3D material): FieldFFT::transformF2P -> stress -> transformP2F
+            const int nr = e.nr;
+            std::vector<Real> sR((size_t)6 * nPE * nr), tR((size_t)6 * nPE * nr);
+            std::vector<C> col(n);
+            for (int c = 0; c < 6; c++)
+                for (int p = 0; p < nPE; p++) {
+                    for (int a = 0; a < n; a++) col[a] = strain[a][c][p];
+                    c2r(col.data(), nr, &sR[((size_t)c * nPE + p) * nr]);
+                }
+            const Real *md = e.mod.data();
+            for (int k = 0; k < nr; k++)
+                for (int p = 0; p < nPE; p++) {
+                    Real eps[6], sig[6];
+                    for (int c = 0; c < 6; c++) eps[c] = sR[((size_t)c * nPE + p) * nr + k];
+                    elastic(e.mat, eps, sig,
+                            [&](int m) { return md[((int64_t)m * nr + k) * nPE + p]; });
+                    if (e.att) {
+                        int q = e.att == 2 ? cg4_index(p) : p;
+                        if (q >= 0) {
+                            const int64_t sl = (int64_t)nr * 6 * npa;
+                            Real *R = &e.mem3[(int64_t)k * 6 * npa + q];
+                            Real *SR = R + (int64_t)nsls * sl;
+                            for (int l = 0; l < nsls; l++)
+                                for (int c = 0; c < 6; c++) sig[c] -= R[l * sl + c * npa];
+                            Real dk = e.attm[(int64_t)k * npa + q];
+                            Real dm = e.attm[(int64_t)nr * npa + (int64_t)k * npa + q];
+                            sls_update(R, SR, (int)sl, npa, eps, dk, dm);
+                        }
+                    }
+                    for (int c = 0; c < 6; c++) tR[((size_t)c * nPE + p) * nr + k] = sig[c];
+                }
+            for (int c = 0; c < 6; c++)
+                for (int p = 0; p < nPE; p++) {
+                    r2c(&tR[((size_t)c * nPE + p) * nr], nr, col.data());
+                    for (int a = 0; a < n; a++) stress[a][c][p] = col[a];
+                }
+        }
+        force.assign((size_t)n * 3 * nPE, C(0));
+        for (int a = 0; a < n; a++) {
+            C sig[6][nPE];
+            for (int c = 0; c < 6; c++)
+                for (int p = 0; p < nPE; p++) sig[c][p] = stress[a][c][p];
+            if (e.tiso)
+                for (int p = 0; p < nPE; p++) {
+                    C *pp[6] = {&sig[0][p], &sig[1][p], &sig[2][p], &sig[3][p], &sig[4][p], &sig[5][p]};
+                    rtz_spz(e, pp, p);
+                }
+            if (a > lim) continue;  // Nyquist order masked by quad6
+            C f[3][nPE];
+            quad6(e, a, sig, f);
+            for (int c = 0; c < 3; c++)
+                for (int p = 0; p < nPE; p++) force[((size_t)a * 3 + c) * nPE + p] = f[c][p];
+        }
+    }
+
+    // FluidElement::computeStiff + displToStiff (FluidElement.cpp:43-65, 333-355), no PRT.
+    // Acoustic1D.cpp:8-16, Acoustic3D.cpp:9-16.  Returns [alpha][25].
+    void fluid_stiff(Elem &e, const std::vector<C> &u, std::vector<C> &force) {
+        const int n = e.nu + 1;
+        const int lim = e.nu - e.nyq;
+        std::vector<std::array<std::array<C, nPE>, 3>> strain(n), stress(n);
+        for (int a = 0; a < n; a++) {
+            C ua[nPE];
+            for (int p = 0; p < nPE; p++) ua[p] = fluid_u_elem(u, pts[e.pts[p]], a);
+            C eps[3][nPE];
+            if (a <= lim)
+                grad1(e, a, ua, eps);
+            else
+                for (int c = 0; c < 3; c++)
+                    for (int p = 0; p < nPE; p++) eps[c][p] = C(0);
+            for (int c = 0; c < 3; c++)
+                for (int p = 0; p < nPE; p++) strain[a][c][p] = eps[c][p];
+        }
+        if (!e.in3d) {
+            for (int a = 0; a < n; a++)
+                for (int c = 0; c < 3; c++)
+                    for (int p = 0; p < nPE; p++) stress[a][c][p] = e.mod[p] * strain[a][c][p];
+        } else {
+            const int nr = e.nr;
+            std::vector<Real> x(nr);
+            std::vector<C> col(n);
+            for (int c = 0; c < 3; c++)
+                for (int p = 0; p < nPE; p++) {
+                    for (int a = 0; a < n; a++) col[a] = strain[a][c][p];
+                    c2r(col.data(), nr, x.data());
+                    for (int k = 0; k < nr; k++) x[k] = e.mod[(int64_t)k * nPE + p] * x[k];
+                    r2c(x.data(), nr, col.data());
+                    for (int a = 0; a < n; a++) stress[a][c][p] = col[a];
+                }
+        }
+        force.assign((size_t)n * nPE, C(0));
+        for (int a = 0; a <= lim; a++) {
+            C sig[3][nPE], f[nPE];
+            for (int c = 0; c < 3; c++)
+                for (int p = 0; p < nPE; p++) sig[c][p] = stress[a][c][p];
+            quad1(e, a, sig, f);
+            for (int p = 0; p < nPE; p++) force[(size_t)a * nPE + p] = f[p];
+        }
+    }
+
+    // Domain::computeStiff (Domain.cpp:82-94) with gatherStiffFromElement
+    // (SolidPoint.cpp:197-209, FluidPoint.cpp:184-195): stiff -= element force.
+    void compute_stiff() {
+        std::vector<C> force;
+        for (auto &e : elems) {
+            if (e.fluid) {
+                fluid_stiff(e, fu, force);
+                for (int p = 0; p < nPE; p++) {
+                    const Point &pt = pts[e.pts[p]];
+                    int lim = pt.nu - (pt.nr % 2 == 0);
+                    for (int a = 0; a <= lim; a++) fs[pt.fofs + a] -= force[(size_t)a * nPE + p];
+                    if (pt.nr % 2 == 0) fs[pt.fofs + pt.nu] = C(0);
+                }
+            } else {
+                solid_stiff(e, su, force);
+                for (int p = 0; p < nPE; p++) {
+                    const Point &pt = pts[e.pts[p]];
+                    int lim = pt.nu - (pt.nr % 2 == 0);
+                    for (int a = 0; a <= lim; a++)
+                        for (int c = 0; c < 3; c++)
+                            ss[pt.sofs + (int64_t)a * 3 + c] -= force[((size_t)a * 3 + c) * nPE + p];
+                    if (pt.nr % 2 == 0)
+                        for (int c = 0; c < 3; c++) ss[pt.sofs + (int64_t)pt.nu * 3 + c] = C(0);
+                }
+            }
+        }
+    }
+
+    // ================= points =================
+    // SolidPoint::maskField (SolidPoint.cpp:216-238)
+    void mask_solid(const Point &p, C *f) const {
+        for (int c = 0; c < 3; c++) f[c] = C(f[c].real(), 0);
+        if (p.axial) {
+            f[0] = C(0);
+            f[1] = C(0);
+            if (p.nu >= 1) {
+                C s0 = f[3], s1 = f[4];
+                const C ii(0, 1);
+                f[3] = Real(0.5) * (s0 - ii * s1);
+                f[4] = Real(0.5) * (s1 + ii * s0);
+                f[5] = C(0);
+                for (int a = 2; a <= p.nu; a++)
+                    for (int c = 0; c < 3; c++) f[a * 3 + c] = C(0);
+            }
+        }
+        if (p.nr % 2 == 0)
+            for (int c = 0; c < 3; c++) f[p.nu * 3 + c] = C(0);
+    }
+    // FluidPoint::maskField (FluidPoint.cpp:197-207)
+    void mask_fluid(const Point &p, C *f) const {
+        f[0] = C(f[0].real(), 0);
+        if (p.axial)
+            for (int a = 1; a <= p.nu; a++) f[a] = C(0);
+        if (p.nr % 2 == 0) f[p.nu] = C(0);
+    }
+    // Mass1D::computeAccel (Mass1D.cpp:12-18) / Mass3D::computeAccel (Mass3D.cpp:13-57)
+    void mass_accel(const std::vector<Real> &im, const Point &p, C *f, int ncomp) const {
+        if (im.size() == 1) {
+            for (int i = 0; i < (p.nu + 1) * ncomp; i++) f[i] *= im[0];
+            return;
+        }
+        std::vector<Real> x(p.nr);
+        for (int c = 0; c < ncomp; c++) {
+            c2r(f + c, p.nr, x.data(), ncomp);
+            for (int k = 0; k < p.nr; k++) x[k] = x[k] * im[k];
+            r2c(x.data(), p.nr, f + c, ncomp);
+        }
+    }
+    // Newmark with optional compensated sums: out += d.
+    static void kadd(C &out, C &comp, C d) {
+        C y = d - comp;
+        C t = out + y;
+        comp = (t - out) - y;
+        out = t;
+    }
+    // SolidPoint::updateNewmark (SolidPoint.cpp:23-38), FluidPoint::updateNewmark
+    // (FluidPoint.cpp:23-44).
+    void newmark(const Point &p, int ncomp, const std::vector<Real> &im, C *u, C *v, C *a, C *s,
+                 C *ku, C *kv, bool fluid) {
+        int len = (p.nu + 1) * ncomp;
+        if (fluid && p.fsurf) {
+            for (int i = 0; i < len; i++) u[i] = v[i] = a[i] = s[i] = ku[i] = kv[i] = C(0);
+            return;
+        }
+        if (fluid) mask_fluid(p, s); else mask_solid(p, s);
+        mass_accel(im, p, s, ncomp);
+        if (fluid) mask_fluid(p, s); else mask_solid(p, s);
+        double half_dt = 0.5 * dt;
+        double half_dt_dt = half_dt * dt;
+        Real hd = (Real)half_dt, hdd = (Real)half_dt_dt, rdt = (Real)dt;
+        for (int i = 0; i < len; i++) {
+            if (kahan) {
+                kadd(v[i], kv[i], hd * (a[i] + s[i]));
+                a[i] = s[i];
+                kadd(u[i], ku[i], rdt * v[i] + hdd * a[i]);
+            } else {
+                v[i] += hd * (a[i] + s[i]);
+                a[i] = s[i];
+                u[i] += rdt * v[i] + hdd * a[i];
+            }
+            s[i] = C(0);
+        }
+    }
+    void update_newmark() {  // Domain::updateNewmark (Domain.cpp:165-177)
+        for (auto &p : pts) {
+            if (p.kind != 1)
+                newmark(p, 3, p.ims, &su[p.sofs], &sv[p.sofs], &sa[p.sofs], &ss[p.sofs], &sku[p.sofs],
+                        &skv[p.sofs], false);
+            if (p.kind != 0)
+                newmark(p, 1, p.imf, &fu[p.fofs], &fv[p.fofs], &fa[p.fofs], &fs[p.fofs], &fku[p.fofs],
+                        &fkv[p.fofs], true);
+        }
+    }
+
+    // SolidFluidPoint::coupleSolidFluid (SolidFluidPoint.cpp:106-110): solid->fluid first.
+    // SFCoupling1D.cpp:9-17, SFCoupling3D.cpp:9-56.
+    void couple_solid_fluid() {
+        for (auto &p : pts) {
+            if (p.kind != 2) continue;
+            C *us = &su[p.sofs];
+            C *ssf = &ss[p.sofs];
+            C *sf = &fs[p.fofs];
+            int n = p.nu + 1;
+            if (p.sfn.size() == 3) {
+                Real ns = p.sfn[0], nz = p.sfn[2], nsi = p.sfni[0], nzi = p.sfni[2];
+                for (int a = 0; a < n; a++) sf[a] += ns * us[a * 3 + 0] + nz * us[a * 3 + 2];
+                for (int a = 0; a < n; a++) {
+                    ssf[a * 3 + 0] -= nsi * sf[a];
+                    ssf[a * 3 + 2] -= nzi * sf[a];
+                }
+            } else {
+                const int nr = p.nr;
+                std::vector<Real> x(nr), y(nr, 0);
+                std::vector<C> tmp(n);
+                for (int c = 0; c < 3; c++) {
+                    c2r(us + c, nr, x.data(), 3);
+                    for (int k = 0; k < nr; k++) y[k] += p.sfn[k * 3 + c] * x[k];
+                }
+                r2c(y.data(), nr, tmp.data());
+                for (int a = 0; a < n; a++) sf[a] += tmp[a];
+                c2r(sf, nr, x.data());
+                for (int c = 0; c < 3; c++) {
+                    for (int k = 0; k < nr; k++) y[k] = p.sfni[k * 3 + c] * x[k];
+                    r2c(y.data(), nr, tmp.data());
+                    for (int a = 0; a < n; a++) ssf[a * 3 + c] -= tmp[a];
+                }
+            }
+        }
+    }
+
+    // SourceTerm::apply (SourceTerm.cpp:29-35) via Element::addSourceTerm / addToStiff.
+    void apply_source(int t) {
+        if (srcs.empty()) return;
+        if (t < 0 || t >= (int)stf.size()) throw std::runtime_error("Domain::applySource || step out of range");
+        Real f = stf[t];
+        for (auto &s : srcs) {
+            const Elem &e = elems[s.elem];
+            for (int p = 0; p < nPE; p++) {
+                const Point &pt = pts[e.pts[p]];
+                int rows = std::min(s.nord, pt.nu + 1);
+                for (int a = 0; a < rows; a++)
+                    for (int c = 0; c < 3; c++)
+                        ss[pt.sofs + a * 3 + c] += s.force[((size_t)p * s.nord + a) * 3 + c] * f;
+            }
+        }
+    }
+
+    // SolidElement::computeGroundMotion (SolidElement.cpp:189-216) for every receiver.
+    void record(int t) {
+        if (recs.empty()) return;
+        size_t need = (size_t)(t + 1) * recs.size() * 3;
+        if (seis.size() < need) seis.resize(need, Real(0));
+        for (size_t r = 0; r < recs.size(); r++) {
+            const Rec &rc = recs[r];
+            const Elem &e = elems[rc.elem];
+            Real out[3] = {0, 0, 0};
+            for (int p = 0; p < nPE; p++) {
+                if (std::abs((double)rc.w[p]) < 1e-10) continue;
+                const Point &pt = pts[e.pts[p]];
+                Real up[3];
+                for (int c = 0; c < 3; c++) up[c] = solid_u_elem(su, pt, 0, c).real();
+                for (int a = 1; a <= e.nu - e.nyq; a++) {
+                    Real th = (Real)a * rc.phi;
+                    C ex = Real(2) * C(std::cos(th), std::sin(th));
+                    for (int c = 0; c < 3; c++) up[c] += (ex * solid_u_elem(su, pt, a, c)).real();
+                }
+                for (int c = 0; c < 3; c++) out[c] += rc.w[p] * up[c];
+            }
+            for (int c = 0; c < 3; c++) seis[((size_t)t * recs.size() + r) * 3 + c] = out[c];
+        }
+    }
+
+    bool stable() const {  // SolidPoint::stable / FluidPoint::stable (allFinite of displ)
+        for (auto &v : su)
+            if (!std::isfinite((double)v.real()) || !std::isfinite((double)v.imag())) return false;
+        for (auto &v : fu)
+            if (!std::isfinite((double)v.real()) || !std::isfinite((double)v.imag())) return false;
+        return true;
+    }
+
+    // Newmark::solve loop body (Newmark.cpp:47-93).
+    int step(int nsteps) {
+        for (int s = 0; s < nsteps; s++) {
+            update_newmark();
+            if (!srcs.empty()) apply_source(tstep - 1);
+            compute_stiff();
+            couple_solid_fluid();
+            record(tstep - 1);
+            if (stab_interval > 0 && tstep % stab_interval == 0 && !stable()) {
+                tstep++;
+                return 4;
+            }
+            tstep++;
+        }
+        return 0;
+    }
+};
+
+}  // namespace axo

@@ -1,0 +1,197 @@
+// ax3d_oracle_capi.cpp -- C entry points of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+//
+// Mirrors include/ax3d.h with the prefixes axo_ (Real = float, the reference's default
+// build) and axod_ (Real = double, the FP64 oracle).  Only tests, smoke() and the
+// cpu_baseline leg of bench.py load this library.
+#include <cstring>
+#include <string>
+
+#include "../include/ax3d.h"
+#include "ax3d_oracle.hpp"
+
+namespace {
+thread_local std::string g_err;
+template <typename F>
+int guard(F f) {
+    try {
+        return f();
+    } catch (const std::exception &e) {
+        g_err = e.what();
+        return AX3D_ERR_ARG;
+    }
+}
+}  // namespace
+
+#define AXO_DEFINE(P, REAL)                                                                      \
+    extern "C" {                                                                                 \
+    typedef axo::Oracle<REAL> P##dom;                                                            \
+    int P##create(const ax3d_config *c, void **out) {                                            \
+        return guard([&] {                                                                       \
+            if (!c || c->npol != 4) throw std::runtime_error("create || npol must be 4");        \
+            auto *d = new P##dom();                                                              \
+            d->config(c->dt, c->g_gll, c->g_glj, c->nsls, c->att_alpha, c->att_beta,             \
+                      c->att_gamma, c->att_do_kappa != 0, c->kahan != 0, c->stability_interval); \
+            *out = d;                                                                            \
+            return 0;                                                                            \
+        });                                                                                      \
+    }                                                                                            \
+    int P##add_points(void *d, int32_t n, const int32_t *nr, const int8_t *kind,                 \
+                      const uint8_t *axial, const uint8_t *fs, const int32_t *msl,               \
+                      const float *ms, const int32_t *mfl, const float *mf, const int32_t *sfl, \
+                      const float *sfn, const float *sfni) {                                     \
+        return guard([&] {                                                                       \
+            static_cast<P##dom *>(d)->add_points(n, nr, kind, axial, fs, msl, ms, mfl, mf, sfl, \
+                                                 sfn, sfni);                                     \
+            return 0;                                                                            \
+        });                                                                                      \
+    }                                                                                            \
+    int P##add_elements(void *d, int32_t n, const int32_t *pts, const int8_t *mat,               \
+                        const uint8_t *ax, const uint8_t *in3d, const float *geo,                \
+                        const float *trig, const int64_t *mofs, const float *mod,                \
+                        const int8_t *att, const int64_t *aofs, const float *attm) {             \
+        return guard([&] {                                                                       \
+            static_cast<P##dom *>(d)->add_elements(n, pts, mat, ax, in3d, geo, trig, mofs, mod, \
+                                                   att, aofs, attm);                             \
+            return 0;                                                                            \
+        });                                                                                      \
+    }                                                                                            \
+    int P##add_source(void *dv, int32_t elem, int32_t nord, const float *force) {                \
+        return guard([&] {                                                                       \
+            auto *d = static_cast<P##dom *>(dv);                                                 \
+            if (elem < 0 || elem >= (int)d->elems.size())                                        \
+                throw std::runtime_error("add_source || element out of range");                  \
+            typename P##dom::Source s;                                                           \
+            s.elem = elem;                                                                       \
+            s.nord = nord;                                                                       \
+            s.force.resize((size_t)25 * nord * 3);                                               \
+            for (size_t i = 0; i < s.force.size(); i++)                                          \
+                s.force[i] = std::complex<REAL>(force[2 * i], force[2 * i + 1]);                 \
+            d->srcs.push_back(s);                                                                \
+            return 0;                                                                            \
+        });                                                                                      \
+    }                                                                                            \
+    int P##set_stf(void *dv, int32_t n, const float *stf) {                                      \
+        auto *d = static_cast<P##dom *>(dv);                                                     \
+        d->stf.assign(stf, stf + n);                                                             \
+        return 0;                                                                                \
+    }                                                                                            \
+    int P##add_receivers(void *dv, int32_t n, const int32_t *elem, const float *phi,             \
+                         const float *w) {                                                       \
+        auto *d = static_cast<P##dom *>(dv);                                                     \
+        for (int i = 0; i < n; i++) {                                                            \
+            typename P##dom::Rec r;                                                              \
+            r.elem = elem[i];                                                                    \
+            r.phi = phi[i];                                                                      \
+            for (int p = 0; p < 25; p++) r.w[p] = w[i * 25 + p];                                 \
+            d->recs.push_back(r);                                                                \
+        }                                                                                        \
+        return 0;                                                                                \
+    }                                                                                            \
+    int P##finalize(void *d) {                                                                   \
+        return guard([&] {                                                                       \
+            static_cast<P##dom *>(d)->finalize();                                                \
+            return 0;                                                                            \
+        });                                                                                      \
+    }                                                                                            \
+    int64_t P##field_size(void *dv, int32_t phase) {                                             \
+        auto *d = static_cast<P##dom *>(dv);                                                     \
+        return phase == 0 ? (int64_t)d->su.size() : (int64_t)d->fu.size();                       \
+    }                                                                                            \
+    static std::vector<std::complex<REAL>> *P##pick(P##dom *d, int which, int phase) {           \
+        if (phase == 0) {                                                                        \
+            switch (which) {                                                                     \
+                case 0: return &d->su;                                                           \
+                case 1: return &d->sv;                                                           \
+                case 2: return &d->sa;                                                           \
+                case 3: return &d->ss;                                                           \
+            }                                                                                    \
+        } else {                                                                                 \
+            switch (which) {                                                                     \
+                case 0: return &d->fu;                                                           \
+                case 1: return &d->fv;                                                           \
+                case 2: return &d->fa;                                                           \
+                case 3: return &d->fs;                                                           \
+            }                                                                                    \
+        }                                                                                        \
+        return nullptr;                                                                          \
+    }                                                                                            \
+    int P##get_field(void *dv, int32_t which, int32_t phase, double *out) {                      \
+        auto *v = P##pick(static_cast<P##dom *>(dv), which, phase);                              \
+        if (!v) return AX3D_ERR_ARG;                                                             \
+        for (size_t i = 0; i < v->size(); i++) {                                                 \
+            out[2 * i] = (double)(*v)[i].real();                                                 \
+            out[2 * i + 1] = (double)(*v)[i].imag();                                             \
+        }                                                                                        \
+        return 0;                                                                                \
+    }                                                                                            \
+    int P##set_field(void *dv, int32_t which, int32_t phase, const double *in) {                 \
+        auto *v = P##pick(static_cast<P##dom *>(dv), which, phase);                              \
+        if (!v) return AX3D_ERR_ARG;                                                             \
+        for (size_t i = 0; i < v->size(); i++)                                                   \
+            (*v)[i] = std::complex<REAL>((REAL)in[2 * i], (REAL)in[2 * i + 1]);                  \
+        return 0;                                                                                \
+    }                                                                                            \
+    int P##update_newmark(void *d) {                                                             \
+        return guard([&] {                                                                       \
+            static_cast<P##dom *>(d)->update_newmark();                                          \
+            return 0;                                                                            \
+        });                                                                                      \
+    }                                                                                            \
+    int P##apply_source(void *d, int32_t t) {                                                    \
+        return guard([&] {                                                                       \
+            static_cast<P##dom *>(d)->apply_source(t);                                           \
+            return 0;                                                                            \
+        });                                                                                      \
+    }                                                                                            \
+    int P##compute_stiff(void *d) {                                                              \
+        return guard([&] {                                                                       \
+            static_cast<P##dom *>(d)->compute_stiff();                                           \
+            return 0;                                                                            \
+        });                                                                                      \
+    }                                                                                            \
+    int P##couple_solid_fluid(void *d) {                                                         \
+        return guard([&] {                                                                       \
+            static_cast<P##dom *>(d)->couple_solid_fluid();                                      \
+            return 0;                                                                            \
+        });                                                                                      \
+    }                                                                                            \
+    int P##record(void *d, int32_t t) {                                                          \
+        return guard([&] {                                                                       \
+            static_cast<P##dom *>(d)->record(t);                                                 \
+            return 0;                                                                            \
+        });                                                                                      \
+    }                                                                                            \
+    int P##step(void *d, int32_t n) {                                                            \
+        return guard([&] { return static_cast<P##dom *>(d)->step(n); });                         \
+    }                                                                                            \
+    int P##read_seismograms(void *dv, int32_t first, int32_t n, double *out) {                   \
+        auto *d = static_cast<P##dom *>(dv);                                                     \
+        size_t nrec = d->recs.size();                                                            \
+        size_t need = (size_t)(first + n) * nrec * 3;                                            \
+        if (first < 0 || d->seis.size() < need) return AX3D_ERR_ARG;                             \
+        for (size_t i = 0; i < (size_t)n * nrec * 3; i++)                                        \
+            out[i] = (double)d->seis[(size_t)first * nrec * 3 + i];                              \
+        return 0;                                                                                \
+    }                                                                                            \
+    int P##reset(void *d) {                                                                      \
+        static_cast<P##dom *>(d)->reset();                                                       \
+        return 0;                                                                                \
+    }                                                                                            \
+    int32_t P##current_step(void *d) { return static_cast<P##dom *>(d)->tstep; }                 \
+    int P##destroy(void *d) {                                                                    \
+        delete static_cast<P##dom *>(d);                                                         \
+        return 0;                                                                                \
+    }                                                                                            \
+    }
+
+AXO_DEFINE(axo_, float)
+AXO_DEFINE(axod_, double)
+
+extern "C" size_t axo_last_error(char *buf, size_t len) {
+    if (buf && len) {
+        size_t n = std::min(len - 1, g_err.size());
+        std::memcpy(buf, g_err.data(), n);
+        buf[n] = 0;
+    }
+    return g_err.size();
+}

@@ -1,0 +1,129 @@
+"""CPU tests: oracle against golden tables and invariants, host precompute, C-ABI exports."""
+import ctypes
+import json
+import re
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from axisem3d_gb300 import geometry as GEO
+from axisem3d_gb300 import spectral as S
+from axisem3d_gb300 import synth
+from axisem3d_gb300.spec import ATT_CG4, ATT_FULL, MAT_ANISO, MAT_TISO
+
+ROOT = Path(__file__).resolve().parents[1]
+GOLD = json.loads((ROOT / "tests/golden/spectral_npol4.json").read_text())
+
+
+def test_spectral_constants_match_reference_table():
+    x, w, G = S.gll()
+    xj, wj, Gj = S.glj()
+    np.testing.assert_allclose(x, GOLD["pgll_4"], atol=1e-11)
+    np.testing.assert_allclose(w, GOLD["wgll_4"], atol=1e-11)
+    np.testing.assert_allclose(G.ravel(), GOLD["Ggll_4"], atol=1e-11)
+    np.testing.assert_allclose(xj, GOLD["pglj_4"], atol=1e-11)
+    np.testing.assert_allclose(wj, GOLD["wglj_4"], atol=1e-11)
+    np.testing.assert_allclose(Gj.ravel(), GOLD["Gglj_4"], atol=1e-11)
+
+
+def test_geometry_integral_factor_is_volume():
+    """sum(ifact) over a spherical element = its meridional 'volume' int s ds dz."""
+    r0, r1, t0, t1 = 5000e3, 5200e3, 0.1, 0.15
+    nodes = np.array([[r0 * np.sin(t0), r0 * np.sin(t1), r1 * np.sin(t1), r1 * np.sin(t0)],
+                      [r0 * np.cos(t0), r0 * np.cos(t1), r1 * np.cos(t1), r1 * np.cos(t0)]])
+    _, ifact, _, _ = GEO.element_geometry(nodes, axial=False)
+    exact = (r1 ** 3 - r0 ** 3) / 3 * (np.cos(t0) - np.cos(t1))  # int r^2 sin t dr dt
+    assert abs(ifact.sum() - exact) / exact < 1e-6
+
+
+def _oracle():
+    from oracle.oracle_py import OracleDomain
+    return OracleDomain
+
+
+def _stiffness_matrix(spec, double=True):
+    """Element stiffness matrix by unit impulses (SolidElement::test, SolidElement.cpp:96-187)."""
+    OD = _oracle()
+    d = OD(spec, double=double)
+    n = d.nsolid
+    so, _ = spec.point_offsets()
+    cols = []
+    idx = []
+    for p in range(spec.n_points):
+        na = spec.p_nr[p] // 2 + 1
+        for a in range(na):
+            for c in range(3):
+                if spec.p_axial[p] and ((a == 0 and c != 2) or (a == 1 and c == 2) or a >= 2):
+                    continue
+                idx.append(so[p] + a * 3 + c)
+    K = np.zeros((len(idx), len(idx)))
+    for j, col in enumerate(idx):
+        u = np.zeros(n, complex)
+        u[col] = 2.0 if (col - so[np.searchsorted(so, col, side='right') - 1]) // 3 == 0 else 1.0
+        d.set("displ", "solid", u)
+        d.set("stiff", "solid", np.zeros(n, complex))
+        d.compute_stiff()
+        s = -d.get("stiff", "solid")
+        K[:, j] = s[idx].real
+    return K
+
+
+@pytest.mark.parametrize("kw", [dict(nu=1), dict(nu=2, mat=MAT_TISO), dict(nu=1, mat=MAT_ANISO)])
+def test_oracle_stiffness_positive_and_symmetric(kw):
+    """The reference's own self-test: K positive diagonal and self-adjoint."""
+    spec = synth.annulus_domain(n_theta=1, n_r=1, source=False, n_receivers=0, **kw)
+    K = _stiffness_matrix(spec)
+    assert (np.diag(K) > 0).all()
+    scale = np.abs(K).max()
+    assert np.abs(K - K.T).max() <= 1e-8 * scale
+
+
+def test_oracle_float_vs_double():
+    OD = _oracle()
+    for kw in (dict(), dict(in3d=True, mat=MAT_TISO, att=ATT_CG4, nu=3), dict(fluid_layers=(0,), att=ATT_FULL)):
+        spec = synth.annulus_domain(stf_len=16, **kw)
+        a, b = OD(spec), OD(spec, double=True)
+        a.step(16)
+        b.step(16)
+        ua, ub = a.get("displ"), b.get("displ")
+        assert np.linalg.norm(ua - ub) <= 1e-5 * np.linalg.norm(ub)
+
+
+def test_oracle_dft_conventions():
+    """C2R/R2C follow FFTW: C2R unnormalised ignoring Im(X0), R2C scaled by 1/nr."""
+    from oracle.oracle_py import load_oracle
+    load_oracle()
+    rng = np.random.default_rng(0)
+    for nr in (1, 2, 5, 8, 17):
+        x = rng.normal(size=nr)
+        X = np.fft.rfft(x) / nr
+        back = np.fft.irfft(X * nr, nr)
+        np.testing.assert_allclose(back, x, atol=1e-12)
+
+
+def test_header_declares_every_export():
+    decl = re.findall(r"^(?:int|int64_t|int32_t|size_t)\s+(ax3d_\w+)\(", (ROOT / "include/ax3d.h").read_text(), re.M)
+    assert len(decl) >= 20
+    lib = ROOT / "axisem3d_gb300/libax3d.so"
+    if not lib.exists():
+        from axisem3d_gb300 import build
+        build.build()
+    out = subprocess.run(["nm", "-D", "--defined-only", str(lib)], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\bT (ax3d_\w+)", out))
+    assert set(decl) <= exported, set(decl) - exported
+    ctypes.CDLL(str(lib))  # loads without a GPU
+
+
+def test_capi_rejects_bad_input_without_gpu():
+    """Argument checks happen before any device work."""
+    from axisem3d_gb300 import capi
+    lib = capi.load_library()
+    cfg = capi.Config()
+    cfg.npol = 5
+    h = ctypes.c_void_p()
+    assert lib.ax3d_create(ctypes.byref(cfg), ctypes.byref(h)) == 6
+    buf = ctypes.create_string_buffer(256)
+    lib.ax3d_last_error(buf, 256)
+    assert b"nPol" in buf.value

@@ -1,0 +1,119 @@
+"""GPU parity: the CUDA path through the C-ABI against the CPU oracle.
+
+Tolerance: relative L2 <= 1e-5 against the FP32 oracle (the reference's default Real),
+the spec bar for floating-point parity; the FP64 oracle error is reported too.
+"""
+import numpy as np
+import pytest
+
+from axisem3d_gb300 import synth
+from axisem3d_gb300.spec import ATT_CG4, ATT_FULL, ATT_NONE, MAT_ANISO, MAT_ISO, MAT_TISO
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+
+CASES = {
+    "iso1d": dict(),
+    "iso1d_fluid_mixednu": dict(fluid_layers=(0,), nu_random=True, nu_max=5),
+    "ti1d_full": dict(mat=MAT_TISO, att=ATT_FULL, nu=3),
+    "aniso1d_cg4": dict(mat=MAT_ANISO, att=ATT_CG4, nu=2),
+    "iso3d": dict(in3d=True, nu=4),
+    "ti3d_cg4": dict(in3d=True, mat=MAT_TISO, att=ATT_CG4, nu=6),
+    "ti3d_full_mixednu": dict(in3d=True, mat=MAT_TISO, att=ATT_FULL, nu_random=True, nu_max=9),
+    "aniso3d_full": dict(in3d=True, mat=MAT_ANISO, att=ATT_FULL, nu=5),
+    "fluid3d_mass3d_couple3d": dict(fluid_layers=(1,), in3d=True, fluid3d=True, mass3d=True,
+                                    couple3d=True, nu=4, mat=MAT_TISO),
+    "fluid_surface": dict(fluid_layers=(2,), nu=3),
+}
+
+
+def rel(a, b):
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
+
+
+def _pair(name, **extra):
+    from oracle.oracle_py import OracleDomain
+    from axisem3d_gb300.capi import Ax3dDomain
+    spec = synth.annulus_domain(**{**CASES[name], **extra})
+    return spec, Ax3dDomain(spec), OracleDomain(spec), OracleDomain(spec, double=True)
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_compute_stiff_matches_oracle(ax3d_lib, name):
+    spec, g, o, od = _pair(name)
+    su, fu = synth.random_fields(spec, seed=3)
+    for d in (g, o, od):
+        d.set("displ", "solid", su)
+        if d.nfluid:
+            d.set("displ", "fluid", fu)
+        d.compute_stiff()
+    for phase in ("solid", "fluid"):
+        if phase == "fluid" and not g.nfluid:
+            continue
+        a, b, c = g.get("stiff", phase), o.get("stiff", phase), od.get("stiff", phase)
+        assert rel(a, b) <= TOL, (phase, rel(a, b), rel(a, c))
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_time_loop_matches_oracle(ax3d_lib, name):
+    spec, g, o, od = _pair(name, stf_len=40, stability_interval=10)
+    su, fu = synth.random_fields(spec, seed=5, scale=1e-6)
+    for d in (g, o, od):
+        d.set("displ", "solid", su)
+        if d.nfluid:
+            d.set("displ", "fluid", fu)
+        d.step(40)
+    for which in ("displ", "veloc", "accel"):
+        a, b = g.get(which, "solid"), o.get(which, "solid")
+        assert rel(a, b) <= TOL, (which, rel(a, b))
+        if g.nfluid:
+            a, b = g.get(which, "fluid"), o.get(which, "fluid")
+            assert rel(a, b) <= TOL, (which, "fluid", rel(a, b))
+    sa, sb = g.seismograms(0, 40), o.seismograms(0, 40)
+    assert rel(sa, sb) <= TOL, rel(sa, sb)
+    assert g.current_step == o.current_step == 41
+
+
+@pytest.mark.parametrize("name", ["iso1d", "ti3d_cg4", "fluid3d_mass3d_couple3d"])
+def test_fine_grained_loop_bodies(ax3d_lib, name):
+    """Domain's loop bodies one at a time (update, source, stiff, couple, record)."""
+    spec, g, o, _ = _pair(name, stf_len=8)
+    su, fu = synth.random_fields(spec, seed=9, scale=1e-5)
+    for d in (g, o):
+        d.set("displ", "solid", su)
+        if d.nfluid:
+            d.set("displ", "fluid", fu)
+        for t in range(3):
+            d.update_newmark()
+            d.apply_source(t)
+            d.compute_stiff()
+            d.couple_solid_fluid()
+            d.record(t)
+    for which in ("displ", "veloc", "accel", "stiff"):
+        assert rel(g.get(which, "solid"), o.get(which, "solid")) <= TOL, which
+
+
+def test_kahan_closer_to_fp64(ax3d_lib):
+    """Compensated Newmark: the GPU run stays as close to the FP64 oracle as plain FP32."""
+    from oracle.oracle_py import OracleDomain
+    from axisem3d_gb300.capi import Ax3dDomain
+    spec = synth.annulus_domain(nu=2, stf_len=200, kahan=True)
+    g = Ax3dDomain(spec)
+    od = OracleDomain(spec, double=True)
+    g.step(200)
+    od.step(200)
+    assert rel(g.get("displ"), od.get("displ")) <= TOL
+
+
+def test_unstable_is_reported(ax3d_lib):
+    from axisem3d_gb300.capi import Ax3dDomain, Ax3dError
+    spec = synth.annulus_domain(nu=1, stf_len=8, stability_interval=2)
+    g = Ax3dDomain(spec)
+    su, _ = synth.random_fields(spec)
+    su[0] = np.nan
+    g.set("displ", "solid", su)
+    with pytest.raises(Ax3dError) as ei:
+        g.step(4)
+    assert ei.value.code == 4
