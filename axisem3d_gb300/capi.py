@@ -90,6 +90,8 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
     bind(lib, "ax3d_", P_F32)
     lib.ax3d_last_error.argtypes = [C.c_char_p, C.c_size_t]
     lib.ax3d_last_error.restype = C.c_size_t
+    lib.ax3d_enable_timers.argtypes = [C.c_void_p, C.c_int32]
+    lib.ax3d_read_timers.argtypes = [C.c_void_p, P_F64, P_I64]
     if path is None:
         _LIB = lib
     return lib
@@ -184,18 +186,25 @@ class _DomainBase:
     def current_step(self) -> int:
         return int(self._call("current_step", self.h))
 
-    def get(self, which: str = "displ", phase: str = "solid") -> np.ndarray:
+    @property
+    def complex_dtype(self):
+        return np.complex64 if self.field_dtype == np.float32 else np.complex128
+
+    def get(self, which: str = "displ", phase: str = "solid", out: np.ndarray | None = None) -> np.ndarray:
+        """Copy a field to the host as complex64 (GPU) / complex128 (FP64 oracle) values."""
         n = self.nsolid if phase == "solid" else self.nfluid
-        out = np.zeros(2 * max(n, 1), self.field_dtype)
-        self._ck(self._call("get_field", self.h, FIELD[which], PHASE[phase], _p(out, self.field_ctype)))
-        return out[:2 * n].astype(np.float64).view(np.complex128)
+        if out is None:
+            out = np.zeros(max(n, 1), self.complex_dtype)
+        buf = out.view(self.field_dtype)
+        self._ck(self._call("get_field", self.h, FIELD[which], PHASE[phase], _p(buf, self.field_ctype)))
+        return out[:n]
 
     def set(self, which: str, phase: str, values: np.ndarray):
         n = self.nsolid if phase == "solid" else self.nfluid
-        v = np.asarray(values, np.complex128)
+        v = np.ascontiguousarray(values, self.complex_dtype)
         if v.size != n:
             raise ValueError(f"field size {v.size} != {n}")
-        buf = np.ascontiguousarray(v.view(np.float64).astype(self.field_dtype))
+        buf = v.view(self.field_dtype)
         self._ck(self._call("set_field", self.h, FIELD[which], PHASE[phase], _p(buf, self.field_ctype)))
 
     def seismograms(self, first: int, n: int) -> np.ndarray:
@@ -222,9 +231,22 @@ class _DomainBase:
         self.close()
 
 
+TIMERS = ("step", "elements", "points", "assemble", "couple", "source", "record", "other")
+
+
 class Ax3dDomain(_DomainBase):
     """A domain resident on one GB300, driven through libax3d.so."""
 
     def __init__(self, spec: DomainSpec, device: int = 0, lib: C.CDLL | None = None):
         self.lib = lib or load_library()
         self._build(spec, device, with_first=True)
+
+    def enable_timers(self, on: bool = True):
+        self._ck(self.lib.ax3d_enable_timers(self.h, int(on)))
+
+    def read_timers(self) -> dict:
+        """{phase: (device ms, kernel launches)} accumulated since the last read."""
+        ms = np.zeros(len(TIMERS))
+        n = np.zeros(len(TIMERS), np.int64)
+        self._ck(self.lib.ax3d_read_timers(self.h, _p(ms, C.c_double), _p(n, C.c_int64)))
+        return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(TIMERS)}

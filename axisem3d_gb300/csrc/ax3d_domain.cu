@@ -134,7 +134,60 @@ struct ax3d_domain {
     int64_t nsolid = 0, nfluid = 0;  // complex sizes
     int nitems_s = 0, nitems_f = 0;
 
+    // ---------------- phase timers ----------------
+    bool timers = false;
+    double t_ms[AX3D_NTIMERS] = {};
+    int64_t t_launch[AX3D_NTIMERS] = {};
+    struct Mark {
+        int phase;
+        cudaEvent_t a, b;
+    };
+    std::vector<Mark> marks;
+    std::vector<cudaEvent_t> pool;
+    int open_phase = -1;
+    cudaEvent_t open_ev = nullptr;
+
+    cudaEvent_t get_event() {
+        if (!pool.empty()) {
+            cudaEvent_t e = pool.back();
+            pool.pop_back();
+            return e;
+        }
+        cudaEvent_t e;
+        CK(cudaEventCreate(&e));
+        return e;
+    }
+    void tbegin(int ph) {
+        if (!timers) return;
+        open_phase = ph;
+        open_ev = get_event();
+        CK(cudaEventRecord(open_ev, stream));
+    }
+    void tend(int nlaunch) {
+        if (open_phase < 0) return;
+        cudaEvent_t b = get_event();
+        CK(cudaEventRecord(b, stream));
+        marks.push_back({open_phase, open_ev, b});
+        t_launch[open_phase] += nlaunch;
+        open_phase = -1;
+    }
+    void collect_timers() {  // stream already synchronised
+        for (auto &m : marks) {
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, m.a, m.b));
+            t_ms[m.phase] += ms;
+            pool.push_back(m.a);
+            pool.push_back(m.b);
+        }
+        marks.clear();
+    }
+
     ~ax3d_domain() {
+        for (auto &m : marks) {
+            cudaEventDestroy(m.a);
+            cudaEventDestroy(m.b);
+        }
+        for (auto e : pool) cudaEventDestroy(e);
         if (stream) cudaStreamDestroy(stream);
     }
 
@@ -510,22 +563,60 @@ struct ax3d_domain {
         std::swap(nb.n, d_seis.n);
         seis_cap = cap;
     }
+    int n_elem_launches() const {
+        return (nitems_s > 0) + (nitems_f > 0) + (int)buckets_s.size() + (int)buckets_f.size();
+    }
     int step(int nsteps) {
         need_final();
+        cudaEvent_t s0 = nullptr, s1 = nullptr;
+        if (timers) {
+            s0 = get_event();
+            CK(cudaEventRecord(s0, stream));
+        }
+        const int nrow = (P.nsrows > 0) + (P.nfrows > 0);
         for (int s = 0; s < nsteps; s++) {
+            tbegin(AX3D_TIMER_POINTS);
             update_newmark();
-            if (!s_elem.empty()) apply_source(tstep - 1);
-            compute_stiff();
+            tend(nrow + (n_pts3d > 0));
+            if (!s_elem.empty()) {
+                tbegin(AX3D_TIMER_SOURCE);
+                apply_source(tstep - 1);
+                tend(1);
+            }
+            tbegin(AX3D_TIMER_ELEMENTS);
+            ax3d::launch_elem_fourier_solid(T, P, F.su, d_items_s.p, nitems_s, sls, stream);
+            ax3d::launch_elem_fourier_fluid(T, P, F.fu, d_items_f.p, nitems_f, stream);
+            for (auto &b : buckets_s) ax3d::launch_elem_phys_solid(T, P, F.su, b, sls, stream);
+            for (auto &b : buckets_f) ax3d::launch_elem_phys_fluid(T, P, F.fu, b, stream);
+            tend(n_elem_launches());
+            tbegin(AX3D_TIMER_ASSEMBLE);
+            ax3d::launch_gather(P, T, F, stream);
+            tend(nrow);
+            tbegin(AX3D_TIMER_COUPLE);
             couple();
-            record(tstep - 1);
-            if (stab_interval > 0 && tstep % stab_interval == 0)
+            tend((P.nsrows > 0) + (n_sf3d > 0));
+            if (!r_elem.empty()) {
+                tbegin(AX3D_TIMER_RECORD);
+                record(tstep - 1);
+                tend(1);
+            }
+            if (stab_interval > 0 && tstep % stab_interval == 0) {
+                tbegin(AX3D_TIMER_OTHER);
                 ax3d::launch_stability(F.su, nsolid, F.fu, nfluid, d_flag.p, stream);
+                tend(1);
+            }
             tstep++;
+        }
+        if (timers) {
+            s1 = get_event();
+            CK(cudaEventRecord(s1, stream));
+            marks.push_back({AX3D_TIMER_STEP, s0, s1});
         }
         CK(cudaGetLastError());
         int32_t flag = 0;
         CK(cudaMemcpyAsync(&flag, d_flag.p, sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
         CK(cudaStreamSynchronize(stream));
+        if (timers) collect_timers();
         if (flag) throw Error(AX3D_ERR_UNSTABLE, "Domain::checkStability || Simulation blew up.");
         return AX3D_OK;
     }
@@ -751,6 +842,25 @@ int ax3d_reset(ax3d_domain *d) {
 }
 
 int32_t ax3d_current_step(const ax3d_domain *d) { return d ? d->tstep : -1; }
+
+int ax3d_enable_timers(ax3d_domain *d, int32_t enable) {
+    return guard([&] {
+        if (!d) throw Error(AX3D_ERR_ARG, "ax3d_enable_timers || null domain");
+        d->timers = enable != 0;
+    });
+}
+
+int ax3d_read_timers(ax3d_domain *d, double *ms, int64_t *launches) {
+    return guard([&] {
+        if (!d) throw Error(AX3D_ERR_ARG, "ax3d_read_timers || null domain");
+        for (int i = 0; i < AX3D_NTIMERS; i++) {
+            if (ms) ms[i] = d->t_ms[i];
+            if (launches) launches[i] = d->t_launch[i];
+            d->t_ms[i] = 0.;
+            d->t_launch[i] = 0;
+        }
+    });
+}
 
 int ax3d_destroy(ax3d_domain *d) {
     delete d;

@@ -27,11 +27,11 @@ void set_g_matrices(const float *g_gll, const float *g_glj, cudaStream_t s) {
 }
 
 constexpr int FW_WARPS = 8;   // warps per CTA in the Fourier-space kernels
-constexpr int PH_THREADS = 256;
+constexpr int PH_THREADS = 512;
 constexpr int PH_WARPS = PH_THREADS / 32;
 constexpr int QSCR = 14 * 25;  // per-warp scratch (float2) for grad/quad
-constexpr int KT = 8;          // DFT tile: samples (or orders) per thread
-constexpr int CT = 4;          // DFT tile: columns per thread
+constexpr int CG = 16;         // DFT: column padding (warp tasks take 8 or 16 columns)
+constexpr int RESEED = 8;      // DFT: exact twiddle reload interval
 constexpr size_t SMEM_MAX = 227 * 1024;
 
 // scatterDisplToElement (SolidPoint.cpp:175-195): orders above the point's Nu, and its
@@ -184,17 +184,21 @@ void launch_elem_fourier_fluid(const ElemTable &T, const PointTable &P, const fl
 // ------------------------------------------------------------------------------------
 // Physical-space elements: CTA per element
 // ------------------------------------------------------------------------------------
-// Shared layout (bytes): tw[nr] float2 | F[n][ncolp] float2 | X[nr][ncolp] float,
-// where the per-warp grad/quad scratch aliases X (X is dead in those phases).
-__host__ __device__ inline int pad4(int x) { return (x + 3) & ~3; }
+// Shared layout: tw[nr] float2 | F[n][SF] float2 | X[nr][SX] float.  The per-warp
+// grad/quad scratch aliases X (X is dead in phases 1 and 5).  Column counts are padded
+// to CG; SF = 2 (mod 16) and SX = 4 (mod 32) keep the row-wise vector stores of the
+// transforms free of bank conflicts.
+__host__ __device__ inline int round_up(int x, int m) { return (x + m - 1) / m * m; }
+__host__ __device__ inline int stride_f(int ncolg) { return ncolg + 2; }                        // = 2 mod 16
+__host__ __device__ inline int stride_x(int ncolg) { return ncolg + ((ncolg % 32) ? 20 : 4); }  // = 4 mod 32
 
 size_t phys_smem_bytes(int nr, int ncomp, int npts_chunk) {
-    int n = nr / 2 + 1;
-    int ncolp = pad4(ncomp * npts_chunk);
-    size_t tw = (size_t)8 * ((nr + 1) & ~1);
-    size_t F = (size_t)8 * n * ncolp;
-    size_t X = (size_t)4 * nr * ncolp;
-    size_t scr = (size_t)PH_WARPS * QSCR * 8;
+    const int n = nr / 2 + 1;
+    const int ncolg = round_up(ncomp * npts_chunk, CG);
+    const size_t tw = (size_t)8 * ((nr + 1) & ~1);
+    const size_t F = (size_t)8 * n * stride_f(ncolg);
+    const size_t X = (size_t)4 * nr * stride_x(ncolg);
+    const size_t scr = (size_t)PH_WARPS * QSCR * 8;
     return tw + F + (X > scr ? X : scr);
 }
 
@@ -206,121 +210,196 @@ int phys_points_per_chunk(int nr, int ncomp) {
     return 0;  // does not fit even one point per pass
 }
 
-// C2R of ncolp columns: X[k][col] = Re F[0][col] + 2 sum_{a=1}^{lim} Re(F[a][col] e^{+i 2pi k a/nr})
-__device__ void phys_c2r(const float2 *__restrict__ tw, const float2 *__restrict__ F,
-                         float *__restrict__ X, int nr, int lim, int ncolp) {
-    const int kh = nr / 2 + 1;  // k = 0 .. nr/2 computed, mirrors filled by parity
-    const int nkb = (kh + KT - 1) / KT, ncb = ncolp / CT;
-    for (int tile = threadIdx.x; tile < nkb * ncb; tile += blockDim.x) {
-        const int kb = tile / ncb, cb = tile - kb * ncb;
-        const int k0 = kb * KT, c0 = cb * CT;
-        float cs[KT][CT], sn[KT][CT];
-        int idx[KT], inc[KT];
+// C2R, lane = output sample: X[k][c] = Re F[0][c] + 2 sum_{a=1}^{lim} Re(F[a][c] w^{k a}),
+// w = e^{i 2 pi / nr}, for k = 0..nr/2; the mirror sample nr - k follows from the parity of
+// cos / sin.  Each warp task covers KL*32 samples x CG columns; F rows are read with
+// broadcast vector loads, the twiddle w^{ka} is advanced by one complex rotation per
+// order and reloaded exactly from the table every RESEED orders.
+template <int KL, int CG>
+__device__ __forceinline__ void c2r_task(const float2 *__restrict__ tw, const float2 *__restrict__ F, int SF,
+                                         float *__restrict__ X, int SX, int nr, int lim, int kb, int c0, int lane) {
+    const int kh = nr / 2 + 1;
+    int k[KL], idx[KL];
+    float2 w[KL], w1[KL];
+    float cs[KL][CG], sn[KL][CG];
 #pragma unroll
-        for (int t = 0; t < KT; t++) {
-            idx[t] = 0;
-            inc[t] = (k0 + t) % nr;
+    for (int j = 0; j < KL; j++) {
+        k[j] = kb * (32 * KL) + j * 32 + lane;
+        const int kk = k[j] < kh ? k[j] : 0;
+        idx[j] = kk;
+        w1[j] = tw[kk];
+        w[j] = w1[j];
 #pragma unroll
-            for (int c = 0; c < CT; c++) cs[t][c] = sn[t][c] = 0.f;
-        }
-        for (int a = 1; a <= lim; a++) {
-            const float4 f01 = *reinterpret_cast<const float4 *>(F + (int64_t)a * ncolp + c0);
-            const float4 f23 = *reinterpret_cast<const float4 *>(F + (int64_t)a * ncolp + c0 + 2);
-            const float fr[4] = {f01.x, f01.z, f23.x, f23.z};
-            const float fi[4] = {f01.y, f01.w, f23.y, f23.w};
+        for (int c = 0; c < CG; c++) cs[j][c] = sn[j][c] = 0.f;
+    }
+    int step8[KL];
 #pragma unroll
-            for (int t = 0; t < KT; t++) {
-                int m = idx[t] + inc[t];  // (k * a) mod nr, incrementally
-                m = m >= nr ? m - nr : m;
-                idx[t] = m;
-                const float2 w = tw[m];
+    for (int j = 0; j < KL; j++) step8[j] = (RESEED * (k[j] < kh ? k[j] : 0)) % nr;
+    for (int a0 = 1; a0 <= lim; a0 += RESEED) {
+        // exact twiddle w^{k a0} at the start of every block, rotations inside it
 #pragma unroll
-                for (int c = 0; c < CT; c++) {
-                    cs[t][c] = fmaf(fr[c], w.x, cs[t][c]);
-                    sn[t][c] = fmaf(fi[c], w.y, sn[t][c]);
+        for (int j = 0; j < KL; j++) w[j] = tw[idx[j]];
+        const int aend = min(a0 + RESEED, lim + 1);
+#pragma unroll 2
+        for (int a = a0; a < aend; a++) {
+            const float4 *fp = reinterpret_cast<const float4 *>(F + (int64_t)a * SF + c0);
+#pragma unroll
+            for (int q = 0; q < CG / 2; q++) {
+                const float4 f = fp[q];
+#pragma unroll
+                for (int j = 0; j < KL; j++) {
+                    cs[j][2 * q] = fmaf(f.x, w[j].x, cs[j][2 * q]);
+                    sn[j][2 * q] = fmaf(f.y, w[j].y, sn[j][2 * q]);
+                    cs[j][2 * q + 1] = fmaf(f.z, w[j].x, cs[j][2 * q + 1]);
+                    sn[j][2 * q + 1] = fmaf(f.w, w[j].y, sn[j][2 * q + 1]);
                 }
             }
+#pragma unroll
+            for (int j = 0; j < KL; j++) w[j] = cmul(w[j], w1[j]);
         }
-        float f0[CT];
 #pragma unroll
-        for (int c = 0; c < CT; c++) f0[c] = F[c0 + c].x;
+        for (int j = 0; j < KL; j++) {
+            idx[j] += step8[j];
+            if (idx[j] >= nr) idx[j] -= nr;
+        }
+    }
+    float f0[CG];
 #pragma unroll
-        for (int t = 0; t < KT; t++) {
-            const int k = k0 + t;
-            if (k >= kh) break;
-            float lo[CT], hi[CT];
+    for (int c = 0; c < CG; c++) f0[c] = F[c0 + c].x;
 #pragma unroll
-            for (int c = 0; c < CT; c++) {
-                lo[c] = f0[c] + 2.f * (cs[t][c] - sn[t][c]);
-                hi[c] = f0[c] + 2.f * (cs[t][c] + sn[t][c]);
-            }
-            *reinterpret_cast<float4 *>(X + (int64_t)k * ncolp + c0) = make_float4(lo[0], lo[1], lo[2], lo[3]);
-            const int km = nr - k;
-            if (k > 0 && km != k)
-                *reinterpret_cast<float4 *>(X + (int64_t)km * ncolp + c0) =
-                    make_float4(hi[0], hi[1], hi[2], hi[3]);
+    for (int j = 0; j < KL; j++) {
+        if (k[j] >= kh) continue;
+        float4 *lo = reinterpret_cast<float4 *>(X + (int64_t)k[j] * SX + c0);
+#pragma unroll
+        for (int q = 0; q < CG / 4; q++)
+            lo[q] = make_float4(f0[4 * q] + 2.f * (cs[j][4 * q] - sn[j][4 * q]),
+                                f0[4 * q + 1] + 2.f * (cs[j][4 * q + 1] - sn[j][4 * q + 1]),
+                                f0[4 * q + 2] + 2.f * (cs[j][4 * q + 2] - sn[j][4 * q + 2]),
+                                f0[4 * q + 3] + 2.f * (cs[j][4 * q + 3] - sn[j][4 * q + 3]));
+        const int km = nr - k[j];
+        if (k[j] > 0 && km != k[j]) {
+            float4 *hi = reinterpret_cast<float4 *>(X + (int64_t)km * SX + c0);
+#pragma unroll
+            for (int q = 0; q < CG / 4; q++)
+                hi[q] = make_float4(f0[4 * q] + 2.f * (cs[j][4 * q] + sn[j][4 * q]),
+                                    f0[4 * q + 1] + 2.f * (cs[j][4 * q + 1] + sn[j][4 * q + 1]),
+                                    f0[4 * q + 2] + 2.f * (cs[j][4 * q + 2] + sn[j][4 * q + 2]),
+                                    f0[4 * q + 3] + 2.f * (cs[j][4 * q + 3] + sn[j][4 * q + 3]));
         }
     }
 }
 
-// R2C of ncolp columns scaled by 1/nr, orders 0..lim:
-// F[a] = (x_0 + sum_{k=1}^{(nr-1)/2} (x_k + x_{nr-k}) cos - i (x_k - x_{nr-k}) sin
-//         + [nr even] (-1)^a x_{nr/2}) / nr
-__device__ void phys_r2c(const float2 *__restrict__ tw, const float *__restrict__ X,
-                         float2 *__restrict__ F, int nr, int lim, int ncolp) {
+__device__ void phys_c2r(const float2 *tw, const float2 *F, int SF, float *X, int SX, int nr, int lim, int ncolg) {
+    const int kh = nr / 2 + 1;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    if (kh >= 96) {
+        const int ncg = ncolg / 8, nkb = (kh + 63) / 64;
+        for (int t = warp; t < nkb * ncg; t += nw) c2r_task<2, 8>(tw, F, SF, X, SX, nr, lim, t / ncg, (t % ncg) * 8, lane);
+    } else {
+        const int ncg = ncolg / 16, nkb = (kh + 31) / 32;
+        for (int t = warp; t < nkb * ncg; t += nw) c2r_task<1, 16>(tw, F, SF, X, SX, nr, lim, t / ncg, (t % ncg) * 16, lane);
+    }
+}
+
+// In place: X[k] <- X[k] + X[nr-k], X[nr-k] <- X[k] - X[nr-k] for k = 1..(nr-1)/2.
+__device__ void phys_fold(float *X, int SX, int nr, int ncolg) {
     const int k2 = (nr - 1) / 2;
-    const int na = lim + 1;
-    const int nab = (na + KT - 1) / KT, ncb = ncolp / CT;
-    const float inv_nr = 1.f / (float)nr;
-    for (int tile = threadIdx.x; tile < nab * ncb; tile += blockDim.x) {
-        const int ab = tile / ncb, cb = tile - ab * ncb;
-        const int a0 = ab * KT, c0 = cb * CT;
-        float re[KT][CT], im[KT][CT];
-        int idx[KT], inc[KT];
+    const int nq = ncolg / 4;
+    for (int t = threadIdx.x; t < k2 * nq; t += blockDim.x) {
+        const int k = 1 + t / nq, q = t - (k - 1) * nq;
+        float4 *a = reinterpret_cast<float4 *>(X + (int64_t)k * SX) + q;
+        float4 *b = reinterpret_cast<float4 *>(X + (int64_t)(nr - k) * SX) + q;
+        const float4 x = *a, y = *b;
+        *a = make_float4(x.x + y.x, x.y + y.y, x.z + y.z, x.w + y.w);
+        *b = make_float4(x.x - y.x, x.y - y.y, x.z - y.z, x.w - y.w);
+    }
+}
+
+// R2C (after phys_fold), lane = output order a = 0..lim, scaled by 1/nr:
+// F[a] = (x_0 + sum_k s_k cos(k a t) + [nr even] (-1)^a x_{nr/2}, -sum_k d_k sin(k a t)) / nr.
+template <int KL, int CG>
+__device__ __forceinline__ void r2c_task(const float2 *__restrict__ tw, const float *__restrict__ X, int SX,
+                                         float2 *__restrict__ F, int SF, int nr, int lim, int ab, int c0, int lane) {
+    const int na = lim + 1, k2 = (nr - 1) / 2;
+    int a[KL], idx[KL];
+    float2 w[KL], w1[KL];
+    float re[KL][CG], im[KL][CG];
 #pragma unroll
-        for (int t = 0; t < KT; t++) {
-            idx[t] = 0;
-            inc[t] = (a0 + t) % nr;
+    for (int j = 0; j < KL; j++) {
+        a[j] = ab * (32 * KL) + j * 32 + lane;
+        const int aa = a[j] < na ? a[j] : 0;
+        idx[j] = aa;
+        w1[j] = tw[aa];
+        w[j] = w1[j];
 #pragma unroll
-            for (int c = 0; c < CT; c++) re[t][c] = im[t][c] = 0.f;
-        }
-        for (int k = 1; k <= k2; k++) {
-            const float4 xl = *reinterpret_cast<const float4 *>(X + (int64_t)k * ncolp + c0);
-            const float4 xh = *reinterpret_cast<const float4 *>(X + (int64_t)(nr - k) * ncolp + c0);
-            const float sm[4] = {xl.x + xh.x, xl.y + xh.y, xl.z + xh.z, xl.w + xh.w};
-            const float df[4] = {xl.x - xh.x, xl.y - xh.y, xl.z - xh.z, xl.w - xh.w};
+        for (int c = 0; c < CG; c++) re[j][c] = im[j][c] = 0.f;
+    }
+    int step8[KL];
 #pragma unroll
-            for (int t = 0; t < KT; t++) {
-                int m = idx[t] + inc[t];  // (k * a) mod nr, incrementally in k
-                m = m >= nr ? m - nr : m;
-                idx[t] = m;
-                const float2 w = tw[m];
+    for (int j = 0; j < KL; j++) step8[j] = (RESEED * (a[j] < na ? a[j] : 0)) % nr;
+    for (int k0 = 1; k0 <= k2; k0 += RESEED) {
 #pragma unroll
-                for (int c = 0; c < CT; c++) {
-                    re[t][c] = fmaf(sm[c], w.x, re[t][c]);
-                    im[t][c] = fmaf(df[c], w.y, im[t][c]);
+        for (int j = 0; j < KL; j++) w[j] = tw[idx[j]];
+        const int kend = min(k0 + RESEED, k2 + 1);
+#pragma unroll 2
+        for (int k = k0; k < kend; k++) {
+            const float4 *sp = reinterpret_cast<const float4 *>(X + (int64_t)k * SX + c0);
+            const float4 *dp = reinterpret_cast<const float4 *>(X + (int64_t)(nr - k) * SX + c0);
+#pragma unroll
+            for (int q = 0; q < CG / 4; q++) {
+                const float4 sv = sp[q], d = dp[q];
+#pragma unroll
+                for (int j = 0; j < KL; j++) {
+                    re[j][4 * q] = fmaf(sv.x, w[j].x, re[j][4 * q]);
+                    re[j][4 * q + 1] = fmaf(sv.y, w[j].x, re[j][4 * q + 1]);
+                    re[j][4 * q + 2] = fmaf(sv.z, w[j].x, re[j][4 * q + 2]);
+                    re[j][4 * q + 3] = fmaf(sv.w, w[j].x, re[j][4 * q + 3]);
+                    im[j][4 * q] = fmaf(d.x, w[j].y, im[j][4 * q]);
+                    im[j][4 * q + 1] = fmaf(d.y, w[j].y, im[j][4 * q + 1]);
+                    im[j][4 * q + 2] = fmaf(d.z, w[j].y, im[j][4 * q + 2]);
+                    im[j][4 * q + 3] = fmaf(d.w, w[j].y, im[j][4 * q + 3]);
                 }
             }
-        }
-        const float4 x0 = *reinterpret_cast<const float4 *>(X + c0);
-        const float x0v[4] = {x0.x, x0.y, x0.z, x0.w};
-        float xn[4] = {0.f, 0.f, 0.f, 0.f};
-        if (nr % 2 == 0) {
-            const float4 t4 = *reinterpret_cast<const float4 *>(X + (int64_t)(nr / 2) * ncolp + c0);
-            xn[0] = t4.x; xn[1] = t4.y; xn[2] = t4.z; xn[3] = t4.w;
+#pragma unroll
+            for (int j = 0; j < KL; j++) w[j] = cmul(w[j], w1[j]);
         }
 #pragma unroll
-        for (int t = 0; t < KT; t++) {
-            const int a = a0 + t;
-            if (a >= na) break;
-            const float sgn = (a & 1) ? -1.f : 1.f;
-            float2 o[CT];
-#pragma unroll
-            for (int c = 0; c < CT; c++)
-                o[c] = make_float2((x0v[c] + re[t][c] + sgn * xn[c]) * inv_nr, -im[t][c] * inv_nr);
-            *reinterpret_cast<float4 *>(F + (int64_t)a * ncolp + c0) = make_float4(o[0].x, o[0].y, o[1].x, o[1].y);
-            *reinterpret_cast<float4 *>(F + (int64_t)a * ncolp + c0 + 2) = make_float4(o[2].x, o[2].y, o[3].x, o[3].y);
+        for (int j = 0; j < KL; j++) {
+            idx[j] += step8[j];
+            if (idx[j] >= nr) idx[j] -= nr;
         }
+    }
+    const float inv_nr = 1.f / (float)nr;
+    float x0[CG], xn[CG];
+#pragma unroll
+    for (int c = 0; c < CG; c++) {
+        x0[c] = X[c0 + c];
+        xn[c] = (nr % 2 == 0) ? X[(int64_t)(nr / 2) * SX + c0 + c] : 0.f;
+    }
+#pragma unroll
+    for (int j = 0; j < KL; j++) {
+        if (a[j] >= na) continue;
+        const float sgn = (a[j] & 1) ? -1.f : 1.f;
+        float4 *o = reinterpret_cast<float4 *>(F + (int64_t)a[j] * SF + c0);
+#pragma unroll
+        for (int q = 0; q < CG / 2; q++)
+            o[q] = make_float4((x0[2 * q] + re[j][2 * q] + sgn * xn[2 * q]) * inv_nr, -im[j][2 * q] * inv_nr,
+                               (x0[2 * q + 1] + re[j][2 * q + 1] + sgn * xn[2 * q + 1]) * inv_nr,
+                               -im[j][2 * q + 1] * inv_nr);
+    }
+}
+
+__device__ void phys_r2c(const float2 *tw, float *X, int SX, float2 *F, int SF, int nr, int lim, int ncolg) {
+    phys_fold(X, SX, nr, ncolg);
+    __syncthreads();
+    const int na = lim + 1;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    if (na >= 96) {
+        const int ncg = ncolg / 8, nab = (na + 63) / 64;
+        for (int t = warp; t < nab * ncg; t += nw) r2c_task<2, 8>(tw, X, SX, F, SF, nr, lim, t / ncg, (t % ncg) * 8, lane);
+    } else {
+        const int ncg = ncolg / 16, nab = (na + 31) / 32;
+        for (int t = warp; t < nab * ncg; t += nw) r2c_task<1, 16>(tw, X, SX, F, SF, nr, lim, t / ncg, (t % ncg) * 16, lane);
     }
 }
 
@@ -330,18 +409,117 @@ __device__ void fill_twiddles(float2 *tw, const ElemTable &T, int nr) {
     for (int m = threadIdx.x; m < nr; m += blockDim.x) tw[m] = src[m];
 }
 
-template <int NCOMP>
-__device__ __forceinline__ void phys_layout(int nr, int P, float2 *&tw, float2 *&F, float *&X,
-                                            float2 *&scr, int &ncolp, char *smem) {
-    const int n = nr / 2 + 1;
-    ncolp = pad4(NCOMP * P);
-    tw = reinterpret_cast<float2 *>(smem);
-    F = tw + ((nr + 1) & ~1);  // keep F 16-byte aligned
-    X = reinterpret_cast<float *>(F + (int64_t)n * ncolp);
-    scr = reinterpret_cast<float2 *>(X);
+// Phase 3a of the physical-space solid kernel: SLS memory variables (Attenuation3D_Full
+// / _CG4 applyToStress + updateMemoryVariables) with one thread per (sample, attenuated
+// point, component): the loads of R and stressR are independent across threads and the
+// dependent chain per thread is one load-update-store.  The sum of the old memory
+// variables, which applyToStress subtracts from the stress, goes to dR[k][c][q] (the
+// Fourier buffer, dead during this phase; 6 Pc nr floats fit in its n * SF complex).
+__device__ __forceinline__ void sls_phase(const float *X, int SX, float *mem, const float *__restrict__ am,
+                                          int64_t sl, int npa, int att, const SLS &sls, int nr, int Pc, int p0,
+                                          float *dR) {
+    // attenuated points: CG4 -> (6, 8, 16, 18) when inside this chunk; full -> all
+    const int npts = att == 2 ? 4 : Pc;
+    const int total = nr * npts * 6;
+    const float third = (float)(1.0 / 3.0);
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        const int c = t % 6, r = t / 6, k = r / npts, j = r - k * npts;
+        int pp, qq;
+        if (att == 2) {
+            const int pg = j < 2 ? 6 + 2 * j : 16 + 2 * (j - 2);
+            if (pg < p0 || pg >= p0 + Pc) continue;
+            pp = pg - p0;
+            qq = j;
+        } else {
+            pp = j;
+            qq = p0 + j;
+        }
+        float e[6];
+#pragma unroll
+        for (int i = 0; i < 6; i++) e[i] = X[(int64_t)k * SX + i * Pc + pp];
+        float *R = mem + (int64_t)k * 6 * npa + (int64_t)c * npa + qq;
+        float *SR = R + sls.nsls * sl;
+        const float sr_old = *SR;
+        const float dk = am[(int64_t)k * npa + qq], dmu = am[(int64_t)nr * npa + (int64_t)k * npa + qq];
+        const float e3 = (e[0] + e[1] + e[2]) * third;
+        float snew;
+        if (c < 3) {
+            if (sls.do_kappa) {
+                snew = 3.f * dk * e3 + 2.f * dmu * (e[c] - e3);
+            } else if (c < 2) {
+                snew = 2.f * dmu * (e[c] - e3);
+            } else {
+                snew = -(2.f * dmu * (e[0] - e3) + 2.f * dmu * (e[1] - e3));
+            }
+        } else {
+            snew = dmu * e[c];
+        }
+        float acc = 0.f;
+        for (int l = 0; l < sls.nsls; l++) {
+            const float r0 = R[l * sl];
+            acc += r0;
+            R[l * sl] = (sls.a[l] * r0 + sls.b[l] * sr_old) + sls.g[l] * snew;
+        }
+        *SR = snew;
+        dR[((int64_t)k * 6 + c) * Pc + pp] = acc;
+    }
 }
 
-__global__ void __launch_bounds__(PH_THREADS)
+// Phase 3b: strain -> stress at every (sample, point) of the chunk, in place in X, minus
+// the memory-variable sum from phase 3a.  Each thread takes IT items and issues all their
+// modulus loads before any arithmetic, so enough loads are in flight to keep HBM busy.
+template <int MAT, int IT>
+__device__ __forceinline__ void stress_phase(float *X, int SX, const float *__restrict__ md, int att,
+                                             int nr, int Pc, int p0, const float *dR) {
+    constexpr int NM = MAT == 0 ? 2 : MAT == 1 ? 5 : 21;
+    const int total = nr * Pc;
+    for (int t0 = threadIdx.x; t0 < total; t0 += blockDim.x * IT) {
+        float mv[IT][NM];
+#pragma unroll
+        for (int i = 0; i < IT; i++) {
+            const int t = t0 + i * blockDim.x;
+            if (t < total) {
+                const int k = t / Pc, pg = p0 + (t - k * Pc);
+#pragma unroll
+                for (int m = 0; m < NM; m++) mv[i][m] = __ldg(md + ((int64_t)m * nr + k) * NPE + pg);
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < IT; i++) {
+            const int t = t0 + i * blockDim.x;
+            if (t >= total) break;
+            const int k = t / Pc, pp = t - k * Pc, pg = p0 + pp;
+            float e6[6], s6[6];
+#pragma unroll
+            for (int c = 0; c < 6; c++) e6[c] = X[(int64_t)k * SX + c * Pc + pp];
+            elastic(MAT, e6, s6, [&](int m) { return mv[i][m]; });
+            if (att && (att == 1 || cg4_index(pg) >= 0)) {
+#pragma unroll
+                for (int c = 0; c < 6; c++) s6[c] -= dR[((int64_t)k * 6 + c) * Pc + pp];
+            }
+#pragma unroll
+            for (int c = 0; c < 6; c++) X[(int64_t)k * SX + c * Pc + pp] = s6[c];
+        }
+    }
+}
+
+struct PhysLayout {
+    float2 *tw, *F, *scr;
+    float *X;
+    int ncolg, SF, SX;
+    __device__ PhysLayout(char *smem, int nr, int ncomp, int Pmax) {
+        const int n = nr / 2 + 1;
+        ncolg = round_up(ncomp * Pmax, CG);
+        SF = stride_f(ncolg);
+        SX = stride_x(ncolg);
+        tw = reinterpret_cast<float2 *>(smem);
+        F = tw + ((nr + 1) & ~1);
+        X = reinterpret_cast<float *>(F + (int64_t)n * SF);
+        scr = reinterpret_cast<float2 *>(X);
+    }
+};
+
+__global__ void __launch_bounds__(PH_THREADS, 1)
     k_elem_phys_solid(ElemTable T, PointTable P, const float2 *__restrict__ su,
                       const int32_t *__restrict__ elems, int Pmax, SLS sls) {
     extern __shared__ __align__(16) char smem[];
@@ -352,12 +530,12 @@ __global__ void __launch_bounds__(PH_THREADS)
     const int mat = ef_mat(flags), att = ef_att(flags);
     const bool tiso = (mat == 1 || mat == 2);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    float2 *tw, *F, *scr;
-    float *X;
-    int ncolp;
-    phys_layout<6>(nr, Pmax, tw, F, X, scr, ncolp, smem);
+    PhysLayout S(smem, nr, 6, Pmax);
+    float2 *tw = S.tw, *F = S.F;
+    float *X = S.X;
+    const int SF = S.SF, SX = S.SX;
     fill_twiddles(tw, T, nr);
-    float2 *q = scr + warp * QSCR;
+    float2 *q = S.scr + warp * QSCR;
     const bool active = lane < NPE;
     const int p = active ? lane : 0;
     LaneOps L;
@@ -383,15 +561,17 @@ __global__ void __launch_bounds__(PH_THREADS)
     for (int p0 = 0; p0 < NPE; p0 += Pmax) {
         const int Pc = min(Pmax, NPE - p0);
         const int ncol = 6 * Pc;
+        const int ncolg = round_up(ncol, CG);
         const bool mine = active && p >= p0 && p < p0 + Pc;
         // ---- phase 1: strain (grad6 + rotation) of the chunk's points, all orders ----
+        float2 un[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+        if (active && warp < n) load_solid_u(P, su, pt_me, warp, un);
         for (int a = warp; a < n; a += PH_WARPS) {
             if (active) {
-                float2 u[3];
-                load_solid_u(P, su, pt_me, a, u);
-                q[p] = u[0];
-                q[25 + p] = u[1];
-                q[50 + p] = u[2];
+                q[p] = un[0];
+                q[25 + p] = un[1];
+                q[50 + p] = un[2];
+                if (a + PH_WARPS < n) load_solid_u(P, su, pt_me, a + PH_WARPS, un);  // prefetch
             }
             __syncwarp();
             float2 eps[6];
@@ -403,68 +583,58 @@ __global__ void __launch_bounds__(PH_THREADS)
             }
             if (mine)
 #pragma unroll
-                for (int c = 0; c < 6; c++) F[(int64_t)a * ncolp + c * Pc + (p - p0)] = eps[c];
-            for (int c = ncol + lane; c < ncolp; c += 32) F[(int64_t)a * ncolp + c] = make_float2(0.f, 0.f);
+                for (int c = 0; c < 6; c++) F[(int64_t)a * SF + c * Pc + (p - p0)] = eps[c];
+            for (int c = ncol + lane; c < ncolg; c += 32) F[(int64_t)a * SF + c] = make_float2(0.f, 0.f);
             __syncwarp();
         }
         __syncthreads();
         // ---- phase 2: C2R to nr samples ----
-        phys_c2r(tw, F, X, nr, lim, ncolp);
+        phys_c2r(tw, F, SF, X, SX, nr, lim, ncolg);
         __syncthreads();
-        // ---- phase 3: stress (+ SLS) per sample and point ----
-        for (int t = threadIdx.x; t < nr * Pc; t += blockDim.x) {
-            const int k = t / Pc, pp = t - k * Pc, pg = p0 + pp;
-            float e6[6], s6[6];
-#pragma unroll
-            for (int c = 0; c < 6; c++) e6[c] = X[(int64_t)k * ncolp + c * Pc + pp];
-            elastic(mat, e6, s6, [&](int m) { return md[((int64_t)m * nr + k) * NPE + pg]; });
-            if (att) {
-                const int qq = att == 2 ? cg4_index(pg) : pg;
-                if (qq >= 0) {
-                    float *R = mem + (int64_t)k * 6 * npa + qq;
-                    float *SR = R + sls.nsls * sl;
-                    for (int l = 0; l < sls.nsls; l++)
-#pragma unroll
-                        for (int c = 0; c < 6; c++) s6[c] -= R[l * sl + c * npa];
-                    sls_update(sls, R, SR, sl, (int64_t)npa, e6, am[(int64_t)k * npa + qq],
-                               am[(int64_t)nr * npa + (int64_t)k * npa + qq]);
-                }
-            }
-#pragma unroll
-            for (int c = 0; c < 6; c++) X[(int64_t)k * ncolp + c * Pc + pp] = s6[c];
+        // ---- phase 3: SLS update, then stress per sample and point ----
+        float *dR = reinterpret_cast<float *>(F);  // nr * 6 * Pc floats (<= F size), F is dead here
+        if (att) {
+            sls_phase(X, SX, mem, am, sl, npa, att, sls, nr, Pc, p0, dR);
+            __syncthreads();
         }
+        if (mat == 0)
+            stress_phase<0, 8>(X, SX, md, att, nr, Pc, p0, dR);
+        else if (mat == 1)
+            stress_phase<1, 4>(X, SX, md, att, nr, Pc, p0, dR);
+        else
+            stress_phase<2, 1>(X, SX, md, att, nr, Pc, p0, dR);
         __syncthreads();
         // ---- phase 4: R2C back to orders 0..lim ----
-        phys_r2c(tw, X, F, nr, lim, ncolp);
+        phys_r2c(tw, X, SX, F, SF, nr, lim, ncolg);
         __syncthreads();
         // ---- phase 5: back-rotation + quad6, accumulate into the element force ----
         for (int a = warp; a < n; a += PH_WARPS) {
             float2 sig[6];
 #pragma unroll
             for (int c = 0; c < 6; c++)
-                sig[c] = (mine && a <= lim) ? F[(int64_t)a * ncolp + c * Pc + (p - p0)] : make_float2(0.f, 0.f);
+                sig[c] = (mine && a <= lim) ? F[(int64_t)a * SF + c * Pc + (p - p0)] : make_float2(0.f, 0.f);
             if (mine && tiso) rtz_spz(sig, s1, c1, s2, c2);
+            float2 old[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+            float2 *o = ef + ((int64_t)p * n + a) * 3;
+            if (active && p0 > 0) {  // issued before the divergence so the load overlaps it
+                old[0] = o[0];
+                old[1] = o[1];
+                old[2] = o[2];
+            }
             float2 f[3];
             quad6_lane(L, g, axial, a, sig, q, active && a <= lim, f);
             if (active) {
-                float2 *o = ef + ((int64_t)p * n + a) * 3;
                 if (a > lim) f[0] = f[1] = f[2] = make_float2(0.f, 0.f);
-                if (p0 == 0) {
-                    o[0] = f[0];
-                    o[1] = f[1];
-                    o[2] = f[2];
-                } else {
-                    o[0] = cadd(o[0], f[0]);
-                    o[1] = cadd(o[1], f[1]);
-                    o[2] = cadd(o[2], f[2]);
-                }
+                o[0] = cadd(old[0], f[0]);
+                o[1] = cadd(old[1], f[1]);
+                o[2] = cadd(old[2], f[2]);
             }
         }
         __syncthreads();
     }
 }
 
-__global__ void __launch_bounds__(PH_THREADS)
+__global__ void __launch_bounds__(PH_THREADS, 1)
     k_elem_phys_fluid(ElemTable T, PointTable P, const float2 *__restrict__ fu,
                       const int32_t *__restrict__ elems, int Pmax) {
     extern __shared__ __align__(16) char smem[];
@@ -472,12 +642,12 @@ __global__ void __launch_bounds__(PH_THREADS)
     const bool axial = T.flags[e] & EF_AXIAL;
     const int nr = T.nr[e], nu = nr / 2, n = nu + 1, lim = nu - (nr % 2 == 0);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    float2 *tw, *F, *scr;
-    float *X;
-    int ncolp;
-    phys_layout<3>(nr, Pmax, tw, F, X, scr, ncolp, smem);
+    PhysLayout S(smem, nr, 3, Pmax);
+    float2 *tw = S.tw, *F = S.F;
+    float *X = S.X;
+    const int SF = S.SF, SX = S.SX;
     fill_twiddles(tw, T, nr);
-    float2 *q = scr + warp * QSCR;
+    float2 *q = S.scr + warp * QSCR;
     const bool active = lane < NPE;
     const int p = active ? lane : 0;
     LaneOps L;
@@ -490,6 +660,7 @@ __global__ void __launch_bounds__(PH_THREADS)
     for (int p0 = 0; p0 < NPE; p0 += Pmax) {
         const int Pc = min(Pmax, NPE - p0);
         const int ncol = 3 * Pc;
+        const int ncolg = round_up(ncol, CG);
         const bool mine = active && p >= p0 && p < p0 + Pc;
         for (int a = warp; a < n; a += PH_WARPS) {
             if (active) q[p] = load_fluid_u(P, fu, pt_me, a);
@@ -498,27 +669,27 @@ __global__ void __launch_bounds__(PH_THREADS)
             if (mine && a <= lim) grad1_lane(L, g, axial, a, q, eps);
             if (mine)
 #pragma unroll
-                for (int c = 0; c < 3; c++) F[(int64_t)a * ncolp + c * Pc + (p - p0)] = eps[c];
-            for (int c = ncol + lane; c < ncolp; c += 32) F[(int64_t)a * ncolp + c] = make_float2(0.f, 0.f);
+                for (int c = 0; c < 3; c++) F[(int64_t)a * SF + c * Pc + (p - p0)] = eps[c];
+            for (int c = ncol + lane; c < ncolg; c += 32) F[(int64_t)a * SF + c] = make_float2(0.f, 0.f);
             __syncwarp();
         }
         __syncthreads();
-        phys_c2r(tw, F, X, nr, lim, ncolp);
+        phys_c2r(tw, F, SF, X, SX, nr, lim, ncolg);
         __syncthreads();
         for (int t = threadIdx.x; t < nr * Pc; t += blockDim.x) {
             const int k = t / Pc, pp = t - k * Pc, pg = p0 + pp;
             const float K = md[(int64_t)k * NPE + pg];  // Acoustic3D.cpp:9-16
 #pragma unroll
-            for (int c = 0; c < 3; c++) X[(int64_t)k * ncolp + c * Pc + pp] *= K;
+            for (int c = 0; c < 3; c++) X[(int64_t)k * SX + c * Pc + pp] *= K;
         }
         __syncthreads();
-        phys_r2c(tw, X, F, nr, lim, ncolp);
+        phys_r2c(tw, X, SX, F, SF, nr, lim, ncolg);
         __syncthreads();
         for (int a = warp; a < n; a += PH_WARPS) {
             float2 sig[3];
 #pragma unroll
             for (int c = 0; c < 3; c++)
-                sig[c] = (mine && a <= lim) ? F[(int64_t)a * ncolp + c * Pc + (p - p0)] : make_float2(0.f, 0.f);
+                sig[c] = (mine && a <= lim) ? F[(int64_t)a * SF + c * Pc + (p - p0)] : make_float2(0.f, 0.f);
             float2 f;
             quad1_lane(L, g, axial, a, sig, q, active && a <= lim, f);
             if (active) {

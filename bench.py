@@ -1,0 +1,307 @@
+"""Benchmark: GLL-point x azimuth updates/s of the AxiSEM3D time step on GB300.
+
+Workload (default): the element-level stiffness batching benchmark -- 200,000
+independent solid elements, nPol = 4, spherical geometry in the mantle, Nu_e
+log-uniform in [8, 256] (nr = 2 Nu + 1), transversely isotropic moduli perturbed +-5 %
+per GLL point and azimuthal sample (physical-space path), 3 SLS with Q_mu in [80, 600]
+(CG4), complex FP32 displacement ~ N(0,1) alpha^-1.5.  One step = Newmark update +
+element stiffness + assembly (Newmark::solve's loop body).  Inputs are seeded synthetic
+data resident in HBM; the working set (~70 GB) is far larger than L2, so no flush is
+needed between steps.
+
+value  = sum_e 25 nr_e x steps / device time (CUDA events on the library's stream).
+e2e    = the same through the C-ABI with host buffers: each step copies the
+         displacement in from pinned host memory, steps, and copies it back.
+Reference arm (--impl reference): the CPU oracle port of the same loop, one process
+per host core over a static element partition, on a bounded sample.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "GLL-pt*azimuth updates/s (element-local count), fused stiffness+Newmark step"
+UNIT = "updates/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--elements", type=int, default=200_000)
+    ap.add_argument("--att", default="cg4", choices=["cg4", "full", "none"])
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample", type=int, default=0, help="elements per CPU worker (0 = auto)")
+    return ap.parse_args()
+
+
+def att_kind(name):
+    from axisem3d_gb300.spec import ATT_CG4, ATT_FULL, ATT_NONE
+    return {"cg4": ATT_CG4, "full": ATT_FULL, "none": ATT_NONE}[name]
+
+
+def algorithmic_bytes(spec, att):
+    """Compulsory HBM bytes of one element-stiffness pass (each array read/written once).
+
+    Per element with n = Nu+1 orders and nr samples: displacement in 600 n, element force
+    out 600 n, geometry 500 B, theta tables 400 B, TI moduli 5*25*4*nr, SLS state
+    (nsls+1)*nr*6*npa*4 read + write, attenuation moduli 2*nr*npa*4 (npa = 4 CG4 / 25)."""
+    nr = spec.element_nr().astype(np.int64)
+    n = nr // 2 + 1
+    b = 600 * n + 600 * n + 500 + 400 + 5 * 25 * 4 * nr
+    if att != "none":
+        npa = 4 if att == "cg4" else 25
+        b = b + 2 * (spec.nsls + 1) * nr * 6 * npa * 4 + 2 * nr * npa * 4
+    return int(b.sum())
+
+
+def point_bytes(spec):
+    """Newmark update + assembly per step: stiff, u, v, a read and written, element
+    force read once, 1/M per point (row kernels)."""
+    ns, _ = spec.field_sizes()
+    return int(8 * ns * (4 + 4) + 8 * ns * 2 + 4 * spec.n_points)
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        rows = [r.split(",") for r in getattr(self, "out", "").strip().splitlines() if r.count(",") >= 8]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if "Active" in r[5 + i] and "Not" not in r[5 + i]})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(world, x):
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+    return x
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------------ CPU (oracle) arm
+def _cpu_worker(a):
+    """Build one partition sample and time the oracle's loop body on it."""
+    seed, n_elem, att, steps = a
+    import numpy as _np  # noqa
+    sys.path.insert(0, str(ROOT))
+    from axisem3d_gb300 import workloads as W
+    from oracle.oracle_py import OracleDomain
+    spec = W.element_benchmark(n_elem=n_elem, seed=seed, att=att_kind(att))
+    d = OracleDomain(spec)
+    d.set("displ", "solid", W.benchmark_displacement(spec, seed=seed + 1).astype(np.complex128))
+    d.step(1)  # first touch
+    t0 = time.perf_counter()
+    d.step(steps)
+    dt = time.perf_counter() - t0
+    return W.updates_per_step(spec) * steps, dt
+
+
+def cpu_baseline(att, cores, sample, steps=1, seed=1000):
+    import multiprocessing as mp
+    from oracle.oracle_py import build_oracle
+    build_oracle()
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_cpu_worker, [(seed + 7 * i, sample, att, steps) for i in range(cores)])
+    upd = sum(r[0] for r in res)
+    wall = max(r[1] for r in res)
+    return upd / wall, dict(cores=cores, sample=f"{cores} partitions x {sample} elements x {steps} step(s), "
+                            f"same Nu/material distribution, seeds {seed}..", wall_s=wall)
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    sample = args.cpu_sample or 24
+    vals = []
+    for _ in range(args.warmup):
+        pass  # each oracle partition does its own first-touch step
+    for _ in range(max(1, min(args.steps, 3))):
+        v, info = cpu_baseline(args.att, cores, sample)
+        vals.append(v)
+    v = float(np.median(vals))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": f"element stiffness batching, {args.elements} TI elements, Nu 8-256 "
+                                   f"log-uniform, 3 SLS {args.att}, 3-D (physical-space) material"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": info["cores"], "kind": "port",
+                             "sample": info["sample"]},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "the reference (C++/Eigen/FFTW/MPI) does not build here; the CPU oracle port of the "
+                    "same loop is timed, one process per core"}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ GB300 arm
+def run_gb300(args, world, rank, local):
+    from axisem3d_gb300 import build
+    from axisem3d_gb300 import workloads as W
+    from axisem3d_gb300.capi import Ax3dDomain
+    build.build()
+    t_build = time.perf_counter()
+    spec = W.element_benchmark(n_elem=args.elements, seed=args.seed + rank, att=att_kind(args.att))
+    u0 = W.benchmark_displacement(spec, seed=args.seed + 100 + rank)
+    dom = Ax3dDomain(spec, device=local)
+    dom.set("displ", "solid", u0)
+    t_build = time.perf_counter() - t_build
+    upd = W.updates_per_step(spec)
+
+    dom.enable_timers(True)
+    dom.step(args.warmup)
+    dom.read_timers()
+    barrier(world)
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        dom.step(args.steps)
+        wall = time.perf_counter() - t0
+    tm = dom.read_timers()
+    dev_s = tm["step"][0] / 1e3
+    dev_s_max = allmax(world, dev_s)
+    barrier(world)
+
+    # e2e through the C-ABI with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        import torch
+        n = dom.nsolid
+        pin_in = torch.empty(n, dtype=torch.complex64, pin_memory=True).numpy()
+        pin_out = torch.empty(n, dtype=torch.complex64, pin_memory=True).numpy()
+        pin_in[:] = dom.get("displ")
+        ke = max(3, min(args.steps, 10))
+        t0 = time.perf_counter()
+        for _ in range(ke):
+            dom.set("displ", "solid", pin_in)
+            dom.step(1)
+            dom.get("displ", "solid", out=pin_out)
+        e2e_s = allmax(world, (time.perf_counter() - t0) / ke)
+        e2e = {"value": upd * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(8 * n),
+               "d2h_bytes_per_step": int(8 * n), "ms_per_step": e2e_s * 1e3}
+
+    if rank != 0:
+        return
+    elem_ms = tm["elements"][0] / args.steps
+    abytes = algorithmic_bytes(spec, args.att)
+    peak, src = peaks()
+    achieved = abytes / (elem_ms / 1e3) / 1e9
+    launches = sum(v[1] for k, v in tm.items() if k != "step")
+    cpu = None
+    if not args.no_cpu_baseline:
+        try:
+            v, info = cpu_baseline(args.att, os.cpu_count() or 1, args.cpu_sample or 24)
+            cpu = {"value": v, "unit": UNIT, "cores": info["cores"], "kind": "port", "sample": info["sample"]}
+        except Exception as e:  # the CPU leg must not hide the GPU number
+            cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {e}"}
+    line = {
+        "metric": METRIC, "value": upd * args.steps * world / dev_s_max, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_s_max * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded)",
+        "config": {"workload": f"element stiffness batching, {args.elements} TI elements, Nu 8-256 "
+                               f"log-uniform (nr = 2Nu+1), 3 SLS {args.att}, 3-D (physical-space) material, "
+                               f"fused stiffness+Newmark step", "elements": args.elements,
+                   "updates_per_step": upd, "parallelism": f"replicas x{world}",
+                   "l2": "working set > L2 (no flush needed)"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None, "peak_source": src,
+                     "kernel": "element stiffness (k_elem_phys_solid, all buckets)",
+                     "algorithmic_bytes_per_step": abytes, "kernel_ms_per_step": elem_ms},
+        "phases_ms_per_step": {k: v[0] / args.steps for k, v in tm.items()},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+        "host_wall_ms_per_step": wall * 1e3 / args.steps,
+        "setup_s": t_build,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_gb300(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

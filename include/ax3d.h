@@ -171,6 +171,25 @@ int ax3d_reset(ax3d_domain *d);
 /* Current internal step counter (next step to run, 1-based like Newmark::solve). */
 int32_t ax3d_current_step(const ax3d_domain *d);
 
+/* Time-loop phase timers: the reference's _MEASURE_TIMELOOP timers (Domain.h:111-118,
+   reported by Domain::reportCost, Domain.cpp:349-382).  When enabled, ax3d_step brackets
+   every phase with CUDA events on the domain's stream.  ax3d_read_timers fills
+   ms[AX3D_NTIMERS] (accumulated device milliseconds) and launches[AX3D_NTIMERS]
+   (kernel launches) indexed by AX3D_TIMER_*, and resets the accumulators. */
+enum {
+    AX3D_TIMER_STEP = 0,      /* whole ax3d_step calls             */
+    AX3D_TIMER_ELEMENTS = 1,  /* Domain::computeStiff element loop */
+    AX3D_TIMER_POINTS = 2,    /* Domain::updateNewmark             */
+    AX3D_TIMER_ASSEMBLE = 3,  /* gatherStiffFromElement            */
+    AX3D_TIMER_COUPLE = 4,    /* Domain::coupleSolidFluid          */
+    AX3D_TIMER_SOURCE = 5,    /* Domain::applySource               */
+    AX3D_TIMER_RECORD = 6,    /* Domain::record                    */
+    AX3D_TIMER_OTHER = 7,     /* stability checks                  */
+    AX3D_NTIMERS = 8
+};
+int ax3d_enable_timers(ax3d_domain *d, int32_t enable);
+int ax3d_read_timers(ax3d_domain *d, double *ms, int64_t *launches);
+
 int ax3d_destroy(ax3d_domain *d);
 
 /* Text of the last error on this thread (always NUL terminated); returns its length. */
