@@ -654,6 +654,10 @@ struct ax3d_domain {
     }
 };
 
+namespace ax3d {
+void set_last_error(const std::string &msg) { g_err = msg; }
+}  // namespace ax3d
+
 // ================================================================ C ABI
 namespace {
 template <typename F>

@@ -23,11 +23,11 @@ struct LaneOps {
     float gxr[5];  // G_xi[i][k]  (row i)     -> (G_xi X)(i,j)
     float ger[5];  // G_eta[j][k] (row j)     -> (Y G_eta^T)(i,j)
     int i, j;
-    __device__ void init(int p, bool axial) {
+    __device__ void init(int p, bool axial) { init_from(p, c_G[axial ? 1 : 0], c_G[0]); }
+    // Gx: G of the xi direction (GLJ on axial elements), Ge: G of eta (GLL), both [25].
+    __device__ void init_from(int p, const float *Gx, const float *Ge) {
         i = p / 5;
         j = p - 5 * (p / 5);
-        const float *Gx = c_G[axial ? 1 : 0];
-        const float *Ge = c_G[0];
 #pragma unroll
         for (int k = 0; k < 5; k++) {
             gxc[k] = Gx[k * 5 + i];

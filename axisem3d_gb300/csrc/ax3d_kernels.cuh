@@ -1,6 +1,8 @@
 // ax3d_kernels.cuh -- launch interface of the GB300 kernels (host side).
 #pragma once
 
+#include <string>
+
 #include "ax3d_common.cuh"
 
 namespace ax3d {
@@ -12,6 +14,9 @@ struct PhysBucket {
     int npts_chunk = 25;       // GLL points per pass (shared-memory budget)
     size_t smem = 0;
 };
+
+// Sets the text ax3d_last_error returns on this thread.
+void set_last_error(const std::string &msg);
 
 void set_g_matrices(const float *g_gll, const float *g_glj, cudaStream_t s);
 

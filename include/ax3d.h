@@ -192,6 +192,38 @@ int ax3d_read_timers(ax3d_domain *d, double *ms, int64_t *launches);
 
 int ax3d_destroy(ax3d_domain *d);
 
+/* Size of the static device scratch of ax3d_compute_stiff_iso1d_noalloc, in MiB. */
+#define AX3D_NOALLOC_SCRATCH_MIB 32
+
+/* No counterpart in the reference.  Element stiffness plus assembly, stiff -= K u, for
+   callers that cannot allocate device memory (a code that hands out every device byte
+   from its own pre-sized pool, or one that must not allocate once a run has started):
+   nothing is allocated, every pointer below is the caller's device buffer, and the element
+   forces between the element pass and the assembly pass live in one static __device__
+   array of AX3D_NOALLOC_SCRATCH_MIB MiB that every GPU loading the library holds until
+   the process exits.
+   Scope: Fourier-space isotropic solid elements without attenuation, all points with the
+   same nu (nr = 2 nu + 1); layouts as the domain path:
+     d_points    [nelem][25] point indices      d_axial     [nelem] 1 for axial elements
+     d_geometry  [nelem][5][25] (ax3d_add_elements)  d_lambda_mu [nelem][2][25]
+     d_gather_ptr[npoints + 1], d_gather_ref: CSR of (element * 25 + local point) per point,
+                 ascending element order (the order the reference's element loop sums in)
+     d_displ, d_stiff [npoints][nu + 1][3] complex
+     g_gll, g_glj host [25] G matrices (as ax3d_config).
+   Runs asynchronously on `stream` (a cudaStream_t, NULL = default stream).  Returns
+   AX3D_ERR_ARG without launching when nelem * 25 * (nu + 1) * 24 bytes exceeds the
+   scratch.  The first call on a device resolves the scratch's device address
+   (cudaGetSymbolAddress) with that device current; make it before any stream capture.
+   All calls share the one scratch: calls that overlap on the GPU (two streams, two
+   threads) race and must be serialised by the caller.  The scratch keeps the last
+   call's contents; every entry a call reads is written by the same call first. */
+int ax3d_compute_stiff_iso1d_noalloc(int32_t nelem, int32_t nu, const int32_t *d_points,
+                                     const uint8_t *d_axial, const float *d_geometry,
+                                     const float *d_lambda_mu, int32_t npoints,
+                                     const int32_t *d_gather_ptr, const int32_t *d_gather_ref,
+                                     const float *d_displ, float *d_stiff, const double *g_gll,
+                                     const double *g_glj, void *stream);
+
 /* Text of the last error on this thread (always NUL terminated); returns its length. */
 size_t ax3d_last_error(char *buf, size_t len);
 
