@@ -1,0 +1,528 @@
+"""Host driver mirroring axisem_main (SOLVER/src/axisem.cpp:12-207) for the GB300 path.
+
+Reads the reference's inputs -- the four inparam.* parfiles, an Exodus meridian mesh
+(NetCDF classic), CMTSOLUTION and STATIONS -- builds the packed domain (the counterpart
+of Mesh::release), runs Newmark::solve's loop on the GPU through the C-ABI, and writes
+the station seismograms as NetCDF with the reference's variable names
+(SOLVER/src/core/output/pointwise/PointwiseIONetCDF.cpp:63-195).
+Pre-computation is FP64 (geometry, materials, masses, normals, source, receivers).
+"""
+from __future__ import annotations
+
+import math
+import os
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+from . import attenuation as ATT
+from . import geometry as GEO
+from . import netcdf as NC
+from . import spectral as S
+from .spec import (ATT_CG4, ATT_FULL, ATT_NONE, MAT_ACOUSTIC, MAT_ISO, POINT_FLUID, POINT_SOLID,
+                   POINT_SOLID_FLUID, DomainSpec)
+
+# the parameter registry (Parameters::registerAll, Parameters.cpp:23-100)
+REGISTRY = """MODEL_1D_EXODUS_MESH_FILE MODEL_3D_VOLUMETRIC_NUM MODEL_3D_VOLUMETRIC_LIST MODEL_3D_GEOMETRIC_NUM
+MODEL_3D_GEOMETRIC_LIST MODEL_3D_ELLIPTICITY_MODE MODEL_3D_ELLIPTICITY_INVF MODEL_3D_OCEAN_LOAD MODEL_2D_MODE
+MODEL_2D_LATITUDE MODEL_2D_LONGITUDE MODEL_2D_AZIMUTH MODEL_PLOT_SLICES_NUM MODEL_PLOT_SLICES_LIST ATTENUATION
+NU_TYPE NU_CONST NU_EMP_REF NU_EMP_MIN NU_EMP_SCALE_AXIS NU_EMP_POW_AXIS NU_EMP_SCALE_THETA NU_EMP_POW_THETA
+NU_EMP_FACTOR_PI NU_EMP_THETA_START NU_EMP_SCALE_DEPTH NU_EMP_FACTOR_SURF NU_EMP_DEPTH_START NU_EMP_DEPTH_END
+NU_WISDOM_LEARN NU_WISDOM_LEARN_EPSILON NU_WISDOM_LEARN_INTERVAL NU_WISDOM_LEARN_OUTPUT NU_WISDOM_REUSE_INPUT
+NU_WISDOM_REUSE_FACTOR NU_USER_PARAMETER_LIST TIME_DELTA_T TIME_DELTA_T_FACTOR TIME_RECORD_LENGTH SOURCE_TYPE
+SOURCE_FILE SOURCE_TIME_FUNCTION SOURCE_STF_HALF_DURATION OUT_STATIONS_FILE OUT_STATIONS_DUPLICATED
+OUT_STATIONS_SYSTEM OUT_STATIONS_FORMAT OUT_STATIONS_COMPONENTS OUT_STATIONS_RECORD_INTERVAL
+OUT_STATIONS_DUMP_INTERVAL OUT_STATIONS_WHOLE_SURFACE OUT_STATIONS_DEPTH_REF ATTENUATION_CG4
+ATTENUATION_SPECFEM_LEGACY ATTENUATION_QKAPPA DD_PROC_INTERVAL DD_NCUTS_PER_PROC OPTION_VERBOSE_LEVEL
+OPTION_STABILITY_INTERVAL OPTION_LOOP_INFO_INTERVAL DEVELOP_MAX_TIME_STEPS DEVELOP_NON_SOURCE_MODE
+DEVELOP_DIAGNOSE_PRELOOP DEVELOP_MEASURED_COSTS DEVELOP_RANDOMIZE_DISP0 FFTW_LUCKY_NUMBER FFTW_DISABLE_WISDOM""".split()
+
+PARFILES = ("inparam.model", "inparam.nu", "inparam.time_src_recv", "inparam.advanced")
+
+
+class Parameters:
+    """Parameters::readParFile / parseLine / getValue (Parameters.cpp:15-137, Parameters.h:25-49):
+    whitespace-separated KEY value... lines, '#' comments, registered keys only."""
+
+    def __init__(self, input_dir):
+        self.values = {k: [] for k in REGISTRY}
+        for f in PARFILES:
+            p = Path(input_dir) / f
+            if not p.exists():
+                raise FileNotFoundError(f"Parameters::readParFile || Error opening parameter file: || {p}")
+            for line in p.read_text().splitlines():
+                strs = line.strip().split()
+                if not strs or strs[0].startswith("#"):
+                    continue
+                if strs[0] in self.values:
+                    self.values[strs[0]].extend(strs[1:])
+
+    def get(self, key, typ=str, index=0):
+        v = self.values.get(key)
+        if not v or index >= len(v):
+            raise KeyError(f"Parameters::getValue || Parameter {key} not found or incomplete")
+        s = v[index]
+        if typ is bool:
+            if s.lower() in ("true", "yes", "on", "1"):
+                return True
+            if s.lower() in ("false", "no", "off", "0"):
+                return False
+            raise ValueError(f"Parameters::getValue || bad bool for {key}: {s}")
+        return typ(s)
+
+
+@dataclass
+class Exodus:
+    """The quantities ExodusModel::buildInparam exposes (ExodusModel.cpp:53-247, 519-573)."""
+    nodes: np.ndarray       # [N, 2] (s, z)
+    conn: np.ndarray        # [E, 4] 0-based
+    etype: np.ndarray       # [E]
+    fluid: np.ndarray       # [E] bool
+    dt: np.ndarray          # [E]
+    nodal: dict             # name -> [E, 4]
+    side: dict              # side-set name -> [E] side (-1 none)
+    glob: dict              # global variables
+
+    @staticmethod
+    def read(path):
+        d = NC.read(path)
+        names = d.strings("name_glo_var")
+        glob = dict(zip(names, np.asarray(d["vals_glo_var"], float).ravel()))
+        conn = np.asarray(d["connect1"], np.int64) - 1
+        E = len(conn)
+        ss = d.strings("ss_names")
+        side = {}
+        for i, nm in enumerate(ss):
+            v = np.full(E, -1)
+            v[np.asarray(d[f"elem_ss{i + 1}"]) - 1] = np.asarray(d[f"side_ss{i + 1}"]) - 1
+            side[nm] = v
+        enames = d.strings("name_elem_var")
+        ev = {nm: np.asarray(d[f"vals_elem_var{i + 1}eb1"], float).ravel() for i, nm in enumerate(enames)}
+        nodal = {}
+        for base in ("VP", "VS", "RHO", "QMU", "QKAPPA"):
+            if f"{base}_0" in ev:
+                nodal[base] = np.stack([ev[f"{base}_{k}"] for k in range(4)], 1)
+        info = d.strings("info_records")
+        if not any("spherical" in s for s in info):
+            raise ValueError("Exodus || only crdsys = spherical meshes are supported")
+        return Exodus(np.stack([d["coordx"], d["coordy"]], 1).astype(float), conn,
+                      ev["element_type"].astype(int), ev["fluid"] > 0.5, ev.get("dt", np.zeros(E)), nodal, side, glob)
+
+
+def _lagrange(x, nodes):
+    """XMath::interpLagrange: basis values of the Lagrange polynomials on nodes at x."""
+    out = np.ones(len(nodes))
+    for i in range(len(nodes)):
+        for j in range(len(nodes)):
+            if i != j:
+                out[i] *= (x - nodes[j]) / (nodes[i] - nodes[j])
+    return out
+
+
+def _rot(theta, phi):
+    """Geodesy::rotationMatrix (Geodesy.cpp:56-68)."""
+    ct, st, cp, sp = math.cos(theta), math.sin(theta), math.cos(phi), math.sin(phi)
+    return np.array([[ct * cp, -sp, st * cp], [ct * sp, cp, st * sp], [-st, 0.0, ct]])
+
+
+def glob_to_src(theta_g, phi_g, src_theta, src_phi):
+    """Geodesy::rotateGlob2Src on the unit sphere (no ellipticity)."""
+    x = np.array([math.sin(theta_g) * math.cos(phi_g), math.sin(theta_g) * math.sin(phi_g), math.cos(theta_g)])
+    xs = _rot(src_theta, src_phi).T @ x
+    t = math.acos(max(-1.0, min(1.0, xs[2])))
+    p = math.atan2(xs[1], xs[0])
+    return t, (p + 2 * math.pi) % (2 * math.pi)
+
+
+class Simulation:
+    def __init__(self, input_dir, output_dir=None):
+        self.input_dir = Path(input_dir)
+        self.output_dir = Path(output_dir or self.input_dir.parent / "output")
+        self.par = Parameters(self.input_dir)
+
+    # ------------------------------------------------------------------ build
+    def build(self, kahan=False) -> DomainSpec:
+        par = self.par
+        ex = Exodus.read(self.input_dir / par.get("MODEL_1D_EXODUS_MESH_FILE"))
+        self.ex = ex
+        self.R = float(ex.glob.get("radius", 6371e3))
+        E = len(ex.conn)
+        axial_e = ex.side.get("t0", np.full(E, -1)) >= 0
+        if (ex.side["t0"][axial_e] != 3).any():
+            raise ValueError("Quad::Quad || Axial side must be 3.")
+        r = np.hypot(ex.nodes[ex.conn][..., 0], ex.nodes[ex.conn][..., 1])
+        co = np.full(E, -1)
+        sph = ex.etype == 0
+        co[sph] = np.where(r[sph, 2] > r[sph, 0] + 1e-6, 2, 0)
+        semi = ex.etype == 2
+        co[semi] = np.where(np.abs(r[semi, 2] - r[semi, 3]) < 1e-3 * self.R, 2, 0)
+        nodes = np.transpose(ex.nodes[ex.conn], (0, 2, 1))
+        geo, ifact, crds, theta, jac = GEO.batch_geometry(nodes, ex.etype, co, axial_e)
+        self.nodes4, self.co, self.axial_e = nodes, co, axial_e
+        # unique GLL points by coordinates (Connectivity::formElemToGLL)
+        tol = 1e-3
+        key = np.round(crds.reshape(-1, 2) / tol).astype(np.int64)
+        _, pid, inv = np.unique(key, axis=0, return_index=True, return_inverse=True)
+        e_pts = inv.reshape(E, 25).astype(np.int32)
+        P = int(e_pts.max()) + 1
+        pcrd = np.zeros((P, 2))
+        pcrd[e_pts.ravel()] = crds.reshape(-1, 2)
+        pcrd[np.abs(pcrd[:, 0]) < 1e-6, 0] = 0.0
+        # materials at GLL points: bilinear in (xi, eta) of the element's nodal values
+        xg = S.gll()[0]
+        xj = S.glj()[0]
+        XI = np.where(axial_e[:, None, None], xj[None, :, None], xg[None, :, None]) * np.ones((1, 1, 5))
+        ETA = np.broadcast_to(xg[None, None, :], (E, 5, 5))
+        shp = np.stack([(1 - XI) * (1 - ETA), (1 + XI) * (1 - ETA), (1 + XI) * (1 + ETA), (1 - XI) * (1 + ETA)], -1) / 4
+        mat = {k: np.einsum("epqk,ek->epq", shp, v).reshape(E, 25) for k, v in ex.nodal.items()}
+        vp, vs, rho = mat["VP"], mat["VS"], mat["RHO"]
+        fl = ex.fluid
+        # Nr field: NU_TYPE constant (ConstNrField) with Quad::formNrField's axis limit
+        nutype = par.get("NU_TYPE")
+        if nutype.lower() != "constant":
+            raise NotImplementedError("NU_TYPE: only 'constant' is built")
+        nr0 = 2 * par.get("NU_CONST", int) + 1
+        size_e = np.sqrt(np.abs(ifact.sum(1) / np.maximum(crds[..., 0].mean(1), 1.0)))  # ~ element edge
+        spacing = np.full(P, np.inf)
+        np.minimum.at(spacing, e_pts.ravel(), np.repeat(size_e / 4.0, 25))
+        upper = np.maximum(3, (2 * np.pi * pcrd[:, 0] / spacing).astype(int))
+        p_nr = np.minimum(nr0, upper)
+        p_axial = np.abs(pcrd[:, 0]) < 1e-6
+        near_axis = np.zeros(P, bool)
+        near_axis[e_pts[axial_e].ravel()] = True
+        p_nr = np.where((p_nr % 2 == 0) & near_axis, p_nr + 1, p_nr)
+        # point phases, masses (Material::computeElementalMass), coupling normals
+        has_s = np.zeros(P, bool)
+        has_f = np.zeros(P, bool)
+        has_s[e_pts[~fl].ravel()] = True
+        has_f[e_pts[fl].ravel()] = True
+        kind = np.where(has_s & has_f, POINT_SOLID_FLUID, np.where(has_f, POINT_FLUID, POINT_SOLID)).astype(np.int8)
+        ms = np.zeros(P)
+        mf = np.zeros(P)
+        np.add.at(ms, e_pts[~fl].ravel(), (rho[~fl] * ifact[~fl]).ravel())
+        np.add.at(mf, e_pts[fl].ravel(), (ifact[fl] / (rho[fl] * vp[fl] ** 2)).ravel())
+        sfn = np.zeros((P, 3))
+        sfside = ex.side.get("solid_fluid_boundary", np.full(E, -1))
+        wg, wjw = S.gll()[1], S.glj()[1]
+        for e in np.nonzero(sfside >= 0)[0]:
+            side = sfside[e]
+            n0, n1 = nodes[e][:, side], nodes[e][:, (side + 1) % 4]
+            r0, t0 = np.hypot(*n0), math.acos(n0[1] / np.hypot(*n0))
+            r1, t1 = np.hypot(*n1), math.acos(n1[1] / np.hypot(*n1))
+            rsf = 0.5 * (r0 + r1)
+            h_r_dt, h_r2_dt = 0.5 * rsf * abs(t1 - t0), 0.5 * rsf * rsf * abs(t1 - t0)
+            for ip in range(5):
+                for jp in range(5):
+                    on = (side == 0 and jp == 0) or (side == 1 and ip == 4) or (side == 2 and jp == 4) or \
+                         (side == 3 and ip == 0)
+                    if not on:
+                        continue
+                    k = ip * 5 + jp
+                    sz = crds[e, k]
+                    rr = np.hypot(*sz)
+                    sint, cost = sz[0] / rr, sz[1] / rr
+                    nvec = np.array([sint, 0.0, cost])  # Quad::computeNormal (Quad.cpp:661-715)
+                    wsf = (wjw if axial_e[e] else wg)[ip] if side in (0, 2) else wg[jp]
+                    if axial_e[e]:
+                        if ip == 0:
+                            nvec *= wsf * jac[0][e, ip, jp] * h_r_dt
+                        else:
+                            xi = xj[ip]
+                            nvec *= wsf / (1 + xi) * sint * h_r2_dt
+                    else:
+                        nvec *= wsf * sint * h_r2_dt
+                    if side != co[e]:
+                        nvec = -nvec
+                    if not fl[e]:
+                        nvec = -nvec
+                    sfn[e_pts[e, k]] += 0.5 * nvec  # GLLPoint::addSFNormal
+        # moduli (Material::createElastic / createAcoustic, isotropic)
+        att_on = par.get("ATTENUATION", bool)
+        cg4 = par.get("ATTENUATION_CG4", bool)
+        dokappa = par.get("ATTENUATION_QKAPPA", bool)
+        # time step (Mesh::getDeltaT x TIME_DELTA_T_FACTOR, or TIME_DELTA_T)
+        dt_user = par.get("TIME_DELTA_T", float)
+        dt = dt_user if dt_user > 0 else float(ex.dt.min()) * par.get("TIME_DELTA_T_FACTOR", float)
+        self.dt = dt
+        attk = ATT_NONE
+        alpha = beta = gamma = np.zeros(0)
+        nsls = 0
+        if att_on and "nr_lin_solids" in ex.glob:
+            nsls = int(ex.glob["nr_lin_solids"])
+            w = np.array([ex.glob[f"w_{i}"] for i in range(nsls)])
+            y = np.array([ex.glob[f"y_{i}"] for i in range(nsls)])
+            fmin, fmax, fref = ex.glob["f_min"], ex.glob["f_max"], ex.glob["f_ref"]
+            alpha, beta, gamma, _, _ = ATT.att_factors(w, y, fmin, fmax, fref, dt, np.ones(1), np.ones(1), dokappa)
+            attk = ATT_CG4 if cg4 else ATT_FULL
+        e_mod, e_attm, e_mat, e_att = [], [], [], []
+        for e in range(E):
+            f = ifact[e]
+            if fl[e]:
+                e_mod.append(f / rho[e])
+                e_attm.append(np.zeros(0))
+                e_mat.append(MAT_ACOUSTIC)
+                e_att.append(ATT_NONE)
+                continue
+            lam = rho[e] * (vp[e] ** 2 - 2 * vs[e] ** 2) * f
+            mu = rho[e] * vs[e] ** 2 * f
+            attm = np.zeros(0)
+            if attk != ATT_NONE:
+                A = C = lam + 2 * mu
+                F, L, N = lam, mu, mu
+                kappa, mu_v = ATT.voigt_ti(A, C, F, L, N)
+                qk = mat["QKAPPA"][e][None, :]
+                qm = mat["QMU"][e][None, :]
+                fac = ATT.att_factors(w, y, fmin, fmax, fref, dt, qk, qm, dokappa)
+                kap2, mu2, dk, dm = ATT.apply_attenuation(kappa[None, :], mu_v[None, :], qk, qm, f, cg4,
+                                                          (fac[3], fac[4]))
+                lam = (kap2 - 2.0 / 3.0 * mu2)[0]
+                mu = mu2[0]
+                attm = np.concatenate([dk.ravel(), dm.ravel()])
+            e_mod.append(np.stack([lam, mu]).ravel())
+            e_attm.append(attm)
+            e_mat.append(MAT_ISO)
+            e_att.append(attk)
+        mofs = np.concatenate([[0], np.cumsum([len(m) for m in e_mod])[:-1]]).astype(np.int64)
+        aofs = np.concatenate([[0], np.cumsum([len(m) for m in e_attm])[:-1]]).astype(np.int64)
+        # fluid points on the free surface (FluidPoint mFluidSurf)
+        fsurf = np.zeros(P, bool)
+        surf = ex.side.get("r1", np.full(E, -1))
+        for e in np.nonzero((surf >= 0) & fl)[0]:
+            s_ = surf[e]
+            for ip in range(5):
+                for jp in range(5):
+                    if (s_ == 0 and jp == 0) or (s_ == 1 and ip == 4) or (s_ == 2 and jp == 4) or (s_ == 3 and ip == 0):
+                        fsurf[e_pts[e, ip * 5 + jp]] = True
+        sflen = np.where(kind == POINT_SOLID_FLUID, 1, 0).astype(np.int32)
+        sfrows = sfn[kind == POINT_SOLID_FLUID]
+        mf_sf = mf[kind == POINT_SOLID_FLUID]
+        spec = DomainSpec(
+            dt=dt, p_nr=p_nr.astype(np.int32), p_kind=kind, p_axial=p_axial.astype(np.uint8),
+            p_fsurf=fsurf.astype(np.uint8),
+            p_mslen=has_s.astype(np.int32), p_ms=(1.0 / ms[has_s]).astype(np.float32),
+            p_mflen=has_f.astype(np.int32), p_mf=(1.0 / mf[has_f]).astype(np.float32),
+            p_sflen=sflen, p_sfn=sfrows.astype(np.float32), p_sfni=(sfrows / mf_sf[:, None]).astype(np.float32),
+            e_pts=e_pts, e_mat=np.array(e_mat, np.int8), e_axial=axial_e.astype(np.uint8),
+            e_in3d=np.zeros(E, np.uint8), e_geo=geo.astype(np.float32),
+            e_trig=GEO.trig_tables(theta).transpose(1, 0, 2).astype(np.float32),
+            e_mofs=mofs, e_mod=np.concatenate(e_mod).astype(np.float32), e_att=np.array(e_att, np.int8),
+            e_aofs=aofs, e_attm=(np.concatenate(e_attm) if e_attm else np.zeros(0)).astype(np.float32),
+            nsls=nsls, att_alpha=alpha, att_beta=beta, att_gamma=gamma, att_do_kappa=dokappa,
+            kahan=kahan, stability_interval=par.get("OPTION_STABILITY_INTERVAL", int))
+        self.e_pts, self.crds, self.jac, self.fluid = e_pts, crds, jac, fl
+        self._source(spec)
+        self._stf(spec)
+        self._receivers(spec)
+        self.spec = spec
+        return spec
+
+    # ------------------------------------------------------------------ source
+    def _source(self, spec):
+        """CMTSOLUTION (Source.cpp:121-234) -> Earthquake::computeSourceFourier (Earthquake.cpp:20-88)."""
+        par = self.par
+        if par.get("SOURCE_TYPE").lower() != "earthquake":
+            raise NotImplementedError("SOURCE_TYPE: only earthquake is built")
+        vals = {}
+        for line in (self.input_dir / par.get("SOURCE_FILE")).read_text().splitlines()[1:]:
+            if ":" in line:
+                k, v = line.split(":", 1)
+                vals[k.strip()] = v.strip()
+        self.src_lat, self.src_lon = float(vals["latitude"]), float(vals["longitude"])
+        self.src_dep = float(vals["depth"]) * 1e3
+        M = {k: float(vals[k]) * 1e-7 for k in ("Mrr", "Mtt", "Mpp", "Mrt", "Mrp", "Mtp")}  # dyn*cm -> N*m
+        self.half_duration = float(vals.get("half duration", 0.0))
+        zsrc = self.R - self.src_dep
+        # locate: axial solid element whose axis side spans z (Source::locate, Source.cpp:61-94)
+        ex = self.ex
+        host, eta = None, None
+        for e in np.nonzero(self.axial_e & ~self.fluid)[0]:
+            z = self.crds[e].reshape(5, 5, 2)[0, :, 1]  # axis column, jpol = 0..4
+            zmin, zmax = z.min(), z.max()
+            if zmin - 1e-3 <= zsrc <= zmax + 1e-3 and z[0] > -1e-6 and z[4] > -1e-6:
+                # eta from the linear radius on the axis (exact for spherical and linear mappings)
+                eta = -1.0 + 2.0 * (zsrc - z[0]) / (z[4] - z[0])
+                host = e
+                break
+        if host is None:
+            raise RuntimeError("Source::release || Error locating source.")
+        fz = _lagrange(eta, S.gll()[0])
+        Ggll, Gglj = S.gll()[2], S.glj()[2]
+        J00, J01, J10, J11, det = (a[host] for a in self.jac)
+        Mxx, Myy, Mzz, Mxy, Mxz, Myz = M["Mtt"], M["Mpp"], M["Mrr"], M["Mtp"], M["Mrt"], M["Mrp"]
+        f = np.zeros((25, 3, 3), complex)
+        for ip in range(5):
+            for jp in range(5):
+                for js in range(5):
+                    fact = fz[js]
+                    a00, a01, a10, a11 = (J00[0, js] / det[0, js], J01[0, js] / det[0, js],
+                                          J10[0, js] / det[0, js], J11[0, js] / det[0, js])
+                    GU = Gglj[ip, 0] * (1.0 if js == jp else 0.0)  # (G^T w)(0, js)
+                    UG = (Ggll[jp, js] if ip == 0 else 0.0)          # (w G)(0, js)
+                    dwds = a11 * GU - a10 * UG
+                    dwdz = a00 * UG - a01 * GU
+                    k = ip * 5 + jp
+                    f[k, 0, 0] += fact * dwds * (Mxx + Myy) / (2 * np.pi)
+                    f[k, 0, 2] += fact * dwdz * Mzz / (2 * np.pi)
+                    f[k, 1, 0] += fact * dwdz * (Mxz - 1j * Myz) / (4 * np.pi)
+                    f[k, 1, 1] += fact * dwdz * (Mxz - 1j * Myz) / (4 * np.pi) * 1j
+                    f[k, 1, 2] += fact * dwds * (Mxz - 1j * Myz) / (2 * np.pi)
+                    f[k, 2, 0] += fact * dwds * ((Mxx - Myy) / 2 - 1j * Mxy) / (2 * np.pi)
+                    f[k, 2, 1] += fact * dwds * ((Mxx - Myy) / 2 - 1j * Mxy) / (2 * np.pi) * 1j
+        spec.sources = [(int(host), f.astype(np.complex64))]
+        self.src_elem = int(host)
+
+    # ------------------------------------------------------------------ STF
+    def _stf(self, spec):
+        """STF::buildInparam (STF.cpp:21-62) with Erf/Gauss/Ricker (ErfSTF.cpp, GaussSTF.cpp:10-21)."""
+        par = self.par
+        dt = self.dt
+        hdur = par.get("SOURCE_STF_HALF_DURATION", float)
+        if hdur < 5 * dt:
+            hdur = 5 * dt
+        decay = 1.628
+        duration = par.get("TIME_RECORD_LENGTH", float)
+        nb = math.ceil(2.5 * hdur / dt)
+        na = math.ceil(duration / dt)
+        shift = nb * dt
+        t = -shift + np.arange(nb + na + 1) * dt
+        kind = par.get("SOURCE_TIME_FUNCTION").lower()
+        if kind == "erf":
+            from scipy.special import erf
+            stf = erf(decay / hdur * t) * 0.5 + 0.5
+        elif kind == "gauss":
+            stf = np.exp(-(decay / hdur * t) ** 2) * decay / (hdur * math.sqrt(math.pi))
+        elif kind == "ricker":
+            a = decay / hdur
+            stf = 2 * a * a * np.exp(-(a * t) ** 2) * (2 * t * t * a * a - 1)
+        else:
+            raise ValueError(f"STF::buildInparam || Unknown stf type: {kind}")
+        cap = par.get("DEVELOP_MAX_TIME_STEPS", int)
+        if cap > 0:
+            stf = stf[:cap]
+        spec.stf = stf.astype(np.float32)
+        self.shift = shift
+        self.nsteps = len(stf)
+
+    # ------------------------------------------------------------------ receivers
+    def _receivers(self, spec):
+        """STATIONS -> Receiver (Receiver.cpp:23-117): source-centred (theta, phi), element and
+        Lagrange weights (GLJ along xi on axial elements)."""
+        par = self.par
+        system = par.get("OUT_STATIONS_SYSTEM").lower()
+        self.components = par.get("OUT_STATIONS_COMPONENTS").upper()
+        lines = [l.split() for l in (self.input_dir / par.get("OUT_STATIONS_FILE")).read_text().splitlines() if l.strip()]
+        src_t = math.pi / 2 - math.radians(self.src_lat)
+        src_p = math.radians(self.src_lon % 360)
+        rec = []
+        for name, net, la, lo, _elev, bur in lines:
+            la, lo, bur = float(la), float(lo), float(bur)
+            if system == "geographic":
+                th, ph = glob_to_src(math.pi / 2 - math.radians(la), math.radians(lo % 360), src_t, src_p)
+            else:
+                th, ph = math.radians(la), math.radians(lo)
+            r = self.R - bur
+            e, xi, eta = self._locate(r * math.sin(th), r * math.cos(th))
+            wxi = _lagrange(xi, S.glj()[0] if self.axial_e[e] else S.gll()[0])
+            weta = _lagrange(eta, S.gll()[0])
+            rec.append((name, net, la, lo, bur, th, ph, e, np.outer(wxi, weta).ravel()))
+        self.receivers = rec
+        spec.r_elem = np.array([r[7] for r in rec], np.int32)
+        spec.r_phi = np.array([r[6] for r in rec], np.float32)
+        spec.r_w = np.array([r[8] for r in rec], np.float32).reshape(len(rec), 25)
+
+    def _locate(self, s, z):
+        """Quad::invMapping by Newton iterations (Mapping.cpp:17-28) over candidate elements."""
+        cen = self.crds.mean(1)
+        order = np.argsort(np.hypot(cen[:, 0] - s, cen[:, 1] - z))
+        for e in order[:64]:
+            if self.fluid[e]:
+                continue
+            xe = np.zeros(2)
+            n = self.nodes4[e:e + 1]
+            for _ in range(12):
+                ss, zz, J00, J01, J10, J11 = GEO._batch_map_jac(n, np.array([[xe[0]]]), np.array([[xe[1]]]),
+                                                               int(self.ex.etype[e]), int(self.co[e]))
+                d = np.array([s - ss[0, 0], z - zz[0, 0]])
+                if np.hypot(*d) < 1e-7:
+                    break
+                J = np.array([[J00[0, 0], J01[0, 0]], [J10[0, 0], J11[0, 0]]])
+                xe = xe + np.linalg.solve(J, d)
+            if np.all(np.abs(xe) <= 1.000001):
+                return int(e), float(np.clip(xe[0], -1, 1)), float(np.clip(xe[1], -1, 1))
+        raise RuntimeError(f"Receiver::locate || station at (s, z) = ({s}, {z}) not found")
+
+    # ------------------------------------------------------------------ output
+    def rotate(self, seis):
+        """PointwiseRecorder::record's SPZ -> RTZ rotation (PointwiseRecorder.cpp:76-93)."""
+        out = np.array(seis, np.float64)
+        if self.components == "SPZ":
+            return out
+        for i, r in enumerate(self.receivers):
+            th = r[5]
+            s_, p_, z_ = seis[:, i, 0], seis[:, i, 1], seis[:, i, 2]
+            ur = s_ * math.sin(th) + z_ * math.cos(th)
+            ut = s_ * math.cos(th) - z_ * math.sin(th)
+            out[:, i, 0], out[:, i, 1], out[:, i, 2] = ut, p_, ur
+        return out
+
+    def write_netcdf(self, seis_rtz, path=None):
+        """output/stations/axisem3d_synthetics.nc with time_points and NET.NAME.<comp>."""
+        path = Path(path or self.output_dir / "stations" / "axisem3d_synthetics.nc")
+        path.parent.mkdir(parents=True, exist_ok=True)
+        n = seis_rtz.shape[0]
+        ds = NC.Dataset()
+        ds.add_dim("ntime", n)
+        ds.add_dim("ncomp", 3)
+        ds.add_var("time_points", ("ntime",), -self.shift + np.arange(n) * self.dt)
+        for i, r in enumerate(self.receivers):
+            ds.add_var(f"{r[1]}.{r[0]}.{self.components}", ("ntime", "ncomp"), seis_rtz[:, i].astype(np.float32),
+                       attrs={"latitude": float(r[2]), "longitude": float(r[3]), "depth": float(r[4])})
+        NC.write(path, ds)
+        return path
+
+    # ------------------------------------------------------------------ run
+    def run(self, domain=None, nsteps=None):
+        from .capi import Ax3dDomain
+        dom = domain or Ax3dDomain(self.spec)
+        n = nsteps or self.nsteps
+        dom.step(n)
+        seis = dom.seismograms(0, n)
+        return self.rotate(seis), dom
+
+
+def write_inputs(input_dir, mesh_kw=None, nu=2, stf="gauss", hdur=50.0, steps=2000, record_length=None,
+                 n_stations=20, depth_km=100.0, seed=0, attenuation=False, system="source_centered"):
+    """Seeded inputs of the small benchmark configuration: mesh, four parfiles, CMTSOLUTION
+    (moment tensor ~ N(0, 1e20 N*m) written in dyn*cm) and STATIONS at uniform distance."""
+    from . import mesher
+    d = Path(input_dir)
+    d.mkdir(parents=True, exist_ok=True)
+    ds = mesher.write_half_disk(d / "mesh.e", seed=seed, **(mesh_kw or {}))
+    dt = float(ds["vals_glo_var"][1])
+    rl = record_length if record_length is not None else steps * dt
+    (d / "inparam.model").write_text(f"MODEL_1D_EXODUS_MESH_FILE mesh.e\nMODEL_3D_VOLUMETRIC_NUM 0\n"
+                                     f"MODEL_3D_GEOMETRIC_NUM 0\nMODEL_3D_OCEAN_LOAD none\nMODEL_2D_MODE off\n"
+                                     f"MODEL_PLOT_SLICES_NUM 0\nATTENUATION {'true' if attenuation else 'false'}\n")
+    (d / "inparam.nu").write_text(f"NU_TYPE constant\nNU_CONST {nu}\nNU_WISDOM_LEARN false\n")
+    (d / "inparam.time_src_recv").write_text(
+        f"TIME_DELTA_T 0.0\nTIME_DELTA_T_FACTOR 1.0\nTIME_RECORD_LENGTH {rl}\nSOURCE_TYPE earthquake\n"
+        f"SOURCE_FILE CMTSOLUTION\nSOURCE_TIME_FUNCTION {stf}\nSOURCE_STF_HALF_DURATION {hdur}\n"
+        f"OUT_STATIONS_FILE STATIONS\nOUT_STATIONS_SYSTEM {system}\nOUT_STATIONS_DUPLICATED rename\n"
+        f"OUT_STATIONS_FORMAT netcdf\nOUT_STATIONS_COMPONENTS RTZ\nOUT_STATIONS_RECORD_INTERVAL 1\n"
+        f"OUT_STATIONS_DUMP_INTERVAL 1000\nOUT_STATIONS_WHOLE_SURFACE false\nOUT_STATIONS_DEPTH_REF false\n")
+    (d / "inparam.advanced").write_text(
+        f"ATTENUATION_CG4 true\nATTENUATION_SPECFEM_LEGACY false\nATTENUATION_QKAPPA true\n"
+        f"OPTION_VERBOSE_LEVEL essential\nOPTION_STABILITY_INTERVAL 100\nOPTION_LOOP_INFO_INTERVAL 1000\n"
+        f"DEVELOP_MAX_TIME_STEPS {steps}\nDEVELOP_NON_SOURCE_MODE false\nFFTW_LUCKY_NUMBER false\n")
+    rng = np.random.default_rng(seed)
+    m = rng.normal(0.0, 1e20, 6) * 1e7  # N*m -> dyn*cm (Source.cpp:171-177)
+    names = ["Mrr", "Mtt", "Mpp", "Mrt", "Mrp", "Mtp"]
+    (d / "CMTSOLUTION").write_text(
+        "PDE 2026 1 1 0 0 0.0 0.0 0.0 100.0 6.0 6.0 SYNTHETIC\nevent name:     synthetic\ntime shift:      0.00\n"
+        f"half duration:   {hdur:.2f}\nlatitude:       0.0\nlongitude:      0.0\ndepth:          {depth_km:.4f}\n"
+        + "".join(f"{k}:       {v:.6e}\n" for k, v in zip(names, m)))
+    dist = np.linspace(10.0, 170.0, n_stations)
+    (d / "STATIONS").write_text("".join(f"S{i:03d}       SY       {t:.4f}     {(37.0 * i) % 360:.4f}    0.0    0.0\n"
+                                        for i, t in enumerate(dist)))
+    return d

@@ -1,0 +1,96 @@
+"""Inputs/outputs boundary: parfiles, Exodus (NetCDF classic) mesh, CMTSOLUTION, STATIONS,
+station NetCDF output, and the full time loop GPU vs oracle on a generated mesh."""
+import numpy as np
+import pytest
+
+from axisem3d_gb300 import netcdf as NC
+from axisem3d_gb300 import solver
+
+SMALL_MESH = dict(n_theta=16, h_mantle=600e3, h_core=700e3, r_c=1500e3)
+
+
+@pytest.fixture(scope="module")
+def small_inputs(tmp_path_factory):
+    d = tmp_path_factory.mktemp("c0") / "input"
+    return solver.write_inputs(d, mesh_kw=SMALL_MESH, steps=200, hdur=20.0, n_stations=6, seed=3)
+
+
+def test_netcdf_roundtrip(tmp_path):
+    ds = NC.Dataset()
+    ds.add_dim("n", 4)
+    ds.add_dim("m", 3)
+    a = np.arange(12, dtype=np.float32).reshape(4, 3)
+    ds.add_var("a", ("n", "m"), a, attrs={"latitude": 12.5, "units": "m"})
+    ds.add_var("i", ("n",), np.array([1, 2, 3, 4]), dtype=np.int32)
+    ds.add_strings("names", "num_names", "len_string", ["t0", "solid_fluid_boundary"])
+    NC.write(tmp_path / "x.nc", ds)
+    back = NC.read(tmp_path / "x.nc")
+    np.testing.assert_array_equal(back["a"], a)
+    np.testing.assert_array_equal(back["i"], [1, 2, 3, 4])
+    assert back.strings("names") == ["t0", "solid_fluid_boundary"]
+    assert float(back.variables["a"].attrs["latitude"][0]) == 12.5
+    assert (tmp_path / "x.nc").read_bytes()[:4] == b"CDF\x02"
+
+
+def test_netcdf_rejects_hdf5(tmp_path):
+    (tmp_path / "h.e").write_bytes(b"\x89HDF\r\n\x1a\n" + b"\0" * 64)
+    with pytest.raises(ValueError, match="HDF5"):
+        NC.read(tmp_path / "h.e")
+
+
+def test_parameters_parsing(small_inputs):
+    par = solver.Parameters(small_inputs)
+    assert par.get("NU_CONST", int) == 2
+    assert par.get("ATTENUATION", bool) is False
+    assert par.get("SOURCE_TIME_FUNCTION") == "gauss"
+    with pytest.raises(KeyError):
+        par.get("NU_EMP_REF")
+
+
+def test_missing_parfile_raises(tmp_path):
+    with pytest.raises(FileNotFoundError, match="inparam"):
+        solver.Parameters(tmp_path)
+
+
+def test_mesh_and_domain_build(small_inputs):
+    sim = solver.Simulation(small_inputs)
+    spec = sim.build()
+    ex = sim.ex
+    # every axial element has its axis on side 3, fluid core, CMB coupling points exist
+    assert (ex.side["t0"][ex.side["t0"] >= 0] == 3).all()
+    assert ex.fluid.any() and (~ex.fluid).any()
+    assert (spec.p_kind == 2).sum() > 0
+    # 2 pi sum of integral factors = volume of the Earth (ifact carries s ds dz)
+    assert spec.stf.size == 200 and len(spec.r_elem) == 6
+    assert spec.sources and spec.sources[0][1].shape == (25, 3, 3)
+
+
+def test_oracle_run_and_netcdf_output(small_inputs, tmp_path):
+    from oracle.oracle_py import OracleDomain
+    sim = solver.Simulation(small_inputs, output_dir=tmp_path)
+    spec = sim.build()
+    o = OracleDomain(spec)
+    o.step(200)
+    rtz = sim.rotate(o.seismograms(0, 200))
+    assert np.isfinite(rtz).all() and np.abs(rtz).max() > 0
+    p = sim.write_netcdf(rtz)
+    ds = NC.read(p)
+    assert ds["time_points"].shape == (200,)
+    np.testing.assert_allclose(ds["SY.S001.RTZ"], rtz[:, 1], rtol=1e-6, atol=1e-30)
+
+
+@pytest.mark.gpu
+def test_full_solver_gpu_matches_oracle(small_inputs, ax3d_lib):
+    """Seismograms of the whole loop (source, fluid core, solid-fluid coupling, axis, receivers)."""
+    from oracle.oracle_py import OracleDomain
+    from axisem3d_gb300.capi import Ax3dDomain
+    sim = solver.Simulation(small_inputs)
+    spec = sim.build()
+    g, o = Ax3dDomain(spec), OracleDomain(spec)
+    g.step(200)
+    o.step(200)
+    a, b = g.seismograms(0, 200), o.seismograms(0, 200)
+    assert np.linalg.norm(a - b) <= 1e-5 * np.linalg.norm(b)
+    for which in ("displ", "veloc"):
+        x, y = g.get(which, "solid"), o.get(which, "solid")
+        assert np.linalg.norm(x - y) <= 1e-5 * np.linalg.norm(y)
