@@ -127,6 +127,10 @@ struct ax3d_domain {
     DevBuf<float> d_rphi, d_rw, d_seis;
     int seis_cap = 0;
     DevBuf<int32_t> d_flag;
+    DevBuf<int32_t> d_tstep, d_targ;  // step counter (1-based) and explicit step index
+    int32_t h_targ = 0;
+    bool use_graphs = true;
+    cudaGraphExec_t graph_exec = nullptr;
 
     ax3d::ElemTable T{};
     ax3d::PointTable P{};
@@ -188,6 +192,7 @@ struct ax3d_domain {
             cudaEventDestroy(m.b);
         }
         for (auto e : pool) cudaEventDestroy(e);
+        drop_graph();
         if (stream) cudaStreamDestroy(stream);
     }
 
@@ -472,6 +477,10 @@ struct ax3d_domain {
         d_seis.zero(st);
         d_flag.alloc(1);
         d_flag.zero(st);
+        d_tstep.alloc(1);
+        d_targ.alloc(1);
+        tstep = 1;
+        CK(cudaMemcpyAsync(d_tstep.p, &tstep, sizeof(int32_t), cudaMemcpyHostToDevice, st));
 
         P.n = np;
         P.nr = d_pnr.p;
@@ -530,11 +539,17 @@ struct ax3d_domain {
         ax3d::launch_newmark(P, F, (float)dt, (float)half_dt, (float)half_dt_dt, kahan, d_pts3d.p, n_pts3d,
                              stream);
     }
+    // explicit step index for the fine-grained entry points (the step loop reads d_tstep)
+    void set_targ(int t) {
+        h_targ = t;
+        CK(cudaMemcpyAsync(d_targ.p, &h_targ, sizeof(int32_t), cudaMemcpyHostToDevice, stream));
+    }
     void apply_source(int t) {
         if (s_elem.empty()) return;
         if (t < 0 || t >= (int)stf.size()) throw Error(AX3D_ERR_ARG, "ax3d_apply_source || step out of range");
+        set_targ(t);
         ax3d::launch_source(P, T, F, d_selem.p, d_snord.p, d_sofs_src.p, d_sforce.p, (int)s_elem.size(),
-                            d_stf.p, t, stream);
+                            d_stf.p, (int)stf.size(), d_targ.p, 0, stream);
     }
     void compute_stiff() {
         ax3d::launch_elem_fourier_solid(T, P, F.su, d_items_s.p, nitems_s, sls, stream);
@@ -548,8 +563,9 @@ struct ax3d_domain {
         if (r_elem.empty()) return;
         if (t < 0) throw Error(AX3D_ERR_ARG, "ax3d_record || negative step");
         if (t >= seis_cap) grow_seis(t + 1);
-        ax3d::launch_record(P, T, F.su, d_relem.p, d_rphi.p, d_rw.p, (int)r_elem.size(),
-                            d_seis.p + (size_t)t * r_elem.size() * 3, stream);
+        set_targ(t);
+        ax3d::launch_record(P, T, F.su, d_relem.p, d_rphi.p, d_rw.p, (int)r_elem.size(), d_seis.p, seis_cap,
+                            d_targ.p, 0, stream);
     }
     void grow_seis(int need) {
         int cap = std::max(need, seis_cap * 2);
@@ -562,6 +578,49 @@ struct ax3d_domain {
         std::swap(nb.p, d_seis.p);
         std::swap(nb.n, d_seis.n);
         seis_cap = cap;
+        drop_graph();  // the captured step holds the old buffer address
+    }
+    void drop_graph() {
+        if (graph_exec) cudaGraphExecDestroy(graph_exec);
+        graph_exec = nullptr;
+    }
+    // One time step of Newmark::solve with the step index read on the device (d_tstep),
+    // so the same launches serve every step; used directly or captured as a CUDA graph.
+    void enqueue_step() {
+        const int nrow = (P.nsrows > 0) + (P.nfrows > 0);
+        tbegin(AX3D_TIMER_POINTS);
+        update_newmark();
+        tend(nrow + (n_pts3d > 0));
+        if (!s_elem.empty()) {
+            tbegin(AX3D_TIMER_SOURCE);
+            ax3d::launch_source(P, T, F, d_selem.p, d_snord.p, d_sofs_src.p, d_sforce.p, (int)s_elem.size(),
+                                d_stf.p, (int)stf.size(), d_tstep.p, -1, stream);
+            tend(1);
+        }
+        tbegin(AX3D_TIMER_ELEMENTS);
+        ax3d::launch_elem_fourier_solid(T, P, F.su, d_items_s.p, nitems_s, sls, stream);
+        ax3d::launch_elem_fourier_fluid(T, P, F.fu, d_items_f.p, nitems_f, stream);
+        for (auto &b : buckets_s) ax3d::launch_elem_phys_solid(T, P, F.su, b, sls, stream);
+        for (auto &b : buckets_f) ax3d::launch_elem_phys_fluid(T, P, F.fu, b, stream);
+        tend(n_elem_launches());
+        tbegin(AX3D_TIMER_ASSEMBLE);
+        ax3d::launch_gather(P, T, F, stream);
+        tend(nrow);
+        tbegin(AX3D_TIMER_COUPLE);
+        couple();
+        tend((P.nsrows > 0) + (n_sf3d > 0));
+        if (!r_elem.empty()) {
+            tbegin(AX3D_TIMER_RECORD);
+            ax3d::launch_record(P, T, F.su, d_relem.p, d_rphi.p, d_rw.p, (int)r_elem.size(), d_seis.p, seis_cap,
+                                d_tstep.p, -1, stream);
+            tend(1);
+        }
+        if (stab_interval > 0) {
+            tbegin(AX3D_TIMER_OTHER);
+            ax3d::launch_stability(F.su, nsolid, F.fu, nfluid, d_flag.p, d_tstep.p, stab_interval, stream);
+            tend(1);
+        }
+        ax3d::launch_advance(d_tstep.p, stream);
     }
     int n_elem_launches() const {
         return (nitems_s > 0) + (nitems_f > 0) + (int)buckets_s.size() + (int)buckets_f.size();
@@ -573,40 +632,22 @@ struct ax3d_domain {
             s0 = get_event();
             CK(cudaEventRecord(s0, stream));
         }
-        const int nrow = (P.nsrows > 0) + (P.nfrows > 0);
-        for (int s = 0; s < nsteps; s++) {
-            tbegin(AX3D_TIMER_POINTS);
-            update_newmark();
-            tend(nrow + (n_pts3d > 0));
-            if (!s_elem.empty()) {
-                tbegin(AX3D_TIMER_SOURCE);
-                apply_source(tstep - 1);
-                tend(1);
+        if (!r_elem.empty() && tstep - 1 + nsteps > seis_cap) grow_seis(tstep - 1 + nsteps);
+        if (timers || !use_graphs) {
+            // phase timers need events between the phases: plain launches
+            for (int s = 0; s < nsteps; s++) enqueue_step();
+        } else {
+            if (!graph_exec) {
+                cudaGraph_t g = nullptr;
+                CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+                enqueue_step();
+                CK(cudaStreamEndCapture(stream, &g));
+                CK(cudaGraphInstantiate(&graph_exec, g, 0));
+                CK(cudaGraphDestroy(g));
             }
-            tbegin(AX3D_TIMER_ELEMENTS);
-            ax3d::launch_elem_fourier_solid(T, P, F.su, d_items_s.p, nitems_s, sls, stream);
-            ax3d::launch_elem_fourier_fluid(T, P, F.fu, d_items_f.p, nitems_f, stream);
-            for (auto &b : buckets_s) ax3d::launch_elem_phys_solid(T, P, F.su, b, sls, stream);
-            for (auto &b : buckets_f) ax3d::launch_elem_phys_fluid(T, P, F.fu, b, stream);
-            tend(n_elem_launches());
-            tbegin(AX3D_TIMER_ASSEMBLE);
-            ax3d::launch_gather(P, T, F, stream);
-            tend(nrow);
-            tbegin(AX3D_TIMER_COUPLE);
-            couple();
-            tend((P.nsrows > 0) + (n_sf3d > 0));
-            if (!r_elem.empty()) {
-                tbegin(AX3D_TIMER_RECORD);
-                record(tstep - 1);
-                tend(1);
-            }
-            if (stab_interval > 0 && tstep % stab_interval == 0) {
-                tbegin(AX3D_TIMER_OTHER);
-                ax3d::launch_stability(F.su, nsolid, F.fu, nfluid, d_flag.p, stream);
-                tend(1);
-            }
-            tstep++;
+            for (int s = 0; s < nsteps; s++) CK(cudaGraphLaunch(graph_exec, stream));
         }
+        tstep += nsteps;
         if (timers) {
             s1 = get_event();
             CK(cudaEventRecord(s1, stream));
@@ -649,8 +690,9 @@ struct ax3d_domain {
         d_mem.zero(stream);
         d_seis.zero(stream);
         d_flag.zero(stream);
-        CK(cudaStreamSynchronize(stream));
         tstep = 1;
+        CK(cudaMemcpyAsync(d_tstep.p, &tstep, sizeof(int32_t), cudaMemcpyHostToDevice, stream));
+        CK(cudaStreamSynchronize(stream));
     }
 };
 

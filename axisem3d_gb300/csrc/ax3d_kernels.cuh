@@ -40,12 +40,13 @@ void launch_couple(const PointTable &P, const Fields &F, const int32_t *sf3d, in
                    cudaStream_t s);
 void launch_source(const PointTable &P, const ElemTable &T, const Fields &F,
                    const int32_t *src_elem, const int32_t *src_nord, const int64_t *src_ofs,
-                   const float2 *src_force, int nsrc, const float *stf, int tstep,
-                   cudaStream_t s);
+                   const float2 *src_force, int nsrc, const float *stf, int nstf,
+                   const int32_t *tptr, int tofs, cudaStream_t s);
 void launch_record(const PointTable &P, const ElemTable &T, const float2 *su,
                    const int32_t *rec_elem, const float *rec_phi, const float *rec_w, int nrec,
-                   float *out, cudaStream_t s);
+                   float *out_base, int cap, const int32_t *tptr, int tofs, cudaStream_t s);
 void launch_stability(const float2 *su, int64_t ns, const float2 *fu, int64_t nf,
-                      int32_t *flag, cudaStream_t s);
+                      int32_t *flag, const int32_t *tptr, int interval, cudaStream_t s);
+void launch_advance(int32_t *tptr, cudaStream_t s);
 
 }  // namespace ax3d

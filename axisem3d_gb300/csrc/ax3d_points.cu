@@ -375,9 +375,13 @@ void launch_couple(const PointTable &P, const Fields &F, const int32_t *sf3d, in
 }
 
 // ---------------- source (SourceTerm.cpp:29-35) ----------------
+// The step index is read on the device (*tptr + tofs) so that one captured step serves
+// every time step of a CUDA graph replay.
 __global__ void k_source(PointTable P, ElemTable T, float2 *__restrict__ ss, const int32_t *src_elem,
                          const int32_t *src_nord, const int64_t *src_ofs, const float2 *force, int nsrc,
-                         const float *stf, int tstep) {
+                         const float *stf, int nstf, const int32_t *tptr, int tofs) {
+    const int tstep = *tptr + tofs;
+    if (tstep < 0 || tstep >= nstf) return;  // beyond the source-time function: no force
     const float f = stf[tstep];
     for (int s = 0; s < nsrc; s++) {
         const int e = src_elem[s], nord = src_nord[s];
@@ -396,16 +400,19 @@ __global__ void k_source(PointTable P, ElemTable T, float2 *__restrict__ ss, con
 
 void launch_source(const PointTable &P, const ElemTable &T, const Fields &F, const int32_t *src_elem,
                    const int32_t *src_nord, const int64_t *src_ofs, const float2 *src_force, int nsrc,
-                   const float *stf, int tstep, cudaStream_t s) {
+                   const float *stf, int nstf, const int32_t *tptr, int tofs, cudaStream_t s) {
     if (nsrc <= 0) return;
-    k_source<<<1, 128, 0, s>>>(P, T, F.ss, src_elem, src_nord, src_ofs, src_force, nsrc, stf, tstep);
+    k_source<<<1, 128, 0, s>>>(P, T, F.ss, src_elem, src_nord, src_ofs, src_force, nsrc, stf, nstf, tptr, tofs);
 }
 
 // ---------------- receivers (SolidElement::computeGroundMotion, SolidElement.cpp:189-216) ----------------
 __global__ void k_record(PointTable P, ElemTable T, const float2 *__restrict__ su, const int32_t *rec_elem,
-                         const float *rec_phi, const float *rec_w, int nrec, float *out) {
+                         const float *rec_phi, const float *rec_w, int nrec, float *out_base, int cap,
+                         const int32_t *tptr, int tofs) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (warp >= nrec) return;
+    const int t = *tptr + tofs;
+    if (warp >= nrec || t < 0 || t >= cap) return;
+    float *out = out_base + (size_t)t * nrec * 3;
     const int e = rec_elem[warp];
     const float phi = rec_phi[warp];
     const int nr = T.nr[e], lim = nr / 2 - (nr % 2 == 0);
@@ -442,16 +449,18 @@ __global__ void k_record(PointTable P, ElemTable T, const float2 *__restrict__ s
 }
 
 void launch_record(const PointTable &P, const ElemTable &T, const float2 *su, const int32_t *rec_elem,
-                   const float *rec_phi, const float *rec_w, int nrec, float *out, cudaStream_t s) {
+                   const float *rec_phi, const float *rec_w, int nrec, float *out_base, int cap,
+                   const int32_t *tptr, int tofs, cudaStream_t s) {
     if (nrec <= 0) return;
     const int threads = 128;
     const int blocks = (nrec * 32 + threads - 1) / threads;
-    k_record<<<blocks, threads, 0, s>>>(P, T, su, rec_elem, rec_phi, rec_w, nrec, out);
+    k_record<<<blocks, threads, 0, s>>>(P, T, su, rec_elem, rec_phi, rec_w, nrec, out_base, cap, tptr, tofs);
 }
 
 // ---------------- stability (Domain::checkStability, Domain.cpp:237-275) ----------------
 __global__ void k_stability(const float2 *__restrict__ su, int64_t ns, const float2 *__restrict__ fu, int64_t nf,
-                            int32_t *flag) {
+                            int32_t *flag, const int32_t *tptr, int interval) {
+    if (interval <= 0 || (*tptr) % interval != 0) return;  // Newmark.cpp:68-70
     bool bad = false;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < ns + nf;
          i += (int64_t)gridDim.x * blockDim.x) {
@@ -462,9 +471,13 @@ __global__ void k_stability(const float2 *__restrict__ su, int64_t ns, const flo
 }
 
 void launch_stability(const float2 *su, int64_t ns, const float2 *fu, int64_t nf, int32_t *flag,
-                      cudaStream_t s) {
+                      const int32_t *tptr, int interval, cudaStream_t s) {
     if (ns + nf == 0) return;
-    k_stability<<<grid_for(ns + nf, ROW_THREADS), ROW_THREADS, 0, s>>>(su, ns, fu, nf, flag);
+    k_stability<<<grid_for(ns + nf, ROW_THREADS), ROW_THREADS, 0, s>>>(su, ns, fu, nf, flag, tptr, interval);
 }
+
+__global__ void k_advance(int32_t *tptr) { *tptr += 1; }
+
+void launch_advance(int32_t *tptr, cudaStream_t s) { k_advance<<<1, 1, 0, s>>>(tptr); }
 
 }  // namespace ax3d
