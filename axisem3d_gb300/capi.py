@@ -73,6 +73,9 @@ def bind(lib: C.CDLL, prefix: str, field_ctype, extra_double_io: bool = False):
     f("read_seismograms").argtypes = [C.c_void_p, C.c_int32, C.c_int32, field_ctype]
     f("current_step").argtypes = [C.c_void_p]
     f("current_step").restype = C.c_int32
+    f("set_wisdom_learning").argtypes = [C.c_void_p, C.c_int32, C.c_float]
+    f("learn_wisdom").argtypes = [C.c_void_p, C.c_float]
+    f("get_wisdom").argtypes = [C.c_void_p, P_I32]
 
 
 _LIB = None
@@ -185,6 +188,19 @@ class _DomainBase:
     @property
     def current_step(self) -> int:
         return int(self._call("current_step", self.h))
+
+    def set_wisdom_learning(self, interval: int, cutoff: float):
+        """Domain::learnWisdom every `interval` steps during step() (NU_WISDOM_LEARN_INTERVAL/_EPSILON)."""
+        self._ck(self._call("set_wisdom_learning", self.h, int(interval), float(cutoff)))
+
+    def learn_wisdom(self, cutoff: float):
+        self._ck(self._call("learn_wisdom", self.h, float(cutoff)))
+
+    def get_wisdom(self) -> np.ndarray:
+        """Per point Nu wisdom (SolidPoint::getNuWisdom)."""
+        out = np.zeros(max(self.spec.n_points, 1), np.int32)
+        self._ck(self._call("get_wisdom", self.h, _p(out, C.c_int32)))
+        return out[:self.spec.n_points]
 
     @property
     def complex_dtype(self):

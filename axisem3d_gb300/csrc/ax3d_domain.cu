@@ -128,6 +128,10 @@ struct ax3d_domain {
     int seis_cap = 0;
     DevBuf<int32_t> d_flag;
     DevBuf<int32_t> d_tstep, d_targ;  // step counter (1-based) and explicit step index
+    DevBuf<float> d_wis_max;          // [P][4] largest Hilbert norm per component (s, phi, z, fluid)
+    DevBuf<int32_t> d_wis_nu;         // [P][4] Nu wisdom per component
+    int wis_interval = 0;
+    float wis_cutoff = 0.f;
     int32_t h_targ = 0;
     bool use_graphs = true;
     cudaGraphExec_t graph_exec = nullptr;
@@ -479,6 +483,7 @@ struct ax3d_domain {
         d_flag.zero(st);
         d_tstep.alloc(1);
         d_targ.alloc(1);
+        reset_wisdom(st);
         tstep = 1;
         CK(cudaMemcpyAsync(d_tstep.p, &tstep, sizeof(int32_t), cudaMemcpyHostToDevice, st));
 
@@ -580,6 +585,32 @@ struct ax3d_domain {
         seis_cap = cap;
         drop_graph();  // the captured step holds the old buffer address
     }
+    // mMaxDisplWisdom = -1, mNuWisdom = Nu (SolidPoint.cpp:9-17, FluidPoint.cpp:9-17)
+    void reset_wisdom(cudaStream_t st) {
+        const int np = (int)p_nr.size();
+        std::vector<float> mx((size_t)np * 4, -1.f);
+        std::vector<int32_t> nu((size_t)np * 4);
+        for (int p = 0; p < np; p++)
+            for (int c = 0; c < 4; c++) nu[(size_t)p * 4 + c] = p_nr[p] / 2;
+        d_wis_max.upload(mx.empty() ? std::vector<float>{0.f} : mx, st);
+        d_wis_nu.upload(nu.empty() ? std::vector<int32_t>{0} : nu, st);
+        drop_graph();
+    }
+    std::vector<int32_t> get_wisdom() {
+        const int np = (int)p_nr.size();
+        std::vector<int32_t> nu((size_t)np * 4);
+        CK(cudaMemcpyAsync(nu.data(), d_wis_nu.p, nu.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
+        CK(cudaStreamSynchronize(stream));
+        std::vector<int32_t> out(np, 0);
+        for (int p = 0; p < np; p++) {
+            int m = 0;
+            if (p_kind[p] != AX3D_POINT_FLUID)
+                m = std::max({nu[(size_t)p * 4], nu[(size_t)p * 4 + 1], nu[(size_t)p * 4 + 2]});
+            if (p_kind[p] != AX3D_POINT_SOLID) m = std::max(m, nu[(size_t)p * 4 + 3]);
+            out[p] = m;
+        }
+        return out;
+    }
     void drop_graph() {
         if (graph_exec) cudaGraphExecDestroy(graph_exec);
         graph_exec = nullptr;
@@ -613,6 +644,11 @@ struct ax3d_domain {
             tbegin(AX3D_TIMER_RECORD);
             ax3d::launch_record(P, T, F.su, d_relem.p, d_rphi.p, d_rw.p, (int)r_elem.size(), d_seis.p, seis_cap,
                                 d_tstep.p, -1, stream);
+            tend(1);
+        }
+        if (wis_interval > 0) {
+            tbegin(AX3D_TIMER_OTHER);
+            ax3d::launch_learn_wisdom(P, F, d_wis_max.p, d_wis_nu.p, wis_cutoff, d_tstep.p, wis_interval, stream);
             tend(1);
         }
         if (stab_interval > 0) {
@@ -690,6 +726,7 @@ struct ax3d_domain {
         d_mem.zero(stream);
         d_seis.zero(stream);
         d_flag.zero(stream);
+        reset_wisdom(stream);
         tstep = 1;
         CK(cudaMemcpyAsync(d_tstep.p, &tstep, sizeof(int32_t), cudaMemcpyHostToDevice, stream));
         CK(cudaStreamSynchronize(stream));
@@ -888,6 +925,36 @@ int ax3d_reset(ax3d_domain *d) {
 }
 
 int32_t ax3d_current_step(const ax3d_domain *d) { return d ? d->tstep : -1; }
+
+int ax3d_set_wisdom_learning(ax3d_domain *d, int32_t interval, float cutoff) {
+    return guard([&] {
+        if (!d) throw Error(AX3D_ERR_ARG, "ax3d_set_wisdom_learning || null domain");
+        if (interval > 0 && !(cutoff > 0.f)) throw Error(AX3D_ERR_ARG, "ax3d_set_wisdom_learning || cutoff must be > 0");
+        d->wis_interval = interval > 0 ? interval : 0;
+        d->wis_cutoff = cutoff;
+        d->drop_graph();
+    });
+}
+
+int ax3d_learn_wisdom(ax3d_domain *d, float cutoff) {
+    return guard([&] {
+        if (!d) throw Error(AX3D_ERR_ARG, "ax3d_learn_wisdom || null domain");
+        d->need_final();
+        if (!(cutoff > 0.f)) throw Error(AX3D_ERR_ARG, "ax3d_learn_wisdom || cutoff must be > 0");
+        ax3d::launch_learn_wisdom(d->P, d->F, d->d_wis_max.p, d->d_wis_nu.p, cutoff, nullptr, 0, d->stream);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(d->stream));
+    });
+}
+
+int ax3d_get_wisdom(ax3d_domain *d, int32_t *nu_wisdom) {
+    return guard([&] {
+        if (!d || !nu_wisdom) throw Error(AX3D_ERR_ARG, "ax3d_get_wisdom || null argument");
+        d->need_final();
+        auto v = d->get_wisdom();
+        std::copy(v.begin(), v.end(), nu_wisdom);
+    });
+}
 
 int ax3d_enable_timers(ax3d_domain *d, int32_t enable) {
     return guard([&] {

@@ -48,5 +48,8 @@ void launch_record(const PointTable &P, const ElemTable &T, const float2 *su,
 void launch_stability(const float2 *su, int64_t ns, const float2 *fu, int64_t nf,
                       int32_t *flag, const int32_t *tptr, int interval, cudaStream_t s);
 void launch_advance(int32_t *tptr, cudaStream_t s);
+// tptr == nullptr: learn now; otherwise only when (*tptr - 1) % interval == 0
+void launch_learn_wisdom(const PointTable &P, const Fields &F, float *maxh, int32_t *nuw, float cutoff,
+                         const int32_t *tptr, int interval, cudaStream_t s);
 
 }  // namespace ax3d

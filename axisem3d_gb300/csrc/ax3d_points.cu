@@ -481,3 +481,51 @@ __global__ void k_advance(int32_t *tptr) { *tptr += 1; }
 void launch_advance(int32_t *tptr, cudaStream_t s) { k_advance<<<1, 1, 0, s>>>(tptr); }
 
 }  // namespace ax3d
+
+namespace ax3d {
+
+// ---------------- Nu wisdom (SolidPoint::learnWisdom, SolidPoint.cpp:240-272) ----------------
+// One thread per point; per component the L2 norm, the Hilbert norm (order 0 halved) and,
+// when the Hilbert norm is a new maximum, the smallest order whose tail energy is below
+// h2 * cutoff^2.  Sums run over orders in increasing order (the oracle's order).
+__device__ int wisdom_component(const float2 *u, int stride, int nu, float cutoff, float &maxh, int nu_old) {
+    float l2 = 0.f;
+    for (int a = 0; a <= nu; a++) {
+        const float2 v = u[a * stride];
+        l2 += v.x * v.x + v.y * v.y;
+    }
+    const float2 v0 = u[0];
+    // Real h2norm = L2norm - .5 * |u_0|^2, the .5 being a double literal
+    const float h2 = (float)((double)l2 - 0.5 * (double)(v0.x * v0.x + v0.y * v0.y));
+    if (h2 <= maxh) return nu_old;
+    maxh = h2;
+    const float tol = h2 * cutoff * cutoff;
+    float head = 0.f;
+    for (int nn = 0; nn < nu; nn++) {
+        const float2 v = u[nn * stride];
+        head += v.x * v.x + v.y * v.y;
+        if (l2 - head <= tol) return nn;
+    }
+    return nu;
+}
+
+__global__ void k_learn_wisdom(PointTable P, const float2 *__restrict__ su, const float2 *__restrict__ fu,
+                               float *maxh, int32_t *nuw, float cutoff, const int32_t *tptr, int interval) {
+    if (tptr && (interval <= 0 || (*tptr - 1) % interval != 0)) return;  // Domain::learnWisdom(tstep - 1)
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P.n; p += gridDim.x * blockDim.x) {
+        const int nu = P.nr[p] / 2;
+        if (P.sofs[p] >= 0)
+            for (int c = 0; c < 3; c++)
+                nuw[p * 4 + c] = wisdom_component(su + P.sofs[p] + c, 3, nu, cutoff, maxh[p * 4 + c], nuw[p * 4 + c]);
+        if (P.fofs[p] >= 0)
+            nuw[p * 4 + 3] = wisdom_component(fu + P.fofs[p], 1, nu, cutoff, maxh[p * 4 + 3], nuw[p * 4 + 3]);
+    }
+}
+
+void launch_learn_wisdom(const PointTable &P, const Fields &F, float *maxh, int32_t *nuw, float cutoff,
+                         const int32_t *tptr, int interval, cudaStream_t s) {
+    if (P.n <= 0) return;
+    k_learn_wisdom<<<grid_for(P.n, ROW_THREADS), ROW_THREADS, 0, s>>>(P, F.su, F.fu, maxh, nuw, cutoff, tptr, interval);
+}
+
+}  // namespace ax3d

@@ -1,0 +1,196 @@
+"""Volumetric 3-D models: the MODEL_3D_VOLUMETRIC_LIST entries of inparam.model.
+
+Each entry is "name$param1$param2...", split on '$' (Volumetric3D::buildInparam,
+SOLVER/src/3d_model/3d_volumetric/Volumetric3D.cpp:23-95).  A model returns, for points
+given in the source-centred Cartesian frame, a value and an in-range mask; the caller
+applies it to one material property with one of the four reference types
+(Material::addVolumetric3D, SOLVER/src/preloop/physics/material/Material.cpp:125-212):
+
+    Absolute          X = value (SI)
+    Reference1D       X = X1D * (1 + value)
+    Reference3D       X = X * (1 + value)
+    ReferencePerturb  X = (X - X1D) * (1 + value) + X1D
+
+Built models:
+  bubble           SOLVER/src/3d_model/3d_volumetric/simple_shapes/Volumetric3D_bubble.cpp:11-137
+                   bubble$PROP$REF$value$radius_km$depth_km$lat$lon[$src_centred$fluid$hwhm_km]
+  gaussian_random  a seeded stationary Gaussian random field (a synthetic stand-in for
+                   tomography models whose data files are not shipped):
+                   gaussian_random$PROP$REF$rms$lateral_corr_km$radial_corr_km$seed[$fluid]
+PROP is VP, VS or RHO (VP/VS act on both the vertical and horizontal velocities).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+PROPS = ("VP", "VS", "RHO")
+REFS = {"absolute": 0, "abs": 0, "reference1d": 1, "ref1d": 1, "reference3d": 2, "ref3d": 2,
+        "referenceperturb": 3, "refptb": 3}
+ABS_SI = {"VP": 1e3, "VS": 1e3, "RHO": 1e3}   # km/s, g/cm^3 -> SI (MaterialPropertyAbsSI)
+
+
+def _truthy(s):
+    return s.strip().lower() in ("true", "1", "yes", "on")
+
+
+def _rotation(theta, phi):
+    ct, st, cp, sp = math.cos(theta), math.sin(theta), math.cos(phi), math.sin(phi)
+    return np.array([[ct * cp, -sp, st * cp], [ct * sp, cp, st * sp], [-st, 0.0, ct]])
+
+
+class Model3D:
+    prop = "VP"
+    ref = 1
+    fluid = False
+
+    def _head(self, params, name, nmin):
+        if len(params) < nmin:
+            raise ValueError(f"Volumetric3D_{name}::initialize || need at least {nmin} parameters")
+        prop = params[0].strip().upper()
+        if prop not in PROPS:
+            raise ValueError(f"Volumetric3D_{name}::initialize || Unknown material property, name = {params[0]}")
+        ref = params[1].strip().lower()
+        if ref not in REFS:
+            raise ValueError(f"Volumetric3D_{name}::initialize || Unknown material reference type, type = {params[1]}")
+        self.prop, self.ref = prop, REFS[ref]
+
+    def evaluate(self, xyz):
+        """xyz: (..., 3) source-frame Cartesian [m] -> (value, in_range), both shaped (...)."""
+        raise NotImplementedError
+
+
+class Bubble(Model3D):
+    def __init__(self, params, src, R):
+        self._head(params, "bubble", 7)
+        value, radius, depth, lat, lon = (float(p) for p in params[2:7])
+        self.value, self.radius = value, radius * 1e3
+        src_centred = _truthy(params[7]) if len(params) > 7 else False
+        self.fluid = _truthy(params[8]) if len(params) > 8 else False
+        hwhm = float(params[9]) * 1e3 if len(params) > 9 else -1.0
+        r = R - depth * 1e3
+        if src_centred:
+            t, p = math.radians(lat), math.radians(lon)
+            self.center = r * np.array([math.sin(t) * math.cos(p), math.sin(t) * math.sin(p), math.cos(t)])
+        else:
+            t, p = math.radians(90.0 - lat), math.radians(lon)
+            xg = r * np.array([math.sin(t) * math.cos(p), math.sin(t) * math.sin(p), math.cos(t)])
+            slat, slon = src
+            self.center = _rotation(math.radians(90.0 - slat), math.radians(slon)).T @ xg
+        self.hwhm = self.radius * 0.2 if hwhm < 0 else hwhm
+        if self.ref == 0:
+            self.hwhm = 0.0
+            self.value *= ABS_SI[self.prop]
+
+    def evaluate(self, xyz):
+        d = np.linalg.norm(xyz - self.center, axis=-1) - self.radius
+        d = np.maximum(d, 0.0)
+        inr = d <= 4.0 * self.hwhm
+        if self.hwhm > 0:
+            sd = self.hwhm / math.sqrt(2.0 * math.log(2.0))
+            val = self.value * np.exp(-d * d / (2.0 * sd * sd))
+        else:
+            val = np.full(d.shape, self.value)
+        return np.where(inr, val, 0.0), inr
+
+
+class GaussianRandom(Model3D):
+    """delta(x) = rms sqrt(2/M) sum_j cos(kr_j r + kl_j . (R n) + phase_j), r = |x|, n = x/r,
+    kr_j ~ N(0, 1/Lr^2), kl_j ~ N(0, I/Ll^2): a stationary field with RMS `rms` and
+    covariance rms^2 exp(-dr^2/(2Lr^2) - R^2|dn|^2/(2Ll^2))."""
+    modes = 64
+
+    def __init__(self, params, R):
+        self._head(params, "gaussian_random", 6)
+        self.rms = float(params[2])
+        ll, lr = float(params[3]) * 1e3, float(params[4]) * 1e3
+        seed = int(params[5])
+        self.fluid = _truthy(params[6]) if len(params) > 6 else False
+        rng = np.random.default_rng(seed)
+        self.kr = rng.standard_normal(self.modes) / lr
+        self.kl = rng.standard_normal((self.modes, 3)) / ll
+        self.ph = rng.uniform(0.0, 2 * math.pi, self.modes)
+        self.R = R
+        if self.ref == 0:
+            raise ValueError("Volumetric3D_gaussian_random::initialize || reference type must be relative")
+
+    def evaluate(self, xyz):
+        r = np.linalg.norm(xyz, axis=-1)
+        n = xyz / np.maximum(r, 1e-9)[..., None]
+        arg = r[..., None] * self.kr + self.R * (n @ self.kl.T) + self.ph
+        val = self.rms * math.sqrt(2.0 / self.modes) * np.cos(arg).sum(-1)
+        return val, np.ones(r.shape, bool)
+
+
+def volumetric_models(par, src_latlon, R):
+    """Volumetric3D::buildInparam: the MODEL_3D_VOLUMETRIC_NUM models of the list."""
+    n = par.get("MODEL_3D_VOLUMETRIC_NUM", int)
+    out = []
+    for i in range(n):
+        try:
+            entry = par.get("MODEL_3D_VOLUMETRIC_LIST", str, i)
+        except (KeyError, IndexError):
+            raise ValueError("Volumetric3D::buildInparam || Not enough model names provided in "
+                             f"MODEL_3D_VOLUMETRIC_LIST, MODEL_3D_VOLUMETRIC_NUM = {n}")
+        strs = entry.split("$")
+        name, params = strs[0].lower(), strs[1:]
+        if name == "bubble":
+            out.append(Bubble(params, src_latlon, R))
+        elif name == "gaussian_random":
+            out.append(GaussianRandom(params, R))
+        else:
+            raise NotImplementedError(f"Volumetric3D::buildInparam || volumetric model {strs[0]} is not built "
+                                      "(its data files are not shipped)")
+    return out
+
+
+def apply_models(models, props1d, crds, nr, fluid):
+    """3-D properties of a group of elements sharing one Nr.
+
+    props1d: {"VP","VS","RHO": (n, 25)} 1-D values at the GLL points; crds (n, 25, 2) = (s, z);
+    fluid (n,) bool.  Slice alpha sits at phi = 2 pi alpha / nr.  Returns ({prop: (n, nr, 25)},
+    touched (n,) bool): elements with any point inside any model's range."""
+    phi = 2 * math.pi * np.arange(nr) / nr
+    s, z = crds[..., 0], crds[..., 1]
+    xyz = np.stack([s[:, None, :] * np.cos(phi)[None, :, None], s[:, None, :] * np.sin(phi)[None, :, None],
+                    np.broadcast_to(z[:, None, :], (len(s), nr, 25))], -1)
+    cur = {k: np.repeat(v[:, None, :], nr, 1).astype(float) for k, v in props1d.items()}
+    touched = np.zeros(len(s), bool)
+    for m in models:
+        val, inr = m.evaluate(xyz)
+        if not m.fluid:
+            inr = inr & ~fluid[:, None, None]
+        if not inr.any():
+            continue
+        touched |= inr.any((1, 2))
+        x1 = props1d[m.prop][:, None, :]
+        x = cur[m.prop]
+        if m.ref == 0:
+            new = np.broadcast_to(val, x.shape)
+        elif m.ref == 1:
+            new = x1 * (1.0 + val)
+        elif m.ref == 2:
+            new = x * (1.0 + val)
+        else:
+            new = (x - x1) * (1.0 + val) + x1
+        cur[m.prop] = np.where(inr, new, x)
+    return cur, touched
+
+
+def linear_resampling(new_size, original):
+    """XMath::linearResampling (SOLVER/src/preloop/utilities/XMath.cpp:161-186): slice values of a
+    ring of len(original) samples, resampled onto new_size equally spaced slices."""
+    n = len(original)
+    if new_size == n:
+        return np.asarray(original, float)
+    if np.all(original == original[0]):
+        return np.full(new_size, float(original[0]))
+    dphi, dphi0 = 2 * math.pi / new_size, 2 * math.pi / n
+    out = np.empty(new_size)
+    for i in range(new_size):
+        p = i * dphi
+        l0 = int(p / dphi0)
+        l1 = 0 if l0 + 1 == n else l0 + 1
+        out[i] = (original[l1] - original[l0]) / dphi0 * (p - l0 * dphi0) + original[l0]
+    return out

@@ -17,6 +17,7 @@ from pathlib import Path
 import numpy as np
 
 from . import attenuation as ATT
+from . import model3d as M3D
 from . import geometry as GEO
 from . import netcdf as NC
 from . import spectral as S
@@ -142,7 +143,9 @@ class Simulation:
         self.par = Parameters(self.input_dir)
 
     # ------------------------------------------------------------------ build
-    def build(self, kahan=False) -> DomainSpec:
+    def build(self, kahan=False, nu_elem=None) -> DomainSpec:
+        """Pack the domain.  nu_elem: optional per-element Fourier order (a learned or user
+        Nu field) replacing NU_CONST; each point takes the maximum over its elements."""
         par = self.par
         ex = Exodus.read(self.input_dir / par.get("MODEL_1D_EXODUS_MESH_FILE"))
         self.ex = ex
@@ -183,6 +186,11 @@ class Simulation:
         if nutype.lower() != "constant":
             raise NotImplementedError("NU_TYPE: only 'constant' is built")
         nr0 = 2 * par.get("NU_CONST", int) + 1
+        if nu_elem is not None:
+            # a per-element Nu field (learned or user): point Nu = max over its elements
+            pnu = np.zeros(P, np.int64)
+            np.maximum.at(pnu, e_pts.ravel(), np.repeat(np.asarray(nu_elem, np.int64), 25))
+            nr0 = 2 * pnu + 1
         size_e = np.sqrt(np.abs(ifact.sum(1) / np.maximum(crds[..., 0].mean(1), 1.0)))  # ~ element edge
         spacing = np.full(P, np.inf)
         np.minimum.at(spacing, e_pts.ravel(), np.repeat(size_e / 4.0, 25))
@@ -192,16 +200,50 @@ class Simulation:
         near_axis = np.zeros(P, bool)
         near_axis[e_pts[axial_e].ravel()] = True
         p_nr = np.where((p_nr % 2 == 0) & near_axis, p_nr + 1, p_nr)
+        # volumetric 3-D models (Material::addVolumetric3D) on each element's Nr slices
+        e_nr = p_nr[e_pts].max(1)
+        models = M3D.volumetric_models(par, self._cmt_latlon(), self.R)
+        e3d = np.zeros(E, bool)
+        props3 = {}
+        if models:
+            for nr in np.unique(e_nr):
+                sel = np.nonzero(e_nr == nr)[0]
+                cur, touched = M3D.apply_models(models, {"VP": vp[sel], "VS": vs[sel], "RHO": rho[sel]},
+                                                crds[sel], int(nr), fl[sel])
+                for j in np.nonzero(touched)[0]:
+                    e3d[sel[j]] = True
+                    props3[sel[j]] = {k: v[j] for k, v in cur.items()}
+        self.e3d = e3d
         # point phases, masses (Material::computeElementalMass), coupling normals
         has_s = np.zeros(P, bool)
         has_f = np.zeros(P, bool)
         has_s[e_pts[~fl].ravel()] = True
         has_f[e_pts[fl].ravel()] = True
         kind = np.where(has_s & has_f, POINT_SOLID_FLUID, np.where(has_f, POINT_FLUID, POINT_SOLID)).astype(np.int8)
+        # elements whose mass varies with phi (3-D rho, or 3-D vp in a fluid); the others
+        # add a constant; 3-D masses are resampled onto each point's own Nr
+        # (Material.cpp:215-224, XMath::linearResampling)
+        m3e = [e for e in np.nonzero(e3d)[0] if np.ptp(props3[e]["RHO"], 0).any()
+               or (fl[e] and np.ptp(props3[e]["VP"], 0).any())]
+        m1 = np.ones(E, bool)
+        m1[m3e] = False
         ms = np.zeros(P)
         mf = np.zeros(P)
-        np.add.at(ms, e_pts[~fl].ravel(), (rho[~fl] * ifact[~fl]).ravel())
-        np.add.at(mf, e_pts[fl].ravel(), (ifact[fl] / (rho[fl] * vp[fl] ** 2)).ravel())
+        rho0 = np.array([props3[e]["RHO"][0] if e3d[e] else rho[e] for e in range(E)])
+        vp0 = np.array([props3[e]["VP"][0] if e3d[e] else vp[e] for e in range(E)])
+        sm, fm = m1 & ~fl, m1 & fl
+        np.add.at(ms, e_pts[sm].ravel(), (rho0[sm] * ifact[sm]).ravel())
+        np.add.at(mf, e_pts[fm].ravel(), (ifact[fm] / (rho0[fm] * vp0[fm] ** 2)).ravel())
+        ms3, mf3 = {}, {}
+        for e in m3e:
+            for k in range(25):
+                p = int(e_pts[e, k])
+                rr = M3D.linear_resampling(int(p_nr[p]), props3[e]["RHO"][:, k])
+                if fl[e]:
+                    vv = M3D.linear_resampling(int(p_nr[p]), props3[e]["VP"][:, k])
+                    mf3[p] = mf3.get(p, 0.0) + ifact[e, k] / (rr * vv ** 2)
+                else:
+                    ms3[p] = ms3.get(p, 0.0) + rr * ifact[e, k]
         sfn = np.zeros((P, 3))
         sfside = ex.side.get("solid_fluid_boundary", np.full(E, -1))
         wg, wjw = S.gll()[1], S.glj()[1]
@@ -258,26 +300,27 @@ class Simulation:
         e_mod, e_attm, e_mat, e_att = [], [], [], []
         for e in range(E):
             f = ifact[e]
+            # (nr, 25) for 3-D elements, (1, 25) for 1-D ones
+            vp_e, vs_e, rho_e = ((props3[e]["VP"], props3[e]["VS"], props3[e]["RHO"]) if e3d[e]
+                                 else (vp[e][None, :], vs[e][None, :], rho[e][None, :]))
             if fl[e]:
-                e_mod.append(f / rho[e])
+                e_mod.append((f / rho_e).ravel())
                 e_attm.append(np.zeros(0))
                 e_mat.append(MAT_ACOUSTIC)
                 e_att.append(ATT_NONE)
                 continue
-            lam = rho[e] * (vp[e] ** 2 - 2 * vs[e] ** 2) * f
-            mu = rho[e] * vs[e] ** 2 * f
+            lam = rho_e * (vp_e ** 2 - 2 * vs_e ** 2) * f
+            mu = rho_e * vs_e ** 2 * f
             attm = np.zeros(0)
             if attk != ATT_NONE:
                 A = C = lam + 2 * mu
                 F, L, N = lam, mu, mu
                 kappa, mu_v = ATT.voigt_ti(A, C, F, L, N)
-                qk = mat["QKAPPA"][e][None, :]
-                qm = mat["QMU"][e][None, :]
+                qk = np.broadcast_to(mat["QKAPPA"][e][None, :], lam.shape)
+                qm = np.broadcast_to(mat["QMU"][e][None, :], lam.shape)
                 fac = ATT.att_factors(w, y, fmin, fmax, fref, dt, qk, qm, dokappa)
-                kap2, mu2, dk, dm = ATT.apply_attenuation(kappa[None, :], mu_v[None, :], qk, qm, f, cg4,
-                                                          (fac[3], fac[4]))
-                lam = (kap2 - 2.0 / 3.0 * mu2)[0]
-                mu = mu2[0]
+                lam, mu, dk, dm = ATT.apply_attenuation(kappa, mu_v, qk, qm, f, cg4, (fac[3], fac[4]))
+                lam = lam - 2.0 / 3.0 * mu
                 attm = np.concatenate([dk.ravel(), dm.ravel()])
             e_mod.append(np.stack([lam, mu]).ravel())
             e_attm.append(attm)
@@ -294,17 +337,47 @@ class Simulation:
                 for jp in range(5):
                     if (s_ == 0 and jp == 0) or (s_ == 1 and ip == 4) or (s_ == 2 and jp == 4) or (s_ == 3 and ip == 0):
                         fsurf[e_pts[e, ip * 5 + jp]] = True
+        def pack_mass(has, m1d, m3d):
+            """Point mass rows: 1 value (Mass1D) or Nr values when they vary (Mass3D)."""
+            full = {p: m1d[p] + v for p, v in m3d.items() if np.ptp(m1d[p] + v) > 0}
+            lens = has.astype(np.int64)
+            for p in full:
+                lens[p] = len(full[p])
+            ofs = np.concatenate([[0], np.cumsum(lens)[:-1]])
+            vals = np.zeros(int(lens.sum()))
+            one = has & (lens == 1)
+            tot = m1d.copy()
+            for p, v in m3d.items():
+                if p not in full:
+                    tot[p] += v[0]
+            vals[ofs[one]] = 1.0 / tot[one]
+            for p, v in full.items():
+                vals[ofs[p]:ofs[p] + lens[p]] = 1.0 / v
+            return lens.astype(np.int32), vals.astype(np.float32)
+        p_mslen, p_ms = pack_mass(has_s, ms, ms3)
+        p_mflen, p_mf = pack_mass(has_f, mf, mf3)
+        # coupling rows (SolidFluidCoupling1D / 3D when the fluid mass varies with phi)
         sflen = np.where(kind == POINT_SOLID_FLUID, 1, 0).astype(np.int32)
-        sfrows = sfn[kind == POINT_SOLID_FLUID]
-        mf_sf = mf[kind == POINT_SOLID_FLUID]
+        sfrows, sfirows = [], []
+        for p in np.nonzero(kind == POINT_SOLID_FLUID)[0]:
+            mfp = mf[p] + mf3.get(p, 0.0)
+            if np.ndim(mfp) and np.ptp(mfp) > 0:
+                sflen[p] = len(mfp)
+                rows = np.repeat(sfn[p][None, :], len(mfp), 0)
+                sfrows.append(rows)
+                sfirows.append(rows / mfp[:, None])
+            else:
+                sfrows.append(sfn[p][None, :])
+                sfirows.append(sfn[p][None, :] / float(np.ravel(mfp)[0]))
+        sfrows = np.concatenate(sfrows) if sfrows else np.zeros((0, 3))
+        sfirows = np.concatenate(sfirows) if sfirows else np.zeros((0, 3))
         spec = DomainSpec(
             dt=dt, p_nr=p_nr.astype(np.int32), p_kind=kind, p_axial=p_axial.astype(np.uint8),
             p_fsurf=fsurf.astype(np.uint8),
-            p_mslen=has_s.astype(np.int32), p_ms=(1.0 / ms[has_s]).astype(np.float32),
-            p_mflen=has_f.astype(np.int32), p_mf=(1.0 / mf[has_f]).astype(np.float32),
-            p_sflen=sflen, p_sfn=sfrows.astype(np.float32), p_sfni=(sfrows / mf_sf[:, None]).astype(np.float32),
+            p_mslen=p_mslen, p_ms=p_ms, p_mflen=p_mflen, p_mf=p_mf,
+            p_sflen=sflen, p_sfn=sfrows.astype(np.float32), p_sfni=sfirows.astype(np.float32),
             e_pts=e_pts, e_mat=np.array(e_mat, np.int8), e_axial=axial_e.astype(np.uint8),
-            e_in3d=np.zeros(E, np.uint8), e_geo=geo.astype(np.float32),
+            e_in3d=e3d.astype(np.uint8), e_geo=geo.astype(np.float32),
             e_trig=GEO.trig_tables(theta).transpose(1, 0, 2).astype(np.float32),
             e_mofs=mofs, e_mod=np.concatenate(e_mod).astype(np.float32), e_att=np.array(e_att, np.int8),
             e_aofs=aofs, e_attm=(np.concatenate(e_attm) if e_attm else np.zeros(0)).astype(np.float32),
@@ -318,6 +391,16 @@ class Simulation:
         return spec
 
     # ------------------------------------------------------------------ source
+    def _cmt_latlon(self):
+        """Source latitude/longitude of the CMTSOLUTION (Source.cpp:121-140), needed before
+        the source itself is built to place geographic 3-D anomalies."""
+        vals = {}
+        for line in (self.input_dir / self.par.get("SOURCE_FILE")).read_text().splitlines()[1:]:
+            if ":" in line:
+                k, v = line.split(":", 1)
+                vals[k.strip()] = v.strip()
+        return float(vals["latitude"]), float(vals["longitude"])
+
     def _source(self, spec):
         """CMTSOLUTION (Source.cpp:121-234) -> Earthquake::computeSourceFourier (Earthquake.cpp:20-88)."""
         par = self.par
@@ -492,7 +575,8 @@ class Simulation:
 
 
 def write_inputs(input_dir, mesh_kw=None, nu=2, stf="gauss", hdur=50.0, steps=2000, record_length=None,
-                 n_stations=20, depth_km=100.0, seed=0, attenuation=False, system="source_centered"):
+                 n_stations=20, depth_km=100.0, seed=0, attenuation=False, system="source_centered",
+                 models3d=()):
     """Seeded inputs of the small benchmark configuration: mesh, four parfiles, CMTSOLUTION
     (moment tensor ~ N(0, 1e20 N*m) written in dyn*cm) and STATIONS at uniform distance."""
     from . import mesher
@@ -501,7 +585,9 @@ def write_inputs(input_dir, mesh_kw=None, nu=2, stf="gauss", hdur=50.0, steps=20
     ds = mesher.write_half_disk(d / "mesh.e", seed=seed, **(mesh_kw or {}))
     dt = float(ds["vals_glo_var"][1])
     rl = record_length if record_length is not None else steps * dt
-    (d / "inparam.model").write_text(f"MODEL_1D_EXODUS_MESH_FILE mesh.e\nMODEL_3D_VOLUMETRIC_NUM 0\n"
+    vol = f"MODEL_3D_VOLUMETRIC_NUM {len(models3d)}\n" + \
+        (f"MODEL_3D_VOLUMETRIC_LIST {' '.join(models3d)}\n" if models3d else "")
+    (d / "inparam.model").write_text(f"MODEL_1D_EXODUS_MESH_FILE mesh.e\n{vol}"
                                      f"MODEL_3D_GEOMETRIC_NUM 0\nMODEL_3D_OCEAN_LOAD none\nMODEL_2D_MODE off\n"
                                      f"MODEL_PLOT_SLICES_NUM 0\nATTENUATION {'true' if attenuation else 'false'}\n")
     (d / "inparam.nu").write_text(f"NU_TYPE constant\nNU_CONST {nu}\nNU_WISDOM_LEARN false\n")

@@ -171,6 +171,18 @@ int ax3d_reset(ax3d_domain *d);
 /* Current internal step counter (next step to run, 1-based like Newmark::solve). */
 int32_t ax3d_current_step(const ax3d_domain *d);
 
+/* Nu wisdom (Domain::learnWisdom, Domain.cpp:384-402; SolidPoint::learnWisdom,
+   SolidPoint.cpp:240-272; FluidPoint::learnWisdom, FluidPoint.cpp:209-229).
+   ax3d_set_wisdom_learning: during ax3d_step, learn every `interval` steps (at step index
+   tstep - 1 divisible by interval, as Newmark.cpp:89) with tail-energy cutoff `cutoff`;
+   interval <= 0 switches learning off.  ax3d_learn_wisdom runs one learning pass now.
+   ax3d_get_wisdom writes, per point, the smallest Fourier order holding the tail energy
+   below cutoff^2 of the largest Hilbert norm seen so far (max over components and over
+   the solid and fluid parts, SolidPoint::getNuWisdom). */
+int ax3d_set_wisdom_learning(ax3d_domain *d, int32_t interval, float cutoff);
+int ax3d_learn_wisdom(ax3d_domain *d, float cutoff);
+int ax3d_get_wisdom(ax3d_domain *d, int32_t *nu_wisdom);
+
 /* Time-loop phase timers: the reference's _MEASURE_TIMELOOP timers (Domain.h:111-118,
    reported by Domain::reportCost, Domain.cpp:349-382).  When enabled, ax3d_step brackets
    every phase with CUDA events on the domain's stream.  ax3d_read_timers fills

@@ -222,6 +222,7 @@ struct Oracle {
         for (auto &s : srcs)
             if (elems[s.elem].fluid) throw std::runtime_error("Source || source in fluid element");
         finalized = true;
+        reset_wisdom();
     }
 
     void reset() {
@@ -233,6 +234,7 @@ struct Oracle {
         }
         tstep = 1;
         seis.clear();
+        reset_wisdom();
     }
 
     // ================= FFT (FFTW conventions) =================
@@ -899,6 +901,57 @@ struct Oracle {
         }
     }
 
+    // ---------------- Nu wisdom (SolidPoint.cpp:240-272, FluidPoint.cpp:209-229) ----------------
+    std::vector<Real> wis_max;     // [P][4] (s, phi, z, fluid), -1 initially
+    std::vector<int> wis_nu;       // [P][4], Nu initially
+    int wis_interval = 0;
+    Real wis_cutoff = 0;
+    void reset_wisdom() {
+        wis_max.assign(pts.size() * 4, Real(-1));
+        wis_nu.assign(pts.size() * 4, 0);
+        for (size_t p = 0; p < pts.size(); p++)
+            for (int c = 0; c < 4; c++) wis_nu[p * 4 + c] = pts[p].nu;
+    }
+    // one component: L2 norm, Hilbert norm, smallest order with tail energy <= h2 cutoff^2;
+    // the partial sums run over orders 0, 1, 2, ... (one fixed summation order)
+    static int wisdom_component(const C *u, int stride, int nu, Real cutoff, Real &maxh, int nu_old) {
+        Real l2 = 0;
+        for (int a = 0; a <= nu; a++) l2 += std::norm(u[(size_t)a * stride]);
+        Real h2 = (Real)((double)l2 - .5 * (double)std::norm(u[0]));
+        if (h2 <= maxh) return nu_old;
+        maxh = h2;
+        Real tol = h2 * cutoff * cutoff;
+        Real head = 0;
+        for (int nn = 0; nn < nu; nn++) {
+            head += std::norm(u[(size_t)nn * stride]);
+            if (l2 - head <= tol) return nn;
+        }
+        return nu;
+    }
+    void learn_wisdom(Real cutoff) {  // Domain::learnWisdom (Domain.cpp:384-402)
+        if (wis_max.size() != pts.size() * 4) reset_wisdom();
+        for (size_t p = 0; p < pts.size(); p++) {
+            const Point &pt = pts[p];
+            if (pt.kind != 1)
+                for (int c = 0; c < 3; c++)
+                    wis_nu[p * 4 + c] = wisdom_component(&su[pt.sofs + c], 3, pt.nu, cutoff, wis_max[p * 4 + c],
+                                                         wis_nu[p * 4 + c]);
+            if (pt.kind != 0)
+                wis_nu[p * 4 + 3] = wisdom_component(&fu[pt.fofs], 1, pt.nu, cutoff, wis_max[p * 4 + 3], wis_nu[p * 4 + 3]);
+        }
+    }
+    std::vector<int> get_wisdom() {  // SolidPoint::getNuWisdom / SolidFluidPoint::getNuWisdom
+        if (wis_max.size() != pts.size() * 4) reset_wisdom();
+        std::vector<int> out(pts.size(), 0);
+        for (size_t p = 0; p < pts.size(); p++) {
+            int m = 0;
+            if (pts[p].kind != 1) m = std::max({wis_nu[p * 4], wis_nu[p * 4 + 1], wis_nu[p * 4 + 2]});
+            if (pts[p].kind != 0) m = std::max(m, wis_nu[p * 4 + 3]);
+            out[p] = m;
+        }
+        return out;
+    }
+
     bool stable() const {  // SolidPoint::stable / FluidPoint::stable (allFinite of displ)
         for (auto &v : su)
             if (!std::isfinite((double)v.real()) || !std::isfinite((double)v.imag())) return false;
@@ -915,6 +968,7 @@ struct Oracle {
             compute_stiff();
             couple_solid_fluid();
             record(tstep - 1);
+            if (wis_interval > 0 && (tstep - 1) % wis_interval == 0) learn_wisdom(wis_cutoff);  // Newmark.cpp:89
             if (stab_interval > 0 && tstep % stab_interval == 0 && !stable()) {
                 tstep++;
                 return 4;

@@ -178,6 +178,21 @@ int guard(F f) {
         return 0;                                                                                \
     }                                                                                            \
     int32_t P##current_step(void *d) { return static_cast<P##dom *>(d)->tstep; }                 \
+    int P##set_wisdom_learning(void *dv, int32_t interval, float cutoff) {                       \
+        auto *d = static_cast<P##dom *>(dv);                                                     \
+        d->wis_interval = interval > 0 ? interval : 0;                                           \
+        d->wis_cutoff = (REAL)cutoff;                                                            \
+        return 0;                                                                                \
+    }                                                                                            \
+    int P##learn_wisdom(void *d, float cutoff) {                                                 \
+        static_cast<P##dom *>(d)->learn_wisdom((REAL)cutoff);                                    \
+        return 0;                                                                                \
+    }                                                                                            \
+    int P##get_wisdom(void *d, int32_t *out) {                                                   \
+        auto v = static_cast<P##dom *>(d)->get_wisdom();                                         \
+        std::copy(v.begin(), v.end(), out);                                                      \
+        return 0;                                                                                \
+    }                                                                                            \
     int P##destroy(void *d) {                                                                    \
         delete static_cast<P##dom *>(d);                                                         \
         return 0;                                                                                \

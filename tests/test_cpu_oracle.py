@@ -127,3 +127,22 @@ def test_capi_rejects_bad_input_without_gpu():
     buf = ctypes.create_string_buffer(256)
     lib.ax3d_last_error(buf, 256)
     assert b"nPol" in buf.value
+
+
+def test_oracle_wisdom_labels():
+    """Nu wisdom: a field with energy only in orders <= 3 learns Nu <= 3 everywhere."""
+    OD = _oracle()
+    spec = synth.annulus_domain(nu=8, source=False, n_receivers=0)
+    d = OD(spec)
+    rng = np.random.default_rng(0)
+    so, _ = spec.point_offsets()
+    u = np.zeros(d.nsolid, complex)
+    for p in range(spec.n_points):
+        na = spec.p_nr[p] // 2 + 1
+        blk = np.zeros((na, 3), complex)
+        blk[:4] = rng.normal(size=(4, 3)) + 1j * rng.normal(size=(4, 3))
+        u[so[p]:so[p] + 3 * na] = blk.ravel()
+    d.set("displ", "solid", u)
+    d.learn_wisdom(1e-3)
+    w = d.get_wisdom()
+    assert w.max() <= 3 and w.min() >= 0 and (w == 3).mean() > 0.5

@@ -117,3 +117,16 @@ def test_unstable_is_reported(ax3d_lib):
     with pytest.raises(Ax3dError) as ei:
         g.step(4)
     assert ei.value.code == 4
+
+
+def test_wisdom_learning_matches_oracle(ax3d_lib):
+    """Nu wisdom learned during the time loop (every 5 steps), GPU vs oracle."""
+    spec, g, o, _ = _pair("ti3d_cg4", stf_len=30)
+    su, _ = synth.random_fields(spec, seed=13, scale=1e-6, decay=2.5)
+    for d in (g, o):
+        d.set("displ", "solid", su)
+        d.set_wisdom_learning(5, 1e-2)
+        d.step(30)
+    wg, wo = g.get_wisdom(), o.get_wisdom()
+    assert wg.shape == wo.shape == (spec.n_points,)
+    assert (np.abs(wg - wo) <= 1).all() and (wg != wo).mean() <= 0.01

@@ -138,3 +138,85 @@ def test_ensemble_gpu_graph_matches_oracle(tmp_path_factory, ax3d_lib):
     o.step(120)
     a, b = g.seismograms(0, 120), o.seismograms(0, 120)
     assert np.linalg.norm(a - b) <= 1e-5 * np.linalg.norm(b)
+
+
+MODELS_3D = ("bubble$RHO$Ref1D$0.05$500$2891$20$40$true$true",   # straddles the CMB
+             "bubble$VP$Ref3D$-0.05$500$2891$20$40$true$true",
+             "gaussian_random$VS$Ref1D$0.04$500$200$7")
+
+
+@pytest.fixture(scope="module")
+def inputs_3d(tmp_path_factory):
+    d = tmp_path_factory.mktemp("c3d") / "input"
+    return solver.write_inputs(d, mesh_kw=SMALL_MESH, steps=120, hdur=20.0, n_stations=6, seed=3, nu=4,
+                               models3d=MODELS_3D)
+
+
+def test_volumetric_3d_build(inputs_3d):
+    """3-D elements, Mass3D points (solid and fluid) and 3-D solid-fluid coupling appear; a
+    gaussian_random model acts on solid elements only (no fluid flag)."""
+    sim = solver.Simulation(inputs_3d)
+    spec = sim.build()
+    assert spec.e_in3d[~sim.fluid].all()
+    assert spec.e_in3d[sim.fluid].any() and not spec.e_in3d[sim.fluid].all()
+    assert (spec.p_mslen > 1).any() and (spec.p_mflen > 1).any() and (spec.p_sflen > 1).any()
+    nr = spec.element_nr()
+    sizes = np.diff(np.append(spec.e_mofs, len(spec.e_mod)))
+    # moduli rows: [2][nr][25] solid isotropic, [nr][25] fluid (3-D) or [25] (1-D)
+    want = np.where(sim.fluid, np.where(spec.e_in3d > 0, nr, 1) * 25, 2 * nr * 25)
+    assert (sizes == want).all()
+
+
+def test_volumetric_3d_models_unit():
+    from axisem3d_gb300 import model3d as M3D
+    R = 6371e3
+    b = M3D.Bubble("VS Ref1D 0.1 100 500 30 60 true".split(), (0.0, 0.0), R)
+    v, inr = b.evaluate(b.center[None, :])
+    assert inr[0] and v[0] == pytest.approx(0.1)
+    far = b.center * 0.5
+    assert not b.evaluate(far[None, :])[1][0]
+    g = M3D.GaussianRandom("VP Ref1D 0.04 500 200 1".split(), R)
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal((20000, 3))
+    x = x / np.linalg.norm(x, axis=1, keepdims=True) * rng.uniform(3.5e6, 6.3e6, (20000, 1))
+    val = g.evaluate(x)[0]
+    assert abs(val.mean()) < 0.01 and 0.02 < val.std() < 0.06
+    with pytest.raises(ValueError):
+        M3D.Bubble("VQ Ref1D 0.1 100 500 30 60".split(), (0.0, 0.0), R)
+    ring = np.array([1.0, 2.0, 3.0])
+    np.testing.assert_allclose(M3D.linear_resampling(6, ring), [1.0, 1.5, 2.0, 2.5, 3.0, 2.0])
+
+
+def test_unknown_volumetric_model_raises(tmp_path):
+    d = solver.write_inputs(tmp_path / "input", mesh_kw=SMALL_MESH, steps=10, models3d=("s20rts",))
+    with pytest.raises(NotImplementedError):
+        solver.Simulation(d).build()
+
+
+def test_per_element_nu_field(small_inputs):
+    """A per-element Nu field sets each point's Nr = 2 max(Nu of its elements) + 1 (capped
+    by the point's circumference and odd near the axis)."""
+    sim = solver.Simulation(small_inputs)
+    spec0 = sim.build()
+    E = len(spec0.e_pts)
+    nu = np.where(np.arange(E) % 2 == 0, 1, 3)
+    spec = sim.build(nu_elem=nu)
+    pnu = np.zeros(spec.n_points, int)
+    np.maximum.at(pnu, spec.e_pts.ravel(), np.repeat(nu, 25))
+    assert (spec.p_nr <= 2 * pnu + 2).all() and (spec.p_nr != spec0.p_nr).any()
+
+
+@pytest.mark.gpu
+def test_full_solver_3d_gpu_matches_oracle(inputs_3d, ax3d_lib):
+    """3-D model: 3-D solid/fluid elements, Mass3D points and 3-D coupling through the loop."""
+    from oracle.oracle_py import OracleDomain
+    from axisem3d_gb300.capi import Ax3dDomain
+    sim = solver.Simulation(inputs_3d)
+    spec = sim.build()
+    g, o = Ax3dDomain(spec), OracleDomain(spec)
+    g.step(120)
+    o.step(120)
+    a, b = g.seismograms(0, 120), o.seismograms(0, 120)
+    assert np.linalg.norm(a - b) <= 1e-5 * np.linalg.norm(b)
+    x, y = g.get("displ", "fluid"), o.get("displ", "fluid")
+    assert np.linalg.norm(x - y) <= 1e-5 * np.linalg.norm(y)
