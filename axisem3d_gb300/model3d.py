@@ -22,6 +22,7 @@ PROP is VP, VS or RHO (VP/VS act on both the vertical and horizontal velocities)
 from __future__ import annotations
 
 import math
+import os
 
 import numpy as np
 
@@ -115,12 +116,30 @@ class GaussianRandom(Model3D):
         if self.ref == 0:
             raise ValueError("Volumetric3D_gaussian_random::initialize || reference type must be relative")
 
+    def _eval_flat(self, x):
+        r = np.linalg.norm(x, axis=-1)
+        n = x / np.maximum(r, 1e-9)[:, None]
+        arg = r[:, None] * self.kr + self.R * (n @ self.kl.T) + self.ph
+        return self.rms * math.sqrt(2.0 / self.modes) * np.cos(arg).sum(-1)
+
     def evaluate(self, xyz):
-        r = np.linalg.norm(xyz, axis=-1)
-        n = xyz / np.maximum(r, 1e-9)[..., None]
-        arg = r[..., None] * self.kr + self.R * (n @ self.kl.T) + self.ph
-        val = self.rms * math.sqrt(2.0 / self.modes) * np.cos(arg).sum(-1)
-        return val, np.ones(r.shape, bool)
+        shape = xyz.shape[:-1]
+        flat = np.ascontiguousarray(xyz, np.float64).reshape(-1, 3)
+        out = np.empty(len(flat))
+        chunk = 1 << 15
+        spans = [(i, min(i + chunk, len(flat))) for i in range(0, len(flat), chunk)]
+
+        def work(span):
+            out[span[0]:span[1]] = self._eval_flat(flat[span[0]:span[1]])
+
+        if len(spans) > 4:   # numpy's cos releases the GIL: threads share the cores
+            from concurrent.futures import ThreadPoolExecutor
+            with ThreadPoolExecutor(min(16, os.cpu_count() or 1)) as ex:
+                list(ex.map(work, spans))
+        else:
+            for sp in spans:
+                work(sp)
+        return out.reshape(shape), np.ones(shape, bool)
 
 
 def volumetric_models(par, src_latlon, R):
@@ -152,30 +171,37 @@ def apply_models(models, props1d, crds, nr, fluid):
     fluid (n,) bool.  Slice alpha sits at phi = 2 pi alpha / nr.  Returns ({prop: (n, nr, 25)},
     touched (n,) bool): elements with any point inside any model's range."""
     phi = 2 * math.pi * np.arange(nr) / nr
-    s, z = crds[..., 0], crds[..., 1]
-    xyz = np.stack([s[:, None, :] * np.cos(phi)[None, :, None], s[:, None, :] * np.sin(phi)[None, :, None],
-                    np.broadcast_to(z[:, None, :], (len(s), nr, 25))], -1)
-    cur = {k: np.repeat(v[:, None, :], nr, 1).astype(float) for k, v in props1d.items()}
-    touched = np.zeros(len(s), bool)
-    for m in models:
-        val, inr = m.evaluate(xyz)
-        if not m.fluid:
-            inr = inr & ~fluid[:, None, None]
-        if not inr.any():
-            continue
-        touched |= inr.any((1, 2))
-        x1 = props1d[m.prop][:, None, :]
-        x = cur[m.prop]
-        if m.ref == 0:
-            new = np.broadcast_to(val, x.shape)
-        elif m.ref == 1:
-            new = x1 * (1.0 + val)
-        elif m.ref == 2:
-            new = x * (1.0 + val)
-        else:
-            new = (x - x1) * (1.0 + val) + x1
-        cur[m.prop] = np.where(inr, new, x)
-    return cur, touched
+    n = len(crds)
+    out = {k: np.empty((n, nr, 25), np.float32) for k in props1d}
+    touched = np.zeros(n, bool)
+    step = max(1, (1 << 21) // (nr * 25))   # ~2M samples per chunk
+    for a in range(0, n, step):
+        b = min(n, a + step)
+        s, z = crds[a:b, :, 0], crds[a:b, :, 1]
+        xyz = np.stack([s[:, None, :] * np.cos(phi)[None, :, None], s[:, None, :] * np.sin(phi)[None, :, None],
+                        np.broadcast_to(z[:, None, :], (b - a, nr, 25))], -1)
+        cur = {k: np.repeat(v[a:b, None, :], nr, 1).astype(float) for k, v in props1d.items()}
+        for m in models:
+            val, inr = m.evaluate(xyz)
+            if not m.fluid:
+                inr = inr & ~fluid[a:b, None, None]
+            if not inr.any():
+                continue
+            touched[a:b] |= inr.any((1, 2))
+            x1 = props1d[m.prop][a:b, None, :]
+            x = cur[m.prop]
+            if m.ref == 0:
+                new = np.broadcast_to(val, x.shape)
+            elif m.ref == 1:
+                new = x1 * (1.0 + val)
+            elif m.ref == 2:
+                new = x * (1.0 + val)
+            else:
+                new = (x - x1) * (1.0 + val) + x1
+            cur[m.prop] = np.where(inr, new, x)
+        for k in out:
+            out[k][a:b] = cur[k]
+    return out, touched
 
 
 def linear_resampling(new_size, original):

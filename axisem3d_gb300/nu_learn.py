@@ -1,0 +1,214 @@
+"""Learned Fourier order: element features, wisdom labels, GPU training of the Nu network,
+and the learned-Nu vs full-Nu experiment.
+
+The reference learns a point-wise Nu field ("wisdom") from the spectra of a full-Nu run
+and reuses it in later runs of the same model (SolidPoint.cpp:240-272, NuWisdom.cpp:19-86).
+Here a network trained on the wisdom of full-Nu runs of many seeded 3-D models predicts
+each element's Nu from local model features for a model it has not seen, so the reduced
+run needs no full-Nu run first; a full-Nu run remains the judge and the fallback.
+
+Features (16 per element, at the element's centre GLL point):
+  0 r / R            1 epicentral distance / pi     2 distance to the axis s / R
+  3 period / 100 s   4 element size / 100 km        5 Vp / 10 km/s     6 Vs / 10 km/s
+  7 source depth / 1000 km
+  8-15 azimuthal power of the local dlnVs perturbation on the ring through the centre,
+       orders [1,2), [2,4), ..., [128,256), as (log10(P + 1e-12) + 12) / 12
+Target: log2(1 + Nu) / log2(1 + Nu_full), Nu = max wisdom Nu over the element's points.
+"""
+from __future__ import annotations
+
+import json
+import math
+import time
+from pathlib import Path
+
+import numpy as np
+
+from . import solver
+
+NFEAT = 16
+
+
+def model_strings(seed: int, rms: float = 0.04, lat_km: float = 500.0, rad_km: float = 200.0):
+    """Seeded Gaussian-random dlnVs and dlnVp fields (independent seeds), as list entries."""
+    return (f"gaussian_random$VS$Ref1D${rms}${lat_km}${rad_km}${seed}",
+            f"gaussian_random$VP$Ref1D${rms}${lat_km}${rad_km}${seed + 7919}")
+
+
+def write_case(d, seed, nu_full, steps, mesh_kw=None, n_stations=20):
+    return solver.write_inputs(d, mesh_kw=mesh_kw, nu=nu_full, steps=steps, n_stations=n_stations, seed=0,
+                               models3d=model_strings(seed), lucky=True)
+
+
+def ring_bands(models, s, z, nphi=512):
+    """Band powers (8 octaves of orders 1..255) of the summed dlnVs of `models` on the ring
+    of radius s at height z, per element; (E, 8)."""
+    E = len(s)
+    out = np.zeros((E, 8))
+    phi = 2 * np.pi * np.arange(nphi) / nphi
+    vs_models = [m for m in models if m.prop == "VS" and m.ref != 0]
+    if not vs_models:
+        return out
+    step = 256
+    for a in range(0, E, step):
+        b = min(E, a + step)
+        xyz = np.stack([s[a:b, None] * np.cos(phi), s[a:b, None] * np.sin(phi),
+                        np.broadcast_to(z[a:b, None], (b - a, nphi))], -1)
+        d = np.zeros((b - a, nphi))
+        for m in vs_models:
+            val, inr = m.evaluate(xyz)
+            d += np.where(inr, val, 0.0)
+        P = np.abs(np.fft.rfft(d, axis=1) / nphi) ** 2
+        for i in range(8):
+            out[a:b, i] = P[:, 2 ** i:2 ** (i + 1)].sum(1)
+    return out
+
+
+def element_features(sim, period: float = 50.0) -> np.ndarray:
+    c = sim.crds[:, 12]
+    s, z = c[:, 0], c[:, 1]
+    r = np.hypot(s, z)
+    size = np.hypot(*(sim.crds[:, 24] - sim.crds[:, 0]).T) / np.sqrt(2.0)
+    f = np.zeros((len(s), NFEAT), np.float32)
+    f[:, 0] = r / sim.R
+    f[:, 1] = np.arctan2(s, z) / np.pi
+    f[:, 2] = s / sim.R
+    f[:, 3] = period / 100.0
+    f[:, 4] = size / 100e3
+    f[:, 5] = sim.vp_e / 1e4
+    f[:, 6] = sim.vs_e / 1e4
+    f[:, 7] = sim.src_dep / 1e6
+    f[:, 8:] = (np.log10(ring_bands(sim.models, s, z) + 1e-12) + 12.0) / 12.0
+    return f
+
+
+def element_labels(spec, wisdom) -> np.ndarray:
+    return np.asarray(wisdom)[spec.e_pts].max(1)
+
+
+def encode(nu, nu_full):
+    return (np.log2(1.0 + np.asarray(nu, np.float64)) / math.log2(1.0 + nu_full)).astype(np.float32)
+
+
+def decode(y, nu_full, margin=0.0):
+    nu = (1.0 + nu_full) ** np.asarray(y, np.float64) - 1.0
+    return np.clip(np.ceil(nu * (1.0 + margin)), 1, nu_full).astype(np.int64)
+
+
+def calibrate_margin(y_pred, labels, nu_full, quantile=0.99):
+    """Smallest relative margin with which `quantile` of the elements are not under-predicted."""
+    raw = np.maximum((1.0 + nu_full) ** np.asarray(y_pred, np.float64) - 1.0, 0.5)
+    ratio = np.asarray(labels, np.float64) / raw
+    return float(max(0.0, np.quantile(ratio, quantile) - 1.0))
+
+
+def run(spec, steps, learn=None):
+    """Time-to-seismogram of one GPU run (first step to seismograms on the host).
+    learn = (interval, epsilon) turns the wisdom learner on.  Returns (seis, seconds,
+    wisdom or None, unique-point updates per step)."""
+    import torch
+    from .capi import Ax3dDomain
+    dom = Ax3dDomain(spec)
+    if learn:
+        dom.set_wisdom_learning(int(learn[0]), float(learn[1]))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    dom.step(steps)
+    seis = dom.seismograms(0, steps)
+    t = time.perf_counter() - t0
+    wis = dom.get_wisdom() if learn else None
+    dom.close()
+    return seis, t, wis, int(np.asarray(spec.p_nr, np.int64).sum())
+
+
+def experiment(work, n_train=64, n_test=16, nu_full=64, steps=600, epochs=200, batch=4096, lr=2e-3,
+               eps=1e-3, interval=5, mesh_kw=None, out=None, log=print):
+    """Train on the wisdom of n_train full-Nu runs, judge n_test held-out models.  Returns
+    the summary dict (also written to out/summary.json with the parameters in out/nu_mlp.npz)."""
+    from .nu_mlp import NuMLP
+    work = Path(work)
+    X, Y, pre = [], [], []
+    t_train_runs = 0.0
+    for i in range(n_train):
+        d = write_case(work / f"train{i}", 1000 + i, nu_full, steps, mesh_kw)
+        t0 = time.perf_counter()
+        sim = solver.Simulation(d)
+        spec = sim.build()
+        pre.append(time.perf_counter() - t0)
+        _, t, wis, _ = run(spec, steps, learn=(interval, eps))
+        t_train_runs += t
+        X.append(element_features(sim))
+        Y.append(encode(element_labels(spec, wis), nu_full))
+        log(f"train {i}: {t:.2f} s, mean label Nu {np.mean(element_labels(spec, wis)):.1f}")
+    X, Y = np.concatenate(X), np.concatenate(Y)
+    net = NuMLP(max_batch=batch, seed=0)
+    t0 = time.perf_counter()
+    hist = net.fit(X, Y, epochs=epochs, batch=batch, lr=lr, lr_final=lr * 0.05)
+    t_fit = time.perf_counter() - t0
+    ytr = net.forward(X).cpu().numpy()
+    labels_tr = np.round((1.0 + nu_full) ** Y.astype(np.float64) - 1.0)
+    margin = calibrate_margin(ytr, labels_tr, nu_full)
+    log(f"fit {t_fit:.1f} s, loss {hist[0]:.4g} -> {hist[-1]:.4g}, margin {margin:.3f}")
+    tests = []
+    seis_l_all, specs_l = [], []
+    for i in range(n_test):
+        d = write_case(work / f"test{i}", 5000 + i, nu_full, steps, mesh_kw)
+        sim = solver.Simulation(d)
+        spec_f = sim.build()
+        seis_f, t_f, wis, upd_f = run(spec_f, steps, learn=(interval, eps))
+        x = element_features(sim)
+        y = net.forward(x).cpu().numpy()
+        nu_e = decode(y, nu_full, margin)
+        spec_l = sim.build(nu_elem=nu_e)
+        seis_l, t_l, _, upd_l = run(spec_l, steps)
+        mis = float(np.linalg.norm(seis_l - seis_f) / np.linalg.norm(seis_f))
+        # the reference's route without a network: reuse the wisdom of this model's own
+        # full run (which must be paid first)
+        spec_w = sim.build(nu_elem=np.maximum(element_labels(spec_f, wis), 1))
+        seis_w, t_w, _, upd_w = run(spec_w, steps)
+        mis_w = float(np.linalg.norm(seis_w - seis_f) / np.linalg.norm(seis_f))
+        tests.append(dict(seed=5000 + i, misfit=mis, t_full=t_f, t_learned=t_l, speedup=t_f / t_l,
+                          upd_full=upd_f, upd_learned=upd_l, misfit_wisdom=mis_w, t_wisdom=t_w,
+                          mean_nu_pred=float(nu_e.mean()), mean_nu_label=float(element_labels(spec_f, wis).mean())))
+        specs_l.append(spec_l)
+        seis_l_all.append(seis_l)
+        log(f"test {i}: misfit {mis:.4f} (wisdom {mis_w:.4f}), full {t_f:.2f} s, learned {t_l:.2f} s")
+    # all held-out learned-Nu runs batched into one domain
+    from . import ensemble
+    big, info = ensemble.concat(specs_l)
+    seis_b, t_b, _, upd_b = run(big, steps)
+    parts = ensemble.split_seismograms(seis_b, info)
+    mis_b = max(float(np.linalg.norm(p - s) / np.linalg.norm(s)) for p, s in zip(parts, seis_l_all))
+    t_full_sum = sum(t["t_full"] for t in tests)
+    summary = dict(
+        n_train=n_train, n_test=n_test, nu_full=nu_full, steps=steps, elements=int(len(specs_l[0].e_pts)),
+        epochs=epochs, batch=batch, fit_seconds=t_fit, train_runs_seconds=t_train_runs,
+        preloop_seconds_mean=float(np.mean(pre)), loss_first=float(hist[0]), loss_last=float(hist[-1]),
+        margin=margin, tests=tests,
+        misfit_max=max(t["misfit"] for t in tests), misfit_mean=float(np.mean([t["misfit"] for t in tests])),
+        speedup_mean=float(np.mean([t["speedup"] for t in tests])),
+        batched_seconds=t_b, batched_vs_sequential_full=t_full_sum / t_b,
+        batched_vs_sequential_learned=sum(t["t_learned"] for t in tests) / t_b,
+        batched_split_misfit_max=mis_b)
+    if out:
+        out = Path(out)
+        out.mkdir(parents=True, exist_ok=True)
+        (out / "summary.json").write_text(json.dumps(summary, indent=1))
+        np.savez(out / "nu_mlp.npz", params=net.get_params(), nu_full=nu_full, margin=margin)
+    net.close()
+    return summary
+
+
+if __name__ == "__main__":
+    import argparse
+    ap = argparse.ArgumentParser(description="learned-Nu experiment")
+    ap.add_argument("--work", default="/tmp/ax3d_nu_learn")
+    ap.add_argument("--out", default="nu_learn_out")
+    ap.add_argument("--train", type=int, default=64)
+    ap.add_argument("--test", type=int, default=16)
+    ap.add_argument("--nu", type=int, default=64)
+    ap.add_argument("--steps", type=int, default=600)
+    ap.add_argument("--epochs", type=int, default=200)
+    a = ap.parse_args()
+    s = experiment(a.work, a.train, a.test, a.nu, a.steps, a.epochs, out=a.out)
+    print(json.dumps({k: v for k, v in s.items() if k != "tests"}))

@@ -111,6 +111,45 @@ class Exodus:
                       ev["element_type"].astype(int), ev["fluid"] > 0.5, ev.get("dt", np.zeros(E)), nodal, side, glob)
 
 
+def _flag(par, key):
+    try:
+        return par.get(key, bool)
+    except KeyError:
+        return False
+
+
+def is_lucky(n: int, force_odd: bool) -> bool:
+    """PreloopFFTW::isLuckyNumber (PreloopFFTW.cpp:59-99): FFT-friendly ring sizes, with
+    prime factors <= 13, at most one factor 11 or 13, odd when forced, even above 10."""
+    if force_odd and n % 2 == 0:
+        return False
+    if not force_odd and n % 2 and n > 10:
+        return False
+    m = n
+    for p in (2, 3, 5, 7, 11, 13):
+        while m % p == 0:
+            m //= p
+    if m != 1:
+        return False
+    e = f = 0
+    m = n
+    while m % 11 == 0:
+        m //= 11
+        e += 1
+    m = n
+    while m % 13 == 0:
+        m //= 13
+        f += 1
+    return e + f <= 1
+
+
+def next_lucky(n: int, force_odd: bool) -> int:
+    """PreloopFFTW::nextLuckyNumber (PreloopFFTW.cpp:101-109)."""
+    while not is_lucky(n, force_odd):
+        n += 1
+    return n
+
+
 def _lagrange(x, nodes):
     """XMath::interpLagrange: basis values of the Lagrange polynomials on nodes at x."""
     out = np.ones(len(nodes))
@@ -199,7 +238,10 @@ class Simulation:
         p_axial = np.abs(pcrd[:, 0]) < 1e-6
         near_axis = np.zeros(P, bool)
         near_axis[e_pts[axial_e].ravel()] = True
-        p_nr = np.where((p_nr % 2 == 0) & near_axis, p_nr + 1, p_nr)
+        force_odd = (p_nr % 2 == 0) & near_axis
+        p_nr = np.where(force_odd, p_nr + 1, p_nr)
+        if _flag(par, "FFTW_LUCKY_NUMBER"):
+            p_nr = np.array([next_lucky(int(n), bool(f)) for n, f in zip(p_nr, force_odd)])
         # volumetric 3-D models (Material::addVolumetric3D) on each element's Nr slices
         e_nr = p_nr[e_pts].max(1)
         models = M3D.volumetric_models(par, self._cmt_latlon(), self.R)
@@ -213,7 +255,8 @@ class Simulation:
                 for j in np.nonzero(touched)[0]:
                     e3d[sel[j]] = True
                     props3[sel[j]] = {k: v[j] for k, v in cur.items()}
-        self.e3d = e3d
+        self.e3d, self.models = e3d, models
+        self.vp_e, self.vs_e = vp.mean(1), vs.mean(1)
         # point phases, masses (Material::computeElementalMass), coupling normals
         has_s = np.zeros(P, bool)
         has_f = np.zeros(P, bool)
@@ -576,7 +619,7 @@ class Simulation:
 
 def write_inputs(input_dir, mesh_kw=None, nu=2, stf="gauss", hdur=50.0, steps=2000, record_length=None,
                  n_stations=20, depth_km=100.0, seed=0, attenuation=False, system="source_centered",
-                 models3d=()):
+                 models3d=(), lucky=False):
     """Seeded inputs of the small benchmark configuration: mesh, four parfiles, CMTSOLUTION
     (moment tensor ~ N(0, 1e20 N*m) written in dyn*cm) and STATIONS at uniform distance."""
     from . import mesher
@@ -600,7 +643,8 @@ def write_inputs(input_dir, mesh_kw=None, nu=2, stf="gauss", hdur=50.0, steps=20
     (d / "inparam.advanced").write_text(
         f"ATTENUATION_CG4 true\nATTENUATION_SPECFEM_LEGACY false\nATTENUATION_QKAPPA true\n"
         f"OPTION_VERBOSE_LEVEL essential\nOPTION_STABILITY_INTERVAL 100\nOPTION_LOOP_INFO_INTERVAL 1000\n"
-        f"DEVELOP_MAX_TIME_STEPS {steps}\nDEVELOP_NON_SOURCE_MODE false\nFFTW_LUCKY_NUMBER false\n")
+        f"DEVELOP_MAX_TIME_STEPS {steps}\nDEVELOP_NON_SOURCE_MODE false\n"
+        f"FFTW_LUCKY_NUMBER {'true' if lucky else 'false'}\n")
     rng = np.random.default_rng(seed)
     m = rng.normal(0.0, 1e20, 6) * 1e7  # N*m -> dyn*cm (Source.cpp:171-177)
     names = ["Mrr", "Mtt", "Mpp", "Mrt", "Mrp", "Mtp"]

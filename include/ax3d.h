@@ -236,6 +236,42 @@ int ax3d_compute_stiff_iso1d_noalloc(int32_t nelem, int32_t nu, const int32_t *d
                                      const float *d_displ, float *d_stiff, const double *g_gll,
                                      const double *g_glj, void *stream);
 
+/* ---- Learned Fourier order: the Nu network ------------------------------------------
+   No counterpart in the reference, whose Fourier-order field comes from NU_TYPE rules or
+   from a wisdom file of an earlier run (NuWisdom.cpp:19-86, Domain.cpp:384-440).  A fixed
+   multilayer perceptron maps AX3D_MLP_NIN per-element features to one value:
+     h1 = gelu(W1 x + b1), h2 = gelu(W2 h1 + b2), h3 = gelu(W3 h2 + b3), y = w4 . h3 + b4
+   with AX3D_MLP_NHID hidden units and gelu(z) = z Phi(z) (erf form).  Precision: weights,
+   the features and the hidden activations are BF16 (round to nearest even), products are
+   accumulated in FP32, biases and y are FP32; parameters are kept as an FP32 master copy
+   that Adam (beta1 0.9, beta2 0.999, eps 1e-8) updates.  Loss: mean squared error over
+   the n samples of a call.  Gradients are summed in a fixed order (per 64-sample tile,
+   then over tiles), so repeated calls give identical bits.
+   Parameter vector (FP32, AX3D_MLP_NPARAM values): W1 [128][16], b1 [128], W2 [128][128],
+   b2 [128], W3 [128][128], b3 [128], w4 [128], b4 [1]  (W[j][k]: output j, input k).
+   Device pointers are the caller's (for example torch tensors); calls run asynchronously
+   on `stream` (a cudaStream_t, NULL = default stream). */
+#define AX3D_MLP_NIN 16
+#define AX3D_MLP_NHID 128
+#define AX3D_MLP_NPARAM 35329
+typedef struct ax3d_mlp ax3d_mlp;
+/* max_batch: the largest n of a gradient / training call (inference takes any n). */
+int ax3d_mlp_create(int32_t max_batch, int32_t device, ax3d_mlp **out);
+/* Copies AX3D_MLP_NPARAM host values in (and resets Adam's moments and step count). */
+int ax3d_mlp_set_params(ax3d_mlp *m, const float *params, int64_t n);
+int ax3d_mlp_get_params(ax3d_mlp *m, float *params, int64_t n);
+/* d_x [n][16] FP32 features -> d_y [n] FP32. */
+int ax3d_mlp_forward(ax3d_mlp *m, const float *d_x, int32_t n, float *d_y, void *stream);
+/* Gradient of the loss w.r.t. the parameters into d_grad [AX3D_MLP_NPARAM] (FP32) and
+   the loss into d_loss [1]; no update.  d_t [n] targets. */
+int ax3d_mlp_gradient(ax3d_mlp *m, const float *d_x, const float *d_t, int32_t n, float *d_grad,
+                      float *d_loss, void *stream);
+/* One Adam step on the mini-batch (d_x, d_t) with learning rate lr; the batch loss
+   (before the update) goes to d_loss [1] when d_loss is not NULL. */
+int ax3d_mlp_train_step(ax3d_mlp *m, const float *d_x, const float *d_t, int32_t n, float lr,
+                        float *d_loss, void *stream);
+int ax3d_mlp_destroy(ax3d_mlp *m);
+
 /* Text of the last error on this thread (always NUL terminated); returns its length. */
 size_t ax3d_last_error(char *buf, size_t len);
 
