@@ -289,7 +289,220 @@ __device__ __forceinline__ void c2r_task(const float2 *__restrict__ tw, const fl
     }
 }
 
+// ---- mixed-radix FFT for ring sizes whose prime factors are all <= 13 -----------------
+// (the FFT-friendly "lucky" sizes, PreloopFFTW.cpp:59-109).  Two real columns (2s, 2s+1)
+// travel as one complex sequence z = x_2s + i x_2s+1; a self-sorting (Stockham) pass per
+// radix, ping-ponging between the sample buffer X (viewed as complex [nr][SX/2]) and the
+// order buffer F (viewed as complex [nr][ncolg/2]), one thread per (butterfly, sequence).
+// Twiddles w^m come from the exact table; no recurrence.
+
+constexpr int FFT_MIN = 16;   // below this the direct transform is as fast
+
+// n / d for n < 2^32 by multiply-high (round-up method of Granlund and Montgomery)
+struct FDiv {
+    uint32_t m, s, d;
+};
+__device__ __forceinline__ FDiv make_fdiv(uint32_t d) {
+    uint32_t s = 0;
+    while ((1u << s) < d) s++;
+    const uint64_t m = ((1ull << 32) * ((1ull << s) - d)) / d + 1;
+    return FDiv{(uint32_t)m, s, d};
+}
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FDiv &f) {
+    if (f.d == 1) return n;
+    const uint32_t t = __umulhi(n, f.m);
+    return (t + ((n - t) >> 1)) >> (f.s - 1);
+}
+
+// true when every prime factor of n is at most 13
+__host__ __device__ inline bool fft_size_ok(int n) {
+    for (int p = 2; p <= 13; p++)
+        while (n % p == 0) n /= p;
+    return n == 1;
+}
+
+// v <- DFT_R(v) with e^{+2 pi i rk/R} (inv) or e^{-2 pi i rk/R}; cq/sq = cos/sin(2 pi q/R)
+template <int R>
+__device__ __forceinline__ void butterfly(float2 (&v)[R], bool inv, const float *cq, const float *sq) {
+    if constexpr (R == 2) {
+        const float2 a = v[0], b = v[1];
+        v[0] = cadd(a, b);
+        v[1] = make_float2(a.x - b.x, a.y - b.y);
+    } else if constexpr (R == 4) {
+        const float2 t0 = cadd(v[0], v[2]), t1 = make_float2(v[0].x - v[2].x, v[0].y - v[2].y);
+        const float2 t2 = cadd(v[1], v[3]);
+        const float2 d = make_float2(v[1].x - v[3].x, v[1].y - v[3].y);
+        const float2 t3 = inv ? make_float2(-d.y, d.x) : make_float2(d.y, -d.x);  // +-i d
+        v[0] = cadd(t0, t2);
+        v[2] = make_float2(t0.x - t2.x, t0.y - t2.y);
+        v[1] = cadd(t1, t3);
+        v[3] = make_float2(t1.x - t3.x, t1.y - t3.y);
+    } else {
+        // odd R: out_k = v0 + sum_r (v_r + v_{R-r}) cos(2 pi rk/R) +- i (v_r - v_{R-r}) sin(..)
+        constexpr int H = (R - 1) / 2;
+        float2 sp[H], sm[H];
+        float2 out0 = v[0];
+#pragma unroll
+        for (int r = 1; r <= H; r++) {
+            sp[r - 1] = cadd(v[r], v[R - r]);
+            sm[r - 1] = make_float2(v[r].x - v[R - r].x, v[r].y - v[R - r].y);
+            out0 = cadd(out0, sp[r - 1]);
+        }
+        const float sg = inv ? 1.f : -1.f;
+        float2 o[R];
+        o[0] = out0;
+#pragma unroll
+        for (int k = 1; k <= H; k++) {
+            float2 a = v[0], b = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int r = 1; r <= H; r++) {
+                const int q = (r * k) % R;
+                a.x = fmaf(sp[r - 1].x, cq[q], a.x);
+                a.y = fmaf(sp[r - 1].y, cq[q], a.y);
+                b.x = fmaf(sm[r - 1].x, sq[q], b.x);
+                b.y = fmaf(sm[r - 1].y, sq[q], b.y);
+            }
+            // i sg b = (-sg b.y, sg b.x)
+            o[k] = make_float2(a.x - sg * b.y, a.y + sg * b.x);
+            o[R - k] = make_float2(a.x + sg * b.y, a.y - sg * b.x);
+        }
+#pragma unroll
+        for (int k = 0; k < R; k++) v[k] = o[k];
+    }
+}
+
+// one Stockham pass of radix R over nseq sequences of length N (Ns = product of the
+// radices already applied)
+template <int R>
+__device__ void fft_pass(const float2 *in, int Si, float2 *out, int So, int N, int Ns, int nseq,
+                         const float2 *tw, bool inv, const FDiv &fseq) {
+    const int m = N / R, step = N / (Ns * R);
+    const FDiv fns = make_fdiv((uint32_t)Ns);
+    constexpr bool ODD = (R % 2) == 1;
+    float cq[ODD ? R : 1], sq[ODD ? R : 1];
+    if constexpr (ODD) {
+#pragma unroll
+        for (int q = 0; q < R; q++) {
+            const float2 w = tw[q * m];   // (cos, sin)(2 pi q / R)
+            cq[q] = w.x;
+            sq[q] = w.y;
+        }
+    }
+    const int total = m * nseq;
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        const int j = (int)fdiv((uint32_t)t, fseq), s = t - j * nseq;
+        const int jd = (int)fdiv((uint32_t)j, fns), jm = j - jd * Ns;
+        float2 v[R];
+#pragma unroll
+        for (int r = 0; r < R; r++) v[r] = in[(int64_t)(j + r * m) * Si + s];
+#pragma unroll
+        for (int r = 1; r < R; r++) {
+            float2 w = tw[jm * step * r];
+            if (!inv) w.y = -w.y;
+            v[r] = cmul(v[r], w);
+        }
+        butterfly<R>(v, inv, cq, sq);
+        const int d = jd * Ns * R + jm;
+#pragma unroll
+        for (int r = 0; r < R; r++) out[(int64_t)(d + r * Ns) * So + s] = v[r];
+    }
+}
+
+// all passes; returns the buffer holding the result (a or b)
+__device__ int next_radix(int n) {
+    return n % 4 == 0 ? 4 : n % 2 == 0 ? 2 : n % 3 == 0 ? 3 : n % 5 == 0 ? 5 : n % 7 == 0 ? 7 : n % 11 == 0 ? 11 : 13;
+}
+
+__device__ float2 *fft_run(float2 *a, int Sa, float2 *b, int Sb, int N, int nseq, const float2 *tw, bool inv,
+                           const FDiv &fseq) {
+    float2 *in = a, *out = b;
+    int Si = Sa, So = Sb, Ns = 1;
+    for (int rest = N; rest > 1;) {
+        const int R = next_radix(rest);
+        switch (R) {
+            case 4: fft_pass<4>(in, Si, out, So, N, Ns, nseq, tw, inv, fseq); break;
+            case 2: fft_pass<2>(in, Si, out, So, N, Ns, nseq, tw, inv, fseq); break;
+            case 3: fft_pass<3>(in, Si, out, So, N, Ns, nseq, tw, inv, fseq); break;
+            case 5: fft_pass<5>(in, Si, out, So, N, Ns, nseq, tw, inv, fseq); break;
+            case 7: fft_pass<7>(in, Si, out, So, N, Ns, nseq, tw, inv, fseq); break;
+            case 11: fft_pass<11>(in, Si, out, So, N, Ns, nseq, tw, inv, fseq); break;
+            default: fft_pass<13>(in, Si, out, So, N, Ns, nseq, tw, inv, fseq); break;
+        }
+        __syncthreads();
+        Ns *= R;
+        rest /= R;
+        float2 *tp = in;
+        in = out;
+        out = tp;
+        const int ts = Si;
+        Si = So;
+        So = ts;
+    }
+    return in;
+}
+
+__device__ void copy_rows(const float2 *src, int Ss, float2 *dst, int Sd, int N, int nseq, const FDiv &fseq) {
+    for (int t = threadIdx.x; t < N * nseq; t += blockDim.x) {
+        const int k = (int)fdiv((uint32_t)t, fseq), s = t - k * nseq;
+        dst[(int64_t)k * Sd + s] = src[(int64_t)k * Ss + s];
+    }
+}
+
+// C2R by FFT: X[k][c] = Re F[0][c] + 2 sum_{a=1}^{lim} Re(F[a][c] w^{ka}) for all k < nr
+__device__ void fft_c2r(const float2 *tw, float2 *F, int SF, float *X, int SX, int nr, int lim, int ncolg) {
+    const int nseq = ncolg / 2, SZ = SX / 2;
+    const FDiv fseq = make_fdiv((uint32_t)nseq);
+    float2 *Zx = reinterpret_cast<float2 *>(X);
+    // Hermitian extension of the column pair (2s, 2s+1), packed as A + i B
+    for (int t = threadIdx.x; t < nr * nseq; t += blockDim.x) {
+        const int k = (int)fdiv((uint32_t)t, fseq), s = t - k * nseq;
+        float2 z = make_float2(0.f, 0.f);
+        if (k == 0) {
+            const float4 f = *reinterpret_cast<const float4 *>(F + 2 * s);
+            z = make_float2(f.x, f.z);
+        } else if (k <= lim) {
+            const float4 f = *reinterpret_cast<const float4 *>(F + (int64_t)k * SF + 2 * s);
+            z = make_float2(f.x - f.w, f.y + f.z);
+        } else if (k >= nr - lim) {
+            const float4 f = *reinterpret_cast<const float4 *>(F + (int64_t)(nr - k) * SF + 2 * s);
+            z = make_float2(f.x + f.w, f.z - f.y);
+        }
+        Zx[(int64_t)k * SZ + s] = z;
+    }
+    __syncthreads();
+    float2 *res = fft_run(Zx, SZ, F, nseq, nr, nseq, tw, true, fseq);
+    if (res != Zx) {
+        copy_rows(res, nseq, Zx, SZ, nr, nseq, fseq);
+        __syncthreads();
+    }
+}
+
+// R2C by FFT (after the stress phase): F[a][c] = (1/nr) sum_k X[k][c] w^{-ka}, a <= lim
+__device__ void fft_r2c(const float2 *tw, float *X, int SX, float2 *F, int SF, int nr, int lim, int ncolg) {
+    const int nseq = ncolg / 2, SZ = SX / 2;
+    const FDiv fseq = make_fdiv((uint32_t)nseq);
+    float2 *Zx = reinterpret_cast<float2 *>(X);
+    float2 *res = fft_run(Zx, SZ, F, nseq, nr, nseq, tw, false, fseq);
+    if (res != Zx) {
+        copy_rows(res, nseq, Zx, SZ, nr, nseq, fseq);
+        __syncthreads();
+    }
+    // split the packed spectra: A = (Z_a + conj Z_{nr-a}) / 2, B = (Z_a - conj Z_{nr-a}) / 2i
+    const float h = 0.5f / (float)nr;
+    for (int t = threadIdx.x; t < (lim + 1) * nseq; t += blockDim.x) {
+        const int a = (int)fdiv((uint32_t)t, fseq), s = t - a * nseq;
+        const float2 z1 = Zx[(int64_t)a * SZ + s];
+        const float2 z2 = Zx[(int64_t)(a == 0 ? 0 : nr - a) * SZ + s];
+        *reinterpret_cast<float4 *>(F + (int64_t)a * SF + 2 * s) =
+            make_float4((z1.x + z2.x) * h, (z1.y - z2.y) * h, (z1.y + z2.y) * h, (z2.x - z1.x) * h);
+    }
+}
+
 __device__ void phys_c2r(const float2 *tw, const float2 *F, int SF, float *X, int SX, int nr, int lim, int ncolg) {
+    if (nr >= FFT_MIN && fft_size_ok(nr)) {
+        fft_c2r(tw, const_cast<float2 *>(F), SF, X, SX, nr, lim, ncolg);
+        return;
+    }
     const int kh = nr / 2 + 1;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     if (kh >= 96) {
@@ -390,6 +603,10 @@ __device__ __forceinline__ void r2c_task(const float2 *__restrict__ tw, const fl
 }
 
 __device__ void phys_r2c(const float2 *tw, float *X, int SX, float2 *F, int SF, int nr, int lim, int ncolg) {
+    if (nr >= FFT_MIN && fft_size_ok(nr)) {
+        fft_r2c(tw, X, SX, F, SF, nr, lim, ncolg);
+        return;
+    }
     phys_fold(X, SX, nr, ncolg);
     __syncthreads();
     const int na = lim + 1;

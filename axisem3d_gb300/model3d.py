@@ -113,14 +113,21 @@ class GaussianRandom(Model3D):
         self.kl = rng.standard_normal((self.modes, 3)) / ll
         self.ph = rng.uniform(0.0, 2 * math.pi, self.modes)
         self.R = R
+        self._kr = self.kr.astype(np.float32)
+        self._klR = (R * self.kl.T).astype(np.float32)
+        self._ph = self.ph.astype(np.float32)
         if self.ref == 0:
             raise ValueError("Volumetric3D_gaussian_random::initialize || reference type must be relative")
 
     def _eval_flat(self, x):
+        # phases and cosines in FP32 (|phase| < ~200 rad: error < 1e-5 rad, i.e. < 1e-6 in
+        # the perturbation), the sum over modes in FP64
         r = np.linalg.norm(x, axis=-1)
-        n = x / np.maximum(r, 1e-9)[:, None]
-        arg = r[:, None] * self.kr + self.R * (n @ self.kl.T) + self.ph
-        return self.rms * math.sqrt(2.0 / self.modes) * np.cos(arg).sum(-1)
+        n = (x / np.maximum(r, 1e-9)[:, None]).astype(np.float32)
+        arg = n @ self._klR
+        arg += r.astype(np.float32)[:, None] * self._kr
+        arg += self._ph
+        return self.rms * math.sqrt(2.0 / self.modes) * np.cos(arg, out=arg).sum(-1, dtype=np.float64)
 
     def evaluate(self, xyz):
         shape = xyz.shape[:-1]

@@ -122,13 +122,18 @@ def run(spec, steps, learn=None):
 
 
 def experiment(work, n_train=64, n_test=16, nu_full=64, steps=600, epochs=200, batch=4096, lr=2e-3,
-               eps=1e-3, interval=5, mesh_kw=None, out=None, log=print):
+               eps=1e-3, interval=5, mesh_kw=None, out=None, log=print, train_data=None):
     """Train on the wisdom of n_train full-Nu runs, judge n_test held-out models.  Returns
-    the summary dict (also written to out/summary.json with the parameters in out/nu_mlp.npz)."""
+    the summary dict (also written to out/summary.json with the parameters in out/nu_mlp.npz).
+    train_data: an earlier out/train_data.npz to reuse instead of the training runs."""
     from .nu_mlp import NuMLP
     work = Path(work)
     X, Y, pre = [], [], []
     t_train_runs = 0.0
+    if train_data is not None:
+        z = np.load(train_data)
+        X, Y = [z["X"]], [z["Y"]]
+        n_train = 0
     for i in range(n_train):
         d = write_case(work / f"train{i}", 1000 + i, nu_full, steps, mesh_kw)
         t0 = time.perf_counter()
@@ -138,8 +143,12 @@ def experiment(work, n_train=64, n_test=16, nu_full=64, steps=600, epochs=200, b
         _, t, wis, _ = run(spec, steps, learn=(interval, eps))
         t_train_runs += t
         X.append(element_features(sim))
-        Y.append(encode(element_labels(spec, wis), nu_full))
+        Y.append(encode(np.minimum(element_labels(spec, wis), nu_full), nu_full))
         log(f"train {i}: {t:.2f} s, mean label Nu {np.mean(element_labels(spec, wis)):.1f}")
+        del spec, sim
+        if out:
+            Path(out).mkdir(parents=True, exist_ok=True)
+            np.savez(Path(out) / "train_data.npz", X=np.concatenate(X), Y=np.concatenate(Y))
     X, Y = np.concatenate(X), np.concatenate(Y)
     net = NuMLP(max_batch=batch, seed=0)
     t0 = time.perf_counter()
@@ -155,7 +164,8 @@ def experiment(work, n_train=64, n_test=16, nu_full=64, steps=600, epochs=200, b
         d = write_case(work / f"test{i}", 5000 + i, nu_full, steps, mesh_kw)
         sim = solver.Simulation(d)
         spec_f = sim.build()
-        seis_f, t_f, wis, upd_f = run(spec_f, steps, learn=(interval, eps))
+        seis_f, t_f, _, upd_f = run(spec_f, steps)
+        _, t_fl, wis, _ = run(spec_f, steps, learn=(interval, eps))
         x = element_features(sim)
         y = net.forward(x).cpu().numpy()
         nu_e = decode(y, nu_full, margin)
@@ -167,12 +177,15 @@ def experiment(work, n_train=64, n_test=16, nu_full=64, steps=600, epochs=200, b
         spec_w = sim.build(nu_elem=np.maximum(element_labels(spec_f, wis), 1))
         seis_w, t_w, _, upd_w = run(spec_w, steps)
         mis_w = float(np.linalg.norm(seis_w - seis_f) / np.linalg.norm(seis_f))
-        tests.append(dict(seed=5000 + i, misfit=mis, t_full=t_f, t_learned=t_l, speedup=t_f / t_l,
-                          upd_full=upd_f, upd_learned=upd_l, misfit_wisdom=mis_w, t_wisdom=t_w,
+        tests.append(dict(seed=5000 + i, misfit=mis, t_full=t_f, t_full_learning=t_fl, t_learned=t_l,
+                          speedup=t_f / t_l, upd_full=upd_f, upd_learned=upd_l, misfit_wisdom=mis_w, t_wisdom=t_w,
                           mean_nu_pred=float(nu_e.mean()), mean_nu_label=float(element_labels(spec_f, wis).mean())))
+        del spec_f, spec_w
         specs_l.append(spec_l)
         seis_l_all.append(seis_l)
         log(f"test {i}: misfit {mis:.4f} (wisdom {mis_w:.4f}), full {t_f:.2f} s, learned {t_l:.2f} s")
+        if out:
+            (Path(out) / "tests_partial.json").write_text(json.dumps(tests, indent=1))
     # all held-out learned-Nu runs batched into one domain
     from . import ensemble
     big, info = ensemble.concat(specs_l)
@@ -183,7 +196,7 @@ def experiment(work, n_train=64, n_test=16, nu_full=64, steps=600, epochs=200, b
     summary = dict(
         n_train=n_train, n_test=n_test, nu_full=nu_full, steps=steps, elements=int(len(specs_l[0].e_pts)),
         epochs=epochs, batch=batch, fit_seconds=t_fit, train_runs_seconds=t_train_runs,
-        preloop_seconds_mean=float(np.mean(pre)), loss_first=float(hist[0]), loss_last=float(hist[-1]),
+        preloop_seconds_mean=float(np.mean(pre)) if pre else None, loss_first=float(hist[0]), loss_last=float(hist[-1]),
         margin=margin, tests=tests,
         misfit_max=max(t["misfit"] for t in tests), misfit_mean=float(np.mean([t["misfit"] for t in tests])),
         speedup_mean=float(np.mean([t["speedup"] for t in tests])),
@@ -207,8 +220,11 @@ if __name__ == "__main__":
     ap.add_argument("--train", type=int, default=64)
     ap.add_argument("--test", type=int, default=16)
     ap.add_argument("--nu", type=int, default=64)
-    ap.add_argument("--steps", type=int, default=600)
+    ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--epochs", type=int, default=200)
+    ap.add_argument("--eps", type=float, default=1e-3)
+    ap.add_argument("--train-data", default=None, help="reuse an earlier train_data.npz")
     a = ap.parse_args()
-    s = experiment(a.work, a.train, a.test, a.nu, a.steps, a.epochs, out=a.out)
+    s = experiment(a.work, a.train, a.test, a.nu, a.steps, a.epochs, eps=a.eps, out=a.out,
+                   train_data=a.train_data, log=lambda m: print(m, flush=True))
     print(json.dumps({k: v for k, v in s.items() if k != "tests"}))

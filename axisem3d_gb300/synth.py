@@ -130,7 +130,7 @@ def annulus_domain(seed=0, n_theta=4, n_r=3, r_in=3000e3, r_out=6371e3, theta_ma
                    nu_random=False, nu_max=None, fluid_layers=(), mat=MAT_ISO, in3d=False,
                    att=ATT_NONE, nsls=3, mass3d=False, couple3d=False, dt=0.05, source=True,
                    n_receivers=3, stf_len=64, stability_interval=0, kahan=False, fluid3d=False,
-                   perturb=0.04):
+                   perturb=0.04, lucky=False):
     """Connected spherical-element mesh on an (r, theta) grid.
 
     Element (ir, it) spans radii [rs[ir], rs[ir+1]] and colatitudes [ts[it], ts[it+1]];
@@ -166,7 +166,11 @@ def annulus_domain(seed=0, n_theta=4, n_r=3, r_in=3000e3, r_out=6371e3, theta_ma
     axial_pt = np.zeros(npt, bool)
     for jr in range(NZ):
         axial_pt[jr * NX] = True
-    nr_pt = np.where(axial_pt & (nr_pt % 2 == 0), nr_pt + 1, nr_pt)  # Quad::formNrField: axis odd
+    forced = axial_pt & (nr_pt % 2 == 0)
+    nr_pt = np.where(forced, nr_pt + 1, nr_pt)  # Quad::formNrField: axis odd
+    if lucky:  # FFT-friendly ring sizes (FFTW_LUCKY_NUMBER)
+        from .solver import next_lucky
+        nr_pt = np.array([next_lucky(int(n), bool(f)) for n, f in zip(nr_pt, forced)])
     fsurf = has_f & ~has_s & np.zeros(npt, bool)
     if fluid_layers and (n_r - 1) in fluid_layers:  # fluid at the free surface
         for ix in range(NX):

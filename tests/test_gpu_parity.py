@@ -25,6 +25,13 @@ CASES = {
     "fluid3d_mass3d_couple3d": dict(fluid_layers=(1,), in3d=True, fluid3d=True, mass3d=True,
                                     couple3d=True, nu=4, mat=MAT_TISO),
     "fluid_surface": dict(fluid_layers=(2,), nu=3),
+    # FFT-friendly ring sizes: the mixed-radix transform (radices 2, 3, 4, 5, 7, 11, 13)
+    "ti3d_cg4_fft25": dict(in3d=True, mat=MAT_TISO, att=ATT_CG4, nu=12),
+    "iso3d_full_fft_lucky_mixed": dict(in3d=True, att=ATT_FULL, nu_random=True, nu_max=40, lucky=True),
+    "aniso3d_fft_even50": dict(in3d=True, mat=MAT_ANISO, nu=24, lucky=True),
+    "iso3d_fft44": dict(in3d=True, nu=21, lucky=True),
+    "fluid3d_fft36": dict(fluid_layers=(1,), in3d=True, fluid3d=True, nu=16, lucky=True, mat=MAT_TISO),
+    "ti3d_fft260_chunked": dict(in3d=True, mat=MAT_TISO, att=ATT_CG4, nu=128, lucky=True),
 }
 
 
