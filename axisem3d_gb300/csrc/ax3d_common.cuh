@@ -31,8 +31,6 @@ struct ElemTable {
     float *mem;
     const int64_t *efofs;   // [E] complex offset into ef (element forces, [l][alpha][ncomp])
     float2 *ef;
-    const float2 *twtab;    // twiddles (cos, sin)(2 pi m / nr) for every nr in use
-    const int64_t *twofs;   // [nr_max + 1] offset of the table of each nr
 };
 
 // Device view of the point table.

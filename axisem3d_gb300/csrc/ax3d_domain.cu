@@ -111,8 +111,12 @@ struct ax3d_domain {
     DevBuf<float> d_ms, d_mf, d_sfn, d_sfni;
     DevBuf<int32_t> d_epts, d_eflags, d_enr;
     DevBuf<float> d_geo, d_trig, d_mod, d_attm, d_mem;
-    DevBuf<int64_t> d_mofs, d_aofs, d_memofs, d_efofs, d_twofs;
-    DevBuf<float2> d_ef, d_tw;
+    DevBuf<int64_t> d_mofs, d_aofs, d_memofs, d_efofs;
+    DevBuf<float2> d_ef, d_f2;
+    DevBuf<int32_t> d_i32;
+    DevBuf<ax3d::FftPlan> d_plans;
+    std::vector<DevBuf<float2>> bucket_scratch;
+    ax3d::PhysTables X{};
     DevBuf<float2> d_su, d_sv, d_sa, d_ss, d_sku, d_skv, d_fu, d_fv, d_fa, d_fs, d_fku, d_fkv;
     DevBuf<int2> d_items_s, d_items_f;
     std::vector<ax3d::PhysBucket> buckets_s, buckets_f;
@@ -326,6 +330,7 @@ struct ax3d_domain {
         std::vector<std::vector<int64_t>> sref(np), fref(np);
         std::vector<int2> items_s, items_f;
         std::map<int, std::vector<int32_t>> phys_s, phys_f;  // keyed by bucket id
+        std::vector<int32_t> phys3_s, phys3_f;
         int nr_max = 1;
         for (int e = 0; e < ne; e++) {
             const int nr = e_nr[e], n = nr / 2 + 1, flags = e_flags[e];
@@ -342,9 +347,7 @@ struct ax3d_domain {
             memofs[e] = memsize;
             if (a) memsize += (int64_t)(sls.nsls + 1) * 6 * npa * (e3d ? nr : 2 * n);
             if (e3d) {
-                // geometric buckets of nr so shared memory is sized per bucket
-                int b = (int)std::floor(std::log((double)nr) / std::log(1.15));
-                (fluid ? phys_f : phys_s)[b].push_back(e);
+                (fluid ? phys3_f : phys3_s).push_back(e);
             } else {
                 for (int al = 0; al < n; al++) (fluid ? items_f : items_s).push_back(make_int2(e, al));
             }
@@ -357,21 +360,17 @@ struct ax3d_domain {
             sg_ref.insert(sg_ref.end(), sref[p].begin(), sref[p].end());
             fg_ref.insert(fg_ref.end(), fref[p].begin(), fref[p].end());
         }
-        // twiddle tables (cos, sin)(2 pi m / nr) in FP64, for every nr used by 3D elements
-        std::vector<int64_t> twofs(nr_max + 1, 0);
-        std::vector<float2> tw;
+        // transform plans (FP64 tables) for every ring size of a 3D element, then
+        // geometric buckets of the transform length so shared memory is sized per bucket
         std::vector<char> used(nr_max + 1, 0);
         for (int e = 0; e < ne; e++)
             if (e_flags[e] & ax3d::EF_IN3D) used[e_nr[e]] = 1;
-        for (int r = 1; r <= nr_max; r++) {
-            if (!used[r]) continue;
-            twofs[r] = (int64_t)tw.size();
-            for (int m = 0; m < r; m++) {
-                const double th = 2.0 * M_PI * (double)m / (double)r;
-                tw.push_back(make_float2((float)std::cos(th), (float)std::sin(th)));
+        ax3d::FftTables ft = ax3d::build_fft_tables(used);
+        for (int fl = 0; fl < 2; fl++)
+            for (int e : fl ? phys3_f : phys3_s) {
+                const int b = (int)std::floor(std::log((double)ft.plans[e_nr[e]].L) / std::log(1.12));
+                (fl ? phys_f : phys_s)[b].push_back(e);
             }
-        }
-        if (tw.empty()) tw.push_back(make_float2(1.f, 0.f));
         // 3D points (Mass3D) and 3D couplings
         std::vector<int32_t> pts3d, sf3d;
         for (int p = 0; p < np; p++) {
@@ -421,8 +420,12 @@ struct ax3d_domain {
         d_efofs.upload(efofs, st);
         d_ef.alloc(std::max<int64_t>(efsize, 1));
         d_ef.zero(st);
-        d_tw.upload(tw, st);
-        d_twofs.upload(twofs, st);
+        d_plans.upload(ft.plans, st);
+        d_f2.upload(ft.f2, st);
+        d_i32.upload(ft.i32, st);
+        X.plans = d_plans.p;
+        X.f2 = d_f2.p;
+        X.i32 = d_i32.p;
         for (auto *b : {&d_su, &d_sv, &d_sa, &d_ss}) {
             b->alloc(std::max<int64_t>(nsolid, 1));
             b->zero(st);
@@ -440,6 +443,12 @@ struct ax3d_domain {
         nitems_s = (int)items_s.size();
         nitems_f = (int)items_f.size();
         bucket_lists.resize(phys_s.size() + phys_f.size());
+        bucket_scratch.clear();
+        bucket_scratch.resize(phys_s.size() + phys_f.size());
+        buckets_s.clear();
+        buckets_f.clear();
+        int num_sms = 0;
+        CK(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, device));
         size_t bi = 0;
         for (int fl = 0; fl < 2; fl++) {
             auto &src = fl ? phys_f : phys_s;
@@ -447,12 +456,19 @@ struct ax3d_domain {
             for (auto &kv : src) {
                 ax3d::PhysBucket b;
                 b.count = (int)kv.second.size();
-                for (int e : kv.second) b.nr_max = std::max(b.nr_max, e_nr[e]);
-                const int nc = fl ? 3 : 6;
-                b.npts_chunk = ax3d::phys_points_per_chunk(b.nr_max, nc);
+                for (int e : kv.second) {
+                    b.L_max = std::max(b.L_max, ft.plans[e_nr[e]].L);
+                    b.n_max = std::max(b.n_max, e_nr[e] / 2 + 1);
+                }
+                ax3d::size_phys_bucket(b, !fl);
                 if (b.npts_chunk <= 0)
                     throw Error(AX3D_ERR_UNSUPPORTED, "ax3d_finalize || nr too large for the physical-space kernel");
-                b.smem = ax3d::phys_smem_bytes(b.nr_max, nc, b.npts_chunk);
+                b.grid = ax3d::phys_grid(b, !fl, num_sms);
+                if (b.npts_chunk < 25) {
+                    b.scr_stride = (int64_t)25 * (fl ? 3 : 6) * b.n_max;
+                    bucket_scratch[bi].alloc((size_t)b.grid * b.scr_stride);
+                    b.scratch = bucket_scratch[bi].p;
+                }
                 bucket_lists[bi].upload(kv.second, st);
                 b.elems = bucket_lists[bi].p;
                 bi++;
@@ -525,8 +541,6 @@ struct ax3d_domain {
         T.mem = d_mem.p;
         T.efofs = d_efofs.p;
         T.ef = d_ef.p;
-        T.twtab = d_tw.p;
-        T.twofs = d_twofs.p;
         F.su = d_su.p; F.sv = d_sv.p; F.sa = d_sa.p; F.ss = d_ss.p; F.sku = d_sku.p; F.skv = d_skv.p;
         F.fu = d_fu.p; F.fv = d_fv.p; F.fa = d_fa.p; F.fs = d_fs.p; F.fku = d_fku.p; F.fkv = d_fkv.p;
         CK(cudaStreamSynchronize(st));
@@ -559,8 +573,8 @@ struct ax3d_domain {
     void compute_stiff() {
         ax3d::launch_elem_fourier_solid(T, P, F.su, d_items_s.p, nitems_s, sls, stream);
         ax3d::launch_elem_fourier_fluid(T, P, F.fu, d_items_f.p, nitems_f, stream);
-        for (auto &b : buckets_s) ax3d::launch_elem_phys_solid(T, P, F.su, b, sls, stream);
-        for (auto &b : buckets_f) ax3d::launch_elem_phys_fluid(T, P, F.fu, b, stream);
+        for (auto &b : buckets_s) ax3d::launch_elem_phys(true, T, P, F.su, b, X, sls, stream);
+        for (auto &b : buckets_f) ax3d::launch_elem_phys(false, T, P, F.fu, b, X, sls, stream);
         ax3d::launch_gather(P, T, F, stream);
     }
     void couple() { ax3d::launch_couple(P, F, d_sf3d.p, n_sf3d, stream); }
@@ -631,8 +645,8 @@ struct ax3d_domain {
         tbegin(AX3D_TIMER_ELEMENTS);
         ax3d::launch_elem_fourier_solid(T, P, F.su, d_items_s.p, nitems_s, sls, stream);
         ax3d::launch_elem_fourier_fluid(T, P, F.fu, d_items_f.p, nitems_f, stream);
-        for (auto &b : buckets_s) ax3d::launch_elem_phys_solid(T, P, F.su, b, sls, stream);
-        for (auto &b : buckets_f) ax3d::launch_elem_phys_fluid(T, P, F.fu, b, stream);
+        for (auto &b : buckets_s) ax3d::launch_elem_phys(true, T, P, F.su, b, X, sls, stream);
+        for (auto &b : buckets_f) ax3d::launch_elem_phys(false, T, P, F.fu, b, X, sls, stream);
         tend(n_elem_launches());
         tbegin(AX3D_TIMER_ASSEMBLE);
         ax3d::launch_gather(P, T, F, stream);

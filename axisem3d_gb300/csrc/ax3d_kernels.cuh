@@ -2,17 +2,47 @@
 #pragma once
 
 #include <string>
+#include <vector>
 
 #include "ax3d_common.cuh"
 
 namespace ax3d {
 
+// Transform plan of one ring size nr (device table indexed by nr).  kind 0: in-place
+// mixed radix of length L = nr; kind 1: Bluestein chirp convolution of smooth length L.
+constexpr int FFT_MAXRAD = 12;
+struct FftPlan {
+    int32_t kind = 0, L = 1, nrad = 0, pad = 0;
+    int32_t rad[FFT_MAXRAD] = {};  // radices in decimation-in-frequency order
+    int64_t tw = 0;                // L twiddles (cos, sin)(2 pi m / L) in the float2 table
+    int64_t rev = 0;               // kind 0: position -> sample map (nr int32)
+    int64_t chirp = 0;             // kind 1: h_n = e^{i pi n^2 / nr}, n < nr
+    int64_t bc2r = 0, br2c = 0;    // kind 1: kernel spectra (L float2, digit-reversed)
+};
+struct FftTables {
+    std::vector<FftPlan> plans;
+    std::vector<float2> f2;
+    std::vector<int32_t> i32;
+};
+// Device view of the transform tables plus the scratch of one bucket.
+struct PhysTables {
+    const FftPlan *plans = nullptr;
+    const float2 *f2 = nullptr;
+    const int32_t *i32 = nullptr;
+    float2 *scratch = nullptr;  // [grid][scr_stride] when elements go through in chunks
+    int64_t scr_stride = 0;
+};
+
 struct PhysBucket {
     int32_t *elems = nullptr;  // device list of element indices
     int count = 0;
-    int nr_max = 0;
+    int L_max = 0;             // longest transform in the bucket
+    int n_max = 0;             // most Fourier orders in the bucket
     int npts_chunk = 25;       // GLL points per pass (shared-memory budget)
     size_t smem = 0;
+    int grid = 0;              // persistent CTAs
+    float2 *scratch = nullptr;
+    int64_t scr_stride = 0;
 };
 
 // Sets the text ax3d_last_error returns on this thread.
@@ -20,18 +50,21 @@ void set_last_error(const std::string &msg);
 
 void set_g_matrices(const float *g_gll, const float *g_glj, cudaStream_t s);
 
-size_t phys_smem_bytes(int nr, int ncomp, int npts_chunk);
-int phys_points_per_chunk(int nr, int ncomp);
 void init_kernel_attributes();
+void init_phys_attributes();
+void set_g_matrices_phys(const float *g_gll, const float *g_glj, cudaStream_t s);
+// FP64 plans, twiddles, chirps and kernel spectra for every used ring size (used[nr] != 0)
+FftTables build_fft_tables(const std::vector<char> &used);
+size_t phys_smem_bytes(int Lmax, int nsq, int npts_chunk);
+void size_phys_bucket(PhysBucket &b, bool solid);
+int phys_grid(const PhysBucket &b, bool solid, int num_sms);
 
 void launch_elem_fourier_solid(const ElemTable &T, const PointTable &P, const float2 *su,
                                const int2 *items, int nitems, const SLS &sls, cudaStream_t s);
 void launch_elem_fourier_fluid(const ElemTable &T, const PointTable &P, const float2 *fu,
                                const int2 *items, int nitems, cudaStream_t s);
-void launch_elem_phys_solid(const ElemTable &T, const PointTable &P, const float2 *su,
-                            const PhysBucket &b, const SLS &sls, cudaStream_t s);
-void launch_elem_phys_fluid(const ElemTable &T, const PointTable &P, const float2 *fu,
-                            const PhysBucket &b, cudaStream_t s);
+void launch_elem_phys(bool solid, const ElemTable &T, const PointTable &P, const float2 *u, const PhysBucket &b,
+                      const PhysTables &X, const SLS &sls, cudaStream_t s);
 
 void launch_gather(const PointTable &P, const ElemTable &T, const Fields &F, cudaStream_t s);
 void launch_newmark(const PointTable &P, const Fields &F, float dt, float half_dt,

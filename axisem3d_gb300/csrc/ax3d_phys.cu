@@ -1,0 +1,1034 @@
+// ax3d_phys.cu -- physical-space element stiffness (3-D material) for sm_103a.
+//
+// Restates the 3-D branch of SolidElement::displToStiff and FluidElement::displToStiff
+// (SOLVER/src/core/element/SolidElement.cpp:404-443, FluidElement.cpp:333-355): the
+// gradient per Fourier order, FieldFFT::transformF2P to the nr azimuthal samples
+// (FieldFFT.cpp:19-25; SolverFFTW_N6::computeC2R, unnormalised, SolverFFTW_N6.cpp:39-44),
+// strain -> stress with the SLS memory variables at every sample, transformP2F
+// (computeR2C then x 1/nr, SolverFFTW_N6.cpp:45-53) and the divergence per order.
+//
+// One CTA of 256 threads works on one element at a time; the grid is persistent over a
+// bucket of elements of similar transform length, sized so that at least two CTAs are
+// resident per SM and the HBM streams of one element overlap the arithmetic of another.
+//
+// Each pair of real strain columns (components 2s and 2s+1 of one GLL point) travels as
+// one complex sequence z = a + i b of length L in shared memory, laid out
+// [position][sequence] so that consecutive threads touch consecutive sequences.  The
+// Hermitian spectra of a and b pack into z's spectrum as Z_k = A_k + i B_k and
+// Z_{nr-k} = conj(A_k) + i conj(B_k).  The transforms run in place:
+//  * mixed radix: decimation-in-frequency passes (radix 2, 3, 4, 5, 7, 11 and 13
+//    butterflies in registers; a warp-cooperative symmetric direct DFT for a prime factor
+//    above 13) take the spectrum in natural order to the samples in digit-reversed order.
+//    The stress is computed there, with the sample index from a table, and
+//    decimation-in-time passes take the reversed samples back to the natural spectrum.
+//  * Bluestein (ring sizes with a large prime factor): the length-nr DFT as a chirp
+//    convolution of smooth length M >= 2 nr - 1, with the same passes and the chirp
+//    kernel's spectrum stored in digit-reversed order.
+// All twiddles, chirps and kernel spectra are computed in FP64 on the host.
+// When an element's sequences do not fit in shared memory its GLL points go through in
+// chunks; the strain of later chunks and the stress of earlier ones wait in a per-CTA
+// global scratch (L2-resident), so the gradient and the divergence run once per element.
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <vector>
+
+#include "ax3d_elem_ops.cuh"
+#include "ax3d_kernels.cuh"
+
+namespace ax3d {
+
+namespace {
+
+constexpr int NT = 256;      // threads per CTA
+constexpr int NW = NT / 32;  // warps per CTA
+constexpr int WSCR = 125;    // per-warp grad / divergence scratch (float2)
+constexpr int RESEED = 8;    // direct DFT: exact twiddle reload interval
+constexpr int DIRECT_MAX = 513;  // largest prime handled by a direct pass
+constexpr size_t SMEM_CAP = 227 * 1024;
+constexpr size_t SMEM_TWO = 112 * 1024;  // two CTAs per SM
+
+// n / d for n < 2^32 by multiply-high (round-up method of Granlund and Montgomery)
+struct FDiv {
+    uint32_t m, s, d;
+};
+__device__ __forceinline__ FDiv make_fdiv(uint32_t d) {
+    uint32_t s = 0;
+    while ((1u << s) < d) s++;
+    const uint64_t m = ((1ull << 32) * ((1ull << s) - d)) / d + 1;
+    return FDiv{(uint32_t)m, s, d};
+}
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FDiv &f) {
+    if (f.d == 1) return n;
+    const uint32_t t = __umulhi(n, f.m);
+    return (t + ((n - t) >> 1)) >> (f.s - 1);
+}
+
+__device__ __forceinline__ float2 conjf2(float2 a) { return make_float2(a.x, -a.y); }
+// w_L^idx with the transform's sign (+1: e^{+i..}, -1: e^{-i..})
+__device__ __forceinline__ float2 twv(const float2 *tw, int idx, int sg) {
+    const float2 w = tw[idx];
+    return sg > 0 ? w : make_float2(w.x, -w.y);
+}
+
+// v <- DFT_R(v) with e^{+2 pi i rk/R} (inv) or e^{-2 pi i rk/R}; cq/sq = cos/sin(2 pi q/R)
+template <int R>
+__device__ __forceinline__ void butterfly(float2 (&v)[R], bool inv, const float *cq, const float *sq) {
+    if constexpr (R == 2) {
+        const float2 a = v[0], b = v[1];
+        v[0] = cadd(a, b);
+        v[1] = csub(a, b);
+    } else if constexpr (R == 4) {
+        const float2 t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]);
+        const float2 t2 = cadd(v[1], v[3]), d = csub(v[1], v[3]);
+        const float2 t3 = inv ? make_float2(-d.y, d.x) : make_float2(d.y, -d.x);  // +-i d
+        v[0] = cadd(t0, t2);
+        v[2] = csub(t0, t2);
+        v[1] = cadd(t1, t3);
+        v[3] = csub(t1, t3);
+    } else {
+        // odd R: out_k = v0 + sum_r (v_r + v_{R-r}) cos(2 pi rk/R) +- i (v_r - v_{R-r}) sin(..)
+        constexpr int H = (R - 1) / 2;
+        float2 sp[H], sm[H];
+        float2 out0 = v[0];
+#pragma unroll
+        for (int r = 1; r <= H; r++) {
+            sp[r - 1] = cadd(v[r], v[R - r]);
+            sm[r - 1] = csub(v[r], v[R - r]);
+            out0 = cadd(out0, sp[r - 1]);
+        }
+        const float sg = inv ? 1.f : -1.f;
+        float2 o[R];
+        o[0] = out0;
+#pragma unroll
+        for (int k = 1; k <= H; k++) {
+            float2 a = v[0], b = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int r = 1; r <= H; r++) {
+                const int qk = (r * k) % R;
+                a.x = fmaf(sp[r - 1].x, cq[qk], a.x);
+                a.y = fmaf(sp[r - 1].y, cq[qk], a.y);
+                b.x = fmaf(sm[r - 1].x, sq[qk], b.x);
+                b.y = fmaf(sm[r - 1].y, sq[qk], b.y);
+            }
+            o[k] = make_float2(a.x - sg * b.y, a.y + sg * b.x);  // a + i sg b
+            o[R - k] = make_float2(a.x + sg * b.y, a.y - sg * b.x);
+        }
+#pragma unroll
+        for (int k = 0; k < R; k++) v[k] = o[k];
+    }
+}
+
+// One in-place pass of radix R over ns sequences (row stride S) of length L; the pass
+// works on blocks of length Ls with butterfly stride m = Ls / R.
+//   DIF: butterfly, then output k of butterfly j times w_Ls^{jk}.
+//   DIT: input k of butterfly j times w_Ls^{jk}, then butterfly.
+template <int R>
+__device__ __noinline__ void rad_pass(float2 *buf, int S, int ns, int L, int Ls, const float2 *tw, int sg, bool dit) {
+    const int m = Ls / R, ts = L / Ls;
+    const int total = (L / R) * ns;
+    const FDiv fs = make_fdiv((uint32_t)ns), fm = make_fdiv((uint32_t)m);
+    constexpr bool ODD = (R % 2) == 1;
+    float cq[ODD ? R : 1], sq[ODD ? R : 1];
+    if constexpr (ODD) {
+#pragma unroll
+        for (int qk = 0; qk < R; qk++) {
+            const float2 w = tw[qk * (L / R)];
+            cq[qk] = w.x;
+            sq[qk] = w.y;
+        }
+    }
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        const int bj = (int)fdiv((uint32_t)t, fs), s = t - bj * ns;
+        const int b = (int)fdiv((uint32_t)bj, fm), j = bj - b * m;
+        float2 *p0 = buf + (int64_t)(b * Ls + j) * S + s;
+        const int64_t rs = (int64_t)m * S;
+        float2 v[R];
+#pragma unroll
+        for (int r = 0; r < R; r++) v[r] = p0[r * rs];
+        if (dit) {
+#pragma unroll
+            for (int r = 1; r < R; r++) v[r] = cmul(v[r], twv(tw, j * r * ts, sg));
+        }
+        butterfly<R>(v, sg > 0, cq, sq);
+        if (!dit) {
+#pragma unroll
+            for (int r = 1; r < R; r++) v[r] = cmul(v[r], twv(tw, j * r * ts, sg));
+        }
+#pragma unroll
+        for (int r = 0; r < R; r++) p0[r * rs] = v[r];
+    }
+}
+
+// One in-place pass of a prime radix p > 13 by the symmetric direct DFT.  A group of GS
+// lanes owns one butterfly of SG sequences; lane gl computes outputs k = 1 + gl + GS q
+// (q < KL) and p - k.  The group first replaces (v_r, v_{p-r}) by (v_r + v_{p-r},
+// v_r - v_{p-r}) in place, then accumulates with twiddles advanced by complex rotation and
+// reloaded exactly every RESEED orders, and writes after a warp barrier (only the group
+// reads or writes its butterfly).
+template <int GS, int KL, int SG>
+__device__ __noinline__ void direct_pass(float2 *buf, int S, int ns, int L, int Ls, int p, const float2 *tw, int sg, bool dit) {
+    const int H = (p - 1) >> 1, m = Ls / p, ts = L / Ls, ps = L / p;
+    const int nsg = (ns + SG - 1) / SG;
+    const int ntask = (L / Ls) * m * nsg;
+    constexpr int GPW = 32 / GS;
+    const int lane = threadIdx.x & 31, gi = lane / GS, gl = lane - gi * GS;
+    const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const FDiv fn = make_fdiv((uint32_t)nsg), fm = make_fdiv((uint32_t)m);
+    const int64_t rs = (int64_t)m * S;
+    for (int t0 = warp * GPW; t0 < ntask; t0 += nw * GPW) {
+        const int t = t0 + gi;
+        const bool act = t < ntask;
+        const int tt = act ? t : 0;
+        const int bj = (int)fdiv((uint32_t)tt, fn), sgi = tt - bj * nsg;
+        const int b = (int)fdiv((uint32_t)bj, fm), j = bj - b * m;
+        const int s0 = sgi * SG;
+        const int nv = act ? min(SG, ns - s0) : 0;
+        float2 *base = buf + (int64_t)(b * Ls + j) * S + s0;
+        // (DIT input twiddles and) sums / differences, in place
+        for (int r = 1 + gl; r <= H; r += GS) {
+            float2 wr = make_float2(1.f, 0.f), wm = make_float2(1.f, 0.f);
+            if (dit) {
+                wr = twv(tw, j * r * ts, sg);
+                wm = twv(tw, j * (p - r) * ts, sg);
+            }
+#pragma unroll
+            for (int s = 0; s < SG; s++) {
+                if (s < nv) {
+                    float2 a = base[r * rs + s], c = base[(p - r) * rs + s];
+                    if (dit) {
+                        a = cmul(a, wr);
+                        c = cmul(c, wm);
+                    }
+                    base[r * rs + s] = cadd(a, c);
+                    base[(p - r) * rs + s] = csub(a, c);
+                }
+            }
+        }
+        __syncwarp();
+        float2 v0[SG], sum0[SG], ca[KL][SG], cb[KL][SG];
+#pragma unroll
+        for (int s = 0; s < SG; s++) {
+            v0[s] = s < nv ? base[s] : make_float2(0.f, 0.f);
+            sum0[s] = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int qk = 0; qk < KL; qk++) ca[qk][s] = cb[qk][s] = make_float2(0.f, 0.f);
+        }
+        int idx[KL], step[KL];
+        float2 w[KL], w1[KL];
+#pragma unroll
+        for (int qk = 0; qk < KL; qk++) {
+            const int k = 1 + gl + GS * qk;
+            const int kk = k <= H ? k : 0;
+            idx[qk] = (kk * ps) % L;  // w_p^{k r} at r = 1
+            step[qk] = (RESEED * kk * ps) % L;
+            w1[qk] = tw[idx[qk]];
+            w[qk] = w1[qk];
+        }
+        for (int r0 = 1; r0 <= H; r0 += RESEED) {
+#pragma unroll
+            for (int qk = 0; qk < KL; qk++) w[qk] = tw[idx[qk]];
+            const int rend = min(r0 + RESEED, H + 1);
+            for (int r = r0; r < rend; r++) {
+                float2 sp[SG], sm[SG];
+#pragma unroll
+                for (int s = 0; s < SG; s++) {
+                    sp[s] = s < nv ? base[r * rs + s] : make_float2(0.f, 0.f);
+                    sm[s] = s < nv ? base[(p - r) * rs + s] : make_float2(0.f, 0.f);
+                    sum0[s] = cadd(sum0[s], sp[s]);
+                }
+#pragma unroll
+                for (int qk = 0; qk < KL; qk++) {
+#pragma unroll
+                    for (int s = 0; s < SG; s++) {
+                        ca[qk][s].x = fmaf(w[qk].x, sp[s].x, ca[qk][s].x);
+                        ca[qk][s].y = fmaf(w[qk].x, sp[s].y, ca[qk][s].y);
+                        cb[qk][s].x = fmaf(w[qk].y, sm[s].x, cb[qk][s].x);
+                        cb[qk][s].y = fmaf(w[qk].y, sm[s].y, cb[qk][s].y);
+                    }
+                    w[qk] = cmul(w[qk], w1[qk]);
+                }
+            }
+#pragma unroll
+            for (int qk = 0; qk < KL; qk++) {
+                idx[qk] += step[qk];
+                if (idx[qk] >= L) idx[qk] -= L;
+            }
+        }
+        __syncwarp();
+#pragma unroll
+        for (int qk = 0; qk < KL; qk++) {
+            const int k = 1 + gl + GS * qk;
+            if (k > H) continue;
+            float2 wk = make_float2(1.f, 0.f), wpk = make_float2(1.f, 0.f);
+            if (!dit) {
+                wk = twv(tw, j * k * ts, sg);
+                wpk = twv(tw, j * (p - k) * ts, sg);
+            }
+#pragma unroll
+            for (int s = 0; s < SG; s++) {
+                if (s < nv) {
+                    const float2 a = cadd(v0[s], ca[qk][s]), bb = cb[qk][s];
+                    const float2 ib = sg > 0 ? make_float2(-bb.y, bb.x) : make_float2(bb.y, -bb.x);
+                    float2 ok = cadd(a, ib), opk = csub(a, ib);
+                    if (!dit) {
+                        ok = cmul(ok, wk);
+                        opk = cmul(opk, wpk);
+                    }
+                    base[k * rs + s] = ok;
+                    base[(p - k) * rs + s] = opk;
+                }
+            }
+        }
+        if (gl == 0) {
+#pragma unroll
+            for (int s = 0; s < SG; s++)
+                if (s < nv) base[s] = cadd(v0[s], sum0[s]);
+        }
+        __syncwarp();
+    }
+}
+
+__device__ void run_pass(int R, float2 *buf, int S, int ns, int L, int Ls, const float2 *tw, int sg, bool dit) {
+    switch (R) {
+        case 2: rad_pass<2>(buf, S, ns, L, Ls, tw, sg, dit); break;
+        case 3: rad_pass<3>(buf, S, ns, L, Ls, tw, sg, dit); break;
+        case 4: rad_pass<4>(buf, S, ns, L, Ls, tw, sg, dit); break;
+        case 5: rad_pass<5>(buf, S, ns, L, Ls, tw, sg, dit); break;
+        case 7: rad_pass<7>(buf, S, ns, L, Ls, tw, sg, dit); break;
+        case 11: rad_pass<11>(buf, S, ns, L, Ls, tw, sg, dit); break;
+        case 13: rad_pass<13>(buf, S, ns, L, Ls, tw, sg, dit); break;
+        default:
+            if (R <= 17)
+                direct_pass<8, 1, 8>(buf, S, ns, L, Ls, R, tw, sg, dit);
+            else if (R <= 33)
+                direct_pass<16, 1, 8>(buf, S, ns, L, Ls, R, tw, sg, dit);
+            else if (R <= 65)
+                direct_pass<32, 1, 8>(buf, S, ns, L, Ls, R, tw, sg, dit);
+            else if (R <= 129)
+                direct_pass<32, 2, 4>(buf, S, ns, L, Ls, R, tw, sg, dit);
+            else if (R <= 257)
+                direct_pass<32, 4, 2>(buf, S, ns, L, Ls, R, tw, sg, dit);
+            else
+                direct_pass<32, 8, 1>(buf, S, ns, L, Ls, R, tw, sg, dit);
+    }
+}
+
+// All passes of a plan: DIF (natural -> reversed) or DIT (reversed -> natural).
+__device__ void fft_passes(float2 *buf, int S, int ns, const FftPlan &pl, const float2 *tw, int sg, bool dit) {
+    const int L = pl.L;
+    if (!dit) {
+        int Ls = L;
+        for (int i = 0; i < pl.nrad; i++) {
+            run_pass(pl.rad[i], buf, S, ns, L, Ls, tw, sg, false);
+            __syncthreads();
+            Ls /= pl.rad[i];
+        }
+    } else {
+        int Ls = 1;
+        for (int i = pl.nrad - 1; i >= 0; i--) {
+            Ls *= pl.rad[i];
+            run_pass(pl.rad[i], buf, S, ns, L, Ls, tw, sg, true);
+            __syncthreads();
+        }
+    }
+}
+
+__device__ void pointwise(float2 *buf, int S, int ns, int L, const float2 *__restrict__ K) {
+    const FDiv fs = make_fdiv((uint32_t)ns);
+    for (int t = threadIdx.x; t < L * ns; t += blockDim.x) {
+        const int pos = (int)fdiv((uint32_t)t, fs), s = t - pos * ns;
+        buf[(int64_t)pos * S + s] = cmul(buf[(int64_t)pos * S + s], __ldg(K + pos));
+    }
+    __syncthreads();
+}
+
+// spectrum (natural) -> samples: mixed radix leaves them digit-reversed, Bluestein natural
+// (before the post-chirp h_k, which the stress phase applies)
+__device__ void transform_c2r(float2 *buf, int S, int ns, const FftPlan &pl, const float2 *tw, const float2 *f2) {
+    if (pl.kind == 0) {
+        fft_passes(buf, S, ns, pl, tw, +1, false);
+    } else {
+        fft_passes(buf, S, ns, pl, tw, -1, false);
+        pointwise(buf, S, ns, pl.L, f2 + pl.bc2r);
+        fft_passes(buf, S, ns, pl, tw, +1, true);
+    }
+}
+// samples -> spectrum (natural); scaled by 1/nr in the extraction (mixed) or the kernel
+// spectrum (Bluestein)
+__device__ void transform_r2c(float2 *buf, int S, int ns, const FftPlan &pl, const float2 *tw, const float2 *f2) {
+    if (pl.kind == 0) {
+        fft_passes(buf, S, ns, pl, tw, -1, true);
+    } else {
+        fft_passes(buf, S, ns, pl, tw, -1, false);
+        pointwise(buf, S, ns, pl.L, f2 + pl.br2c);
+        fft_passes(buf, S, ns, pl, tw, +1, true);
+    }
+}
+
+// Hermitian packing of order a of the column pair (A, B) into sequence col.
+__device__ __forceinline__ void zput(float2 *buf, int S, int col, int a, int nr, float2 A, float2 B,
+                                     const float2 *chirp) {
+    if (a == 0) {
+        buf[col] = make_float2(A.x, B.x);  // only Re of order 0 enters the C2R
+        return;
+    }
+    float2 z1 = make_float2(A.x - B.y, A.y + B.x);  // A + i B
+    float2 z2 = make_float2(A.x + B.y, B.x - A.y);  // conj(A) + i conj(B)
+    if (chirp) {
+        z1 = cmul(z1, __ldg(chirp + a));
+        z2 = cmul(z2, __ldg(chirp + nr - a));
+    }
+    buf[(int64_t)a * S + col] = z1;
+    buf[(int64_t)(nr - a) * S + col] = z2;
+}
+// Order a of the column pair of sequence col from the transformed spectrum (x h).
+__device__ __forceinline__ void zget(const float2 *buf, int S, int col, int a, int nr, const float2 *chirp,
+                                     float h, float2 &A, float2 &B) {
+    float2 z1 = buf[(int64_t)a * S + col];
+    float2 z2 = a == 0 ? z1 : buf[(int64_t)(nr - a) * S + col];
+    if (chirp) {
+        z1 = cmul(z1, conjf2(__ldg(chirp + a)));
+        z2 = a == 0 ? z1 : cmul(z2, conjf2(__ldg(chirp + nr - a)));
+    }
+    A = make_float2((z1.x + z2.x) * h, (z1.y - z2.y) * h);
+    B = make_float2((z1.y + z2.y) * h, (z2.x - z1.x) * h);
+}
+
+// scatterDisplToElement (SolidPoint.cpp:175-195): orders above the point's Nu, and its
+// Nyquist order, read as zero.
+__device__ __forceinline__ void load_u(const PointTable &P, const float2 *u, bool solid, int pt, int a,
+                                       float2 v[3]) {
+    const int pnr = P.nr[pt];
+    const int plim = pnr / 2 - (pnr % 2 == 0);
+    v[0] = v[1] = v[2] = make_float2(0.f, 0.f);
+    if (a > plim) return;
+    if (solid) {
+        const float2 *s = u + P.sofs[pt] + (int64_t)a * 3;
+        v[0] = s[0];
+        v[1] = s[1];
+        v[2] = s[2];
+    } else {
+        v[0] = u[P.fofs[pt] + a];
+    }
+}
+
+// Divergence of one Fourier order (computeQuad6, Gradient.cpp:267-317) with one
+// component at a time through a 5 x 25 scratch.
+__device__ __forceinline__ void quad6_split(const LaneOps &L, const Geo &g, bool axial, int beta,
+                                            const float2 sig[6], float2 *q, bool active, float2 f[3]) {
+    const int p = L.i * 5 + L.j;
+    const float b = -(float)beta;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        if (active) {
+            float2 X, Y, gg;
+            if (c == 0) {
+                X = cadd(cscale(g.dzdeta, sig[0]), cscale(g.dsdeta, sig[4]));
+                Y = cadd(cscale(g.dzdxii, sig[0]), cscale(g.dsdxii, sig[4]));
+                gg = cadd(sig[1], cimul(b, sig[5]));
+            } else if (c == 1) {
+                X = cadd(cscale(g.dzdeta, sig[5]), cscale(g.dsdeta, sig[3]));
+                Y = cadd(cscale(g.dzdxii, sig[5]), cscale(g.dsdxii, sig[3]));
+                gg = csub(cimul(b, sig[1]), sig[5]);
+            } else {
+                X = cadd(cscale(g.dzdeta, sig[4]), cscale(g.dsdeta, sig[2]));
+                Y = cadd(cscale(g.dzdxii, sig[4]), cscale(g.dsdxii, sig[2]));
+                gg = cimul(b, sig[3]);
+            }
+            q[p] = X;
+            q[25 + p] = Y;
+            q[50 + p] = gg;
+            q[75 + p] = cscale(g.dzdeta, gg);   // DzDeta o g (axial column term)
+            q[100 + p] = cscale(g.dzdxii, gg);  // DzDxii o g (axial, beta = 1)
+        }
+        __syncwarp();
+        if (active) {
+            float2 acc = make_float2(0.f, 0.f), acc2 = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int k = 0; k < 5; k++) {
+                const float2 x = q[k * 5 + L.j], y = q[25 + L.i * 5 + k];
+                acc.x += L.gxr[k] * x.x;
+                acc.y += L.gxr[k] * x.y;
+                acc2.x += y.x * L.ger[k];
+                acc2.y += y.y * L.ger[k];
+            }
+            float2 fc = cadd(cadd(acc, acc2), cscale(g.inv_s, q[50 + p]));
+            if (axial) {
+                fc = cadd(fc, cscale(L.gxr[0], q[75 + L.j]));  // Gradient.cpp:300-303
+                if (beta == 1 && L.i == 0 && c < 2) {            // Gradient.cpp:304-307
+                    float2 h = make_float2(0.f, 0.f);
+#pragma unroll
+                    for (int k = 0; k < 5; k++) {
+                        const float2 t = q[100 + k];
+                        h.x += t.x * L.ger[k];
+                        h.y += t.y * L.ger[k];
+                    }
+                    fc = cadd(fc, h);
+                }
+            }
+            f[c] = fc;
+        }
+        __syncwarp();
+    }
+}
+
+struct PhysSmem {
+    float2 *tw, *buf, *wscr;
+    int32_t *rev, *lst;
+    __device__ PhysSmem(char *smem, int Lmax, int S) {
+        tw = reinterpret_cast<float2 *>(smem);
+        rev = reinterpret_cast<int32_t *>(tw + Lmax);
+        lst = rev + ((Lmax + 1) & ~1);
+        buf = reinterpret_cast<float2 *>(lst + 64);
+        wscr = buf + (int64_t)Lmax * S;
+    }
+};
+
+}  // namespace
+
+size_t phys_smem_bytes(int Lmax, int nsq, int npts_chunk) {
+    return (size_t)8 * Lmax + (size_t)4 * ((Lmax + 1) & ~1) + 4 * 64 + (size_t)8 * Lmax * nsq * npts_chunk +
+           (size_t)8 * NW * WSCR;
+}
+
+// ------------------------------------------------------------------------------------
+// Phases.  Each is a separate (not inlined) function so that registers are allocated per
+// phase: the per-lane element operators live only in the gradient and divergence.
+// ------------------------------------------------------------------------------------
+namespace {
+
+// Phase 1 of the first chunk: gradient (computeGrad6 / computeGrad, with the RTZ
+// rotation for TI) of every order at all 25 points, warp per order and lane per point;
+// points of the chunk go into the packed sequences, the others into the scratch.
+template <bool SOLID>
+__device__ __noinline__ void phase_grad(const ElemTable &T, const PointTable &P, const float2 *u, int e, int nr,
+                                        bool axial, bool tiso, const float2 *chirp, float2 *buf, int S, int pc,
+                                        float2 *scr, float2 *q) {
+    constexpr int NSQ = SOLID ? 3 : 2;
+    constexpr int NC = SOLID ? 6 : 3;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const bool active = lane < NPE;
+    const int p = active ? lane : 0;
+    const int nu = nr / 2, n = nu + 1, lim = nu - (nr % 2 == 0);
+    LaneOps Lo;
+    Lo.init(p, axial);
+    Geo g;
+    g.load(T.geo + (int64_t)e * 125, p);
+    float s1 = 0.f, c1 = 0.f, s2 = 0.f, c2 = 0.f;
+    if (tiso) {
+        const float *tr = T.trig + (int64_t)e * 100;
+        s1 = tr[p];
+        c1 = tr[25 + p];
+        s2 = tr[50 + p];
+        c2 = tr[75 + p];
+    }
+    const int pt_me = T.pts[e * NPE + p];
+    float2 un[3];
+    if (active && warp < n) load_u(P, u, SOLID, pt_me, warp, un);
+    for (int a = warp; a < n; a += NW) {
+        if (active) {
+            q[p] = un[0];
+            if (SOLID) {
+                q[25 + p] = un[1];
+                q[50 + p] = un[2];
+            }
+            if (a + NW < n) load_u(P, u, SOLID, pt_me, a + NW, un);  // prefetch
+        }
+        __syncwarp();
+        if (active && a <= lim) {
+            float2 eps[NC];
+            if constexpr (SOLID) {
+                grad6_lane(Lo, g, axial, a, q, eps);
+                if (tiso) spz_rtz(eps, s1, c1, s2, c2);
+            } else {
+                grad1_lane(Lo, g, axial, a, q, eps);
+            }
+            if (p < pc) {
+#pragma unroll
+                for (int s = 0; s < NSQ; s++)
+                    zput(buf, S, NSQ * p + s, a, nr, eps[2 * s], 2 * s + 1 < NC ? eps[2 * s + 1] : make_float2(0.f, 0.f),
+                         chirp);
+            } else {
+                float2 *o = scr + ((int64_t)a * NPE + p) * NC;
+#pragma unroll
+                for (int i = 0; i < NC; i++) o[i] = eps[i];
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// Phase 3, points without memory variables: elastic stress at every sample.
+template <int MAT>
+__device__ __noinline__ void phase_stress(float2 *buf, int S, int nr, int ne_, const int32_t *lst, const int32_t *rev,
+                                          const float *md, const float2 *chirp, int p0) {
+    for (int t = threadIdx.x; t < nr * ne_; t += blockDim.x) {
+        const int pos = t / ne_, pp = lst[t - pos * ne_], pg = p0 + pp;
+        const int k = chirp ? pos : rev[pos];
+        float2 *z = buf + (int64_t)pos * S + 3 * pp;
+        const float2 hk = chirp ? __ldg(chirp + k) : make_float2(1.f, 0.f);
+        float2 zz[3];
+#pragma unroll
+        for (int s = 0; s < 3; s++) zz[s] = chirp ? cmul(z[s], hk) : z[s];
+        const float e6[6] = {zz[0].x, zz[0].y, zz[1].x, zz[1].y, zz[2].x, zz[2].y};
+        float s6[6];
+        elastic(MAT, e6, s6, [&](int mm) { return __ldg(md + ((int64_t)mm * nr + k) * NPE + pg); });
+#pragma unroll
+        for (int s = 0; s < 3; s++) {
+            const float2 o = make_float2(s6[2 * s], s6[2 * s + 1]);
+            z[s] = chirp ? cmul(o, conjf2(hk)) : o;
+        }
+    }
+}
+
+// Phase 3, attenuated points: elastic stress minus the memory variables (applyToStress),
+// then updateMemoryVariables (Attenuation3D_Full.cpp:16-50, Attenuation3D_CG4.cpp:16-62).
+template <int MAT>
+__device__ __noinline__ void phase_stress_att(float2 *buf, int S, int nr, int na_, const int32_t *lst,
+                                              const int32_t *rev, const float *md, const float2 *chirp, int p0,
+                                              int att, float *mem, const float *am, const SLS &sls) {
+    const int npa = att == 2 ? 4 : NPE;
+    const int64_t sl = (int64_t)nr * 6 * npa;
+    for (int t = threadIdx.x; t < nr * na_; t += blockDim.x) {
+        const int pos = t / na_, pp = lst[t - pos * na_], pg = p0 + pp;
+        const int qq = att == 2 ? cg4_index(pg) : pg;
+        const int k = chirp ? pos : rev[pos];
+        float2 *z = buf + (int64_t)pos * S + 3 * pp;
+        const float2 hk = chirp ? __ldg(chirp + k) : make_float2(1.f, 0.f);
+        float2 zz[3];
+#pragma unroll
+        for (int s = 0; s < 3; s++) zz[s] = chirp ? cmul(z[s], hk) : z[s];
+        const float e6[6] = {zz[0].x, zz[0].y, zz[1].x, zz[1].y, zz[2].x, zz[2].y};
+        float s6[6];
+        elastic(MAT, e6, s6, [&](int mm) { return __ldg(md + ((int64_t)mm * nr + k) * NPE + pg); });
+        float *R = mem + (int64_t)k * 6 * npa + qq;
+        float *SR = R + sls.nsls * sl;
+        for (int l = 0; l < sls.nsls; l++)
+#pragma unroll
+            for (int i = 0; i < 6; i++) s6[i] -= R[l * sl + i * npa];
+        sls_update(sls, R, SR, sl, (int64_t)npa, e6, am[(int64_t)k * npa + qq],
+                   am[(int64_t)nr * npa + (int64_t)k * npa + qq]);
+#pragma unroll
+        for (int s = 0; s < 3; s++) {
+            const float2 o = make_float2(s6[2 * s], s6[2 * s + 1]);
+            z[s] = chirp ? cmul(o, conjf2(hk)) : o;
+        }
+    }
+}
+
+// Phase 3 of a fluid element: sigma_i = K d_i chi (Acoustic3D.cpp:9-16) at every sample.
+__device__ __noinline__ void phase_stress_fluid(float2 *buf, int S, int nr, int pc, const int32_t *rev,
+                                                const float *md, const float2 *chirp, int p0) {
+    for (int t = threadIdx.x; t < nr * pc; t += blockDim.x) {
+        const int pos = t / pc, pp = t - pos * pc;
+        const int k = chirp ? pos : rev[pos];
+        float2 *z = buf + (int64_t)pos * S + 2 * pp;
+        const float K = __ldg(md + (int64_t)k * NPE + p0 + pp);
+        // the chirp factors h_k conj(h_k) cancel around a real scaling
+        z[0] = cscale(K, z[0]);
+        z[1] = cscale(K, z[1]);
+    }
+}
+
+// Phase 6: divergence (computeQuad6 / computeQuad, after the TI back-rotation) of every
+// order into the element force; the last chunk's stress spectra come from the packed
+// sequences, the earlier chunks' from the scratch.
+template <bool SOLID>
+__device__ __noinline__ void phase_quad(const ElemTable &T, int e, int nr, bool axial, bool tiso,
+                                        const float2 *chirp, float hsc, const float2 *buf, int S, int pl0,
+                                        const float2 *scr, float2 *q) {
+    constexpr int NSQ = SOLID ? 3 : 2;
+    constexpr int NC = SOLID ? 6 : 3;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const bool active = lane < NPE;
+    const int p = active ? lane : 0;
+    const int nu = nr / 2, n = nu + 1, lim = nu - (nr % 2 == 0);
+    LaneOps Lo;
+    Lo.init(p, axial);
+    Geo g;
+    g.load(T.geo + (int64_t)e * 125, p);
+    float s1 = 0.f, c1 = 0.f, s2 = 0.f, c2 = 0.f;
+    if (tiso) {
+        const float *tr = T.trig + (int64_t)e * 100;
+        s1 = tr[p];
+        c1 = tr[25 + p];
+        s2 = tr[50 + p];
+        c2 = tr[75 + p];
+    }
+    float2 *ef = T.ef + T.efofs[e];
+    for (int a = warp; a < n; a += NW) {
+        float2 sig[NC];
+#pragma unroll
+        for (int i = 0; i < NC; i++) sig[i] = make_float2(0.f, 0.f);
+        if (active && a <= lim) {
+            if (p >= pl0) {
+#pragma unroll
+                for (int s = 0; s < NSQ; s++) {
+                    float2 A, B;
+                    zget(buf, S, NSQ * (p - pl0) + s, a, nr, chirp, hsc, A, B);
+                    sig[2 * s] = A;
+                    if (2 * s + 1 < NC) sig[2 * s + 1] = B;
+                }
+            } else {
+                const float2 *o = scr + ((int64_t)a * NPE + p) * NC;
+#pragma unroll
+                for (int i = 0; i < NC; i++) sig[i] = o[i];
+            }
+        }
+        if constexpr (SOLID) {
+            if (active && tiso) rtz_spz(sig, s1, c1, s2, c2);
+            float2 f[3];
+            quad6_split(Lo, g, axial, a, sig, q, active && a <= lim, f);
+            if (active) {
+                float2 *o = ef + ((int64_t)p * n + a) * 3;
+                if (a > lim) f[0] = f[1] = f[2] = make_float2(0.f, 0.f);
+                o[0] = f[0];
+                o[1] = f[1];
+                o[2] = f[2];
+            }
+        } else {
+            float2 f;
+            quad1_lane(Lo, g, axial, a, sig, q, active && a <= lim, f);
+            if (active) ef[(int64_t)p * n + a] = a <= lim ? f : make_float2(0.f, 0.f);
+        }
+    }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------
+// The kernel: SOLID = 6 strain components (3 sequences per point), else the fluid's 3
+// potential-gradient components (2 sequences per point).
+// ------------------------------------------------------------------------------------
+template <bool SOLID>
+__global__ void __launch_bounds__(NT, 2)
+    k_elem_phys(const __grid_constant__ ElemTable T, const __grid_constant__ PointTable P,
+                const float2 *__restrict__ u, const int32_t *__restrict__ elems, int count, int Pc, int Lmax,
+                const __grid_constant__ PhysTables X, const __grid_constant__ SLS sls) {
+    constexpr int NSQ = SOLID ? 3 : 2;
+    constexpr int NC = SOLID ? 6 : 3;
+    extern __shared__ __align__(16) char smem[];
+    const int S = NSQ * Pc;
+    PhysSmem sm(smem, Lmax, S);
+    float2 *tw = sm.tw, *buf = sm.buf;
+    float2 *q = sm.wscr + (threadIdx.x >> 5) * WSCR;
+    float2 *scr = X.scratch ? X.scratch + (int64_t)blockIdx.x * X.scr_stride : nullptr;
+
+    for (int ei = blockIdx.x; ei < count; ei += gridDim.x) {
+        const int e = elems[ei];
+        const int flags = T.flags[e];
+        const bool axial = flags & EF_AXIAL;
+        const int nr = T.nr[e], lim = nr / 2 - (nr % 2 == 0);
+        const int mat = ef_mat(flags), att = SOLID ? ef_att(flags) : 0;
+        const bool tiso = SOLID && (mat == 1 || mat == 2);
+        const FftPlan &pl = X.plans[nr];
+        const int L = pl.L;
+        const bool blue = pl.kind == 1;
+        const float2 *chirp = blue ? X.f2 + pl.chirp : nullptr;
+        const float hsc = blue ? 0.5f : 0.5f / (float)nr;
+        const float *md = T.moduli + T.mofs[e];
+        const int nch = (NPE + Pc - 1) / Pc;
+        __syncthreads();  // the previous element is done with shared memory
+        for (int m = threadIdx.x; m < L; m += NT) tw[m] = X.f2[pl.tw + m];
+        if (!blue)
+            for (int m = threadIdx.x; m < nr; m += NT) sm.rev[m] = X.i32[pl.rev + m];
+
+        for (int c = 0; c < nch; c++) {
+            const int p0 = c * Pc, pc = min(Pc, NPE - p0);
+            const int ns = NSQ * pc;
+            // positions the packing does not write: the Nyquist order (even nr) and the
+            // Bluestein padding [nr, L)
+            if (nr % 2 == 0)
+                for (int s = threadIdx.x; s < ns; s += NT) buf[(int64_t)(nr / 2) * S + s] = make_float2(0.f, 0.f);
+            for (int t = threadIdx.x; t < (L - nr) * ns; t += NT)
+                buf[(int64_t)(nr + t / ns) * S + t % ns] = make_float2(0.f, 0.f);
+            // point lists of this chunk: elastic-only and attenuated
+            if (threadIdx.x == 0) {
+                int ne_ = 0, na_ = 0;
+                for (int pp = 0; pp < pc; pp++) {
+                    const int pg = p0 + pp;
+                    if (att == 1 || (att == 2 && cg4_index(pg) >= 0))
+                        sm.lst[32 + na_++] = pp;
+                    else
+                        sm.lst[ne_++] = pp;
+                }
+                sm.lst[30] = ne_;
+                sm.lst[31] = na_;
+            }
+            // ---- phase 1: Hermitian-packed strain spectra of the chunk ----
+            if (c == 0) {
+                phase_grad<SOLID>(T, P, u, e, nr, axial, tiso, chirp, buf, S, pc, scr, q);
+            } else {
+                for (int t = threadIdx.x; t < (lim + 1) * ns; t += NT) {
+                    const int a = t / ns, col = t - a * ns, pp = col / NSQ, s = col - pp * NSQ;
+                    const float2 *o = scr + ((int64_t)a * NPE + p0 + pp) * NC;
+                    zput(buf, S, col, a, nr, o[2 * s], 2 * s + 1 < NC ? o[2 * s + 1] : make_float2(0.f, 0.f), chirp);
+                }
+            }
+            __syncthreads();
+            // ---- phase 2: to the nr azimuthal samples ----
+            transform_c2r(buf, S, ns, pl, tw, X.f2);
+            // ---- phase 3: stress at every sample (SLS where attenuated) ----
+            if constexpr (SOLID) {
+                const int ne_ = sm.lst[30], na_ = sm.lst[31];
+                if (ne_ > 0) {
+                    if (mat == 0)
+                        phase_stress<0>(buf, S, nr, ne_, sm.lst, sm.rev, md, chirp, p0);
+                    else if (mat == 1)
+                        phase_stress<1>(buf, S, nr, ne_, sm.lst, sm.rev, md, chirp, p0);
+                    else
+                        phase_stress<2>(buf, S, nr, ne_, sm.lst, sm.rev, md, chirp, p0);
+                }
+                if (na_ > 0) {
+                    float *mem = T.mem + T.memofs[e];
+                    const float *am = T.attm + T.aofs[e];
+                    if (mat == 0)
+                        phase_stress_att<0>(buf, S, nr, na_, sm.lst + 32, sm.rev, md, chirp, p0, att, mem, am, sls);
+                    else if (mat == 1)
+                        phase_stress_att<1>(buf, S, nr, na_, sm.lst + 32, sm.rev, md, chirp, p0, att, mem, am, sls);
+                    else
+                        phase_stress_att<2>(buf, S, nr, na_, sm.lst + 32, sm.rev, md, chirp, p0, att, mem, am, sls);
+                }
+            } else {
+                phase_stress_fluid(buf, S, nr, pc, sm.rev, md, chirp, p0);
+            }
+            if (blue)
+                for (int t = threadIdx.x; t < (L - nr) * ns; t += NT)
+                    buf[(int64_t)(nr + t / ns) * S + t % ns] = make_float2(0.f, 0.f);
+            __syncthreads();
+            // ---- phase 4: back to orders 0..lim ----
+            transform_r2c(buf, S, ns, pl, tw, X.f2);
+            // ---- phase 5: stress spectra of all but the last chunk wait in the scratch ----
+            if (c < nch - 1) {
+                for (int t = threadIdx.x; t < (lim + 1) * ns; t += NT) {
+                    const int a = t / ns, col = t - a * ns, pp = col / NSQ, s = col - pp * NSQ;
+                    float2 A, B;
+                    zget(buf, S, col, a, nr, chirp, hsc, A, B);
+                    float2 *o = scr + ((int64_t)a * NPE + p0 + pp) * NC;
+                    o[2 * s] = A;
+                    if (2 * s + 1 < NC) o[2 * s + 1] = B;
+                }
+                __syncthreads();
+            }
+        }
+        // ---- phase 6: divergence of every order, into the element force ----
+        phase_quad<SOLID>(T, e, nr, axial, tiso, chirp, hsc, buf, S, (nch - 1) * Pc, scr, q);
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// host side
+// ------------------------------------------------------------------------------------
+void set_g_matrices_phys(const float *g_gll, const float *g_glj, cudaStream_t s) {
+    cudaMemcpyToSymbolAsync(c_G, g_gll, 25 * sizeof(float), 0, cudaMemcpyHostToDevice, s);
+    cudaMemcpyToSymbolAsync(c_G, g_glj, 25 * sizeof(float), 25 * sizeof(float), cudaMemcpyHostToDevice, s);
+}
+
+void init_phys_attributes() {
+    cudaFuncSetAttribute(k_elem_phys<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_CAP);
+    cudaFuncSetAttribute(k_elem_phys<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_CAP);
+}
+
+namespace {
+
+std::vector<int> prime_factors(int n) {
+    std::vector<int> f;
+    for (int p = 2; n > 1; p++)
+        while (n % p == 0) {
+            f.push_back(p);
+            n /= p;
+        }
+    return f;
+}
+
+// DIF radix order: prime factors above 13 first (direct passes), then radix 4, one
+// radix 2, and the odd radices in descending order.
+std::vector<int> radices(int L) {
+    std::vector<int> f = prime_factors(L), big, odd, out;
+    int n2 = 0;
+    for (int x : f) {
+        if (x == 2)
+            n2++;
+        else if (x > 13)
+            big.push_back(x);
+        else
+            odd.push_back(x);
+    }
+    std::sort(odd.rbegin(), odd.rend());
+    out = big;
+    for (int i = 0; i < n2 / 2; i++) out.push_back(4);
+    if (n2 % 2) out.push_back(2);
+    out.insert(out.end(), odd.begin(), odd.end());
+    return out;
+}
+
+// modelled cost of one length-L transform of one sequence (FP32 operations plus shared
+// traffic per pass)
+double pass_cost(int L) {
+    double c = 0;
+    for (int r : radices(L)) c += (double)L * (r == 2 ? 12 : r == 4 ? 15 : r <= 13 ? r + 8 : r + 10);
+    return c;
+}
+bool smooth13(int n) {
+    for (int p : prime_factors(n))
+        if (p > 13) return false;
+    return true;
+}
+
+// position -> frequency index after the DIF passes
+std::vector<int32_t> digit_reversal(const std::vector<int> &rad, int L) {
+    std::vector<int32_t> pos2k(L);
+    for (int k = 0; k < L; k++) {
+        int pos = 0, rem = k, Ls = L;
+        for (int r : rad) {
+            const int d = rem % r;
+            rem /= r;
+            Ls /= r;
+            pos += d * Ls;
+        }
+        pos2k[pos] = k;
+    }
+    return pos2k;
+}
+
+using cd = std::complex<double>;
+// exact (FP64) DFT with e^{-2 pi i nk/L} by recursive mixed radix
+void dft64(std::vector<cd> &x) {
+    const int L = (int)x.size();
+    if (L <= 1) return;
+    int r = 2;
+    while (L % r) r++;
+    const int m = L / r;
+    std::vector<std::vector<cd>> sub(r, std::vector<cd>(m));
+    for (int j = 0; j < m; j++)
+        for (int q = 0; q < r; q++) sub[q][j] = x[j * r + q];
+    for (auto &s : sub) dft64(s);
+    for (int k = 0; k < L; k++) {
+        cd acc = 0;
+        for (int q = 0; q < r; q++) acc += sub[q][k % m] * std::polar(1.0, -2.0 * M_PI * (double)(q * k % L) / L);
+        x[k] = acc;
+    }
+}
+
+}  // namespace
+
+FftTables build_fft_tables(const std::vector<char> &used) {
+    FftTables T;
+    const int nmax = (int)used.size() - 1;
+    T.plans.assign(std::max(nmax + 1, 1), FftPlan{});
+    std::vector<int> tw_ofs;  // by length
+    auto twiddles = [&](int L) -> int64_t {
+        if ((int)tw_ofs.size() <= L) tw_ofs.resize(L + 1, -1);
+        if (tw_ofs[L] >= 0) return tw_ofs[L];
+        tw_ofs[L] = (int)T.f2.size();
+        for (int m = 0; m < L; m++) {
+            const double th = 2.0 * M_PI * (double)m / (double)L;
+            T.f2.push_back(make_float2((float)std::cos(th), (float)std::sin(th)));
+        }
+        return tw_ofs[L];
+    };
+    for (int nr = 1; nr <= nmax; nr++) {
+        if (!used[nr]) continue;
+        FftPlan pl{};
+        // candidate Bluestein length: the cheapest 13-smooth M in [2 nr - 1, 2.3 (2 nr - 1)]
+        int M = 0;
+        double cb = 1e300;
+        if (nr > 2 && !smooth13(nr)) {
+            const int lo = 2 * nr - 1;
+            for (int m = lo; m <= lo + lo * 3 / 10; m++) {
+                if (!smooth13(m)) continue;
+                const double c = 2.0 * pass_cost(m) + 16.0 * m;
+                if (c < cb) {
+                    cb = c;
+                    M = m;
+                }
+            }
+        }
+        int bigp = 0;
+        for (int x : prime_factors(nr)) bigp = std::max(bigp, x);
+        const bool mixed_ok = bigp <= DIRECT_MAX;
+        const bool use_blue = M > 0 && (!mixed_ok || cb < pass_cost(nr));
+        pl.kind = use_blue ? 1 : 0;
+        pl.L = use_blue ? M : nr;
+        const std::vector<int> rad = radices(pl.L);
+        if ((int)rad.size() > FFT_MAXRAD) throw std::runtime_error("ax3d_finalize || ring size has too many factors");
+        pl.nrad = (int)rad.size();
+        for (size_t i = 0; i < rad.size(); i++) pl.rad[i] = rad[i];
+        pl.tw = twiddles(pl.L);
+        if (!use_blue) {
+            const std::vector<int32_t> rv = digit_reversal(rad, nr);
+            pl.rev = (int64_t)T.i32.size();
+            T.i32.insert(T.i32.end(), rv.begin(), rv.end());
+        } else {
+            // h_n = e^{i pi n^2 / nr}, n^2 reduced mod 2 nr exactly
+            std::vector<cd> h(nr);
+            for (int nn = 0; nn < nr; nn++) {
+                const int64_t r2 = ((int64_t)nn * nn) % (2 * (int64_t)nr);
+                h[nn] = std::polar(1.0, M_PI * (double)r2 / (double)nr);
+            }
+            pl.chirp = (int64_t)T.f2.size();
+            for (auto &z : h) T.f2.push_back(make_float2((float)z.real(), (float)z.imag()));
+            const std::vector<int32_t> rv = digit_reversal(rad, M);
+            for (int which = 0; which < 2; which++) {
+                // C2R kernel conj(h_m), R2C kernel h_m (with 1/nr), both / M, |m| < nr
+                std::vector<cd> b(M, 0.0);
+                for (int m = 0; m < nr; m++) {
+                    const cd v = which == 0 ? std::conj(h[m]) : h[m];
+                    b[m] = v;
+                    if (m > 0) b[M - m] = v;
+                }
+                dft64(b);
+                const double sc = which == 0 ? 1.0 / M : 1.0 / ((double)M * nr);
+                (which == 0 ? pl.bc2r : pl.br2c) = (int64_t)T.f2.size();
+                for (int pos = 0; pos < M; pos++) {
+                    const cd v = b[rv[pos]] * sc;
+                    T.f2.push_back(make_float2((float)v.real(), (float)v.imag()));
+                }
+            }
+        }
+        T.plans[nr] = pl;
+    }
+    if (T.f2.empty()) T.f2.push_back(make_float2(1.f, 0.f));
+    if (T.i32.empty()) T.i32.push_back(0);
+    return T;
+}
+
+// Points per chunk and shared memory of a bucket: all 25 points when two CTAs per SM
+// fit, else the largest chunk that does.
+void size_phys_bucket(PhysBucket &b, bool solid) {
+    const int nsq = solid ? 3 : 2;
+    for (int pc = NPE; pc >= 1; pc--) {
+        const size_t sm = phys_smem_bytes(b.L_max, nsq, pc);
+        if (sm <= SMEM_TWO || (pc == 1 && sm <= SMEM_CAP)) {
+            b.npts_chunk = pc;
+            b.smem = sm;
+            return;
+        }
+    }
+    b.npts_chunk = 0;
+}
+
+int phys_grid(const PhysBucket &b, bool solid, int num_sms) {
+    int per_sm = 0;
+    if (solid)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_elem_phys<true>, NT, b.smem);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_elem_phys<false>, NT, b.smem);
+    per_sm = std::max(per_sm, 1);
+    return std::max(1, std::min(b.count, per_sm * num_sms));
+}
+
+void launch_elem_phys(bool solid, const ElemTable &T, const PointTable &P, const float2 *u, const PhysBucket &b,
+                      const PhysTables &X, const SLS &sls, cudaStream_t s) {
+    if (b.count <= 0) return;
+    PhysTables x = X;
+    x.scratch = b.scratch;
+    x.scr_stride = b.scr_stride;
+    if (solid)
+        k_elem_phys<true><<<b.grid, NT, b.smem, s>>>(T, P, u, b.elems, b.count, b.npts_chunk, b.L_max, x, sls);
+    else
+        k_elem_phys<false><<<b.grid, NT, b.smem, s>>>(T, P, u, b.elems, b.count, b.npts_chunk, b.L_max, x, sls);
+}
+
+}  // namespace ax3d

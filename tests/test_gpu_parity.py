@@ -32,7 +32,21 @@ CASES = {
     "iso3d_fft44": dict(in3d=True, nu=21, lucky=True),
     "fluid3d_fft36": dict(fluid_layers=(1,), in3d=True, fluid3d=True, nu=16, lucky=True, mat=MAT_TISO),
     "ti3d_fft260_chunked": dict(in3d=True, mat=MAT_TISO, att=ATT_CG4, nu=128, lucky=True),
+    # ring sizes with a prime factor above 13: direct prime passes and Bluestein
+    "ti3d_cg4_direct131": dict(in3d=True, mat=MAT_TISO, att=ATT_CG4, nu=65, n_theta=2, n_r=2),
+    "iso3d_full_direct391": dict(in3d=True, att=ATT_FULL, nu=195, n_theta=2, n_r=2),
+    "ti3d_cg4_bluestein509": dict(in3d=True, mat=MAT_TISO, att=ATT_CG4, nu=254, n_theta=2, n_r=2),
+    "fluid3d_bluestein257": dict(fluid_layers=(1,), in3d=True, fluid3d=True, nu=128, mat=MAT_TISO, n_theta=2,
+                                 n_r=2),
 }
+# time-loop steps for the cases whose O(nr^2) FP64 oracle transform is slow
+STEPS = {"ti3d_fft260_chunked": 6, "ti3d_cg4_direct131": 10, "iso3d_full_direct391": 4,
+         "ti3d_cg4_bluestein509": 4, "fluid3d_bluestein257": 6}
+
+# Every transform path of the physical-space kernel: each direct-pass shape (prime
+# factors 17, 23, 37, 71, 131 and 47 x 3, 43 x 7, 17 x 23), Bluestein (257, 509) and
+# smooth sizes, with transversely isotropic moduli and CG4 attenuation.
+RING_NU = [8, 11, 18, 35, 65, 70, 100, 128, 150, 195, 254]
 
 
 def rel(a, b):
@@ -63,24 +77,39 @@ def test_compute_stiff_matches_oracle(ax3d_lib, name):
         assert rel(a, b) <= TOL, (phase, rel(a, b), rel(a, c))
 
 
+@pytest.mark.parametrize("nu", RING_NU)
+def test_compute_stiff_ring_sizes(ax3d_lib, nu):
+    from oracle.oracle_py import OracleDomain
+    from axisem3d_gb300.capi import Ax3dDomain
+    spec = synth.annulus_domain(n_theta=2, n_r=2, in3d=True, mat=MAT_TISO, att=ATT_CG4, nu=nu, seed=nu)
+    g, o = Ax3dDomain(spec), OracleDomain(spec)
+    su, _ = synth.random_fields(spec, seed=nu + 1)
+    for d in (g, o):
+        d.set("displ", "solid", su)
+        d.compute_stiff()
+        d.compute_stiff()  # second pass: the memory variables were updated by the first
+    assert rel(g.get("stiff", "solid"), o.get("stiff", "solid")) <= TOL
+
+
 @pytest.mark.parametrize("name", list(CASES))
 def test_time_loop_matches_oracle(ax3d_lib, name):
-    spec, g, o, od = _pair(name, stf_len=40, stability_interval=10)
+    n = STEPS.get(name, 40)
+    spec, g, o, _ = _pair(name, stf_len=n, stability_interval=min(10, n))
     su, fu = synth.random_fields(spec, seed=5, scale=1e-6)
-    for d in (g, o, od):
+    for d in (g, o):
         d.set("displ", "solid", su)
         if d.nfluid:
             d.set("displ", "fluid", fu)
-        d.step(40)
+        d.step(n)
     for which in ("displ", "veloc", "accel"):
         a, b = g.get(which, "solid"), o.get(which, "solid")
         assert rel(a, b) <= TOL, (which, rel(a, b))
         if g.nfluid:
             a, b = g.get(which, "fluid"), o.get(which, "fluid")
             assert rel(a, b) <= TOL, (which, "fluid", rel(a, b))
-    sa, sb = g.seismograms(0, 40), o.seismograms(0, 40)
+    sa, sb = g.seismograms(0, n), o.seismograms(0, n)
     assert rel(sa, sb) <= TOL, rel(sa, sb)
-    assert g.current_step == o.current_step == 41
+    assert g.current_step == o.current_step == n + 1
 
 
 @pytest.mark.parametrize("name", ["iso1d", "ti3d_cg4", "fluid3d_mass3d_couple3d"])
