@@ -368,7 +368,7 @@ struct ax3d_domain {
         ax3d::FftTables ft = ax3d::build_fft_tables(used);
         for (int fl = 0; fl < 2; fl++)
             for (int e : fl ? phys3_f : phys3_s) {
-                const int b = (int)std::floor(std::log((double)ft.plans[e_nr[e]].L) / std::log(1.12));
+                const int b = (int)std::floor(std::log((double)ft.plans[e_nr[e]].Lbuf) / std::log(1.12));
                 (fl ? phys_f : phys_s)[b].push_back(e);
             }
         // 3D points (Mass3D) and 3D couplings
@@ -457,7 +457,7 @@ struct ax3d_domain {
                 ax3d::PhysBucket b;
                 b.count = (int)kv.second.size();
                 for (int e : kv.second) {
-                    b.L_max = std::max(b.L_max, ft.plans[e_nr[e]].L);
+                    b.L_max = std::max(b.L_max, ft.plans[e_nr[e]].Lbuf);
                     b.n_max = std::max(b.n_max, e_nr[e] / 2 + 1);
                 }
                 ax3d::size_phys_bucket(b, !fl);

@@ -282,12 +282,10 @@ __device__ __forceinline__ void elastic(int mat, const T e[6], T s[6], M mod) {
 // R points at memvar[l=0][c=0] of this point, stride_l between SLS, stride_c between
 // components; SR (stressR) likewise.  The caller has already subtracted sum R from
 // the stress (applyToStress).
+// As sls_update, with the old stressR (sr_old) already loaded by the caller.
 template <typename T>
-__device__ __forceinline__ void sls_update(const SLS &sls, T *R, T *SR, int64_t stride_l,
-                                           int64_t stride_c, const T e[6], float dk, float dmu) {
-    T sr_old[6];
-#pragma unroll
-    for (int c = 0; c < 6; c++) sr_old[c] = SR[c * stride_c];
+__device__ __forceinline__ void sls_update_from(const SLS &sls, T *R, T *SR, int64_t stride_l, int64_t stride_c,
+                                                const T e[6], const T sr_old[6], float dk, float dmu) {
     const float third = (float)(1.0 / 3.0);
     float dk3 = 3.f * dk, dmu2 = 2.f * dmu;
     T e3 = vmul(third, vadd(vadd(e[0], e[1]), e[2]));
@@ -316,6 +314,15 @@ __device__ __forceinline__ void sls_update(const SLS &sls, T *R, T *SR, int64_t 
     }
 #pragma unroll
     for (int c = 0; c < 6; c++) SR[c * stride_c] = s[c];
+}
+
+template <typename T>
+__device__ __forceinline__ void sls_update(const SLS &sls, T *R, T *SR, int64_t stride_l,
+                                           int64_t stride_c, const T e[6], float dk, float dmu) {
+    T sr_old[6];
+#pragma unroll
+    for (int c = 0; c < 6; c++) sr_old[c] = SR[c * stride_c];
+    sls_update_from(sls, R, SR, stride_l, stride_c, e, sr_old, dk, dmu);
 }
 
 __device__ __forceinline__ int cg4_index(int p) {

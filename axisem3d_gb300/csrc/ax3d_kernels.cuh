@@ -8,16 +8,20 @@
 
 namespace ax3d {
 
-// Transform plan of one ring size nr (device table indexed by nr).  kind 0: in-place
-// mixed radix of length L = nr; kind 1: Bluestein chirp convolution of smooth length L.
+// Transform plan of one ring size nr (device table indexed by nr).
+//   kind 0: in-place mixed radix of length L = nr;
+//   kind 1: Bluestein chirp convolution of smooth length L >= 2 nr - 1;
+//   kind 2: Rader (prime nr): cyclic convolution of length L = nr - 1 over the
+//           generator-ordered spectrum, plus two slots for the zero-frequency terms.
 constexpr int FFT_MAXRAD = 12;
 struct FftPlan {
-    int32_t kind = 0, L = 1, nrad = 0, pad = 0;
-    int32_t rad[FFT_MAXRAD] = {};  // radices in decimation-in-frequency order
+    int32_t kind = 0, L = 1, nrad = 0, Lbuf = 1;  // Lbuf: buffer positions per sequence
+    int32_t rad[FFT_MAXRAD] = {};  // radices of L in decimation-in-frequency order
     int64_t tw = 0;                // L twiddles (cos, sin)(2 pi m / L) in the float2 table
-    int64_t rev = 0;               // kind 0: position -> sample map (nr int32)
+    int64_t rev = 0;               // kinds 0, 2: position -> sample map (nr int32)
+    int64_t ord = 0;               // kind 2: order -> position map (nr int32)
     int64_t chirp = 0;             // kind 1: h_n = e^{i pi n^2 / nr}, n < nr
-    int64_t bc2r = 0, br2c = 0;    // kind 1: kernel spectra (L float2, digit-reversed)
+    int64_t bc2r = 0, br2c = 0;    // kinds 1, 2: kernel spectra (L float2, digit-reversed)
 };
 struct FftTables {
     std::vector<FftPlan> plans;

@@ -138,25 +138,40 @@ __device__ __noinline__ void rad_pass(float2 *buf, int S, int ns, int L, int Ls,
             sq[qk] = w.y;
         }
     }
-    for (int t = threadIdx.x; t < total; t += blockDim.x) {
-        const int bj = (int)fdiv((uint32_t)t, fs), s = t - bj * ns;
-        const int b = (int)fdiv((uint32_t)bj, fm), j = bj - b * m;
-        float2 *p0 = buf + (int64_t)(b * Ls + j) * S + s;
-        const int64_t rs = (int64_t)m * S;
-        float2 v[R];
+    // U butterflies per iteration, their shared-memory loads issued together
+    constexpr int U = R <= 7 ? 2 : 1;
+    const int64_t rs = (int64_t)m * S;
+    for (int t0 = threadIdx.x; t0 < total; t0 += blockDim.x * U) {
+        float2 v[U][R];
+        float2 *p0[U];
+        int jj[U];
 #pragma unroll
-        for (int r = 0; r < R; r++) v[r] = p0[r * rs];
-        if (dit) {
+        for (int uu = 0; uu < U; uu++) {
+            const int t = min(t0 + uu * (int)blockDim.x, total - 1);
+            const int bj = (int)fdiv((uint32_t)t, fs), s = t - bj * ns;
+            const int b = (int)fdiv((uint32_t)bj, fm);
+            jj[uu] = bj - b * m;
+            p0[uu] = buf + (int64_t)(b * Ls + jj[uu]) * S + s;
 #pragma unroll
-            for (int r = 1; r < R; r++) v[r] = cmul(v[r], twv(tw, j * r * ts, sg));
+            for (int r = 0; r < R; r++) v[uu][r] = p0[uu][r * rs];
         }
-        butterfly<R>(v, sg > 0, cq, sq);
-        if (!dit) {
 #pragma unroll
-            for (int r = 1; r < R; r++) v[r] = cmul(v[r], twv(tw, j * r * ts, sg));
+        for (int uu = 0; uu < U; uu++) {
+            const int j = jj[uu];
+            if (dit) {
+#pragma unroll
+                for (int r = 1; r < R; r++) v[uu][r] = cmul(v[uu][r], twv(tw, j * r * ts, sg));
+            }
+            butterfly<R>(v[uu], sg > 0, cq, sq);
+            if (!dit) {
+#pragma unroll
+                for (int r = 1; r < R; r++) v[uu][r] = cmul(v[uu][r], twv(tw, j * r * ts, sg));
+            }
+            if (t0 + uu * (int)blockDim.x < total) {
+#pragma unroll
+                for (int r = 0; r < R; r++) p0[uu][r * rs] = v[uu][r];
+            }
         }
-#pragma unroll
-        for (int r = 0; r < R; r++) p0[r * rs] = v[r];
     }
 }
 
@@ -334,83 +349,154 @@ __device__ void fft_passes(float2 *buf, int S, int ns, const FftPlan &pl, const 
     }
 }
 
-__device__ void pointwise(float2 *buf, int S, int ns, int L, const float2 *__restrict__ K) {
+// buf[pos] *= K[pos] over L positions; with save >= 0 the zero-frequency sum at position
+// 0 is first kept in slot save (Rader).
+__device__ void pointwise(float2 *buf, int S, int ns, int L, const float2 *__restrict__ K, int save) {
     const FDiv fs = make_fdiv((uint32_t)ns);
     for (int t = threadIdx.x; t < L * ns; t += blockDim.x) {
         const int pos = (int)fdiv((uint32_t)t, fs), s = t - pos * ns;
-        buf[(int64_t)pos * S + s] = cmul(buf[(int64_t)pos * S + s], __ldg(K + pos));
+        const float2 v = buf[(int64_t)pos * S + s];
+        if (save >= 0 && pos == 0) buf[(int64_t)save * S + s] = v;
+        buf[(int64_t)pos * S + s] = cmul(v, __ldg(K + pos));
     }
     __syncthreads();
 }
 
-// spectrum (natural) -> samples: mixed radix leaves them digit-reversed, Bluestein natural
-// (before the post-chirp h_k, which the stress phase applies)
-__device__ void transform_c2r(float2 *buf, int S, int ns, const FftPlan &pl, const float2 *tw, const float2 *f2) {
+// spectrum -> samples: mixed radix leaves them digit-reversed, Bluestein natural (before the
+// post-chirp h_k, which the stress phase applies), Rader in generator order (before the
+// zero-frequency term, which the stress phase adds)
+__device__ void transform_c2r(float2 *buf, int S, int ns, int nr, const FftPlan &pl, const float2 *tw,
+                              const float2 *f2) {
     if (pl.kind == 0) {
         fft_passes(buf, S, ns, pl, tw, +1, false);
     } else {
         fft_passes(buf, S, ns, pl, tw, -1, false);
-        pointwise(buf, S, ns, pl.L, f2 + pl.bc2r);
+        pointwise(buf, S, ns, pl.L, f2 + pl.bc2r, pl.kind == 2 ? nr : -1);
         fft_passes(buf, S, ns, pl, tw, +1, true);
     }
 }
-// samples -> spectrum (natural); scaled by 1/nr in the extraction (mixed) or the kernel
-// spectrum (Bluestein)
-__device__ void transform_r2c(float2 *buf, int S, int ns, const FftPlan &pl, const float2 *tw, const float2 *f2) {
+// samples -> spectrum; scaled by 1/nr in the extraction (mixed radix) or in the kernel
+// spectrum (Bluestein, Rader)
+__device__ void transform_r2c(float2 *buf, int S, int ns, int nr, const FftPlan &pl, const float2 *tw,
+                              const float2 *f2) {
     if (pl.kind == 0) {
         fft_passes(buf, S, ns, pl, tw, -1, true);
     } else {
         fft_passes(buf, S, ns, pl, tw, -1, false);
-        pointwise(buf, S, ns, pl.L, f2 + pl.br2c);
+        pointwise(buf, S, ns, pl.L, f2 + pl.br2c, pl.kind == 2 ? nr - 1 : -1);
         fft_passes(buf, S, ns, pl, tw, +1, true);
     }
 }
 
+// Where an element's orders and samples live in its packed sequences.
+struct Pk {
+    int kind, nr;
+    const float2 *chirp;  // kind 1
+    const int32_t *ord;   // kind 2: order -> position
+    float inv_nr;
+};
+
 // Hermitian packing of order a of the column pair (A, B) into sequence col.
-__device__ __forceinline__ void zput(float2 *buf, int S, int col, int a, int nr, float2 A, float2 B,
-                                     const float2 *chirp) {
+__device__ __forceinline__ void zput(float2 *buf, int S, int col, int a, const Pk &k, float2 A, float2 B) {
     if (a == 0) {
-        buf[col] = make_float2(A.x, B.x);  // only Re of order 0 enters the C2R
+        // only Re of order 0 enters the C2R
+        buf[(int64_t)(k.kind == 2 ? k.nr - 1 : 0) * S + col] = make_float2(A.x, B.x);
         return;
     }
     float2 z1 = make_float2(A.x - B.y, A.y + B.x);  // A + i B
     float2 z2 = make_float2(A.x + B.y, B.x - A.y);  // conj(A) + i conj(B)
-    if (chirp) {
-        z1 = cmul(z1, __ldg(chirp + a));
-        z2 = cmul(z2, __ldg(chirp + nr - a));
+    int s1 = a, s2 = k.nr - a;
+    if (k.kind == 1) {
+        z1 = cmul(z1, __ldg(k.chirp + a));
+        z2 = cmul(z2, __ldg(k.chirp + k.nr - a));
+    } else if (k.kind == 2) {
+        s1 = __ldg(k.ord + a);
+        s2 = __ldg(k.ord + k.nr - a);
     }
-    buf[(int64_t)a * S + col] = z1;
-    buf[(int64_t)(nr - a) * S + col] = z2;
+    buf[(int64_t)s1 * S + col] = z1;
+    buf[(int64_t)s2 * S + col] = z2;
 }
 // Order a of the column pair of sequence col from the transformed spectrum (x h).
-__device__ __forceinline__ void zget(const float2 *buf, int S, int col, int a, int nr, const float2 *chirp,
-                                     float h, float2 &A, float2 &B) {
-    float2 z1 = buf[(int64_t)a * S + col];
-    float2 z2 = a == 0 ? z1 : buf[(int64_t)(nr - a) * S + col];
-    if (chirp) {
-        z1 = cmul(z1, conjf2(__ldg(chirp + a)));
-        z2 = a == 0 ? z1 : cmul(z2, conjf2(__ldg(chirp + nr - a)));
+__device__ __forceinline__ void zget(const float2 *buf, int S, int col, int a, const Pk &k, float h, float2 &A,
+                                     float2 &B) {
+    float2 z1, z2;
+    if (k.kind == 2) {
+        const float2 x0 = buf[(int64_t)k.nr * S + col];
+        if (a == 0) {
+            z1 = z2 = cscale(k.inv_nr, cadd(x0, buf[(int64_t)(k.nr - 1) * S + col]));
+        } else {
+            const float2 xs = cscale(k.inv_nr, x0);
+            z1 = cadd(buf[(int64_t)__ldg(k.ord + a) * S + col], xs);
+            z2 = cadd(buf[(int64_t)__ldg(k.ord + k.nr - a) * S + col], xs);
+        }
+    } else {
+        z1 = buf[(int64_t)a * S + col];
+        z2 = a == 0 ? z1 : buf[(int64_t)(k.nr - a) * S + col];
+        if (k.kind == 1) {
+            z1 = cmul(z1, conjf2(__ldg(k.chirp + a)));
+            z2 = a == 0 ? z1 : cmul(z2, conjf2(__ldg(k.chirp + k.nr - a)));
+        }
     }
     A = make_float2((z1.x + z2.x) * h, (z1.y - z2.y) * h);
     B = make_float2((z1.y + z2.y) * h, (z2.x - z1.x) * h);
 }
 
-// scatterDisplToElement (SolidPoint.cpp:175-195): orders above the point's Nu, and its
-// Nyquist order, read as zero.
-__device__ __forceinline__ void load_u(const PointTable &P, const float2 *u, bool solid, int pt, int a,
-                                       float2 v[3]) {
-    const int pnr = P.nr[pt];
-    const int plim = pnr / 2 - (pnr % 2 == 0);
-    v[0] = v[1] = v[2] = make_float2(0.f, 0.f);
-    if (a > plim) return;
-    if (solid) {
-        const float2 *s = u + P.sofs[pt] + (int64_t)a * 3;
-        v[0] = s[0];
-        v[1] = s[1];
-        v[2] = s[2];
-    } else {
-        v[0] = u[P.fofs[pt] + a];
+// Sample of position pos in the transformed sequences: its azimuth index k, its slot,
+// and (Bluestein) the chirp factor, (Rader) the zero-frequency slot to add.
+struct SampleAt {
+    int k, slot;
+    float2 h;
+    __device__ __forceinline__ SampleAt(int pos, const Pk &pk, const int32_t *rev) {
+        h = make_float2(1.f, 0.f);
+        if (pk.kind == 1) {
+            k = slot = pos;
+            h = __ldg(pk.chirp + pos);
+        } else {
+            k = rev[pos];
+            slot = (pk.kind == 2 && pos == pk.nr - 1) ? pk.nr : pos;
+        }
     }
+};
+__device__ __forceinline__ float2 sample_in(const float2 *buf, int S, int col, const SampleAt &sa, const Pk &pk) {
+    float2 v = buf[(int64_t)sa.slot * S + col];
+    if (pk.kind == 1) v = cmul(v, sa.h);
+    if (pk.kind == 2) v = cadd(v, buf[(int64_t)(pk.nr - 1) * S + col]);
+    return v;
+}
+__device__ __forceinline__ void sample_out(float2 *buf, int S, int col, const SampleAt &sa, const Pk &pk, float2 v) {
+    buf[(int64_t)sa.slot * S + col] = pk.kind == 1 ? cmul(v, conjf2(sa.h)) : v;
+}
+
+// scatterDisplToElement (SolidPoint.cpp:175-195): orders above the point's Nu, and its
+// Nyquist order, read as zero.  The point's block and order limit are read once.
+struct USrc {
+    const float2 *base;
+    int plim;
+    __device__ void init(const PointTable &P, const float2 *u, bool solid, int pt) {
+        const int pnr = P.nr[pt];
+        plim = pnr / 2 - (pnr % 2 == 0);
+        base = u + (solid ? P.sofs[pt] : P.fofs[pt]);
+    }
+    __device__ __forceinline__ void load(bool solid, int a, float2 v[3]) const {
+        v[0] = v[1] = v[2] = make_float2(0.f, 0.f);
+        if (a > plim) return;
+        if (solid) {
+            const float2 *s = base + (int64_t)a * 3;
+            v[0] = s[0];
+            v[1] = s[1];
+            v[2] = s[2];
+        } else {
+            v[0] = base[a];
+        }
+    }
+};
+
+// Ask L2 for [ptr, ptr + bytes) ahead of a phase that reads it in scattered order.
+__device__ __forceinline__ void prefetch_l2(const void *ptr, int64_t bytes) {
+    const char *c = static_cast<const char *>(ptr);
+    const int64_t first = reinterpret_cast<uintptr_t>(c) & 127;
+    for (int64_t o = (int64_t)threadIdx.x * 128 - first; o < bytes; o += (int64_t)blockDim.x * 128)
+        if (o >= 0) asm volatile("prefetch.global.L2 [%0];" ::"l"(c + o));
 }
 
 // Divergence of one Fourier order (computeQuad6, Gradient.cpp:267-317) with one
@@ -503,7 +589,7 @@ namespace {
 // points of the chunk go into the packed sequences, the others into the scratch.
 template <bool SOLID>
 __device__ __noinline__ void phase_grad(const ElemTable &T, const PointTable &P, const float2 *u, int e, int nr,
-                                        bool axial, bool tiso, const float2 *chirp, float2 *buf, int S, int pc,
+                                        bool axial, bool tiso, const Pk pk, float2 *buf, int S, int pc,
                                         float2 *scr, float2 *q) {
     constexpr int NSQ = SOLID ? 3 : 2;
     constexpr int NC = SOLID ? 6 : 3;
@@ -523,9 +609,14 @@ __device__ __noinline__ void phase_grad(const ElemTable &T, const PointTable &P,
         s2 = tr[50 + p];
         c2 = tr[75 + p];
     }
-    const int pt_me = T.pts[e * NPE + p];
-    float2 un[3];
-    if (active && warp < n) load_u(P, u, SOLID, pt_me, warp, un);
+    USrc us;
+    us.init(P, u, SOLID, T.pts[e * NPE + p]);
+    // displacement of orders a and a + NW in flight while order a is differentiated
+    float2 un[3], un2[3];
+    if (active) {
+        us.load(SOLID, warp, un);
+        us.load(SOLID, warp + NW, un2);
+    }
     for (int a = warp; a < n; a += NW) {
         if (active) {
             q[p] = un[0];
@@ -533,7 +624,9 @@ __device__ __noinline__ void phase_grad(const ElemTable &T, const PointTable &P,
                 q[25 + p] = un[1];
                 q[50 + p] = un[2];
             }
-            if (a + NW < n) load_u(P, u, SOLID, pt_me, a + NW, un);  // prefetch
+#pragma unroll
+            for (int i = 0; i < 3; i++) un[i] = un2[i];
+            us.load(SOLID, a + 2 * NW, un2);
         }
         __syncwarp();
         if (active && a <= lim) {
@@ -547,8 +640,7 @@ __device__ __noinline__ void phase_grad(const ElemTable &T, const PointTable &P,
             if (p < pc) {
 #pragma unroll
                 for (int s = 0; s < NSQ; s++)
-                    zput(buf, S, NSQ * p + s, a, nr, eps[2 * s], 2 * s + 1 < NC ? eps[2 * s + 1] : make_float2(0.f, 0.f),
-                         chirp);
+                    zput(buf, S, NSQ * p + s, a, pk, eps[2 * s], 2 * s + 1 < NC ? eps[2 * s + 1] : make_float2(0.f, 0.f));
             } else {
                 float2 *o = scr + ((int64_t)a * NPE + p) * NC;
 #pragma unroll
@@ -559,75 +651,110 @@ __device__ __noinline__ void phase_grad(const ElemTable &T, const PointTable &P,
     }
 }
 
-// Phase 3, points without memory variables: elastic stress at every sample.
+// Phase 3, points without memory variables: elastic stress at every sample.  Each thread
+// takes IT items and issues all their modulus loads before any arithmetic.
 template <int MAT>
 __device__ __noinline__ void phase_stress(float2 *buf, int S, int nr, int ne_, const int32_t *lst, const int32_t *rev,
-                                          const float *md, const float2 *chirp, int p0) {
-    for (int t = threadIdx.x; t < nr * ne_; t += blockDim.x) {
-        const int pos = t / ne_, pp = lst[t - pos * ne_], pg = p0 + pp;
-        const int k = chirp ? pos : rev[pos];
-        float2 *z = buf + (int64_t)pos * S + 3 * pp;
-        const float2 hk = chirp ? __ldg(chirp + k) : make_float2(1.f, 0.f);
-        float2 zz[3];
+                                          const float *md, const Pk pk, int p0) {
+    constexpr int NM = MAT == 0 ? 2 : MAT == 1 ? 5 : 21;
+    constexpr int IT = MAT == 2 ? 1 : 4;
+    const int total = nr * ne_;
+    for (int t0 = threadIdx.x; t0 < total; t0 += blockDim.x * IT) {
+        float mv[IT][NM];
+        int kk[IT];
 #pragma unroll
-        for (int s = 0; s < 3; s++) zz[s] = chirp ? cmul(z[s], hk) : z[s];
-        const float e6[6] = {zz[0].x, zz[0].y, zz[1].x, zz[1].y, zz[2].x, zz[2].y};
-        float s6[6];
-        elastic(MAT, e6, s6, [&](int mm) { return __ldg(md + ((int64_t)mm * nr + k) * NPE + pg); });
+        for (int i = 0; i < IT; i++) {
+            const int t = min(t0 + i * (int)blockDim.x, total - 1);
+            const int pos = t / ne_, pg = p0 + lst[t - pos * ne_];
+            kk[i] = pk.kind == 1 ? pos : rev[pos];
 #pragma unroll
-        for (int s = 0; s < 3; s++) {
-            const float2 o = make_float2(s6[2 * s], s6[2 * s + 1]);
-            z[s] = chirp ? cmul(o, conjf2(hk)) : o;
+            for (int mm = 0; mm < NM; mm++) mv[i][mm] = __ldg(md + ((int64_t)mm * nr + kk[i]) * NPE + pg);
+        }
+#pragma unroll
+        for (int i = 0; i < IT; i++) {
+            const int t = t0 + i * (int)blockDim.x;
+            if (t >= total) break;
+            const int pos = t / ne_, pp = lst[t - pos * ne_];
+            const SampleAt sa(pos, pk, rev);
+            float2 zz[3];
+#pragma unroll
+            for (int s = 0; s < 3; s++) zz[s] = sample_in(buf, S, 3 * pp + s, sa, pk);
+            const float e6[6] = {zz[0].x, zz[0].y, zz[1].x, zz[1].y, zz[2].x, zz[2].y};
+            float s6[6];
+            elastic(MAT, e6, s6, [&](int mm) { return mv[i][mm]; });
+#pragma unroll
+            for (int s = 0; s < 3; s++) sample_out(buf, S, 3 * pp + s, sa, pk, make_float2(s6[2 * s], s6[2 * s + 1]));
         }
     }
 }
 
 // Phase 3, attenuated points: elastic stress minus the memory variables (applyToStress),
 // then updateMemoryVariables (Attenuation3D_Full.cpp:16-50, Attenuation3D_CG4.cpp:16-62).
+// Two items per thread with their loads issued together.
 template <int MAT>
 __device__ __noinline__ void phase_stress_att(float2 *buf, int S, int nr, int na_, const int32_t *lst,
-                                              const int32_t *rev, const float *md, const float2 *chirp, int p0,
+                                              const int32_t *rev, const float *md, const Pk pk, int p0,
                                               int att, float *mem, const float *am, const SLS &sls) {
+    constexpr int NM = MAT == 0 ? 2 : MAT == 1 ? 5 : 21;
+    constexpr int IT = MAT == 2 ? 1 : 2;
     const int npa = att == 2 ? 4 : NPE;
     const int64_t sl = (int64_t)nr * 6 * npa;
-    for (int t = threadIdx.x; t < nr * na_; t += blockDim.x) {
-        const int pos = t / na_, pp = lst[t - pos * na_], pg = p0 + pp;
-        const int qq = att == 2 ? cg4_index(pg) : pg;
-        const int k = chirp ? pos : rev[pos];
-        float2 *z = buf + (int64_t)pos * S + 3 * pp;
-        const float2 hk = chirp ? __ldg(chirp + k) : make_float2(1.f, 0.f);
-        float2 zz[3];
+    const int total = nr * na_;
+    const int nsls = sls.nsls;
+    for (int t0 = threadIdx.x; t0 < total; t0 += blockDim.x * IT) {
+        float mv[IT][NM], rs[IT][6], sr[IT][6], dk[IT], dm[IT];
+        int kk[IT], qq[IT];
 #pragma unroll
-        for (int s = 0; s < 3; s++) zz[s] = chirp ? cmul(z[s], hk) : z[s];
-        const float e6[6] = {zz[0].x, zz[0].y, zz[1].x, zz[1].y, zz[2].x, zz[2].y};
-        float s6[6];
-        elastic(MAT, e6, s6, [&](int mm) { return __ldg(md + ((int64_t)mm * nr + k) * NPE + pg); });
-        float *R = mem + (int64_t)k * 6 * npa + qq;
-        float *SR = R + sls.nsls * sl;
-        for (int l = 0; l < sls.nsls; l++)
+        for (int i = 0; i < IT; i++) {
+            const int t = min(t0 + i * (int)blockDim.x, total - 1);
+            const int pos = t / na_, pg = p0 + lst[t - pos * na_];
+            qq[i] = att == 2 ? cg4_index(pg) : pg;
+            kk[i] = pk.kind == 1 ? pos : rev[pos];
 #pragma unroll
-            for (int i = 0; i < 6; i++) s6[i] -= R[l * sl + i * npa];
-        sls_update(sls, R, SR, sl, (int64_t)npa, e6, am[(int64_t)k * npa + qq],
-                   am[(int64_t)nr * npa + (int64_t)k * npa + qq]);
+            for (int mm = 0; mm < NM; mm++) mv[i][mm] = __ldg(md + ((int64_t)mm * nr + kk[i]) * NPE + pg);
+            const float *R = mem + (int64_t)kk[i] * 6 * npa + qq[i];
 #pragma unroll
-        for (int s = 0; s < 3; s++) {
-            const float2 o = make_float2(s6[2 * s], s6[2 * s + 1]);
-            z[s] = chirp ? cmul(o, conjf2(hk)) : o;
+            for (int c = 0; c < 6; c++) {
+                sr[i][c] = R[nsls * sl + c * npa];
+                rs[i][c] = 0.f;
+            }
+            for (int l = 0; l < nsls; l++)
+#pragma unroll
+                for (int c = 0; c < 6; c++) rs[i][c] += R[l * sl + c * npa];
+            dk[i] = am[(int64_t)kk[i] * npa + qq[i]];
+            dm[i] = am[(int64_t)nr * npa + (int64_t)kk[i] * npa + qq[i]];
+        }
+#pragma unroll
+        for (int i = 0; i < IT; i++) {
+            const int t = t0 + i * (int)blockDim.x;
+            if (t >= total) break;
+            const int pos = t / na_, pp = lst[t - pos * na_];
+            const SampleAt sa(pos, pk, rev);
+            float2 zz[3];
+#pragma unroll
+            for (int s = 0; s < 3; s++) zz[s] = sample_in(buf, S, 3 * pp + s, sa, pk);
+            const float e6[6] = {zz[0].x, zz[0].y, zz[1].x, zz[1].y, zz[2].x, zz[2].y};
+            float s6[6];
+            elastic(MAT, e6, s6, [&](int mm) { return mv[i][mm]; });
+#pragma unroll
+            for (int c = 0; c < 6; c++) s6[c] -= rs[i][c];
+            float *R = mem + (int64_t)kk[i] * 6 * npa + qq[i];
+            sls_update_from(sls, R, R + nsls * sl, sl, (int64_t)npa, e6, sr[i], dk[i], dm[i]);
+#pragma unroll
+            for (int s = 0; s < 3; s++) sample_out(buf, S, 3 * pp + s, sa, pk, make_float2(s6[2 * s], s6[2 * s + 1]));
         }
     }
 }
 
 // Phase 3 of a fluid element: sigma_i = K d_i chi (Acoustic3D.cpp:9-16) at every sample.
 __device__ __noinline__ void phase_stress_fluid(float2 *buf, int S, int nr, int pc, const int32_t *rev,
-                                                const float *md, const float2 *chirp, int p0) {
+                                                const float *md, const Pk pk, int p0) {
     for (int t = threadIdx.x; t < nr * pc; t += blockDim.x) {
         const int pos = t / pc, pp = t - pos * pc;
-        const int k = chirp ? pos : rev[pos];
-        float2 *z = buf + (int64_t)pos * S + 2 * pp;
-        const float K = __ldg(md + (int64_t)k * NPE + p0 + pp);
-        // the chirp factors h_k conj(h_k) cancel around a real scaling
-        z[0] = cscale(K, z[0]);
-        z[1] = cscale(K, z[1]);
+        const SampleAt sa(pos, pk, rev);
+        const float K = __ldg(md + (int64_t)sa.k * NPE + p0 + pp);
+#pragma unroll
+        for (int s = 0; s < 2; s++) sample_out(buf, S, 2 * pp + s, sa, pk, cscale(K, sample_in(buf, S, 2 * pp + s, sa, pk)));
     }
 }
 
@@ -636,7 +763,7 @@ __device__ __noinline__ void phase_stress_fluid(float2 *buf, int S, int nr, int 
 // sequences, the earlier chunks' from the scratch.
 template <bool SOLID>
 __device__ __noinline__ void phase_quad(const ElemTable &T, int e, int nr, bool axial, bool tiso,
-                                        const float2 *chirp, float hsc, const float2 *buf, int S, int pl0,
+                                        const Pk pk, float hsc, const float2 *buf, int S, int pl0,
                                         const float2 *scr, float2 *q) {
     constexpr int NSQ = SOLID ? 3 : 2;
     constexpr int NC = SOLID ? 6 : 3;
@@ -666,7 +793,7 @@ __device__ __noinline__ void phase_quad(const ElemTable &T, int e, int nr, bool 
 #pragma unroll
                 for (int s = 0; s < NSQ; s++) {
                     float2 A, B;
-                    zget(buf, S, NSQ * (p - pl0) + s, a, nr, chirp, hsc, A, B);
+                    zget(buf, S, NSQ * (p - pl0) + s, a, pk, hsc, A, B);
                     sig[2 * s] = A;
                     if (2 * s + 1 < NC) sig[2 * s + 1] = B;
                 }
@@ -723,10 +850,15 @@ __global__ void __launch_bounds__(NT, 2)
         const int mat = ef_mat(flags), att = SOLID ? ef_att(flags) : 0;
         const bool tiso = SOLID && (mat == 1 || mat == 2);
         const FftPlan &pl = X.plans[nr];
-        const int L = pl.L;
+        const int L = pl.L, Lb = pl.Lbuf;
         const bool blue = pl.kind == 1;
-        const float2 *chirp = blue ? X.f2 + pl.chirp : nullptr;
-        const float hsc = blue ? 0.5f : 0.5f / (float)nr;
+        Pk pk;
+        pk.kind = pl.kind;
+        pk.nr = nr;
+        pk.chirp = X.f2 + pl.chirp;
+        pk.ord = X.i32 + pl.ord;
+        pk.inv_nr = 1.f / (float)nr;
+        const float hsc = pl.kind == 0 ? 0.5f / (float)nr : 0.5f;
         const float *md = T.moduli + T.mofs[e];
         const int nch = (NPE + Pc - 1) / Pc;
         __syncthreads();  // the previous element is done with shared memory
@@ -741,8 +873,9 @@ __global__ void __launch_bounds__(NT, 2)
             // Bluestein padding [nr, L)
             if (nr % 2 == 0)
                 for (int s = threadIdx.x; s < ns; s += NT) buf[(int64_t)(nr / 2) * S + s] = make_float2(0.f, 0.f);
-            for (int t = threadIdx.x; t < (L - nr) * ns; t += NT)
-                buf[(int64_t)(nr + t / ns) * S + t % ns] = make_float2(0.f, 0.f);
+            if (blue)
+                for (int t = threadIdx.x; t < (Lb - nr) * ns; t += NT)
+                    buf[(int64_t)(nr + t / ns) * S + t % ns] = make_float2(0.f, 0.f);
             // point lists of this chunk: elastic-only and attenuated
             if (threadIdx.x == 0) {
                 int ne_ = 0, na_ = 0;
@@ -758,53 +891,61 @@ __global__ void __launch_bounds__(NT, 2)
             }
             // ---- phase 1: Hermitian-packed strain spectra of the chunk ----
             if (c == 0) {
-                phase_grad<SOLID>(T, P, u, e, nr, axial, tiso, chirp, buf, S, pc, scr, q);
+                phase_grad<SOLID>(T, P, u, e, nr, axial, tiso, pk, buf, S, pc, scr, q);
             } else {
                 for (int t = threadIdx.x; t < (lim + 1) * ns; t += NT) {
                     const int a = t / ns, col = t - a * ns, pp = col / NSQ, s = col - pp * NSQ;
                     const float2 *o = scr + ((int64_t)a * NPE + p0 + pp) * NC;
-                    zput(buf, S, col, a, nr, o[2 * s], 2 * s + 1 < NC ? o[2 * s + 1] : make_float2(0.f, 0.f), chirp);
+                    zput(buf, S, col, a, pk, o[2 * s], 2 * s + 1 < NC ? o[2 * s + 1] : make_float2(0.f, 0.f));
                 }
             }
             __syncthreads();
             // ---- phase 2: to the nr azimuthal samples ----
-            transform_c2r(buf, S, ns, pl, tw, X.f2);
+            transform_c2r(buf, S, ns, nr, pl, tw, X.f2);
             // ---- phase 3: stress at every sample (SLS where attenuated) ----
             if constexpr (SOLID) {
                 const int ne_ = sm.lst[30], na_ = sm.lst[31];
+                if (c == 0) {
+                    prefetch_l2(md, (int64_t)4 * NPE * nr * (mat == 0 ? 2 : mat == 1 ? 5 : 21));
+                    if (att) {
+                        const int npa = att == 2 ? 4 : NPE;
+                        prefetch_l2(T.mem + T.memofs[e], (int64_t)4 * (sls.nsls + 1) * nr * 6 * npa);
+                        prefetch_l2(T.attm + T.aofs[e], (int64_t)4 * 2 * nr * npa);
+                    }
+                }
                 if (ne_ > 0) {
                     if (mat == 0)
-                        phase_stress<0>(buf, S, nr, ne_, sm.lst, sm.rev, md, chirp, p0);
+                        phase_stress<0>(buf, S, nr, ne_, sm.lst, sm.rev, md, pk, p0);
                     else if (mat == 1)
-                        phase_stress<1>(buf, S, nr, ne_, sm.lst, sm.rev, md, chirp, p0);
+                        phase_stress<1>(buf, S, nr, ne_, sm.lst, sm.rev, md, pk, p0);
                     else
-                        phase_stress<2>(buf, S, nr, ne_, sm.lst, sm.rev, md, chirp, p0);
+                        phase_stress<2>(buf, S, nr, ne_, sm.lst, sm.rev, md, pk, p0);
                 }
                 if (na_ > 0) {
                     float *mem = T.mem + T.memofs[e];
                     const float *am = T.attm + T.aofs[e];
                     if (mat == 0)
-                        phase_stress_att<0>(buf, S, nr, na_, sm.lst + 32, sm.rev, md, chirp, p0, att, mem, am, sls);
+                        phase_stress_att<0>(buf, S, nr, na_, sm.lst + 32, sm.rev, md, pk, p0, att, mem, am, sls);
                     else if (mat == 1)
-                        phase_stress_att<1>(buf, S, nr, na_, sm.lst + 32, sm.rev, md, chirp, p0, att, mem, am, sls);
+                        phase_stress_att<1>(buf, S, nr, na_, sm.lst + 32, sm.rev, md, pk, p0, att, mem, am, sls);
                     else
-                        phase_stress_att<2>(buf, S, nr, na_, sm.lst + 32, sm.rev, md, chirp, p0, att, mem, am, sls);
+                        phase_stress_att<2>(buf, S, nr, na_, sm.lst + 32, sm.rev, md, pk, p0, att, mem, am, sls);
                 }
             } else {
-                phase_stress_fluid(buf, S, nr, pc, sm.rev, md, chirp, p0);
+                phase_stress_fluid(buf, S, nr, pc, sm.rev, md, pk, p0);
             }
             if (blue)
-                for (int t = threadIdx.x; t < (L - nr) * ns; t += NT)
+                for (int t = threadIdx.x; t < (Lb - nr) * ns; t += NT)
                     buf[(int64_t)(nr + t / ns) * S + t % ns] = make_float2(0.f, 0.f);
             __syncthreads();
             // ---- phase 4: back to orders 0..lim ----
-            transform_r2c(buf, S, ns, pl, tw, X.f2);
+            transform_r2c(buf, S, ns, nr, pl, tw, X.f2);
             // ---- phase 5: stress spectra of all but the last chunk wait in the scratch ----
             if (c < nch - 1) {
                 for (int t = threadIdx.x; t < (lim + 1) * ns; t += NT) {
                     const int a = t / ns, col = t - a * ns, pp = col / NSQ, s = col - pp * NSQ;
                     float2 A, B;
-                    zget(buf, S, col, a, nr, chirp, hsc, A, B);
+                    zget(buf, S, col, a, pk, hsc, A, B);
                     float2 *o = scr + ((int64_t)a * NPE + p0 + pp) * NC;
                     o[2 * s] = A;
                     if (2 * s + 1 < NC) o[2 * s + 1] = B;
@@ -813,7 +954,7 @@ __global__ void __launch_bounds__(NT, 2)
             }
         }
         // ---- phase 6: divergence of every order, into the element force ----
-        phase_quad<SOLID>(T, e, nr, axial, tiso, chirp, hsc, buf, S, (nch - 1) * Pc, scr, q);
+        phase_quad<SOLID>(T, e, nr, axial, tiso, pk, hsc, buf, S, (nch - 1) * Pc, scr, q);
     }
 }
 
@@ -928,39 +1069,58 @@ FftTables build_fft_tables(const std::vector<char> &used) {
         }
         return tw_ofs[L];
     };
+    // FP64 kernel spectrum of the cyclic sequence b (length M), / scale, digit-reversed
+    auto kernel_spectrum = [&](std::vector<cd> b, const std::vector<int32_t> &rv, double scale) -> int64_t {
+        dft64(b);
+        const int64_t ofs = (int64_t)T.f2.size();
+        for (size_t pos = 0; pos < b.size(); pos++) {
+            const cd v = b[rv[pos]] / scale;
+            T.f2.push_back(make_float2((float)v.real(), (float)v.imag()));
+        }
+        return ofs;
+    };
     for (int nr = 1; nr <= nmax; nr++) {
         if (!used[nr]) continue;
         FftPlan pl{};
-        // candidate Bluestein length: the cheapest 13-smooth M in [2 nr - 1, 2.3 (2 nr - 1)]
+        const std::vector<int> fac = prime_factors(nr);
+        const int bigp = fac.empty() ? 1 : fac.back();
+        // candidates: mixed radix (direct passes for primes up to DIRECT_MAX), Bluestein
+        // (the cheapest 13-smooth M in [2 nr - 1, 1.3 (2 nr - 1)]) and, for a prime nr,
+        // Rader over the length nr - 1
+        const double c_mixed = bigp <= DIRECT_MAX ? pass_cost(nr) : 1e300;
         int M = 0;
-        double cb = 1e300;
+        double c_blue = 1e300;
         if (nr > 2 && !smooth13(nr)) {
             const int lo = 2 * nr - 1;
             for (int m = lo; m <= lo + lo * 3 / 10; m++) {
                 if (!smooth13(m)) continue;
                 const double c = 2.0 * pass_cost(m) + 16.0 * m;
-                if (c < cb) {
-                    cb = c;
+                if (c < c_blue) {
+                    c_blue = c;
                     M = m;
                 }
             }
         }
-        int bigp = 0;
-        for (int x : prime_factors(nr)) bigp = std::max(bigp, x);
-        const bool mixed_ok = bigp <= DIRECT_MAX;
-        const bool use_blue = M > 0 && (!mixed_ok || cb < pass_cost(nr));
-        pl.kind = use_blue ? 1 : 0;
-        pl.L = use_blue ? M : nr;
+        const bool prime = nr > 13 && fac.size() == 1;
+        double c_rader = 1e300;
+        if (prime) {
+            int big1 = 1;
+            for (int x : prime_factors(nr - 1)) big1 = std::max(big1, x);
+            if (big1 <= DIRECT_MAX) c_rader = 2.0 * pass_cost(nr - 1) + 16.0 * nr;
+        }
+        pl.kind = c_rader < std::min(c_mixed, c_blue) ? 2 : c_blue < c_mixed ? 1 : 0;
+        pl.L = pl.kind == 0 ? nr : pl.kind == 1 ? M : nr - 1;
+        pl.Lbuf = pl.kind == 2 ? nr + 1 : pl.L;
         const std::vector<int> rad = radices(pl.L);
         if ((int)rad.size() > FFT_MAXRAD) throw std::runtime_error("ax3d_finalize || ring size has too many factors");
         pl.nrad = (int)rad.size();
         for (size_t i = 0; i < rad.size(); i++) pl.rad[i] = rad[i];
         pl.tw = twiddles(pl.L);
-        if (!use_blue) {
-            const std::vector<int32_t> rv = digit_reversal(rad, nr);
+        const std::vector<int32_t> rv = digit_reversal(rad, pl.L);
+        if (pl.kind == 0) {
             pl.rev = (int64_t)T.i32.size();
             T.i32.insert(T.i32.end(), rv.begin(), rv.end());
-        } else {
+        } else if (pl.kind == 1) {
             // h_n = e^{i pi n^2 / nr}, n^2 reduced mod 2 nr exactly
             std::vector<cd> h(nr);
             for (int nn = 0; nn < nr; nn++) {
@@ -969,23 +1129,51 @@ FftTables build_fft_tables(const std::vector<char> &used) {
             }
             pl.chirp = (int64_t)T.f2.size();
             for (auto &z : h) T.f2.push_back(make_float2((float)z.real(), (float)z.imag()));
-            const std::vector<int32_t> rv = digit_reversal(rad, M);
+            // C2R kernel conj(h_m), R2C kernel h_m (with 1/nr), |m| < nr, cyclic in M
             for (int which = 0; which < 2; which++) {
-                // C2R kernel conj(h_m), R2C kernel h_m (with 1/nr), both / M, |m| < nr
                 std::vector<cd> b(M, 0.0);
                 for (int m = 0; m < nr; m++) {
                     const cd v = which == 0 ? std::conj(h[m]) : h[m];
                     b[m] = v;
                     if (m > 0) b[M - m] = v;
                 }
-                dft64(b);
-                const double sc = which == 0 ? 1.0 / M : 1.0 / ((double)M * nr);
-                (which == 0 ? pl.bc2r : pl.br2c) = (int64_t)T.f2.size();
-                for (int pos = 0; pos < M; pos++) {
-                    const cd v = b[rv[pos]] * sc;
-                    T.f2.push_back(make_float2((float)v.real(), (float)v.imag()));
-                }
+                (which == 0 ? pl.bc2r : pl.br2c) = kernel_spectrum(b, rv, which == 0 ? M : (double)M * nr);
             }
+        } else {
+            // Rader with the smallest primitive root g: order a = g^-m at position m, order 0
+            // at position nr - 1; sample k = g^q at position q, sample 0 at position nr
+            const int P = nr - 1;
+            std::vector<int> pf1 = prime_factors(P);
+            pf1.erase(std::unique(pf1.begin(), pf1.end()), pf1.end());
+            int g = 2;
+            for (;; g++) {
+                bool ok = true;
+                for (int q : pf1) {
+                    int64_t r = 1, b = g, ex = P / q;
+                    for (; ex; ex >>= 1, b = b * b % nr)
+                        if (ex & 1) r = r * b % nr;
+                    if (r == 1) ok = false;
+                }
+                if (ok) break;
+            }
+            std::vector<int32_t> gpow(P), ord(nr), samp(nr);
+            for (int q = 0, x = 1; q < P; q++, x = (int)((int64_t)x * g % nr)) gpow[q] = x;
+            ord[0] = nr - 1;
+            for (int q = 0; q < P; q++) ord[gpow[q]] = (P - q) % P;
+            for (int q = 0; q < P; q++) samp[q] = gpow[q];
+            samp[P] = 0;
+            pl.rev = (int64_t)T.i32.size();
+            T.i32.insert(T.i32.end(), samp.begin(), samp.end());
+            pl.ord = (int64_t)T.i32.size();
+            T.i32.insert(T.i32.end(), ord.begin(), ord.end());
+            // C2R kernel w^{g^j}, R2C kernel w^{-g^{-j}} (with 1/nr), w = e^{2 pi i / nr}
+            std::vector<cd> bc(P), br(P);
+            for (int j = 0; j < P; j++) {
+                bc[j] = std::polar(1.0, 2.0 * M_PI * (double)gpow[j] / nr);
+                br[j] = std::polar(1.0, -2.0 * M_PI * (double)gpow[(P - j) % P] / nr);
+            }
+            pl.bc2r = kernel_spectrum(bc, rv, (double)P);
+            pl.br2c = kernel_spectrum(br, rv, (double)P * nr);
         }
         T.plans[nr] = pl;
     }
