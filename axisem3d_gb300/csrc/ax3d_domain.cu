@@ -115,7 +115,6 @@ struct ax3d_domain {
     DevBuf<float2> d_ef, d_f2;
     DevBuf<int32_t> d_i32;
     DevBuf<ax3d::FftPlan> d_plans;
-    std::vector<DevBuf<float2>> bucket_scratch;
     ax3d::PhysTables X{};
     DevBuf<float2> d_su, d_sv, d_sa, d_ss, d_sku, d_skv, d_fu, d_fv, d_fa, d_fs, d_fku, d_fkv;
     DevBuf<int2> d_items_s, d_items_f;
@@ -443,8 +442,6 @@ struct ax3d_domain {
         nitems_s = (int)items_s.size();
         nitems_f = (int)items_f.size();
         bucket_lists.resize(phys_s.size() + phys_f.size());
-        bucket_scratch.clear();
-        bucket_scratch.resize(phys_s.size() + phys_f.size());
         buckets_s.clear();
         buckets_f.clear();
         int num_sms = 0;
@@ -464,11 +461,6 @@ struct ax3d_domain {
                 if (b.npts_chunk <= 0)
                     throw Error(AX3D_ERR_UNSUPPORTED, "ax3d_finalize || nr too large for the physical-space kernel");
                 b.grid = ax3d::phys_grid(b, !fl, num_sms);
-                if (b.npts_chunk < 25) {
-                    b.scr_stride = (int64_t)25 * (fl ? 3 : 6) * b.n_max;
-                    bucket_scratch[bi].alloc((size_t)b.grid * b.scr_stride);
-                    b.scratch = bucket_scratch[bi].p;
-                }
                 bucket_lists[bi].upload(kv.second, st);
                 b.elems = bucket_lists[bi].p;
                 bi++;

@@ -28,13 +28,11 @@ struct FftTables {
     std::vector<float2> f2;
     std::vector<int32_t> i32;
 };
-// Device view of the transform tables plus the scratch of one bucket.
+// Device view of the transform tables.
 struct PhysTables {
     const FftPlan *plans = nullptr;
     const float2 *f2 = nullptr;
     const int32_t *i32 = nullptr;
-    float2 *scratch = nullptr;  // [grid][scr_stride] when elements go through in chunks
-    int64_t scr_stride = 0;
 };
 
 struct PhysBucket {
@@ -42,11 +40,10 @@ struct PhysBucket {
     int count = 0;
     int L_max = 0;             // longest transform in the bucket
     int n_max = 0;             // most Fourier orders in the bucket
-    int npts_chunk = 25;       // GLL points per pass (shared-memory budget)
+    int npts_chunk = 25;       // GLL points per CTA (shared-memory budget)
+    int csize = 1;             // CTAs per cluster sharing one element
     size_t smem = 0;
-    int grid = 0;              // persistent CTAs
-    float2 *scratch = nullptr;
-    int64_t scr_stride = 0;
+    int grid = 0;              // persistent CTAs (a multiple of csize)
 };
 
 // Sets the text ax3d_last_error returns on this thread.

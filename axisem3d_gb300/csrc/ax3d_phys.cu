@@ -25,16 +25,22 @@
 //    convolution of smooth length M >= 2 nr - 1, with the same passes and the chirp
 //    kernel's spectrum stored in digit-reversed order.
 // All twiddles, chirps and kernel spectra are computed in FP64 on the host.
-// When an element's sequences do not fit in shared memory its GLL points go through in
-// chunks; the strain of later chunks and the stress of earlier ones wait in a per-CTA
-// global scratch (L2-resident), so the gradient and the divergence run once per element.
+// When an element's sequences do not fit in one CTA's shared memory, a thread-block
+// cluster of C CTAs (on C SMs) shares it: CTA r holds the sequences of GLL points
+// [r Pc, (r + 1) Pc) and transforms them; the gradient and the divergence are split over
+// the cluster by Fourier order and write / read the owning CTA's shared memory through
+// distributed shared memory, so nothing leaves the chip between them.
 #include <algorithm>
 #include <cmath>
 #include <complex>
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "ax3d_elem_ops.cuh"
 #include "ax3d_kernels.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace ax3d {
 
@@ -47,6 +53,8 @@ constexpr int RESEED = 8;    // direct DFT: exact twiddle reload interval
 constexpr int DIRECT_MAX = 513;  // largest prime handled by a direct pass
 constexpr size_t SMEM_CAP = 227 * 1024;
 constexpr size_t SMEM_TWO = 112 * 1024;  // two CTAs per SM
+constexpr int64_t PREFETCH_MAX = 256 * 1024;  // largest per-element block asked of L2 ahead
+constexpr int CLUSTER_MAX = 8;
 
 // n / d for n < 2^32 by multiply-high (round-up method of Granlund and Montgomery)
 struct FDiv {
@@ -589,14 +597,17 @@ namespace {
 // points of the chunk go into the packed sequences, the others into the scratch.
 template <bool SOLID>
 __device__ __noinline__ void phase_grad(const ElemTable &T, const PointTable &P, const float2 *u, int e, int nr,
-                                        bool axial, bool tiso, const Pk pk, float2 *buf, int S, int pc,
-                                        float2 *scr, float2 *q) {
+                                        bool axial, bool tiso, const Pk pk, float2 *buf, int S, int Pc, int crank,
+                                        int C, float2 *q) {
     constexpr int NSQ = SOLID ? 3 : 2;
     constexpr int NC = SOLID ? 6 : 3;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const bool active = lane < NPE;
     const int p = active ? lane : 0;
     const int nu = nr / 2, n = nu + 1, lim = nu - (nr % 2 == 0);
+    // sequences of point p live in cluster CTA p / Pc
+    float2 *ob = cg::this_cluster().map_shared_rank(buf, p / Pc);
+    const int col0 = NSQ * (p - (p / Pc) * Pc);
     LaneOps Lo;
     Lo.init(p, axial);
     Geo g;
@@ -611,13 +622,15 @@ __device__ __noinline__ void phase_grad(const ElemTable &T, const PointTable &P,
     }
     USrc us;
     us.init(P, u, SOLID, T.pts[e * NPE + p]);
-    // displacement of orders a and a + NW in flight while order a is differentiated
+    // this CTA's orders: a = crank NW + warp + k C NW; the displacement of the next two
+    // of them is in flight while one is differentiated
+    const int a0 = crank * NW + warp, da = C * NW;
     float2 un[3], un2[3];
     if (active) {
-        us.load(SOLID, warp, un);
-        us.load(SOLID, warp + NW, un2);
+        us.load(SOLID, a0, un);
+        us.load(SOLID, a0 + da, un2);
     }
-    for (int a = warp; a < n; a += NW) {
+    for (int a = a0; a < n; a += da) {
         if (active) {
             q[p] = un[0];
             if (SOLID) {
@@ -626,7 +639,7 @@ __device__ __noinline__ void phase_grad(const ElemTable &T, const PointTable &P,
             }
 #pragma unroll
             for (int i = 0; i < 3; i++) un[i] = un2[i];
-            us.load(SOLID, a + 2 * NW, un2);
+            us.load(SOLID, a + 2 * da, un2);
         }
         __syncwarp();
         if (active && a <= lim) {
@@ -637,15 +650,9 @@ __device__ __noinline__ void phase_grad(const ElemTable &T, const PointTable &P,
             } else {
                 grad1_lane(Lo, g, axial, a, q, eps);
             }
-            if (p < pc) {
 #pragma unroll
-                for (int s = 0; s < NSQ; s++)
-                    zput(buf, S, NSQ * p + s, a, pk, eps[2 * s], 2 * s + 1 < NC ? eps[2 * s + 1] : make_float2(0.f, 0.f));
-            } else {
-                float2 *o = scr + ((int64_t)a * NPE + p) * NC;
-#pragma unroll
-                for (int i = 0; i < NC; i++) o[i] = eps[i];
-            }
+            for (int s = 0; s < NSQ; s++)
+                zput(ob, S, col0 + s, a, pk, eps[2 * s], 2 * s + 1 < NC ? eps[2 * s + 1] : make_float2(0.f, 0.f));
         }
         __syncwarp();
     }
@@ -762,15 +769,16 @@ __device__ __noinline__ void phase_stress_fluid(float2 *buf, int S, int nr, int 
 // order into the element force; the last chunk's stress spectra come from the packed
 // sequences, the earlier chunks' from the scratch.
 template <bool SOLID>
-__device__ __noinline__ void phase_quad(const ElemTable &T, int e, int nr, bool axial, bool tiso,
-                                        const Pk pk, float hsc, const float2 *buf, int S, int pl0,
-                                        const float2 *scr, float2 *q) {
+__device__ __noinline__ void phase_quad(const ElemTable &T, int e, int nr, bool axial, bool tiso, const Pk pk,
+                                        float hsc, float2 *buf, int S, int Pc, int crank, int C, float2 *q) {
     constexpr int NSQ = SOLID ? 3 : 2;
     constexpr int NC = SOLID ? 6 : 3;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const bool active = lane < NPE;
     const int p = active ? lane : 0;
     const int nu = nr / 2, n = nu + 1, lim = nu - (nr % 2 == 0);
+    const float2 *ob = cg::this_cluster().map_shared_rank(buf, p / Pc);
+    const int col0 = NSQ * (p - (p / Pc) * Pc);
     LaneOps Lo;
     Lo.init(p, axial);
     Geo g;
@@ -784,23 +792,17 @@ __device__ __noinline__ void phase_quad(const ElemTable &T, int e, int nr, bool 
         c2 = tr[75 + p];
     }
     float2 *ef = T.ef + T.efofs[e];
-    for (int a = warp; a < n; a += NW) {
+    for (int a = crank * NW + warp; a < n; a += C * NW) {
         float2 sig[NC];
 #pragma unroll
         for (int i = 0; i < NC; i++) sig[i] = make_float2(0.f, 0.f);
         if (active && a <= lim) {
-            if (p >= pl0) {
 #pragma unroll
-                for (int s = 0; s < NSQ; s++) {
-                    float2 A, B;
-                    zget(buf, S, NSQ * (p - pl0) + s, a, pk, hsc, A, B);
-                    sig[2 * s] = A;
-                    if (2 * s + 1 < NC) sig[2 * s + 1] = B;
-                }
-            } else {
-                const float2 *o = scr + ((int64_t)a * NPE + p) * NC;
-#pragma unroll
-                for (int i = 0; i < NC; i++) sig[i] = o[i];
+            for (int s = 0; s < NSQ; s++) {
+                float2 A, B;
+                zget(ob, S, col0 + s, a, pk, hsc, A, B);
+                sig[2 * s] = A;
+                if (2 * s + 1 < NC) sig[2 * s + 1] = B;
             }
         }
         if constexpr (SOLID) {
@@ -834,19 +836,21 @@ __global__ void __launch_bounds__(NT, 2)
                 const float2 *__restrict__ u, const int32_t *__restrict__ elems, int count, int Pc, int Lmax,
                 const __grid_constant__ PhysTables X, const __grid_constant__ SLS sls) {
     constexpr int NSQ = SOLID ? 3 : 2;
-    constexpr int NC = SOLID ? 6 : 3;
     extern __shared__ __align__(16) char smem[];
+    cg::cluster_group cl = cg::this_cluster();
+    const int crank = (int)cl.block_rank(), C = (int)cl.num_blocks();
     const int S = NSQ * Pc;
     PhysSmem sm(smem, Lmax, S);
     float2 *tw = sm.tw, *buf = sm.buf;
     float2 *q = sm.wscr + (threadIdx.x >> 5) * WSCR;
-    float2 *scr = X.scratch ? X.scratch + (int64_t)blockIdx.x * X.scr_stride : nullptr;
+    // this CTA's GLL points
+    const int p0 = crank * Pc, pc = min(Pc, NPE - p0), ns = NSQ * pc;
 
-    for (int ei = blockIdx.x; ei < count; ei += gridDim.x) {
+    for (int ei = blockIdx.x / C; ei < count; ei += gridDim.x / C) {
         const int e = elems[ei];
         const int flags = T.flags[e];
         const bool axial = flags & EF_AXIAL;
-        const int nr = T.nr[e], lim = nr / 2 - (nr % 2 == 0);
+        const int nr = T.nr[e];
         const int mat = ef_mat(flags), att = SOLID ? ef_att(flags) : 0;
         const bool tiso = SOLID && (mat == 1 || mat == 2);
         const FftPlan &pl = X.plans[nr];
@@ -860,102 +864,82 @@ __global__ void __launch_bounds__(NT, 2)
         pk.inv_nr = 1.f / (float)nr;
         const float hsc = pl.kind == 0 ? 0.5f / (float)nr : 0.5f;
         const float *md = T.moduli + T.mofs[e];
-        const int nch = (NPE + Pc - 1) / Pc;
-        __syncthreads();  // the previous element is done with shared memory
+        cl.sync();  // the whole cluster is done with the previous element's sequences
         for (int m = threadIdx.x; m < L; m += NT) tw[m] = X.f2[pl.tw + m];
         if (!blue)
             for (int m = threadIdx.x; m < nr; m += NT) sm.rev[m] = X.i32[pl.rev + m];
-
-        for (int c = 0; c < nch; c++) {
-            const int p0 = c * Pc, pc = min(Pc, NPE - p0);
-            const int ns = NSQ * pc;
-            // positions the packing does not write: the Nyquist order (even nr) and the
-            // Bluestein padding [nr, L)
-            if (nr % 2 == 0)
-                for (int s = threadIdx.x; s < ns; s += NT) buf[(int64_t)(nr / 2) * S + s] = make_float2(0.f, 0.f);
-            if (blue)
-                for (int t = threadIdx.x; t < (Lb - nr) * ns; t += NT)
-                    buf[(int64_t)(nr + t / ns) * S + t % ns] = make_float2(0.f, 0.f);
-            // point lists of this chunk: elastic-only and attenuated
-            if (threadIdx.x == 0) {
-                int ne_ = 0, na_ = 0;
-                for (int pp = 0; pp < pc; pp++) {
-                    const int pg = p0 + pp;
-                    if (att == 1 || (att == 2 && cg4_index(pg) >= 0))
-                        sm.lst[32 + na_++] = pp;
-                    else
-                        sm.lst[ne_++] = pp;
-                }
-                sm.lst[30] = ne_;
-                sm.lst[31] = na_;
+        // positions the packing does not write: the Nyquist order (even nr) and the
+        // Bluestein padding [nr, Lb)
+        if (nr % 2 == 0)
+            for (int s = threadIdx.x; s < ns; s += NT) buf[(int64_t)(nr / 2) * S + s] = make_float2(0.f, 0.f);
+        if (blue)
+            for (int t = threadIdx.x; t < (Lb - nr) * ns; t += NT)
+                buf[(int64_t)(nr + t / ns) * S + t % ns] = make_float2(0.f, 0.f);
+        // point lists of this CTA: elastic-only and attenuated
+        if (threadIdx.x == 0) {
+            int ne_ = 0, na_ = 0;
+            for (int pp = 0; pp < pc; pp++) {
+                const int pg = p0 + pp;
+                if (att == 1 || (att == 2 && cg4_index(pg) >= 0))
+                    sm.lst[32 + na_++] = pp;
+                else
+                    sm.lst[ne_++] = pp;
             }
-            // ---- phase 1: Hermitian-packed strain spectra of the chunk ----
-            if (c == 0) {
-                phase_grad<SOLID>(T, P, u, e, nr, axial, tiso, pk, buf, S, pc, scr, q);
-            } else {
-                for (int t = threadIdx.x; t < (lim + 1) * ns; t += NT) {
-                    const int a = t / ns, col = t - a * ns, pp = col / NSQ, s = col - pp * NSQ;
-                    const float2 *o = scr + ((int64_t)a * NPE + p0 + pp) * NC;
-                    zput(buf, S, col, a, pk, o[2 * s], 2 * s + 1 < NC ? o[2 * s + 1] : make_float2(0.f, 0.f));
-                }
-            }
-            __syncthreads();
-            // ---- phase 2: to the nr azimuthal samples ----
-            transform_c2r(buf, S, ns, nr, pl, tw, X.f2);
-            // ---- phase 3: stress at every sample (SLS where attenuated) ----
-            if constexpr (SOLID) {
-                const int ne_ = sm.lst[30], na_ = sm.lst[31];
-                if (c == 0) {
-                    prefetch_l2(md, (int64_t)4 * NPE * nr * (mat == 0 ? 2 : mat == 1 ? 5 : 21));
+            sm.lst[30] = ne_;
+            sm.lst[31] = na_;
+        }
+        // ---- phase 1: Hermitian-packed strain spectra (this CTA's orders, all points) ----
+        phase_grad<SOLID>(T, P, u, e, nr, axial, tiso, pk, buf, S, Pc, crank, C, q);
+        cl.sync();
+        // ---- phase 2: to the nr azimuthal samples ----
+        transform_c2r(buf, S, ns, nr, pl, tw, X.f2);
+        // ---- phase 3: stress at every sample (SLS where attenuated) ----
+        if constexpr (SOLID) {
+            const int ne_ = sm.lst[30], na_ = sm.lst[31];
+            if (C == 1) {
+                const int nm = mat == 0 ? 2 : mat == 1 ? 5 : 21;
+                const int npa = att == 2 ? 4 : NPE;
+                const int64_t sb = (int64_t)4 * nr * (NPE * nm + (att ? (sls.nsls + 1) * 6 * npa + 2 * npa : 0));
+                if (sb <= PREFETCH_MAX) {
+                    prefetch_l2(md, (int64_t)4 * NPE * nr * nm);
                     if (att) {
-                        const int npa = att == 2 ? 4 : NPE;
                         prefetch_l2(T.mem + T.memofs[e], (int64_t)4 * (sls.nsls + 1) * nr * 6 * npa);
                         prefetch_l2(T.attm + T.aofs[e], (int64_t)4 * 2 * nr * npa);
                     }
                 }
-                if (ne_ > 0) {
-                    if (mat == 0)
-                        phase_stress<0>(buf, S, nr, ne_, sm.lst, sm.rev, md, pk, p0);
-                    else if (mat == 1)
-                        phase_stress<1>(buf, S, nr, ne_, sm.lst, sm.rev, md, pk, p0);
-                    else
-                        phase_stress<2>(buf, S, nr, ne_, sm.lst, sm.rev, md, pk, p0);
-                }
-                if (na_ > 0) {
-                    float *mem = T.mem + T.memofs[e];
-                    const float *am = T.attm + T.aofs[e];
-                    if (mat == 0)
-                        phase_stress_att<0>(buf, S, nr, na_, sm.lst + 32, sm.rev, md, pk, p0, att, mem, am, sls);
-                    else if (mat == 1)
-                        phase_stress_att<1>(buf, S, nr, na_, sm.lst + 32, sm.rev, md, pk, p0, att, mem, am, sls);
-                    else
-                        phase_stress_att<2>(buf, S, nr, na_, sm.lst + 32, sm.rev, md, pk, p0, att, mem, am, sls);
-                }
-            } else {
-                phase_stress_fluid(buf, S, nr, pc, sm.rev, md, pk, p0);
             }
-            if (blue)
-                for (int t = threadIdx.x; t < (Lb - nr) * ns; t += NT)
-                    buf[(int64_t)(nr + t / ns) * S + t % ns] = make_float2(0.f, 0.f);
-            __syncthreads();
-            // ---- phase 4: back to orders 0..lim ----
-            transform_r2c(buf, S, ns, nr, pl, tw, X.f2);
-            // ---- phase 5: stress spectra of all but the last chunk wait in the scratch ----
-            if (c < nch - 1) {
-                for (int t = threadIdx.x; t < (lim + 1) * ns; t += NT) {
-                    const int a = t / ns, col = t - a * ns, pp = col / NSQ, s = col - pp * NSQ;
-                    float2 A, B;
-                    zget(buf, S, col, a, pk, hsc, A, B);
-                    float2 *o = scr + ((int64_t)a * NPE + p0 + pp) * NC;
-                    o[2 * s] = A;
-                    if (2 * s + 1 < NC) o[2 * s + 1] = B;
-                }
-                __syncthreads();
+            if (ne_ > 0) {
+                if (mat == 0)
+                    phase_stress<0>(buf, S, nr, ne_, sm.lst, sm.rev, md, pk, p0);
+                else if (mat == 1)
+                    phase_stress<1>(buf, S, nr, ne_, sm.lst, sm.rev, md, pk, p0);
+                else
+                    phase_stress<2>(buf, S, nr, ne_, sm.lst, sm.rev, md, pk, p0);
             }
+            if (na_ > 0) {
+                float *mem = T.mem + T.memofs[e];
+                const float *am = T.attm + T.aofs[e];
+                if (mat == 0)
+                    phase_stress_att<0>(buf, S, nr, na_, sm.lst + 32, sm.rev, md, pk, p0, att, mem, am, sls);
+                else if (mat == 1)
+                    phase_stress_att<1>(buf, S, nr, na_, sm.lst + 32, sm.rev, md, pk, p0, att, mem, am, sls);
+                else
+                    phase_stress_att<2>(buf, S, nr, na_, sm.lst + 32, sm.rev, md, pk, p0, att, mem, am, sls);
+            }
+        } else {
+            phase_stress_fluid(buf, S, nr, pc, sm.rev, md, pk, p0);
         }
-        // ---- phase 6: divergence of every order, into the element force ----
-        phase_quad<SOLID>(T, e, nr, axial, tiso, pk, hsc, buf, S, (nch - 1) * Pc, scr, q);
+        if (blue)
+            for (int t = threadIdx.x; t < (Lb - nr) * ns; t += NT)
+                buf[(int64_t)(nr + t / ns) * S + t % ns] = make_float2(0.f, 0.f);
+        __syncthreads();
+        // ---- phase 4: back to orders 0..lim ----
+        transform_r2c(buf, S, ns, nr, pl, tw, X.f2);
+        cl.sync();
+        // ---- phase 5: divergence of this CTA's orders, all points, into the element force ----
+        phase_quad<SOLID>(T, e, nr, axial, tiso, pk, hsc, buf, S, Pc, crank, C, q);
     }
+    cl.sync();  // no CTA leaves while a peer may still read its shared memory
 }
 
 // ------------------------------------------------------------------------------------
@@ -1182,41 +1166,71 @@ FftTables build_fft_tables(const std::vector<char> &used) {
     return T;
 }
 
-// Points per chunk and shared memory of a bucket: all 25 points when two CTAs per SM
-// fit, else the largest chunk that does.
+// Points per CTA, cluster size and shared memory of a bucket: all 25 points in one CTA
+// when two CTAs per SM fit, else the smallest cluster whose CTAs fit (two per SM if
+// possible).
 void size_phys_bucket(PhysBucket &b, bool solid) {
     const int nsq = solid ? 3 : 2;
-    for (int pc = NPE; pc >= 1; pc--) {
-        const size_t sm = phys_smem_bytes(b.L_max, nsq, pc);
-        if (sm <= SMEM_TWO || (pc == 1 && sm <= SMEM_CAP)) {
-            b.npts_chunk = pc;
-            b.smem = sm;
-            return;
+    b.npts_chunk = 0;
+    for (size_t cap : {SMEM_TWO, SMEM_CAP}) {
+        for (int pc = NPE; pc >= 1; pc--) {
+            const size_t sm = phys_smem_bytes(b.L_max, nsq, pc);
+            const int C = (NPE + pc - 1) / pc;
+            if (sm <= cap && C <= CLUSTER_MAX) {
+                b.npts_chunk = pc;
+                b.csize = C;
+                b.smem = sm;
+                return;
+            }
         }
     }
-    b.npts_chunk = 0;
 }
 
+namespace {
+template <bool SOLID>
+cudaLaunchConfig_t phys_config(const PhysBucket &b, cudaLaunchAttribute *at, cudaStream_t s) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)std::max(b.grid, b.csize));
+    cfg.blockDim = dim3(NT);
+    cfg.dynamicSmemBytes = b.smem;
+    cfg.stream = s;
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)b.csize;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cfg;
+}
+}  // namespace
+
 int phys_grid(const PhysBucket &b, bool solid, int num_sms) {
-    int per_sm = 0;
-    if (solid)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_elem_phys<true>, NT, b.smem);
-    else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_elem_phys<false>, NT, b.smem);
-    per_sm = std::max(per_sm, 1);
-    return std::max(1, std::min(b.count, per_sm * num_sms));
+    cudaLaunchAttribute at[1];
+    int ncl = 0;
+    if (solid) {
+        cudaLaunchConfig_t cfg = phys_config<true>(b, at, nullptr);
+        cudaOccupancyMaxActiveClusters(&ncl, k_elem_phys<true>, &cfg);
+    } else {
+        cudaLaunchConfig_t cfg = phys_config<false>(b, at, nullptr);
+        cudaOccupancyMaxActiveClusters(&ncl, k_elem_phys<false>, &cfg);
+    }
+    if (ncl <= 0) ncl = std::max(1, num_sms / b.csize);
+    return b.csize * std::max(1, std::min(b.count, ncl));
 }
 
 void launch_elem_phys(bool solid, const ElemTable &T, const PointTable &P, const float2 *u, const PhysBucket &b,
                       const PhysTables &X, const SLS &sls, cudaStream_t s) {
     if (b.count <= 0) return;
-    PhysTables x = X;
-    x.scratch = b.scratch;
-    x.scr_stride = b.scr_stride;
-    if (solid)
-        k_elem_phys<true><<<b.grid, NT, b.smem, s>>>(T, P, u, b.elems, b.count, b.npts_chunk, b.L_max, x, sls);
-    else
-        k_elem_phys<false><<<b.grid, NT, b.smem, s>>>(T, P, u, b.elems, b.count, b.npts_chunk, b.L_max, x, sls);
+    cudaLaunchAttribute at[1];
+    if (solid) {
+        cudaLaunchConfig_t cfg = phys_config<true>(b, at, s);
+        cudaLaunchKernelEx(&cfg, k_elem_phys<true>, T, P, u, (const int32_t *)b.elems, b.count, b.npts_chunk,
+                           b.L_max, X, sls);
+    } else {
+        cudaLaunchConfig_t cfg = phys_config<false>(b, at, s);
+        cudaLaunchKernelEx(&cfg, k_elem_phys<false>, T, P, u, (const int32_t *)b.elems, b.count, b.npts_chunk,
+                           b.L_max, X, sls);
+    }
 }
 
 }  // namespace ax3d
