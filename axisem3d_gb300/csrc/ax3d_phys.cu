@@ -79,6 +79,21 @@ __device__ __forceinline__ float2 twv(const float2 *tw, int idx, int sg) {
     return sg > 0 ? w : make_float2(w.x, -w.y);
 }
 
+// The threads that share one set of sequences and the barrier between their passes.
+struct Grp {
+    int tid, n, warp, nwarp;
+    bool cta;
+    __device__ __forceinline__ void sync() const {
+        if (cta)
+            __syncthreads();
+        else
+            __syncwarp();
+    }
+};
+__device__ __forceinline__ Grp grp_cta() {
+    return Grp{(int)threadIdx.x, (int)blockDim.x, (int)(threadIdx.x >> 5), (int)(blockDim.x >> 5), true};
+}
+
 // v <- DFT_R(v) with e^{+2 pi i rk/R} (inv) or e^{-2 pi i rk/R}; cq/sq = cos/sin(2 pi q/R)
 template <int R>
 __device__ __forceinline__ void butterfly(float2 (&v)[R], bool inv, const float *cq, const float *sq) {
@@ -132,7 +147,8 @@ __device__ __forceinline__ void butterfly(float2 (&v)[R], bool inv, const float 
 //   DIF: butterfly, then output k of butterfly j times w_Ls^{jk}.
 //   DIT: input k of butterfly j times w_Ls^{jk}, then butterfly.
 template <int R>
-__device__ __noinline__ void rad_pass(float2 *buf, int S, int ns, int L, int Ls, const float2 *tw, int sg, bool dit) {
+__device__ __noinline__ void rad_pass(float2 *buf, int S, int ns, int L, int Ls, const float2 *tw, int sg, bool dit,
+                                      const Grp g) {
     const int m = Ls / R, ts = L / Ls;
     const int total = (L / R) * ns;
     const FDiv fs = make_fdiv((uint32_t)ns), fm = make_fdiv((uint32_t)m);
@@ -147,15 +163,15 @@ __device__ __noinline__ void rad_pass(float2 *buf, int S, int ns, int L, int Ls,
         }
     }
     // U butterflies per iteration, their shared-memory loads issued together
-    constexpr int U = R <= 7 ? 2 : 1;
+    constexpr int U = R <= 4 ? 4 : R <= 7 ? 2 : 1;
     const int64_t rs = (int64_t)m * S;
-    for (int t0 = threadIdx.x; t0 < total; t0 += blockDim.x * U) {
+    for (int t0 = g.tid; t0 < total; t0 += g.n * U) {
         float2 v[U][R];
         float2 *p0[U];
         int jj[U];
 #pragma unroll
         for (int uu = 0; uu < U; uu++) {
-            const int t = min(t0 + uu * (int)blockDim.x, total - 1);
+            const int t = min(t0 + uu * g.n, total - 1);
             const int bj = (int)fdiv((uint32_t)t, fs), s = t - bj * ns;
             const int b = (int)fdiv((uint32_t)bj, fm);
             jj[uu] = bj - b * m;
@@ -175,7 +191,7 @@ __device__ __noinline__ void rad_pass(float2 *buf, int S, int ns, int L, int Ls,
 #pragma unroll
                 for (int r = 1; r < R; r++) v[uu][r] = cmul(v[uu][r], twv(tw, j * r * ts, sg));
             }
-            if (t0 + uu * (int)blockDim.x < total) {
+            if (t0 + uu * g.n < total) {
 #pragma unroll
                 for (int r = 0; r < R; r++) p0[uu][r * rs] = v[uu][r];
             }
@@ -190,13 +206,14 @@ __device__ __noinline__ void rad_pass(float2 *buf, int S, int ns, int L, int Ls,
 // reloaded exactly every RESEED orders, and writes after a warp barrier (only the group
 // reads or writes its butterfly).
 template <int GS, int KL, int SG>
-__device__ __noinline__ void direct_pass(float2 *buf, int S, int ns, int L, int Ls, int p, const float2 *tw, int sg, bool dit) {
+__device__ __noinline__ void direct_pass(float2 *buf, int S, int ns, int L, int Ls, int p, const float2 *tw, int sg, bool dit,
+                                         const Grp g) {
     const int H = (p - 1) >> 1, m = Ls / p, ts = L / Ls, ps = L / p;
     const int nsg = (ns + SG - 1) / SG;
     const int ntask = (L / Ls) * m * nsg;
     constexpr int GPW = 32 / GS;
     const int lane = threadIdx.x & 31, gi = lane / GS, gl = lane - gi * GS;
-    const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int warp = g.warp, nw = g.nwarp;
     const FDiv fn = make_fdiv((uint32_t)nsg), fm = make_fdiv((uint32_t)m);
     const int64_t rs = (int64_t)m * S;
     for (int t0 = warp * GPW; t0 < ntask; t0 += nw * GPW) {
@@ -312,87 +329,89 @@ __device__ __noinline__ void direct_pass(float2 *buf, int S, int ns, int L, int 
     }
 }
 
-__device__ void run_pass(int R, float2 *buf, int S, int ns, int L, int Ls, const float2 *tw, int sg, bool dit) {
+__device__ void run_pass(int R, float2 *buf, int S, int ns, int L, int Ls, const float2 *tw, int sg, bool dit,
+                         const Grp g) {
     switch (R) {
-        case 2: rad_pass<2>(buf, S, ns, L, Ls, tw, sg, dit); break;
-        case 3: rad_pass<3>(buf, S, ns, L, Ls, tw, sg, dit); break;
-        case 4: rad_pass<4>(buf, S, ns, L, Ls, tw, sg, dit); break;
-        case 5: rad_pass<5>(buf, S, ns, L, Ls, tw, sg, dit); break;
-        case 7: rad_pass<7>(buf, S, ns, L, Ls, tw, sg, dit); break;
-        case 11: rad_pass<11>(buf, S, ns, L, Ls, tw, sg, dit); break;
-        case 13: rad_pass<13>(buf, S, ns, L, Ls, tw, sg, dit); break;
+        case 2: rad_pass<2>(buf, S, ns, L, Ls, tw, sg, dit, g); break;
+        case 3: rad_pass<3>(buf, S, ns, L, Ls, tw, sg, dit, g); break;
+        case 4: rad_pass<4>(buf, S, ns, L, Ls, tw, sg, dit, g); break;
+        case 5: rad_pass<5>(buf, S, ns, L, Ls, tw, sg, dit, g); break;
+        case 7: rad_pass<7>(buf, S, ns, L, Ls, tw, sg, dit, g); break;
+        case 11: rad_pass<11>(buf, S, ns, L, Ls, tw, sg, dit, g); break;
+        case 13: rad_pass<13>(buf, S, ns, L, Ls, tw, sg, dit, g); break;
         default:
             if (R <= 17)
-                direct_pass<8, 1, 8>(buf, S, ns, L, Ls, R, tw, sg, dit);
+                direct_pass<8, 1, 8>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
             else if (R <= 33)
-                direct_pass<16, 1, 8>(buf, S, ns, L, Ls, R, tw, sg, dit);
+                direct_pass<16, 1, 8>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
             else if (R <= 65)
-                direct_pass<32, 1, 8>(buf, S, ns, L, Ls, R, tw, sg, dit);
+                direct_pass<32, 1, 8>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
             else if (R <= 129)
-                direct_pass<32, 2, 4>(buf, S, ns, L, Ls, R, tw, sg, dit);
+                direct_pass<32, 2, 4>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
             else if (R <= 257)
-                direct_pass<32, 4, 2>(buf, S, ns, L, Ls, R, tw, sg, dit);
+                direct_pass<32, 4, 2>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
             else
-                direct_pass<32, 8, 1>(buf, S, ns, L, Ls, R, tw, sg, dit);
+                direct_pass<32, 8, 1>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
     }
 }
 
 // All passes of a plan: DIF (natural -> reversed) or DIT (reversed -> natural).
-__device__ void fft_passes(float2 *buf, int S, int ns, const FftPlan &pl, const float2 *tw, int sg, bool dit) {
+__device__ void fft_passes(float2 *buf, int S, int ns, const FftPlan &pl, const float2 *tw, int sg, bool dit,
+                           const Grp g) {
     const int L = pl.L;
     if (!dit) {
         int Ls = L;
         for (int i = 0; i < pl.nrad; i++) {
-            run_pass(pl.rad[i], buf, S, ns, L, Ls, tw, sg, false);
-            __syncthreads();
+            run_pass(pl.rad[i], buf, S, ns, L, Ls, tw, sg, false, g);
+            g.sync();
             Ls /= pl.rad[i];
         }
     } else {
         int Ls = 1;
         for (int i = pl.nrad - 1; i >= 0; i--) {
             Ls *= pl.rad[i];
-            run_pass(pl.rad[i], buf, S, ns, L, Ls, tw, sg, true);
-            __syncthreads();
+            run_pass(pl.rad[i], buf, S, ns, L, Ls, tw, sg, true, g);
+            g.sync();
         }
     }
 }
 
 // buf[pos] *= K[pos] over L positions; with save >= 0 the zero-frequency sum at position
 // 0 is first kept in slot save (Rader).
-__device__ void pointwise(float2 *buf, int S, int ns, int L, const float2 *__restrict__ K, int save) {
+__device__ void pointwise(float2 *buf, int S, int ns, int L, const float2 *__restrict__ K, int save, const Grp g) {
     const FDiv fs = make_fdiv((uint32_t)ns);
-    for (int t = threadIdx.x; t < L * ns; t += blockDim.x) {
+    for (int t = g.tid; t < L * ns; t += g.n) {
         const int pos = (int)fdiv((uint32_t)t, fs), s = t - pos * ns;
         const float2 v = buf[(int64_t)pos * S + s];
         if (save >= 0 && pos == 0) buf[(int64_t)save * S + s] = v;
         buf[(int64_t)pos * S + s] = cmul(v, __ldg(K + pos));
     }
-    __syncthreads();
+    g.sync();
 }
 
 // spectrum -> samples: mixed radix leaves them digit-reversed, Bluestein natural (before the
 // post-chirp h_k, which the stress phase applies), Rader in generator order (before the
 // zero-frequency term, which the stress phase adds)
 __device__ void transform_c2r(float2 *buf, int S, int ns, int nr, const FftPlan &pl, const float2 *tw,
-                              const float2 *f2) {
+                              const float2 *f2, const Grp g) {
     if (pl.kind == 0) {
-        fft_passes(buf, S, ns, pl, tw, +1, false);
+        fft_passes(buf, S, ns, pl, tw, +1, false, g);
     } else {
-        fft_passes(buf, S, ns, pl, tw, -1, false);
-        pointwise(buf, S, ns, pl.L, f2 + pl.bc2r, pl.kind == 2 ? nr : -1);
-        fft_passes(buf, S, ns, pl, tw, +1, true);
+        fft_passes(buf, S, ns, pl, tw, -1, false, g);
+        pointwise(buf, S, ns, pl.L, f2 + pl.bc2r, pl.kind == 2 ? nr : -1, g);
+        fft_passes(buf, S, ns, pl, tw, +1, true, g);
     }
 }
 // samples -> spectrum; scaled by 1/nr in the extraction (mixed radix) or in the kernel
 // spectrum (Bluestein, Rader)
 __device__ void transform_r2c(float2 *buf, int S, int ns, int nr, const FftPlan &pl, const float2 *tw,
-                              const float2 *f2) {
+                              const float2 *f2, const Grp g) {
     if (pl.kind == 0) {
-        fft_passes(buf, S, ns, pl, tw, -1, true);
+        fft_passes(buf, S, ns, pl, tw, -1, true, g);
     } else {
-        fft_passes(buf, S, ns, pl, tw, -1, false);
-        pointwise(buf, S, ns, pl.L, f2 + pl.br2c, pl.kind == 2 ? nr - 1 : -1);
-        fft_passes(buf, S, ns, pl, tw, +1, true);
+        fft_passes(buf, S, ns, pl, tw, -1, false, g);
+        pointwise(buf, S, ns, pl.L, f2 + pl.br2c, pl.kind == 2 ? nr - 1 : -1, g);
+        fft_passes(buf, S, ns, pl, tw, +1, true, g);
     }
 }
 
@@ -662,16 +681,16 @@ __device__ __noinline__ void phase_grad(const ElemTable &T, const PointTable &P,
 // takes IT items and issues all their modulus loads before any arithmetic.
 template <int MAT>
 __device__ __noinline__ void phase_stress(float2 *buf, int S, int nr, int ne_, const int32_t *lst, const int32_t *rev,
-                                          const float *md, const Pk pk, int p0) {
+                                          const float *md, const Pk pk, int p0, const Grp g) {
     constexpr int NM = MAT == 0 ? 2 : MAT == 1 ? 5 : 21;
-    constexpr int IT = MAT == 2 ? 1 : 4;
+    constexpr int IT = MAT == 2 ? 1 : MAT == 1 ? 6 : 8;
     const int total = nr * ne_;
-    for (int t0 = threadIdx.x; t0 < total; t0 += blockDim.x * IT) {
+    for (int t0 = g.tid; t0 < total; t0 += g.n * IT) {
         float mv[IT][NM];
         int kk[IT];
 #pragma unroll
         for (int i = 0; i < IT; i++) {
-            const int t = min(t0 + i * (int)blockDim.x, total - 1);
+            const int t = min(t0 + i * g.n, total - 1);
             const int pos = t / ne_, pg = p0 + lst[t - pos * ne_];
             kk[i] = pk.kind == 1 ? pos : rev[pos];
 #pragma unroll
@@ -679,7 +698,7 @@ __device__ __noinline__ void phase_stress(float2 *buf, int S, int nr, int ne_, c
         }
 #pragma unroll
         for (int i = 0; i < IT; i++) {
-            const int t = t0 + i * (int)blockDim.x;
+            const int t = t0 + i * g.n;
             if (t >= total) break;
             const int pos = t / ne_, pp = lst[t - pos * ne_];
             const SampleAt sa(pos, pk, rev);
@@ -701,19 +720,19 @@ __device__ __noinline__ void phase_stress(float2 *buf, int S, int nr, int ne_, c
 template <int MAT>
 __device__ __noinline__ void phase_stress_att(float2 *buf, int S, int nr, int na_, const int32_t *lst,
                                               const int32_t *rev, const float *md, const Pk pk, int p0,
-                                              int att, float *mem, const float *am, const SLS &sls) {
+                                              int att, float *mem, const float *am, const SLS &sls, const Grp g) {
     constexpr int NM = MAT == 0 ? 2 : MAT == 1 ? 5 : 21;
     constexpr int IT = MAT == 2 ? 1 : 2;
     const int npa = att == 2 ? 4 : NPE;
     const int64_t sl = (int64_t)nr * 6 * npa;
     const int total = nr * na_;
     const int nsls = sls.nsls;
-    for (int t0 = threadIdx.x; t0 < total; t0 += blockDim.x * IT) {
+    for (int t0 = g.tid; t0 < total; t0 += g.n * IT) {
         float mv[IT][NM], rs[IT][6], sr[IT][6], dk[IT], dm[IT];
         int kk[IT], qq[IT];
 #pragma unroll
         for (int i = 0; i < IT; i++) {
-            const int t = min(t0 + i * (int)blockDim.x, total - 1);
+            const int t = min(t0 + i * g.n, total - 1);
             const int pos = t / na_, pg = p0 + lst[t - pos * na_];
             qq[i] = att == 2 ? cg4_index(pg) : pg;
             kk[i] = pk.kind == 1 ? pos : rev[pos];
@@ -733,7 +752,7 @@ __device__ __noinline__ void phase_stress_att(float2 *buf, int S, int nr, int na
         }
 #pragma unroll
         for (int i = 0; i < IT; i++) {
-            const int t = t0 + i * (int)blockDim.x;
+            const int t = t0 + i * g.n;
             if (t >= total) break;
             const int pos = t / na_, pp = lst[t - pos * na_];
             const SampleAt sa(pos, pk, rev);
@@ -755,8 +774,8 @@ __device__ __noinline__ void phase_stress_att(float2 *buf, int S, int nr, int na
 
 // Phase 3 of a fluid element: sigma_i = K d_i chi (Acoustic3D.cpp:9-16) at every sample.
 __device__ __noinline__ void phase_stress_fluid(float2 *buf, int S, int nr, int pc, const int32_t *rev,
-                                                const float *md, const Pk pk, int p0) {
-    for (int t = threadIdx.x; t < nr * pc; t += blockDim.x) {
+                                                const float *md, const Pk pk, int p0, const Grp g) {
+    for (int t = g.tid; t < nr * pc; t += g.n) {
         const int pos = t / pc, pp = t - pos * pc;
         const SampleAt sa(pos, pk, rev);
         const float K = __ldg(md + (int64_t)sa.k * NPE + p0 + pp);
@@ -875,27 +894,9 @@ __global__ void __launch_bounds__(NT, 2)
         if (blue)
             for (int t = threadIdx.x; t < (Lb - nr) * ns; t += NT)
                 buf[(int64_t)(nr + t / ns) * S + t % ns] = make_float2(0.f, 0.f);
-        // point lists of this CTA: elastic-only and attenuated
-        if (threadIdx.x == 0) {
-            int ne_ = 0, na_ = 0;
-            for (int pp = 0; pp < pc; pp++) {
-                const int pg = p0 + pp;
-                if (att == 1 || (att == 2 && cg4_index(pg) >= 0))
-                    sm.lst[32 + na_++] = pp;
-                else
-                    sm.lst[ne_++] = pp;
-            }
-            sm.lst[30] = ne_;
-            sm.lst[31] = na_;
-        }
         // ---- phase 1: Hermitian-packed strain spectra (this CTA's orders, all points) ----
         phase_grad<SOLID>(T, P, u, e, nr, axial, tiso, pk, buf, S, Pc, crank, C, q);
-        cl.sync();
-        // ---- phase 2: to the nr azimuthal samples ----
-        transform_c2r(buf, S, ns, nr, pl, tw, X.f2);
-        // ---- phase 3: stress at every sample (SLS where attenuated) ----
         if constexpr (SOLID) {
-            const int ne_ = sm.lst[30], na_ = sm.lst[31];
             if (C == 1) {
                 const int nm = mat == 0 ? 2 : mat == 1 ? 5 : 21;
                 const int npa = att == 2 ? 4 : NPE;
@@ -908,33 +909,63 @@ __global__ void __launch_bounds__(NT, 2)
                     }
                 }
             }
-            if (ne_ > 0) {
-                if (mat == 0)
-                    phase_stress<0>(buf, S, nr, ne_, sm.lst, sm.rev, md, pk, p0);
-                else if (mat == 1)
-                    phase_stress<1>(buf, S, nr, ne_, sm.lst, sm.rev, md, pk, p0);
-                else
-                    phase_stress<2>(buf, S, nr, ne_, sm.lst, sm.rev, md, pk, p0);
-            }
-            if (na_ > 0) {
-                float *mem = T.mem + T.memofs[e];
-                const float *am = T.attm + T.aofs[e];
-                if (mat == 0)
-                    phase_stress_att<0>(buf, S, nr, na_, sm.lst + 32, sm.rev, md, pk, p0, att, mem, am, sls);
-                else if (mat == 1)
-                    phase_stress_att<1>(buf, S, nr, na_, sm.lst + 32, sm.rev, md, pk, p0, att, mem, am, sls);
-                else
-                    phase_stress_att<2>(buf, S, nr, na_, sm.lst + 32, sm.rev, md, pk, p0, att, mem, am, sls);
-            }
-        } else {
-            phase_stress_fluid(buf, S, nr, pc, sm.rev, md, pk, p0);
         }
-        if (blue)
-            for (int t = threadIdx.x; t < (Lb - nr) * ns; t += NT)
-                buf[(int64_t)(nr + t / ns) * S + t % ns] = make_float2(0.f, 0.f);
-        __syncthreads();
-        // ---- phase 4: back to orders 0..lim ----
-        transform_r2c(buf, S, ns, nr, pl, tw, X.f2);
+        cl.sync();
+        // ---- phases 2-4: the CTA's points, all its threads on each pass ----
+        {
+            const Grp g = grp_cta();
+            const int gp0 = 0, gpc = pc;
+            float2 *gbuf = buf;
+            const int gns = ns;
+            int32_t *lst = sm.lst;
+            // the group's point lists: elastic-only and attenuated
+            if (g.tid == 0) {
+                int ne_ = 0, na_ = 0;
+                for (int pp = 0; pp < gpc; pp++) {
+                    const int pg = p0 + gp0 + pp;
+                    if (att == 1 || (att == 2 && cg4_index(pg) >= 0))
+                        lst[32 + na_++] = pp;
+                    else
+                        lst[ne_++] = pp;
+                }
+                lst[30] = ne_;
+                lst[31] = na_;
+            }
+            g.sync();
+            // ---- phase 2: to the nr azimuthal samples ----
+            transform_c2r(gbuf, S, gns, nr, pl, tw, X.f2, g);
+            // ---- phase 3: stress at every sample (SLS where attenuated) ----
+            const int gpg = p0 + gp0;  // global index of the group's first point
+            if constexpr (SOLID) {
+                const int ne_ = lst[30], na_ = lst[31];
+                if (ne_ > 0) {
+                    if (mat == 0)
+                        phase_stress<0>(gbuf, S, nr, ne_, lst, sm.rev, md, pk, gpg, g);
+                    else if (mat == 1)
+                        phase_stress<1>(gbuf, S, nr, ne_, lst, sm.rev, md, pk, gpg, g);
+                    else
+                        phase_stress<2>(gbuf, S, nr, ne_, lst, sm.rev, md, pk, gpg, g);
+                }
+                if (na_ > 0) {
+                    float *mem = T.mem + T.memofs[e];
+                    const float *am = T.attm + T.aofs[e];
+                    if (mat == 0)
+                        phase_stress_att<0>(gbuf, S, nr, na_, lst + 32, sm.rev, md, pk, gpg, att, mem, am, sls, g);
+                    else if (mat == 1)
+                        phase_stress_att<1>(gbuf, S, nr, na_, lst + 32, sm.rev, md, pk, gpg, att, mem, am, sls, g);
+                    else
+                        phase_stress_att<2>(gbuf, S, nr, na_, lst + 32, sm.rev, md, pk, gpg, att, mem, am, sls, g);
+                }
+            } else {
+                phase_stress_fluid(gbuf, S, nr, gpc, sm.rev, md, pk, gpg, g);
+            }
+            if (blue)
+                for (int t = g.tid; t < (Lb - nr) * gns; t += g.n)
+                    gbuf[(int64_t)(nr + t / gns) * S + t % gns] = make_float2(0.f, 0.f);
+            g.sync();
+            // ---- phase 4: back to orders 0..lim ----
+            transform_r2c(gbuf, S, gns, nr, pl, tw, X.f2, g);
+        }
         cl.sync();
         // ---- phase 5: divergence of this CTA's orders, all points, into the element force ----
         phase_quad<SOLID>(T, e, nr, axial, tiso, pk, hsc, buf, S, Pc, crank, C, q);
