@@ -50,7 +50,7 @@ constexpr int NT = 256;      // threads per CTA
 constexpr int NW = NT / 32;  // warps per CTA
 constexpr int WSCR = 125;    // per-warp grad / divergence scratch (float2)
 constexpr int RESEED = 8;    // direct DFT: exact twiddle reload interval
-constexpr int DIRECT_MAX = 513;  // largest prime handled by a direct pass
+constexpr int DIRECT_MAX = 257;  // largest prime handled by a direct pass
 constexpr size_t SMEM_CAP = 227 * 1024;
 constexpr size_t SMEM_TWO = 112 * 1024;  // two CTAs per SM
 constexpr int64_t PREFETCH_MAX = 256 * 1024;  // largest per-element block asked of L2 ahead
@@ -163,7 +163,7 @@ __device__ __noinline__ void rad_pass(float2 *buf, int S, int ns, int L, int Ls,
         }
     }
     // U butterflies per iteration, their shared-memory loads issued together
-    constexpr int U = R <= 4 ? 4 : R <= 7 ? 2 : 1;
+    constexpr int U = R <= 4 ? 4 : R <= 5 ? 2 : 1;
     const int64_t rs = (int64_t)m * S;
     for (int t0 = g.tid; t0 < total; t0 += g.n * U) {
         float2 v[U][R];
@@ -182,18 +182,59 @@ __device__ __noinline__ void rad_pass(float2 *buf, int S, int ns, int L, int Ls,
 #pragma unroll
         for (int uu = 0; uu < U; uu++) {
             const int j = jj[uu];
+            const bool ok = t0 + uu * g.n < total;
             if (dit) {
 #pragma unroll
                 for (int r = 1; r < R; r++) v[uu][r] = cmul(v[uu][r], twv(tw, j * r * ts, sg));
             }
-            butterfly<R>(v[uu], sg > 0, cq, sq);
-            if (!dit) {
+            if constexpr (!ODD) {
+                butterfly<R>(v[uu], sg > 0, cq, sq);
+                if (!dit) {
 #pragma unroll
-                for (int r = 1; r < R; r++) v[uu][r] = cmul(v[uu][r], twv(tw, j * r * ts, sg));
-            }
-            if (t0 + uu * g.n < total) {
+                    for (int r = 1; r < R; r++) v[uu][r] = cmul(v[uu][r], twv(tw, j * r * ts, sg));
+                }
+                if (ok) {
 #pragma unroll
-                for (int r = 0; r < R; r++) p0[uu][r * rs] = v[uu][r];
+                    for (int r = 0; r < R; r++) p0[uu][r * rs] = v[uu][r];
+                }
+            } else {
+                // odd R: out_k = v0 + sum_r (v_r + v_{R-r}) cos(2 pi rk/R) +- i (v_r - v_{R-r})
+                // sin(..); each pair (k, R - k) is stored as soon as it is formed (the
+                // butterfly's inputs are all in registers, and only this thread owns them)
+                constexpr int H = (R - 1) / 2;
+                float2 sp[H], sm[H];
+                float2 out0 = v[uu][0];
+#pragma unroll
+                for (int r = 1; r <= H; r++) {
+                    sp[r - 1] = cadd(v[uu][r], v[uu][R - r]);
+                    sm[r - 1] = csub(v[uu][r], v[uu][R - r]);
+                    out0 = cadd(out0, sp[r - 1]);
+                }
+                const float2 x0 = v[uu][0];
+                if (ok) p0[uu][0] = out0;
+                const float sgf = sg > 0 ? 1.f : -1.f;
+#pragma unroll
+                for (int k = 1; k <= H; k++) {
+                    float2 a = x0, bb = make_float2(0.f, 0.f);
+#pragma unroll
+                    for (int r = 1; r <= H; r++) {
+                        const int qk = (r * k) % R;
+                        a.x = fmaf(sp[r - 1].x, cq[qk], a.x);
+                        a.y = fmaf(sp[r - 1].y, cq[qk], a.y);
+                        bb.x = fmaf(sm[r - 1].x, sq[qk], bb.x);
+                        bb.y = fmaf(sm[r - 1].y, sq[qk], bb.y);
+                    }
+                    float2 o1 = make_float2(a.x - sgf * bb.y, a.y + sgf * bb.x);  // a + i sg b
+                    float2 o2 = make_float2(a.x + sgf * bb.y, a.y - sgf * bb.x);
+                    if (!dit) {
+                        o1 = cmul(o1, twv(tw, j * k * ts, sg));
+                        o2 = cmul(o2, twv(tw, j * (R - k) * ts, sg));
+                    }
+                    if (ok) {
+                        p0[uu][k * rs] = o1;
+                        p0[uu][(R - k) * rs] = o2;
+                    }
+                }
             }
         }
     }
@@ -341,17 +382,15 @@ __device__ void run_pass(int R, float2 *buf, int S, int ns, int L, int Ls, const
         case 13: rad_pass<13>(buf, S, ns, L, Ls, tw, sg, dit, g); break;
         default:
             if (R <= 17)
-                direct_pass<8, 1, 8>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
+                direct_pass<8, 1, 4>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
             else if (R <= 33)
-                direct_pass<16, 1, 8>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
+                direct_pass<16, 1, 4>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
             else if (R <= 65)
-                direct_pass<32, 1, 8>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
+                direct_pass<32, 1, 4>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
             else if (R <= 129)
-                direct_pass<32, 2, 4>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
-            else if (R <= 257)
-                direct_pass<32, 4, 2>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
+                direct_pass<32, 2, 2>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
             else
-                direct_pass<32, 8, 1>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
+                direct_pass<32, 4, 1>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
     }
 }
 
@@ -683,7 +722,7 @@ template <int MAT>
 __device__ __noinline__ void phase_stress(float2 *buf, int S, int nr, int ne_, const int32_t *lst, const int32_t *rev,
                                           const float *md, const Pk pk, int p0, const Grp g) {
     constexpr int NM = MAT == 0 ? 2 : MAT == 1 ? 5 : 21;
-    constexpr int IT = MAT == 2 ? 1 : MAT == 1 ? 6 : 8;
+    constexpr int IT = MAT == 2 ? 1 : MAT == 1 ? 4 : 8;
     const int total = nr * ne_;
     for (int t0 = g.tid; t0 < total; t0 += g.n * IT) {
         float mv[IT][NM];
@@ -716,13 +755,13 @@ __device__ __noinline__ void phase_stress(float2 *buf, int S, int nr, int ne_, c
 
 // Phase 3, attenuated points: elastic stress minus the memory variables (applyToStress),
 // then updateMemoryVariables (Attenuation3D_Full.cpp:16-50, Attenuation3D_CG4.cpp:16-62).
-// Two items per thread with their loads issued together.
+// All loads of an item are issued before its arithmetic.
 template <int MAT>
 __device__ __noinline__ void phase_stress_att(float2 *buf, int S, int nr, int na_, const int32_t *lst,
                                               const int32_t *rev, const float *md, const Pk pk, int p0,
                                               int att, float *mem, const float *am, const SLS &sls, const Grp g) {
     constexpr int NM = MAT == 0 ? 2 : MAT == 1 ? 5 : 21;
-    constexpr int IT = MAT == 2 ? 1 : 2;
+    constexpr int IT = 1;
     const int npa = att == 2 ? 4 : NPE;
     const int64_t sl = (int64_t)nr * 6 * npa;
     const int total = nr * na_;
