@@ -79,6 +79,10 @@ struct ax3d_domain {
     int kahan = 0;
     int stab_interval = 0;
     cudaStream_t stream = nullptr;
+    // side streams for the physical-space buckets, forked from / joined into `stream`
+    static constexpr int NSIDE = 3;
+    cudaStream_t side[NSIDE] = {};
+    cudaEvent_t ev_fork = nullptr, ev_join[NSIDE] = {};
     bool finalized = false;
     int tstep = 1;
 
@@ -200,6 +204,11 @@ struct ax3d_domain {
         }
         for (auto e : pool) cudaEventDestroy(e);
         drop_graph();
+        for (int k = 0; k < NSIDE; k++) {
+            if (ev_join[k]) cudaEventDestroy(ev_join[k]);
+            if (side[k]) cudaStreamDestroy(side[k]);
+        }
+        if (ev_fork) cudaEventDestroy(ev_fork);
         if (stream) cudaStreamDestroy(stream);
     }
 
@@ -304,6 +313,11 @@ struct ax3d_domain {
         if (finalized) throw Error(AX3D_ERR_STATE, "ax3d_finalize || already finalized");
         CK(cudaSetDevice(device));
         CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        for (int k = 0; k < NSIDE; k++) {
+            CK(cudaStreamCreateWithFlags(&side[k], cudaStreamNonBlocking));
+            CK(cudaEventCreateWithFlags(&ev_join[k], cudaEventDisableTiming));
+        }
+        CK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
         ax3d::init_kernel_attributes();
         ax3d::set_g_matrices(g_gll, g_glj, stream);
         const int np = (int)p_nr.size(), ne = (int)e_nr.size();
@@ -562,11 +576,34 @@ struct ax3d_domain {
         ax3d::launch_source(P, T, F, d_selem.p, d_snord.p, d_sofs_src.p, d_sforce.p, (int)s_elem.size(),
                             d_stf.p, (int)stf.size(), d_targ.p, 0, stream);
     }
-    void compute_stiff() {
+    // Element stiffness (Domain::computeStiff's element loop).  The physical-space buckets
+    // go round-robin, longest transforms first, over side streams forked from and joined
+    // back into the main stream, so one bucket's tail overlaps the next bucket's start;
+    // a graph capture of the step records the same fork and join.
+    void launch_elements() {
         ax3d::launch_elem_fourier_solid(T, P, F.su, d_items_s.p, nitems_s, sls, stream);
         ax3d::launch_elem_fourier_fluid(T, P, F.fu, d_items_f.p, nitems_f, stream);
-        for (auto &b : buckets_s) ax3d::launch_elem_phys(true, T, P, F.su, b, X, sls, stream);
-        for (auto &b : buckets_f) ax3d::launch_elem_phys(false, T, P, F.fu, b, X, sls, stream);
+        const int nb = (int)(buckets_s.size() + buckets_f.size());
+        if (nb == 0) return;
+        if (nb == 1) {
+            for (auto &b : buckets_s) ax3d::launch_elem_phys(true, T, P, F.su, b, X, sls, stream);
+            for (auto &b : buckets_f) ax3d::launch_elem_phys(false, T, P, F.fu, b, X, sls, stream);
+            return;
+        }
+        CK(cudaEventRecord(ev_fork, stream));
+        for (int k = 0; k < NSIDE; k++) CK(cudaStreamWaitEvent(side[k], ev_fork, 0));
+        int i = 0;
+        for (auto it = buckets_s.rbegin(); it != buckets_s.rend(); ++it)
+            ax3d::launch_elem_phys(true, T, P, F.su, *it, X, sls, side[i++ % NSIDE]);
+        for (auto it = buckets_f.rbegin(); it != buckets_f.rend(); ++it)
+            ax3d::launch_elem_phys(false, T, P, F.fu, *it, X, sls, side[i++ % NSIDE]);
+        for (int k = 0; k < NSIDE; k++) {
+            CK(cudaEventRecord(ev_join[k], side[k]));
+            CK(cudaStreamWaitEvent(stream, ev_join[k], 0));
+        }
+    }
+    void compute_stiff() {
+        launch_elements();
         ax3d::launch_gather(P, T, F, stream);
     }
     void couple() { ax3d::launch_couple(P, F, d_sf3d.p, n_sf3d, stream); }
@@ -635,10 +672,7 @@ struct ax3d_domain {
             tend(1);
         }
         tbegin(AX3D_TIMER_ELEMENTS);
-        ax3d::launch_elem_fourier_solid(T, P, F.su, d_items_s.p, nitems_s, sls, stream);
-        ax3d::launch_elem_fourier_fluid(T, P, F.fu, d_items_f.p, nitems_f, stream);
-        for (auto &b : buckets_s) ax3d::launch_elem_phys(true, T, P, F.su, b, X, sls, stream);
-        for (auto &b : buckets_f) ax3d::launch_elem_phys(false, T, P, F.fu, b, X, sls, stream);
+        launch_elements();
         tend(n_elem_launches());
         tbegin(AX3D_TIMER_ASSEMBLE);
         ax3d::launch_gather(P, T, F, stream);

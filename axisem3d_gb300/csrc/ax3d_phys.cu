@@ -55,6 +55,7 @@ constexpr size_t SMEM_CAP = 227 * 1024;
 constexpr size_t SMEM_TWO = 112 * 1024;  // two CTAs per SM
 constexpr int64_t PREFETCH_MAX = 256 * 1024;  // largest per-element block asked of L2 ahead
 constexpr int CLUSTER_MAX = 8;
+constexpr int PLAN_BYTES = (sizeof(FftPlan) + 15) / 16 * 16;
 
 // n / d for n < 2^32 by multiply-high (round-up method of Granlund and Montgomery)
 struct FDiv {
@@ -458,7 +459,7 @@ __device__ void transform_r2c(float2 *buf, int S, int ns, int nr, const FftPlan 
 struct Pk {
     int kind, nr;
     const float2 *chirp;  // kind 1
-    const int32_t *ord;   // kind 2: order -> position
+    const int32_t *ord;   // kind 2: order -> position (shared memory)
     float inv_nr;
 };
 
@@ -476,8 +477,8 @@ __device__ __forceinline__ void zput(float2 *buf, int S, int col, int a, const P
         z1 = cmul(z1, __ldg(k.chirp + a));
         z2 = cmul(z2, __ldg(k.chirp + k.nr - a));
     } else if (k.kind == 2) {
-        s1 = __ldg(k.ord + a);
-        s2 = __ldg(k.ord + k.nr - a);
+        s1 = k.ord[a];
+        s2 = k.ord[k.nr - a];
     }
     buf[(int64_t)s1 * S + col] = z1;
     buf[(int64_t)s2 * S + col] = z2;
@@ -492,8 +493,8 @@ __device__ __forceinline__ void zget(const float2 *buf, int S, int col, int a, c
             z1 = z2 = cscale(k.inv_nr, cadd(x0, buf[(int64_t)(k.nr - 1) * S + col]));
         } else {
             const float2 xs = cscale(k.inv_nr, x0);
-            z1 = cadd(buf[(int64_t)__ldg(k.ord + a) * S + col], xs);
-            z2 = cadd(buf[(int64_t)__ldg(k.ord + k.nr - a) * S + col], xs);
+            z1 = cadd(buf[(int64_t)k.ord[a] * S + col], xs);
+            z2 = cadd(buf[(int64_t)k.ord[k.nr - a] * S + col], xs);
         }
     } else {
         z1 = buf[(int64_t)a * S + col];
@@ -627,11 +628,14 @@ __device__ __forceinline__ void quad6_split(const LaneOps &L, const Geo &g, bool
 
 struct PhysSmem {
     float2 *tw, *buf, *wscr;
-    int32_t *rev, *lst;
+    int32_t *rev, *ord, *lst;
+    FftPlan *pl;  // this element's plan
     __device__ PhysSmem(char *smem, int Lmax, int S) {
-        tw = reinterpret_cast<float2 *>(smem);
+        pl = reinterpret_cast<FftPlan *>(smem);
+        tw = reinterpret_cast<float2 *>(smem + PLAN_BYTES);
         rev = reinterpret_cast<int32_t *>(tw + Lmax);
-        lst = rev + ((Lmax + 1) & ~1);
+        ord = rev + ((Lmax + 1) & ~1);
+        lst = ord + ((Lmax + 1) & ~1);
         buf = reinterpret_cast<float2 *>(lst + 64);
         wscr = buf + (int64_t)Lmax * S;
     }
@@ -640,7 +644,7 @@ struct PhysSmem {
 }  // namespace
 
 size_t phys_smem_bytes(int Lmax, int nsq, int npts_chunk) {
-    return (size_t)8 * Lmax + (size_t)4 * ((Lmax + 1) & ~1) + 4 * 64 + (size_t)8 * Lmax * nsq * npts_chunk +
+    return (size_t)PLAN_BYTES + (size_t)8 * Lmax + (size_t)8 * ((Lmax + 1) & ~1) + 4 * 64 + (size_t)8 * Lmax * nsq * npts_chunk +
            (size_t)8 * NW * WSCR;
 }
 
@@ -724,13 +728,14 @@ __device__ __noinline__ void phase_stress(float2 *buf, int S, int nr, int ne_, c
     constexpr int NM = MAT == 0 ? 2 : MAT == 1 ? 5 : 21;
     constexpr int IT = MAT == 2 ? 1 : MAT == 1 ? 4 : 8;
     const int total = nr * ne_;
+    const FDiv fe = make_fdiv((uint32_t)ne_);
     for (int t0 = g.tid; t0 < total; t0 += g.n * IT) {
         float mv[IT][NM];
         int kk[IT];
 #pragma unroll
         for (int i = 0; i < IT; i++) {
             const int t = min(t0 + i * g.n, total - 1);
-            const int pos = t / ne_, pg = p0 + lst[t - pos * ne_];
+            const int pos = (int)fdiv((uint32_t)t, fe), pg = p0 + lst[t - pos * ne_];
             kk[i] = pk.kind == 1 ? pos : rev[pos];
 #pragma unroll
             for (int mm = 0; mm < NM; mm++) mv[i][mm] = __ldg(md + ((int64_t)mm * nr + kk[i]) * NPE + pg);
@@ -739,7 +744,7 @@ __device__ __noinline__ void phase_stress(float2 *buf, int S, int nr, int ne_, c
         for (int i = 0; i < IT; i++) {
             const int t = t0 + i * g.n;
             if (t >= total) break;
-            const int pos = t / ne_, pp = lst[t - pos * ne_];
+            const int pos = (int)fdiv((uint32_t)t, fe), pp = lst[t - pos * ne_];
             const SampleAt sa(pos, pk, rev);
             float2 zz[3];
 #pragma unroll
@@ -766,13 +771,14 @@ __device__ __noinline__ void phase_stress_att(float2 *buf, int S, int nr, int na
     const int64_t sl = (int64_t)nr * 6 * npa;
     const int total = nr * na_;
     const int nsls = sls.nsls;
+    const FDiv fa = make_fdiv((uint32_t)na_);
     for (int t0 = g.tid; t0 < total; t0 += g.n * IT) {
         float mv[IT][NM], rs[IT][6], sr[IT][6], dk[IT], dm[IT];
         int kk[IT], qq[IT];
 #pragma unroll
         for (int i = 0; i < IT; i++) {
             const int t = min(t0 + i * g.n, total - 1);
-            const int pos = t / na_, pg = p0 + lst[t - pos * na_];
+            const int pos = (int)fdiv((uint32_t)t, fa), pg = p0 + lst[t - pos * na_];
             qq[i] = att == 2 ? cg4_index(pg) : pg;
             kk[i] = pk.kind == 1 ? pos : rev[pos];
 #pragma unroll
@@ -793,7 +799,7 @@ __device__ __noinline__ void phase_stress_att(float2 *buf, int S, int nr, int na
         for (int i = 0; i < IT; i++) {
             const int t = t0 + i * g.n;
             if (t >= total) break;
-            const int pos = t / na_, pp = lst[t - pos * na_];
+            const int pos = (int)fdiv((uint32_t)t, fa), pp = lst[t - pos * na_];
             const SampleAt sa(pos, pk, rev);
             float2 zz[3];
 #pragma unroll
@@ -814,8 +820,9 @@ __device__ __noinline__ void phase_stress_att(float2 *buf, int S, int nr, int na
 // Phase 3 of a fluid element: sigma_i = K d_i chi (Acoustic3D.cpp:9-16) at every sample.
 __device__ __noinline__ void phase_stress_fluid(float2 *buf, int S, int nr, int pc, const int32_t *rev,
                                                 const float *md, const Pk pk, int p0, const Grp g) {
+    const FDiv fp = make_fdiv((uint32_t)pc);
     for (int t = g.tid; t < nr * pc; t += g.n) {
-        const int pos = t / pc, pp = t - pos * pc;
+        const int pos = (int)fdiv((uint32_t)t, fp), pp = t - pos * pc;
         const SampleAt sa(pos, pk, rev);
         const float K = __ldg(md + (int64_t)sa.k * NPE + p0 + pp);
 #pragma unroll
@@ -911,21 +918,28 @@ __global__ void __launch_bounds__(NT, 2)
         const int nr = T.nr[e];
         const int mat = ef_mat(flags), att = SOLID ? ef_att(flags) : 0;
         const bool tiso = SOLID && (mat == 1 || mat == 2);
-        const FftPlan &pl = X.plans[nr];
+        cl.sync();  // the whole cluster is done with the previous element's sequences
+        // the plan in shared memory: the transform passes read it once per pass
+        if (threadIdx.x < (int)(sizeof(FftPlan) / 4))
+            reinterpret_cast<int32_t *>(sm.pl)[threadIdx.x] =
+                reinterpret_cast<const int32_t *>(X.plans + nr)[threadIdx.x];
+        __syncthreads();
+        const FftPlan &pl = *sm.pl;
         const int L = pl.L, Lb = pl.Lbuf;
         const bool blue = pl.kind == 1;
         Pk pk;
         pk.kind = pl.kind;
         pk.nr = nr;
         pk.chirp = X.f2 + pl.chirp;
-        pk.ord = X.i32 + pl.ord;
+        pk.ord = sm.ord;
         pk.inv_nr = 1.f / (float)nr;
         const float hsc = pl.kind == 0 ? 0.5f / (float)nr : 0.5f;
         const float *md = T.moduli + T.mofs[e];
-        cl.sync();  // the whole cluster is done with the previous element's sequences
         for (int m = threadIdx.x; m < L; m += NT) tw[m] = X.f2[pl.tw + m];
         if (!blue)
             for (int m = threadIdx.x; m < nr; m += NT) sm.rev[m] = X.i32[pl.rev + m];
+        if (pl.kind == 2)
+            for (int m = threadIdx.x; m < nr; m += NT) sm.ord[m] = X.i32[pl.ord + m];
         // positions the packing does not write: the Nyquist order (even nr) and the
         // Bluestein padding [nr, Lb)
         if (nr % 2 == 0)
@@ -933,6 +947,7 @@ __global__ void __launch_bounds__(NT, 2)
         if (blue)
             for (int t = threadIdx.x; t < (Lb - nr) * ns; t += NT)
                 buf[(int64_t)(nr + t / ns) * S + t % ns] = make_float2(0.f, 0.f);
+        __syncthreads();  // the order table is read by the packing in phase 1
         // ---- phase 1: Hermitian-packed strain spectra (this CTA's orders, all points) ----
         phase_grad<SOLID>(T, P, u, e, nr, axial, tiso, pk, buf, S, Pc, crank, C, q);
         if constexpr (SOLID) {
