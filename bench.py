@@ -145,6 +145,19 @@ def allmax(world, x):
     return x
 
 
+def traffic_ratio():
+    """DRAM bytes per algorithmic byte of the element pass, from the committed ncu summary
+    (dram__bytes_read.sum + dram__bytes_write.sum of every element launch of one step of
+    the 20,000-element case, which has the benchmark's distributions): the full workload's
+    traffic is this ratio times its algorithmic bytes."""
+    p = ROOT / "profiles" / "k_elem_phys_dram_20k.md"
+    if p.exists():
+        for line in p.read_text().splitlines():
+            if line.startswith("dram bytes per algorithmic byte:"):
+                return float(line.split(":")[1].split()[0])
+    return None
+
+
 def peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -279,8 +292,10 @@ def run_gb300(args, world, rank, local):
                    "updates_per_step": upd, "parallelism": f"replicas x{world}",
                    "l2": "working set > L2 (no flush needed)"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None, "peak_source": src,
-                     "kernel": "element stiffness (k_elem_phys_solid, all buckets)",
+                     "frac": achieved / peak, "traffic": (tr * abytes if (tr := traffic_ratio()) else None),
+                     "traffic_unit": "bytes per step (ncu DRAM bytes per algorithmic byte x algorithmic bytes)",
+                     "peak_source": src,
+                     "kernel": "element stiffness (k_elem_phys, all buckets)",
                      "algorithmic_bytes_per_step": abytes, "kernel_ms_per_step": elem_ms},
         "phases_ms_per_step": {k: v[0] / args.steps for k, v in tm.items()},
         "gpu_launches": launches,
