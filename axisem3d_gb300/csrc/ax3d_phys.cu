@@ -904,6 +904,13 @@ __global__ void __launch_bounds__(NT, 2)
     extern __shared__ __align__(16) char smem[];
     cg::cluster_group cl = cg::this_cluster();
     const int crank = (int)cl.block_rank(), C = (int)cl.num_blocks();
+    // a barrier over the cluster (with its shared-memory fence) only when there is one
+    auto csync = [&]() {
+        if (C > 1)
+            cl.sync();
+        else
+            __syncthreads();
+    };
     const int S = NSQ * Pc;
     PhysSmem sm(smem, Lmax, S);
     float2 *tw = sm.tw, *buf = sm.buf;
@@ -918,7 +925,7 @@ __global__ void __launch_bounds__(NT, 2)
         const int nr = T.nr[e];
         const int mat = ef_mat(flags), att = SOLID ? ef_att(flags) : 0;
         const bool tiso = SOLID && (mat == 1 || mat == 2);
-        cl.sync();  // the whole cluster is done with the previous element's sequences
+        csync();  // the whole cluster is done with the previous element's sequences
         // the plan in shared memory: the transform passes read it once per pass
         if (threadIdx.x < (int)(sizeof(FftPlan) / 4))
             reinterpret_cast<int32_t *>(sm.pl)[threadIdx.x] =
@@ -964,7 +971,7 @@ __global__ void __launch_bounds__(NT, 2)
                 }
             }
         }
-        cl.sync();
+        csync();
         // ---- phases 2-4: the CTA's points, all its threads on each pass ----
         {
             const Grp g = grp_cta();
@@ -1020,11 +1027,11 @@ __global__ void __launch_bounds__(NT, 2)
             // ---- phase 4: back to orders 0..lim ----
             transform_r2c(gbuf, S, gns, nr, pl, tw, X.f2, g);
         }
-        cl.sync();
+        csync();
         // ---- phase 5: divergence of this CTA's orders, all points, into the element force ----
         phase_quad<SOLID>(T, e, nr, axial, tiso, pk, hsc, buf, S, Pc, crank, C, q);
     }
-    cl.sync();  // no CTA leaves while a peer may still read its shared memory
+    csync();  // no CTA leaves while a peer may still read its shared memory
 }
 
 // ------------------------------------------------------------------------------------
