@@ -13,6 +13,8 @@ constexpr int NPE = 25;  // GLL points per element
 constexpr int EF_AXIAL = 1;
 constexpr int EF_IN3D = 2;
 constexpr int EF_FLUID = 4;
+constexpr int EF_DIRECT = 1 << 12;  // owns all its points: assembles into their stiffness itself
+constexpr int EF_SOURCE = 1 << 13;  // carries a source term (its points' stiffness is not zero before assembly)
 __host__ __device__ inline int ef_mat(int f) { return (f >> 4) & 15; }
 __host__ __device__ inline int ef_att(int f) { return (f >> 8) & 3; }
 
@@ -31,6 +33,7 @@ struct ElemTable {
     float *mem;
     const int64_t *efofs;   // [E] complex offset into ef (element forces, [l][alpha][ncomp])
     float2 *ef;
+    float2 *stiff;          // solid point stiffness, written directly by EF_DIRECT elements
 };
 
 // Device view of the point table.
@@ -57,6 +60,8 @@ struct PointTable {
     const int64_t *sg_ref;
     const int32_t *fg_ptr;
     const int64_t *fg_ref;
+    const uint8_t *gskip;   // 1: the point's only element assembles it directly
+    int32_t sgather;        // some solid point needs the gather
     // row -> point maps (a row = one Fourier order of one point)
     int64_t nsrows, nfrows;
     const int32_t *srow_pt;

@@ -110,7 +110,7 @@ struct ax3d_domain {
     // ---------------- device ----------------
     DevBuf<int32_t> d_pnr, d_mslen, d_mflen, d_sflen, d_sg_ptr, d_fg_ptr, d_srow, d_frow;
     DevBuf<int8_t> d_pkind;
-    DevBuf<uint8_t> d_paxial, d_pfsurf;
+    DevBuf<uint8_t> d_paxial, d_pfsurf, d_gskip;
     DevBuf<int64_t> d_sofs, d_fofs, d_msofs, d_mfofs, d_sfofs, d_sg_ref, d_fg_ref;
     DevBuf<float> d_ms, d_mf, d_sfn, d_sfni;
     DevBuf<int32_t> d_epts, d_eflags, d_enr;
@@ -365,6 +365,25 @@ struct ax3d_domain {
                 for (int al = 0; al < n; al++) (fluid ? items_f : items_s).push_back(make_int2(e, al));
             }
         }
+        // physical-space solid elements that own all their points (solid points of no other
+        // element) subtract their forces straight into the point stiffness; the gather
+        // skips those points
+        std::vector<uint8_t> p_gskip(np, 0);
+        for (int e = 0; e < ne; e++) {
+            if ((e_flags[e] & ax3d::EF_FLUID) || !(e_flags[e] & ax3d::EF_IN3D)) continue;
+            bool own = true;
+            for (int l = 0; l < 25 && own; l++) {
+                const int p = e_pts[(int64_t)e * 25 + l];
+                own = p_kind[p] == AX3D_POINT_SOLID && sref[p].size() == 1;
+            }
+            if (!own) continue;
+            e_flags[e] |= ax3d::EF_DIRECT;
+            if (std::find(s_elem.begin(), s_elem.end(), e) != s_elem.end()) e_flags[e] |= ax3d::EF_SOURCE;
+            for (int l = 0; l < 25; l++) p_gskip[e_pts[(int64_t)e * 25 + l]] = 1;
+        }
+        int32_t sgather = 0;
+        for (int p = 0; p < np; p++)
+            if (p_kind[p] != AX3D_POINT_FLUID && !p_gskip[p]) sgather = 1;
         std::vector<int32_t> sg_ptr(np + 1, 0), fg_ptr(np + 1, 0);
         std::vector<int64_t> sg_ref, fg_ref;
         for (int p = 0; p < np; p++) {
@@ -413,6 +432,7 @@ struct ax3d_domain {
         d_sfn.upload(p_sfn.empty() ? std::vector<float>{0.f} : p_sfn, st);
         d_sfni.upload(p_sfni.empty() ? std::vector<float>{0.f} : p_sfni, st);
         d_sg_ptr.upload(sg_ptr, st);
+        d_gskip.upload(p_gskip.empty() ? std::vector<uint8_t>{0} : p_gskip, st);
         d_fg_ptr.upload(fg_ptr, st);
         d_sg_ref.upload(sg_ref.empty() ? std::vector<int64_t>{0} : sg_ref, st);
         d_fg_ref.upload(fg_ref.empty() ? std::vector<int64_t>{0} : fg_ref, st);
@@ -527,6 +547,8 @@ struct ax3d_domain {
         P.sfn = d_sfn.p;
         P.sfni = d_sfni.p;
         P.sg_ptr = d_sg_ptr.p;
+        P.gskip = d_gskip.p;
+        P.sgather = sgather;
         P.sg_ref = d_sg_ref.p;
         P.fg_ptr = d_fg_ptr.p;
         P.fg_ref = d_fg_ref.p;
@@ -547,6 +569,7 @@ struct ax3d_domain {
         T.mem = d_mem.p;
         T.efofs = d_efofs.p;
         T.ef = d_ef.p;
+        T.stiff = d_ss.p;
         F.su = d_su.p; F.sv = d_sv.p; F.sa = d_sa.p; F.ss = d_ss.p; F.sku = d_sku.p; F.skv = d_skv.p;
         F.fu = d_fu.p; F.fv = d_fv.p; F.fa = d_fa.p; F.fs = d_fs.p; F.fku = d_fku.p; F.fkv = d_fkv.p;
         CK(cudaStreamSynchronize(st));
@@ -580,30 +603,30 @@ struct ax3d_domain {
     // go round-robin, longest transforms first, over side streams forked from and joined
     // back into the main stream, so one bucket's tail overlaps the next bucket's start;
     // a graph capture of the step records the same fork and join.
-    void launch_elements() {
+    void launch_elements(bool overwrite) {
         ax3d::launch_elem_fourier_solid(T, P, F.su, d_items_s.p, nitems_s, sls, stream);
         ax3d::launch_elem_fourier_fluid(T, P, F.fu, d_items_f.p, nitems_f, stream);
         const int nb = (int)(buckets_s.size() + buckets_f.size());
         if (nb == 0) return;
         if (nb == 1) {
-            for (auto &b : buckets_s) ax3d::launch_elem_phys(true, T, P, F.su, b, X, sls, stream);
-            for (auto &b : buckets_f) ax3d::launch_elem_phys(false, T, P, F.fu, b, X, sls, stream);
+            for (auto &b : buckets_s) ax3d::launch_elem_phys(true, T, P, F.su, b, X, sls, overwrite, stream);
+            for (auto &b : buckets_f) ax3d::launch_elem_phys(false, T, P, F.fu, b, X, sls, overwrite, stream);
             return;
         }
         CK(cudaEventRecord(ev_fork, stream));
         for (int k = 0; k < NSIDE; k++) CK(cudaStreamWaitEvent(side[k], ev_fork, 0));
         int i = 0;
         for (auto it = buckets_s.rbegin(); it != buckets_s.rend(); ++it)
-            ax3d::launch_elem_phys(true, T, P, F.su, *it, X, sls, side[i++ % NSIDE]);
+            ax3d::launch_elem_phys(true, T, P, F.su, *it, X, sls, overwrite, side[i++ % NSIDE]);
         for (auto it = buckets_f.rbegin(); it != buckets_f.rend(); ++it)
-            ax3d::launch_elem_phys(false, T, P, F.fu, *it, X, sls, side[i++ % NSIDE]);
+            ax3d::launch_elem_phys(false, T, P, F.fu, *it, X, sls, overwrite, side[i++ % NSIDE]);
         for (int k = 0; k < NSIDE; k++) {
             CK(cudaEventRecord(ev_join[k], side[k]));
             CK(cudaStreamWaitEvent(stream, ev_join[k], 0));
         }
     }
     void compute_stiff() {
-        launch_elements();
+        launch_elements(false);
         ax3d::launch_gather(P, T, F, stream);
     }
     void couple() { ax3d::launch_couple(P, F, d_sf3d.p, n_sf3d, stream); }
@@ -672,11 +695,11 @@ struct ax3d_domain {
             tend(1);
         }
         tbegin(AX3D_TIMER_ELEMENTS);
-        launch_elements();
+        launch_elements(true);  // the Newmark update above cleared the point stiffness
         tend(n_elem_launches());
         tbegin(AX3D_TIMER_ASSEMBLE);
         ax3d::launch_gather(P, T, F, stream);
-        tend(nrow);
+        tend((P.nsrows > 0 && P.sgather) + (P.nfrows > 0));
         tbegin(AX3D_TIMER_COUPLE);
         couple();
         tend((P.nsrows > 0) + (n_sf3d > 0));

@@ -64,8 +64,11 @@ void launch_elem_fourier_solid(const ElemTable &T, const PointTable &P, const fl
                                const int2 *items, int nitems, const SLS &sls, cudaStream_t s);
 void launch_elem_fourier_fluid(const ElemTable &T, const PointTable &P, const float2 *fu,
                                const int2 *items, int nitems, cudaStream_t s);
+// overwrite: the point stiffness of direct-assembly elements without a source term is known
+// to be zero (the Newmark update just cleared it), so they store -force instead of
+// subtracting
 void launch_elem_phys(bool solid, const ElemTable &T, const PointTable &P, const float2 *u, const PhysBucket &b,
-                      const PhysTables &X, const SLS &sls, cudaStream_t s);
+                      const PhysTables &X, const SLS &sls, bool overwrite, cudaStream_t s);
 
 void launch_gather(const PointTable &P, const ElemTable &T, const Fields &F, cudaStream_t s);
 void launch_newmark(const PointTable &P, const Fields &F, float dt, float half_dt,

@@ -53,7 +53,7 @@ constexpr int RESEED = 8;    // direct DFT: exact twiddle reload interval
 constexpr int DIRECT_MAX = 257;  // largest prime handled by a direct pass
 constexpr size_t SMEM_CAP = 227 * 1024;
 constexpr size_t SMEM_TWO = 112 * 1024;  // two CTAs per SM
-constexpr int64_t PREFETCH_MAX = 256 * 1024;  // largest per-element block asked of L2 ahead
+constexpr int64_t PREFETCH_MAX = 1024 * 1024;  // largest per-element block asked of L2 ahead
 constexpr int CLUSTER_MAX = 8;
 constexpr int PLAN_BYTES = (sizeof(FftPlan) + 15) / 16 * 16;
 
@@ -558,12 +558,14 @@ struct USrc {
     }
 };
 
-// Ask L2 for [ptr, ptr + bytes) ahead of a phase that reads it in scattered order.
-__device__ __forceinline__ void prefetch_l2(const void *ptr, int64_t bytes) {
+// Ask L2 for slice `part` of `parts` of [ptr, ptr + bytes), ahead of a phase that reads it
+// in scattered order.
+__device__ __forceinline__ void prefetch_l2(const void *ptr, int64_t bytes, int part = 0, int parts = 1) {
     const char *c = static_cast<const char *>(ptr);
-    const int64_t first = reinterpret_cast<uintptr_t>(c) & 127;
-    for (int64_t o = (int64_t)threadIdx.x * 128 - first; o < bytes; o += (int64_t)blockDim.x * 128)
-        if (o >= 0) asm volatile("prefetch.global.L2 [%0];" ::"l"(c + o));
+    const int64_t lo = bytes * part / parts, hi = bytes * (part + 1) / parts;
+    const int64_t first = (reinterpret_cast<uintptr_t>(c) + lo) & 127;
+    for (int64_t o = lo + (int64_t)threadIdx.x * 128 - first; o < hi; o += (int64_t)blockDim.x * 128)
+        if (o >= lo) asm volatile("prefetch.global.L2 [%0];" ::"l"(c + o));
 }
 
 // Divergence of one Fourier order (computeQuad6, Gradient.cpp:267-317) with one
@@ -760,60 +762,75 @@ __device__ __noinline__ void phase_stress(float2 *buf, int S, int nr, int ne_, c
 
 // Phase 3, attenuated points: elastic stress minus the memory variables (applyToStress),
 // then updateMemoryVariables (Attenuation3D_Full.cpp:16-50, Attenuation3D_CG4.cpp:16-62).
-// All loads of an item are issued before its arithmetic.
-template <int MAT>
+// All loads of an item (moduli, every memory variable, stressR, the two attenuation
+// moduli) are issued together and the memory variables stay in registers for the update,
+// so an item costs one round trip to memory.  LMAX (>= nsls) bounds the registers held.
+template <int MAT, int LMAX>
 __device__ __noinline__ void phase_stress_att(float2 *buf, int S, int nr, int na_, const int32_t *lst,
                                               const int32_t *rev, const float *md, const Pk pk, int p0,
                                               int att, float *mem, const float *am, const SLS &sls, const Grp g) {
     constexpr int NM = MAT == 0 ? 2 : MAT == 1 ? 5 : 21;
-    constexpr int IT = 1;
     const int npa = att == 2 ? 4 : NPE;
     const int64_t sl = (int64_t)nr * 6 * npa;
     const int total = nr * na_;
     const int nsls = sls.nsls;
     const FDiv fa = make_fdiv((uint32_t)na_);
-    for (int t0 = g.tid; t0 < total; t0 += g.n * IT) {
-        float mv[IT][NM], rs[IT][6], sr[IT][6], dk[IT], dm[IT];
-        int kk[IT], qq[IT];
+    const float third = (float)(1.0 / 3.0);
+    for (int t = g.tid; t < total; t += g.n) {
+        const int pos = (int)fdiv((uint32_t)t, fa), pp = lst[t - pos * na_], pg = p0 + pp;
+        const int qq = att == 2 ? cg4_index(pg) : pg;
+        const int k = pk.kind == 1 ? pos : rev[pos];
+        float mv[NM], rv[LMAX][6], sr[6];
 #pragma unroll
-        for (int i = 0; i < IT; i++) {
-            const int t = min(t0 + i * g.n, total - 1);
-            const int pos = (int)fdiv((uint32_t)t, fa), pg = p0 + lst[t - pos * na_];
-            qq[i] = att == 2 ? cg4_index(pg) : pg;
-            kk[i] = pk.kind == 1 ? pos : rev[pos];
+        for (int mm = 0; mm < NM; mm++) mv[mm] = __ldg(md + ((int64_t)mm * nr + k) * NPE + pg);
+        float *R = mem + (int64_t)k * 6 * npa + qq;
 #pragma unroll
-            for (int mm = 0; mm < NM; mm++) mv[i][mm] = __ldg(md + ((int64_t)mm * nr + kk[i]) * NPE + pg);
-            const float *R = mem + (int64_t)kk[i] * 6 * npa + qq[i];
+        for (int l = 0; l < LMAX; l++)
 #pragma unroll
-            for (int c = 0; c < 6; c++) {
-                sr[i][c] = R[nsls * sl + c * npa];
-                rs[i][c] = 0.f;
-            }
-            for (int l = 0; l < nsls; l++)
+            for (int c = 0; c < 6; c++) rv[l][c] = l < nsls ? R[l * sl + c * npa] : 0.f;
 #pragma unroll
-                for (int c = 0; c < 6; c++) rs[i][c] += R[l * sl + c * npa];
-            dk[i] = am[(int64_t)kk[i] * npa + qq[i]];
-            dm[i] = am[(int64_t)nr * npa + (int64_t)kk[i] * npa + qq[i]];
+        for (int c = 0; c < 6; c++) sr[c] = R[nsls * sl + c * npa];
+        const float dk = am[(int64_t)k * npa + qq], dm = am[(int64_t)nr * npa + (int64_t)k * npa + qq];
+        const SampleAt sa(pos, pk, rev);
+        float2 zz[3];
+#pragma unroll
+        for (int s = 0; s < 3; s++) zz[s] = sample_in(buf, S, 3 * pp + s, sa, pk);
+        const float e6[6] = {zz[0].x, zz[0].y, zz[1].x, zz[1].y, zz[2].x, zz[2].y};
+        float s6[6];
+        elastic(MAT, e6, s6, [&](int mm) { return mv[mm]; });
+        // applyToStress: sigma -= R_l, one solid after another
+#pragma unroll
+        for (int l = 0; l < LMAX; l++)
+            if (l < nsls)
+#pragma unroll
+                for (int c = 0; c < 6; c++) s6[c] -= rv[l][c];
+        // updateMemoryVariables: R_l <- a_l R_l + b_l stressR_old + g_l stressR_new
+        const float dk3 = 3.f * dk, dmu2 = 2.f * dm;
+        const float e3 = third * ((e6[0] + e6[1]) + e6[2]);
+        float sn[6];
+        if (sls.do_kappa) {
+            const float sii3 = dk3 * e3;
+            sn[0] = sii3 + dmu2 * (e6[0] - e3);
+            sn[1] = sii3 + dmu2 * (e6[1] - e3);
+            sn[2] = sii3 + dmu2 * (e6[2] - e3);
+        } else {
+            sn[0] = dmu2 * (e6[0] - e3);
+            sn[1] = dmu2 * (e6[1] - e3);
+            sn[2] = -(sn[0] + sn[1]);
         }
+        sn[3] = dm * e6[3];
+        sn[4] = dm * e6[4];
+        sn[5] = dm * e6[5];
 #pragma unroll
-        for (int i = 0; i < IT; i++) {
-            const int t = t0 + i * g.n;
-            if (t >= total) break;
-            const int pos = (int)fdiv((uint32_t)t, fa), pp = lst[t - pos * na_];
-            const SampleAt sa(pos, pk, rev);
-            float2 zz[3];
+        for (int l = 0; l < LMAX; l++)
+            if (l < nsls)
 #pragma unroll
-            for (int s = 0; s < 3; s++) zz[s] = sample_in(buf, S, 3 * pp + s, sa, pk);
-            const float e6[6] = {zz[0].x, zz[0].y, zz[1].x, zz[1].y, zz[2].x, zz[2].y};
-            float s6[6];
-            elastic(MAT, e6, s6, [&](int mm) { return mv[i][mm]; });
+                for (int c = 0; c < 6; c++)
+                    R[l * sl + c * npa] = (sls.a[l] * rv[l][c] + sls.b[l] * sr[c]) + sls.g[l] * sn[c];
 #pragma unroll
-            for (int c = 0; c < 6; c++) s6[c] -= rs[i][c];
-            float *R = mem + (int64_t)kk[i] * 6 * npa + qq[i];
-            sls_update_from(sls, R, R + nsls * sl, sl, (int64_t)npa, e6, sr[i], dk[i], dm[i]);
+        for (int c = 0; c < 6; c++) R[nsls * sl + c * npa] = sn[c];
 #pragma unroll
-            for (int s = 0; s < 3; s++) sample_out(buf, S, 3 * pp + s, sa, pk, make_float2(s6[2 * s], s6[2 * s + 1]));
-        }
+        for (int s = 0; s < 3; s++) sample_out(buf, S, 3 * pp + s, sa, pk, make_float2(s6[2 * s], s6[2 * s + 1]));
     }
 }
 
@@ -834,8 +851,9 @@ __device__ __noinline__ void phase_stress_fluid(float2 *buf, int S, int nr, int 
 // order into the element force; the last chunk's stress spectra come from the packed
 // sequences, the earlier chunks' from the scratch.
 template <bool SOLID>
-__device__ __noinline__ void phase_quad(const ElemTable &T, int e, int nr, bool axial, bool tiso, const Pk pk,
-                                        float hsc, float2 *buf, int S, int Pc, int crank, int C, float2 *q) {
+__device__ __noinline__ void phase_quad(const ElemTable &T, const PointTable &P, int e, int nr, bool axial,
+                                        bool tiso, bool direct, bool rmw, const Pk pk, float hsc, float2 *buf, int S,
+                                        int Pc, int crank, int C, float2 *q) {
     constexpr int NSQ = SOLID ? 3 : 2;
     constexpr int NC = SOLID ? 6 : 3;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -857,7 +875,25 @@ __device__ __noinline__ void phase_quad(const ElemTable &T, int e, int nr, bool 
         c2 = tr[75 + p];
     }
     float2 *ef = T.ef + T.efofs[e];
+    // direct assembly (gatherStiffFromElement, SolidPoint.cpp:197-209, for the point's only
+    // element): stiff -= force up to the point's own Nyquist limit, its Nyquist row zeroed
+    float2 *st = nullptr;
+    int pnu = 0, plim = 0;
+    if (SOLID && direct) {
+        const int pt = T.pts[e * NPE + p];
+        const int pnr = P.nr[pt];
+        pnu = pnr / 2;
+        plim = pnu - (pnr % 2 == 0);
+        st = T.stiff + P.sofs[pt];
+    }
     for (int a = crank * NW + warp; a < n; a += C * NW) {
+        float2 old[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+        const bool row = SOLID && direct && active && a <= pnu;
+        if (rmw && row && a <= plim) {  // issued before the divergence so the loads overlap it
+            old[0] = st[(int64_t)a * 3];
+            old[1] = st[(int64_t)a * 3 + 1];
+            old[2] = st[(int64_t)a * 3 + 2];
+        }
         float2 sig[NC];
 #pragma unroll
         for (int i = 0; i < NC; i++) sig[i] = make_float2(0.f, 0.f);
@@ -874,9 +910,17 @@ __device__ __noinline__ void phase_quad(const ElemTable &T, int e, int nr, bool 
             if (active && tiso) rtz_spz(sig, s1, c1, s2, c2);
             float2 f[3];
             quad6_split(Lo, g, axial, a, sig, q, active && a <= lim, f);
-            if (active) {
+            if (a > lim) f[0] = f[1] = f[2] = make_float2(0.f, 0.f);
+            if (direct) {
+                if (row) {
+                    float2 *o = st + (int64_t)a * 3;
+                    const bool keep = a <= plim;
+                    o[0] = keep ? csub(old[0], f[0]) : make_float2(0.f, 0.f);
+                    o[1] = keep ? csub(old[1], f[1]) : make_float2(0.f, 0.f);
+                    o[2] = keep ? csub(old[2], f[2]) : make_float2(0.f, 0.f);
+                }
+            } else if (active) {
                 float2 *o = ef + ((int64_t)p * n + a) * 3;
-                if (a > lim) f[0] = f[1] = f[2] = make_float2(0.f, 0.f);
                 o[0] = f[0];
                 o[1] = f[1];
                 o[2] = f[2];
@@ -899,7 +943,7 @@ template <bool SOLID>
 __global__ void __launch_bounds__(NT, 2)
     k_elem_phys(const __grid_constant__ ElemTable T, const __grid_constant__ PointTable P,
                 const float2 *__restrict__ u, const int32_t *__restrict__ elems, int count, int Pc, int Lmax,
-                const __grid_constant__ PhysTables X, const __grid_constant__ SLS sls) {
+                const __grid_constant__ PhysTables X, const __grid_constant__ SLS sls, int overwrite) {
     constexpr int NSQ = SOLID ? 3 : 2;
     extern __shared__ __align__(16) char smem[];
     cg::cluster_group cl = cg::this_cluster();
@@ -958,16 +1002,16 @@ __global__ void __launch_bounds__(NT, 2)
         // ---- phase 1: Hermitian-packed strain spectra (this CTA's orders, all points) ----
         phase_grad<SOLID>(T, P, u, e, nr, axial, tiso, pk, buf, S, Pc, crank, C, q);
         if constexpr (SOLID) {
-            if (C == 1) {
-                const int nm = mat == 0 ? 2 : mat == 1 ? 5 : 21;
-                const int npa = att == 2 ? 4 : NPE;
-                const int64_t sb = (int64_t)4 * nr * (NPE * nm + (att ? (sls.nsls + 1) * 6 * npa + 2 * npa : 0));
-                if (sb <= PREFETCH_MAX) {
-                    prefetch_l2(md, (int64_t)4 * NPE * nr * nm);
-                    if (att) {
-                        prefetch_l2(T.mem + T.memofs[e], (int64_t)4 * (sls.nsls + 1) * nr * 6 * npa);
-                        prefetch_l2(T.attm + T.aofs[e], (int64_t)4 * 2 * nr * npa);
-                    }
+            // the stress phase's moduli and memory variables, asked of L2 while the C2R
+            // runs; each CTA of a cluster asks for its share
+            const int nm = mat == 0 ? 2 : mat == 1 ? 5 : 21;
+            const int npa = att == 2 ? 4 : NPE;
+            const int64_t sb = (int64_t)4 * nr * (NPE * nm + (att ? (sls.nsls + 1) * 6 * npa + 2 * npa : 0));
+            if (sb <= PREFETCH_MAX) {
+                prefetch_l2(md, (int64_t)4 * NPE * nr * nm, crank, C);
+                if (att) {
+                    prefetch_l2(T.mem + T.memofs[e], (int64_t)4 * (sls.nsls + 1) * nr * 6 * npa, crank, C);
+                    prefetch_l2(T.attm + T.aofs[e], (int64_t)4 * 2 * nr * npa, crank, C);
                 }
             }
         }
@@ -1010,12 +1054,21 @@ __global__ void __launch_bounds__(NT, 2)
                 if (na_ > 0) {
                     float *mem = T.mem + T.memofs[e];
                     const float *am = T.attm + T.aofs[e];
-                    if (mat == 0)
-                        phase_stress_att<0>(gbuf, S, nr, na_, lst + 32, sm.rev, md, pk, gpg, att, mem, am, sls, g);
-                    else if (mat == 1)
-                        phase_stress_att<1>(gbuf, S, nr, na_, lst + 32, sm.rev, md, pk, gpg, att, mem, am, sls, g);
-                    else
-                        phase_stress_att<2>(gbuf, S, nr, na_, lst + 32, sm.rev, md, pk, gpg, att, mem, am, sls, g);
+                    if (sls.nsls <= 3) {
+                        if (mat == 0)
+                            phase_stress_att<0, 3>(gbuf, S, nr, na_, lst + 32, sm.rev, md, pk, gpg, att, mem, am, sls, g);
+                        else if (mat == 1)
+                            phase_stress_att<1, 3>(gbuf, S, nr, na_, lst + 32, sm.rev, md, pk, gpg, att, mem, am, sls, g);
+                        else
+                            phase_stress_att<2, 3>(gbuf, S, nr, na_, lst + 32, sm.rev, md, pk, gpg, att, mem, am, sls, g);
+                    } else {
+                        if (mat == 0)
+                            phase_stress_att<0, 8>(gbuf, S, nr, na_, lst + 32, sm.rev, md, pk, gpg, att, mem, am, sls, g);
+                        else if (mat == 1)
+                            phase_stress_att<1, 8>(gbuf, S, nr, na_, lst + 32, sm.rev, md, pk, gpg, att, mem, am, sls, g);
+                        else
+                            phase_stress_att<2, 8>(gbuf, S, nr, na_, lst + 32, sm.rev, md, pk, gpg, att, mem, am, sls, g);
+                    }
                 }
             } else {
                 phase_stress_fluid(gbuf, S, nr, gpc, sm.rev, md, pk, gpg, g);
@@ -1029,7 +1082,8 @@ __global__ void __launch_bounds__(NT, 2)
         }
         csync();
         // ---- phase 5: divergence of this CTA's orders, all points, into the element force ----
-        phase_quad<SOLID>(T, e, nr, axial, tiso, pk, hsc, buf, S, Pc, crank, C, q);
+        phase_quad<SOLID>(T, P, e, nr, axial, tiso, (flags & EF_DIRECT) != 0, !overwrite || (flags & EF_SOURCE), pk, hsc,
+                          buf, S, Pc, crank, C, q);
     }
     csync();  // no CTA leaves while a peer may still read its shared memory
 }
@@ -1311,17 +1365,17 @@ int phys_grid(const PhysBucket &b, bool solid, int num_sms) {
 }
 
 void launch_elem_phys(bool solid, const ElemTable &T, const PointTable &P, const float2 *u, const PhysBucket &b,
-                      const PhysTables &X, const SLS &sls, cudaStream_t s) {
+                      const PhysTables &X, const SLS &sls, bool overwrite, cudaStream_t s) {
     if (b.count <= 0) return;
     cudaLaunchAttribute at[1];
     if (solid) {
         cudaLaunchConfig_t cfg = phys_config<true>(b, at, s);
         cudaLaunchKernelEx(&cfg, k_elem_phys<true>, T, P, u, (const int32_t *)b.elems, b.count, b.npts_chunk,
-                           b.L_max, X, sls);
+                           b.L_max, X, sls, (int)overwrite);
     } else {
         cudaLaunchConfig_t cfg = phys_config<false>(b, at, s);
         cudaLaunchKernelEx(&cfg, k_elem_phys<false>, T, P, u, (const int32_t *)b.elems, b.count, b.npts_chunk,
-                           b.L_max, X, sls);
+                           b.L_max, X, sls, (int)overwrite);
     }
 }
 

@@ -26,6 +26,7 @@ __global__ void k_gather_solid(PointTable P, ElemTable T, float2 *__restrict__ s
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < P.nsrows;
          r += (int64_t)gridDim.x * blockDim.x) {
         const int pt = P.srow_pt[r];
+        if (P.gskip[pt]) continue;  // assembled by its element
         const int a = (int)(r - P.sofs[pt] / 3);
         const int nr = P.nr[pt], lim = nr / 2 - (nr % 2 == 0);
         float2 *s = ss + r * 3;
@@ -63,7 +64,7 @@ __global__ void k_gather_fluid(PointTable P, ElemTable T, float2 *__restrict__ f
 }
 
 void launch_gather(const PointTable &P, const ElemTable &T, const Fields &F, cudaStream_t s) {
-    if (P.nsrows) k_gather_solid<<<grid_for(P.nsrows, ROW_THREADS), ROW_THREADS, 0, s>>>(P, T, F.ss);
+    if (P.nsrows && P.sgather) k_gather_solid<<<grid_for(P.nsrows, ROW_THREADS), ROW_THREADS, 0, s>>>(P, T, F.ss);
     if (P.nfrows) k_gather_fluid<<<grid_for(P.nfrows, ROW_THREADS), ROW_THREADS, 0, s>>>(P, T, F.fs);
 }
 

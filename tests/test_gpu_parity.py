@@ -166,3 +166,23 @@ def test_wisdom_learning_matches_oracle(ax3d_lib):
     wg, wo = g.get_wisdom(), o.get_wisdom()
     assert wg.shape == wo.shape == (spec.n_points,)
     assert (np.abs(wg - wo) <= 1).all() and (wg != wo).mean() <= 0.01
+
+
+@pytest.mark.parametrize("att", [ATT_CG4, ATT_FULL])
+def test_element_benchmark_matches_oracle(ax3d_lib, att):
+    """The element-stiffness benchmark's domain (elements that own their points, so they
+    assemble directly into the point stiffness), Nu 8-40, a few Newmark steps."""
+    from oracle.oracle_py import OracleDomain
+    from axisem3d_gb300 import workloads as W
+    from axisem3d_gb300.capi import Ax3dDomain
+    spec = W.element_benchmark(n_elem=24, seed=7, att=att, nu_min=8, nu_max=40)
+    u0 = W.benchmark_displacement(spec, seed=8)
+    g, o = Ax3dDomain(spec), OracleDomain(spec)
+    for d in (g, o):
+        d.set("displ", "solid", u0)
+        d.compute_stiff()
+    assert rel(g.get("stiff", "solid"), o.get("stiff", "solid")) <= TOL
+    for d in (g, o):
+        d.step(3)
+    for which in ("displ", "veloc", "accel"):
+        assert rel(g.get(which, "solid"), o.get(which, "solid")) <= TOL, which
