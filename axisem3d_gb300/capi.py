@@ -76,6 +76,10 @@ def bind(lib: C.CDLL, prefix: str, field_ctype, extra_double_io: bool = False):
     f("set_wisdom_learning").argtypes = [C.c_void_p, C.c_int32, C.c_float]
     f("learn_wisdom").argtypes = [C.c_void_p, C.c_float]
     f("get_wisdom").argtypes = [C.c_void_p, P_I32]
+    f("add_surface").argtypes = [C.c_void_p, C.c_int32, P_I32, P_I32, C.c_int32]
+    f("surface_record_size").argtypes = [C.c_void_p]
+    f("surface_record_size").restype = C.c_int64
+    f("read_surface").argtypes = [C.c_void_p, C.c_int32, C.c_int32, field_ctype]
 
 
 _LIB = None
@@ -159,6 +163,9 @@ class _DomainBase:
         if len(spec.r_elem):
             self._ck(self._call("add_receivers", h, len(spec.r_elem), _p(c(spec.r_elem, np.int32), C.c_int32),
                                 _p(c(spec.r_phi, np.float32), C.c_float), _p(c(spec.r_w, np.float32), C.c_float)))
+        if len(spec.sf_elem):
+            self._ck(self._call("add_surface", h, len(spec.sf_elem), _p(c(spec.sf_elem, np.int32), C.c_int32),
+                                _p(c(spec.sf_side, np.int32), C.c_int32), int(spec.sf_interval)))
         self._ck(self._call("finalize", h))
         self.nsolid = int(self._call("field_size", h, 0))
         self.nfluid = int(self._call("field_size", h, 1))
@@ -228,6 +235,21 @@ class _DomainBase:
         out = np.zeros(max(n * nrec * 3, 1), self.field_dtype)
         self._ck(self._call("read_seismograms", self.h, int(first), int(n), _p(out, self.field_ctype)))
         return out[:n * nrec * 3].astype(np.float64).reshape(n, nrec, 3)
+
+    def surface(self, first: int, n: int) -> list[np.ndarray]:
+        """Whole-surface records first..first+n-1 (SurfaceRecorder): one complex array per
+        edge, shaped [n][3][5][Nu_e + 1] ([component][point on the side][order])."""
+        row = int(self._call("surface_record_size", self.h))
+        out = np.zeros(max(n * row, 1), self.complex_dtype)
+        self._ck(self._call("read_surface", self.h, int(first), int(n), _p(out.view(self.field_dtype),
+                                                                             self.field_ctype)))
+        out = out[:n * row].reshape(n, row)
+        edges, ofs = [], 0
+        for e in self.spec.sf_elem:
+            na = int(self.spec.element_nr()[e]) // 2 + 1
+            edges.append(out[:, ofs:ofs + 15 * na].reshape(n, 3, 5, na))
+            ofs += 15 * na
+        return edges
 
     def close(self):
         if getattr(self, "h", None):

@@ -133,6 +133,14 @@ struct ax3d_domain {
     DevBuf<int32_t> d_relem;
     DevBuf<float> d_rphi, d_rw, d_seis;
     int seis_cap = 0;
+    // whole-surface recorder: edges (element, side), record every sf_interval steps
+    std::vector<int32_t> sf_elem, sf_side;
+    int sf_interval = 1;
+    int64_t sf_row = 0;  // complex values per record
+    int sf_cap = 0;      // records the buffer holds
+    DevBuf<int32_t> d_sfe, d_sfs;
+    DevBuf<int64_t> d_sfrofs;
+    DevBuf<float2> d_surf;
     DevBuf<int32_t> d_flag;
     DevBuf<int32_t> d_tstep, d_targ;  // step counter (1-based) and explicit step index
     DevBuf<float> d_wis_max;          // [P][4] largest Hilbert norm per component (s, phi, z, fluid)
@@ -518,6 +526,20 @@ struct ax3d_domain {
         d_relem.upload(r_elem.empty() ? std::vector<int32_t>{0} : r_elem, st);
         d_rphi.upload(r_phi.empty() ? std::vector<float>{0.f} : r_phi, st);
         d_rw.upload(r_w.empty() ? std::vector<float>{0.f} : r_w, st);
+        if (!sf_elem.empty()) {
+            std::vector<int64_t> rofs(sf_elem.size());
+            sf_row = 0;
+            for (size_t i = 0; i < sf_elem.size(); i++) {
+                rofs[i] = sf_row;
+                sf_row += (int64_t)15 * (e_nr[sf_elem[i]] / 2 + 1);
+            }
+            d_sfe.upload(sf_elem, st);
+            d_sfs.upload(sf_side, st);
+            d_sfrofs.upload(rofs, st);
+            sf_cap = std::max<int>(((int)stf.size() + sf_interval - 1) / sf_interval, 1);
+            d_surf.alloc((size_t)sf_cap * sf_row);
+            d_surf.zero(st);
+        }
         seis_cap = std::max<int>((int)stf.size(), 1);
         d_seis.alloc((size_t)seis_cap * std::max<size_t>(r_elem.size(), 1) * 3);
         d_seis.zero(st);
@@ -631,12 +653,32 @@ struct ax3d_domain {
     }
     void couple() { ax3d::launch_couple(P, F, d_sf3d.p, n_sf3d, stream); }
     void record(int t) {
-        if (r_elem.empty()) return;
         if (t < 0) throw Error(AX3D_ERR_ARG, "ax3d_record || negative step");
-        if (t >= seis_cap) grow_seis(t + 1);
+        if (r_elem.empty() && sf_elem.empty()) return;
         set_targ(t);
-        ax3d::launch_record(P, T, F.su, d_relem.p, d_rphi.p, d_rw.p, (int)r_elem.size(), d_seis.p, seis_cap,
-                            d_targ.p, 0, stream);
+        if (!r_elem.empty()) {
+            if (t >= seis_cap) grow_seis(t + 1);
+            ax3d::launch_record(P, T, F.su, d_relem.p, d_rphi.p, d_rw.p, (int)r_elem.size(), d_seis.p, seis_cap,
+                                d_targ.p, 0, stream);
+        }
+        if (!sf_elem.empty()) {
+            if (t / sf_interval >= sf_cap) grow_surf(t / sf_interval + 1);
+            ax3d::launch_record_surface(P, T, F.su, d_sfe.p, d_sfs.p, d_sfrofs.p, (int)sf_elem.size(), d_surf.p, sf_row,
+                                        sf_cap, d_targ.p, 0, sf_interval, stream);
+        }
+    }
+    void grow_surf(int need) {
+        const int cap = std::max(need, sf_cap * 2);
+        DevBuf<float2> nb;
+        nb.alloc((size_t)cap * sf_row);
+        nb.zero(stream);
+        CK(cudaMemcpyAsync(nb.p, d_surf.p, (size_t)sf_cap * sf_row * sizeof(float2), cudaMemcpyDeviceToDevice,
+                           stream));
+        CK(cudaStreamSynchronize(stream));
+        std::swap(nb.p, d_surf.p);
+        std::swap(nb.n, d_surf.n);
+        sf_cap = cap;
+        drop_graph();  // the captured step holds the old buffer address
     }
     void grow_seis(int need) {
         int cap = std::max(need, seis_cap * 2);
@@ -709,6 +751,12 @@ struct ax3d_domain {
                                 d_tstep.p, -1, stream);
             tend(1);
         }
+        if (!sf_elem.empty()) {
+            tbegin(AX3D_TIMER_RECORD);
+            ax3d::launch_record_surface(P, T, F.su, d_sfe.p, d_sfs.p, d_sfrofs.p, (int)sf_elem.size(), d_surf.p, sf_row,
+                                        sf_cap, d_tstep.p, -1, sf_interval, stream);
+            tend(1);
+        }
         if (wis_interval > 0) {
             tbegin(AX3D_TIMER_OTHER);
             ax3d::launch_learn_wisdom(P, F, d_wis_max.p, d_wis_nu.p, wis_cutoff, d_tstep.p, wis_interval, stream);
@@ -732,6 +780,8 @@ struct ax3d_domain {
             CK(cudaEventRecord(s0, stream));
         }
         if (!r_elem.empty() && tstep - 1 + nsteps > seis_cap) grow_seis(tstep - 1 + nsteps);
+        if (!sf_elem.empty() && nsteps > 0 && (tstep - 2 + nsteps) / sf_interval >= sf_cap)
+            grow_surf((tstep - 2 + nsteps) / sf_interval + 1);
         if (timers || !use_graphs) {
             // phase timers need events between the phases: plain launches
             for (int s = 0; s < nsteps; s++) enqueue_step();
@@ -788,6 +838,7 @@ struct ax3d_domain {
             for (auto *b : {&d_sku, &d_skv, &d_fku, &d_fkv}) b->zero(stream);
         d_mem.zero(stream);
         d_seis.zero(stream);
+        if (!sf_elem.empty()) d_surf.zero(stream);
         d_flag.zero(stream);
         reset_wisdom(stream);
         tstep = 1;
@@ -915,6 +966,26 @@ int ax3d_add_receivers(ax3d_domain *d, int32_t n, const int32_t *elem, const flo
     });
 }
 
+int ax3d_add_surface(ax3d_domain *d, int32_t n, const int32_t *elem, const int32_t *side, int32_t interval) {
+    return guard([&] {
+        if (!d || n < 0 || (n && (!elem || !side)) || interval < 1)
+            throw Error(AX3D_ERR_ARG, "ax3d_add_surface || bad argument");
+        if (d->finalized) throw Error(AX3D_ERR_STATE, "ax3d_add_surface || domain already finalized");
+        if (!d->sf_elem.empty() && interval != d->sf_interval)
+            throw Error(AX3D_ERR_ARG, "ax3d_add_surface || one record interval per domain");
+        for (int i = 0; i < n; i++) {
+            if (elem[i] < 0 || elem[i] >= (int)d->e_nr.size())
+                throw Error(AX3D_ERR_ARG, "ax3d_add_surface || element out of range");
+            if (d->e_flags[elem[i]] & ax3d::EF_FLUID)
+                throw Error(AX3D_ERR_ARG, "ax3d_add_surface || surface edge on a fluid element");
+            if (side[i] < 0 || side[i] > 3) throw Error(AX3D_ERR_ARG, "ax3d_add_surface || side must be 0..3");
+        }
+        d->sf_interval = interval;
+        d->sf_elem.insert(d->sf_elem.end(), elem, elem + n);
+        d->sf_side.insert(d->sf_side.end(), side, side + n);
+    });
+}
+
 int ax3d_finalize(ax3d_domain *d) {
     return guard([&] {
         if (!d) throw Error(AX3D_ERR_ARG, "ax3d_finalize || null domain");
@@ -975,6 +1046,20 @@ int ax3d_read_seismograms(ax3d_domain *d, int32_t first, int32_t nsteps, float *
         if (first + nsteps > d->seis_cap) throw Error(AX3D_ERR_ARG, "ax3d_read_seismograms || steps not recorded");
         const size_t row = d->r_elem.size() * 3;
         CK(cudaMemcpyAsync(out, d->d_seis.p + (size_t)first * row, (size_t)nsteps * row * sizeof(float),
+                           cudaMemcpyDeviceToHost, d->stream));
+        CK(cudaStreamSynchronize(d->stream));
+    });
+}
+
+int64_t ax3d_surface_record_size(const ax3d_domain *d) { return d && d->finalized ? d->sf_row : -1; }
+
+int ax3d_read_surface(ax3d_domain *d, int32_t first, int32_t count, float *out) {
+    return guard([&] {
+        if (!d || !out || first < 0 || count < 0) throw Error(AX3D_ERR_ARG, "ax3d_read_surface || bad argument");
+        d->need_final();
+        if (d->sf_elem.empty()) throw Error(AX3D_ERR_STATE, "ax3d_read_surface || no surface recorder");
+        if (first + count > d->sf_cap) throw Error(AX3D_ERR_ARG, "ax3d_read_surface || records not taken");
+        CK(cudaMemcpyAsync(out, d->d_surf.p + (size_t)first * d->sf_row, (size_t)count * d->sf_row * sizeof(float2),
                            cudaMemcpyDeviceToHost, d->stream));
         CK(cudaStreamSynchronize(d->stream));
     });

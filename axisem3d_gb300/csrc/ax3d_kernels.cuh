@@ -82,6 +82,9 @@ void launch_source(const PointTable &P, const ElemTable &T, const Fields &F,
 void launch_record(const PointTable &P, const ElemTable &T, const float2 *su,
                    const int32_t *rec_elem, const float *rec_phi, const float *rec_w, int nrec,
                    float *out_base, int cap, const int32_t *tptr, int tofs, cudaStream_t s);
+void launch_record_surface(const PointTable &P, const ElemTable &T, const float2 *su, const int32_t *elem,
+                           const int32_t *side, const int64_t *rofs, int nedge, float2 *out_base, int64_t rowlen,
+                           int cap, const int32_t *tptr, int tofs, int interval, cudaStream_t s);
 void launch_stability(const float2 *su, int64_t ns, const float2 *fu, int64_t nf,
                       int32_t *flag, const int32_t *tptr, int interval, cudaStream_t s);
 void launch_advance(int32_t *tptr, cudaStream_t s);

@@ -6,6 +6,8 @@
 // use one thread per row.  Points with a physical-space (3D) mass or coupling
 // (Mass3D.cpp:13-57, SFCoupling3D.cpp:9-56) take one CTA each and transform their nr
 // azimuthal samples with a direct DFT in shared memory.
+#include <algorithm>
+
 #include "ax3d_elem_ops.cuh"
 #include "ax3d_kernels.cuh"
 
@@ -459,6 +461,39 @@ void launch_record(const PointTable &P, const ElemTable &T, const float2 *su, co
 }
 
 // ---------------- stability (Domain::checkStability, Domain.cpp:237-275) ----------------
+// SurfaceRecorder::record with SolidElement::feedDispOnSide (SolidElement.cpp:354-390):
+// when the step index t is a multiple of interval, record t / interval gets, per edge,
+// [component][point q on the side][order a], a <= Nu_e; a point's rows 0..Nu_p are copied,
+// the orders above them are zero.  Block per edge.
+__global__ void k_record_surface(PointTable P, ElemTable T, const float2 *__restrict__ su, const int32_t *elem,
+                                 const int32_t *side, const int64_t *rofs, int nedge, float2 *out_base,
+                                 int64_t rowlen, int cap, const int32_t *tptr, int tofs, int interval) {
+    const int t = *tptr + tofs;
+    if (t < 0 || t % interval) return;
+    const int rec = t / interval;
+    if (rec >= cap) return;
+    for (int i = blockIdx.x; i < nedge; i += gridDim.x) {
+        const int e = elem[i], sd = side[i];
+        const int n = T.nr[e] / 2 + 1;
+        float2 *o = out_base + (int64_t)rec * rowlen + rofs[i];
+        for (int idx = threadIdx.x; idx < 15 * n; idx += blockDim.x) {
+            const int c = idx / (5 * n), rem = idx - c * 5 * n, q = rem / n, a = rem - q * n;
+            const int ipol = sd == 1 ? 4 : sd == 3 ? 0 : q;
+            const int jpol = sd == 0 ? 0 : sd == 2 ? 4 : q;
+            const int pt = T.pts[e * NPE + ipol * 5 + jpol];
+            o[idx] = a <= P.nr[pt] / 2 ? su[P.sofs[pt] + (int64_t)a * 3 + c] : make_float2(0.f, 0.f);
+        }
+    }
+}
+
+void launch_record_surface(const PointTable &P, const ElemTable &T, const float2 *su, const int32_t *elem,
+                           const int32_t *side, const int64_t *rofs, int nedge, float2 *out_base, int64_t rowlen,
+                           int cap, const int32_t *tptr, int tofs, int interval, cudaStream_t s) {
+    if (nedge <= 0) return;
+    k_record_surface<<<std::min(nedge, 152 * 8), 128, 0, s>>>(P, T, su, elem, side, rofs, nedge, out_base, rowlen,
+                                                             cap, tptr, tofs, interval);
+}
+
 __global__ void k_stability(const float2 *__restrict__ su, int64_t ns, const float2 *__restrict__ fu, int64_t nf,
                             int32_t *flag, const int32_t *tptr, int interval) {
     if (interval <= 0 || (*tptr) % interval != 0) return;  // Newmark.cpp:68-70

@@ -166,6 +166,12 @@ def _rot(theta, phi):
     return np.array([[ct * cp, -sp, st * cp], [ct * sp, cp, st * sp], [-st, 0.0, ct]])
 
 
+def _colat(s, z):
+    """Geodesy::rtheta (Geodesy.cpp:13-16): colatitude of (s, z), 0 at the centre."""
+    r = math.hypot(s, z)
+    return 0.0 if r < 1e-300 else math.acos(max(-1.0, min(1.0, z / r)))
+
+
 def glob_to_src(theta_g, phi_g, src_theta, src_phi):
     """Geodesy::rotateGlob2Src on the unit sphere (no ellipticity)."""
     x = np.array([math.sin(theta_g) * math.cos(phi_g), math.sin(theta_g) * math.sin(phi_g), math.cos(theta_g)])
@@ -430,6 +436,7 @@ class Simulation:
         self._source(spec)
         self._stf(spec)
         self._receivers(spec)
+        self._surface(spec)
         self.spec = spec
         return spec
 
@@ -557,6 +564,86 @@ class Simulation:
         spec.r_phi = np.array([r[6] for r in rec], np.float32)
         spec.r_w = np.array([r[8] for r in rec], np.float32).reshape(len(rec), 25)
 
+    def _surface(self, spec):
+        """OUT_STATIONS_WHOLE_SURFACE (ReceiverCollection.cpp:186-220, 281-300): 'false', or
+        'true [radius_km [dist_min_deg dist_max_deg [from_upper]]]'.  Every solid element
+        whose centre lies inside the distance window and on the requested side of the radius
+        contributes its edge at that radius (Quad::edgeAtRadius, Quad.cpp:747-770); edges are
+        tagged by their smallest colatitude (SurfaceRecorder::initialize)."""
+        par = self.par
+        v = par.values.get("OUT_STATIONS_WHOLE_SURFACE") or ["false"]
+        self.surface_edges = []
+        if not par.get("OUT_STATIONS_WHOLE_SURFACE", bool):
+            return
+        if len(v) not in (1, 2, 4, 5):
+            raise ValueError("ReceiverCollection::buildInparam || Invalid parameter, keyword = OUT_STATIONS_WHOLE_SURFACE.")
+        r, dmin, dmax, upper = self.R, 0.0, 180.0, False
+        if len(v) >= 2:
+            r = float(v[1]) * 1e3
+        if len(v) >= 4:
+            dmin, dmax = float(v[2]), float(v[3])
+        if len(v) == 5:
+            upper = par.get("OUT_STATIONS_WHOLE_SURFACE", bool, 4)
+        nodes = self.nodes4  # [E, 2, 4] (s, z) of the four corners
+        rn = np.hypot(nodes[:, 0], nodes[:, 1])
+        # ExodusModel::mDistTolerance: the shortest quad side / 1000 (ExodusModel.cpp:70-86)
+        dn = nodes - np.roll(nodes, -1, axis=2)
+        tol = float(np.hypot(dn[:, 0], dn[:, 1]).min()) / 1000.0
+        edges = []
+        for e in range(len(rn)):
+            if self.fluid[e]:
+                continue
+            sc, zc = nodes[e, 0].mean(), nodes[e, 1].mean()
+            dist = math.degrees(_colat(sc, zc))
+            if dist < dmin or dist > dmax or upper != (rn[e].mean() > r):
+                continue
+            for k in range(4):
+                if abs(rn[e, k] - r) < tol and abs(rn[e, (k + 1) % 4] - r) < tol:
+                    # colatitudes of the side's first and last GLL points (SurfaceInfo.cpp:9-16,
+                    # Element::getCoordsOnSide); point index ipol * 5 + jpol
+                    q0, q1 = ((0, 20), (20, 24), (4, 24), (0, 4))[k]
+                    c = self.crds[e].reshape(25, 2)
+                    th0, th1 = _colat(*c[q0]), _colat(*c[q1])
+                    edges.append((min(th0, th1), e, k, th0, th1))
+                    break
+        edges.sort()
+        self.surface_edges = edges
+        spec.sf_elem = np.array([x[1] for x in edges], np.int32)
+        spec.sf_side = np.array([x[2] for x in edges], np.int32)
+        spec.sf_interval = max(par.get("OUT_STATIONS_RECORD_INTERVAL", int), 1)
+
+    def write_surface_netcdf(self, records, path=None):
+        """output/stations/axisem3d_surface.nc (SurfaceIO.cpp:63-150): time_points, per edge
+        edge_<tag>r / edge_<tag>i [steps][5 x 3 x (Nu + 1)] with the record's
+        [component][point][order] layout, theta [edges][2], GLL, GLJ and the source
+        attributes.  records: one [steps][3][5][Nu + 1] complex array per edge."""
+        from . import spectral as S
+        path = Path(path or self.output_dir / "stations" / "axisem3d_surface.nc")
+        path.parent.mkdir(parents=True, exist_ok=True)
+        n = records[0].shape[0] if records else 0
+        iv = self.spec.sf_interval
+        ds = NC.Dataset()
+        ds.add_dim("ntime", n)
+        ds.add_dim("nedge", len(records))
+        ds.add_dim("two", 2)
+        ds.add_dim("npol", 5)
+        ds.add_var("time_points", ("ntime",), -self.shift + np.arange(n) * iv * self.dt)
+        for tag, rec in enumerate(records):
+            w = rec.shape[1] * rec.shape[2] * rec.shape[3]
+            ds.add_dim(f"ncol_{tag}", w)
+            flat = rec.reshape(n, w)
+            ds.add_var(f"edge_{tag}r", ("ntime", f"ncol_{tag}"), flat.real.astype(np.float32))
+            ds.add_var(f"edge_{tag}i", ("ntime", f"ncol_{tag}"), flat.imag.astype(np.float32))
+        ds.add_var("theta", ("nedge", "two"), np.array([[x[3], x[4]] for x in self.surface_edges], np.float64))
+        ds.add_var("GLL", ("npol",), S.gll()[0])
+        ds.add_var("GLJ", ("npol",), S.glj()[0])
+        # spherical geometry: both flattenings are zero
+        ds.attrs.update({"source_latitude": float(self.src_lat), "source_longitude": float(self.src_lon),
+                         "source_depth": float(self.src_dep), "source_flattening": 0.0,
+                         "surface_flattening": 0.0, "radius": float(self.R)})
+        NC.write(path, ds)
+        return path
+
     def _locate(self, s, z):
         """Quad::invMapping by Newton iterations (Mapping.cpp:17-28) over candidate elements."""
         cen = self.crds.mean(1)
@@ -616,10 +703,18 @@ class Simulation:
         seis = dom.seismograms(0, n)
         return self.rotate(seis), dom
 
+    def surface_records(self, dom, nsteps=None):
+        """The whole-surface records of steps 0..nsteps-1 (one per OUT_STATIONS_RECORD_INTERVAL
+        steps, ReceiverCollection.cpp:314-321), one complex array per edge in tag order."""
+        n = nsteps or self.nsteps
+        if not self.surface_edges:
+            return []
+        return dom.surface(0, -(-n // self.spec.sf_interval))
+
 
 def write_inputs(input_dir, mesh_kw=None, nu=2, stf="gauss", hdur=50.0, steps=2000, record_length=None,
                  n_stations=20, depth_km=100.0, seed=0, attenuation=False, system="source_centered",
-                 models3d=(), lucky=False):
+                 models3d=(), lucky=False, whole_surface="false"):
     """Seeded inputs of the small benchmark configuration: mesh, four parfiles, CMTSOLUTION
     (moment tensor ~ N(0, 1e20 N*m) written in dyn*cm) and STATIONS at uniform distance."""
     from . import mesher
@@ -639,7 +734,7 @@ def write_inputs(input_dir, mesh_kw=None, nu=2, stf="gauss", hdur=50.0, steps=20
         f"SOURCE_FILE CMTSOLUTION\nSOURCE_TIME_FUNCTION {stf}\nSOURCE_STF_HALF_DURATION {hdur}\n"
         f"OUT_STATIONS_FILE STATIONS\nOUT_STATIONS_SYSTEM {system}\nOUT_STATIONS_DUPLICATED rename\n"
         f"OUT_STATIONS_FORMAT netcdf\nOUT_STATIONS_COMPONENTS RTZ\nOUT_STATIONS_RECORD_INTERVAL 1\n"
-        f"OUT_STATIONS_DUMP_INTERVAL 1000\nOUT_STATIONS_WHOLE_SURFACE false\nOUT_STATIONS_DEPTH_REF false\n")
+        f"OUT_STATIONS_DUMP_INTERVAL 1000\nOUT_STATIONS_WHOLE_SURFACE {whole_surface}\nOUT_STATIONS_DEPTH_REF false\n")
     (d / "inparam.advanced").write_text(
         f"ATTENUATION_CG4 true\nATTENUATION_SPECFEM_LEGACY false\nATTENUATION_QKAPPA true\n"
         f"OPTION_VERBOSE_LEVEL essential\nOPTION_STABILITY_INTERVAL 100\nOPTION_LOOP_INFO_INTERVAL 1000\n"

@@ -59,6 +59,10 @@ class DomainSpec:
     r_elem: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
     r_phi: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
     r_w: np.ndarray = field(default_factory=lambda: np.zeros((0, 25), np.float32))
+    # whole-surface recorder: edges (element, side 0..3) recorded every sf_interval steps
+    sf_elem: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    sf_side: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    sf_interval: int = 1
     kahan: bool = False
     stability_interval: int = 0
 

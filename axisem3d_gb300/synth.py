@@ -130,11 +130,13 @@ def annulus_domain(seed=0, n_theta=4, n_r=3, r_in=3000e3, r_out=6371e3, theta_ma
                    nu_random=False, nu_max=None, fluid_layers=(), mat=MAT_ISO, in3d=False,
                    att=ATT_NONE, nsls=3, mass3d=False, couple3d=False, dt=0.05, source=True,
                    n_receivers=3, stf_len=64, stability_interval=0, kahan=False, fluid3d=False,
-                   perturb=0.04, lucky=False):
+                   perturb=0.04, lucky=False, surface_interval=0):
     """Connected spherical-element mesh on an (r, theta) grid.
 
     Element (ir, it) spans radii [rs[ir], rs[ir+1]] and colatitudes [ts[it], ts[it+1]];
-    elements with it = 0 touch the axis.  fluid_layers lists the ir that are fluid."""
+    elements with it = 0 touch the axis.  fluid_layers lists the ir that are fluid.
+    surface_interval > 0 records the outer surface (side 2, eta = +1, of every solid
+    element of the top layer) every surface_interval steps."""
     rng = np.random.default_rng(seed)
     rs = np.linspace(r_in, r_out, n_r + 1)
     ts = np.linspace(0.0, theta_max, n_theta + 1)
@@ -339,6 +341,11 @@ def annulus_domain(seed=0, n_theta=4, n_r=3, r_in=3000e3, r_out=6371e3, theta_ma
         nsls=nsls if att != ATT_NONE else 0, att_alpha=alpha, att_beta=beta, att_gamma=gamma,
         att_do_kappa=True, sources=sources, stf=stf, r_elem=r_elem, r_phi=r_phi, r_w=r_w,
         kahan=kahan, stability_interval=stability_interval, **ea)
+    if surface_interval > 0:
+        top = n_r - 1
+        spec.sf_elem = np.array([top * n_theta + it for it in range(n_theta) if not fluid_elem[top, it]], np.int32)
+        spec.sf_side = np.full(len(spec.sf_elem), 2, np.int32)
+        spec.sf_interval = int(surface_interval)
     return spec
 
 

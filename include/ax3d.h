@@ -137,6 +137,15 @@ int ax3d_set_stf(ax3d_domain *d, int32_t nsteps, const float *stf);
 int ax3d_add_receivers(ax3d_domain *d, int32_t n, const int32_t *elem, const float *phi,
                        const float *weights);
 
+/* Whole-surface recorder (SurfaceRecorder::addElement / record,
+   SOLVER/src/core/output/surface/SurfaceRecorder.cpp:22-104): the Fourier displacement of
+   the 5 GLL points on side side[i] (0: jpol = 0, 1: ipol = nPol, 2: jpol = nPol, 3: ipol = 0)
+   of solid element elem[i], recorded when the step index is a multiple of interval.  One
+   record holds, per edge in the order given, [component][point on the side][order] for
+   orders 0..Nu_e (Nu_e = element nr / 2); orders a point does not hold are zero
+   (SolidElement::feedDispOnSide, SolidElement.cpp:354-390).  Before ax3d_finalize. */
+int ax3d_add_surface(ax3d_domain *d, int32_t n, const int32_t *elem, const int32_t *side, int32_t interval);
+
 /* Ends set-up (Mesh::release + Domain::initializeRecorders): checks sizes, builds the
    gather lists and element buckets, uploads everything. */
 int ax3d_finalize(ax3d_domain *d);
@@ -163,6 +172,13 @@ int ax3d_step(ax3d_domain *d, int32_t nsteps);
 
 /* Recorded (s, phi, z) displacement [nsteps][nrec][3] for steps first..first+nsteps-1. */
 int ax3d_read_seismograms(ax3d_domain *d, int32_t first, int32_t nsteps, float *out);
+
+/* Complex values in one whole-surface record: sum over edges of 15 (Nu_e + 1). */
+int64_t ax3d_surface_record_size(const ax3d_domain *d);
+
+/* Whole-surface records first..first+count-1 (record r = step index r * interval), complex
+   interleaved: count x ax3d_surface_record_size values. */
+int ax3d_read_surface(ax3d_domain *d, int32_t first, int32_t count, float *out);
 
 /* Zero every field and memory variable (Domain::resetZero, Domain.cpp:67-74); the
    internal step counter restarts at 1. */

@@ -93,6 +93,10 @@ struct Oracle {
     };
     std::vector<Rec> recs;
     std::vector<Real> seis;  // [step][nrec][3]
+    // whole-surface recorder: edges (element, side), one record per sf_interval steps
+    std::vector<int> sf_elem, sf_side;
+    int sf_interval = 1;
+    std::vector<C> surf;     // [record][edges: [c][q][alpha]]
 
     bool finalized = false;
     int tstep = 1;  // next step (1-based)
@@ -234,6 +238,7 @@ struct Oracle {
         }
         tstep = 1;
         seis.clear();
+        surf.clear();
         reset_wisdom();
     }
 
@@ -876,8 +881,39 @@ struct Oracle {
         }
     }
 
-    // SolidElement::computeGroundMotion (SolidElement.cpp:189-216) for every receiver.
+    // Complex values of one whole-surface record: 15 (Nu_e + 1) per edge.
+    int64_t surface_record_size() const {
+        int64_t n = 0;
+        for (int e : sf_elem) n += 15 * (int64_t)(elems[e].nu + 1);
+        return n;
+    }
+    // SurfaceRecorder::record (SurfaceRecorder.cpp:86-104) with SolidElement::feedDispOnSide
+    // (SolidElement.cpp:354-390): every point's Fourier rows 0..Nu_p, orders above them zero.
+    void record_surface(int t) {
+        if (sf_elem.empty() || t % sf_interval) return;
+        const int64_t row = surface_record_size();
+        const size_t rec = (size_t)(t / sf_interval);
+        if (surf.size() < (rec + 1) * row) surf.resize((rec + 1) * row, C(0));
+        C *o = surf.data() + rec * row;
+        for (size_t i = 0; i < sf_elem.size(); i++) {
+            const Elem &e = elems[sf_elem[i]];
+            const int n = e.nu + 1, sd = sf_side[i];
+            for (int q = 0; q < nPol + 1; q++) {
+                const int ipol = sd == 1 ? nPol : sd == 3 ? 0 : q;
+                const int jpol = sd == 0 ? 0 : sd == 2 ? nPol : q;
+                const Point &pt = pts[e.pts[ipol * (nPol + 1) + jpol]];
+                for (int c = 0; c < 3; c++)
+                    for (int a = 0; a < n; a++)
+                        o[(c * (nPol + 1) + q) * n + a] = a <= pt.nu ? su[pt.sofs + (int64_t)a * 3 + c] : C(0);
+            }
+            o += 15 * n;
+        }
+    }
+
+    // SolidElement::computeGroundMotion (SolidElement.cpp:189-216) for every receiver; the
+    // whole-surface recorder records with it (Domain::record).
     void record(int t) {
+        record_surface(t);
         if (recs.empty()) return;
         size_t need = (size_t)(t + 1) * recs.size() * 3;
         if (seis.size() < need) seis.resize(need, Real(0));

@@ -87,6 +87,28 @@ int guard(F f) {
         }                                                                                        \
         return 0;                                                                                \
     }                                                                                            \
+    int P##add_surface(void *dv, int32_t n, const int32_t *elem, const int32_t *side,            \
+                       int32_t interval) {                                                       \
+        auto *d = static_cast<P##dom *>(dv);                                                     \
+        if (interval < 1) return AX3D_ERR_ARG;                                                   \
+        d->sf_interval = interval;                                                               \
+        d->sf_elem.insert(d->sf_elem.end(), elem, elem + n);                                     \
+        d->sf_side.insert(d->sf_side.end(), side, side + n);                                     \
+        return 0;                                                                                \
+    }                                                                                            \
+    int64_t P##surface_record_size(void *d) {                                                    \
+        return static_cast<P##dom *>(d)->surface_record_size();                                  \
+    }                                                                                            \
+    int P##read_surface(void *dv, int32_t first, int32_t n, double *out) {                       \
+        auto *d = static_cast<P##dom *>(dv);                                                     \
+        const size_t row = (size_t)d->surface_record_size();                                     \
+        if (first < 0 || d->surf.size() < (size_t)(first + n) * row) return AX3D_ERR_ARG;        \
+        for (size_t i = 0; i < (size_t)n * row; i++) {                                           \
+            out[2 * i] = (double)d->surf[(size_t)first * row + i].real();                        \
+            out[2 * i + 1] = (double)d->surf[(size_t)first * row + i].imag();                    \
+        }                                                                                        \
+        return 0;                                                                                \
+    }                                                                                            \
     int P##finalize(void *d) {                                                                   \
         return guard([&] {                                                                       \
             static_cast<P##dom *>(d)->finalize();                                                \

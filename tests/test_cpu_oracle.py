@@ -146,3 +146,30 @@ def test_oracle_wisdom_labels():
     d.learn_wisdom(1e-3)
     w = d.get_wisdom()
     assert w.max() <= 3 and w.min() >= 0 and (w == 3).mean() > 0.5
+
+
+def test_oracle_surface_record_is_side_displacement():
+    """The whole-surface record holds every side point's own Fourier rows (orders above a
+    point's Nu zero), [component][point on the side][order] (SolidElement::feedDispOnSide)."""
+    from axisem3d_gb300 import synth
+    from oracle.oracle_py import OracleDomain
+    spec = synth.annulus_domain(n_theta=3, n_r=2, nu_random=True, nu_max=6, stf_len=6, surface_interval=2)
+    o = OracleDomain(spec)
+    su, _ = synth.random_fields(spec, seed=21)
+    o.set("displ", "solid", su)
+    o.record(0)
+    o.record(1)  # not a multiple of the interval: no record
+    o.record(2)
+    rec = o.surface(0, 2)
+    so, _ = spec.point_offsets()
+    enr = spec.element_nr()
+    for k, e in enumerate(spec.sf_elem):
+        na = enr[e] // 2 + 1
+        for q in range(5):
+            pt = spec.e_pts[e, q * 5 + 4]  # side 2: jpol = 4
+            nu = spec.p_nr[pt] // 2
+            for c in range(3):
+                want = np.zeros(na, complex)
+                want[:nu + 1] = su[so[pt] + 3 * np.arange(nu + 1) + c]
+                np.testing.assert_allclose(rec[k][0, c, q], want, rtol=1e-6, atol=1e-12)
+    np.testing.assert_allclose(rec[0][0], rec[0][1])  # the field did not change between the records

@@ -186,3 +186,18 @@ def test_element_benchmark_matches_oracle(ax3d_lib, att):
         d.step(3)
     for which in ("displ", "veloc", "accel"):
         assert rel(g.get(which, "solid"), o.get(which, "solid")) <= TOL, which
+
+
+def test_surface_recorder_matches_oracle(ax3d_lib):
+    """Whole-surface recording every 3 steps of a time loop (SurfaceRecorder), GPU vs oracle."""
+    from oracle.oracle_py import OracleDomain
+    from axisem3d_gb300.capi import Ax3dDomain
+    spec = synth.annulus_domain(in3d=True, mat=MAT_TISO, att=ATT_CG4, nu_random=True, nu_max=9, stf_len=13,
+                                surface_interval=3)
+    g, o = Ax3dDomain(spec), OracleDomain(spec)
+    su, _ = synth.random_fields(spec, seed=17, scale=1e-6)
+    for d in (g, o):
+        d.set("displ", "solid", su)
+        d.step(13)
+    for a, b in zip(g.surface(0, 5), o.surface(0, 5)):
+        assert rel(a, b) <= TOL

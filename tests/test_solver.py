@@ -220,3 +220,50 @@ def test_full_solver_3d_gpu_matches_oracle(inputs_3d, ax3d_lib):
     assert np.linalg.norm(a - b) <= 1e-5 * np.linalg.norm(b)
     x, y = g.get("displ", "fluid"), o.get("displ", "fluid")
     assert np.linalg.norm(x - y) <= 1e-5 * np.linalg.norm(y)
+
+
+def test_whole_surface_edges_and_netcdf(tmp_path_factory):
+    """OUT_STATIONS_WHOLE_SURFACE: every solid element touching the outer radius gives its
+    outer side, tags follow the smallest colatitude, records land in axisem3d_surface.nc."""
+    from oracle.oracle_py import OracleDomain
+    d = tmp_path_factory.mktemp("sf") / "input"
+    solver.write_inputs(d, mesh_kw=SMALL_MESH, steps=30, hdur=20.0, n_stations=2, seed=4,
+                        whole_surface="true 6371.0 0 90")
+    sim = solver.Simulation(d, output_dir=d.parent / "output")
+    spec = sim.build()
+    edges = sim.surface_edges
+    assert len(edges) > 0 and len(spec.sf_elem) == len(edges)
+    th = np.array([min(x[3], x[4]) for x in edges])
+    assert (np.diff(th) >= 0).all() and th.min() >= 0 and th.max() < np.pi / 2
+    sides = {0: (0, 20), 1: (20, 24), 2: (4, 24), 3: (0, 4)}
+    for _, e, k, t0, t1 in edges:
+        c = sim.crds[e].reshape(25, 2)
+        q0, q1 = sides[k]
+        np.testing.assert_allclose(np.hypot(*c[[q0, q1]].T), sim.R, rtol=1e-9)
+        assert not sim.fluid[e]
+    # the same window from below the surface is empty; a bad option size raises
+    par = solver.Parameters(d)
+    par.values["OUT_STATIONS_WHOLE_SURFACE"] = ["true", "6371.0", "0", "90", "true"]
+    sim.par = par
+    sim._surface(spec)
+    assert sim.surface_edges == []
+    par.values["OUT_STATIONS_WHOLE_SURFACE"] = ["true", "6371.0", "0"]
+    with pytest.raises(ValueError, match="WHOLE_SURFACE"):
+        sim._surface(spec)
+    sim = solver.Simulation(d, output_dir=d.parent / "output")
+    spec = sim.build()
+    o = OracleDomain(spec)
+    o.step(30)
+    recs = sim.surface_records(o, 30)
+    assert len(recs) == len(edges) and recs[0].shape == (30, 3, 5, 3)
+    assert max(np.abs(r).max() for r in recs) > 0
+    path = sim.write_surface_netcdf(recs)
+    ds = NC.read(path)
+    assert path.name == "axisem3d_surface.nc"
+    assert ds["time_points"].shape == (30,) and ds["theta"].shape == (len(edges), 2)
+    np.testing.assert_allclose(ds["theta"][:, 0], [x[3] for x in edges])
+    w = 15 * 3
+    for tag in (0, len(edges) - 1):
+        np.testing.assert_allclose(ds[f"edge_{tag}r"], recs[tag].real.reshape(30, w).astype(np.float32))
+        np.testing.assert_allclose(ds[f"edge_{tag}i"], recs[tag].imag.reshape(30, w).astype(np.float32))
+    assert float(ds.attrs["radius"][0]) == sim.R
