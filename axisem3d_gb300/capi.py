@@ -77,6 +77,7 @@ def bind(lib: C.CDLL, prefix: str, field_ctype, extra_double_io: bool = False):
     f("learn_wisdom").argtypes = [C.c_void_p, C.c_float]
     f("get_wisdom").argtypes = [C.c_void_p, P_I32]
     f("add_surface").argtypes = [C.c_void_p, C.c_int32, P_I32, P_I32, C.c_int32]
+    f("add_ocean_load").argtypes = [C.c_void_p, C.c_int32, P_I32, P_I32, C.POINTER(C.c_float)]
     f("surface_record_size").argtypes = [C.c_void_p]
     f("surface_record_size").restype = C.c_int64
     f("read_surface").argtypes = [C.c_void_p, C.c_int32, C.c_int32, field_ctype]
@@ -163,6 +164,9 @@ class _DomainBase:
         if len(spec.r_elem):
             self._ck(self._call("add_receivers", h, len(spec.r_elem), _p(c(spec.r_elem, np.int32), C.c_int32),
                                 _p(c(spec.r_phi, np.float32), C.c_float), _p(c(spec.r_w, np.float32), C.c_float)))
+        if len(spec.oc_pt):
+            self._ck(self._call("add_ocean_load", h, len(spec.oc_pt), _p(c(spec.oc_pt, np.int32), C.c_int32),
+                                _p(c(spec.oc_len, np.int32), C.c_int32), _p(c(spec.oc_vals, np.float32), C.c_float)))
         if len(spec.sf_elem):
             self._ck(self._call("add_surface", h, len(spec.sf_elem), _p(c(spec.sf_elem, np.int32), C.c_int32),
                                 _p(c(spec.sf_side, np.int32), C.c_int32), int(spec.sf_interval)))

@@ -51,6 +51,12 @@ struct PointTable {
     const int32_t *mflen;
     const int64_t *mfofs;
     const float *mf;
+    // ocean load on the solid part (MassOcean1D / MassOcean3D): oclen 0 none, 1 -> four
+    // values (1/(m + m_ocean), 1/m, sin theta, cos theta), nr -> nr x (1/m, scaled normal s,
+    // phi, z); replaces the solid mass
+    const int32_t *oclen;
+    const int64_t *ocofs;
+    const float *oc;
     const int32_t *sflen;  // solid-fluid coupling length (1 or nr), 0 if none
     const int64_t *sfofs;  // row offset into sfn/sfni ([row][3])
     const float *sfn;

@@ -93,6 +93,8 @@ struct ax3d_domain {
     std::vector<int32_t> p_mslen, p_mflen, p_sflen;
     std::vector<int64_t> p_msofs, p_mfofs, p_sfofs;
     std::vector<float> p_ms, p_mf, p_sfn, p_sfni;
+    std::vector<int32_t> oc_pt, oc_len;  // ocean load rows as added
+    std::vector<float> oc_vals;
 
     std::vector<int32_t> e_pts, e_flags, e_nr;
     std::vector<float> e_geo, e_trig;
@@ -112,7 +114,9 @@ struct ax3d_domain {
     DevBuf<int8_t> d_pkind;
     DevBuf<uint8_t> d_paxial, d_pfsurf, d_gskip;
     DevBuf<int64_t> d_sofs, d_fofs, d_msofs, d_mfofs, d_sfofs, d_sg_ref, d_fg_ref;
-    DevBuf<float> d_ms, d_mf, d_sfn, d_sfni;
+    DevBuf<float> d_ms, d_mf, d_sfn, d_sfni, d_oc;
+    DevBuf<int32_t> d_oclen;
+    DevBuf<int64_t> d_ocofs;
     DevBuf<int32_t> d_epts, d_eflags, d_enr;
     DevBuf<float> d_geo, d_trig, d_mod, d_attm, d_mem;
     DevBuf<int64_t> d_mofs, d_aofs, d_memofs, d_efofs;
@@ -411,10 +415,21 @@ struct ax3d_domain {
                 const int b = (int)std::floor(std::log((double)ft.plans[e_nr[e]].Lbuf) / std::log(1.12));
                 (fl ? phys_f : phys_s)[b].push_back(e);
             }
-        // 3D points (Mass3D) and 3D couplings
+        // ocean load per point (GLLPoint.cpp:57-72 picks MassOcean1D / MassOcean3D)
+        std::vector<int32_t> p_oclen(np, 0);
+        std::vector<int64_t> p_ocofs(np, 0);
+        {
+            int64_t o = 0;
+            for (size_t i = 0; i < oc_pt.size(); i++) {
+                p_oclen[oc_pt[i]] = oc_len[i];
+                p_ocofs[oc_pt[i]] = o;
+                o += 4 * (int64_t)oc_len[i];
+            }
+        }
+        // 3D points (Mass3D, MassOcean3D) and 3D couplings
         std::vector<int32_t> pts3d, sf3d;
         for (int p = 0; p < np; p++) {
-            if ((p_mslen[p] > 1) || (p_mflen[p] > 1)) pts3d.push_back(p);
+            if ((p_mslen[p] > 1) || (p_mflen[p] > 1) || (p_oclen[p] > 1)) pts3d.push_back(p);
             if (p_sflen[p] > 1) sf3d.push_back(p);
         }
         // sources
@@ -432,6 +447,9 @@ struct ax3d_domain {
         d_mslen.upload(p_mslen, st);
         d_msofs.upload(p_msofs, st);
         d_ms.upload(p_ms.empty() ? std::vector<float>{0.f} : p_ms, st);
+        d_oclen.upload(p_oclen, st);
+        d_ocofs.upload(p_ocofs, st);
+        d_oc.upload(oc_vals.empty() ? std::vector<float>{0.f} : oc_vals, st);
         d_mflen.upload(p_mflen, st);
         d_mfofs.upload(p_mfofs, st);
         d_mf.upload(p_mf.empty() ? std::vector<float>{0.f} : p_mf, st);
@@ -561,6 +579,9 @@ struct ax3d_domain {
         P.mslen = d_mslen.p;
         P.msofs = d_msofs.p;
         P.ms = d_ms.p;
+        P.oclen = d_oclen.p;
+        P.ocofs = d_ocofs.p;
+        P.oc = d_oc.p;
         P.mflen = d_mflen.p;
         P.mfofs = d_mfofs.p;
         P.mf = d_mf.p;
@@ -983,6 +1004,31 @@ int ax3d_add_surface(ax3d_domain *d, int32_t n, const int32_t *elem, const int32
         d->sf_interval = interval;
         d->sf_elem.insert(d->sf_elem.end(), elem, elem + n);
         d->sf_side.insert(d->sf_side.end(), side, side + n);
+    });
+}
+
+int ax3d_add_ocean_load(ax3d_domain *d, int32_t n, const int32_t *point, const int32_t *len, const float *vals) {
+    return guard([&] {
+        if (!d || n < 0 || (n && (!point || !len || !vals)))
+            throw Error(AX3D_ERR_ARG, "ax3d_add_ocean_load || bad argument");
+        if (d->finalized) throw Error(AX3D_ERR_STATE, "ax3d_add_ocean_load || domain already finalized");
+        std::vector<char> seen(d->p_nr.size(), 0);
+        for (int32_t p : d->oc_pt) seen[p] = 1;
+        int64_t o = 0;
+        for (int i = 0; i < n; i++) {
+            const int p = point[i];
+            if (p < 0 || p >= (int)d->p_nr.size()) throw Error(AX3D_ERR_ARG, "ax3d_add_ocean_load || point out of range");
+            if (d->p_kind[p] == AX3D_POINT_FLUID)
+                throw Error(AX3D_ERR_ARG, "MassOcean3D::checkCompatibility || Fluid point with ocean load.");
+            if (!(len[i] == 1 || len[i] == d->p_nr[p]))
+                throw Error(AX3D_ERR_ARG, "MassOcean3D::checkCompatibility || Incompatible size.");
+            if (seen[p]) throw Error(AX3D_ERR_ARG, "ax3d_add_ocean_load || point already has an ocean load");
+            seen[p] = 1;
+            o += 4 * (int64_t)len[i];
+        }
+        d->oc_pt.insert(d->oc_pt.end(), point, point + n);
+        d->oc_len.insert(d->oc_len.end(), len, len + n);
+        d->oc_vals.insert(d->oc_vals.end(), vals, vals + o);
     });
 }
 

@@ -115,23 +115,41 @@ __device__ __forceinline__ void newmark_entry(float2 &u, float2 &v, float2 &a, f
     }
 }
 
-// Row-local Newmark (points with a Mass1D), SolidPoint::updateNewmark.
+// MassOcean1D::computeAccel (MassOcean1D.cpp:17-32) on one order: the radial component
+// (s sin + z cos) takes 1/(m + m_ocean), the tangential ones 1/m.
+__device__ __forceinline__ void ocean_accel_row(float2 (&s)[3], const float *__restrict__ o) {
+    const float imz = o[0], imr = o[1], st = o[2], ct = o[3];
+    float2 z = cadd(cscale(st, s[0]), cscale(ct, s[2]));
+    float2 r = csub(cscale(ct, s[0]), cscale(st, s[2]));
+    z = cscale(imz, z);
+    r = cscale(imr, r);
+    s[0] = cadd(cscale(st, z), cscale(ct, r));
+    s[2] = csub(cscale(ct, z), cscale(st, r));
+    s[1] = cscale(imr, s[1]);
+}
+
+// Row-local Newmark (points with a Mass1D or MassOcean1D), SolidPoint::updateNewmark.
 __global__ void k_newmark_solid_rows(PointTable P, Fields F, float dt, float hd, float hdd, int kahan) {
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < P.nsrows;
          r += (int64_t)gridDim.x * blockDim.x) {
         const int pt = P.srow_pt[r];
-        if (P.mslen[pt] != 1) continue;  // Mass3D point: CTA kernel
+        const int ocl = P.oclen[pt];
+        if (ocl > 1 || (ocl == 0 && P.mslen[pt] != 1)) continue;  // Mass3D / MassOcean3D: CTA kernel
         const int a = (int)(r - P.sofs[pt] / 3);
         const int nr = P.nr[pt], nu = nr / 2;
         const bool even = nr % 2 == 0, axial = P.axial[pt];
-        const float im = P.ms[P.msofs[pt]];
         float2 s[3];
         const int64_t o = r * 3;
 #pragma unroll
         for (int c = 0; c < 3; c++) s[c] = F.ss[o + c];
         mask_solid_row(s, a, nu, even, axial);
+        if (ocl == 1) {
+            ocean_accel_row(s, P.oc + P.ocofs[pt]);
+        } else {
+            const float im = P.ms[P.msofs[pt]];
 #pragma unroll
-        for (int c = 0; c < 3; c++) s[c] = cscale(im, s[c]);  // Mass1D::computeAccel
+            for (int c = 0; c < 3; c++) s[c] = cscale(im, s[c]);  // Mass1D::computeAccel
+        }
         mask_solid_row(s, a, nu, even, axial);
 #pragma unroll
         for (int c = 0; c < 3; c++) {
@@ -225,7 +243,8 @@ __device__ void blk_r2c(const float *x, int ncol, int nr, float2 *Y, int stride)
     }
 }
 
-// Mass3D::computeAccel + Newmark for one point per CTA (solid and/or fluid part).
+// Mass3D::computeAccel (or MassOcean3D::computeAccel, MassOcean3D.cpp:24-55, on the solid
+// part) + Newmark for one point per CTA (solid and/or fluid part).
 __global__ void __launch_bounds__(PT3_THREADS)
     k_newmark_3d(PointTable P, Fields F, const int32_t *__restrict__ pts, int n, float dt, float hd,
                  float hdd, int kahan) {
@@ -239,8 +258,9 @@ __global__ void __launch_bounds__(PT3_THREADS)
         const int ncomp = phase == 0 ? 3 : 1;
         int64_t ofs;
         const float *im;
+        const int ocl = P.oclen[pt];
         if (phase == 0) {
-            if (P.kind[pt] == 1 || P.mslen[pt] == 1) continue;
+            if (P.kind[pt] == 1 || !(ocl > 1 || (ocl == 0 && P.mslen[pt] > 1))) continue;
             ofs = P.sofs[pt];
             im = P.ms + P.msofs[pt];
         } else {
@@ -275,7 +295,20 @@ __global__ void __launch_bounds__(PT3_THREADS)
         __syncthreads();
         blk_c2r(S, 3, ncomp, nr, x);
         __syncthreads();
-        for (int t = threadIdx.x; t < ncomp * nr; t += blockDim.x) x[t] *= im[t % nr];
+        if (phase == 0 && ocl > 1) {
+            // a = f / m - (f . n') n', n' = unit normal * sqrt(m_ocean / (m (m + m_ocean)))
+            const float *o = P.oc + P.ocofs[pt];
+            for (int k = threadIdx.x; k < nr; k += blockDim.x) {
+                const float m = o[4 * k], n0 = o[4 * k + 1], n1 = o[4 * k + 2], n2 = o[4 * k + 3];
+                const float f0 = x[k], f1 = x[nr + k], f2 = x[2 * nr + k];
+                const float fn = f0 * n0 + f1 * n1 + f2 * n2;
+                x[k] = f0 * m - fn * n0;
+                x[nr + k] = f1 * m - fn * n1;
+                x[2 * nr + k] = f2 * m - fn * n2;
+            }
+        } else {
+            for (int t = threadIdx.x; t < ncomp * nr; t += blockDim.x) x[t] *= im[t % nr];
+        }
         __syncthreads();
         blk_r2c(x, ncomp, nr, S, 3);
         __syncthreads();

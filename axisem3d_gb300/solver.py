@@ -296,13 +296,15 @@ class Simulation:
         sfn = np.zeros((P, 3))
         sfside = ex.side.get("solid_fluid_boundary", np.full(E, -1))
         wg, wjw = S.gll()[1], S.glj()[1]
-        for e in np.nonzero(sfside >= 0)[0]:
-            side = sfside[e]
+        def side_normal(e, side):
+            """Quad::computeNormal (Quad.cpp:661-715) without relabelling, for the five
+            points (local index, normal) of one side."""
             n0, n1 = nodes[e][:, side], nodes[e][:, (side + 1) % 4]
-            r0, t0 = np.hypot(*n0), math.acos(n0[1] / np.hypot(*n0))
-            r1, t1 = np.hypot(*n1), math.acos(n1[1] / np.hypot(*n1))
+            r0, t0 = np.hypot(*n0), _colat(*n0)
+            r1, t1 = np.hypot(*n1), _colat(*n1)
             rsf = 0.5 * (r0 + r1)
             h_r_dt, h_r2_dt = 0.5 * rsf * abs(t1 - t0), 0.5 * rsf * rsf * abs(t1 - t0)
+            out = []
             for ip in range(5):
                 for jp in range(5):
                     on = (side == 0 and jp == 0) or (side == 1 and ip == 4) or (side == 2 and jp == 4) or \
@@ -313,7 +315,7 @@ class Simulation:
                     sz = crds[e, k]
                     rr = np.hypot(*sz)
                     sint, cost = sz[0] / rr, sz[1] / rr
-                    nvec = np.array([sint, 0.0, cost])  # Quad::computeNormal (Quad.cpp:661-715)
+                    nvec = np.array([sint, 0.0, cost])
                     wsf = (wjw if axial_e[e] else wg)[ip] if side in (0, 2) else wg[jp]
                     if axial_e[e]:
                         if ip == 0:
@@ -325,9 +327,12 @@ class Simulation:
                         nvec *= wsf * sint * h_r2_dt
                     if side != co[e]:
                         nvec = -nvec
-                    if not fl[e]:
-                        nvec = -nvec
-                    sfn[e_pts[e, k]] += 0.5 * nvec  # GLLPoint::addSFNormal
+                    out.append((k, nvec))
+            return out
+
+        for e in np.nonzero(sfside >= 0)[0]:
+            for k, nvec in side_normal(e, sfside[e]):
+                sfn[e_pts[e, k]] += 0.5 * (nvec if fl[e] else -nvec)  # GLLPoint::addSFNormal
         # moduli (Material::createElastic / createAcoustic, isotropic)
         att_on = par.get("ATTENUATION", bool)
         cg4 = par.get("ATTENUATION_CG4", bool)
@@ -404,6 +409,7 @@ class Simulation:
                 vals[ofs[p]:ofs[p] + lens[p]] = 1.0 / v
             return lens.astype(np.int32), vals.astype(np.float32)
         p_mslen, p_ms = pack_mass(has_s, ms, ms3)
+        oc_pt, oc_len, oc_vals = self._ocean_load(ex, fl, e_pts, crds, side_normal, ms, ms3, p_nr)
         p_mflen, p_mf = pack_mass(has_f, mf, mf3)
         # coupling rows (SolidFluidCoupling1D / 3D when the fluid mass varies with phi)
         sflen = np.where(kind == POINT_SOLID_FLUID, 1, 0).astype(np.int32)
@@ -431,7 +437,8 @@ class Simulation:
             e_mofs=mofs, e_mod=np.concatenate(e_mod).astype(np.float32), e_att=np.array(e_att, np.int8),
             e_aofs=aofs, e_attm=(np.concatenate(e_attm) if e_attm else np.zeros(0)).astype(np.float32),
             nsls=nsls, att_alpha=alpha, att_beta=beta, att_gamma=gamma, att_do_kappa=dokappa,
-            kahan=kahan, stability_interval=par.get("OPTION_STABILITY_INTERVAL", int))
+            kahan=kahan, stability_interval=par.get("OPTION_STABILITY_INTERVAL", int),
+            oc_pt=oc_pt, oc_len=oc_len, oc_vals=oc_vals)
         self.e_pts, self.crds, self.jac, self.fluid = e_pts, crds, jac, fl
         self._source(spec)
         self._stf(spec)
@@ -441,6 +448,40 @@ class Simulation:
         return spec
 
     # ------------------------------------------------------------------ source
+    def _ocean_load(self, ex, fl, e_pts, crds, side_normal, ms, ms3, p_nr):
+        """MODEL_3D_OCEAN_LOAD (OceanLoad3D::buildInparam, OceanLoad3D.cpp:20-52): 'none' or
+        'constant$<depth km>' (OceanLoad3D_const, 3 km by default).  Solid elements on the
+        surface side set give their outer points the summed side normal and the ocean depth
+        (Quad::setOceanLoad3D, Quad.cpp:254-282, and Quad.cpp:367-373); GLLPoint::release
+        (GLLPoint.cpp:57-72) turns each into MassOcean1D or MassOcean3D rows."""
+        from .synth import ocean_rows
+        name, *params = self.par.get("MODEL_3D_OCEAN_LOAD").split("$")
+        self.ocean_depth = 0.0
+        none = (np.zeros(0, np.int32), np.zeros(0, np.int32), np.zeros(0, np.float32))
+        if name.lower() == "none":
+            return none
+        if name.lower() == "crust1":
+            raise ValueError("OceanLoad3D_crust1::initialize || the crust1.0 tables are not part of this "
+                             "package; use constant$<depth km>.")
+        if name.lower() != "constant":
+            raise ValueError(f"OceanLoad3D::buildInparam || Unknown ocean-load model name {name}.")
+        depth = float(params[0]) * 1e3 if params else 3000.0
+        self.ocean_depth = depth
+        surf = ex.side.get("r1", np.full(len(fl), -1))
+        normal = {}
+        for e in np.nonzero((surf >= 0) & ~fl)[0]:
+            for k, nvec in side_normal(e, surf[e]):
+                p = int(e_pts[e, k])
+                normal[p] = normal.get(p, 0.0) + nvec  # GLLPoint::addSurfNormal
+        pts = sorted(normal)
+        if depth == 0.0 or not pts:
+            return none
+        _, first = np.unique(e_pts.ravel(), return_index=True)  # one element slot per point
+        coords = crds.reshape(-1, 2)[first[np.array(pts)]]
+        mass = [ms[p] + ms3.get(p, 0.0) for p in pts]
+        return ocean_rows(pts, [normal[p] for p in pts], mass, p_nr,
+                          [_colat(*c) for c in coords], [depth] * len(pts))
+
     def _cmt_latlon(self):
         """Source latitude/longitude of the CMTSOLUTION (Source.cpp:121-140), needed before
         the source itself is built to place geographic 3-D anomalies."""
@@ -714,7 +755,7 @@ class Simulation:
 
 def write_inputs(input_dir, mesh_kw=None, nu=2, stf="gauss", hdur=50.0, steps=2000, record_length=None,
                  n_stations=20, depth_km=100.0, seed=0, attenuation=False, system="source_centered",
-                 models3d=(), lucky=False, whole_surface="false"):
+                 models3d=(), lucky=False, whole_surface="false", ocean="none"):
     """Seeded inputs of the small benchmark configuration: mesh, four parfiles, CMTSOLUTION
     (moment tensor ~ N(0, 1e20 N*m) written in dyn*cm) and STATIONS at uniform distance."""
     from . import mesher
@@ -726,7 +767,7 @@ def write_inputs(input_dir, mesh_kw=None, nu=2, stf="gauss", hdur=50.0, steps=20
     vol = f"MODEL_3D_VOLUMETRIC_NUM {len(models3d)}\n" + \
         (f"MODEL_3D_VOLUMETRIC_LIST {' '.join(models3d)}\n" if models3d else "")
     (d / "inparam.model").write_text(f"MODEL_1D_EXODUS_MESH_FILE mesh.e\n{vol}"
-                                     f"MODEL_3D_GEOMETRIC_NUM 0\nMODEL_3D_OCEAN_LOAD none\nMODEL_2D_MODE off\n"
+                                     f"MODEL_3D_GEOMETRIC_NUM 0\nMODEL_3D_OCEAN_LOAD {ocean}\nMODEL_2D_MODE off\n"
                                      f"MODEL_PLOT_SLICES_NUM 0\nATTENUATION {'true' if attenuation else 'false'}\n")
     (d / "inparam.nu").write_text(f"NU_TYPE constant\nNU_CONST {nu}\nNU_WISDOM_LEARN false\n")
     (d / "inparam.time_src_recv").write_text(

@@ -63,6 +63,11 @@ class DomainSpec:
     sf_elem: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
     sf_side: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
     sf_interval: int = 1
+    # ocean load (MassOcean1D / MassOcean3D) on solid points: len 1 -> (1/(m + m_ocean), 1/m,
+    # sin theta, cos theta), len nr -> nr x (1/m, scaled unit normal s, phi, z)
+    oc_pt: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    oc_len: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    oc_vals: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
     kahan: bool = False
     stability_interval: int = 0
 

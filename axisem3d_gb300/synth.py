@@ -130,13 +130,15 @@ def annulus_domain(seed=0, n_theta=4, n_r=3, r_in=3000e3, r_out=6371e3, theta_ma
                    nu_random=False, nu_max=None, fluid_layers=(), mat=MAT_ISO, in3d=False,
                    att=ATT_NONE, nsls=3, mass3d=False, couple3d=False, dt=0.05, source=True,
                    n_receivers=3, stf_len=64, stability_interval=0, kahan=False, fluid3d=False,
-                   perturb=0.04, lucky=False, surface_interval=0):
+                   perturb=0.04, lucky=False, surface_interval=0, ocean=""):
     """Connected spherical-element mesh on an (r, theta) grid.
 
     Element (ir, it) spans radii [rs[ir], rs[ir+1]] and colatitudes [ts[it], ts[it+1]];
     elements with it = 0 touch the axis.  fluid_layers lists the ir that are fluid.
     surface_interval > 0 records the outer surface (side 2, eta = +1, of every solid
-    element of the top layer) every surface_interval steps."""
+    element of the top layer) every surface_interval steps.  ocean = "1d" puts a 3 km
+    ocean on the outer surface points (MassOcean1D); "3d" varies its depth with azimuth
+    and tilts the surface normal (MassOcean3D)."""
     rng = np.random.default_rng(seed)
     rs = np.linspace(r_in, r_out, n_r + 1)
     ts = np.linspace(0.0, theta_max, n_theta + 1)
@@ -191,6 +193,7 @@ def annulus_domain(seed=0, n_theta=4, n_r=3, r_in=3000e3, r_out=6371e3, theta_ma
     ms_acc = [None] * npt
     mf_acc = [None] * npt
     sfn_acc = [None] * npt
+    surf_acc = [None] * npt  # summed outer-surface normals (GLLPoint::addSurfNormal)
     crds_pt = np.zeros((npt, 2))
     for ir in range(n_r):
         for it in range(n_theta):
@@ -256,23 +259,19 @@ def annulus_domain(seed=0, n_theta=4, n_r=3, r_in=3000e3, r_out=6371e3, theta_ma
                     sz = crds[k]
                     sint = sz[0] / np.hypot(*sz)
                     cost = sz[1] / np.hypot(*sz)
-                    nvec = np.array([sint, 0.0, cost])
-                    from .spectral import weights, xi_eta
-                    wsf = weights(ip, jp, axial)[0]
-                    if axial:
-                        if ip == 0:
-                            J = GEO.jacobian(nodes, xi_eta(ip, jp, axial))
-                            nvec = nvec * wsf * J[0, 0] * h_r_dt
-                        else:
-                            nvec = nvec * wsf / (1 + xi_eta(ip, jp, axial)[0]) * sint * h_r2_dt
-                    else:
-                        nvec = nvec * wsf * sint * h_r2_dt
+                    nvec = _side_normal(nodes, crds, ip, jp, axial, h_r_dt, h_r2_dt)
                     if side != 2:
                         nvec = -nvec
                     if not fluid_elem[ir, it]:
                         nvec = -nvec
                     p = gid(ir, it, ip, jp)
                     sfn_acc[p] = nvec * 0.5 if sfn_acc[p] is None else sfn_acc[p] + nvec * 0.5
+            if ocean and ir == n_r - 1 and not fluid_elem[ir, it]:  # outer side 2 (Quad.cpp:367-373)
+                h_r_dt, h_r2_dt = 0.5 * r1 * abs(t1 - t0), 0.5 * r1 * r1 * abs(t1 - t0)
+                for ip in range(5):
+                    p = gid(ir, it, ip, 4)
+                    nvec = _side_normal(nodes, crds, ip, 4, axial, h_r_dt, h_r2_dt)
+                    surf_acc[p] = nvec if surf_acc[p] is None else surf_acc[p] + nvec
     # points
     mslen, ms, mflen, mf, sflen, sfn, sfni = [], [], [], [], [], [], []
     for p in range(npt):
@@ -341,12 +340,83 @@ def annulus_domain(seed=0, n_theta=4, n_r=3, r_in=3000e3, r_out=6371e3, theta_ma
         nsls=nsls if att != ATT_NONE else 0, att_alpha=alpha, att_beta=beta, att_gamma=gamma,
         att_do_kappa=True, sources=sources, stf=stf, r_elem=r_elem, r_phi=r_phi, r_w=r_w,
         kahan=kahan, stability_interval=stability_interval, **ea)
+    if ocean:
+        spec.oc_pt, spec.oc_len, spec.oc_vals = _ocean_rows(ocean, surf_acc, ms_acc, nr_pt, crds_pt, rng)
     if surface_interval > 0:
         top = n_r - 1
         spec.sf_elem = np.array([top * n_theta + it for it in range(n_theta) if not fluid_elem[top, it]], np.int32)
         spec.sf_side = np.full(len(spec.sf_elem), 2, np.int32)
         spec.sf_interval = int(surface_interval)
     return spec
+
+
+def _side_normal(nodes, crds, ip, jp, axial, h_r_dt, h_r2_dt):
+    """Quad::computeNormal (Quad.cpp:661-715) without relabelling, before the sign flip:
+    (sin theta, 0, cos theta) times the side's quadrature area."""
+    from .spectral import weights, xi_eta
+    sz = crds[ip * 5 + jp]
+    sint, cost = sz[0] / np.hypot(*sz), sz[1] / np.hypot(*sz)
+    nvec = np.array([sint, 0.0, cost])
+    wsf = weights(ip, jp, axial)[0]
+    if axial:
+        if ip == 0:
+            J = GEO.jacobian(nodes, xi_eta(ip, jp, axial))
+            return nvec * wsf * J[0, 0] * h_r_dt
+        return nvec * wsf / (1 + xi_eta(ip, jp, axial)[0]) * sint * h_r2_dt
+    return nvec * wsf * sint * h_r2_dt
+
+
+WATER_DENSITY = 1027.0  # OceanLoad3D::mWaterDensity
+
+
+def ocean_rows(points, normal, mass, nr, colat, depth):
+    """Ocean-load rows of GLLPoint::release (GLLPoint.cpp:57-72) for solid points.
+
+    normal[i]: summed surface normal, [3] or [nr][3]; mass[i]: solid mass, [1] or [nr];
+    depth[i]: ocean depth (m), scalar or [nr]; colat[i]: colatitude of the point.  Rows
+    whose mass, depth and normal do not vary with azimuth become MassOcean1D (four values),
+    the others MassOcean3D (nr x four values)."""
+    lens, vals = [], []
+    for i, p in enumerate(points):
+        n = np.atleast_2d(np.asarray(normal[i], np.float64))
+        m = np.atleast_1d(np.asarray(mass[i], np.float64))
+        d = np.atleast_1d(np.asarray(depth[i], np.float64))
+        flat = all(len(x) == 1 or np.ptp(x, 0).max() == 0 for x in (m, d, n))
+        if flat:
+            area = np.linalg.norm(n[0])
+            mo = WATER_DENSITY * d[0] * area
+            lens.append(1)
+            vals.append([1.0 / (m[0] + mo), 1.0 / m[0], np.sin(colat[i]), np.cos(colat[i])])
+        else:
+            k = int(nr[p])
+            n = np.broadcast_to(n, (k, 3))
+            m = np.broadcast_to(m, (k,))
+            d = np.broadcast_to(d, (k,))
+            area = np.linalg.norm(n, axis=1)
+            mo = WATER_DENSITY * d * area
+            scal = np.sqrt(mo / (m * (m + mo)))
+            lens.append(k)
+            vals.append(np.column_stack([1.0 / m, n / area[:, None] * scal[:, None]]).ravel())
+    return (np.asarray(points, np.int32), np.asarray(lens, np.int32),
+            np.concatenate([np.ravel(v) for v in vals]).astype(np.float32) if vals else np.zeros(0, np.float32))
+
+
+def _ocean_rows(kind, surf_acc, ms_acc, nr_pt, crds_pt, rng):
+    pts = [p for p in range(len(surf_acc)) if surf_acc[p] is not None]
+    normal, mass, depth, colat = [], [], [], []
+    for p in pts:
+        colat.append(np.arctan2(crds_pt[p][0], crds_pt[p][1]))
+        mass.append(ms_acc[p])
+        if kind == "3d":
+            ang = 2 * np.pi * np.arange(nr_pt[p]) / nr_pt[p]
+            nn = np.outer(1 + 0.05 * np.cos(ang), surf_acc[p])
+            nn[:, 1] = 0.1 * np.sin(ang + rng.uniform(0, 2 * np.pi)) * np.linalg.norm(surf_acc[p])
+            normal.append(nn)
+            depth.append(3000.0 * (1 + 0.5 * np.cos(ang + rng.uniform(0, 2 * np.pi))))
+        else:
+            normal.append(surf_acc[p])
+            depth.append(3000.0)
+    return ocean_rows(pts, normal, mass, nr_pt, colat, depth)
 
 
 def random_fields(spec: DomainSpec, seed=1, scale=1e-3, decay=1.5):

@@ -146,6 +146,15 @@ int ax3d_add_receivers(ax3d_domain *d, int32_t n, const int32_t *elem, const flo
    (SolidElement::feedDispOnSide, SolidElement.cpp:354-390).  Before ax3d_finalize. */
 int ax3d_add_surface(ax3d_domain *d, int32_t n, const int32_t *elem, const int32_t *side, int32_t interval);
 
+/* Ocean load on the solid part of n points (GLLPoint::release, GLLPoint.cpp:57-72), replacing
+   the mass given to ax3d_add_points.  len[i] = 1: MassOcean1D (MassOcean1D.cpp), four values
+   1/(m + m_ocean), 1/m, sin theta, cos theta (theta = colatitude of the point); len[i] = nr:
+   MassOcean3D (MassOcean3D.cpp), nr rows of four values 1/m, and the unit surface normal
+   (s, phi, z) scaled by sqrt(m_ocean / (m (m + m_ocean))).  Values back to back.  Fluid
+   points and other lengths are rejected with the reference's messages.  Before
+   ax3d_finalize. */
+int ax3d_add_ocean_load(ax3d_domain *d, int32_t n, const int32_t *point, const int32_t *len, const float *vals);
+
 /* Ends set-up (Mesh::release + Domain::initializeRecorders): checks sizes, builds the
    gather lists and element buckets, uploads everything. */
 int ax3d_finalize(ax3d_domain *d);

@@ -56,6 +56,8 @@ struct Oracle {
         int64_t fofs = -1;  // complex offset into fluid fields ([alpha])
         std::vector<Real> ims, imf;     // inverse mass, size 1 or nr
         std::vector<Real> sfn, sfni;    // [len][3]
+        int oclen = 0;                  // ocean load: 0 none, 1 MassOcean1D, nr MassOcean3D
+        std::vector<Real> oc;           // [oclen][4]
     };
     std::vector<Point> pts;
     std::vector<C> su, sv, sa, ss;   // solid displ, veloc, accel, stiff
@@ -152,6 +154,20 @@ struct Oracle {
             }
             osf += lsf;
             pts.push_back(p);
+        }
+    }
+
+    // GLLPoint::release (GLLPoint.cpp:57-72): MassOcean1D / MassOcean3D replace the solid mass
+    void add_ocean_load(int n, const int32_t *point, const int32_t *len, const float *vals) {
+        int64_t o = 0;
+        for (int i = 0; i < n; i++) {
+            Point &p = pts.at(point[i]);
+            if (p.kind == 1) throw std::runtime_error("MassOcean3D::checkCompatibility || Fluid point with ocean load.");
+            if (!(len[i] == 1 || len[i] == p.nr))
+                throw std::runtime_error("MassOcean3D::checkCompatibility || Incompatible size.");
+            p.oclen = len[i];
+            p.oc.assign(vals + o, vals + o + 4 * len[i]);
+            o += 4 * len[i];
         }
     }
 
@@ -782,6 +798,34 @@ struct Oracle {
             r2c(x.data(), p.nr, f + c, ncomp);
         }
     }
+    // MassOcean1D::computeAccel (MassOcean1D.cpp:17-32): radial (s sin + z cos) over
+    // m + m_ocean, tangential over m; MassOcean3D::computeAccel (MassOcean3D.cpp:24-55):
+    // per sample a = f / m - (f . n') n'.
+    void ocean_accel(const Point &p, C *f) const {
+        if (p.oclen == 1) {
+            const Real imz = p.oc[0], imr = p.oc[1], st = p.oc[2], ct = p.oc[3];
+            for (int a = 0; a <= p.nu; a++) {
+                C *r = f + 3 * a;
+                C z = r[0] * st + r[2] * ct;
+                C t = r[0] * ct - r[2] * st;
+                z *= imz;
+                t *= imr;
+                r[0] = z * st + t * ct;
+                r[2] = z * ct - t * st;
+                r[1] *= imr;
+            }
+            return;
+        }
+        const int nr = p.nr;
+        std::vector<Real> x(3 * nr), y(3 * nr);
+        for (int c = 0; c < 3; c++) c2r(f + c, nr, x.data() + c * nr, 3);
+        for (int k = 0; k < nr; k++) {
+            const Real *o = p.oc.data() + 4 * k;
+            const Real fn = x[k] * o[1] + x[nr + k] * o[2] + x[2 * nr + k] * o[3];
+            for (int c = 0; c < 3; c++) y[c * nr + k] = x[c * nr + k] * o[0] - fn * o[1 + c];
+        }
+        for (int c = 0; c < 3; c++) r2c(y.data() + c * nr, nr, f + c, 3);
+    }
     // Newmark with optional compensated sums: out += d.
     static void kadd(C &out, C &comp, C d) {
         C y = d - comp;
@@ -799,7 +843,8 @@ struct Oracle {
             return;
         }
         if (fluid) mask_fluid(p, s); else mask_solid(p, s);
-        mass_accel(im, p, s, ncomp);
+        if (!fluid && p.oclen) ocean_accel(p, s);
+        else mass_accel(im, p, s, ncomp);
         if (fluid) mask_fluid(p, s); else mask_solid(p, s);
         double half_dt = 0.5 * dt;
         double half_dt_dt = half_dt * dt;

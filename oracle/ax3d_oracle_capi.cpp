@@ -87,6 +87,13 @@ int guard(F f) {
         }                                                                                        \
         return 0;                                                                                \
     }                                                                                            \
+    int P##add_ocean_load(void *dv, int32_t n, const int32_t *point, const int32_t *len,         \
+                          const float *vals) {                                                   \
+        return guard([&] {                                                                       \
+            static_cast<P##dom *>(dv)->add_ocean_load(n, point, len, vals);                      \
+            return 0;                                                                            \
+        });                                                                                      \
+    }                                                                                            \
     int P##add_surface(void *dv, int32_t n, const int32_t *elem, const int32_t *side,            \
                        int32_t interval) {                                                       \
         auto *d = static_cast<P##dom *>(dv);                                                     \

@@ -173,3 +173,65 @@ def test_oracle_surface_record_is_side_displacement():
                 want[:nu + 1] = su[so[pt] + 3 * np.arange(nu + 1) + c]
                 np.testing.assert_allclose(rec[k][0, c, q], want, rtol=1e-6, atol=1e-12)
     np.testing.assert_allclose(rec[0][0], rec[0][1])  # the field did not change between the records
+
+
+@pytest.mark.parametrize("ocean", ["1d", "3d"])
+def test_oracle_ocean_load_accel(ocean):
+    """MassOcean1D / MassOcean3D: the oracle's acceleration on ocean points equals a numpy
+    restatement (radial over m + m_ocean, tangential over m; per sample f/m - (f.n')n')."""
+    from oracle.oracle_py import OracleDomain
+    spec = synth.annulus_domain(seed=4, n_theta=3, n_r=2, nu=3, nu_random=True, nu_max=6, source=False,
+                                n_receivers=0, ocean=ocean)
+    assert (spec.oc_len > 1).any() == (ocean == "3d")
+    o = OracleDomain(spec, double=True)
+    so, _ = spec.point_offsets()
+    rng = np.random.default_rng(5)
+    f = np.zeros(o.nsolid, complex)
+    for p in range(spec.n_points):
+        if so[p] < 0:
+            continue
+        nr = spec.p_nr[p]
+        blk = rng.normal(size=(nr // 2 + 1, 3)) + 1j * rng.normal(size=(nr // 2 + 1, 3))
+        blk[0] = blk[0].real
+        if nr % 2 == 0:
+            blk[-1] = 0
+        f[so[p]:so[p] + blk.size] = blk.ravel()
+    o.set("stiff", "solid", f)
+    o.update_newmark()
+    acc = o.get("accel", "solid")
+    ofs = 0
+    for p, ln in zip(spec.oc_pt, spec.oc_len):
+        v = spec.oc_vals[ofs:ofs + 4 * ln].astype(np.float64).reshape(ln, 4)
+        ofs += 4 * ln
+        if spec.p_axial[p]:
+            continue
+        nr = spec.p_nr[p]
+        na = nr // 2 + 1
+        F = f[so[p]:so[p] + 3 * na].reshape(na, 3)
+        if ln == 1:
+            imz, imr, st, ct = v[0]
+            z = (F[:, 0] * st + F[:, 2] * ct) * imz
+            r = (F[:, 0] * ct - F[:, 2] * st) * imr
+            want = np.stack([z * st + r * ct, F[:, 1] * imr, z * ct - r * st], 1)
+        else:
+            x = np.stack([np.real(np.fft.ifft(_herm(F[:, c], nr)) * nr) for c in range(3)], 1)
+            fn = (x * v[:, 1:]).sum(1)
+            y = x * v[:, :1] - fn[:, None] * v[:, 1:]
+            want = np.fft.rfft(y, axis=0)[:na] / nr
+            want[0] = want[0].real
+            if nr % 2 == 0:
+                want[-1] = 0
+        got = acc[so[p]:so[p] + 3 * na].reshape(na, 3)
+        np.testing.assert_allclose(got, want, rtol=1e-9, atol=1e-12 * np.abs(want).max())
+
+
+def _herm(X, nr):
+    """Full spectrum of a real length-nr signal from orders 0..nr/2 (Hermitian)."""
+    full = np.zeros(nr, complex)
+    na = len(X)
+    full[:na] = X
+    for a in range(1, na):
+        if nr - a != a:
+            full[nr - a] = np.conj(X[a])
+    full[0] = X[0].real
+    return full

@@ -38,6 +38,9 @@ CASES = {
     "ti3d_cg4_bluestein509": dict(in3d=True, mat=MAT_TISO, att=ATT_CG4, nu=254, n_theta=2, n_r=2),
     "fluid3d_bluestein257": dict(fluid_layers=(1,), in3d=True, fluid3d=True, nu=128, mat=MAT_TISO, n_theta=2,
                                  n_r=2),
+    # ocean load on the outer surface points (MassOcean1D, MassOcean3D)
+    "iso1d_ocean1d_mixednu": dict(ocean="1d", nu_random=True, nu_max=6),
+    "ti3d_ocean3d_mass3d": dict(in3d=True, mat=MAT_TISO, mass3d=True, ocean="3d", nu_random=True, nu_max=7),
 }
 # time-loop steps for the cases whose O(nr^2) FP64 oracle transform is slow
 STEPS = {"ti3d_fft260_chunked": 6, "ti3d_cg4_direct131": 10, "iso3d_full_direct391": 4,
@@ -201,3 +204,23 @@ def test_surface_recorder_matches_oracle(ax3d_lib):
         d.step(13)
     for a, b in zip(g.surface(0, 5), o.surface(0, 5)):
         assert rel(a, b) <= TOL
+
+
+@pytest.mark.parametrize("ocean", ["1d", "3d"])
+def test_ocean_load_newmark_matches_oracle(ax3d_lib, ocean):
+    """One Newmark update from a random stiffness: ocean points take MassOcean1D (row-local)
+    or MassOcean3D (per-sample normal projection) on the GPU as in the oracle."""
+    from oracle.oracle_py import OracleDomain
+    from axisem3d_gb300.capi import Ax3dDomain
+    spec = synth.annulus_domain(seed=6, n_theta=3, n_r=2, nu_random=True, nu_max=9, source=False,
+                                n_receivers=0, ocean=ocean)
+    g, o = Ax3dDomain(spec), OracleDomain(spec)
+    su, _ = synth.random_fields(spec, seed=8)
+    for d in (g, o):
+        d.set("stiff", "solid", su)
+        d.update_newmark()
+    a, b = g.get("accel", "solid"), o.get("accel", "solid")
+    assert rel(a, b) <= TOL, rel(a, b)
+    so, _ = spec.point_offsets()
+    rows = np.concatenate([np.arange(so[p], so[p] + 3 * (spec.p_nr[p] // 2 + 1)) for p in spec.oc_pt])
+    assert rel(a[rows], b[rows]) <= TOL

@@ -267,3 +267,32 @@ def test_whole_surface_edges_and_netcdf(tmp_path_factory):
         np.testing.assert_allclose(ds[f"edge_{tag}r"], recs[tag].real.reshape(30, w).astype(np.float32))
         np.testing.assert_allclose(ds[f"edge_{tag}i"], recs[tag].imag.reshape(30, w).astype(np.float32))
     assert float(ds.attrs["radius"][0]) == sim.R
+
+
+def test_ocean_load_constant(tmp_path_factory):
+    """MODEL_3D_OCEAN_LOAD constant$4.0: every solid surface point gets a MassOcean1D row
+    (1-D model), the ocean adds mass to the radial direction only, and the oracle's
+    seismograms change; unknown names raise."""
+    from oracle.oracle_py import OracleDomain
+    d = tmp_path_factory.mktemp("oc") / "input"
+    solver.write_inputs(d, mesh_kw=SMALL_MESH, steps=60, hdur=20.0, n_stations=3, seed=4, ocean="constant$4.0")
+    sim = solver.Simulation(d)
+    spec = sim.build()
+    surf = set()
+    for e in np.nonzero((sim.ex.side["r1"] >= 0) & ~sim.fluid)[0]:
+        c = sim.crds[e].reshape(25, 2)
+        surf |= {int(sim.e_pts[e, k]) for k in range(25) if abs(np.hypot(*c[k]) - sim.R) < 1.0}
+    assert set(spec.oc_pt.tolist()) == surf and (spec.oc_len == 1).all()
+    v = spec.oc_vals.reshape(-1, 4).astype(np.float64)
+    assert (v[:, 0] < v[:, 1]).all()                        # 1/(m + m_ocean) < 1/m
+    np.testing.assert_allclose(v[:, 2] ** 2 + v[:, 3] ** 2, 1.0, rtol=1e-6)
+    o1 = OracleDomain(spec)
+    o1.step(60)
+    spec.oc_pt = spec.oc_pt[:0]
+    o0 = OracleDomain(spec)
+    o0.step(60)
+    a, b = o1.seismograms(0, 60), o0.seismograms(0, 60)
+    assert np.abs(a - b).max() > 1e-6 * np.abs(b).max()
+    (d / "inparam.model").write_text((d / "inparam.model").read_text().replace("constant$4.0", "marsocean"))
+    with pytest.raises(ValueError, match="Unknown ocean-load model"):
+        solver.Simulation(d).build()
