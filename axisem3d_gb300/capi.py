@@ -77,6 +77,8 @@ def bind(lib: C.CDLL, prefix: str, field_ctype, extra_double_io: bool = False):
     f("learn_wisdom").argtypes = [C.c_void_p, C.c_float]
     f("get_wisdom").argtypes = [C.c_void_p, P_I32]
     f("add_surface").argtypes = [C.c_void_p, C.c_int32, P_I32, P_I32, C.c_int32]
+    f("set_receiver_dumps").argtypes = [C.c_void_p, C.c_int32, P_I32]
+    f("read_strain_curl").argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, field_ctype]
     f("add_ocean_load").argtypes = [C.c_void_p, C.c_int32, P_I32, P_I32, C.POINTER(C.c_float)]
     f("surface_record_size").argtypes = [C.c_void_p]
     f("surface_record_size").restype = C.c_int64
@@ -164,6 +166,8 @@ class _DomainBase:
         if len(spec.r_elem):
             self._ck(self._call("add_receivers", h, len(spec.r_elem), _p(c(spec.r_elem, np.int32), C.c_int32),
                                 _p(c(spec.r_phi, np.float32), C.c_float), _p(c(spec.r_w, np.float32), C.c_float)))
+        if len(spec.r_dump) and np.any(spec.r_dump):
+            self._ck(self._call("set_receiver_dumps", h, len(spec.r_dump), _p(c(spec.r_dump, np.int32), C.c_int32)))
         if len(spec.oc_pt):
             self._ck(self._call("add_ocean_load", h, len(spec.oc_pt), _p(c(spec.oc_pt, np.int32), C.c_int32),
                                 _p(c(spec.oc_len, np.int32), C.c_int32), _p(c(spec.oc_vals, np.float32), C.c_float)))
@@ -233,6 +237,16 @@ class _DomainBase:
             raise ValueError(f"field size {v.size} != {n}")
         buf = v.view(self.field_dtype)
         self._ck(self._call("set_field", self.h, FIELD[which], PHASE[phase], _p(buf, self.field_ctype)))
+
+    def strain_curl(self, which: str, first: int, n: int) -> np.ndarray:
+        """Strain ([n][strain receivers][6], RTZ) or curl ([n][curl receivers][3]) of steps
+        first..first+n-1 for the receivers flagged dump_strain / dump_curl."""
+        bit, k = (1, 6) if which == "strain" else (2, 3)
+        nrec = int(np.count_nonzero(np.asarray(self.spec.r_dump, np.int32) & bit)) if len(self.spec.r_dump) else 0
+        out = np.zeros(max(n * nrec * k, 1), self.field_dtype)
+        self._ck(self._call("read_strain_curl", self.h, 0 if bit == 1 else 1, int(first), int(n),
+                            _p(out, self.field_ctype)))
+        return out[:n * nrec * k].astype(np.float64).reshape(n, nrec, k)
 
     def seismograms(self, first: int, n: int) -> np.ndarray:
         nrec = len(self.spec.r_elem)

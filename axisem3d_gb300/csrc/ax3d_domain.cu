@@ -98,6 +98,7 @@ struct ax3d_domain {
 
     std::vector<int32_t> e_pts, e_flags, e_nr;
     std::vector<float> e_geo, e_trig;
+    std::vector<uint8_t> e_hastrig;
     std::vector<int64_t> e_mofs, e_aofs;
     std::vector<float> e_mod, e_attm;
 
@@ -137,6 +138,11 @@ struct ax3d_domain {
     DevBuf<int32_t> d_relem;
     DevBuf<float> d_rphi, d_rw, d_seis;
     int seis_cap = 0;
+    // dump_strain / dump_curl receivers: list of (receiver, strain slot, curl slot)
+    std::vector<int32_t> r_dump;
+    int n_strain = 0, n_curl = 0, n_sclist = 0;
+    DevBuf<int32_t> d_sclist;
+    DevBuf<float> d_strain, d_curl;
     // whole-surface recorder: edges (element, side), record every sf_interval steps
     std::vector<int32_t> sf_elem, sf_side;
     int sf_interval = 1;
@@ -309,6 +315,7 @@ struct ax3d_domain {
                 e_trig.insert(e_trig.end(), trig + (int64_t)e * 100, trig + (int64_t)e * 100 + 100);
             else
                 e_trig.insert(e_trig.end(), 100, 0.f);
+            e_hastrig.push_back(trig ? 1 : 0);
             const int64_t mlen = (int64_t)km * 25 * (e3d ? nr : 1);
             e_mofs.push_back((int64_t)e_mod.size());
             e_mod.insert(e_mod.end(), mod + mofs[e], mod + mofs[e] + mlen);
@@ -561,6 +568,24 @@ struct ax3d_domain {
         seis_cap = std::max<int>((int)stf.size(), 1);
         d_seis.alloc((size_t)seis_cap * std::max<size_t>(r_elem.size(), 1) * 3);
         d_seis.zero(st);
+        {
+            std::vector<int32_t> list;
+            n_strain = n_curl = 0;
+            for (size_t r = 0; r < r_dump.size(); r++) {
+                if (!r_dump[r]) continue;
+                if (!e_hastrig[r_elem[r]])  // Receiver.cpp:49-51 forces the RTZ transform
+                    throw Error(AX3D_ERR_ARG, "ax3d_set_receiver_dumps || strain / curl receivers need theta tables");
+                list.push_back((int32_t)r);
+                list.push_back((r_dump[r] & 1) ? n_strain++ : -1);
+                list.push_back((r_dump[r] & 2) ? n_curl++ : -1);
+            }
+            n_sclist = (int)list.size() / 3;
+            d_sclist.upload(list.empty() ? std::vector<int32_t>{0} : list, st);
+            d_strain.alloc((size_t)seis_cap * std::max(n_strain, 1) * 6);
+            d_strain.zero(st);
+            d_curl.alloc((size_t)seis_cap * std::max(n_curl, 1) * 3);
+            d_curl.zero(st);
+        }
         d_flag.alloc(1);
         d_flag.zero(st);
         d_tstep.alloc(1);
@@ -681,6 +706,8 @@ struct ax3d_domain {
             if (t >= seis_cap) grow_seis(t + 1);
             ax3d::launch_record(P, T, F.su, d_relem.p, d_rphi.p, d_rw.p, (int)r_elem.size(), d_seis.p, seis_cap,
                                 d_targ.p, 0, stream);
+            ax3d::launch_record_strain_curl(P, T, F.su, d_relem.p, d_rphi.p, d_rw.p, d_sclist.p, n_sclist,
+                                            d_strain.p, n_strain, d_curl.p, n_curl, seis_cap, d_targ.p, 0, stream);
         }
         if (!sf_elem.empty()) {
             if (t / sf_interval >= sf_cap) grow_surf(t / sf_interval + 1);
@@ -711,6 +738,18 @@ struct ax3d_domain {
         CK(cudaStreamSynchronize(stream));
         std::swap(nb.p, d_seis.p);
         std::swap(nb.n, d_seis.n);
+        for (int which = 0; which < 2; which++) {
+            DevBuf<float> &buf = which ? d_curl : d_strain;
+            const size_t row = which ? (size_t)std::max(n_curl, 1) * 3 : (size_t)std::max(n_strain, 1) * 6;
+            DevBuf<float> nc;
+            nc.alloc((size_t)cap * row);
+            nc.zero(stream);
+            CK(cudaMemcpyAsync(nc.p, buf.p, (size_t)seis_cap * row * sizeof(float), cudaMemcpyDeviceToDevice,
+                               stream));
+            CK(cudaStreamSynchronize(stream));
+            std::swap(nc.p, buf.p);
+            std::swap(nc.n, buf.n);
+        }
         seis_cap = cap;
         drop_graph();  // the captured step holds the old buffer address
     }
@@ -770,7 +809,9 @@ struct ax3d_domain {
             tbegin(AX3D_TIMER_RECORD);
             ax3d::launch_record(P, T, F.su, d_relem.p, d_rphi.p, d_rw.p, (int)r_elem.size(), d_seis.p, seis_cap,
                                 d_tstep.p, -1, stream);
-            tend(1);
+            ax3d::launch_record_strain_curl(P, T, F.su, d_relem.p, d_rphi.p, d_rw.p, d_sclist.p, n_sclist,
+                                            d_strain.p, n_strain, d_curl.p, n_curl, seis_cap, d_tstep.p, -1, stream);
+            tend(1 + (n_sclist > 0));
         }
         if (!sf_elem.empty()) {
             tbegin(AX3D_TIMER_RECORD);
@@ -859,6 +900,8 @@ struct ax3d_domain {
             for (auto *b : {&d_sku, &d_skv, &d_fku, &d_fkv}) b->zero(stream);
         d_mem.zero(stream);
         d_seis.zero(stream);
+        d_strain.zero(stream);
+        d_curl.zero(stream);
         if (!sf_elem.empty()) d_surf.zero(stream);
         d_flag.zero(stream);
         reset_wisdom(stream);
@@ -1092,6 +1135,33 @@ int ax3d_read_seismograms(ax3d_domain *d, int32_t first, int32_t nsteps, float *
         if (first + nsteps > d->seis_cap) throw Error(AX3D_ERR_ARG, "ax3d_read_seismograms || steps not recorded");
         const size_t row = d->r_elem.size() * 3;
         CK(cudaMemcpyAsync(out, d->d_seis.p + (size_t)first * row, (size_t)nsteps * row * sizeof(float),
+                           cudaMemcpyDeviceToHost, d->stream));
+        CK(cudaStreamSynchronize(d->stream));
+    });
+}
+
+int ax3d_set_receiver_dumps(ax3d_domain *d, int32_t n, const int32_t *flags) {
+    return guard([&] {
+        if (!d || n < 0 || (n && !flags)) throw Error(AX3D_ERR_ARG, "ax3d_set_receiver_dumps || bad argument");
+        if (d->finalized) throw Error(AX3D_ERR_STATE, "ax3d_set_receiver_dumps || domain already finalized");
+        if (n != (int)d->r_elem.size())
+            throw Error(AX3D_ERR_ARG, "ax3d_set_receiver_dumps || one flag per receiver added");
+        for (int i = 0; i < n; i++)
+            if (flags[i] < 0 || flags[i] > 3) throw Error(AX3D_ERR_ARG, "ax3d_set_receiver_dumps || flags must be 0..3");
+        d->r_dump.assign(flags, flags + n);
+    });
+}
+
+int ax3d_read_strain_curl(ax3d_domain *d, int32_t which, int32_t first, int32_t nsteps, float *out) {
+    return guard([&] {
+        if (!d || !out || first < 0 || nsteps < 0 || which < 0 || which > 1)
+            throw Error(AX3D_ERR_ARG, "ax3d_read_strain_curl || bad argument");
+        d->need_final();
+        if (first + nsteps > d->seis_cap) throw Error(AX3D_ERR_ARG, "ax3d_read_strain_curl || steps not recorded");
+        const size_t row = which ? (size_t)d->n_curl * 3 : (size_t)d->n_strain * 6;
+        const float *src = which ? d->d_curl.p : d->d_strain.p;
+        if (row == 0 || nsteps == 0) return;
+        CK(cudaMemcpyAsync(out, src + (size_t)first * row, (size_t)nsteps * row * sizeof(float),
                            cudaMemcpyDeviceToHost, d->stream));
         CK(cudaStreamSynchronize(d->stream));
     });

@@ -101,6 +101,39 @@ __device__ __forceinline__ void grad6_lane(const LaneOps &L, const Geo &g, bool 
     }
 }
 
+// computeGrad9 at one point for order alpha (Gradient.cpp:84-152): g[3c + d] = d-th
+// derivative (s, phi, z) of component c, with grad6's axial rows.
+__device__ __forceinline__ void grad9_lane(const LaneOps &L, const Geo &g, bool axial, int alpha,
+                                          const float2 *su, float2 g9[9]) {
+    const int p = L.i * 5 + L.j;
+    float2 GU[3], UG[3];
+    gu_ug(L, su, GU[0], UG[0]);
+    gu_ug(L, su + 25, GU[1], UG[1]);
+    gu_ug(L, su + 50, GU[2], UG[2]);
+    const float a = (float)alpha;
+    float2 u0 = su[p], u1 = su[25 + p], u2 = su[50 + p];
+    float2 v0 = cadd(u0, cimul(a, u1));
+    float2 v1 = csub(cimul(a, u0), u1);
+    float2 v2 = cimul(a, u2);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        g9[3 * c] = cadd(cscale(g.dzdeta, GU[c]), cscale(g.dzdxii, UG[c]));
+        g9[3 * c + 2] = cadd(cscale(g.dsdeta, GU[c]), cscale(g.dsdxii, UG[c]));
+    }
+    g9[1] = cscale(g.inv_s, v1);
+    g9[4] = cscale(g.inv_s, v0);
+    g9[7] = cscale(g.inv_s, v2);
+    if (axial && L.i == 0) {
+        g9[4] = cadd(g9[4], cscale(g.dzdeta, cadd(GU[0], cimul(a, GU[1]))));
+        g9[1] = cadd(g9[1], cscale(g.dzdeta, csub(cimul(a, GU[0]), GU[1])));
+        g9[7] = cadd(g9[7], cscale(g.dzdeta, cimul(a, GU[2])));
+        if (alpha == 1) {
+            g9[4] = cadd(g9[4], cscale(g.dzdxii, cadd(UG[0], cimul(a, UG[1]))));
+            g9[1] = cadd(g9[1], cscale(g.dzdxii, csub(cimul(a, UG[0]), UG[1])));
+        }
+    }
+}
+
 // computeQuad6 at one point for order beta.  Each lane first writes its X, Y, g terms
 // into the scratch q ([14][25] complex), then reads its neighbours'.  Must be called by
 // all lanes of the warp (lanes >= 25 pass active = false).
@@ -225,6 +258,21 @@ __device__ __forceinline__ void rtz_spz(float2 u[6], float s1, float c1, float s
     u[0] = cadd(cadd(cscale(0.5f, sum02), cscale(c2, dif02)), cscale(s2, u[4]));
     u[2] = csub(sum02, u[0]);
     u[4] = csub(cscale(c2, u[4]), cscale(s2, dif02));
+    u[3] = csub(cscale(c1, u3), cscale(s1, u[5]));
+    u[5] = cadd(cscale(c1, u[5]), cscale(s1, u3));
+}
+
+// CrdTransTIsoSolid::transformSPZ_RTZ of a nine-component gradient (CrdTransTIsoSolid.cpp:44-66)
+__device__ __forceinline__ void spz_rtz9(float2 u[9], float s1, float c1, float s2, float c2) {
+    const float2 sum08 = cadd(u[0], u[8]), dif08 = csub(u[0], u[8]);
+    const float2 sum26 = cadd(u[2], u[6]), dif26 = csub(u[2], u[6]);
+    const float2 u1 = u[1], u3 = u[3];
+    u[0] = cscale(0.5f, csub(cadd(sum08, cscale(c2, dif08)), cscale(s2, sum26)));
+    u[2] = cscale(0.5f, cadd(cadd(dif26, cscale(c2, sum26)), cscale(s2, dif08)));
+    u[6] = csub(u[2], dif26);
+    u[8] = csub(sum08, u[0]);
+    u[1] = csub(cscale(c1, u1), cscale(s1, u[7]));
+    u[7] = cadd(cscale(c1, u[7]), cscale(s1, u1));
     u[3] = csub(cscale(c1, u3), cscale(s1, u[5]));
     u[5] = cadd(cscale(c1, u[5]), cscale(s1, u3));
 }

@@ -3,12 +3,105 @@
 // order loop of SolidElement::displToStiff (SOLVER/src/core/element/SolidElement.cpp:
 // 404-443) and FluidElement::displToStiff (FluidElement.cpp:333-355) is embarrassingly
 // parallel there.  The physical-space (3D material) elements are in ax3d_phys.cu.
+#include <algorithm>
+
 #include "ax3d_elem_ops.cuh"
 #include "ax3d_kernels.cuh"
 
 namespace ax3d {
 
 
+
+// SolidElement::computeStrain / computeCurl (SolidElement.cpp:219-345, no relabelling) at
+// receivers with dump_strain / dump_curl.  One CTA of four warps per receiver: warp w takes
+// orders w, w + 4, ...; lane p < 25 owns GLL point p: grad6 (strain) or grad9 (curl),
+// rotated to RTZ, synthesised at the receiver's phi; the weighted sum is reduced in the CTA.
+// list[i] = (receiver, strain slot or -1, curl slot or -1).
+__global__ void __launch_bounds__(128)
+    k_record_strain_curl(PointTable P, ElemTable T, const float2 *__restrict__ su, const int32_t *rec_elem,
+                         const float *rec_phi, const float *rec_w, const int32_t *list, int n, float *strain_out,
+                         int nst, float *curl_out, int ncu, int cap, const int32_t *tptr, int tofs) {
+    __shared__ float2 sh[4][75];
+    __shared__ float red[4][9];
+    const int t = *tptr + tofs;
+    if (t < 0 || t >= cap) return;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const bool active = lane < NPE;
+    const int p = active ? lane : 0;
+    for (int i = blockIdx.x; i < n; i += gridDim.x) {
+        const int r = list[3 * i], sslot = list[3 * i + 1], cslot = list[3 * i + 2];
+        const int e = rec_elem[r];
+        const float phi = rec_phi[r];
+        const int nr = T.nr[e], lim = nr / 2 - (nr % 2 == 0);
+        const bool axial = T.flags[e] & EF_AXIAL;
+        LaneOps L;
+        L.init(p, axial);
+        Geo g;
+        g.load(T.geo + (int64_t)e * 125, p);
+        const float *tr = T.trig + (int64_t)e * 100;
+        const float s1 = tr[p], c1 = tr[25 + p], s2 = tr[50 + p], c2 = tr[75 + p];
+        const int pt = T.pts[e * NPE + p];
+        const int pnr = P.nr[pt], plim = pnr / 2 - (pnr % 2 == 0);  // scatterDisplToElement drops the Nyquist order
+        const float2 *up = su + P.sofs[pt];
+        float acc[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) acc[k] = 0.f;
+        for (int a = warp; a <= lim; a += 4) {
+            if (active)
+#pragma unroll
+                for (int c = 0; c < 3; c++)
+                    sh[warp][c * 25 + lane] = a <= plim ? up[a * 3 + c] : make_float2(0.f, 0.f);
+            __syncwarp();
+            if (active) {
+                float sn, cs;
+                sincosf((float)a * phi, &sn, &cs);
+                const float ex = a == 0 ? 1.f : 2.f * cs, ey = a == 0 ? 0.f : 2.f * sn;
+                if (sslot >= 0) {
+                    float2 e6[6];
+                    grad6_lane(L, g, axial, a, sh[warp], e6);
+                    spz_rtz(e6, s1, c1, s2, c2);
+#pragma unroll
+                    for (int k = 0; k < 6; k++) acc[k] += ex * e6[k].x - ey * e6[k].y;
+                }
+                if (cslot >= 0) {
+                    float2 g9[9];
+                    grad9_lane(L, g, axial, a, sh[warp], g9);
+                    spz_rtz9(g9, s1, c1, s2, c2);
+                    const float2 k0 = csub(g9[7], g9[5]), k1 = csub(g9[2], g9[6]), k2 = csub(g9[3], g9[1]);
+                    acc[6] += ex * k0.x - ey * k0.y;
+                    acc[7] += ex * k1.x - ey * k1.y;
+                    acc[8] += ex * k2.x - ey * k2.y;
+                }
+            }
+            __syncwarp();
+        }
+        const float w = active ? rec_w[(int64_t)r * NPE + lane] : 0.f;
+        const bool use = active && fabsf(w) >= 1e-10f;  // SolidElement.cpp:262 skips tiny weights
+#pragma unroll
+        for (int k = 0; k < 9; k++) {
+            float v = use ? w * acc[k] : 0.f;
+            for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+            if (lane == 0) red[warp][k] = v;
+        }
+        __syncthreads();
+        if (threadIdx.x < 9) {
+            const int k = threadIdx.x;
+            const float v = red[0][k] + red[1][k] + red[2][k] + red[3][k];
+            if (k < 6 && sslot >= 0) strain_out[((int64_t)t * nst + sslot) * 6 + k] = v;
+            if (k >= 6 && cslot >= 0) curl_out[((int64_t)t * ncu + cslot) * 3 + (k - 6)] = v;
+        }
+        __syncthreads();
+    }
+}
+
+void launch_record_strain_curl(const PointTable &P, const ElemTable &T, const float2 *su, const int32_t *rec_elem,
+                               const float *rec_phi, const float *rec_w, const int32_t *list, int n,
+                               float *strain_out, int nst, float *curl_out, int ncu, int cap, const int32_t *tptr,
+                               int tofs, cudaStream_t s) {
+    if (n <= 0) return;
+    k_record_strain_curl<<<std::min(n, 152 * 8), 128, 0, s>>>(P, T, su, rec_elem, rec_phi, rec_w, list, n,
+                                                               strain_out, nst, curl_out, ncu, cap, tptr, tofs);
+}
 
 void set_g_matrices(const float *g_gll, const float *g_glj, cudaStream_t s) {
     cudaMemcpyToSymbolAsync(c_G, g_gll, 25 * sizeof(float), 0, cudaMemcpyHostToDevice, s);

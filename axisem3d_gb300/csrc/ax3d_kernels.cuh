@@ -79,6 +79,10 @@ void launch_source(const PointTable &P, const ElemTable &T, const Fields &F,
                    const int32_t *src_elem, const int32_t *src_nord, const int64_t *src_ofs,
                    const float2 *src_force, int nsrc, const float *stf, int nstf,
                    const int32_t *tptr, int tofs, cudaStream_t s);
+void launch_record_strain_curl(const PointTable &P, const ElemTable &T, const float2 *su, const int32_t *rec_elem,
+                               const float *rec_phi, const float *rec_w, const int32_t *list, int n,
+                               float *strain_out, int nst, float *curl_out, int ncu, int cap, const int32_t *tptr,
+                               int tofs, cudaStream_t s);
 void launch_record(const PointTable &P, const ElemTable &T, const float2 *su,
                    const int32_t *rec_elem, const float *rec_phi, const float *rec_w, int nrec,
                    float *out_base, int cap, const int32_t *tptr, int tofs, cudaStream_t s);

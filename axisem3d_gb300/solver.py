@@ -172,6 +172,34 @@ def _colat(s, z):
     return 0.0 if r < 1e-300 else math.acos(max(-1.0, min(1.0, z / r)))
 
 
+def src_to_glob(theta_s, phi_s, src_theta, src_phi):
+    """Geodesy::rotateSrc2Glob on the unit sphere (no ellipticity)."""
+    x = np.array([math.sin(theta_s) * math.cos(phi_s), math.sin(theta_s) * math.sin(phi_s), math.cos(theta_s)])
+    xg = _rot(src_theta, src_phi) @ x
+    t = math.acos(max(-1.0, min(1.0, xg[2])))
+    p = math.atan2(xg[1], xg[0]) if math.hypot(xg[0], xg[1]) > 1e-300 else phi_s
+    return t, (p + 2 * math.pi) % (2 * math.pi)
+
+
+def back_azimuth(src_theta, src_phi, rec_theta, rec_phi):
+    """Geodesy::backAzimuth (Geodesy.cpp:149-174) with atan4 (Geodesy.cpp:24-38): geocentric
+    colatitudes and longitudes in radians, spherical Earth."""
+    d, e, f, c = math.sin(src_phi), -math.cos(src_phi), -math.sin(src_theta), math.cos(src_theta)
+    a, b = f * e, -f * d
+    d1, e1, f1, c1 = math.sin(rec_phi), -math.cos(rec_phi), -math.sin(rec_theta), math.cos(rec_theta)
+    g1, h1 = -c1 * e1, c1 * d1
+    ss = (a - d1) ** 2 + (b - e1) ** 2 + c * c - 2.0
+    sc = (a - g1) ** 2 + (b - h1) ** 2 + (c - f1) ** 2 - 2.0
+    if math.hypot(ss, sc) < 1e-300:
+        return 0.0
+    t = math.atan2(ss, sc)
+    if t < 0.0:
+        t += math.pi
+    if ss < 0.0:
+        t += math.pi
+    return t
+
+
 def glob_to_src(theta_g, phi_g, src_theta, src_phi):
     """Geodesy::rotateGlob2Src on the unit sphere (no ellipticity)."""
     x = np.array([math.sin(theta_g) * math.cos(phi_g), math.sin(theta_g) * math.sin(phi_g), math.cos(theta_g)])
@@ -581,26 +609,41 @@ class Simulation:
     # ------------------------------------------------------------------ receivers
     def _receivers(self, spec):
         """STATIONS -> Receiver (Receiver.cpp:23-117): source-centred (theta, phi), element and
-        Lagrange weights (GLJ along xi on axial elements)."""
+        Lagrange weights (GLJ along xi on axial elements), back azimuth, and the optional
+        dump_strain / dump_curl keywords after the sixth column (ReceiverCollection.cpp:48-81;
+        lines with fewer than six columns or bad numbers are skipped)."""
         par = self.par
+        self.baz = []
         system = par.get("OUT_STATIONS_SYSTEM").lower()
         self.components = par.get("OUT_STATIONS_COMPONENTS").upper()
         lines = [l.split() for l in (self.input_dir / par.get("OUT_STATIONS_FILE")).read_text().splitlines() if l.strip()]
         src_t = math.pi / 2 - math.radians(self.src_lat)
         src_p = math.radians(self.src_lon % 360)
-        rec = []
-        for name, net, la, lo, _elev, bur in lines:
-            la, lo, bur = float(la), float(lo), float(bur)
+        rec, dumps = [], []
+        for toks in lines:
+            if len(toks) < 6:
+                continue
+            name, net = toks[0], toks[1]
+            try:
+                la, lo, bur = float(toks[2]), float(toks[3]), float(toks[5])
+            except ValueError:
+                continue
+            extra = {t.lower() for t in toks[6:]}
+            dumps.append((1 if "dump_strain" in extra else 0) | (2 if "dump_curl" in extra else 0))
             if system == "geographic":
-                th, ph = glob_to_src(math.pi / 2 - math.radians(la), math.radians(lo % 360), src_t, src_p)
+                th_g, ph_g = math.pi / 2 - math.radians(la), math.radians(lo % 360)
+                th, ph = glob_to_src(th_g, ph_g, src_t, src_p)
             else:
                 th, ph = math.radians(la), math.radians(lo)
+                th_g, ph_g = src_to_glob(th, ph, src_t, src_p)
+            self.baz.append(back_azimuth(src_t, src_p, th_g, ph_g))
             r = self.R - bur
             e, xi, eta = self._locate(r * math.sin(th), r * math.cos(th))
             wxi = _lagrange(xi, S.glj()[0] if self.axial_e[e] else S.gll()[0])
             weta = _lagrange(eta, S.gll()[0])
             rec.append((name, net, la, lo, bur, th, ph, e, np.outer(wxi, weta).ravel()))
         self.receivers = rec
+        spec.r_dump = np.array(dumps, np.int32)
         spec.r_elem = np.array([r[7] for r in rec], np.int32)
         spec.r_phi = np.array([r[6] for r in rec], np.float32)
         spec.r_w = np.array([r[8] for r in rec], np.float32).reshape(len(rec), 25)
@@ -708,7 +751,7 @@ class Simulation:
 
     # ------------------------------------------------------------------ output
     def rotate(self, seis):
-        """PointwiseRecorder::record's SPZ -> RTZ rotation (PointwiseRecorder.cpp:76-93)."""
+        """PointwiseRecorder::record's SPZ -> RTZ / ENZ rotation (PointwiseRecorder.cpp:76-93)."""
         out = np.array(seis, np.float64)
         if self.components == "SPZ":
             return out
@@ -717,11 +760,30 @@ class Simulation:
             s_, p_, z_ = seis[:, i, 0], seis[:, i, 1], seis[:, i, 2]
             ur = s_ * math.sin(th) + z_ * math.cos(th)
             ut = s_ * math.cos(th) - z_ * math.sin(th)
-            out[:, i, 0], out[:, i, 1], out[:, i, 2] = ut, p_, ur
+            if self.components == "ENZ":
+                cb, sb = math.cos(self.baz[i]), math.sin(self.baz[i])
+                out[:, i, 0], out[:, i, 1], out[:, i, 2] = -ut * sb + p_ * cb, -ut * cb - p_ * sb, ur
+            else:
+                out[:, i, 0], out[:, i, 1], out[:, i, 2] = ut, p_, ur
         return out
 
-    def write_netcdf(self, seis_rtz, path=None):
-        """output/stations/axisem3d_synthetics.nc with time_points and NET.NAME.<comp>."""
+    def rotate_curl(self, curl):
+        """Curl of the flagged receivers (theta, phi, r) -> ENZ when OUT_STATIONS_COMPONENTS is
+        ENZ (PointwiseRecorder.cpp:116-129); strain stays in RTZ."""
+        out = np.array(curl, np.float64)
+        if self.components != "ENZ":
+            return out
+        idx = [i for i in range(len(self.receivers)) if self.spec.r_dump[i] & 2]
+        for k, i in enumerate(idx):
+            cb, sb = math.cos(self.baz[i]), math.sin(self.baz[i])
+            ut, up, ur = curl[:, k, 0], curl[:, k, 1], curl[:, k, 2]
+            out[:, k, 0], out[:, k, 1], out[:, k, 2] = -ut * sb + up * cb, -ut * cb - up * sb, ur
+        return out
+
+    def write_netcdf(self, seis_rtz, path=None, strain=None, curl=None):
+        """output/stations/axisem3d_synthetics.nc with time_points and NET.NAME.<comp>, plus
+        NET.NAME.RTZ.strain [steps][6] and NET.NAME.RTZ.curl [steps][3] for the receivers
+        flagged dump_strain / dump_curl (PointwiseIONetCDF.cpp:56-95)."""
         path = Path(path or self.output_dir / "stations" / "axisem3d_synthetics.nc")
         path.parent.mkdir(parents=True, exist_ok=True)
         n = seis_rtz.shape[0]
@@ -732,6 +794,16 @@ class Simulation:
         for i, r in enumerate(self.receivers):
             ds.add_var(f"{r[1]}.{r[0]}.{self.components}", ("ntime", "ncomp"), seis_rtz[:, i].astype(np.float32),
                        attrs={"latitude": float(r[2]), "longitude": float(r[3]), "depth": float(r[4])})
+        dump = np.asarray(self.spec.r_dump, np.int32) if len(self.spec.r_dump) else np.zeros(len(self.receivers), np.int32)
+        for bit, arr, tag, k in ((1, strain, "strain", 6), (2, curl, "curl", 3)):
+            if arr is None:
+                continue
+            if k == 6:
+                ds.add_dim("nstrain", 6)
+            for j, i in enumerate(np.flatnonzero(dump & bit)):
+                r = self.receivers[i]
+                ds.add_var(f"{r[1]}.{r[0]}.RTZ.{tag}", ("ntime", "nstrain" if k == 6 else "ncomp"),
+                           arr[:, j].astype(np.float32))
         NC.write(path, ds)
         return path
 
@@ -755,7 +827,8 @@ class Simulation:
 
 def write_inputs(input_dir, mesh_kw=None, nu=2, stf="gauss", hdur=50.0, steps=2000, record_length=None,
                  n_stations=20, depth_km=100.0, seed=0, attenuation=False, system="source_centered",
-                 models3d=(), lucky=False, whole_surface="false", ocean="none"):
+                 models3d=(), lucky=False, whole_surface="false", ocean="none", station_extra=(),
+                 components="RTZ"):
     """Seeded inputs of the small benchmark configuration: mesh, four parfiles, CMTSOLUTION
     (moment tensor ~ N(0, 1e20 N*m) written in dyn*cm) and STATIONS at uniform distance."""
     from . import mesher
@@ -774,7 +847,7 @@ def write_inputs(input_dir, mesh_kw=None, nu=2, stf="gauss", hdur=50.0, steps=20
         f"TIME_DELTA_T 0.0\nTIME_DELTA_T_FACTOR 1.0\nTIME_RECORD_LENGTH {rl}\nSOURCE_TYPE earthquake\n"
         f"SOURCE_FILE CMTSOLUTION\nSOURCE_TIME_FUNCTION {stf}\nSOURCE_STF_HALF_DURATION {hdur}\n"
         f"OUT_STATIONS_FILE STATIONS\nOUT_STATIONS_SYSTEM {system}\nOUT_STATIONS_DUPLICATED rename\n"
-        f"OUT_STATIONS_FORMAT netcdf\nOUT_STATIONS_COMPONENTS RTZ\nOUT_STATIONS_RECORD_INTERVAL 1\n"
+        f"OUT_STATIONS_FORMAT netcdf\nOUT_STATIONS_COMPONENTS {components}\nOUT_STATIONS_RECORD_INTERVAL 1\n"
         f"OUT_STATIONS_DUMP_INTERVAL 1000\nOUT_STATIONS_WHOLE_SURFACE {whole_surface}\nOUT_STATIONS_DEPTH_REF false\n")
     (d / "inparam.advanced").write_text(
         f"ATTENUATION_CG4 true\nATTENUATION_SPECFEM_LEGACY false\nATTENUATION_QKAPPA true\n"
@@ -789,6 +862,7 @@ def write_inputs(input_dir, mesh_kw=None, nu=2, stf="gauss", hdur=50.0, steps=20
         f"half duration:   {hdur:.2f}\nlatitude:       0.0\nlongitude:      0.0\ndepth:          {depth_km:.4f}\n"
         + "".join(f"{k}:       {v:.6e}\n" for k, v in zip(names, m)))
     dist = np.linspace(10.0, 170.0, n_stations)
-    (d / "STATIONS").write_text("".join(f"S{i:03d}       SY       {t:.4f}     {(37.0 * i) % 360:.4f}    0.0    0.0\n"
-                                        for i, t in enumerate(dist)))
+    extra = [f"  {station_extra[i % len(station_extra)]}" if station_extra else "" for i in range(n_stations)]
+    (d / "STATIONS").write_text("".join(f"S{i:03d}       SY       {t:.4f}     {(37.0 * i) % 360:.4f}    0.0    0.0"
+                                        f"{extra[i]}\n" for i, t in enumerate(dist)))
     return d

@@ -130,7 +130,7 @@ def annulus_domain(seed=0, n_theta=4, n_r=3, r_in=3000e3, r_out=6371e3, theta_ma
                    nu_random=False, nu_max=None, fluid_layers=(), mat=MAT_ISO, in3d=False,
                    att=ATT_NONE, nsls=3, mass3d=False, couple3d=False, dt=0.05, source=True,
                    n_receivers=3, stf_len=64, stability_interval=0, kahan=False, fluid3d=False,
-                   perturb=0.04, lucky=False, surface_interval=0, ocean=""):
+                   perturb=0.04, lucky=False, surface_interval=0, ocean="", dumps=False):
     """Connected spherical-element mesh on an (r, theta) grid.
 
     Element (ir, it) spans radii [rs[ir], rs[ir+1]] and colatitudes [ts[it], ts[it+1]];
@@ -138,7 +138,8 @@ def annulus_domain(seed=0, n_theta=4, n_r=3, r_in=3000e3, r_out=6371e3, theta_ma
     surface_interval > 0 records the outer surface (side 2, eta = +1, of every solid
     element of the top layer) every surface_interval steps.  ocean = "1d" puts a 3 km
     ocean on the outer surface points (MassOcean1D); "3d" varies its depth with azimuth
-    and tilts the surface normal (MassOcean3D)."""
+    and tilts the surface normal (MassOcean3D).  dumps = True flags the receivers
+    dump_strain / dump_curl in turn (3, 1, 2, 0, ...)."""
     rng = np.random.default_rng(seed)
     rs = np.linspace(r_in, r_out, n_r + 1)
     ts = np.linspace(0.0, theta_max, n_theta + 1)
@@ -340,6 +341,9 @@ def annulus_domain(seed=0, n_theta=4, n_r=3, r_in=3000e3, r_out=6371e3, theta_ma
         nsls=nsls if att != ATT_NONE else 0, att_alpha=alpha, att_beta=beta, att_gamma=gamma,
         att_do_kappa=True, sources=sources, stf=stf, r_elem=r_elem, r_phi=r_phi, r_w=r_w,
         kahan=kahan, stability_interval=stability_interval, **ea)
+    spec.p_crds = crds_pt
+    if dumps:
+        spec.r_dump = np.array([(3, 1, 2, 0)[i % 4] for i in range(len(r_elem))], np.int32)
     if ocean:
         spec.oc_pt, spec.oc_len, spec.oc_vals = _ocean_rows(ocean, surf_acc, ms_acc, nr_pt, crds_pt, rng)
     if surface_interval > 0:

@@ -182,6 +182,17 @@ int ax3d_step(ax3d_domain *d, int32_t nsteps);
 /* Recorded (s, phi, z) displacement [nsteps][nrec][3] for steps first..first+nsteps-1. */
 int ax3d_read_seismograms(ax3d_domain *d, int32_t first, int32_t nsteps, float *out);
 
+/* Strain and curl at receivers (PointwiseRecorder::record, PointwiseRecorder.cpp:96-130;
+   SolidElement::computeStrain / computeCurl, SolidElement.cpp:219-345): flags[i] for each
+   receiver added so far, bit 0 dump_strain, bit 1 dump_curl (the STATIONS keywords,
+   ReceiverCollection.cpp:58-72).  Before ax3d_finalize. */
+int ax3d_set_receiver_dumps(ax3d_domain *d, int32_t n, const int32_t *flags);
+
+/* Strain (which = 0: six RTZ components per flagged receiver) or curl (which = 1: three)
+   of steps first..first+nsteps-1, recorded with the seismograms; [step][receiver][k] in
+   the order of the flagged receivers. */
+int ax3d_read_strain_curl(ax3d_domain *d, int32_t which, int32_t first, int32_t nsteps, float *out);
+
 /* Complex values in one whole-surface record: sum over edges of 15 (Nu_e + 1). */
 int64_t ax3d_surface_record_size(const ax3d_domain *d);
 

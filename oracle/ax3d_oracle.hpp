@@ -92,9 +92,12 @@ struct Oracle {
         int elem;
         Real phi;
         Real w[nPE];
+        int strain_slot = -1, curl_slot = -1;  // dump_strain / dump_curl (Receiver.cpp:21-53)
     };
     std::vector<Rec> recs;
     std::vector<Real> seis;  // [step][nrec][3]
+    int n_strain = 0, n_curl = 0;
+    std::vector<Real> strain_rec, curl_rec;  // [step][n_strain][6], [step][n_curl][3]
     // whole-surface recorder: edges (element, side), one record per sf_interval steps
     std::vector<int> sf_elem, sf_side;
     int sf_interval = 1;
@@ -205,7 +208,7 @@ struct Oracle {
                 for (int i = 0; i < nPE; i++) el.geo[k][i] = geo[(int64_t)e * 125 + k * 25 + i];
             for (int k = 0; k < 4; k++)
                 for (int i = 0; i < nPE; i++)
-                    el.trig[k][i] = (el.tiso && trig) ? trig[(int64_t)e * 100 + k * 25 + i] : Real(0);
+                    el.trig[k][i] = trig ? trig[(int64_t)e * 100 + k * 25 + i] : Real(0);
             if (el.tiso && !trig) throw std::runtime_error("Element || trig needed");
             int km = n_moduli(el.mat);
             int64_t len = (int64_t)km * nPE * (el.in3d ? el.nr : 1);
@@ -254,6 +257,8 @@ struct Oracle {
         }
         tstep = 1;
         seis.clear();
+        strain_rec.clear();
+        curl_rec.clear();
         surf.clear();
         reset_wisdom();
     }
@@ -451,6 +456,81 @@ struct Oracle {
         if (e.axial && beta > 0)
             for (int i = 0; i < nP; i++)
                 for (int j = 0; j < nP; j++) f[i * nP + j] += Gx[i][0] * (dzdeta[j] * g[j]);
+    }
+
+    // computeGrad9 (Gradient.cpp:84-152): the nine derivatives u_{i,j} in the order
+    // [s,s  s,phi  s,z  phi,s  phi,phi  phi,z  z,s  z,phi  z,z] (row = component), with
+    // the same axial rows as grad6; at alpha = 0 the formulas give the hardcoded branch.
+    void grad9(const Elem &e, int alpha, const C u[3][nPE], C g9[9][nPE]) const {
+        const Real(*Gx)[nP] = e.axial ? G_glj : G_gll;
+        const Real(*Ge)[nP] = G_gll;
+        const Real *dsdxii = e.geo[0], *dsdeta = e.geo[1], *dzdxii = e.geo[2], *dzdeta = e.geo[3],
+                   *inv_s = e.geo[4];
+        C ia(0, (Real)alpha);
+        C GU[3][nPE], UG[3][nPE], v[3][nPE];
+        for (int c = 0; c < 3; c++)
+            for (int i = 0; i < nP; i++)
+                for (int j = 0; j < nP; j++) {
+                    C gu(0), ug(0);
+                    for (int k = 0; k < nP; k++) {
+                        gu += Gx[k][i] * u[c][k * nP + j];
+                        ug += u[c][i * nP + k] * Ge[k][j];
+                    }
+                    GU[c][i * nP + j] = gu;
+                    UG[c][i * nP + j] = ug;
+                }
+        for (int p = 0; p < nPE; p++) {
+            v[0][p] = u[0][p] + ia * u[1][p];
+            v[1][p] = ia * u[0][p] - u[1][p];
+            v[2][p] = ia * u[2][p];
+            for (int c = 0; c < 3; c++) {
+                g9[3 * c][p] = dzdeta[p] * GU[c][p] + dzdxii[p] * UG[c][p];
+                g9[3 * c + 2][p] = dsdeta[p] * GU[c][p] + dsdxii[p] * UG[c][p];
+            }
+            g9[1][p] = inv_s[p] * v[1][p];
+            g9[4][p] = inv_s[p] * v[0][p];
+            g9[7][p] = inv_s[p] * v[2][p];
+        }
+        if (e.axial) {
+            for (int j = 0; j < nP; j++) {
+                C h0(0), h1(0), h2(0);
+                for (int k = 0; k < nP; k++) {
+                    h0 += Gx[k][0] * v[0][k * nP + j];
+                    h1 += Gx[k][0] * v[1][k * nP + j];
+                    h2 += Gx[k][0] * v[2][k * nP + j];
+                }
+                g9[4][j] += dzdeta[j] * h0;
+                g9[1][j] += dzdeta[j] * h1;
+                g9[7][j] += dzdeta[j] * h2;
+            }
+            if (alpha == 1) {
+                for (int j = 0; j < nP; j++) {
+                    C h0(0), h1(0);
+                    for (int k = 0; k < nP; k++) {
+                        h0 += v[0][k] * Ge[k][j];
+                        h1 += v[1][k] * Ge[k][j];
+                    }
+                    g9[4][j] += dzdxii[j] * h0;
+                    g9[1][j] += dzdxii[j] * h1;
+                }
+            }
+        }
+    }
+    // CrdTransTIsoSolid::transformSPZ_RTZ of the nine-component gradient
+    // (CrdTransTIsoSolid.cpp:44-66)
+    void spz_rtz9(const Elem &e, C *u[9], int p) const {
+        Real s1 = e.trig[0][p], c1 = e.trig[1][p], s2 = e.trig[2][p], c2 = e.trig[3][p];
+        C sum08 = *u[0] + *u[8], dif08 = *u[0] - *u[8];
+        C sum26 = *u[2] + *u[6], dif26 = *u[2] - *u[6];
+        C u1 = *u[1], u3 = *u[3];
+        *u[0] = Real(0.5) * (sum08 + c2 * dif08 - s2 * sum26);
+        *u[2] = Real(0.5) * (dif26 + c2 * sum26 + s2 * dif08);
+        *u[6] = *u[2] - dif26;
+        *u[8] = sum08 - *u[0];
+        *u[1] = c1 * u1 - s1 * *u[7];
+        *u[7] = c1 * *u[7] + s1 * u1;
+        *u[3] = c1 * u3 - s1 * *u[5];
+        *u[5] = c1 * *u[5] + s1 * u3;
     }
 
     // ================= CrdTransTIsoSolid (CrdTransTIsoSolid.cpp:14-42) =================
@@ -979,6 +1059,67 @@ struct Oracle {
                 for (int c = 0; c < 3; c++) out[c] += rc.w[p] * up[c];
             }
             for (int c = 0; c < 3; c++) seis[((size_t)t * recs.size() + r) * 3 + c] = out[c];
+        }
+        record_strain_curl(t);
+    }
+
+    // SolidElement::computeStrain / computeCurl (SolidElement.cpp:219-345) without PRT:
+    // grad6 (strain) or grad9 (curl) of every order, rotated to RTZ, then synthesised at the
+    // receiver's phi and summed with its weights.
+    void record_strain_curl(int t) {
+        if (n_strain == 0 && n_curl == 0) return;
+        if (strain_rec.size() < (size_t)(t + 1) * n_strain * 6) strain_rec.resize((size_t)(t + 1) * n_strain * 6, 0);
+        if (curl_rec.size() < (size_t)(t + 1) * n_curl * 3) curl_rec.resize((size_t)(t + 1) * n_curl * 3, 0);
+        static thread_local C u[3][nPE], g6[6][nPE], g9[9][nPE];
+        for (const Rec &rc : recs) {
+            if (rc.strain_slot < 0 && rc.curl_slot < 0) continue;
+            const Elem &e = elems[rc.elem];
+            Real st[6] = {0, 0, 0, 0, 0, 0}, cu[3] = {0, 0, 0};
+            std::vector<Real> sp((size_t)nPE * 6, 0), cp((size_t)nPE * 3, 0);  // per point sums
+            for (int a = 0; a <= e.nu - e.nyq; a++) {
+                for (int p = 0; p < nPE; p++)
+                    for (int c = 0; c < 3; c++) u[c][p] = solid_u_elem(su, pts[e.pts[p]], a, c);
+                C ex = a == 0 ? C(1) : Real(2) * C(std::cos((Real)a * rc.phi), std::sin((Real)a * rc.phi));
+                if (rc.strain_slot >= 0) {
+                    grad6(e, a, u, g6);
+                    for (int p = 0; p < nPE; p++) {
+                        C *ua[6] = {&g6[0][p], &g6[1][p], &g6[2][p], &g6[3][p], &g6[4][p], &g6[5][p]};
+                        spz_rtz(e, ua, p);
+                        for (int k = 0; k < 6; k++) sp[p * 6 + k] += (ex * g6[k][p]).real();
+                    }
+                }
+                if (rc.curl_slot >= 0) {
+                    grad9(e, a, u, g9);
+                    for (int p = 0; p < nPE; p++) {
+                        C *ua[9];
+                        for (int k = 0; k < 9; k++) ua[k] = &g9[k][p];
+                        spz_rtz9(e, ua, p);
+                        cp[p * 3] += (ex * (g9[7][p] - g9[5][p])).real();
+                        cp[p * 3 + 1] += (ex * (g9[2][p] - g9[6][p])).real();
+                        cp[p * 3 + 2] += (ex * (g9[3][p] - g9[1][p])).real();
+                    }
+                }
+            }
+            for (int p = 0; p < nPE; p++) {
+                if (std::abs((double)rc.w[p]) < 1e-10) continue;
+                for (int k = 0; k < 6; k++) st[k] += rc.w[p] * sp[p * 6 + k];
+                for (int k = 0; k < 3; k++) cu[k] += rc.w[p] * cp[p * 3 + k];
+            }
+            if (rc.strain_slot >= 0)
+                for (int k = 0; k < 6; k++) strain_rec[((size_t)t * n_strain + rc.strain_slot) * 6 + k] = st[k];
+            if (rc.curl_slot >= 0)
+                for (int k = 0; k < 3; k++) curl_rec[((size_t)t * n_curl + rc.curl_slot) * 3 + k] = cu[k];
+        }
+    }
+    // dump_strain / dump_curl flags for receivers 0..n-1 (bit 0 strain, bit 1 curl)
+    void set_receiver_dumps(int n, const int32_t *flags) {
+        if (n != (int)recs.size()) throw std::runtime_error("receiver dumps || one flag per receiver");
+        n_strain = n_curl = 0;
+        for (int i = 0; i < n; i++) {
+            if (elems[recs[i].elem].fluid && flags[i])
+                throw std::runtime_error("receiver dumps || strain / curl in a fluid element");
+            recs[i].strain_slot = (flags[i] & 1) ? n_strain++ : -1;
+            recs[i].curl_slot = (flags[i] & 2) ? n_curl++ : -1;
         }
     }
 

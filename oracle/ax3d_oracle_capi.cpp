@@ -202,6 +202,20 @@ int guard(F f) {
             out[i] = (double)d->seis[(size_t)first * nrec * 3 + i];                              \
         return 0;                                                                                \
     }                                                                                            \
+    int P##set_receiver_dumps(void *dv, int32_t n, const int32_t *flags) {                       \
+        return guard([&] {                                                                       \
+            static_cast<P##dom *>(dv)->set_receiver_dumps(n, flags);                             \
+            return 0;                                                                            \
+        });                                                                                      \
+    }                                                                                            \
+    int P##read_strain_curl(void *dv, int32_t which, int32_t first, int32_t n, double *out) {    \
+        auto *d = static_cast<P##dom *>(dv);                                                     \
+        const auto &v = which == 0 ? d->strain_rec : d->curl_rec;                                \
+        size_t row = which == 0 ? (size_t)d->n_strain * 6 : (size_t)d->n_curl * 3;               \
+        if (first < 0 || v.size() < (size_t)(first + n) * row) return AX3D_ERR_ARG;              \
+        for (size_t i = 0; i < (size_t)n * row; i++) out[i] = (double)v[(size_t)first * row + i]; \
+        return 0;                                                                                \
+    }                                                                                            \
     int P##reset(void *d) {                                                                      \
         static_cast<P##dom *>(d)->reset();                                                       \
         return 0;                                                                                \

@@ -235,3 +235,49 @@ def _herm(X, nr):
             full[nr - a] = np.conj(X[a])
     full[0] = X[0].real
     return full
+
+
+@pytest.mark.parametrize("field", ["translation", "rotation", "expansion"])
+def test_oracle_strain_curl_of_analytic_fields(field):
+    """Receivers flagged dump_strain / dump_curl (SolidElement::computeStrain/computeCurl):
+    a rigid translation has no strain and no curl; a rigid rotation about z (u_phi = w s)
+    has no strain and curl 2w z = (-2w sin t, 0, 2w cos t) in (theta, phi, r); u_s = w s
+    has strain w (cos^2 t, 1, sin^2 t, 0, 2 sin t cos t, 0) (shear doubled), curl 0."""
+    spec = synth.annulus_domain(seed=3, n_theta=6, n_r=4, nu=3, n_receivers=8, dumps=True, source=False,
+                                stf_len=4, theta_max=1.0)
+    o = _oracle()(spec, double=True)
+    so, _ = spec.point_offsets()
+    w = 1e-3
+    u = np.zeros(o.nsolid, complex)
+    for p in range(spec.n_points):
+        na = spec.p_nr[p] // 2 + 1
+        blk = np.zeros((na, 3), complex)
+        s_ = spec.p_crds[p][0]
+        if field == "translation":
+            blk[0, 2], blk[1, 0], blk[1, 1] = 0.7 * w, (1 + 0.5j) * w / 2, (-0.5 + 1j) * w / 2
+        elif field == "rotation":
+            blk[0, 1] = w * s_
+        else:
+            blk[0, 0] = w * s_
+        u[so[p]:so[p] + 3 * na] = blk.ravel()
+    o.set("displ", "solid", u)
+    o.record(0)
+    st, cu = o.strain_curl("strain", 0, 1)[0], o.strain_curl("curl", 0, 1)[0]
+    th = np.arctan2(spec.p_crds[:, 0], spec.p_crds[:, 1])
+    i_s = i_c = 0
+    for r in range(len(spec.r_elem)):
+        wts = spec.r_w[r].astype(np.float64)
+        t = th[spec.e_pts[spec.r_elem[r]]]
+        want_s, want_c = np.zeros(6), np.zeros(3)
+        if field == "rotation":
+            want_c = 2 * w * np.array([-(wts * np.sin(t)).sum(), 0.0, (wts * np.cos(t)).sum()])
+        if field == "expansion":
+            want_s = w * np.array([(wts * np.cos(t) ** 2).sum(), wts.sum(), (wts * np.sin(t) ** 2).sum(), 0.0,
+                                   (wts * np.sin(2 * t)).sum(), 0.0])
+        if spec.r_dump[r] & 1:
+            np.testing.assert_allclose(st[i_s], want_s, atol=2e-3 * w)
+            i_s += 1
+        if spec.r_dump[r] & 2:
+            np.testing.assert_allclose(cu[i_c], want_c, atol=2e-3 * w)
+            i_c += 1
+    assert i_s == 4 and i_c == 4

@@ -224,3 +224,21 @@ def test_ocean_load_newmark_matches_oracle(ax3d_lib, ocean):
     so, _ = spec.point_offsets()
     rows = np.concatenate([np.arange(so[p], so[p] + 3 * (spec.p_nr[p] // 2 + 1)) for p in spec.oc_pt])
     assert rel(a[rows], b[rows]) <= TOL
+
+
+@pytest.mark.parametrize("name", ["iso1d_fluid_mixednu", "ti3d_cg4", "aniso3d_full"])
+def test_strain_curl_receivers_match_oracle(ax3d_lib, name):
+    """dump_strain / dump_curl receivers (SolidElement::computeStrain / computeCurl,
+    PointwiseRecorder) recorded every step of a time loop, GPU vs oracle."""
+    n = 12
+    spec, g, o, _ = _pair(name, stf_len=n, n_receivers=9, dumps=True)
+    su, fu = synth.random_fields(spec, seed=9, scale=1e-6)
+    for d in (g, o):
+        d.set("displ", "solid", su)
+        if d.nfluid:
+            d.set("displ", "fluid", fu)
+        d.step(n)
+    for which in ("strain", "curl"):
+        a, b = g.strain_curl(which, 0, n), o.strain_curl(which, 0, n)
+        assert a.shape == b.shape and a.shape[1] > 0
+        assert rel(a, b) <= TOL, (which, rel(a, b))

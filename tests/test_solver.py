@@ -296,3 +296,37 @@ def test_ocean_load_constant(tmp_path_factory):
     (d / "inparam.model").write_text((d / "inparam.model").read_text().replace("constant$4.0", "marsocean"))
     with pytest.raises(ValueError, match="Unknown ocean-load model"):
         solver.Simulation(d).build()
+
+
+def test_station_strain_curl_and_enz(tmp_path_factory):
+    """STATIONS keywords dump_strain / dump_curl (ReceiverCollection.cpp:58-72) flag the
+    receivers; their strain (RTZ) and curl land in the synthetics file as NET.NAME.RTZ.strain
+    and .RTZ.curl; ENZ rotates displacement by the back azimuth (PointwiseRecorder.cpp:80-88)."""
+    from oracle.oracle_py import OracleDomain
+    d = tmp_path_factory.mktemp("sc") / "input"
+    solver.write_inputs(d, mesh_kw=SMALL_MESH, steps=40, hdur=20.0, n_stations=6, seed=4,
+                        station_extra=("dump_strain", "dump_curl", "dump_strain dump_curl", "", "bogus"),
+                        components="ENZ")
+    (d / "STATIONS").write_text((d / "STATIONS").read_text() + "BAD LINE\nX1 SY notanumber 0 0 0\n")
+    sim = solver.Simulation(d, output_dir=d.parent / "output")
+    spec = sim.build()
+    assert spec.r_dump.tolist() == [1, 2, 3, 0, 0, 1] and len(spec.r_elem) == 6
+    assert all(0.0 <= b < 2 * np.pi for b in sim.baz)
+    o = OracleDomain(spec)
+    o.step(40)
+    seis = o.seismograms(0, 40)
+    enz = sim.rotate(seis)
+    sim.components = "RTZ"
+    rtz = sim.rotate(seis)
+    sim.components = "ENZ"
+    # ENZ is a rotation of (T, phi) about the vertical: horizontal norm and Z unchanged
+    np.testing.assert_allclose(np.hypot(enz[..., 0], enz[..., 1]), np.hypot(rtz[..., 0], rtz[..., 1]), rtol=1e-9,
+                               atol=1e-30)
+    np.testing.assert_allclose(enz[..., 2], rtz[..., 2])
+    st, cu = o.strain_curl("strain", 0, 40), o.strain_curl("curl", 0, 40)
+    assert st.shape == (40, 3, 6) and cu.shape == (40, 2, 3) and np.abs(st).max() > 0
+    p = sim.write_netcdf(enz, strain=st, curl=sim.rotate_curl(cu))
+    ds = NC.read(p)
+    np.testing.assert_allclose(ds["SY.S000.RTZ.strain"], st[:, 0].astype(np.float32))
+    np.testing.assert_allclose(ds["SY.S005.RTZ.strain"], st[:, 2].astype(np.float32))
+    assert ds["SY.S002.RTZ.curl"].shape == (40, 3) and "SY.S003.RTZ.curl" not in ds.variables
