@@ -254,11 +254,9 @@ class Simulation:
         mat = {k: np.einsum("epqk,ek->epq", shp, v).reshape(E, 25) for k, v in ex.nodal.items()}
         vp, vs, rho = mat["VP"], mat["VS"], mat["RHO"]
         fl = ex.fluid
-        # Nr field: NU_TYPE constant (ConstNrField) with Quad::formNrField's axis limit
-        nutype = par.get("NU_TYPE")
-        if nutype.lower() != "constant":
-            raise NotImplementedError("NU_TYPE: only 'constant' is built")
-        nr0 = 2 * par.get("NU_CONST", int) + 1
+        # Nr field (NrField::buildInparam, NrField.cpp:20-64) with Quad::formNrField's limits;
+        # point coordinates rounded as formNrField does (offset = min(1e-5, distTol / 1e3))
+        nr0 = self._nr_field(pcrd, nodes)
         if nu_elem is not None:
             # a per-element Nu field (learned or user): point Nu = max over its elements
             pnu = np.zeros(P, np.int64)
@@ -466,7 +464,7 @@ class Simulation:
             e_aofs=aofs, e_attm=(np.concatenate(e_attm) if e_attm else np.zeros(0)).astype(np.float32),
             nsls=nsls, att_alpha=alpha, att_beta=beta, att_gamma=gamma, att_do_kappa=dokappa,
             kahan=kahan, stability_interval=par.get("OPTION_STABILITY_INTERVAL", int),
-            oc_pt=oc_pt, oc_len=oc_len, oc_vals=oc_vals)
+            oc_pt=oc_pt, oc_len=oc_len, oc_vals=oc_vals, p_crds=pcrd)
         self.e_pts, self.crds, self.jac, self.fluid = e_pts, crds, jac, fl
         self._source(spec)
         self._stf(spec)
@@ -476,6 +474,48 @@ class Simulation:
         return spec
 
     # ------------------------------------------------------------------ source
+    def _nr_field(self, pcrd, nodes):
+        """NU_TYPE constant (ConstNrField), empirical (EmpNrField) or wisdom (WisdomNrField,
+        reading NU_WISDOM_REUSE_INPUT from the input directory)."""
+        from . import wisdom as W
+        par = self.par
+        nutype = par.get("NU_TYPE").lower()
+        dn = nodes - np.roll(nodes, -1, axis=2)
+        dist_tol = float(np.hypot(dn[:, 0], dn[:, 1]).min()) / 1000.0
+        off = min(1e-5, dist_tol / 1e3)
+        sz = np.round(pcrd / off) * off
+        self.wisdom_ratio = None
+        if nutype == "constant":
+            return 2 * par.get("NU_CONST", int) + 1
+        if nutype == "empirical":
+            return W.empirical_nr(par, sz[:, 0], sz[:, 1], self.R)
+        if nutype == "wisdom":
+            data = W.read_wisdom(self.input_dir / par.get("NU_WISDOM_REUSE_INPUT"))
+            factor = par.get("NU_WISDOM_REUSE_FACTOR", float)
+            factor = 1.0 if factor <= 1e-10 else factor
+            self.wisdom_ratio = W.compression_ratio(data)
+            return 2 * W._round(W.wisdom_nu(data, sz[:, 0], sz[:, 1]) * factor).astype(np.int64) + 1
+        raise ValueError("NrField::build || Invalid parameter, keyword = NU_TYPE.")
+
+    def learn_parameters(self):
+        """LearnParameters (NuWisdom.cpp:134-150): (interval, cutoff, output path) when
+        NU_WISDOM_LEARN is on, else None."""
+        par = self.par
+        if not _flag(par, "NU_WISDOM_LEARN"):
+            return None
+        eps = min(max(par.get("NU_WISDOM_LEARN_EPSILON", float), 1e-5), 0.1)
+        interval = par.get("NU_WISDOM_LEARN_INTERVAL", int)
+        interval = 5 if interval <= 0 else interval
+        return interval, eps, self.output_dir / par.get("NU_WISDOM_LEARN_OUTPUT")
+
+    def dump_wisdom(self, dom, path=None):
+        """Domain::dumpWisdom (Domain.cpp:404-438): (s, z, learned Nu, Nu) of every point."""
+        from . import wisdom as W
+        lp = self.learn_parameters()
+        path = path or (lp[2] if lp else self.output_dir / "wisdom.nc")
+        nu = dom.get_wisdom()
+        return W.write_wisdom(path, self.spec.p_crds[:, 0], self.spec.p_crds[:, 1], nu, self.spec.p_nr // 2)
+
     def _ocean_load(self, ex, fl, e_pts, crds, side_normal, ms, ms3, p_nr):
         """MODEL_3D_OCEAN_LOAD (OceanLoad3D::buildInparam, OceanLoad3D.cpp:20-52): 'none' or
         'constant$<depth km>' (OceanLoad3D_const, 3 km by default).  Solid elements on the
@@ -809,10 +849,17 @@ class Simulation:
 
     # ------------------------------------------------------------------ run
     def run(self, domain=None, nsteps=None):
+        """Newmark::solve through the library; with NU_WISDOM_LEARN on, learns the wisdom
+        during the loop and writes it to NU_WISDOM_LEARN_OUTPUT afterwards."""
         from .capi import Ax3dDomain
         dom = domain or Ax3dDomain(self.spec)
         n = nsteps or self.nsteps
+        lp = self.learn_parameters()
+        if lp:
+            dom.set_wisdom_learning(lp[0], lp[1])
         dom.step(n)
+        if lp:
+            self.dump_wisdom(dom, lp[2])
         seis = dom.seismograms(0, n)
         return self.rotate(seis), dom
 

@@ -330,3 +330,78 @@ def test_station_strain_curl_and_enz(tmp_path_factory):
     np.testing.assert_allclose(ds["SY.S000.RTZ.strain"], st[:, 0].astype(np.float32))
     np.testing.assert_allclose(ds["SY.S005.RTZ.strain"], st[:, 2].astype(np.float32))
     assert ds["SY.S002.RTZ.curl"].shape == (40, 3) and "SY.S003.RTZ.curl" not in ds.variables
+
+
+def test_wisdom_file_roundtrip_and_lookup(tmp_path):
+    """NuWisdom::writeToFile / readFromFile (three- or four-column variable) and getNu
+    (inverse-distance mean of the four nearest points, exact hits returned as stored)."""
+    from axisem3d_gb300 import wisdom as W
+    s = np.array([0.0, 1.0, 0.0, 1.0, 5.0])
+    z = np.array([0.0, 0.0, 1.0, 1.0, 5.0])
+    W.write_wisdom(tmp_path / "w.nc", s, z, [2, 4, 6, 8, 100], [10, 10, 10, 10, 10])
+    data = W.read_wisdom(tmp_path / "w.nc")
+    assert data.shape == (5, 4) and W.compression_ratio(data) == pytest.approx(120 / 50)
+    assert W.wisdom_nu(data, [1.0], [0.0])[0] == 4                   # exact hit
+    assert W.wisdom_nu(data, [0.5], [0.5])[0] == 5                   # centre of the square: mean 5
+    ds = NC.Dataset()
+    ds.add_dim("a", 2)
+    ds.add_dim("b", 3)
+    ds.add_var("axisem3d_wisdom", ("a", "b"), np.array([[0.0, 0.0, 3.0], [1.0, 0.0, 5.0]]))
+    NC.write(tmp_path / "w3.nc", ds)
+    np.testing.assert_array_equal(W.read_wisdom(tmp_path / "w3.nc")[:, 3], [3, 5])
+    ds.variables.clear()
+    ds.add_dim("c", 2)
+    ds.add_var("axisem3d_wisdom", ("a", "c"), np.zeros((2, 2)))
+    NC.write(tmp_path / "w2.nc", ds)
+    with pytest.raises(ValueError, match="3 or 4 columns"):
+        W.read_wisdom(tmp_path / "w2.nc")
+
+
+def test_empirical_nr_field():
+    """EmpNrField::getNrAtPoint: axis, epicentral-distance and surface scaling, minimum."""
+    from axisem3d_gb300 import wisdom as W
+    vals = {"NU_EMP_REF": "20", "NU_EMP_MIN": "3", "NU_EMP_SCALE_AXIS": "true", "NU_EMP_POW_AXIS": "0.5",
+            "NU_EMP_SCALE_THETA": "true", "NU_EMP_FACTOR_PI": "2.0", "NU_EMP_THETA_START": "90",
+            "NU_EMP_POW_THETA": "1.0", "NU_EMP_SCALE_DEPTH": "true", "NU_EMP_FACTOR_SURF": "3.0",
+            "NU_EMP_DEPTH_START": "100", "NU_EMP_DEPTH_END": "300"}
+    par = solver.Parameters.__new__(solver.Parameters)
+    par.values = {k: [v] for k, v in vals.items()}
+    R = 6371e3
+    r = np.array([R, R - 200e3, R - 1000e3, R - 1000e3, 100.0])
+    th = np.radians([45.0, 45.0, 45.0, 135.0, 45.0])
+    nr = W.empirical_nr(par, r * np.sin(th), r * np.cos(th), R)
+    def want(r_, t_):
+        nu = 20 * np.sqrt(r_ * np.sin(t_) / R)
+        if t_ > np.pi / 2:
+            nu *= 1 + (t_ - np.pi / 2) / (np.pi / 2)
+        d = R - r_
+        if d <= 300e3:
+            nu *= 3.0 if d <= 100e3 else 1 + 2.0 / (100e3 - 300e3) * (d - 300e3)
+        return 2 * max(3, int(np.ceil(nu))) + 1
+    assert nr.tolist() == [want(a, b) for a, b in zip(r, th)]
+
+
+def test_wisdom_learn_then_reuse(tmp_path_factory):
+    """NU_WISDOM_LEARN writes (s, z, learned Nu, Nu) of every point after the loop; a second
+    run with NU_TYPE wisdom reads it back and takes each point's learned Nu."""
+    from oracle.oracle_py import OracleDomain
+    d = tmp_path_factory.mktemp("wl") / "input"
+    solver.write_inputs(d, mesh_kw=SMALL_MESH, nu=6, steps=60, hdur=20.0, n_stations=2, seed=5)
+    (d / "inparam.nu").write_text("NU_TYPE constant\nNU_CONST 6\nNU_WISDOM_LEARN true\nNU_WISDOM_LEARN_EPSILON 1e-3\n"
+                                  "NU_WISDOM_LEARN_INTERVAL 10\nNU_WISDOM_LEARN_OUTPUT wisdom.nc\n")
+    out = d.parent / "output"
+    sim = solver.Simulation(d, output_dir=out)
+    spec = sim.build()
+    sim.run(domain=OracleDomain(spec))
+    from axisem3d_gb300 import wisdom as W
+    data = W.read_wisdom(out / "wisdom.nc")
+    assert data.shape == (spec.n_points, 4) and (data[:, 2] <= data[:, 3]).all() and data[:, 2].min() >= 0
+    (d / "wisdom.nc").write_bytes((out / "wisdom.nc").read_bytes())
+    (d / "inparam.nu").write_text("NU_TYPE wisdom\nNU_WISDOM_REUSE_INPUT wisdom.nc\nNU_WISDOM_REUSE_FACTOR 1.0\n"
+                                  "NU_WISDOM_LEARN false\n")
+    sim2 = solver.Simulation(d, output_dir=out)
+    spec2 = sim2.build()
+    learned = data[:, 2].astype(int)
+    # exact hits: 2 Nu_learned + 1 under the same axis / spacing limit as the first run's Nr
+    np.testing.assert_array_equal(spec2.p_nr, np.minimum(2 * learned + 1, spec.p_nr))
+    assert spec2.p_nr.sum() < spec.p_nr.sum() and sim2.wisdom_ratio == pytest.approx(W.compression_ratio(data))
