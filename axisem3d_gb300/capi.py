@@ -77,6 +77,7 @@ def bind(lib: C.CDLL, prefix: str, field_ctype, extra_double_io: bool = False):
     f("learn_wisdom").argtypes = [C.c_void_p, C.c_float]
     f("get_wisdom").argtypes = [C.c_void_p, P_I32]
     f("add_surface").argtypes = [C.c_void_p, C.c_int32, P_I32, P_I32, C.c_int32]
+    f("set_prt").argtypes = [C.c_void_p, C.c_int32, P_I32, P_I32, C.POINTER(C.c_float)]
     f("set_receiver_dumps").argtypes = [C.c_void_p, C.c_int32, P_I32]
     f("read_strain_curl").argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, field_ctype]
     f("add_ocean_load").argtypes = [C.c_void_p, C.c_int32, P_I32, P_I32, C.POINTER(C.c_float)]
@@ -166,6 +167,9 @@ class _DomainBase:
         if len(spec.r_elem):
             self._ck(self._call("add_receivers", h, len(spec.r_elem), _p(c(spec.r_elem, np.int32), C.c_int32),
                                 _p(c(spec.r_phi, np.float32), C.c_float), _p(c(spec.r_w, np.float32), C.c_float)))
+        if len(spec.prt_elem):
+            self._ck(self._call("set_prt", h, len(spec.prt_elem), _p(c(spec.prt_elem, np.int32), C.c_int32),
+                                _p(c(spec.prt_len, np.int32), C.c_int32), _p(c(spec.prt_x, np.float32), C.c_float)))
         if len(spec.r_dump) and np.any(spec.r_dump):
             self._ck(self._call("set_receiver_dumps", h, len(spec.r_dump), _p(c(spec.r_dump, np.int32), C.c_int32)))
         if len(spec.oc_pt):

@@ -34,6 +34,10 @@ struct ElemTable {
     const int64_t *efofs;   // [E] complex offset into ef (element forces, [l][alpha][ncomp])
     float2 *ef;
     float2 *stiff;          // solid point stiffness, written directly by EF_DIRECT elements
+    const int64_t *prtofs;  // [E] float offset into prtx (particle relabelling X, [4][len][25])
+    const float *prtx;
+    const int64_t *wofs;    // [E] complex offset into w (PRT_3D Fourier strain / stress, [alpha][nc][25])
+    float2 *w;
 };
 
 // Device view of the point table.

@@ -99,6 +99,9 @@ struct ax3d_domain {
     std::vector<int32_t> e_pts, e_flags, e_nr;
     std::vector<float> e_geo, e_trig;
     std::vector<uint8_t> e_hastrig;
+    std::vector<int32_t> e_prtlen;  // particle relabelling: 0 none, 1 PRT_1D, nr PRT_3D
+    std::vector<int64_t> e_prtofs;
+    std::vector<float> e_prtx;
     std::vector<int64_t> e_mofs, e_aofs;
     std::vector<float> e_mod, e_attm;
 
@@ -126,7 +129,12 @@ struct ax3d_domain {
     DevBuf<ax3d::FftPlan> d_plans;
     ax3d::PhysTables X{};
     DevBuf<float2> d_su, d_sv, d_sa, d_ss, d_sku, d_skv, d_fu, d_fv, d_fa, d_fs, d_fku, d_fkv;
-    DevBuf<int2> d_items_s, d_items_f;
+    DevBuf<int2> d_items_s, d_items_f, d_items_p1s, d_items_p1f, d_items_p3s, d_items_p3f;
+    DevBuf<int32_t> d_p3s, d_p3f;
+    DevBuf<int64_t> d_prtofs, d_wofs;
+    DevBuf<float> d_prtx;
+    DevBuf<float2> d_w;
+    int nitems_p1s = 0, nitems_p1f = 0, nitems_p3s = 0, nitems_p3f = 0, n_p3s = 0, n_p3f = 0, nr_p3 = 1;
     std::vector<ax3d::PhysBucket> buckets_s, buckets_f;
     std::vector<DevBuf<int32_t>> bucket_lists;
     DevBuf<int32_t> d_pts3d, d_sf3d;
@@ -363,6 +371,12 @@ struct ax3d_domain {
         std::vector<int2> items_s, items_f;
         std::map<int, std::vector<int32_t>> phys_s, phys_f;  // keyed by bucket id
         std::vector<int32_t> phys3_s, phys3_f;
+        std::vector<int2> items_p1s, items_p1f, items_p3s, items_p3f;
+        std::vector<int32_t> p3s, p3f;
+        std::vector<int64_t> wofs(ne, 0);
+        int64_t wsize = 0;
+        e_prtlen.resize(ne, 0);
+        e_prtofs.resize(ne, 0);
         int nr_max = 1;
         for (int e = 0; e < ne; e++) {
             const int nr = e_nr[e], n = nr / 2 + 1, flags = e_flags[e];
@@ -378,7 +392,16 @@ struct ax3d_domain {
             const int a = ax3d::ef_att(flags), npa = a == AX3D_ATT_CG4 ? 4 : 25;
             memofs[e] = memsize;
             if (a) memsize += (int64_t)(sls.nsls + 1) * 6 * npa * (e3d ? nr : 2 * n);
-            if (e3d) {
+            if (e_prtlen[e] && e3d) {
+                if (nr > 4096) throw Error(AX3D_ERR_ARG, "ax3d_set_prt || PRT_3D elements need nr <= 4096");
+                (fluid ? p3f : p3s).push_back(e);
+                for (int al = 0; al < n; al++) (fluid ? items_p3f : items_p3s).push_back(make_int2(e, al));
+                wofs[e] = wsize;
+                wsize += (int64_t)n * (fluid ? 3 : 9) * 25;
+                nr_p3 = std::max(nr_p3, nr);
+            } else if (e_prtlen[e]) {
+                for (int al = 0; al < n; al++) (fluid ? items_p1f : items_p1s).push_back(make_int2(e, al));
+            } else if (e3d) {
                 (fluid ? phys3_f : phys3_s).push_back(e);
             } else {
                 for (int al = 0; al < n; al++) (fluid ? items_f : items_s).push_back(make_int2(e, al));
@@ -389,7 +412,7 @@ struct ax3d_domain {
         // skips those points
         std::vector<uint8_t> p_gskip(np, 0);
         for (int e = 0; e < ne; e++) {
-            if ((e_flags[e] & ax3d::EF_FLUID) || !(e_flags[e] & ax3d::EF_IN3D)) continue;
+            if ((e_flags[e] & ax3d::EF_FLUID) || !(e_flags[e] & ax3d::EF_IN3D) || e_prtlen[e]) continue;
             bool own = true;
             for (int l = 0; l < 25 && own; l++) {
                 const int p = e_pts[(int64_t)e * 25 + l];
@@ -504,6 +527,23 @@ struct ax3d_domain {
             for (auto *b : {&d_sku, &d_skv}) { b->alloc(std::max<int64_t>(nsolid, 1)); b->zero(st); }
             for (auto *b : {&d_fku, &d_fkv}) { b->alloc(std::max<int64_t>(nfluid, 1)); b->zero(st); }
         }
+        d_items_p1s.upload(items_p1s.empty() ? std::vector<int2>{make_int2(0, 0)} : items_p1s, st);
+        d_items_p1f.upload(items_p1f.empty() ? std::vector<int2>{make_int2(0, 0)} : items_p1f, st);
+        d_items_p3s.upload(items_p3s.empty() ? std::vector<int2>{make_int2(0, 0)} : items_p3s, st);
+        d_items_p3f.upload(items_p3f.empty() ? std::vector<int2>{make_int2(0, 0)} : items_p3f, st);
+        nitems_p1s = (int)items_p1s.size();
+        nitems_p1f = (int)items_p1f.size();
+        nitems_p3s = (int)items_p3s.size();
+        nitems_p3f = (int)items_p3f.size();
+        d_p3s.upload(p3s.empty() ? std::vector<int32_t>{0} : p3s, st);
+        d_p3f.upload(p3f.empty() ? std::vector<int32_t>{0} : p3f, st);
+        n_p3s = (int)p3s.size();
+        n_p3f = (int)p3f.size();
+        d_prtofs.upload(e_prtofs, st);
+        d_prtx.upload(e_prtx.empty() ? std::vector<float>{0.f} : e_prtx, st);
+        d_wofs.upload(wofs, st);
+        d_w.alloc(std::max<int64_t>(wsize, 1));
+        d_w.zero(st);
         d_items_s.upload(items_s, st);
         d_items_f.upload(items_f, st);
         nitems_s = (int)items_s.size();
@@ -573,6 +613,9 @@ struct ax3d_domain {
             n_strain = n_curl = 0;
             for (size_t r = 0; r < r_dump.size(); r++) {
                 if (!r_dump[r]) continue;
+                if (e_prtlen[r_elem[r]])
+                    throw Error(AX3D_ERR_ARG, "ax3d_set_receiver_dumps || strain / curl receivers in relabelled "
+                                              "elements are not supported");
                 if (!e_hastrig[r_elem[r]])  // Receiver.cpp:49-51 forces the RTZ transform
                     throw Error(AX3D_ERR_ARG, "ax3d_set_receiver_dumps || strain / curl receivers need theta tables");
                 list.push_back((int32_t)r);
@@ -637,6 +680,10 @@ struct ax3d_domain {
         T.mem = d_mem.p;
         T.efofs = d_efofs.p;
         T.ef = d_ef.p;
+        T.prtofs = d_prtofs.p;
+        T.prtx = d_prtx.p;
+        T.wofs = d_wofs.p;
+        T.w = d_w.p;
         T.stiff = d_ss.p;
         F.su = d_su.p; F.sv = d_sv.p; F.sa = d_sa.p; F.ss = d_ss.p; F.sku = d_sku.p; F.skv = d_skv.p;
         F.fu = d_fu.p; F.fv = d_fv.p; F.fa = d_fa.p; F.fs = d_fs.p; F.fku = d_fku.p; F.fkv = d_fkv.p;
@@ -674,6 +721,10 @@ struct ax3d_domain {
     void launch_elements(bool overwrite) {
         ax3d::launch_elem_fourier_solid(T, P, F.su, d_items_s.p, nitems_s, sls, stream);
         ax3d::launch_elem_fourier_fluid(T, P, F.fu, d_items_f.p, nitems_f, stream);
+        ax3d::launch_elem_prt1(true, T, P, F.su, d_items_p1s.p, nitems_p1s, sls, stream);
+        ax3d::launch_elem_prt1(false, T, P, F.fu, d_items_p1f.p, nitems_p1f, sls, stream);
+        ax3d::launch_elem_prt3(true, T, P, F.su, d_items_p3s.p, nitems_p3s, d_p3s.p, n_p3s, nr_p3, sls, stream);
+        ax3d::launch_elem_prt3(false, T, P, F.fu, d_items_p3f.p, nitems_p3f, d_p3f.p, n_p3f, nr_p3, sls, stream);
         const int nb = (int)(buckets_s.size() + buckets_f.size());
         if (nb == 0) return;
         if (nb == 1) {
@@ -832,7 +883,8 @@ struct ax3d_domain {
         ax3d::launch_advance(d_tstep.p, stream);
     }
     int n_elem_launches() const {
-        return (nitems_s > 0) + (nitems_f > 0) + (int)buckets_s.size() + (int)buckets_f.size();
+        return (nitems_s > 0) + (nitems_f > 0) + (nitems_p1s > 0) + (nitems_p1f > 0) + 3 * (n_p3s > 0) +
+               3 * (n_p3f > 0) + (int)buckets_s.size() + (int)buckets_f.size();
     }
     int step(int nsteps) {
         need_final();
@@ -1137,6 +1189,36 @@ int ax3d_read_seismograms(ax3d_domain *d, int32_t first, int32_t nsteps, float *
         CK(cudaMemcpyAsync(out, d->d_seis.p + (size_t)first * row, (size_t)nsteps * row * sizeof(float),
                            cudaMemcpyDeviceToHost, d->stream));
         CK(cudaStreamSynchronize(d->stream));
+    });
+}
+
+int ax3d_set_prt(ax3d_domain *d, int32_t n, const int32_t *elem, const int32_t *len, const float *x) {
+    return guard([&] {
+        if (!d || n < 0 || (n && (!elem || !len || !x))) throw Error(AX3D_ERR_ARG, "ax3d_set_prt || bad argument");
+        if (d->finalized) throw Error(AX3D_ERR_STATE, "ax3d_set_prt || domain already finalized");
+        const int ne = (int)d->e_nr.size();
+        d->e_prtlen.resize(ne, 0);
+        d->e_prtofs.resize(ne, 0);
+        for (int i = 0; i < n; i++) {
+            const int e = elem[i];
+            if (e < 0 || e >= ne) throw Error(AX3D_ERR_ARG, "ax3d_set_prt || element out of range");
+            const bool e3d = d->e_flags[e] & ax3d::EF_IN3D, fluid = d->e_flags[e] & ax3d::EF_FLUID;
+            if (len[i] != (e3d ? d->e_nr[e] : 1))
+                throw Error(AX3D_ERR_ARG, fluid ? "FluidElement::FluidElement || Particle Relabelling and Elasticity "
+                                                  "are generated in different spaces."
+                                                : "SolidElement::SolidElement || Particle Relabelling and Elasticity "
+                                                  "are generated in different spaces.");
+            if (!d->e_hastrig[e]) throw Error(AX3D_ERR_ARG, "ax3d_set_prt || relabelled elements need theta tables");
+        }
+        int64_t o = 0;
+        for (int i = 0; i < n; i++) {
+            const int e = elem[i];
+            const int64_t sz = (int64_t)4 * len[i] * 25;
+            d->e_prtlen[e] = len[i];
+            d->e_prtofs[e] = (int64_t)d->e_prtx.size();
+            d->e_prtx.insert(d->e_prtx.end(), x + o, x + o + sz);
+            o += sz;
+        }
     });
 }
 

@@ -196,6 +196,64 @@ __device__ __forceinline__ void quad6_lane(const LaneOps &L, const Geo &g, bool 
     __syncwarp();
 }
 
+// computeQuad9 at one point for order beta (Gradient.cpp:154-212); same scratch use as
+// quad6_lane.  sig9[3c + d] pairs with grad9's u_{c,d}.
+__device__ __forceinline__ void quad9_lane(const LaneOps &L, const Geo &g, bool axial, int beta,
+                                           const float2 sig[9], float2 *q, bool active, float2 f[3]) {
+    const int p = L.i * 5 + L.j;
+    const float b = -(float)beta;
+    if (active) {
+        const float2 g0 = cadd(sig[4], cimul(b, sig[1]));
+        const float2 g1 = csub(cimul(b, sig[4]), sig[1]);
+        const float2 g2 = cimul(b, sig[7]);
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            q[c * 25 + p] = cadd(cscale(g.dzdeta, sig[3 * c]), cscale(g.dsdeta, sig[3 * c + 2]));
+            q[(3 + c) * 25 + p] = cadd(cscale(g.dzdxii, sig[3 * c]), cscale(g.dsdxii, sig[3 * c + 2]));
+        }
+        q[6 * 25 + p] = g0;
+        q[7 * 25 + p] = g1;
+        q[8 * 25 + p] = g2;
+        q[9 * 25 + p] = cscale(g.dzdeta, g0);
+        q[10 * 25 + p] = cscale(g.dzdeta, g1);
+        q[11 * 25 + p] = cscale(g.dzdeta, g2);
+        q[12 * 25 + p] = cscale(g.dzdxii, g0);
+        q[13 * 25 + p] = cscale(g.dzdxii, g1);
+    }
+    __syncwarp();
+    if (active) {
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            float2 acc = make_float2(0.f, 0.f), acc2 = make_float2(0.f, 0.f);
+            const float2 *X = q + c * 25, *Y = q + (3 + c) * 25;
+#pragma unroll
+            for (int k = 0; k < 5; k++) {
+                float2 x = X[k * 5 + L.j];
+                float2 y = Y[L.i * 5 + k];
+                acc.x += L.gxr[k] * x.x;
+                acc.y += L.gxr[k] * x.y;
+                acc2.x += y.x * L.ger[k];
+                acc2.y += y.y * L.ger[k];
+            }
+            f[c] = cadd(cadd(acc, acc2), cscale(g.inv_s, q[(6 + c) * 25 + p]));
+            if (axial) {
+                f[c] = cadd(f[c], cscale(L.gxr[0], q[(9 + c) * 25 + L.j]));
+                if (beta == 1 && L.i == 0 && c < 2) {
+                    float2 h = make_float2(0.f, 0.f);
+#pragma unroll
+                    for (int k = 0; k < 5; k++) {
+                        float2 t = q[(12 + c) * 25 + k];
+                        h.x += t.x * L.ger[k];
+                        h.y += t.y * L.ger[k];
+                    }
+                    f[c] = cadd(f[c], h);
+                }
+            }
+        }
+    }
+    __syncwarp();
+}
+
 // computeGrad (scalar potential) at one point (Gradient.cpp:26-56); su = [25].
 __device__ __forceinline__ void grad1_lane(const LaneOps &L, const Geo &g, bool axial, int alpha,
                                           const float2 *su, float2 eps[3]) {
@@ -277,6 +335,32 @@ __device__ __forceinline__ void spz_rtz9(float2 u[9], float s1, float c1, float 
     u[5] = cadd(cscale(c1, u[5]), cscale(s1, u3));
 }
 
+// CrdTransTIsoSolid::transformRTZ_SPZ of a nine-component tensor (CrdTransTIsoSolid.cpp:68-90)
+__device__ __forceinline__ void rtz_spz9(float2 u[9], float s1, float c1, float s2, float c2) {
+    const float2 sum08 = cadd(u[0], u[8]), dif08 = csub(u[0], u[8]);
+    const float2 sum26 = cadd(u[2], u[6]), dif26 = csub(u[2], u[6]);
+    const float2 u1 = u[1], u3 = u[3];
+    u[0] = cscale(0.5f, cadd(cadd(sum08, cscale(c2, dif08)), cscale(s2, sum26)));
+    u[2] = cscale(0.5f, csub(cadd(dif26, cscale(c2, sum26)), cscale(s2, dif08)));
+    u[6] = csub(u[2], dif26);
+    u[8] = csub(sum08, u[0]);
+    u[1] = cadd(cscale(c1, u1), cscale(s1, u[7]));
+    u[7] = csub(cscale(c1, u[7]), cscale(s1, u1));
+    u[3] = cadd(cscale(c1, u3), cscale(s1, u[5]));
+    u[5] = csub(cscale(c1, u[5]), cscale(s1, u3));
+}
+// CrdTransTIsoFluid::transformSPZ_RTZ / transformRTZ_SPZ (CrdTransTIsoFluid.cpp:14-32)
+__device__ __forceinline__ void spz_rtz3(float2 u[3], float s1, float c1) {
+    const float2 u0 = u[0];
+    u[0] = csub(cscale(c1, u0), cscale(s1, u[2]));
+    u[2] = cadd(cscale(c1, u[2]), cscale(s1, u0));
+}
+__device__ __forceinline__ void rtz_spz3(float2 u[3], float s1, float c1) {
+    const float2 u0 = u[0];
+    u[0] = cadd(cscale(c1, u0), cscale(s1, u[2]));
+    u[2] = csub(cscale(c1, u[2]), cscale(s1, u0));
+}
+
 // Elastic strain -> stress at one point / sample for real (T = float) or complex
 // (T = float2) values.  Isotropic1D.cpp:9-26, TransverselyIsotropic1D.cpp:9-27,
 // Anisotropic1D.cpp:9-54 (3D variants identical per sample).  mod(k) = modulus k.
@@ -323,6 +407,47 @@ __device__ __forceinline__ void elastic(int mat, const T e[6], T s[6], M mod) {
             s[r] = acc;
         }
     }
+}
+
+// Particle relabelling (PRT_1D.cpp, PRT_3D.cpp) at one point / sample, real or complex.
+// x(k) = X component k there.  sph: nine RTZ gradient components; und: six undulated
+// strain components (shear doubled).
+template <typename T, typename XF>
+__device__ __forceinline__ void prt_s2u(const T sph[9], T und[6], XF x) {
+    const float x0 = x(0), x1 = x(1), x2 = x(2), x3 = x(3);
+    und[0] = vadd(vmul(x0, sph[0]), vmul(x1, sph[2]));
+    und[1] = vadd(vmul(x0, sph[4]), vmul(x2, sph[5]));
+    und[2] = vmul(x3, sph[8]);
+    und[3] = vadd(vadd(vmul(x0, sph[7]), vmul(x2, sph[8])), vmul(x3, sph[5]));
+    und[4] = vadd(vadd(vmul(x0, sph[6]), vmul(x1, sph[8])), vmul(x3, sph[2]));
+    und[5] = vadd(vadd(vmul(x0, vadd(sph[3], sph[1])), vmul(x1, sph[5])), vmul(x2, sph[2]));
+}
+template <typename T, typename XF>
+__device__ __forceinline__ void prt_u2s(const T und[6], T sph[9], XF x) {
+    const float x0 = x(0), x1 = x(1), x2 = x(2), x3 = x(3);
+    sph[0] = vmul(x0, und[0]);
+    sph[1] = vmul(x0, und[5]);
+    sph[2] = vadd(vadd(vmul(x1, und[0]), vmul(x3, und[4])), vmul(x2, und[5]));
+    sph[3] = sph[1];
+    sph[4] = vmul(x0, und[1]);
+    sph[5] = vadd(vadd(vmul(x2, und[1]), vmul(x3, und[3])), vmul(x1, und[5]));
+    sph[6] = vmul(x0, und[4]);
+    sph[7] = vmul(x0, und[3]);
+    sph[8] = vadd(vadd(vmul(x3, und[2]), vmul(x2, und[3])), vmul(x1, und[4]));
+}
+template <typename T, typename XF>
+__device__ __forceinline__ void prt_s2u_fluid(T s[3], XF x) {
+    const float x0 = x(0), x1 = x(1), x2 = x(2), x3 = x(3);
+    s[0] = vadd(vmul(x0, s[0]), vmul(x1, s[2]));
+    s[1] = vadd(vmul(x0, s[1]), vmul(x2, s[2]));
+    s[2] = vmul(x3, s[2]);
+}
+template <typename T, typename XF>
+__device__ __forceinline__ void prt_u2s_fluid(T s[3], XF x) {
+    const float x0 = x(0), x1 = x(1), x2 = x(2), x3 = x(3);
+    s[2] = vadd(vadd(vmul(x1, s[0]), vmul(x2, s[1])), vmul(x3, s[2]));
+    s[0] = vmul(x0, s[0]);
+    s[1] = vmul(x0, s[1]);
 }
 
 // SLS memory-variable update at one attenuated point (Attenuation1D_Full.cpp:30-74,

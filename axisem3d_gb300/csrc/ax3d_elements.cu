@@ -245,6 +245,343 @@ __global__ void __launch_bounds__(FW_WARPS * 32)
     }
 }
 
+// ------------------------------------------------------------------------------------
+// Particle relabelling.  PRT_1D elements (1-D material, X per point) stay in Fourier space:
+// warp per (element, order), grad9 -> RTZ -> undulated strain -> stress (+ SLS on the
+// undulated strain) -> back -> SPZ -> quad9 (SolidElement.cpp:404-443); fluids likewise
+// with the three-component gradient (FluidElement.cpp:333-355).  PRT elements always
+// rotate to RTZ (mInTIso = mHasPRT).
+// ------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(FW_WARPS * 32)
+    k_elem_prt1_solid(ElemTable T, PointTable P, const float2 *__restrict__ su, const int2 *__restrict__ items,
+                      int nitems, SLS sls) {
+    __shared__ float2 scr[FW_WARPS][QSCR];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float2 *q = scr[warp];
+    const bool active = lane < NPE;
+    const int p = active ? lane : 0;
+    for (int it = blockIdx.x * FW_WARPS + warp; it < nitems; it += gridDim.x * FW_WARPS) {
+        const int e = items[it].x, a = items[it].y;
+        const int flags = T.flags[e];
+        const bool axial = flags & EF_AXIAL;
+        const int nr = T.nr[e], nu = nr / 2, n = nu + 1, lim = nu - (nr % 2 == 0);
+        const int mat = ef_mat(flags), att = ef_att(flags);
+        LaneOps L;
+        L.init(p, axial);
+        Geo g;
+        g.load(T.geo + (int64_t)e * 125, p);
+        if (active) {
+            float2 u[3];
+            load_solid_u(P, su, T.pts[e * NPE + p], a, u);
+            q[p] = u[0];
+            q[25 + p] = u[1];
+            q[50 + p] = u[2];
+        }
+        __syncwarp();
+        float2 g9[9], s9[9];
+#pragma unroll
+        for (int c = 0; c < 9; c++) g9[c] = s9[c] = make_float2(0.f, 0.f);
+        if (active && a <= lim) grad9_lane(L, g, axial, a, q, g9);
+        __syncwarp();
+        if (active) {
+            const float *tr = T.trig + (int64_t)e * 100;
+            const float s1 = tr[p], c1 = tr[25 + p], s2 = tr[50 + p], c2 = tr[75 + p];
+            spz_rtz9(g9, s1, c1, s2, c2);
+            const float *xp = T.prtx + T.prtofs[e];
+            auto xf = [&](int k) { return xp[k * NPE + p]; };
+            float2 und[6], sig[6];
+            prt_s2u(g9, und, xf);
+            const float *md = T.moduli + T.mofs[e];
+            elastic(mat, und, sig, [&](int k) { return md[k * NPE + p]; });
+            if (att) {
+                const int npa = att == 2 ? 4 : NPE;
+                const int qq = att == 2 ? cg4_index(p) : p;
+                if (qq >= 0) {
+                    float2 *mem = reinterpret_cast<float2 *>(T.mem + T.memofs[e]);
+                    const int64_t sl = (int64_t)n * 6 * npa;
+                    float2 *R = mem + (int64_t)a * 6 * npa + qq;
+                    float2 *SR = R + sls.nsls * sl;
+                    for (int l = 0; l < sls.nsls; l++)
+#pragma unroll
+                        for (int c = 0; c < 6; c++) sig[c] = csub(sig[c], R[l * sl + c * npa]);
+                    const float *am = T.attm + T.aofs[e];
+                    sls_update(sls, R, SR, sl, (int64_t)npa, und, am[qq], am[npa + qq]);
+                }
+            }
+            prt_u2s(sig, s9, xf);
+            rtz_spz9(s9, s1, c1, s2, c2);
+        }
+        float2 f[3];
+        quad9_lane(L, g, axial, a, s9, q, active && a <= lim, f);
+        if (active) {
+            float2 *ef = T.ef + T.efofs[e] + ((int64_t)p * n + a) * 3;
+            const bool on = a <= lim;
+            ef[0] = on ? f[0] : make_float2(0.f, 0.f);
+            ef[1] = on ? f[1] : make_float2(0.f, 0.f);
+            ef[2] = on ? f[2] : make_float2(0.f, 0.f);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(FW_WARPS * 32)
+    k_elem_prt1_fluid(ElemTable T, PointTable P, const float2 *__restrict__ fu, const int2 *__restrict__ items,
+                      int nitems) {
+    __shared__ float2 scr[FW_WARPS][QSCR];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float2 *q = scr[warp];
+    const bool active = lane < NPE;
+    const int p = active ? lane : 0;
+    for (int it = blockIdx.x * FW_WARPS + warp; it < nitems; it += gridDim.x * FW_WARPS) {
+        const int e = items[it].x, a = items[it].y;
+        const bool axial = T.flags[e] & EF_AXIAL;
+        const int nr = T.nr[e], nu = nr / 2, n = nu + 1, lim = nu - (nr % 2 == 0);
+        LaneOps L;
+        L.init(p, axial);
+        Geo g;
+        g.load(T.geo + (int64_t)e * 125, p);
+        if (active) q[p] = load_fluid_u(P, fu, T.pts[e * NPE + p], a);
+        __syncwarp();
+        float2 v[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+        if (active && a <= lim) grad1_lane(L, g, axial, a, q, v);
+        __syncwarp();
+        if (active) {
+            const float *tr = T.trig + (int64_t)e * 100;
+            const float s1 = tr[p], c1 = tr[25 + p];
+            spz_rtz3(v, s1, c1);
+            const float *xp = T.prtx + T.prtofs[e];
+            auto xf = [&](int k) { return xp[k * NPE + p]; };
+            prt_s2u_fluid(v, xf);
+            const float K = T.moduli[T.mofs[e] + p];
+#pragma unroll
+            for (int c = 0; c < 3; c++) v[c] = cscale(K, v[c]);
+            prt_u2s_fluid(v, xf);
+            rtz_spz3(v, s1, c1);
+        }
+        float2 f;
+        quad1_lane(L, g, axial, a, v, q, active && a <= lim, f);
+        if (active) T.ef[T.efofs[e] + (int64_t)p * n + a] = a <= lim ? f : make_float2(0.f, 0.f);
+    }
+}
+
+// PRT_3D elements (3-D material, X per sample): the gradient of every order, rotated to
+// RTZ, goes to a Fourier-space scratch w [alpha][nc][25] (k_prt3_grad); one CTA per
+// (element, point) transforms its nc columns to the nr samples by a direct DFT, relabels,
+// computes the stress (+ SLS) and the relabelled-back stress per sample and transforms
+// back into w (k_prt3_phys, PRT_3D.cpp with FieldFFT's C2R / R2C x 1/nr); the divergence
+// of every order follows (k_prt3_quad).
+template <bool SOLID>
+__global__ void __launch_bounds__(FW_WARPS * 32)
+    k_prt3_grad(ElemTable T, PointTable P, const float2 *__restrict__ u, const int2 *__restrict__ items, int nitems) {
+    constexpr int NC = SOLID ? 9 : 3;
+    __shared__ float2 scr[FW_WARPS][QSCR];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float2 *q = scr[warp];
+    const bool active = lane < NPE;
+    const int p = active ? lane : 0;
+    for (int it = blockIdx.x * FW_WARPS + warp; it < nitems; it += gridDim.x * FW_WARPS) {
+        const int e = items[it].x, a = items[it].y;
+        const bool axial = T.flags[e] & EF_AXIAL;
+        const int nr = T.nr[e], lim = nr / 2 - (nr % 2 == 0);
+        LaneOps L;
+        L.init(p, axial);
+        Geo g;
+        g.load(T.geo + (int64_t)e * 125, p);
+        if (active) {
+            if (SOLID) {
+                float2 uu[3];
+                load_solid_u(P, u, T.pts[e * NPE + p], a, uu);
+                q[p] = uu[0];
+                q[25 + p] = uu[1];
+                q[50 + p] = uu[2];
+            } else {
+                q[p] = load_fluid_u(P, u, T.pts[e * NPE + p], a);
+            }
+        }
+        __syncwarp();
+        float2 v[NC];
+#pragma unroll
+        for (int c = 0; c < NC; c++) v[c] = make_float2(0.f, 0.f);
+        if (active && a <= lim) {
+            const float *tr = T.trig + (int64_t)e * 100;
+            if constexpr (SOLID) {
+                grad9_lane(L, g, axial, a, q, v);
+                spz_rtz9(v, tr[p], tr[25 + p], tr[50 + p], tr[75 + p]);
+            } else {
+                grad1_lane(L, g, axial, a, q, v);
+                spz_rtz3(v, tr[p], tr[25 + p]);
+            }
+        }
+        __syncwarp();
+        if (active) {
+            float2 *w = T.w + T.wofs[e] + (int64_t)a * NC * NPE + p;
+#pragma unroll
+            for (int c = 0; c < NC; c++) w[c * NPE] = v[c];
+        }
+    }
+}
+
+template <bool SOLID>
+__global__ void __launch_bounds__(128) k_prt3_phys(ElemTable T, const int32_t *__restrict__ elems, SLS sls) {
+    constexpr int NC = SOLID ? 9 : 3;
+    extern __shared__ float sm_prt[];
+    const int e = elems[blockIdx.x / NPE], p = blockIdx.x % NPE;
+    const int flags = T.flags[e];
+    const int nr = T.nr[e], n = nr / 2 + 1, lim = nr / 2 - (nr % 2 == 0);
+    float2 *tw = reinterpret_cast<float2 *>(sm_prt);  // (cos, sin)(2 pi m / nr)
+    float *x = sm_prt + 2 * nr;                        // [NC][nr]
+    for (int m = threadIdx.x; m < nr; m += blockDim.x) {
+        float sn, cs;
+        sincospif(2.f * (float)m / (float)nr, &sn, &cs);
+        tw[m] = make_float2(cs, sn);
+    }
+    __syncthreads();
+    float2 *w = T.w + T.wofs[e] + p;
+    // C2R (FFTW convention: unnormalised, Im of order 0 ignored); the Nyquist order is zero
+    for (int t = threadIdx.x; t < NC * nr; t += blockDim.x) {
+        const int c = t / nr, k = t - c * nr;
+        float acc = w[c * NPE].x;
+        int m = 0;
+        for (int a = 1; a <= lim; a++) {
+            m += k;
+            if (m >= nr) m -= nr;
+            const float2 v = w[((int64_t)a * NC + c) * NPE];
+            acc += 2.f * (v.x * tw[m].x - v.y * tw[m].y);
+        }
+        x[c * nr + k] = acc;
+    }
+    __syncthreads();
+    const float *xp = T.prtx + T.prtofs[e];
+    const float *md = T.moduli + T.mofs[e];
+    for (int k = threadIdx.x; k < nr; k += blockDim.x) {
+        auto xf = [&](int m) { return xp[((int64_t)m * nr + k) * NPE + p]; };
+        if constexpr (SOLID) {
+            float s9[9], und[6], sig[6];
+#pragma unroll
+            for (int c = 0; c < 9; c++) s9[c] = x[c * nr + k];
+            prt_s2u(s9, und, xf);
+            elastic(ef_mat(flags), und, sig, [&](int m) { return md[((int64_t)m * nr + k) * NPE + p]; });
+            const int att = ef_att(flags);
+            if (att) {
+                const int npa = att == 2 ? 4 : NPE;
+                const int qq = att == 2 ? cg4_index(p) : p;
+                if (qq >= 0) {
+                    float *mem = T.mem + T.memofs[e];
+                    const int64_t sl = (int64_t)nr * 6 * npa;
+                    float *R = mem + (int64_t)k * 6 * npa + qq;
+                    float *SR = R + sls.nsls * sl;
+                    for (int l = 0; l < sls.nsls; l++)
+#pragma unroll
+                        for (int c = 0; c < 6; c++) sig[c] -= R[l * sl + c * npa];
+                    const float *am = T.attm + T.aofs[e];
+                    sls_update(sls, R, SR, sl, (int64_t)npa, und, am[(int64_t)k * npa + qq],
+                               am[(int64_t)nr * npa + (int64_t)k * npa + qq]);
+                }
+            }
+            prt_u2s(sig, s9, xf);
+#pragma unroll
+            for (int c = 0; c < 9; c++) x[c * nr + k] = s9[c];
+        } else {
+            float v[3] = {x[k], x[nr + k], x[2 * nr + k]};
+            prt_s2u_fluid(v, xf);
+            const float K = md[(int64_t)k * NPE + p];
+#pragma unroll
+            for (int c = 0; c < 3; c++) v[c] *= K;
+            prt_u2s_fluid(v, xf);
+#pragma unroll
+            for (int c = 0; c < 3; c++) x[c * nr + k] = v[c];
+        }
+    }
+    __syncthreads();
+    // R2C x 1/nr, orders 0..nr/2 (the divergence drops the Nyquist order)
+    const float inv = 1.f / (float)nr;
+    for (int t = threadIdx.x; t < NC * n; t += blockDim.x) {
+        const int c = t / n, a = t - c * n;
+        float re = 0.f, im = 0.f;
+        int m = 0;
+        for (int k = 0; k < nr; k++) {
+            const float v = x[c * nr + k];
+            re += v * tw[m].x;
+            im -= v * tw[m].y;
+            m += a;
+            if (m >= nr) m -= nr;
+        }
+        w[((int64_t)a * NC + c) * NPE] = make_float2(re * inv, im * inv);
+    }
+}
+
+template <bool SOLID>
+__global__ void __launch_bounds__(FW_WARPS * 32)
+    k_prt3_quad(ElemTable T, const int2 *__restrict__ items, int nitems) {
+    constexpr int NC = SOLID ? 9 : 3;
+    __shared__ float2 scr[FW_WARPS][QSCR];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float2 *q = scr[warp];
+    const bool active = lane < NPE;
+    const int p = active ? lane : 0;
+    for (int it = blockIdx.x * FW_WARPS + warp; it < nitems; it += gridDim.x * FW_WARPS) {
+        const int e = items[it].x, a = items[it].y;
+        const bool axial = T.flags[e] & EF_AXIAL;
+        const int nr = T.nr[e], n = nr / 2 + 1, lim = nr / 2 - (nr % 2 == 0);
+        LaneOps L;
+        L.init(p, axial);
+        Geo g;
+        g.load(T.geo + (int64_t)e * 125, p);
+        float2 v[NC];
+#pragma unroll
+        for (int c = 0; c < NC; c++) v[c] = make_float2(0.f, 0.f);
+        if (active) {
+            const float2 *w = T.w + T.wofs[e] + (int64_t)a * NC * NPE + p;
+#pragma unroll
+            for (int c = 0; c < NC; c++) v[c] = w[c * NPE];
+            const float *tr = T.trig + (int64_t)e * 100;
+            if constexpr (SOLID) rtz_spz9(v, tr[p], tr[25 + p], tr[50 + p], tr[75 + p]);
+            else rtz_spz3(v, tr[p], tr[25 + p]);
+        }
+        if constexpr (SOLID) {
+            float2 f[3];
+            quad9_lane(L, g, axial, a, v, q, active && a <= lim, f);
+            if (active) {
+                float2 *ef = T.ef + T.efofs[e] + ((int64_t)p * n + a) * 3;
+                const bool on = a <= lim;
+                ef[0] = on ? f[0] : make_float2(0.f, 0.f);
+                ef[1] = on ? f[1] : make_float2(0.f, 0.f);
+                ef[2] = on ? f[2] : make_float2(0.f, 0.f);
+            }
+        } else {
+            float2 f;
+            quad1_lane(L, g, axial, a, v, q, active && a <= lim, f);
+            if (active) T.ef[T.efofs[e] + (int64_t)p * n + a] = a <= lim ? f : make_float2(0.f, 0.f);
+        }
+    }
+}
+
+static int fw_blocks(int nitems) {
+    const int b = (nitems + FW_WARPS - 1) / FW_WARPS;
+    return b > 152 * 16 ? 152 * 16 : b;
+}
+
+void launch_elem_prt1(bool solid, const ElemTable &T, const PointTable &P, const float2 *u, const int2 *items,
+                      int nitems, const SLS &sls, cudaStream_t s) {
+    if (nitems <= 0) return;
+    if (solid) k_elem_prt1_solid<<<fw_blocks(nitems), FW_WARPS * 32, 0, s>>>(T, P, u, items, nitems, sls);
+    else k_elem_prt1_fluid<<<fw_blocks(nitems), FW_WARPS * 32, 0, s>>>(T, P, u, items, nitems);
+}
+
+void launch_elem_prt3(bool solid, const ElemTable &T, const PointTable &P, const float2 *u, const int2 *items,
+                      int nitems, const int32_t *elems, int nelem, int nr_max, const SLS &sls, cudaStream_t s) {
+    if (nitems <= 0 || nelem <= 0) return;
+    const size_t smem = (size_t)(2 + (solid ? 9 : 3)) * nr_max * sizeof(float);
+    if (solid) {
+        k_prt3_grad<true><<<fw_blocks(nitems), FW_WARPS * 32, 0, s>>>(T, P, u, items, nitems);
+        k_prt3_phys<true><<<nelem * NPE, 128, smem, s>>>(T, elems, sls);
+        k_prt3_quad<true><<<fw_blocks(nitems), FW_WARPS * 32, 0, s>>>(T, items, nitems);
+    } else {
+        k_prt3_grad<false><<<fw_blocks(nitems), FW_WARPS * 32, 0, s>>>(T, P, u, items, nitems);
+        k_prt3_phys<false><<<nelem * NPE, 128, smem, s>>>(T, elems, sls);
+        k_prt3_quad<false><<<fw_blocks(nitems), FW_WARPS * 32, 0, s>>>(T, items, nitems);
+    }
+}
+
 void launch_elem_fourier_solid(const ElemTable &T, const PointTable &P, const float2 *su,
                                const int2 *items, int nitems, const SLS &sls, cudaStream_t s) {
     if (nitems <= 0) return;
@@ -260,6 +597,10 @@ void launch_elem_fourier_fluid(const ElemTable &T, const PointTable &P, const fl
     k_elem_fourier_fluid<<<blocks, FW_WARPS * 32, 0, s>>>(T, P, fu, items, nitems);
 }
 
-void init_kernel_attributes() { init_phys_attributes(); }
+void init_kernel_attributes() {
+    init_phys_attributes();
+    cudaFuncSetAttribute(k_prt3_phys<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, PRT3_SMEM_MAX);
+    cudaFuncSetAttribute(k_prt3_phys<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, PRT3_SMEM_MAX);
+}
 
 }  // namespace ax3d

@@ -61,6 +61,10 @@ class DomainSpec:
     r_w: np.ndarray = field(default_factory=lambda: np.zeros((0, 25), np.float32))
     # (s, z) of every point; informational (tests, output), not passed to the library
     p_crds: np.ndarray = field(default_factory=lambda: np.zeros((0, 2)))
+    # particle relabelling (PRT_1D / PRT_3D): elements, length 1 or nr, X [4][len][25] each
+    prt_elem: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    prt_len: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    prt_x: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
     # per receiver: bit 0 dump_strain, bit 1 dump_curl (empty: none)
     r_dump: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
     # whole-surface recorder: edges (element, side 0..3) recorded every sf_interval steps

@@ -130,7 +130,7 @@ def annulus_domain(seed=0, n_theta=4, n_r=3, r_in=3000e3, r_out=6371e3, theta_ma
                    nu_random=False, nu_max=None, fluid_layers=(), mat=MAT_ISO, in3d=False,
                    att=ATT_NONE, nsls=3, mass3d=False, couple3d=False, dt=0.05, source=True,
                    n_receivers=3, stf_len=64, stability_interval=0, kahan=False, fluid3d=False,
-                   perturb=0.04, lucky=False, surface_interval=0, ocean="", dumps=False):
+                   perturb=0.04, lucky=False, surface_interval=0, ocean="", dumps=False, prt=None):
     """Connected spherical-element mesh on an (r, theta) grid.
 
     Element (ir, it) spans radii [rs[ir], rs[ir+1]] and colatitudes [ts[it], ts[it+1]];
@@ -139,7 +139,9 @@ def annulus_domain(seed=0, n_theta=4, n_r=3, r_in=3000e3, r_out=6371e3, theta_ma
     element of the top layer) every surface_interval steps.  ocean = "1d" puts a 3 km
     ocean on the outer surface points (MassOcean1D); "3d" varies its depth with azimuth
     and tilts the surface normal (MassOcean3D).  dumps = True flags the receivers
-    dump_strain / dump_curl in turn (3, 1, 2, 0, ...)."""
+    dump_strain / dump_curl in turn (3, 1, 2, 0, ...).  prt = a (float) relabels every
+    element with X = identity + a * noise (per point; per sample on 3-D elements, PRT_3D);
+    a = 0 gives the identity map."""
     rng = np.random.default_rng(seed)
     rs = np.linspace(r_in, r_out, n_r + 1)
     ts = np.linspace(0.0, theta_max, n_theta + 1)
@@ -342,6 +344,21 @@ def annulus_domain(seed=0, n_theta=4, n_r=3, r_in=3000e3, r_out=6371e3, theta_ma
         att_do_kappa=True, sources=sources, stf=stf, r_elem=r_elem, r_phi=r_phi, r_w=r_w,
         kahan=kahan, stability_interval=stability_interval, **ea)
     spec.p_crds = crds_pt
+    if prt is not None:
+        enr = spec.element_nr()
+        lens = np.where(spec.e_in3d.astype(bool), enr, 1).astype(np.int32)
+        xs = []
+        for e in range(spec.n_elements):
+            L = int(lens[e])
+            ang = 2 * np.pi * np.arange(L) / L
+            base = rng.normal(size=(4, 1, 25)) * (1 + 0.5 * np.cos(ang + rng.uniform(0, 2 * np.pi)))[None, :, None]
+            x = prt * base
+            x[0] += 1.0
+            x[3] += 1.0
+            xs.append(x.ravel())
+        spec.prt_elem = np.arange(spec.n_elements, dtype=np.int32)
+        spec.prt_len = lens
+        spec.prt_x = np.concatenate(xs).astype(np.float32)
     if dumps:
         spec.r_dump = np.array([(3, 1, 2, 0)[i % 4] for i in range(len(r_elem))], np.int32)
     if ocean:

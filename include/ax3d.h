@@ -182,6 +182,15 @@ int ax3d_step(ax3d_domain *d, int32_t nsteps);
 /* Recorded (s, phi, z) displacement [nsteps][nrec][3] for steps first..first+nsteps-1. */
 int ax3d_read_seismograms(ax3d_domain *d, int32_t first, int32_t nsteps, float *out);
 
+/* Particle relabelling (PRT_1D / PRT_3D, core/element/prt; created by
+   Relabelling::createPRT for Quad::releaseSolid / releaseFluid, Quad.cpp:386-420): for n
+   elements, len[i] = 1 (1-D element: X [4][25]) or nr_e (3-D element: X [4][nr_e][25]),
+   X back to back.  The element's strain goes through grad9 (fluid: the potential
+   gradient), RTZ, the relabelling and back (SolidElement.cpp:404-443,
+   FluidElement.cpp:333-355).  A length that does not match the element's space is
+   rejected with the reference's message; theta tables are required.  Before ax3d_finalize. */
+int ax3d_set_prt(ax3d_domain *d, int32_t n, const int32_t *elem, const int32_t *len, const float *x);
+
 /* Strain and curl at receivers (PointwiseRecorder::record, PointwiseRecorder.cpp:96-130;
    SolidElement::computeStrain / computeCurl, SolidElement.cpp:219-345): flags[i] for each
    receiver added so far, bit 0 dump_strain, bit 1 dump_curl (the STATIONS keywords,

@@ -77,6 +77,8 @@ struct Oracle {
         std::vector<Real> attm;  // dkappa, dmu
         std::vector<C> mem1;     // 1D state: (nsls+1) * (nu+1) * 6 * npa (last block = stressR)
         std::vector<Real> mem3;  // 3D state: (nsls+1) * nr * 6 * npa
+        int prt = 0;             // particle relabelling: 0 none, 1 PRT_1D, nr PRT_3D
+        std::vector<Real> X;     // [4][prt][25]
     };
     std::vector<Elem> elems;
 
@@ -396,6 +398,126 @@ struct Oracle {
                         f[c][j] += acc;
                     }
             }
+        }
+    }
+
+    // computeQuad9 (Gradient.cpp:154-212): adjoint of grad9 with -i beta; at beta = 0 the
+    // formulas give the hardcoded branch (order-0 stress is real).
+    void quad9(const Elem &e, int beta, const C sig[9][nPE], C f[3][nPE]) const {
+        const Real(*Gx)[nP] = e.axial ? G_glj : G_gll;
+        const Real(*Ge)[nP] = G_gll;
+        const Real *dsdxii = e.geo[0], *dsdeta = e.geo[1], *dzdxii = e.geo[2], *dzdeta = e.geo[3],
+                   *inv_s = e.geo[4];
+        C ib(0, -(Real)beta);
+        C g[3][nPE], X[3][nPE], Y[3][nPE];
+        for (int p = 0; p < nPE; p++) {
+            g[0][p] = sig[4][p] + ib * sig[1][p];
+            g[1][p] = ib * sig[4][p] - sig[1][p];
+            g[2][p] = ib * sig[7][p];
+            for (int c = 0; c < 3; c++) {
+                X[c][p] = dzdeta[p] * sig[3 * c][p] + dsdeta[p] * sig[3 * c + 2][p];
+                Y[c][p] = dzdxii[p] * sig[3 * c][p] + dsdxii[p] * sig[3 * c + 2][p];
+            }
+        }
+        for (int c = 0; c < 3; c++)
+            for (int i = 0; i < nP; i++)
+                for (int j = 0; j < nP; j++) {
+                    C a(0), b(0);
+                    for (int k = 0; k < nP; k++) {
+                        a += Gx[i][k] * X[c][k * nP + j];
+                        b += Y[c][i * nP + k] * Ge[j][k];
+                    }
+                    f[c][i * nP + j] = a + b + inv_s[i * nP + j] * g[c][i * nP + j];
+                }
+        if (e.axial) {
+            for (int c = 0; c < 3; c++)
+                for (int i = 0; i < nP; i++)
+                    for (int j = 0; j < nP; j++) f[c][i * nP + j] += Gx[i][0] * (dzdeta[j] * g[c][j]);
+            if (beta == 1) {
+                for (int c = 0; c < 2; c++)
+                    for (int j = 0; j < nP; j++) {
+                        C acc(0);
+                        for (int k = 0; k < nP; k++) acc += (dzdxii[k] * g[c][k]) * Ge[j][k];
+                        f[c][j] += acc;
+                    }
+            }
+        }
+    }
+
+    // ================= particle relabelling (PRT_1D.cpp, PRT_3D.cpp) =================
+    // x(k) = X component k at this point (and sample).  sph: nine gradient components in
+    // the RTZ frame; und: six undulated strain components (shear doubled).
+    template <typename T, typename XF>
+    static void prt_s2u(const T sph[9], T und[6], XF x) {
+        und[0] = x(0) * sph[0] + x(1) * sph[2];
+        und[1] = x(0) * sph[4] + x(2) * sph[5];
+        und[2] = x(3) * sph[8];
+        und[3] = x(0) * sph[7] + x(2) * sph[8] + x(3) * sph[5];
+        und[4] = x(0) * sph[6] + x(1) * sph[8] + x(3) * sph[2];
+        und[5] = x(0) * (sph[3] + sph[1]) + x(1) * sph[5] + x(2) * sph[2];
+    }
+    template <typename T, typename XF>
+    static void prt_u2s(const T und[6], T sph[9], XF x) {
+        sph[0] = x(0) * und[0];
+        sph[1] = x(0) * und[5];
+        sph[2] = x(1) * und[0] + x(3) * und[4] + x(2) * und[5];
+        sph[3] = sph[1];
+        sph[4] = x(0) * und[1];
+        sph[5] = x(2) * und[1] + x(3) * und[3] + x(1) * und[5];
+        sph[6] = x(0) * und[4];
+        sph[7] = x(0) * und[3];
+        sph[8] = x(3) * und[2] + x(2) * und[3] + x(1) * und[4];
+    }
+    template <typename T, typename XF>
+    static void prt_s2u_fluid(T s[3], XF x) {
+        s[0] = x(0) * s[0] + x(1) * s[2];
+        s[1] = x(0) * s[1] + x(2) * s[2];
+        s[2] = x(3) * s[2];
+    }
+    template <typename T, typename XF>
+    static void prt_u2s_fluid(T s[3], XF x) {
+        s[2] = x(1) * s[0] + x(2) * s[1] + x(3) * s[2];
+        s[0] = x(0) * s[0];
+        s[1] = x(0) * s[1];
+    }
+    // CrdTransTIsoSolid::transformRTZ_SPZ of a nine-component tensor (CrdTransTIsoSolid.cpp:68-90)
+    void rtz_spz9(const Elem &e, C *u[9], int p) const {
+        Real s1 = e.trig[0][p], c1 = e.trig[1][p], s2 = e.trig[2][p], c2 = e.trig[3][p];
+        C sum08 = *u[0] + *u[8], dif08 = *u[0] - *u[8];
+        C sum26 = *u[2] + *u[6], dif26 = *u[2] - *u[6];
+        C u1 = *u[1], u3 = *u[3];
+        *u[0] = Real(0.5) * (sum08 + c2 * dif08 + s2 * sum26);
+        *u[2] = Real(0.5) * (dif26 + c2 * sum26 - s2 * dif08);
+        *u[6] = *u[2] - dif26;
+        *u[8] = sum08 - *u[0];
+        *u[1] = c1 * u1 + s1 * *u[7];
+        *u[7] = c1 * *u[7] - s1 * u1;
+        *u[3] = c1 * u3 + s1 * *u[5];
+        *u[5] = c1 * *u[5] - s1 * u3;
+    }
+    // CrdTransTIsoFluid (CrdTransTIsoFluid.cpp:14-32): the s and z components of a vector
+    void spz_rtz_fluid(const Elem &e, C u[3], int p, bool back) const {
+        Real s1 = e.trig[0][p], c1 = e.trig[1][p];
+        C u0 = u[0];
+        if (!back) {
+            u[0] = c1 * u0 - s1 * u[2];
+            u[2] = c1 * u[2] + s1 * u0;
+        } else {
+            u[0] = c1 * u0 + s1 * u[2];
+            u[2] = c1 * u[2] - s1 * u0;
+        }
+    }
+    void set_prt(int n, const int32_t *elem, const int32_t *len, const float *x) {
+        int64_t o = 0;
+        for (int i = 0; i < n; i++) {
+            Elem &e = elems.at(elem[i]);
+            if (len[i] != (e.in3d ? e.nr : 1))
+                throw std::runtime_error(std::string(e.fluid ? "FluidElement" : "SolidElement") +
+                                         "::" + (e.fluid ? "FluidElement" : "SolidElement") +
+                                         " || Particle Relabelling and Elasticity are generated in different spaces.");
+            e.prt = len[i];
+            e.X.assign(x + o, x + o + 4 * (int64_t)len[i] * nPE);
+            o += 4 * (int64_t)len[i] * nPE;
         }
     }
 
@@ -765,6 +887,177 @@ struct Oracle {
         }
     }
 
+    // SolidElement::displToStiff with PRT (SolidElement.cpp:404-443): grad9 -> RTZ -> [FFT]
+    // -> undulated strain -> stress (+ SLS on the undulated strain) -> back -> [FFT] -> SPZ
+    // -> quad9.  PRT_1D in Fourier space, PRT_3D per sample.
+    void solid_stiff_prt(Elem &e, const std::vector<C> &u, std::vector<C> &force) {
+        const int n = e.nu + 1;
+        const int lim = e.nu - e.nyq;
+        const int npa = e.att == 2 ? 4 : nPE;
+        std::vector<std::array<std::array<C, nPE>, 9>> sph(n), out(n);
+        for (int a = 0; a < n; a++) {
+            C ua[3][nPE], g9[9][nPE];
+            for (int p = 0; p < nPE; p++)
+                for (int c = 0; c < 3; c++) ua[c][p] = solid_u_elem(u, pts[e.pts[p]], a, c);
+            if (a <= lim) {
+                grad9(e, a, ua, g9);
+            } else {
+                for (int c = 0; c < 9; c++)
+                    for (int p = 0; p < nPE; p++) g9[c][p] = C(0);
+            }
+            for (int p = 0; p < nPE; p++) {
+                C *pp[9];
+                for (int c = 0; c < 9; c++) pp[c] = &g9[c][p];
+                spz_rtz9(e, pp, p);
+                for (int c = 0; c < 9; c++) sph[a][c][p] = g9[c][p];
+            }
+        }
+        const Real *md = e.mod.data();
+        if (!e.in3d) {
+            for (int a = 0; a < n; a++)
+                for (int p = 0; p < nPE; p++) {
+                    C s9[9], und[6], sig[6];
+                    for (int c = 0; c < 9; c++) s9[c] = sph[a][c][p];
+                    auto xf = [&](int k) { return e.X[(size_t)k * nPE + p]; };
+                    prt_s2u(s9, und, xf);
+                    elastic(e.mat, und, sig, [&](int k) { return md[k * nPE + p]; });
+                    if (e.att) {
+                        int q = e.att == 2 ? cg4_index(p) : p;
+                        if (q >= 0) {
+                            const int64_t sl = (int64_t)n * 6 * npa;
+                            C *R = &e.mem1[(int64_t)a * 6 * npa + q];
+                            C *SR = R + (int64_t)nsls * sl;
+                            for (int l = 0; l < nsls; l++)
+                                for (int c = 0; c < 6; c++) sig[c] -= R[l * sl + c * npa];
+                            sls_update(R, SR, (int)sl, npa, und, e.attm[q], e.attm[npa + q]);
+                        }
+                    }
+                    prt_u2s(sig, s9, xf);
+                    for (int c = 0; c < 9; c++) out[a][c][p] = s9[c];
+                }
+        } else {
+            const int nr = e.nr;
+            std::vector<Real> sR((size_t)9 * nPE * nr), tR((size_t)9 * nPE * nr);
+            std::vector<C> col(n);
+            for (int c = 0; c < 9; c++)
+                for (int p = 0; p < nPE; p++) {
+                    for (int a = 0; a < n; a++) col[a] = sph[a][c][p];
+                    c2r(col.data(), nr, &sR[((size_t)c * nPE + p) * nr]);
+                }
+            for (int k = 0; k < nr; k++)
+                for (int p = 0; p < nPE; p++) {
+                    Real s9[9], und[6], sig[6];
+                    for (int c = 0; c < 9; c++) s9[c] = sR[((size_t)c * nPE + p) * nr + k];
+                    auto xf = [&](int m) { return e.X[((size_t)m * nr + k) * nPE + p]; };
+                    prt_s2u(s9, und, xf);
+                    elastic(e.mat, und, sig, [&](int m) { return md[((int64_t)m * nr + k) * nPE + p]; });
+                    if (e.att) {
+                        int q = e.att == 2 ? cg4_index(p) : p;
+                        if (q >= 0) {
+                            const int64_t sl = (int64_t)nr * 6 * npa;
+                            Real *R = &e.mem3[(int64_t)k * 6 * npa + q];
+                            Real *SR = R + (int64_t)nsls * sl;
+                            for (int l = 0; l < nsls; l++)
+                                for (int c = 0; c < 6; c++) sig[c] -= R[l * sl + c * npa];
+                            Real dk = e.attm[(int64_t)k * npa + q];
+                            Real dm = e.attm[(int64_t)nr * npa + (int64_t)k * npa + q];
+                            sls_update(R, SR, (int)sl, npa, und, dk, dm);
+                        }
+                    }
+                    prt_u2s(sig, s9, xf);
+                    for (int c = 0; c < 9; c++) tR[((size_t)c * nPE + p) * nr + k] = s9[c];
+                }
+            for (int c = 0; c < 9; c++)
+                for (int p = 0; p < nPE; p++) {
+                    r2c(&tR[((size_t)c * nPE + p) * nr], nr, col.data());
+                    for (int a = 0; a < n; a++) out[a][c][p] = col[a];
+                }
+        }
+        force.assign((size_t)n * 3 * nPE, C(0));
+        for (int a = 0; a <= lim; a++) {
+            C sig[9][nPE];
+            for (int p = 0; p < nPE; p++) {
+                C *pp[9];
+                for (int c = 0; c < 9; c++) {
+                    sig[c][p] = out[a][c][p];
+                    pp[c] = &sig[c][p];
+                }
+                rtz_spz9(e, pp, p);
+            }
+            C f[3][nPE];
+            quad9(e, a, sig, f);
+            for (int c = 0; c < 3; c++)
+                for (int p = 0; p < nPE; p++) force[((size_t)a * 3 + c) * nPE + p] = f[c][p];
+        }
+    }
+
+    // FluidElement::displToStiff with PRT (FluidElement.cpp:333-355): the gradient goes to
+    // RTZ, is relabelled, scaled, relabelled back and returned to SPZ.
+    void fluid_stiff_prt(Elem &e, const std::vector<C> &u, std::vector<C> &force) {
+        const int n = e.nu + 1;
+        const int lim = e.nu - e.nyq;
+        std::vector<std::array<std::array<C, nPE>, 3>> st(n);
+        for (int a = 0; a < n; a++) {
+            C ua[nPE], eps[3][nPE];
+            for (int p = 0; p < nPE; p++) ua[p] = fluid_u_elem(u, pts[e.pts[p]], a);
+            if (a <= lim)
+                grad1(e, a, ua, eps);
+            else
+                for (int c = 0; c < 3; c++)
+                    for (int p = 0; p < nPE; p++) eps[c][p] = C(0);
+            for (int p = 0; p < nPE; p++) {
+                C v[3] = {eps[0][p], eps[1][p], eps[2][p]};
+                spz_rtz_fluid(e, v, p, false);
+                for (int c = 0; c < 3; c++) st[a][c][p] = v[c];
+            }
+        }
+        if (!e.in3d) {
+            for (int a = 0; a < n; a++)
+                for (int p = 0; p < nPE; p++) {
+                    C v[3] = {st[a][0][p], st[a][1][p], st[a][2][p]};
+                    auto xf = [&](int k) { return e.X[(size_t)k * nPE + p]; };
+                    prt_s2u_fluid(v, xf);
+                    for (int c = 0; c < 3; c++) v[c] = e.mod[p] * v[c];
+                    prt_u2s_fluid(v, xf);
+                    for (int c = 0; c < 3; c++) st[a][c][p] = v[c];
+                }
+        } else {
+            const int nr = e.nr;
+            std::vector<Real> x((size_t)3 * nr);
+            std::vector<C> col(n);
+            for (int p = 0; p < nPE; p++) {
+                for (int c = 0; c < 3; c++) {
+                    for (int a = 0; a < n; a++) col[a] = st[a][c][p];
+                    c2r(col.data(), nr, &x[(size_t)c * nr]);
+                }
+                for (int k = 0; k < nr; k++) {
+                    Real v[3] = {x[k], x[nr + k], x[2 * nr + k]};
+                    auto xf = [&](int m) { return e.X[((size_t)m * nr + k) * nPE + p]; };
+                    prt_s2u_fluid(v, xf);
+                    for (int c = 0; c < 3; c++) v[c] = e.mod[(int64_t)k * nPE + p] * v[c];
+                    prt_u2s_fluid(v, xf);
+                    for (int c = 0; c < 3; c++) x[(size_t)c * nr + k] = v[c];
+                }
+                for (int c = 0; c < 3; c++) {
+                    r2c(&x[(size_t)c * nr], nr, col.data());
+                    for (int a = 0; a < n; a++) st[a][c][p] = col[a];
+                }
+            }
+        }
+        force.assign((size_t)n * nPE, C(0));
+        for (int a = 0; a <= lim; a++) {
+            C sig[3][nPE];
+            for (int p = 0; p < nPE; p++) {
+                C v[3] = {st[a][0][p], st[a][1][p], st[a][2][p]};
+                spz_rtz_fluid(e, v, p, true);
+                for (int c = 0; c < 3; c++) sig[c][p] = v[c];
+            }
+            C f[nPE];
+            quad1(e, a, sig, f);
+            for (int p = 0; p < nPE; p++) force[(size_t)a * nPE + p] = f[p];
+        }
+    }
+
     // FluidElement::computeStiff + displToStiff (FluidElement.cpp:43-65, 333-355), no PRT.
     // Acoustic1D.cpp:8-16, Acoustic3D.cpp:9-16.  Returns [alpha][25].
     void fluid_stiff(Elem &e, const std::vector<C> &u, std::vector<C> &force) {
@@ -816,7 +1109,8 @@ struct Oracle {
         std::vector<C> force;
         for (auto &e : elems) {
             if (e.fluid) {
-                fluid_stiff(e, fu, force);
+                if (e.prt) fluid_stiff_prt(e, fu, force);
+                else fluid_stiff(e, fu, force);
                 for (int p = 0; p < nPE; p++) {
                     const Point &pt = pts[e.pts[p]];
                     int lim = pt.nu - (pt.nr % 2 == 0);
@@ -824,7 +1118,8 @@ struct Oracle {
                     if (pt.nr % 2 == 0) fs[pt.fofs + pt.nu] = C(0);
                 }
             } else {
-                solid_stiff(e, su, force);
+                if (e.prt) solid_stiff_prt(e, su, force);
+                else solid_stiff(e, su, force);
                 for (int p = 0; p < nPE; p++) {
                     const Point &pt = pts[e.pts[p]];
                     int lim = pt.nu - (pt.nr % 2 == 0);
@@ -1118,6 +1413,8 @@ struct Oracle {
         for (int i = 0; i < n; i++) {
             if (elems[recs[i].elem].fluid && flags[i])
                 throw std::runtime_error("receiver dumps || strain / curl in a fluid element");
+            if (elems[recs[i].elem].prt && flags[i])
+                throw std::runtime_error("receiver dumps || strain / curl receivers in relabelled elements are not supported");
             recs[i].strain_slot = (flags[i] & 1) ? n_strain++ : -1;
             recs[i].curl_slot = (flags[i] & 2) ? n_curl++ : -1;
         }

@@ -202,6 +202,12 @@ int guard(F f) {
             out[i] = (double)d->seis[(size_t)first * nrec * 3 + i];                              \
         return 0;                                                                                \
     }                                                                                            \
+    int P##set_prt(void *dv, int32_t n, const int32_t *elem, const int32_t *len, const float *x) { \
+        return guard([&] {                                                                       \
+            static_cast<P##dom *>(dv)->set_prt(n, elem, len, x);                                 \
+            return 0;                                                                            \
+        });                                                                                      \
+    }                                                                                            \
     int P##set_receiver_dumps(void *dv, int32_t n, const int32_t *flags) {                       \
         return guard([&] {                                                                       \
             static_cast<P##dom *>(dv)->set_receiver_dumps(n, flags);                             \

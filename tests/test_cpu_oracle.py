@@ -281,3 +281,41 @@ def test_oracle_strain_curl_of_analytic_fields(field):
             np.testing.assert_allclose(cu[i_c], want_c, atol=2e-3 * w)
             i_c += 1
     assert i_s == 4 and i_c == 4
+
+
+@pytest.mark.parametrize("kw", [dict(), dict(mat=MAT_TISO, att=ATT_FULL, nu=3),
+                                dict(in3d=True, mat=MAT_TISO, att=ATT_CG4, nu=4),
+                                dict(in3d=True, mat=MAT_ANISO, att=ATT_FULL, nu=3),
+                                dict(fluid_layers=(0,), nu_random=True, nu_max=5),
+                                dict(fluid_layers=(1,), in3d=True, fluid3d=True, nu=4)],
+                         ids=["iso1d", "ti1d_full", "ti3d_cg4", "aniso3d_full", "fluid1d", "fluid3d"])
+def test_oracle_identity_relabelling_is_no_relabelling(kw):
+    """PRT with X = (1, 0, 0, 1) maps the nine-component gradient onto the ordinary strain and
+    the stress back onto the symmetric divergence: the stiffness (and, through two passes,
+    the memory variables) equal the run without relabelling.  Isotropic elements go through
+    the RTZ rotation only with relabelling, so they agree to the float theta tables."""
+    out = []
+    for prt in (None, 0.0):
+        spec = synth.annulus_domain(prt=prt, **kw)
+        o = _oracle()(spec, double=True)
+        su, fu = synth.random_fields(spec, seed=3)
+        o.set("displ", "solid", su)
+        if o.nfluid:
+            o.set("displ", "fluid", fu)
+        o.compute_stiff()
+        o.compute_stiff()
+        out.append([o.get("stiff", "solid")] + ([o.get("stiff", "fluid")] if o.nfluid else []))
+    for a, b in zip(*out):
+        assert np.linalg.norm(a - b) <= 1e-7 * np.linalg.norm(b)
+
+
+def test_oracle_relabelling_changes_the_stiffness():
+    """A non-trivial X changes the stiffness (the relabelled path is not bypassed)."""
+    res = []
+    for prt in (0.0, 0.05):
+        spec = synth.annulus_domain(prt=prt, in3d=True, nu=3)
+        o = _oracle()(spec, double=True)
+        o.set("displ", "solid", synth.random_fields(spec, seed=3)[0])
+        o.compute_stiff()
+        res.append(o.get("stiff", "solid"))
+    assert np.linalg.norm(res[1] - res[0]) > 1e-3 * np.linalg.norm(res[0])

@@ -41,6 +41,13 @@ CASES = {
     # ocean load on the outer surface points (MassOcean1D, MassOcean3D)
     "iso1d_ocean1d_mixednu": dict(ocean="1d", nu_random=True, nu_max=6),
     "ti3d_ocean3d_mass3d": dict(in3d=True, mat=MAT_TISO, mass3d=True, ocean="3d", nu_random=True, nu_max=7),
+    # particle relabelling: PRT_1D (Fourier space) and PRT_3D (per sample), solid and fluid
+    "iso1d_prt1d_mixednu": dict(prt=0.05, nu_random=True, nu_max=5),
+    "ti1d_full_prt1d": dict(mat=MAT_TISO, att=ATT_FULL, nu=3, prt=0.05),
+    "fluid1d_prt1d": dict(fluid_layers=(1,), nu=3, prt=0.05),
+    "ti3d_cg4_prt3d": dict(in3d=True, mat=MAT_TISO, att=ATT_CG4, nu=6, prt=0.05),
+    "aniso3d_full_prt3d_mixednu": dict(in3d=True, mat=MAT_ANISO, att=ATT_FULL, nu_random=True, nu_max=7, prt=0.05),
+    "fluid3d_prt3d": dict(fluid_layers=(1,), in3d=True, fluid3d=True, nu=5, prt=0.05),
 }
 # time-loop steps for the cases whose O(nr^2) FP64 oracle transform is slow
 STEPS = {"ti3d_fft260_chunked": 6, "ti3d_cg4_direct131": 10, "iso3d_full_direct391": 4,
