@@ -77,6 +77,9 @@ def bind(lib: C.CDLL, prefix: str, field_ctype, extra_double_io: bool = False):
     f("learn_wisdom").argtypes = [C.c_void_p, C.c_float]
     f("get_wisdom").argtypes = [C.c_void_p, P_I32]
     f("add_surface").argtypes = [C.c_void_p, C.c_int32, P_I32, P_I32, C.c_int32]
+    f("set_field_async").argtypes = [C.c_void_p, C.c_int32, C.c_int32, field_ctype]
+    f("get_field_async").argtypes = [C.c_void_p, C.c_int32, C.c_int32, field_ctype]
+    f("sync_fields").argtypes = [C.c_void_p]
     f("set_prt").argtypes = [C.c_void_p, C.c_int32, P_I32, P_I32, C.POINTER(C.c_float)]
     f("set_receiver_dumps").argtypes = [C.c_void_p, C.c_int32, P_I32]
     f("read_strain_curl").argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, field_ctype]
@@ -241,6 +244,27 @@ class _DomainBase:
             raise ValueError(f"field size {v.size} != {n}")
         buf = v.view(self.field_dtype)
         self._ck(self._call("set_field", self.h, FIELD[which], PHASE[phase], _p(buf, self.field_ctype)))
+
+    def set_async(self, which: str, phase: str, values: np.ndarray):
+        """Queue `values` (keep it alive and unchanged, ideally pinned, until sync_fields) as
+        the field the next step() starts from; at most two queued."""
+        n = self.nsolid if phase == "solid" else self.nfluid
+        if values.dtype != self.complex_dtype or not values.flags.c_contiguous or values.size != n:
+            raise ValueError("set_async needs a contiguous array of the field's dtype and size")
+        self._ck(self._call("set_field_async", self.h, FIELD[which], PHASE[phase],
+                            _p(values.view(self.field_dtype), self.field_ctype)))
+
+    def get_async(self, which: str, phase: str, out: np.ndarray):
+        """Snapshot the field after the steps enqueued so far into `out` (complete after
+        sync_fields)."""
+        n = self.nsolid if phase == "solid" else self.nfluid
+        if out.dtype != self.complex_dtype or not out.flags.c_contiguous or out.size < n:
+            raise ValueError("get_async needs a contiguous array of the field's dtype and size")
+        self._ck(self._call("get_field_async", self.h, FIELD[which], PHASE[phase],
+                            _p(out.view(self.field_dtype), self.field_ctype)))
+
+    def sync_fields(self):
+        self._ck(self._call("sync_fields", self.h))
 
     def strain_curl(self, which: str, first: int, n: int) -> np.ndarray:
         """Strain ([n][strain receivers][6], RTZ) or curl ([n][curl receivers][3]) of steps

@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <deque>
 #include <map>
 #include <stdexcept>
 #include <string>
@@ -223,7 +224,88 @@ struct ax3d_domain {
         marks.clear();
     }
 
+    // ---- asynchronous field transfers: two input staging slots, one output ----
+    struct Queued {
+        int which, phase, slot;
+    };
+    cudaStream_t cp_in = nullptr, cp_out = nullptr;
+    DevBuf<float2> stage_in[2], stage_out;
+    cudaEvent_t ev_in_ready[2] = {}, ev_in_free[2] = {}, ev_out_ready = nullptr, ev_out_free = nullptr;
+    std::deque<Queued> queued;
+    int next_slot = 0;
+
+    void init_async() {
+        if (cp_in) return;
+        CK(cudaStreamCreateWithFlags(&cp_in, cudaStreamNonBlocking));
+        CK(cudaStreamCreateWithFlags(&cp_out, cudaStreamNonBlocking));
+        const int64_t n = std::max<int64_t>(std::max(nsolid, nfluid), 1);
+        for (int k = 0; k < 2; k++) {
+            stage_in[k].alloc(n);
+            CK(cudaEventCreateWithFlags(&ev_in_ready[k], cudaEventDisableTiming));
+            CK(cudaEventCreateWithFlags(&ev_in_free[k], cudaEventDisableTiming));
+            CK(cudaEventRecord(ev_in_free[k], stream));
+        }
+        stage_out.alloc(n);
+        CK(cudaEventCreateWithFlags(&ev_out_ready, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&ev_out_free, cudaEventDisableTiming));
+        CK(cudaEventRecord(ev_out_free, stream));
+    }
+    // host -> staging slot on the input copy stream; consumed by the next step()
+    void set_field_async(int which, int phase, const float *in) {
+        need_final();
+        field(which, phase);  // validates
+        init_async();
+        if (queued.size() >= 2) throw Error(AX3D_ERR_STATE, "ax3d_set_field_async || two inputs already queued");
+        const int slot = next_slot;
+        next_slot ^= 1;
+        CK(cudaStreamWaitEvent(cp_in, ev_in_free[slot], 0));
+        CK(cudaMemcpyAsync(stage_in[slot].p, in, fsize(phase) * sizeof(float2), cudaMemcpyHostToDevice, cp_in));
+        CK(cudaEventRecord(ev_in_ready[slot], cp_in));
+        queued.push_back({which, phase, slot});
+    }
+    // the oldest queued input replaces its field, ordered on the main stream
+    void apply_queued_input() {
+        if (queued.empty()) return;
+        const Queued q = queued.front();
+        queued.pop_front();
+        CK(cudaStreamWaitEvent(stream, ev_in_ready[q.slot], 0));
+        CK(cudaMemcpyAsync(field(q.which, q.phase), stage_in[q.slot].p, fsize(q.phase) * sizeof(float2),
+                           cudaMemcpyDeviceToDevice, stream));
+        CK(cudaEventRecord(ev_in_free[q.slot], stream));
+    }
+    // field -> staging (main stream, so it sees every step enqueued before), then staging ->
+    // host on the output copy stream while later steps run
+    void get_field_async(int which, int phase, float *out) {
+        need_final();
+        float2 *src = field(which, phase);
+        init_async();
+        CK(cudaStreamWaitEvent(stream, ev_out_free, 0));
+        CK(cudaMemcpyAsync(stage_out.p, src, fsize(phase) * sizeof(float2), cudaMemcpyDeviceToDevice, stream));
+        CK(cudaEventRecord(ev_out_ready, stream));
+        CK(cudaStreamWaitEvent(cp_out, ev_out_ready, 0));
+        CK(cudaMemcpyAsync(out, stage_out.p, fsize(phase) * sizeof(float2), cudaMemcpyDeviceToHost, cp_out));
+        CK(cudaEventRecord(ev_out_free, cp_out));
+    }
+    void sync_fields() {
+        if (!cp_in) return;
+        CK(cudaStreamSynchronize(cp_in));
+        CK(cudaStreamSynchronize(cp_out));
+        CK(cudaStreamSynchronize(stream));
+    }
+
     ~ax3d_domain() {
+        if (cp_in) {
+            cudaStreamSynchronize(cp_in);
+            cudaStreamSynchronize(cp_out);
+            for (int k = 0; k < 2; k++) {
+                cudaEventDestroy(ev_in_ready[k]);
+                cudaEventDestroy(ev_in_free[k]);
+            }
+            cudaEventDestroy(ev_out_ready);
+            cudaEventDestroy(ev_out_free);
+            cudaStreamDestroy(cp_in);
+            cudaStreamDestroy(cp_out);
+        }
         for (auto &m : marks) {
             cudaEventDestroy(m.a);
             cudaEventDestroy(m.b);
@@ -896,6 +978,7 @@ struct ax3d_domain {
         if (!r_elem.empty() && tstep - 1 + nsteps > seis_cap) grow_seis(tstep - 1 + nsteps);
         if (!sf_elem.empty() && nsteps > 0 && (tstep - 2 + nsteps) / sf_interval >= sf_cap)
             grow_surf((tstep - 2 + nsteps) / sf_interval + 1);
+        apply_queued_input();
         if (timers || !use_graphs) {
             // phase timers need events between the phases: plain launches
             for (int s = 0; s < nsteps; s++) enqueue_step();
@@ -947,6 +1030,8 @@ struct ax3d_domain {
 
     void reset() {
         need_final();
+        sync_fields();
+        queued.clear();
         for (auto *b : {&d_su, &d_sv, &d_sa, &d_ss, &d_fu, &d_fv, &d_fa, &d_fs, &d_ef}) b->zero(stream);
         if (kahan)
             for (auto *b : {&d_sku, &d_skv, &d_fku, &d_fkv}) b->zero(stream);
@@ -1153,6 +1238,27 @@ int ax3d_set_field(ax3d_domain *d, int32_t which, int32_t phase, const float *in
         float2 *dst = d->field(which, phase);
         CK(cudaMemcpyAsync(dst, in, d->fsize(phase) * sizeof(float2), cudaMemcpyHostToDevice, d->stream));
         CK(cudaStreamSynchronize(d->stream));
+    });
+}
+
+int ax3d_set_field_async(ax3d_domain *d, int32_t which, int32_t phase, const float *in) {
+    return guard([&] {
+        if (!d || !in) throw Error(AX3D_ERR_ARG, "ax3d_set_field_async || null argument");
+        d->set_field_async(which, phase, in);
+    });
+}
+
+int ax3d_get_field_async(ax3d_domain *d, int32_t which, int32_t phase, float *out) {
+    return guard([&] {
+        if (!d || !out) throw Error(AX3D_ERR_ARG, "ax3d_get_field_async || null argument");
+        d->get_field_async(which, phase, out);
+    });
+}
+
+int ax3d_sync_fields(ax3d_domain *d) {
+    return guard([&] {
+        if (!d) throw Error(AX3D_ERR_ARG, "ax3d_sync_fields || null domain");
+        d->sync_fields();
     });
 }
 

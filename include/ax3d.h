@@ -202,6 +202,18 @@ int ax3d_set_receiver_dumps(ax3d_domain *d, int32_t n, const int32_t *flags);
    the order of the flagged receivers. */
 int ax3d_read_strain_curl(ax3d_domain *d, int32_t which, int32_t first, int32_t nsteps, float *out);
 
+/* Asynchronous field transfers for callers that stream one state per step (inputs in,
+   results out) without serialising the copies with the steps.  Host buffers should be
+   pinned and must stay untouched until ax3d_sync_fields.
+   ax3d_set_field_async: copies `in` into one of two device staging slots on a copy stream;
+   each ax3d_step call first replaces the field with the oldest queued input (at most two
+   queued; a third is rejected).  ax3d_get_field_async: snapshots the field on the step
+   stream (after every step enqueued before it) and copies the snapshot to `out` on a second
+   copy stream while later steps run.  ax3d_sync_fields waits for every queued copy. */
+int ax3d_set_field_async(ax3d_domain *d, int32_t which, int32_t phase, const float *in);
+int ax3d_get_field_async(ax3d_domain *d, int32_t which, int32_t phase, float *out);
+int ax3d_sync_fields(ax3d_domain *d);
+
 /* Complex values in one whole-surface record: sum over edges of 15 (Nu_e + 1). */
 int64_t ax3d_surface_record_size(const ax3d_domain *d);
 

@@ -26,6 +26,7 @@
 #include <cstdint>
 #include <stdexcept>
 #include <string>
+#include <deque>
 #include <vector>
 
 namespace axo {
@@ -1480,7 +1481,14 @@ struct Oracle {
     }
 
     // Newmark::solve loop body (Newmark.cpp:47-93).
+    // queued inputs of the asynchronous field API: (field, values); step() applies the
+    // oldest before its first step
+    std::deque<std::pair<std::vector<C> *, std::vector<C>>> queued;
     int step(int nsteps) {
+        if (!queued.empty()) {
+            *queued.front().first = std::move(queued.front().second);
+            queued.pop_front();
+        }
         for (int s = 0; s < nsteps; s++) {
             update_newmark();
             if (!srcs.empty()) apply_source(tstep - 1);

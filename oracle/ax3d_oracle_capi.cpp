@@ -160,6 +160,20 @@ int guard(F f) {
             (*v)[i] = std::complex<REAL>((REAL)in[2 * i], (REAL)in[2 * i + 1]);                  \
         return 0;                                                                                \
     }                                                                                            \
+    int P##set_field_async(void *dv, int32_t which, int32_t phase, const double *in) {           \
+        auto *d = static_cast<P##dom *>(dv);                                                     \
+        auto *v = P##pick(d, which, phase);                                                      \
+        if (!v || d->queued.size() >= 2) return AX3D_ERR_ARG;                                    \
+        std::vector<std::complex<REAL>> c(v->size());                                            \
+        for (size_t i = 0; i < v->size(); i++)                                                   \
+            c[i] = std::complex<REAL>((REAL)in[2 * i], (REAL)in[2 * i + 1]);                     \
+        d->queued.emplace_back(v, std::move(c));                                                 \
+        return 0;                                                                                \
+    }                                                                                            \
+    int P##get_field_async(void *dv, int32_t which, int32_t phase, double *out) {                \
+        return P##get_field(dv, which, phase, out);                                              \
+    }                                                                                            \
+    int P##sync_fields(void *) { return 0; }                                                     \
     int P##update_newmark(void *d) {                                                             \
         return guard([&] {                                                                       \
             static_cast<P##dom *>(d)->update_newmark();                                          \

@@ -319,3 +319,25 @@ def test_oracle_relabelling_changes_the_stiffness():
         o.compute_stiff()
         res.append(o.get("stiff", "solid"))
     assert np.linalg.norm(res[1] - res[0]) > 1e-3 * np.linalg.norm(res[0])
+
+
+def test_oracle_queued_inputs_apply_at_the_next_step():
+    """The oracle's asynchronous field calls mirror the library's: each step() starts from
+    the oldest queued input; a third queued input is refused."""
+    spec = synth.annulus_domain(nu=3, stf_len=6)
+    a, b = _oracle()(spec), _oracle()(spec)
+    x0, x1 = (synth.random_fields(spec, seed=s, scale=1e-6)[0] for s in (1, 2))
+    a.set("displ", "solid", x0)
+    a.step(1)
+    r0 = a.get("displ", "solid")
+    a.set("displ", "solid", x1)
+    a.step(1)
+    r1 = a.get("displ", "solid")
+    b.set_async("displ", "solid", x0.astype(np.complex128))
+    b.set_async("displ", "solid", x1.astype(np.complex128))
+    with pytest.raises(Exception):
+        b.set_async("displ", "solid", x1.astype(np.complex128))
+    b.step(1)
+    np.testing.assert_array_equal(b.get("displ", "solid"), r0)
+    b.step(1)
+    np.testing.assert_array_equal(b.get("displ", "solid"), r1)

@@ -249,3 +249,28 @@ def test_strain_curl_receivers_match_oracle(ax3d_lib, name):
         a, b = g.strain_curl(which, 0, n), o.strain_curl(which, 0, n)
         assert a.shape == b.shape and a.shape[1] > 0
         assert rel(a, b) <= TOL, (which, rel(a, b))
+
+
+def test_streamed_field_transfers_match_synchronous(ax3d_lib):
+    """ax3d_set_field_async / ax3d_get_field_async / ax3d_sync_fields: a loop that queues the
+    next input and reads the last result back while steps run gives, step for step, the
+    results of synchronous set / step / get calls."""
+    from axisem3d_gb300.capi import Ax3dDomain
+    spec = synth.annulus_domain(**CASES["ti3d_cg4"], stf_len=8)
+    a, b = Ax3dDomain(spec), Ax3dDomain(spec)
+    ins = [synth.random_fields(spec, seed=40 + k, scale=1e-6)[0].astype(np.complex64) for k in range(5)]
+    want = []
+    for x in ins:
+        a.set("displ", "solid", x)
+        a.step(1)
+        want.append(a.get("displ", "solid").copy())
+    outs = [np.zeros(b.nsolid, np.complex64) for _ in ins]
+    b.set_async("displ", "solid", ins[0])
+    for k in range(len(ins)):
+        if k + 1 < len(ins):
+            b.set_async("displ", "solid", ins[k + 1])
+        b.step(1)
+        b.get_async("displ", "solid", outs[k])
+    b.sync_fields()
+    for k in range(len(ins)):
+        np.testing.assert_array_equal(outs[k], want[k])
