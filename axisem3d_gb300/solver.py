@@ -216,9 +216,11 @@ class Simulation:
         self.par = Parameters(self.input_dir)
 
     # ------------------------------------------------------------------ build
-    def build(self, kahan=False, nu_elem=None) -> DomainSpec:
+    def build(self, kahan=False, nu_elem=None, preloop="host") -> DomainSpec:
         """Pack the domain.  nu_elem: optional per-element Fourier order (a learned or user
-        Nu field) replacing NU_CONST; each point takes the maximum over its elements."""
+        Nu field) replacing NU_CONST; each point takes the maximum over its elements.
+        preloop = "gpu" computes the solid elements' moduli with ax3d_precompute_elastic
+        (FP64 on the GPU) instead of numpy."""
         par = self.par
         ex = Exodus.read(self.input_dir / par.get("MODEL_1D_EXODUS_MESH_FILE"))
         self.ex = ex
@@ -378,6 +380,9 @@ class Simulation:
             alpha, beta, gamma, _, _ = ATT.att_factors(w, y, fmin, fmax, fref, dt, np.ones(1), np.ones(1), dokappa)
             attk = ATT_CG4 if cg4 else ATT_FULL
         e_mod, e_attm, e_mat, e_att = [], [], [], []
+        gpu_mod = self._moduli_gpu(E, fl, e3d, props3, vp, vs, rho, ifact, mat, attk,
+                                   (w, y, fmin, fmax, fref) if attk != ATT_NONE else None,
+                                   dokappa) if preloop == "gpu" else None
         for e in range(E):
             f = ifact[e]
             # (nr, 25) for 3-D elements, (1, 25) for 1-D ones
@@ -388,6 +393,12 @@ class Simulation:
                 e_attm.append(np.zeros(0))
                 e_mat.append(MAT_ACOUSTIC)
                 e_att.append(ATT_NONE)
+                continue
+            if gpu_mod is not None:
+                e_mod.append(gpu_mod[e][0])
+                e_attm.append(gpu_mod[e][1])
+                e_mat.append(MAT_ISO)
+                e_att.append(attk)
                 continue
             lam = rho_e * (vp_e ** 2 - 2 * vs_e ** 2) * f
             mu = rho_e * vs_e ** 2 * f
@@ -474,6 +485,40 @@ class Simulation:
         return spec
 
     # ------------------------------------------------------------------ source
+    def _moduli_gpu(self, E, fl, e3d, props3, vp, vs, rho, ifact, mat, attk, fit, dokappa):
+        """Isotropic solid moduli of every solid element in one ax3d_precompute_elastic call;
+        returns {element: (moduli [2][rows][25], attenuation moduli)}."""
+        from . import preloop as PL
+        solid = [e for e in range(E) if not fl[e]]
+        rows, model = [], {k: [] for k in ("vpv", "vph", "vsv", "vsh", "eta", "rho", "qkappa", "qmu")}
+        for e in solid:
+            vp_e, vs_e, rho_e = ((props3[e]["VP"], props3[e]["VS"], props3[e]["RHO"]) if e3d[e]
+                                 else (vp[e][None, :], vs[e][None, :], rho[e][None, :]))
+            nr = vp_e.shape[0]
+            rows.append(nr)
+            model["vpv"].append(vp_e)
+            model["vph"].append(vp_e)
+            model["vsv"].append(vs_e)
+            model["vsh"].append(vs_e)
+            model["eta"].append(np.ones((nr, 25)))
+            model["rho"].append(rho_e)
+            if attk != ATT_NONE:
+                model["qkappa"].append(np.broadcast_to(mat["QKAPPA"][e][None, :], (nr, 25)))
+                model["qmu"].append(np.broadcast_to(mat["QMU"][e][None, :], (nr, 25)))
+        if attk == ATT_NONE:
+            model.pop("qkappa")
+            model.pop("qmu")
+        sls = PL.SLSFit(*fit, do_kappa=dokappa) if fit else None
+        mod, att = PL.moduli_gpu(np.array(rows), ifact[solid], model, isotropic=True, att=attk, sls=sls)
+        npa = 4 if attk == ATT_CG4 else 25
+        out, mo, ao = {}, 0, 0
+        for e, nr in zip(solid, rows):
+            na = 2 * nr * npa if attk != ATT_NONE else 0
+            out[e] = (mod[mo:mo + 2 * nr * 25], att[ao:ao + na])
+            mo += 2 * nr * 25
+            ao += na
+        return out
+
     def _nr_field(self, pcrd, nodes):
         """NU_TYPE constant (ConstNrField), empirical (EmpNrField) or wisdom (WisdomNrField,
         reading NU_WISDOM_REUSE_INPUT from the input directory)."""

@@ -191,6 +191,25 @@ int ax3d_read_seismograms(ax3d_domain *d, int32_t first, int32_t nsteps, float *
    rejected with the reference's message; theta tables are required.  Before ax3d_finalize. */
 int ax3d_set_prt(ax3d_domain *d, int32_t n, const int32_t *elem, const int32_t *len, const float *x);
 
+/* Pre-loop on the GPU (FP64): elastic moduli of n_elem elements at once, as
+   Material::createElastic (Material.cpp:280-379) builds them, with the attenuation split
+   of AttBuilder (AttBuilder.cpp:17-129, AttAxiSEM.cpp:14-57) and the CG4 weights of
+   Quad::computeWeightsCG4 (Quad.cpp:438-466).  Stateless: runs on `device`, host buffers in
+   and out.  rows[e] = 1 (1-D element) or nr_e (3-D); ifact [n_elem][25] (FP64); vpv, vph,
+   vsv, vsh, eta, rho and, with attenuation, qkappa, qmu: [sum rows][25], element after
+   element.  isotropic != 0 writes (lambda, mu) = (F, L), else (A, C, F, L, N): moduli
+   [nmod][rows][25] per element, back to back, in the layout ax3d_add_elements takes; att =
+   AX3D_ATT_FULL / AX3D_ATT_CG4 also writes att_moduli [2][rows][npa] per element (dkappa,
+   dmu; npa = 25 or 4) from the SLS fit (w, y over nsls) and f_min, f_max, f_ref.  Errors:
+   ax3d_precompute_last_error. */
+int ax3d_precompute_elastic(int32_t device, int32_t n_elem, const int32_t *rows, const double *ifact,
+                            const float *vpv, const float *vph, const float *vsv, const float *vsh,
+                            const float *eta, const float *rho, const float *qkappa, const float *qmu,
+                            int32_t isotropic, int32_t att, int32_t nsls, const double *w, const double *y,
+                            double f_min, double f_max, double f_ref, int32_t do_kappa, float *moduli,
+                            float *att_moduli);
+size_t ax3d_precompute_last_error(char *buf, size_t n);
+
 /* Strain and curl at receivers (PointwiseRecorder::record, PointwiseRecorder.cpp:96-130;
    SolidElement::computeStrain / computeCurl, SolidElement.cpp:219-345): flags[i] for each
    receiver added so far, bit 0 dump_strain, bit 1 dump_curl (the STATIONS keywords,

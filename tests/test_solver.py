@@ -405,3 +405,42 @@ def test_wisdom_learn_then_reuse(tmp_path_factory):
     # exact hits: 2 Nu_learned + 1 under the same axis / spacing limit as the first run's Nr
     np.testing.assert_array_equal(spec2.p_nr, np.minimum(2 * learned + 1, spec.p_nr))
     assert spec2.p_nr.sum() < spec.p_nr.sum() and sim2.wisdom_ratio == pytest.approx(W.compression_ratio(data))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("attenuation", [False, True])
+def test_gpu_preloop_moduli_match_host(tmp_path_factory, ax3d_lib, attenuation):
+    """ax3d_precompute_elastic (FP64 on the GPU) gives the solver's moduli and attenuation
+    moduli (1-D and 3-D elements, CG4) as the numpy pre-loop does, to float rounding."""
+    d = tmp_path_factory.mktemp("pre") / "input"
+    solver.write_inputs(d, mesh_kw=SMALL_MESH, steps=20, hdur=20.0, n_stations=2, seed=3, nu=4,
+                        models3d=MODELS_3D, attenuation=attenuation)
+    a = solver.Simulation(d).build(preloop="host")
+    b = solver.Simulation(d).build(preloop="gpu")
+    assert a.e_in3d.any() and (a.e_in3d == 0).any()
+    np.testing.assert_allclose(b.e_mod, a.e_mod, rtol=2e-6, atol=0)
+    assert len(a.e_attm) == len(b.e_attm) and (len(a.e_attm) > 0) == attenuation
+    np.testing.assert_allclose(b.e_attm, a.e_attm, rtol=2e-6, atol=1e-30)
+
+
+@pytest.mark.gpu
+def test_gpu_preloop_transversely_isotropic(ax3d_lib):
+    """TI moduli with full and CG4 attenuation, random model values, GPU vs numpy."""
+    from axisem3d_gb300 import preloop as PL
+    from axisem3d_gb300 import attenuation as ATT
+    from axisem3d_gb300.spec import ATT_CG4, ATT_FULL, ATT_NONE
+    rng = np.random.default_rng(2)
+    rows = np.array([1, 7, 1, 13, 5])
+    ifact = rng.uniform(1e9, 5e9, (len(rows), 25))
+    model = {k: [rng.uniform(lo, hi, (r, 25)) for r in rows] for k, lo, hi in
+             (("vpv", 8e3, 9e3), ("vph", 8e3, 9.5e3), ("vsv", 4e3, 5e3), ("vsh", 4e3, 5.2e3), ("eta", 0.9, 1.0),
+              ("rho", 3e3, 4e3), ("qkappa", 1e4, 6e4), ("qmu", 80, 600))}
+    w, y = ATT.fit_sls(3, 1 / 200, 1 / 10)
+    sls = PL.SLSFit(w, y, 1 / 200, 1 / 10, 1.0)
+    for att in (ATT_NONE, ATT_FULL, ATT_CG4):
+        for iso in (False, True):
+            m = dict(model) if att != ATT_NONE else {k: v for k, v in model.items() if k not in ("qkappa", "qmu")}
+            g_mod, g_att = PL.moduli_gpu(rows, ifact, m, isotropic=iso, att=att, sls=sls)
+            h_mod, h_att = PL.moduli_host(rows, ifact, m, isotropic=iso, att=att, sls=sls)
+            np.testing.assert_allclose(g_mod, h_mod, rtol=2e-6)
+            np.testing.assert_allclose(g_att, h_att, rtol=2e-6, atol=1e-30)
