@@ -70,7 +70,9 @@ struct PointTable {
     const int64_t *sg_ref;
     const int32_t *fg_ptr;
     const int64_t *fg_ref;
-    const uint8_t *gskip;   // 1: the point's only element assembles it directly
+    const uint8_t *gskip;   // nonzero: the point's only element assembles it directly (2: and,
+                            // inside ax3d_step, overwrites its stiffness, so the Newmark update
+                            // need not clear it)
     int32_t sgather;        // some solid point needs the gather
     // row -> point maps (a row = one Fourier order of one point)
     int64_t nsrows, nfrows;

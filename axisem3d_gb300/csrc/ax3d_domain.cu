@@ -139,7 +139,7 @@ struct ax3d_domain {
     std::vector<ax3d::PhysBucket> buckets_s, buckets_f;
     std::vector<DevBuf<int32_t>> bucket_lists;
     DevBuf<int32_t> d_pts3d, d_sf3d;
-    int n_pts3d = 0, n_sf3d = 0;
+    int n_pts3d = 0, n_sf3d = 0, n_sf1d = 0;
     DevBuf<int32_t> d_selem, d_snord;
     DevBuf<int64_t> d_sofs_src;
     DevBuf<float2> d_sforce;
@@ -503,7 +503,8 @@ struct ax3d_domain {
             if (!own) continue;
             e_flags[e] |= ax3d::EF_DIRECT;
             if (std::find(s_elem.begin(), s_elem.end(), e) != s_elem.end()) e_flags[e] |= ax3d::EF_SOURCE;
-            for (int l = 0; l < 25; l++) p_gskip[e_pts[(int64_t)e * 25 + l]] = 1;
+            const uint8_t g = (e_flags[e] & ax3d::EF_SOURCE) ? 1 : 2;
+            for (int l = 0; l < 25; l++) p_gskip[e_pts[(int64_t)e * 25 + l]] = g;
         }
         int32_t sgather = 0;
         for (int p = 0; p < np; p++)
@@ -543,6 +544,7 @@ struct ax3d_domain {
         for (int p = 0; p < np; p++) {
             if ((p_mslen[p] > 1) || (p_mflen[p] > 1) || (p_oclen[p] > 1)) pts3d.push_back(p);
             if (p_sflen[p] > 1) sf3d.push_back(p);
+            if (p_kind[p] == AX3D_POINT_SOLID_FLUID && p_sflen[p] == 1) n_sf1d++;
         }
         // sources
         for (size_t s = 0; s < s_elem.size(); s++)
@@ -779,10 +781,10 @@ struct ax3d_domain {
     }
 
     // ================= Domain loop bodies =================
-    void update_newmark() {
+    void update_newmark(bool in_step = false) {
         const double half_dt = 0.5 * dt, half_dt_dt = half_dt * dt;
         ax3d::launch_newmark(P, F, (float)dt, (float)half_dt, (float)half_dt_dt, kahan, d_pts3d.p, n_pts3d,
-                             stream);
+                             in_step, stream);
     }
     // explicit step index for the fine-grained entry points (the step loop reads d_tstep)
     void set_targ(int t) {
@@ -830,7 +832,7 @@ struct ax3d_domain {
         launch_elements(false);
         ax3d::launch_gather(P, T, F, stream);
     }
-    void couple() { ax3d::launch_couple(P, F, d_sf3d.p, n_sf3d, stream); }
+    void couple() { ax3d::launch_couple(P, F, d_sf3d.p, n_sf3d, n_sf1d, stream); }
     void record(int t) {
         if (t < 0) throw Error(AX3D_ERR_ARG, "ax3d_record || negative step");
         if (r_elem.empty() && sf_elem.empty()) return;
@@ -921,7 +923,7 @@ struct ax3d_domain {
     void enqueue_step() {
         const int nrow = (P.nsrows > 0) + (P.nfrows > 0);
         tbegin(AX3D_TIMER_POINTS);
-        update_newmark();
+        update_newmark(true);
         tend(nrow + (n_pts3d > 0));
         if (!s_elem.empty()) {
             tbegin(AX3D_TIMER_SOURCE);
@@ -937,7 +939,7 @@ struct ax3d_domain {
         tend((P.nsrows > 0 && P.sgather) + (P.nfrows > 0));
         tbegin(AX3D_TIMER_COUPLE);
         couple();
-        tend((P.nsrows > 0) + (n_sf3d > 0));
+        tend((P.nsrows > 0 && n_sf1d > 0) + (n_sf3d > 0));
         if (!r_elem.empty()) {
             tbegin(AX3D_TIMER_RECORD);
             ax3d::launch_record(P, T, F.su, d_relem.p, d_rphi.p, d_rw.p, (int)r_elem.size(), d_seis.p, seis_cap,

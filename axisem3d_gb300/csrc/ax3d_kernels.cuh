@@ -71,10 +71,11 @@ void launch_elem_phys(bool solid, const ElemTable &T, const PointTable &P, const
                       const PhysTables &X, const SLS &sls, bool overwrite, cudaStream_t s);
 
 void launch_gather(const PointTable &P, const ElemTable &T, const Fields &F, cudaStream_t s);
-void launch_newmark(const PointTable &P, const Fields &F, float dt, float half_dt,
-                    float half_dt_dt, int kahan, const int32_t *pts3d, int n3d, cudaStream_t s);
-void launch_couple(const PointTable &P, const Fields &F, const int32_t *sf3d, int n3d,
-                   cudaStream_t s);
+// in_step: stiffness rows that direct elements overwrite later in the step are not cleared
+void launch_newmark(const PointTable &P, const Fields &F, float dt, float half_dt, float half_dt_dt, int kahan,
+                    const int32_t *pts3d, int n3d, int in_step, cudaStream_t s);
+// n1d: solid-fluid points with a 1-D coupling (none: the row kernel is not launched)
+void launch_couple(const PointTable &P, const Fields &F, const int32_t *sf3d, int n3d, int n1d, cudaStream_t s);
 void launch_source(const PointTable &P, const ElemTable &T, const Fields &F,
                    const int32_t *src_elem, const int32_t *src_nord, const int64_t *src_ofs,
                    const float2 *src_force, int nsrc, const float *stf, int nstf,

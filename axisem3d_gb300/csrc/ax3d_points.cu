@@ -129,7 +129,8 @@ __device__ __forceinline__ void ocean_accel_row(float2 (&s)[3], const float *__r
 }
 
 // Row-local Newmark (points with a Mass1D or MassOcean1D), SolidPoint::updateNewmark.
-__global__ void k_newmark_solid_rows(PointTable P, Fields F, float dt, float hd, float hdd, int kahan) {
+__global__ void k_newmark_solid_rows(PointTable P, Fields F, float dt, float hd, float hdd, int kahan,
+                                     int in_step) {
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < P.nsrows;
          r += (int64_t)gridDim.x * blockDim.x) {
         const int pt = P.srow_pt[r];
@@ -138,6 +139,7 @@ __global__ void k_newmark_solid_rows(PointTable P, Fields F, float dt, float hd,
         const int a = (int)(r - P.sofs[pt] / 3);
         const int nr = P.nr[pt], nu = nr / 2;
         const bool even = nr % 2 == 0, axial = P.axial[pt];
+        const bool clear = !(in_step && P.gskip[pt] == 2);
         float2 s[3];
         const int64_t o = r * 3;
 #pragma unroll
@@ -164,7 +166,7 @@ __global__ void k_newmark_solid_rows(PointTable P, Fields F, float dt, float hd,
                 F.sku[o + c] = ku;
                 F.skv[o + c] = kv;
             }
-            F.ss[o + c] = make_float2(0.f, 0.f);
+            if (clear) F.ss[o + c] = make_float2(0.f, 0.f);
         }
     }
 }
@@ -337,9 +339,10 @@ __global__ void __launch_bounds__(PT3_THREADS)
 }
 
 void launch_newmark(const PointTable &P, const Fields &F, float dt, float hd, float hdd, int kahan,
-                    const int32_t *pts3d, int n3d, cudaStream_t s) {
+                    const int32_t *pts3d, int n3d, int in_step, cudaStream_t s) {
     if (P.nsrows)
-        k_newmark_solid_rows<<<grid_for(P.nsrows, ROW_THREADS), ROW_THREADS, 0, s>>>(P, F, dt, hd, hdd, kahan);
+        k_newmark_solid_rows<<<grid_for(P.nsrows, ROW_THREADS), ROW_THREADS, 0, s>>>(P, F, dt, hd, hdd, kahan,
+                                                                                  in_step);
     if (P.nfrows)
         k_newmark_fluid_rows<<<grid_for(P.nfrows, ROW_THREADS), ROW_THREADS, 0, s>>>(P, F, dt, hd, hdd, kahan);
     if (n3d > 0)
@@ -405,8 +408,8 @@ __global__ void __launch_bounds__(PT3_THREADS) k_couple_3d(PointTable P, Fields 
     for (int t = threadIdx.x; t < na * 3; t += blockDim.x) F.ss[so + t] = csub(F.ss[so + t], S[t]);
 }
 
-void launch_couple(const PointTable &P, const Fields &F, const int32_t *sf3d, int n3d, cudaStream_t s) {
-    if (P.nsrows) k_couple_1d<<<grid_for(P.nsrows, ROW_THREADS), ROW_THREADS, 0, s>>>(P, F);
+void launch_couple(const PointTable &P, const Fields &F, const int32_t *sf3d, int n3d, int n1d, cudaStream_t s) {
+    if (P.nsrows && n1d > 0) k_couple_1d<<<grid_for(P.nsrows, ROW_THREADS), ROW_THREADS, 0, s>>>(P, F);
     if (n3d > 0) k_couple_3d<<<n3d, PT3_THREADS, 48 * 1024, s>>>(P, F, sf3d);
 }
 
