@@ -168,7 +168,7 @@ struct ax3d_domain {
     float wis_cutoff = 0.f;
     int32_t h_targ = 0;
     bool use_graphs = true;
-    cudaGraphExec_t graph_exec = nullptr;
+    cudaGraphExec_t graph_execs[2] = {};  // one per displacement buffer
 
     ax3d::ElemTable T{};
     ax3d::PointTable P{};
@@ -225,14 +225,24 @@ struct ax3d_domain {
     }
 
     // ---- asynchronous field transfers: two input staging slots, one output ----
+    // The solid displacement is double-buffered instead (buffer su_cur is the field): a queued
+    // displacement is copied straight into the other buffer and step() switches to it, and
+    // reads come straight from the live buffer; one captured graph per buffer.
     struct Queued {
-        int which, phase, slot;
+        int which, phase, slot;  // slot < 0: displacement buffer -1 - slot
     };
     cudaStream_t cp_in = nullptr, cp_out = nullptr;
-    DevBuf<float2> stage_in[2], stage_out;
+    DevBuf<float2> stage_in[2], stage_out, d_su_alt;
     cudaEvent_t ev_in_ready[2] = {}, ev_in_free[2] = {}, ev_out_ready = nullptr, ev_out_free = nullptr;
+    cudaEvent_t ev_su_ready[2] = {}, ev_su_read[2] = {}, ev_main = nullptr;
     std::deque<Queued> queued;
-    int next_slot = 0;
+    int next_slot = 0, su_cur = 0;
+    float2 *su_buf(int k) { return k ? d_su_alt.p : d_su.p; }
+    bool su_async(int which, int phase) const { return which == AX3D_FIELD_DISPL && phase == AX3D_PHASE_SOLID; }
+    // main-stream work that writes the live displacement waits for reads of it in flight
+    void guard_su() {
+        if (cp_in) CK(cudaStreamWaitEvent(stream, ev_su_read[su_cur], 0));
+    }
 
     void init_async() {
         if (cp_in) return;
@@ -249,6 +259,13 @@ struct ax3d_domain {
         CK(cudaEventCreateWithFlags(&ev_out_ready, cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&ev_out_free, cudaEventDisableTiming));
         CK(cudaEventRecord(ev_out_free, stream));
+        d_su_alt.alloc(std::max<int64_t>(nsolid, 1));
+        CK(cudaEventCreateWithFlags(&ev_main, cudaEventDisableTiming));
+        for (int k = 0; k < 2; k++) {
+            CK(cudaEventCreateWithFlags(&ev_su_ready[k], cudaEventDisableTiming));
+            CK(cudaEventCreateWithFlags(&ev_su_read[k], cudaEventDisableTiming));
+            CK(cudaEventRecord(ev_su_read[k], stream));
+        }
     }
     // host -> staging slot on the input copy stream; consumed by the next step()
     void set_field_async(int which, int phase, const float *in) {
@@ -256,6 +273,18 @@ struct ax3d_domain {
         field(which, phase);  // validates
         init_async();
         if (queued.size() >= 2) throw Error(AX3D_ERR_STATE, "ax3d_set_field_async || two inputs already queued");
+        if (su_async(which, phase)) {
+            // the buffer after every queued displacement, flipped
+            int planned = su_cur;
+            for (const Queued &q : queued)
+                if (q.slot < 0) planned = -1 - q.slot;
+            const int target = 1 - planned;
+            CK(cudaStreamWaitEvent(cp_in, ev_su_read[target], 0));
+            CK(cudaMemcpyAsync(su_buf(target), in, nsolid * sizeof(float2), cudaMemcpyHostToDevice, cp_in));
+            CK(cudaEventRecord(ev_su_ready[target], cp_in));
+            queued.push_back({which, phase, -1 - target});
+            return;
+        }
         const int slot = next_slot;
         next_slot ^= 1;
         CK(cudaStreamWaitEvent(cp_in, ev_in_free[slot], 0));
@@ -265,9 +294,20 @@ struct ax3d_domain {
     }
     // the oldest queued input replaces its field, ordered on the main stream
     void apply_queued_input() {
-        if (queued.empty()) return;
+        if (queued.empty()) {
+            guard_su();
+            return;
+        }
         const Queued q = queued.front();
         queued.pop_front();
+        if (q.slot < 0) {
+            su_cur = -1 - q.slot;
+            F.su = su_buf(su_cur);
+            CK(cudaStreamWaitEvent(stream, ev_su_ready[su_cur], 0));
+            guard_su();
+            return;
+        }
+        guard_su();
         CK(cudaStreamWaitEvent(stream, ev_in_ready[q.slot], 0));
         CK(cudaMemcpyAsync(field(q.which, q.phase), stage_in[q.slot].p, fsize(q.phase) * sizeof(float2),
                            cudaMemcpyDeviceToDevice, stream));
@@ -279,6 +319,13 @@ struct ax3d_domain {
         need_final();
         float2 *src = field(which, phase);
         init_async();
+        if (su_async(which, phase)) {
+            CK(cudaEventRecord(ev_main, stream));
+            CK(cudaStreamWaitEvent(cp_out, ev_main, 0));
+            CK(cudaMemcpyAsync(out, src, nsolid * sizeof(float2), cudaMemcpyDeviceToHost, cp_out));
+            CK(cudaEventRecord(ev_su_read[su_cur], cp_out));
+            return;
+        }
         CK(cudaStreamWaitEvent(stream, ev_out_free, 0));
         CK(cudaMemcpyAsync(stage_out.p, src, fsize(phase) * sizeof(float2), cudaMemcpyDeviceToDevice, stream));
         CK(cudaEventRecord(ev_out_ready, stream));
@@ -303,6 +350,11 @@ struct ax3d_domain {
             }
             cudaEventDestroy(ev_out_ready);
             cudaEventDestroy(ev_out_free);
+            cudaEventDestroy(ev_main);
+            for (int k = 0; k < 2; k++) {
+                cudaEventDestroy(ev_su_ready[k]);
+                cudaEventDestroy(ev_su_read[k]);
+            }
             cudaStreamDestroy(cp_in);
             cudaStreamDestroy(cp_out);
         }
@@ -782,6 +834,7 @@ struct ax3d_domain {
 
     // ================= Domain loop bodies =================
     void update_newmark(bool in_step = false) {
+        if (!in_step) guard_su();  // inside a step, apply_queued_input has waited already
         const double half_dt = 0.5 * dt, half_dt_dt = half_dt * dt;
         ax3d::launch_newmark(P, F, (float)dt, (float)half_dt, (float)half_dt_dt, kahan, d_pts3d.p, n_pts3d,
                              in_step, stream);
@@ -915,8 +968,10 @@ struct ax3d_domain {
         return out;
     }
     void drop_graph() {
-        if (graph_exec) cudaGraphExecDestroy(graph_exec);
-        graph_exec = nullptr;
+        for (auto &g : graph_execs) {
+            if (g) cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
     }
     // One time step of Newmark::solve with the step index read on the device (d_tstep),
     // so the same launches serve every step; used directly or captured as a CUDA graph.
@@ -985,6 +1040,7 @@ struct ax3d_domain {
             // phase timers need events between the phases: plain launches
             for (int s = 0; s < nsteps; s++) enqueue_step();
         } else {
+            cudaGraphExec_t &graph_exec = graph_execs[su_cur];
             if (!graph_exec) {
                 cudaGraph_t g = nullptr;
                 CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
@@ -1034,6 +1090,9 @@ struct ax3d_domain {
         need_final();
         sync_fields();
         queued.clear();
+        su_cur = 0;
+        F.su = d_su.p;
+        if (d_su_alt.p) d_su_alt.zero(stream);
         for (auto *b : {&d_su, &d_sv, &d_sa, &d_ss, &d_fu, &d_fv, &d_fa, &d_fs, &d_ef}) b->zero(stream);
         if (kahan)
             for (auto *b : {&d_sku, &d_skv, &d_fku, &d_fkv}) b->zero(stream);
@@ -1238,6 +1297,7 @@ int ax3d_set_field(ax3d_domain *d, int32_t which, int32_t phase, const float *in
         if (!d || !in) throw Error(AX3D_ERR_ARG, "ax3d_set_field || null argument");
         d->need_final();
         float2 *dst = d->field(which, phase);
+        if (d->su_async(which, phase)) d->guard_su();
         CK(cudaMemcpyAsync(dst, in, d->fsize(phase) * sizeof(float2), cudaMemcpyHostToDevice, d->stream));
         CK(cudaStreamSynchronize(d->stream));
     });

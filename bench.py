@@ -11,7 +11,9 @@ needed between steps.
 
 value  = sum_e 25 nr_e x steps / device time (CUDA events on the library's stream).
 e2e    = the same through the C-ABI with host buffers: each step copies the
-         displacement in from pinned host memory, steps, and copies it back.
+         displacement in from pinned host memory, steps, and copies it back, the copies
+         streamed (ax3d_set_field_async / ax3d_get_field_async) so that they overlap the
+         steps; the synchronous form is reported beside it.
 Reference arm (--impl reference): the CPU oracle port of the same loop, one process
 per host core over a static element partition, on a bounded sample.
 """

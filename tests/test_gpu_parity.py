@@ -274,3 +274,15 @@ def test_streamed_field_transfers_match_synchronous(ax3d_lib):
     b.sync_fields()
     for k in range(len(ins)):
         np.testing.assert_array_equal(outs[k], want[k])
+    # the live displacement buffer switched with every queued input: plain calls and plain
+    # steps continue from the last result
+    np.testing.assert_array_equal(b.get("displ", "solid"), want[-1])
+    a.step(2)
+    b.step(2)
+    for which in ("displ", "veloc", "accel"):
+        np.testing.assert_array_equal(b.get(which, "solid"), a.get(which, "solid"))
+    b.reset()
+    a.reset()
+    a.step(1)
+    b.step(1)
+    np.testing.assert_array_equal(b.get("displ", "solid"), a.get("displ", "solid"))
