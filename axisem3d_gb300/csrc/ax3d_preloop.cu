@@ -128,8 +128,10 @@ __global__ void __launch_bounds__(256)
 template <typename T>
 struct Dev {
     T *p = nullptr;
-    ~Dev() {
+    ~Dev() { release(); }
+    void release() {
         if (p) cudaFree(p);
+        p = nullptr;
     }
     cudaError_t up(const T *h, size_t n) {
         cudaError_t e = cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T));
@@ -180,6 +182,8 @@ extern "C" int ax3d_precompute_elastic(int32_t device, int32_t n_elem, const int
         natt += att ? (int64_t)2 * rows[e] * npa : 0;
     }
     const size_t nv = (size_t)nrow * 25;
+    int prev_device = 0;
+    cudaGetDevice(&prev_device);
     cudaError_t err = cudaSetDevice(device);
     Dev<int32_t> d_rows;
     Dev<int64_t> d_rofs, d_mofs, d_aofs;
@@ -204,6 +208,15 @@ extern "C" int ax3d_precompute_elastic(int32_t device, int32_t n_elem, const int
         if (err == cudaSuccess && natt)
             err = cudaMemcpy(att_moduli, d_att.p, natt * sizeof(float), cudaMemcpyDeviceToHost);
     }
+    // the device buffers are freed here, on `device`; then the caller's device is restored
+    for (auto *d : {&d_in[0], &d_in[1], &d_in[2], &d_in[3], &d_in[4], &d_in[5], &d_in[6], &d_in[7], &d_mod, &d_att})
+        d->release();
+    d_rows.release();
+    d_rofs.release();
+    d_mofs.release();
+    d_aofs.release();
+    d_if.release();
+    cudaSetDevice(prev_device);
     if (err != cudaSuccess) {
         g_pre_err = std::string("ax3d_precompute_elastic || CUDA: ") + cudaGetErrorString(err);
         return AX3D_ERR_CUDA;

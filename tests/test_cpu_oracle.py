@@ -341,3 +341,33 @@ def test_oracle_queued_inputs_apply_at_the_next_step():
     np.testing.assert_array_equal(b.get("displ", "solid"), r0)
     b.step(1)
     np.testing.assert_array_equal(b.get("displ", "solid"), r1)
+
+
+def test_oracle_rejects_inconsistent_relabelling_ocean_and_dumps():
+    """The reference's checks, mirrored by the oracle and the library: a PRT whose space does
+    not match the element's (SolidElement::SolidElement), an ocean load on a fluid point or
+    of the wrong length (MassOcean3D::checkCompatibility), strain / curl receivers in
+    relabelled elements (not built)."""
+    from axisem3d_gb300.capi import Ax3dError
+    spec = synth.annulus_domain(prt=0.0, nu=3)
+    spec.prt_len = spec.prt_len.copy()
+    spec.prt_len[0] = 7  # a 1-D element given a 3-D relabelling
+    spec.prt_x = np.ones(int(4 * 25 * spec.prt_len.sum()), np.float32)
+    with pytest.raises(Ax3dError, match="different spaces"):
+        _oracle()(spec)
+    spec = synth.annulus_domain(fluid_layers=(0,), nu=3, ocean="1d")
+    fluid_pt = int(np.flatnonzero(spec.p_kind == 1)[0])
+    spec.oc_pt = np.concatenate([spec.oc_pt, [fluid_pt]]).astype(np.int32)
+    spec.oc_len = np.concatenate([spec.oc_len, [1]]).astype(np.int32)
+    spec.oc_vals = np.concatenate([spec.oc_vals, np.ones(4, np.float32)])
+    with pytest.raises(Ax3dError, match="Fluid point with ocean load"):
+        _oracle()(spec)
+    spec = synth.annulus_domain(nu=3, ocean="1d")
+    spec.oc_len = spec.oc_len.copy()
+    spec.oc_len[0] = 2
+    spec.oc_vals = np.ones(int(4 * spec.oc_len.sum()), np.float32)
+    with pytest.raises(Ax3dError, match="Incompatible size"):
+        _oracle()(spec)
+    spec = synth.annulus_domain(prt=0.02, nu=3, n_receivers=4, dumps=True)
+    with pytest.raises(Ax3dError, match="relabelled elements are not supported"):
+        _oracle()(spec)
