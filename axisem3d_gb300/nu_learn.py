@@ -5,7 +5,7 @@ The reference learns a point-wise Nu field ("wisdom") from the spectra of a full
 and reuses it in later runs of the same model (SolidPoint.cpp:240-272, NuWisdom.cpp:19-86).
 Here a network trained on the wisdom of full-Nu runs of many seeded 3-D models predicts
 each element's Nu from local model features for a model it has not seen, so the reduced
-run needs no full-Nu run first; a full-Nu run remains the judge and the fallback.
+run needs no full-Nu run first; a full-Nu run remains the accuracy reference and the fallback.
 
 Features (16 per element, at the element's centre GLL point):
   0 r / R            1 epicentral distance / pi     2 distance to the axis s / R
@@ -123,7 +123,7 @@ def run(spec, steps, learn=None):
 
 def experiment(work, n_train=64, n_test=16, nu_full=64, steps=600, epochs=200, batch=4096, lr=2e-3,
                eps=1e-3, interval=5, mesh_kw=None, out=None, log=print, train_data=None):
-    """Train on the wisdom of n_train full-Nu runs, judge n_test held-out models.  Returns
+    """Train on the wisdom of n_train full-Nu runs, evaluate on n_test held-out models.  Returns
     the summary dict (also written to out/summary.json with the parameters in out/nu_mlp.npz).
     train_data: an earlier out/train_data.npz to reuse instead of the training runs."""
     from .nu_mlp import NuMLP
