@@ -248,14 +248,11 @@ struct ax3d_domain {
         if (cp_in) return;
         CK(cudaStreamCreateWithFlags(&cp_in, cudaStreamNonBlocking));
         CK(cudaStreamCreateWithFlags(&cp_out, cudaStreamNonBlocking));
-        const int64_t n = std::max<int64_t>(std::max(nsolid, nfluid), 1);
         for (int k = 0; k < 2; k++) {
-            stage_in[k].alloc(n);
             CK(cudaEventCreateWithFlags(&ev_in_ready[k], cudaEventDisableTiming));
             CK(cudaEventCreateWithFlags(&ev_in_free[k], cudaEventDisableTiming));
             CK(cudaEventRecord(ev_in_free[k], stream));
         }
-        stage_out.alloc(n);
         CK(cudaEventCreateWithFlags(&ev_out_ready, cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&ev_out_free, cudaEventDisableTiming));
         CK(cudaEventRecord(ev_out_free, stream));
@@ -266,6 +263,14 @@ struct ax3d_domain {
             CK(cudaEventCreateWithFlags(&ev_su_read[k], cudaEventDisableTiming));
             CK(cudaEventRecord(ev_su_read[k], stream));
         }
+    }
+    // staging for fields other than the solid displacement, allocated on first use
+    void init_staging() {
+        if (stage_out.p) return;
+        const int64_t n = std::max<int64_t>(std::max(nsolid, nfluid), 1);
+        stage_in[0].alloc(n);
+        stage_in[1].alloc(n);
+        stage_out.alloc(n);
     }
     // host -> staging slot on the input copy stream; consumed by the next step()
     void set_field_async(int which, int phase, const float *in) {
@@ -285,6 +290,7 @@ struct ax3d_domain {
             queued.push_back({which, phase, -1 - target});
             return;
         }
+        init_staging();
         const int slot = next_slot;
         next_slot ^= 1;
         CK(cudaStreamWaitEvent(cp_in, ev_in_free[slot], 0));
@@ -326,6 +332,7 @@ struct ax3d_domain {
             CK(cudaEventRecord(ev_su_read[su_cur], cp_out));
             return;
         }
+        init_staging();
         CK(cudaStreamWaitEvent(stream, ev_out_free, 0));
         CK(cudaMemcpyAsync(stage_out.p, src, fsize(phase) * sizeof(float2), cudaMemcpyDeviceToDevice, stream));
         CK(cudaEventRecord(ev_out_ready, stream));

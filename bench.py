@@ -261,27 +261,27 @@ def run_gb300(args, world, rank, local):
         import torch
         n = dom.nsolid
         dom.enable_timers(False)
-        pins_in = [torch.empty(n, dtype=torch.complex64, pin_memory=True).numpy() for _ in range(2)]
-        pins_out = [torch.empty(n, dtype=torch.complex64, pin_memory=True).numpy() for _ in range(2)]
-        cur = dom.get("displ")
-        for b in pins_in:
-            b[:] = cur
-        ke = max(3, min(args.steps, 10))
+        # one pinned buffer each way (8 B x field size each): every step's input is the same
+        # state, and the result copies are ordered on one copy stream
+        pin_in = torch.empty(n, dtype=torch.complex64, pin_memory=True).numpy()
+        pin_out = torch.empty(n, dtype=torch.complex64, pin_memory=True).numpy()
+        pin_in[:] = dom.get("displ")
+        ke = max(3, args.steps)  # the streamed loop fills and drains once: time as many steps as `value`
         barrier(world)
         t0 = time.perf_counter()
         for _ in range(ke):
-            dom.set("displ", "solid", pins_in[0])
+            dom.set("displ", "solid", pin_in)
             dom.step(1)
-            dom.get("displ", "solid", out=pins_out[0])
+            dom.get("displ", "solid", out=pin_out)
         sync_s = allmax(world, (time.perf_counter() - t0) / ke)
         barrier(world)
         t0 = time.perf_counter()
-        dom.set_async("displ", "solid", pins_in[0])
+        dom.set_async("displ", "solid", pin_in)
         for k in range(ke):
             if k + 1 < ke:
-                dom.set_async("displ", "solid", pins_in[(k + 1) % 2])
+                dom.set_async("displ", "solid", pin_in)
             dom.step(1)
-            dom.get_async("displ", "solid", pins_out[k % 2])
+            dom.get_async("displ", "solid", pin_out)
         dom.sync_fields()
         e2e_s = allmax(world, (time.perf_counter() - t0) / ke)
         e2e = {"value": upd * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(8 * n),

@@ -286,3 +286,13 @@ def test_streamed_field_transfers_match_synchronous(ax3d_lib):
     a.step(1)
     b.step(1)
     np.testing.assert_array_equal(b.get("displ", "solid"), a.get("displ", "solid"))
+    # other fields go through the staging buffers
+    v = synth.random_fields(spec, seed=77, scale=1e-6)[0].astype(np.complex64)
+    a.set("veloc", "solid", v)
+    a.step(1)
+    b.set_async("veloc", "solid", v)
+    b.step(1)
+    got = np.zeros(b.nsolid, np.complex64)
+    b.get_async("veloc", "solid", got)
+    b.sync_fields()
+    np.testing.assert_array_equal(got, a.get("veloc", "solid"))
