@@ -371,3 +371,59 @@ def test_oracle_rejects_inconsistent_relabelling_ocean_and_dumps():
     spec = synth.annulus_domain(prt=0.02, nu=3, n_receivers=4, dumps=True)
     with pytest.raises(Ax3dError, match="relabelled elements are not supported"):
         _oracle()(spec)
+
+
+def _as_3d(spec):
+    """The same domain with every element in physical space: moduli, attenuation moduli
+    and relabelling X repeated over the element's samples."""
+    import copy
+    s3 = copy.deepcopy(spec)
+    enr = spec.element_nr()
+    km_of = {0: 2, 1: 5, 2: 21, 3: 1}
+    mods, atts, mofs, aofs, xs = [], [], [], [], []
+    xo = 0
+    for e in range(spec.n_elements):
+        nr = int(enr[e])
+        km = km_of[int(spec.e_mat[e])]
+        md = spec.e_mod[spec.e_mofs[e]:spec.e_mofs[e] + km * 25].reshape(km, 1, 25)
+        mofs.append(sum(m.size for m in mods))
+        mods.append(np.repeat(md, nr, 1).ravel())
+        att = int(spec.e_att[e])
+        npa = 4 if att == ATT_CG4 else 25
+        aofs.append(sum(a.size for a in atts))
+        if att:
+            am = spec.e_attm[spec.e_aofs[e]:spec.e_aofs[e] + 2 * npa].reshape(2, 1, npa)
+            atts.append(np.repeat(am, nr, 1).ravel())
+        x = spec.prt_x[xo:xo + 100].reshape(4, 1, 25)
+        xo += 100
+        xs.append(np.repeat(x, nr, 1).ravel())
+    s3.e_in3d = np.ones(spec.n_elements, np.uint8)
+    s3.e_mod = np.concatenate(mods).astype(np.float32)
+    s3.e_mofs = np.array(mofs, np.int64)
+    s3.e_attm = (np.concatenate(atts) if atts else np.zeros(0)).astype(np.float32)
+    s3.e_aofs = np.array(aofs, np.int64)
+    s3.prt_len = enr.astype(np.int32)
+    s3.prt_x = np.concatenate(xs).astype(np.float32)
+    return s3
+
+
+@pytest.mark.parametrize("kw", [dict(mat=MAT_TISO, att=ATT_CG4, nu=3), dict(mat=MAT_ANISO, att=ATT_FULL, nu=2),
+                                dict(fluid_layers=(1,), nu=3)], ids=["ti_cg4", "aniso_full", "fluid"])
+def test_oracle_prt1d_equals_prt3d_with_repeated_x(kw):
+    """The Fourier-space relabelling (PRT_1D) and the per-sample one (PRT_3D) agree when the
+    3-D element repeats the 1-D moduli and X over its samples (FP64 oracle, two passes so the
+    memory variables take part)."""
+    s1 = synth.annulus_domain(prt=0.05, **kw)
+    s3 = _as_3d(s1)
+    out = []
+    for sp in (s1, s3):
+        o = _oracle()(sp, double=True)
+        su, fu = synth.random_fields(sp, seed=11)
+        o.set("displ", "solid", su)
+        if o.nfluid:
+            o.set("displ", "fluid", fu)
+        o.compute_stiff()
+        o.compute_stiff()
+        out.append([o.get("stiff", "solid")] + ([o.get("stiff", "fluid")] if o.nfluid else []))
+    for a, b in zip(*out):
+        assert np.linalg.norm(a - b) <= 1e-11 * np.linalg.norm(a)
