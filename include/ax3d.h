@@ -150,7 +150,8 @@ int ax3d_add_surface(ax3d_domain *d, int32_t n, const int32_t *elem, const int32
    the mass given to ax3d_add_points.  len[i] = 1: MassOcean1D (MassOcean1D.cpp), four values
    1/(m + m_ocean), 1/m, sin theta, cos theta (theta = colatitude of the point); len[i] = nr:
    MassOcean3D (MassOcean3D.cpp), nr rows of four values 1/m, and the unit surface normal
-   (s, phi, z) scaled by sqrt(m_ocean / (m (m + m_ocean))).  Values back to back.  Fluid
+   (s, phi, z) scaled by sqrt(m_ocean / (m (m + m_ocean))).  Values back to back.  For a
+   point with nr = 1 a length of 1 is the MassOcean1D form (one sample never varies).  Fluid
    points and other lengths are rejected with the reference's messages.  Before
    ax3d_finalize. */
 int ax3d_add_ocean_load(ax3d_domain *d, int32_t n, const int32_t *point, const int32_t *len, const float *vals);

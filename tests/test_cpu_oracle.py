@@ -427,3 +427,37 @@ def test_oracle_prt1d_equals_prt3d_with_repeated_x(kw):
         out.append([o.get("stiff", "solid")] + ([o.get("stiff", "fluid")] if o.nfluid else []))
     for a, b in zip(*out):
         assert np.linalg.norm(a - b) <= 1e-11 * np.linalg.norm(a)
+
+
+def test_oracle_ocean3d_with_constant_rows_equals_ocean1d():
+    """MassOcean3D with mass, depth and normal independent of azimuth (unit normal
+    (sin t, 0, cos t)) gives MassOcean1D's acceleration: radial over m + m_ocean,
+    tangential over m."""
+    import copy
+    spec = synth.annulus_domain(seed=4, n_theta=3, n_r=2, nu=3, nu_random=True, nu_max=6, source=False,
+                                n_receivers=0, ocean="1d")
+    s3 = copy.deepcopy(spec)
+    lens, vals = [], []
+    for i, p in enumerate(spec.oc_pt):
+        imz, imr, st, ct = spec.oc_vals[4 * i:4 * i + 4].astype(np.float64)
+        nr = int(spec.p_nr[p])
+        if nr == 1:  # one sample: length 1 is the 1-D form (GLLPoint.cpp:58 never sees rows differ)
+            lens.append(1)
+            vals.append(spec.oc_vals[4 * i:4 * i + 4].astype(np.float64))
+            continue
+        m, mo = 1.0 / imr, 1.0 / imz - 1.0 / imr
+        scal = np.sqrt(mo / (m * (m + mo)))
+        lens.append(nr)
+        vals.append(np.tile([1.0 / m, st * scal, 0.0, ct * scal], nr))
+    s3.oc_len = np.array(lens, np.int32)
+    s3.oc_vals = np.concatenate(vals).astype(np.float32)
+    acc = []
+    for sp in (spec, s3):
+        o = _oracle()(sp, double=True)
+        o.set("stiff", "solid", synth.random_fields(sp, seed=5)[0])
+        o.update_newmark()
+        acc.append(o.get("accel", "solid"))
+    so, _ = spec.point_offsets()
+    rows = np.concatenate([np.arange(so[p], so[p] + 3 * (spec.p_nr[p] // 2 + 1)) for p in spec.oc_pt])
+    a, b = acc[0][rows], acc[1][rows]
+    assert np.linalg.norm(a) > 0 and np.linalg.norm(a - b) <= 1e-6 * np.linalg.norm(a)
