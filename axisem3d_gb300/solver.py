@@ -166,6 +166,26 @@ def _rot(theta, phi):
     return np.array([[ct * cp, -sp, st * cp], [ct * sp, cp, st * sp], [-st, 0.0, ct]])
 
 
+def _parse_keys(text, keys):
+    """Source::parseLine / checkValue (Source.cpp:104-119): a line whose first token contains
+    the key (case-insensitive) gives the value that follows; every key must be found."""
+    out = {}
+    for line in text.splitlines():
+        toks = line.split()
+        if len(toks) < 2:
+            continue
+        for k in keys:
+            if k.lower() in toks[0].lower():
+                try:
+                    out[k] = float(toks[1])
+                except ValueError:
+                    pass
+    for k in keys:
+        if k not in out:
+            raise ValueError(f"Source::checkValue || Error reading {k}.")
+    return out
+
+
 def _colat(s, z):
     """Geodesy::rtheta (Geodesy.cpp:13-16): colatitude of (s, z), 0 at the centre."""
     r = math.hypot(s, z)
@@ -598,6 +618,9 @@ class Simulation:
     def _cmt_latlon(self):
         """Source latitude/longitude of the CMTSOLUTION (Source.cpp:121-140), needed before
         the source itself is built to place geographic 3-D anomalies."""
+        if self.par.get("SOURCE_TYPE").lower() == "point_force":
+            v = _parse_keys((self.input_dir / self.par.get("SOURCE_FILE")).read_text(), ("latitude", "longitude"))
+            return v["latitude"], v["longitude"]
         vals = {}
         for line in (self.input_dir / self.par.get("SOURCE_FILE")).read_text().splitlines()[1:]:
             if ":" in line:
@@ -606,10 +629,14 @@ class Simulation:
         return float(vals["latitude"]), float(vals["longitude"])
 
     def _source(self, spec):
-        """CMTSOLUTION (Source.cpp:121-234) -> Earthquake::computeSourceFourier (Earthquake.cpp:20-88)."""
+        """CMTSOLUTION (Source.cpp:121-234) -> Earthquake::computeSourceFourier (Earthquake.cpp:20-88);
+        SOURCE_TYPE point_force -> PointForce::computeSourceFourier (PointForce.cpp)."""
         par = self.par
-        if par.get("SOURCE_TYPE").lower() != "earthquake":
-            raise NotImplementedError("SOURCE_TYPE: only earthquake is built")
+        stype = par.get("SOURCE_TYPE").lower()
+        if stype == "point_force":
+            return self._point_force(spec)
+        if stype != "earthquake":
+            raise ValueError(f"Source::buildInparam || Unknown source type: {par.get('SOURCE_TYPE')}")
         vals = {}
         for line in (self.input_dir / par.get("SOURCE_FILE")).read_text().splitlines()[1:]:
             if ":" in line:
@@ -619,20 +646,7 @@ class Simulation:
         self.src_dep = float(vals["depth"]) * 1e3
         M = {k: float(vals[k]) * 1e-7 for k in ("Mrr", "Mtt", "Mpp", "Mrt", "Mrp", "Mtp")}  # dyn*cm -> N*m
         self.half_duration = float(vals.get("half duration", 0.0))
-        zsrc = self.R - self.src_dep
-        # locate: axial solid element whose axis side spans z (Source::locate, Source.cpp:61-94)
-        ex = self.ex
-        host, eta = None, None
-        for e in np.nonzero(self.axial_e & ~self.fluid)[0]:
-            z = self.crds[e].reshape(5, 5, 2)[0, :, 1]  # axis column, jpol = 0..4
-            zmin, zmax = z.min(), z.max()
-            if zmin - 1e-3 <= zsrc <= zmax + 1e-3 and z[0] > -1e-6 and z[4] > -1e-6:
-                # eta from the linear radius on the axis (exact for spherical and linear mappings)
-                eta = -1.0 + 2.0 * (zsrc - z[0]) / (z[4] - z[0])
-                host = e
-                break
-        if host is None:
-            raise RuntimeError("Source::release || Error locating source.")
+        host, eta = self._locate_source(self.R - self.src_dep)
         fz = _lagrange(eta, S.gll()[0])
         Ggll, Gglj = S.gll()[2], S.glj()[2]
         J00, J01, J10, J11, det = (a[host] for a in self.jac)
@@ -658,6 +672,44 @@ class Simulation:
                     f[k, 2, 1] += fact * dwds * ((Mxx - Myy) / 2 - 1j * Mxy) / (2 * np.pi) * 1j
         spec.sources = [(int(host), f.astype(np.complex64))]
         self.src_elem = int(host)
+
+    def _point_force(self, spec):
+        """SOURCE_TYPE point_force (Source.cpp:190-226): latitude, longitude, depth (km) and
+        the force Ft, Fp, Fr (N) from SOURCE_FILE, each line's first token containing the key
+        (Source::parseLine).  PointForce::computeSourceFourier: orders 0 (Fr / 2 pi, z) and 1
+        ((Ft - i Fp) / 4 pi, (Fp + i Ft) / 4 pi on s, phi) on the axis column, weighted by
+        the Lagrange factors of the source depth."""
+        keys = _parse_keys((self.input_dir / self.par.get("SOURCE_FILE")).read_text(),
+                           ("latitude", "longitude", "depth", "ft", "fp", "fr"))
+        self.src_lat, self.src_lon = keys["latitude"], keys["longitude"]
+        self.src_dep = keys["depth"] * 1e3
+        self.half_duration = 0.0
+        host, eta = self._locate_source(self.R - self.src_dep)
+        fz = _lagrange(eta, S.gll()[0])
+        ft, fp, fr = keys["ft"], keys["fp"], keys["fr"]
+        f = np.zeros((25, 2, 3), complex)
+        for jp in range(5):
+            f[jp, 0, 2] = fz[jp] * fr / (2 * np.pi)
+            f[jp, 1, 0] = fz[jp] * (ft - 1j * fp) / (4 * np.pi)
+            f[jp, 1, 1] = fz[jp] * (fp + 1j * ft) / (4 * np.pi)
+        spec.sources = [(int(host), f.astype(np.complex64))]
+        self.src_elem = int(host)
+
+    def _locate_source(self, zsrc):
+        """Source::locate (Source.cpp:61-94): the axial solid element whose axis side spans
+        z = zsrc, and eta there."""
+        host, eta = None, None
+        for e in np.nonzero(self.axial_e & ~self.fluid)[0]:
+            z = self.crds[e].reshape(5, 5, 2)[0, :, 1]  # axis column, jpol = 0..4
+            zmin, zmax = z.min(), z.max()
+            if zmin - 1e-3 <= zsrc <= zmax + 1e-3 and z[0] > -1e-6 and z[4] > -1e-6:
+                # eta from the linear radius on the axis (exact for spherical and linear mappings)
+                eta = -1.0 + 2.0 * (zsrc - z[0]) / (z[4] - z[0])
+                host = e
+                break
+        if host is None:
+            raise RuntimeError("Source::release || Error locating source.")
+        return host, eta
 
     # ------------------------------------------------------------------ STF
     def _stf(self, spec):
@@ -920,7 +972,7 @@ class Simulation:
 def write_inputs(input_dir, mesh_kw=None, nu=2, stf="gauss", hdur=50.0, steps=2000, record_length=None,
                  n_stations=20, depth_km=100.0, seed=0, attenuation=False, system="source_centered",
                  models3d=(), lucky=False, whole_surface="false", ocean="none", station_extra=(),
-                 components="RTZ"):
+                 components="RTZ", force=None):
     """Seeded inputs of the small benchmark configuration: mesh, four parfiles, CMTSOLUTION
     (moment tensor ~ N(0, 1e20 N*m) written in dyn*cm) and STATIONS at uniform distance."""
     from . import mesher
@@ -936,8 +988,8 @@ def write_inputs(input_dir, mesh_kw=None, nu=2, stf="gauss", hdur=50.0, steps=20
                                      f"MODEL_PLOT_SLICES_NUM 0\nATTENUATION {'true' if attenuation else 'false'}\n")
     (d / "inparam.nu").write_text(f"NU_TYPE constant\nNU_CONST {nu}\nNU_WISDOM_LEARN false\n")
     (d / "inparam.time_src_recv").write_text(
-        f"TIME_DELTA_T 0.0\nTIME_DELTA_T_FACTOR 1.0\nTIME_RECORD_LENGTH {rl}\nSOURCE_TYPE earthquake\n"
-        f"SOURCE_FILE CMTSOLUTION\nSOURCE_TIME_FUNCTION {stf}\nSOURCE_STF_HALF_DURATION {hdur}\n"
+        f"TIME_DELTA_T 0.0\nTIME_DELTA_T_FACTOR 1.0\nTIME_RECORD_LENGTH {rl}\nSOURCE_TYPE {'point_force' if force else 'earthquake'}\n"
+        f"SOURCE_FILE {'POINTFORCE' if force else 'CMTSOLUTION'}\nSOURCE_TIME_FUNCTION {stf}\nSOURCE_STF_HALF_DURATION {hdur}\n"
         f"OUT_STATIONS_FILE STATIONS\nOUT_STATIONS_SYSTEM {system}\nOUT_STATIONS_DUPLICATED rename\n"
         f"OUT_STATIONS_FORMAT netcdf\nOUT_STATIONS_COMPONENTS {components}\nOUT_STATIONS_RECORD_INTERVAL 1\n"
         f"OUT_STATIONS_DUMP_INTERVAL 1000\nOUT_STATIONS_WHOLE_SURFACE {whole_surface}\nOUT_STATIONS_DEPTH_REF false\n")
@@ -953,6 +1005,9 @@ def write_inputs(input_dir, mesh_kw=None, nu=2, stf="gauss", hdur=50.0, steps=20
         "PDE 2026 1 1 0 0 0.0 0.0 0.0 100.0 6.0 6.0 SYNTHETIC\nevent name:     synthetic\ntime shift:      0.00\n"
         f"half duration:   {hdur:.2f}\nlatitude:       0.0\nlongitude:      0.0\ndepth:          {depth_km:.4f}\n"
         + "".join(f"{k}:       {v:.6e}\n" for k, v in zip(names, m)))
+    if force:  # point force (Ft, Fp, Fr) in N at the same place (PointForce, Source.cpp:190-226)
+        (d / "POINTFORCE").write_text(f"latitude:  0.0\nlongitude: 0.0\ndepth:     {depth_km:.4f}\n"
+                                      + "".join(f"{k}:  {v:.6e}\n" for k, v in zip(("Ft", "Fp", "Fr"), force)))
     dist = np.linspace(10.0, 170.0, n_stations)
     extra = [f"  {station_extra[i % len(station_extra)]}" if station_extra else "" for i in range(n_stations)]
     (d / "STATIONS").write_text("".join(f"S{i:03d}       SY       {t:.4f}     {(37.0 * i) % 360:.4f}    0.0    0.0"

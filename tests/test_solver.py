@@ -444,3 +444,37 @@ def test_gpu_preloop_transversely_isotropic(ax3d_lib):
             h_mod, h_att = PL.moduli_host(rows, ifact, m, isotropic=iso, att=att, sls=sls)
             np.testing.assert_allclose(g_mod, h_mod, rtol=2e-6)
             np.testing.assert_allclose(g_att, h_att, rtol=2e-6, atol=1e-30)
+
+
+def test_point_force_source(tmp_path_factory):
+    """SOURCE_TYPE point_force (PointForce::computeSourceFourier): orders 0 and 1 on the axis
+    column.  A vertical force excites order 0 only: no transverse motion anywhere.  A force
+    along theta at the pole (x) radiates SH as sin(azimuth) and P-SV as cos(azimuth): no T at
+    azimuth 0, no R or Z at azimuth 90.  An unknown source type raises."""
+    from oracle.oracle_py import OracleDomain
+    out = {}
+    for name, force in (("vertical", (0.0, 0.0, 1e16)), ("horizontal", (1e16, 0.0, 0.0))):
+        d = tmp_path_factory.mktemp("pf" + name) / "input"
+        solver.write_inputs(d, mesh_kw=SMALL_MESH, steps=250, hdur=20.0, n_stations=4, seed=6, force=force)
+        (d / "STATIONS").write_text("".join(f"A{i}  SY  10.0  {az:.1f}  0.0  0.0\n"
+                                            for i, az in enumerate((0.0, 30.0, 60.0, 90.0))))
+        sim = solver.Simulation(d)
+        spec = sim.build()
+        elem, f = spec.sources[0]
+        assert f.shape == (25, 2, 3) and np.abs(f[5:]).max() == 0  # axis column only (ipol = 0)
+        o = OracleDomain(spec, double=True)
+        o.step(250)
+        out[name] = sim.rotate(o.seismograms(0, 250))  # [t][station][R, T, Z]
+    v, h = out["vertical"], out["horizontal"]
+    peak = np.abs(v).max()
+    assert peak > 0 and np.abs(v[..., 1]).max() <= 1e-12 * peak
+    hp = np.abs(h).max()
+    assert np.abs(h[:, 0, 1]).max() <= 1e-10 * hp                        # T at azimuth 0
+    assert np.abs(h[:, 3, [0, 2]]).max() <= 1e-6 * np.abs(h[:, 3, 1]).max()  # R, Z at azimuth 90
+    assert np.abs(h[:, 3, 1]).max() > 1e-2 * hp
+    d = tmp_path_factory.mktemp("pfbad") / "input"
+    solver.write_inputs(d, mesh_kw=SMALL_MESH, steps=10, n_stations=2, seed=6)
+    (d / "inparam.time_src_recv").write_text((d / "inparam.time_src_recv").read_text().replace(
+        "SOURCE_TYPE earthquake", "SOURCE_TYPE explosion"))
+    with pytest.raises(ValueError, match="Unknown source type"):
+        solver.Simulation(d).build()
