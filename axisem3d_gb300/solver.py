@@ -756,6 +756,10 @@ class Simulation:
         lines = [l.split() for l in (self.input_dir / par.get("OUT_STATIONS_FILE")).read_text().splitlines() if l.strip()]
         src_t = math.pi / 2 - math.radians(self.src_lat)
         src_p = math.radians(self.src_lon % 360)
+        dup = par.get("OUT_STATIONS_DUPLICATED").lower()
+        if dup not in ("ignore", "rename", "error"):
+            raise ValueError("ReceiverCollection::buildInparam || Invalid parameter, keyword = OUT_STATIONS_DUPLICATED.")
+        keys_seen = set()
         rec, dumps = [], []
         for toks in lines:
             if len(toks) < 6:
@@ -765,6 +769,17 @@ class Simulation:
                 la, lo, bur = float(toks[2]), float(toks[3]), float(toks[5])
             except ValueError:
                 continue
+            # duplicated NET.NAME keys (ReceiverCollection.cpp:98-117): renamed NAME__DUPLICATED<k>
+            # or an error; "ignore" keeps them as they are
+            if dup != "ignore" and f"{net}.{name}" in keys_seen:
+                if dup == "error":
+                    raise ValueError("ReceiverCollection::ReceiverCollection || Duplicated station keys "
+                                     f"(network_name) found in station data file || Name = {name}; Network = {net}")
+                base, k = name, 0
+                while f"{net}.{name}" in keys_seen:
+                    k += 1
+                    name = f"{base}__DUPLICATED{k}"
+            keys_seen.add(f"{net}.{name}")
             extra = {t.lower() for t in toks[6:]}
             dumps.append((1 if "dump_strain" in extra else 0) | (2 if "dump_curl" in extra else 0))
             if system == "geographic":
@@ -943,6 +958,54 @@ class Simulation:
                            arr[:, j].astype(np.float32))
         NC.write(path, ds)
         return path
+
+    def write_ascii(self, seis_rtz, strain=None, curl=None, out_dir=None):
+        """PointwiseIOAscii (PointwiseIOAscii.cpp): per station NET.NAME.<comp>.ascii with rows
+        (time, 3 components), and NET.NAME.RTZ.strain.ascii (time, 6) /
+        NET.NAME.RTZ.curl.ascii (time, 3) for the flagged receivers; full precision,
+        space-separated."""
+        out = Path(out_dir or self.output_dir / "stations")
+        out.mkdir(parents=True, exist_ok=True)
+        n = seis_rtz.shape[0]
+        t = -self.shift + np.arange(n) * self.dt
+        dump = np.asarray(self.spec.r_dump, np.int32) if len(self.spec.r_dump) else np.zeros(len(self.receivers), np.int32)
+
+        def put(path, cols):
+            rows = np.column_stack([t] + [np.asarray(c, np.float64) for c in cols])
+            path.write_text("".join(" " + " ".join(repr(float(v)) for v in r) + "\n" for r in rows))
+
+        paths = []
+        for i, r in enumerate(self.receivers):
+            base = f"{r[1]}.{r[0]}"
+            p = out / f"{base}.{self.components}.ascii"
+            put(p, [seis_rtz[:, i, k].astype(np.float32) for k in range(3)])
+            paths.append(p)
+        for bit, arr, tag, k in ((1, strain, "strain", 6), (2, curl, "curl", 3)):
+            if arr is None:
+                continue
+            for j, i in enumerate(np.flatnonzero(dump & bit)):
+                r = self.receivers[i]
+                p = out / f"{r[1]}.{r[0]}.RTZ.{tag}.ascii"
+                put(p, [arr[:, j, c].astype(np.float32) for c in range(k)])
+                paths.append(p)
+        return paths
+
+    def write_outputs(self, seis_rtz, strain=None, curl=None):
+        """OUT_STATIONS_FORMAT (ReceiverCollection.cpp:341-372), any of: ascii (one file per
+        station), netcdf (axisem3d_synthetics.nc) and netcdf_no_assemble (one file per rank,
+        here rank 0: axisem3d_synthetics.nc.rank0)."""
+        fmts = {f.lower() for f in self.par.values.get("OUT_STATIONS_FORMAT", [])}
+        if not fmts or not fmts <= {"ascii", "netcdf", "netcdf_no_assemble"}:
+            raise ValueError("ReceiverCollection::buildInparam || Invalid parameter, keyword = OUT_STATIONS_FORMAT.")
+        paths = []
+        if "ascii" in fmts:
+            paths += self.write_ascii(seis_rtz, strain=strain, curl=curl)
+        if "netcdf" in fmts:
+            paths.append(self.write_netcdf(seis_rtz, strain=strain, curl=curl))
+        if "netcdf_no_assemble" in fmts:
+            paths.append(self.write_netcdf(seis_rtz, path=self.output_dir / "stations" / "axisem3d_synthetics.nc.rank0",
+                                           strain=strain, curl=curl))
+        return paths
 
     # ------------------------------------------------------------------ run
     def run(self, domain=None, nsteps=None):

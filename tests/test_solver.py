@@ -478,3 +478,42 @@ def test_point_force_source(tmp_path_factory):
         "SOURCE_TYPE earthquake", "SOURCE_TYPE explosion"))
     with pytest.raises(ValueError, match="Unknown source type"):
         solver.Simulation(d).build()
+
+
+def test_ascii_output_and_duplicated_stations(tmp_path_factory):
+    """OUT_STATIONS_FORMAT ascii netcdf: one text file per station (time + R, T, Z; strain and
+    curl files for flagged receivers) beside the NetCDF file; OUT_STATIONS_DUPLICATED rename
+    appends __DUPLICATED<k> to a repeated NET.NAME, error refuses it."""
+    from oracle.oracle_py import OracleDomain
+    d = tmp_path_factory.mktemp("asc") / "input"
+    solver.write_inputs(d, mesh_kw=SMALL_MESH, steps=30, hdur=20.0, n_stations=3, seed=4,
+                        station_extra=("dump_strain dump_curl", "", ""))
+    st = (d / "STATIONS").read_text().splitlines()
+    (d / "STATIONS").write_text("\n".join(st + [st[1]]) + "\n")  # S001 twice
+    tsr = (d / "inparam.time_src_recv").read_text().replace("OUT_STATIONS_FORMAT netcdf", "OUT_STATIONS_FORMAT ascii netcdf")
+    (d / "inparam.time_src_recv").write_text(tsr)
+    out = d.parent / "output"
+    sim = solver.Simulation(d, output_dir=out)
+    spec = sim.build()
+    assert [r[0] for r in sim.receivers] == ["S000", "S001", "S002", "S001__DUPLICATED1"]
+    o = OracleDomain(spec)
+    o.step(30)
+    rtz = sim.rotate(o.seismograms(0, 30))
+    st_, cu = o.strain_curl("strain", 0, 30), o.strain_curl("curl", 0, 30)
+    paths = sim.write_outputs(rtz, strain=st_, curl=cu)
+    names = sorted(p.name for p in paths)
+    assert "SY.S001__DUPLICATED1.RTZ.ascii" in names and "axisem3d_synthetics.nc" in names
+    a = np.loadtxt(out / "stations" / "SY.S002.RTZ.ascii")
+    assert a.shape == (30, 4)
+    np.testing.assert_allclose(a[:, 0], -sim.shift + np.arange(30) * sim.dt)
+    np.testing.assert_allclose(a[:, 1:], rtz[:, 2].astype(np.float32), rtol=1e-6, atol=1e-37)
+    s0 = np.loadtxt(out / "stations" / "SY.S000.RTZ.strain.ascii")
+    assert s0.shape == (30, 7)
+    np.testing.assert_allclose(s0[:, 1:], st_[:, 0].astype(np.float32), rtol=1e-6, atol=1e-37)
+    assert np.loadtxt(out / "stations" / "SY.S000.RTZ.curl.ascii").shape == (30, 4)
+    (d / "inparam.time_src_recv").write_text(tsr.replace("OUT_STATIONS_DUPLICATED rename", "OUT_STATIONS_DUPLICATED error"))
+    with pytest.raises(ValueError, match="Duplicated station keys"):
+        solver.Simulation(d).build()
+    (d / "inparam.time_src_recv").write_text(tsr.replace("OUT_STATIONS_DUPLICATED rename", "OUT_STATIONS_DUPLICATED maybe"))
+    with pytest.raises(ValueError, match="OUT_STATIONS_DUPLICATED"):
+        solver.Simulation(d).build()
