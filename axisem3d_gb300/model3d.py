@@ -171,13 +171,14 @@ def volumetric_models(par, src_latlon, R):
     return out
 
 
-def apply_models(models, props1d, crds, nr, fluid):
+def apply_models(models, props1d, crds, nr, fluid, phi2d=None):
     """3-D properties of a group of elements sharing one Nr.
 
     props1d: {"VP","VS","RHO": (n, 25)} 1-D values at the GLL points; crds (n, 25, 2) = (s, z);
-    fluid (n,) bool.  Slice alpha sits at phi = 2 pi alpha / nr.  Returns ({prop: (n, nr, 25)},
+    fluid (n,) bool.  Slice alpha sits at phi = 2 pi alpha / nr, or every slice at phi2d in
+    2-D mode (Quad::computeGeocentricGlobal with phi2D).  Returns ({prop: (n, nr, 25)},
     touched (n,) bool): elements with any point inside any model's range."""
-    phi = 2 * math.pi * np.arange(nr) / nr
+    phi = 2 * math.pi * np.arange(nr) / nr if phi2d is None else np.full(nr, float(phi2d))
     n = len(crds)
     out = {k: np.empty((n, nr, 25), np.float32) for k in props1d}
     touched = np.zeros(n, bool)

@@ -299,14 +299,20 @@ class Simulation:
         # volumetric 3-D models (Material::addVolumetric3D) on each element's Nr slices
         e_nr = p_nr[e_pts].max(1)
         models = M3D.volumetric_models(par, self._cmt_latlon(), self.R)
+        self.phi2d = self._phi2d()
         e3d = np.zeros(E, bool)
         props3 = {}
         if models:
             for nr in np.unique(e_nr):
                 sel = np.nonzero(e_nr == nr)[0]
                 cur, touched = M3D.apply_models(models, {"VP": vp[sel], "VS": vs[sel], "RHO": rho[sel]},
-                                                crds[sel], int(nr), fl[sel])
+                                                crds[sel], int(nr), fl[sel], phi2d=self.phi2d)
                 for j in np.nonzero(touched)[0]:
+                    if self.phi2d is not None:
+                        # 2-D mode: every slice sees the model at phi2D, so the element stays
+                        # 1-D with the first row (isSolidPar1D, XMath::structuredUseFirstRow)
+                        vp[sel[j]], vs[sel[j]], rho[sel[j]] = cur["VP"][j, 0], cur["VS"][j, 0], cur["RHO"][j, 0]
+                        continue
                     e3d[sel[j]] = True
                     props3[sel[j]] = {k: v[j] for k, v in cur.items()}
         self.e3d, self.models = e3d, models
@@ -539,6 +545,24 @@ class Simulation:
             ao += na
         return out
 
+    def _phi2d(self):
+        """MODEL_2D_MODE (Mesh.cpp:44-70): off, source-centered (MODEL_2D_AZIMUTH, degrees) or
+        geographic (MODEL_2D_LATITUDE / _LONGITUDE rotated to the source frame): the azimuth
+        at which 3-D models are sampled for every slice, None when off."""
+        par = self.par
+        mode = (par.values.get("MODEL_2D_MODE") or ["off"])[0].lower()
+        if mode == "off":
+            return None
+        if mode == "source-centered":
+            return math.radians(par.get("MODEL_2D_AZIMUTH", float)) % (2 * math.pi)
+        if mode == "geographic":
+            lat, lon = self._cmt_latlon()
+            _, ph = glob_to_src(math.pi / 2 - math.radians(par.get("MODEL_2D_LATITUDE", float)),
+                                math.radians(par.get("MODEL_2D_LONGITUDE", float) % 360),
+                                math.pi / 2 - math.radians(lat), math.radians(lon % 360))
+            return ph
+        raise ValueError("Mesh::Mesh || Invalid input for MODEL_2D_MODE.")
+
     def _nr_field(self, pcrd, nodes):
         """NU_TYPE constant (ConstNrField), empirical (EmpNrField) or wisdom (WisdomNrField,
         reading NU_WISDOM_REUSE_INPUT from the input directory)."""
@@ -618,6 +642,8 @@ class Simulation:
     def _cmt_latlon(self):
         """Source latitude/longitude of the CMTSOLUTION (Source.cpp:121-140), needed before
         the source itself is built to place geographic 3-D anomalies."""
+        if _flag(self.par, "DEVELOP_NON_SOURCE_MODE"):
+            return 90.0, 0.0
         if self.par.get("SOURCE_TYPE").lower() == "point_force":
             v = _parse_keys((self.input_dir / self.par.get("SOURCE_FILE")).read_text(), ("latitude", "longitude"))
             return v["latitude"], v["longitude"]
@@ -632,6 +658,14 @@ class Simulation:
         """CMTSOLUTION (Source.cpp:121-234) -> Earthquake::computeSourceFourier (Earthquake.cpp:20-88);
         SOURCE_TYPE point_force -> PointForce::computeSourceFourier (PointForce.cpp)."""
         par = self.par
+        if _flag(par, "DEVELOP_NON_SOURCE_MODE"):
+            # NullSource (Source.cpp:126-132, NullSource.h): no source term; Source() sits at
+            # the north pole on the surface (Source.h:18)
+            self.src_lat, self.src_lon, self.src_dep = 90.0, 0.0, 0.0
+            self.half_duration = 0.0
+            spec.sources = []
+            self.src_elem = -1
+            return
         stype = par.get("SOURCE_TYPE").lower()
         if stype == "point_force":
             return self._point_force(spec)

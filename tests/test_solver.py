@@ -517,3 +517,40 @@ def test_ascii_output_and_duplicated_stations(tmp_path_factory):
     (d / "inparam.time_src_recv").write_text(tsr.replace("OUT_STATIONS_DUPLICATED rename", "OUT_STATIONS_DUPLICATED maybe"))
     with pytest.raises(ValueError, match="OUT_STATIONS_DUPLICATED"):
         solver.Simulation(d).build()
+
+
+def test_2d_mode_and_null_source(tmp_path_factory):
+    """MODEL_2D_MODE source-centered: the 3-D models are sampled at one azimuth, so every
+    element stays 1-D but takes the model's values there (two azimuths through and beside
+    a bubble differ); DEVELOP_NON_SOURCE_MODE gives no source term and a quiet field."""
+    from oracle.oracle_py import OracleDomain
+    d = tmp_path_factory.mktemp("m2d") / "input"
+    solver.write_inputs(d, mesh_kw=SMALL_MESH, steps=20, hdur=20.0, n_stations=2, seed=3, nu=4,
+                        models3d=MODELS_3D)
+    full = solver.Simulation(d).build()
+    assert full.e_in3d.any()
+    mods = []
+    for az in (0.0, 180.0):
+        txt = (d / "inparam.model").read_text().replace("MODEL_2D_MODE off",
+                                                         f"MODEL_2D_MODE source-centered\nMODEL_2D_AZIMUTH {az}")
+        (d / "inparam.model").write_text(txt)
+        spec = solver.Simulation(d).build()
+        assert not spec.e_in3d.any()
+        mods.append(spec.e_mod.copy())
+        (d / "inparam.model").write_text(txt.replace(f"MODEL_2D_MODE source-centered\nMODEL_2D_AZIMUTH {az}",
+                                                     "MODEL_2D_MODE off"))
+    assert mods[0].shape == mods[1].shape and np.abs(mods[0] - mods[1]).max() > 0
+    (d / "inparam.model").write_text((d / "inparam.model").read_text().replace("MODEL_2D_MODE off",
+                                                                               "MODEL_2D_MODE sideways"))
+    with pytest.raises(ValueError, match="MODEL_2D_MODE"):
+        solver.Simulation(d).build()
+    d2 = tmp_path_factory.mktemp("null") / "input"
+    solver.write_inputs(d2, mesh_kw=SMALL_MESH, steps=20, hdur=20.0, n_stations=2, seed=3)
+    adv = (d2 / "inparam.advanced").read_text().replace("DEVELOP_NON_SOURCE_MODE false", "DEVELOP_NON_SOURCE_MODE true")
+    (d2 / "inparam.advanced").write_text(adv)
+    sim = solver.Simulation(d2)
+    spec = sim.build()
+    assert spec.sources == [] and sim.src_lat == 90.0
+    o = OracleDomain(spec)
+    o.step(20)
+    assert np.abs(o.seismograms(0, 20)).max() == 0
