@@ -111,6 +111,13 @@ class Exodus:
                       ev["element_type"].astype(int), ev["fluid"] > 0.5, ev.get("dt", np.zeros(E)), nodal, side, glob)
 
 
+def _int_or(par, key, default):
+    try:
+        return par.get(key, int)
+    except KeyError:
+        return default
+
+
 def _flag(par, key):
     try:
         return par.get(key, bool)
@@ -966,17 +973,28 @@ class Simulation:
             out[:, k, 0], out[:, k, 1], out[:, k, 2] = -ut * sb + up * cb, -ut * cb - up * sb, ur
         return out
 
+    def _recorded(self, arr):
+        """Rows of the steps PointwiseRecorder::record keeps (tstep % OUT_STATIONS_RECORD_INTERVAL
+        == 0, PointwiseRecorder.cpp:62-66; the library records every step) and their times."""
+        iv = max(_int_or(self.par, "OUT_STATIONS_RECORD_INTERVAL", 1), 1)
+        n = arr.shape[0] if arr is not None else 0
+        return (arr[::iv] if arr is not None else None), -self.shift + np.arange(0, n, iv) * self.dt
+
     def write_netcdf(self, seis_rtz, path=None, strain=None, curl=None):
         """output/stations/axisem3d_synthetics.nc with time_points and NET.NAME.<comp>, plus
         NET.NAME.RTZ.strain [steps][6] and NET.NAME.RTZ.curl [steps][3] for the receivers
-        flagged dump_strain / dump_curl (PointwiseIONetCDF.cpp:56-95)."""
+        flagged dump_strain / dump_curl (PointwiseIONetCDF.cpp:56-95), one row per recorded
+        step."""
         path = Path(path or self.output_dir / "stations" / "axisem3d_synthetics.nc")
         path.parent.mkdir(parents=True, exist_ok=True)
+        seis_rtz, t = self._recorded(seis_rtz)
+        strain, _ = self._recorded(strain)
+        curl, _ = self._recorded(curl)
         n = seis_rtz.shape[0]
         ds = NC.Dataset()
         ds.add_dim("ntime", n)
         ds.add_dim("ncomp", 3)
-        ds.add_var("time_points", ("ntime",), -self.shift + np.arange(n) * self.dt)
+        ds.add_var("time_points", ("ntime",), t)
         for i, r in enumerate(self.receivers):
             ds.add_var(f"{r[1]}.{r[0]}.{self.components}", ("ntime", "ncomp"), seis_rtz[:, i].astype(np.float32),
                        attrs={"latitude": float(r[2]), "longitude": float(r[3]), "depth": float(r[4])})
@@ -1000,8 +1018,9 @@ class Simulation:
         space-separated."""
         out = Path(out_dir or self.output_dir / "stations")
         out.mkdir(parents=True, exist_ok=True)
-        n = seis_rtz.shape[0]
-        t = -self.shift + np.arange(n) * self.dt
+        seis_rtz, t = self._recorded(seis_rtz)
+        strain, _ = self._recorded(strain)
+        curl, _ = self._recorded(curl)
         dump = np.asarray(self.spec.r_dump, np.int32) if len(self.spec.r_dump) else np.zeros(len(self.receivers), np.int32)
 
         def put(path, cols):

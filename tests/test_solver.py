@@ -554,3 +554,25 @@ def test_2d_mode_and_null_source(tmp_path_factory):
     o = OracleDomain(spec)
     o.step(20)
     assert np.abs(o.seismograms(0, 20)).max() == 0
+
+
+def test_record_interval_subsamples_station_output(tmp_path_factory):
+    """OUT_STATIONS_RECORD_INTERVAL 3: the station files keep steps 0, 3, 6, ... with their
+    times (PointwiseRecorder::record)."""
+    from oracle.oracle_py import OracleDomain
+    d = tmp_path_factory.mktemp("riv") / "input"
+    solver.write_inputs(d, mesh_kw=SMALL_MESH, steps=20, hdur=20.0, n_stations=2, seed=4)
+    t = (d / "inparam.time_src_recv").read_text()
+    (d / "inparam.time_src_recv").write_text(t.replace("OUT_STATIONS_RECORD_INTERVAL 1", "OUT_STATIONS_RECORD_INTERVAL 3")
+                                             .replace("OUT_STATIONS_FORMAT netcdf", "OUT_STATIONS_FORMAT netcdf ascii"))
+    sim = solver.Simulation(d, output_dir=d.parent / "out")
+    spec = sim.build()
+    o = OracleDomain(spec)
+    o.step(20)
+    rtz = sim.rotate(o.seismograms(0, 20))
+    sim.write_outputs(rtz)
+    ds = NC.read(d.parent / "out" / "stations" / "axisem3d_synthetics.nc")
+    np.testing.assert_allclose(ds["time_points"], -sim.shift + np.arange(0, 20, 3) * sim.dt)
+    np.testing.assert_allclose(ds["SY.S001.RTZ"], rtz[::3, 1].astype(np.float32))
+    a = np.loadtxt(d.parent / "out" / "stations" / "SY.S000.RTZ.ascii")
+    assert a.shape == (7, 4)
