@@ -307,6 +307,15 @@ class Simulation:
         e_nr = p_nr[e_pts].max(1)
         models = M3D.volumetric_models(par, self._cmt_latlon(), self.R)
         self.phi2d = self._phi2d()
+        # options that would change the physics but are not built here: refuse them rather
+        # than run without them (Geometric3D::buildInparam, ExodusModel.cpp:557-572)
+        if _int_or(par, "MODEL_3D_GEOMETRIC_NUM", 0) > 0:
+            raise ValueError("Geometric3D::buildInparam || 3-D geometric models (particle relabelling from "
+                             "undulations) are not derived by this pre-loop; pass X through ax3d_set_prt.")
+        emode = (par.values.get("MODEL_3D_ELLIPTICITY_MODE") or ["off"])[0].lower()
+        if emode != "off":
+            raise ValueError("ExodusModel::buildInparam || MODEL_3D_ELLIPTICITY_MODE: only 'off' (a spherical "
+                             "Earth) is built.")
         e3d = np.zeros(E, bool)
         props3 = {}
         if models:
@@ -585,6 +594,8 @@ class Simulation:
             return 2 * par.get("NU_CONST", int) + 1
         if nutype == "empirical":
             return W.empirical_nr(par, sz[:, 0], sz[:, 1], self.R)
+        if nutype == "user-defined":
+            return W.user_nr(par.values.get("NU_USER_PARAMETER_LIST", []), sz[:, 0], sz[:, 1], self.R)
         if nutype == "wisdom":
             data = W.read_wisdom(self.input_dir / par.get("NU_WISDOM_REUSE_INPUT"))
             factor = par.get("NU_WISDOM_REUSE_FACTOR", float)

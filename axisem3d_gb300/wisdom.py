@@ -6,7 +6,9 @@ learned, Nu of the run) and writes them as one NetCDF variable "axisem3d_wisdom"
 with NU_TYPE wisdom (WisdomNrField.cpp:10-24) takes, at every GLL point, the inverse-
 distance mean of the learned Nu of the four nearest stored points (the stored value itself
 at distance below 1e-10), times NU_WISDOM_REUSE_FACTOR, rounded.  NU_TYPE empirical is
-EmpNrField::getNrAtPoint (EmpNrField.cpp:26-62).
+EmpNrField::getNrAtPoint (EmpNrField.cpp:26-62); NU_TYPE user-defined is the shipped
+UserNrField (UserNrField.cpp:20-80): Nu linear in depth through NU_USER_PARAMETER_LIST
+(depth0 nu0 depth1 nu1 ..., metres).
 """
 from __future__ import annotations
 
@@ -108,4 +110,23 @@ def empirical_nr(par, s, z, r_outer) -> np.ndarray:
     nr = 2 * np.maximum(nu_min, np.ceil(nu).astype(np.int64)) + 1
     if (nr <= 0).any():
         raise ValueError("EmpNrField::getNrAtPoint || Non-positive Nr.")
+    return nr
+
+
+def user_nr(params, s, z, r_outer) -> np.ndarray:
+    """UserNrField::getNrAtPoint as shipped: Nu interpolated linearly in depth between the
+    (depth, nu) pairs of NU_USER_PARAMETER_LIST, held constant outside them; nr = 2 nu + 1
+    truncated to an integer."""
+    params = [float(v) for v in params]
+    nd = len(params) // 2
+    if nd == 0 or len(params) % 2 == 1:
+        raise ValueError("UserNrField::getNrAtPoint || Using the default UserNrField.cpp, the number of the "
+                         "user-defined parameters must be even and positive.")
+    d = r_outer - np.hypot(np.asarray(s, np.float64), np.asarray(z, np.float64))
+    depths = np.array(params[0::2])
+    nus = np.array(params[1::2])
+    nu = np.interp(d, depths, nus)  # constant beyond the first and last depth
+    nr = (2 * nu + 1).astype(np.int64)
+    if (nr <= 0).any():
+        raise ValueError("UserNrField::getNrAtPoint || Non-positive Nr.")
     return nr

@@ -576,3 +576,26 @@ def test_record_interval_subsamples_station_output(tmp_path_factory):
     np.testing.assert_allclose(ds["SY.S001.RTZ"], rtz[::3, 1].astype(np.float32))
     a = np.loadtxt(d.parent / "out" / "stations" / "SY.S000.RTZ.ascii")
     assert a.shape == (7, 4)
+
+
+def test_user_nr_field_and_refused_options(tmp_path_factory):
+    """NU_TYPE user-defined (UserNrField as shipped: Nu linear in depth through the
+    (depth, nu) pairs); geometric models and ellipticity, not built, are refused."""
+    from axisem3d_gb300 import wisdom as W
+    nr = W.user_nr(["0", "8", "1000e3", "2", "3000e3", "2"], [0.0, 0.0, 0.0, 0.0],
+                   [6371e3, 6371e3 - 500e3, 6371e3 - 1000e3, 100.0], 6371e3)
+    assert nr.tolist() == [17, 11, 5, 5]
+    with pytest.raises(ValueError, match="even and positive"):
+        W.user_nr(["0", "8", "1"], [0.0], [6371e3], 6371e3)
+    d = tmp_path_factory.mktemp("unr") / "input"
+    solver.write_inputs(d, mesh_kw=SMALL_MESH, steps=10, n_stations=2, seed=3)
+    (d / "inparam.nu").write_text("NU_TYPE user-defined\nNU_USER_PARAMETER_LIST 0 6 2000e3 2\nNU_WISDOM_LEARN false\n")
+    spec = solver.Simulation(d).build()
+    assert spec.p_nr.max() <= 13 and spec.p_nr.min() >= 1 and len(np.unique(spec.p_nr)) > 2
+    m = (d / "inparam.model").read_text()
+    (d / "inparam.model").write_text(m.replace("MODEL_3D_GEOMETRIC_NUM 0", "MODEL_3D_GEOMETRIC_NUM 1\nMODEL_3D_GEOMETRIC_LIST crust1"))
+    with pytest.raises(ValueError, match="ax3d_set_prt"):
+        solver.Simulation(d).build()
+    (d / "inparam.model").write_text(m + "MODEL_3D_ELLIPTICITY_MODE full\nMODEL_3D_ELLIPTICITY_INVF 298.3\n")
+    with pytest.raises(ValueError, match="ELLIPTICITY"):
+        solver.Simulation(d).build()
