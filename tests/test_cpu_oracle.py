@@ -461,3 +461,20 @@ def test_oracle_ocean3d_with_constant_rows_equals_ocean1d():
     rows = np.concatenate([np.arange(so[p], so[p] + 3 * (spec.p_nr[p] // 2 + 1)) for p in spec.oc_pt])
     a, b = acc[0][rows], acc[1][rows]
     assert np.linalg.norm(a) > 0 and np.linalg.norm(a - b) <= 1e-6 * np.linalg.norm(a)
+
+
+def test_header_compiles_as_c99(tmp_path):
+    """include/ax3d.h is a C header: a C99 translation unit that takes the address of every
+    declared entry point compiles warning-free with gcc (no C++ in the signatures)."""
+    import shutil
+    if not shutil.which("gcc"):
+        pytest.skip("gcc not available")
+    decl = re.findall(r"^(?:int|int64_t|int32_t|size_t)\s+(ax3d_\w+)\(", (ROOT / "include/ax3d.h").read_text(), re.M)
+    src = tmp_path / "t.c"
+    src.write_text('#include "ax3d.h"\n#include <stdio.h>\ntypedef void (*fn)(void);\nstatic const fn table[] = {\n'
+                   + "".join(f"    (fn)&{f},\n" for f in decl)
+                   + '};\nint main(void) {\n    printf("%d\\n", (int)(sizeof table / sizeof table[0]));\n'
+                   + "    return 0;\n}\n")
+    res = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic", "-c", str(src),
+                          "-I", str(ROOT / "include"), "-o", str(tmp_path / "t.o")], capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr
