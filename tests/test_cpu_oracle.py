@@ -478,3 +478,18 @@ def test_header_compiles_as_c99(tmp_path):
     res = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic", "-c", str(src),
                           "-I", str(ROOT / "include"), "-o", str(tmp_path / "t.o")], capture_output=True, text=True)
     assert res.returncode == 0, res.stderr
+
+
+@pytest.mark.parametrize("kw", [dict(nu=1, prt=0.1), dict(nu=2, mat=MAT_TISO, prt=0.1),
+                                dict(nu=1, mat=MAT_ANISO, prt=0.1), dict(nu=2, in3d=True, prt=0.1)],
+                         ids=["iso_prt1d", "ti_prt1d", "aniso_prt1d", "iso_prt3d"])
+def test_oracle_relabelled_stiffness_positive_and_symmetric(kw):
+    """The reference's self-test on relabelled elements: the back-map of the stress is the
+    adjoint of the strain map, so K stays self-adjoint with a positive diagonal (a
+    transcription error in either map breaks the symmetry)."""
+    spec = synth.annulus_domain(n_theta=1, n_r=1, source=False, n_receivers=0, **kw)
+    assert len(spec.prt_elem) == 1
+    K = _stiffness_matrix(spec)
+    assert (np.diag(K) > 0).all()
+    scale = np.abs(K).max()
+    assert np.abs(K - K.T).max() <= 1e-8 * scale
