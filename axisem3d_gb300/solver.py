@@ -316,6 +316,12 @@ class Simulation:
         if emode != "off":
             raise ValueError("ExodusModel::buildInparam || MODEL_3D_ELLIPTICITY_MODE: only 'off' (a spherical "
                              "Earth) is built.")
+        if _flag(par, "ATTENUATION") and _flag(par, "ATTENUATION_SPECFEM_LEGACY"):
+            raise ValueError("AttBuilder::buildInparam || ATTENUATION_SPECFEM_LEGACY: the SPECFEM SLS fit is "
+                             "not built; set it false.")
+        if _int_or(par, "MODEL_PLOT_SLICES_NUM", 0) > 0:
+            import warnings
+            warnings.warn("MODEL_PLOT_SLICES_NUM > 0: slice plots (SlicePlot) are not written by this solver")
         e3d = np.zeros(E, bool)
         props3 = {}
         if models:

@@ -599,3 +599,19 @@ def test_user_nr_field_and_refused_options(tmp_path_factory):
     (d / "inparam.model").write_text(m + "MODEL_3D_ELLIPTICITY_MODE full\nMODEL_3D_ELLIPTICITY_INVF 298.3\n")
     with pytest.raises(ValueError, match="ELLIPTICITY"):
         solver.Simulation(d).build()
+
+
+def test_legacy_attenuation_refused_and_slice_plots_warned(tmp_path_factory):
+    """ATTENUATION_SPECFEM_LEGACY (a different SLS fit, not built) stops the build; slice plots
+    (output only) give a warning."""
+    d = tmp_path_factory.mktemp("leg") / "input"
+    solver.write_inputs(d, mesh_kw=SMALL_MESH, steps=10, n_stations=2, seed=3, attenuation=True)
+    adv = (d / "inparam.advanced").read_text()
+    (d / "inparam.advanced").write_text(adv.replace("ATTENUATION_SPECFEM_LEGACY false", "ATTENUATION_SPECFEM_LEGACY true"))
+    with pytest.raises(ValueError, match="SPECFEM"):
+        solver.Simulation(d).build()
+    (d / "inparam.advanced").write_text(adv)
+    m = (d / "inparam.model").read_text()
+    (d / "inparam.model").write_text(m.replace("MODEL_PLOT_SLICES_NUM 0", "MODEL_PLOT_SLICES_NUM 1"))
+    with pytest.warns(UserWarning, match="slice plots"):
+        solver.Simulation(d).build()
