@@ -493,3 +493,37 @@ def test_oracle_relabelled_stiffness_positive_and_symmetric(kw):
     assert (np.diag(K) > 0).all()
     scale = np.abs(K).max()
     assert np.abs(K - K.T).max() <= 1e-8 * scale
+
+
+def test_oracle_elastic_energy_is_conserved():
+    """A source-free, non-attenuating elastic run (Newmark::solve on the FP64 oracle) keeps
+    its energy 1/2 v^T M v + 1/2 u^T K u bounded, without drift: the mass, the stiffness
+    and the update agree with one another (the Fourier inner product weighs order 0 once and
+    the others twice)."""
+    spec = synth.annulus_domain(seed=8, n_theta=3, n_r=2, nu=3, nu_random=True, nu_max=5, mat=MAT_TISO,
+                                source=False, n_receivers=0, stf_len=400, dt=0.05)
+    o = _oracle()(spec, double=True)
+    su, _ = synth.random_fields(spec, seed=9, scale=1e-6, decay=2.0)
+    o.set("displ", "solid", su)
+    so, _ = spec.point_offsets()
+    w = np.zeros(o.nsolid)
+    m = np.zeros(o.nsolid)
+    for p in range(spec.n_points):
+        na = spec.p_nr[p] // 2 + 1
+        ww = np.where(np.arange(na) == 0, 1.0, 2.0)
+        w[so[p]:so[p] + 3 * na] = np.repeat(ww, 3)
+        m[so[p]:so[p] + 3 * na] = 1.0 / float(spec.p_ms[spec.p_mslen[:p].sum()])
+    energies = []
+    for k in range(300):
+        o.step(1)
+        u, v = o.get("displ", "solid"), o.get("veloc", "solid")
+        o.set("stiff", "solid", np.zeros(o.nsolid, complex))
+        o.compute_stiff()
+        ku = -o.get("stiff", "solid")
+        kin = 0.5 * np.sum(w * m * np.abs(v) ** 2)
+        pot = 0.5 * np.sum(w * np.real(np.conj(u) * ku))
+        energies.append(kin + pot)
+    e = np.array(energies[20:])
+    assert e.min() > 0
+    assert (e.max() - e.min()) / e.mean() < 0.05
+    assert abs(e[-50:].mean() - e[:50].mean()) / e.mean() < 0.02
