@@ -10,7 +10,6 @@ Pre-computation is FP64 (geometry, materials, masses, normals, source, receivers
 from __future__ import annotations
 
 import math
-import os
 from dataclasses import dataclass
 from pathlib import Path
 

@@ -19,7 +19,7 @@ import numpy as np
 
 from . import attenuation as ATT
 from . import geometry as GEO
-from .spec import (ATT_CG4, ATT_FULL, ATT_NONE, MAT_ACOUSTIC, MAT_ISO, MAT_TISO, POINT_FLUID,
+from .spec import (ATT_CG4, ATT_NONE, MAT_ACOUSTIC, MAT_ISO, MAT_TISO, POINT_FLUID,
                    POINT_SOLID, POINT_SOLID_FLUID, DomainSpec)
 
 

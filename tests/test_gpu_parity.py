@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 from axisem3d_gb300 import synth
-from axisem3d_gb300.spec import ATT_CG4, ATT_FULL, ATT_NONE, MAT_ANISO, MAT_ISO, MAT_TISO
+from axisem3d_gb300.spec import ATT_CG4, ATT_FULL, MAT_ANISO, MAT_TISO
 
 pytestmark = pytest.mark.gpu
 
