@@ -1077,16 +1077,36 @@ class Simulation:
         return paths
 
     # ------------------------------------------------------------------ run
-    def run(self, domain=None, nsteps=None):
+    def run(self, domain=None, nsteps=None, log=None):
         """Newmark::solve through the library; with NU_WISDOM_LEARN on, learns the wisdom
-        during the loop and writes it to NU_WISDOM_LEARN_OUTPUT afterwards."""
+        during the loop and writes it to NU_WISDOM_LEARN_OUTPUT afterwards.  With
+        OPTION_LOOP_INFO_INTERVAL > 0 and a `log` callable, the steps run in chunks of that
+        many and each chunk reports simulation time, steps done and wall time elapsed /
+        remaining / total in hours, as Newmark.cpp:72-88 prints."""
+        import time
         from .capi import Ax3dDomain
         dom = domain or Ax3dDomain(self.spec)
         n = nsteps or self.nsteps
         lp = self.learn_parameters()
         if lp:
             dom.set_wisdom_learning(lp[0], lp[1])
-        dom.step(n)
+        interval = _int_or(self.par, "OPTION_LOOP_INFO_INTERVAL", 0) if log else 0
+        if interval <= 0:
+            dom.step(n)
+        else:
+            t0 = time.perf_counter()
+            done = 0
+            while done < n:
+                k = min(interval, n - done)
+                dom.step(k)
+                done += k
+                elapsed = (time.perf_counter() - t0) / 3600.0
+                total = elapsed / done * n
+                log(f"  SIMULATION TIME / sec     =   {-self.shift + done * self.dt}\n"
+                    f"  TIME STEP / TOTAL STEPS   =   {done} / {n} ({int(100.0 * done / n)}%)\n"
+                    f"  WALLTIME ELAPSED  / h     =   {elapsed}\n"
+                    f"  WALLTIME REMAINED / h     =   {total - elapsed}\n"
+                    f"  WALLTIME TOTAL    / h     =   {total}\n")
         if lp:
             self.dump_wisdom(dom, lp[2])
         seis = dom.seismograms(0, n)

@@ -615,3 +615,20 @@ def test_legacy_attenuation_refused_and_slice_plots_warned(tmp_path_factory):
     (d / "inparam.model").write_text(m.replace("MODEL_PLOT_SLICES_NUM 0", "MODEL_PLOT_SLICES_NUM 1"))
     with pytest.warns(UserWarning, match="slice plots"):
         solver.Simulation(d).build()
+
+
+def test_loop_info_reports_in_chunks(tmp_path_factory):
+    """OPTION_LOOP_INFO_INTERVAL: Simulation.run steps in chunks and reports each (the
+    Newmark::solve screen info); the result equals one uninterrupted run."""
+    from oracle.oracle_py import OracleDomain
+    d = tmp_path_factory.mktemp("loop") / "input"
+    solver.write_inputs(d, mesh_kw=SMALL_MESH, steps=25, hdur=20.0, n_stations=2, seed=3)
+    adv = (d / "inparam.advanced").read_text().replace("OPTION_LOOP_INFO_INTERVAL 1000", "OPTION_LOOP_INFO_INTERVAL 10")
+    (d / "inparam.advanced").write_text(adv)
+    sim = solver.Simulation(d)
+    spec = sim.build()
+    lines = []
+    rtz, dom = sim.run(domain=OracleDomain(spec), log=lines.append)
+    assert len(lines) == 3 and "25 / 25 (100%)" in lines[-1] and "10 / 25 (40%)" in lines[0]
+    ref, _ = sim.run(domain=OracleDomain(spec))
+    np.testing.assert_array_equal(rtz, ref)
