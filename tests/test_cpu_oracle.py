@@ -527,3 +527,20 @@ def test_oracle_elastic_energy_is_conserved():
     assert e.min() > 0
     assert (e.max() - e.min()) / e.mean() < 0.05
     assert abs(e[-50:].mean() - e[:50].mean()) / e.mean() < 0.02
+
+
+def test_oracle_empty_domain_steps():
+    """Edge case: a domain without points or elements is accepted and steps (the step
+    counter advances, no fields)."""
+    from axisem3d_gb300.spec import DomainSpec
+    z = lambda *s, dt=np.float32: np.zeros(s, dt)
+    spec = DomainSpec(dt=0.1, p_nr=z(0, dt=np.int32), p_kind=z(0, dt=np.int8), p_axial=z(0, dt=np.uint8),
+                      p_fsurf=z(0, dt=np.uint8), p_mslen=z(0, dt=np.int32), p_ms=z(0), p_mflen=z(0, dt=np.int32),
+                      p_mf=z(0), p_sflen=z(0, dt=np.int32), p_sfn=z(0, 3), p_sfni=z(0, 3), e_pts=z(0, 25, dt=np.int32),
+                      e_mat=z(0, dt=np.int8), e_axial=z(0, dt=np.uint8), e_in3d=z(0, dt=np.uint8), e_geo=z(0, 5, 25),
+                      e_trig=z(0, 4, 25), e_mofs=z(0, dt=np.int64), e_mod=z(0), e_att=z(0, dt=np.int8),
+                      e_aofs=z(0, dt=np.int64), e_attm=z(0), nsls=0, att_alpha=np.zeros(0), att_beta=np.zeros(0),
+                      att_gamma=np.zeros(0), att_do_kappa=True, stf=np.ones(5, np.float32))
+    o = _oracle()(spec)
+    o.step(3)
+    assert o.nsolid == 0 and o.nfluid == 0 and o.current_step == 4
