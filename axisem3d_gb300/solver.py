@@ -1090,6 +1090,8 @@ class Simulation:
         lp = self.learn_parameters()
         if lp:
             dom.set_wisdom_learning(lp[0], lp[1])
+        if _flag(self.par, "DEVELOP_RANDOMIZE_DISP0"):
+            self.randomize_displacement(dom)
         interval = _int_or(self.par, "OPTION_LOOP_INFO_INTERVAL", 0) if log else 0
         if interval <= 0:
             dom.step(n)
@@ -1111,6 +1113,39 @@ class Simulation:
             self.dump_wisdom(dom, lp[2])
         seis = dom.seismograms(0, n)
         return self.rotate(seis), dom
+
+    def randomize_displacement(self, dom, seed=0):
+        """DEVELOP_RANDOMIZE_DISP0 (Domain::initDisplTinyRandom, Domain.cpp:76-80;
+        SolidPoint::randomDispl): orders 0..2 of every point's displacement uniform in
+        [-1, 1] (real and imaginary) times 1e-30, masked like the points mask their fields
+        (order 0 real; on the axis only the orders and components that survive there).  A
+        seeded numpy generator replaces std::rand."""
+        rng = np.random.default_rng(seed)
+        spec = self.spec
+        so, fo = spec.point_offsets()
+        for phase, ofs, nc in (("solid", so, 3), ("fluid", fo, 1)):
+            n = dom.nsolid if phase == "solid" else dom.nfluid
+            if n == 0:
+                continue
+            u = np.zeros(n, complex)
+            for p in np.flatnonzero(ofs >= 0):
+                na = int(spec.p_nr[p]) // 2 + 1
+                k = min(3, na)
+                blk = (rng.uniform(-1, 1, (k, nc)) + 1j * rng.uniform(-1, 1, (k, nc))) * 1e-30
+                blk[0] = blk[0].real
+                if spec.p_nr[p] % 2 == 0 and k == na:
+                    blk[-1] = 0.0  # Nyquist
+                if spec.p_axial[p]:
+                    if nc == 3:
+                        blk[0, :2] = 0.0      # order 0: only z on the axis
+                        if k > 1:
+                            blk[1, 2] = 0.0   # order 1: no z; s and phi tied
+                            blk[1, 1] = 1j * blk[1, 0]
+                        blk[2:] = 0.0
+                    else:
+                        blk[1:] = 0.0
+                u[ofs[p]:ofs[p] + k * nc] = blk.ravel()
+            dom.set("displ", phase, u)
 
     def surface_records(self, dom, nsteps=None):
         """The whole-surface records of steps 0..nsteps-1 (one per OUT_STATIONS_RECORD_INTERVAL

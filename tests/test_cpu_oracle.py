@@ -544,3 +544,32 @@ def test_oracle_empty_domain_steps():
     o = _oracle()(spec)
     o.step(3)
     assert o.nsolid == 0 and o.nfluid == 0 and o.current_step == 4
+
+
+@pytest.mark.parametrize("kw", [dict(nu=1), dict(nu=2), dict(nu=2, prt=0.1)], ids=["nu1", "nu2", "nu2_prt1d"])
+def test_oracle_fluid_stiffness_positive_and_symmetric(kw):
+    """FluidElement::test (FluidElement.cpp:94-161) on the oracle: unit impulses of the
+    potential (2 for order 0) give a fluid stiffness with positive diagonal, self-adjoint."""
+    spec = synth.annulus_domain(n_theta=1, n_r=1, fluid_layers=(0,), source=False, n_receivers=0, **kw)
+    d = _oracle()(spec, double=True)
+    _, fo = spec.point_offsets()
+    idx = []
+    for p in range(spec.n_points):
+        na = spec.p_nr[p] // 2 + 1
+        for a in range(na):
+            if spec.p_axial[p] and a > 0:
+                continue
+            if spec.p_nr[p] % 2 == 0 and a == na - 1:
+                continue
+            idx.append((fo[p] + a, a))
+    n = d.nfluid
+    K = np.zeros((len(idx), len(idx)))
+    for j, (col, a) in enumerate(idx):
+        u = np.zeros(n, complex)
+        u[col] = 2.0 if a == 0 else 1.0
+        d.set("displ", "fluid", u)
+        d.set("stiff", "fluid", np.zeros(n, complex))
+        d.compute_stiff()
+        K[:, j] = -d.get("stiff", "fluid")[[c for c, _ in idx]].real
+    assert (np.diag(K) > 0).all()
+    assert np.abs(K - K.T).max() <= 1e-8 * np.abs(K).max()

@@ -632,3 +632,24 @@ def test_loop_info_reports_in_chunks(tmp_path_factory):
     assert len(lines) == 3 and "25 / 25 (100%)" in lines[-1] and "10 / 25 (40%)" in lines[0]
     ref, _ = sim.run(domain=OracleDomain(spec))
     np.testing.assert_array_equal(rtz, ref)
+
+
+def test_randomized_initial_displacement_with_null_source(tmp_path_factory):
+    """DEVELOP_RANDOMIZE_DISP0 with DEVELOP_NON_SOURCE_MODE (the reference's scaling-test
+    backends): a tiny random initial field, orders 0-2 only, makes a source-free run move."""
+    from oracle.oracle_py import OracleDomain
+    d = tmp_path_factory.mktemp("rnd") / "input"
+    solver.write_inputs(d, mesh_kw=SMALL_MESH, steps=20, hdur=20.0, n_stations=2, seed=3, nu=4)
+    adv = (d / "inparam.advanced").read_text().replace("DEVELOP_NON_SOURCE_MODE false", "DEVELOP_NON_SOURCE_MODE true")
+    (d / "inparam.advanced").write_text(adv + "DEVELOP_RANDOMIZE_DISP0 true\n")
+    sim = solver.Simulation(d)
+    spec = sim.build()
+    dom = OracleDomain(spec)
+    sim.randomize_displacement(dom)
+    u = dom.get("displ", "solid")
+    so, _ = spec.point_offsets()
+    p = int(np.flatnonzero((spec.p_nr >= 9) & (spec.p_kind == 0))[0])
+    blk = u[so[p]:so[p] + 3 * (spec.p_nr[p] // 2 + 1)].reshape(-1, 3)
+    assert np.abs(blk[:3]).max() > 0 and np.abs(blk[3:]).max() == 0 and np.abs(blk).max() <= 2e-30
+    rtz, _ = sim.run(domain=OracleDomain(spec))
+    assert 0 < np.abs(rtz).max() < 1e-25
