@@ -573,3 +573,48 @@ def test_oracle_fluid_stiffness_positive_and_symmetric(kw):
         K[:, j] = -d.get("stiff", "fluid")[[c for c, _ in idx]].real
     assert (np.diag(K) > 0).all()
     assert np.abs(K - K.T).max() <= 1e-8 * np.abs(K).max()
+
+
+@pytest.mark.parametrize("kw,phase", [(dict(fluid_layers=(1,), in3d=True, fluid3d=True, mass3d=True), "fluid"),
+                                      (dict(ocean="1d"), "solid"), (dict(ocean="3d"), "solid")],
+                         ids=["fluid_mass3d", "ocean1d", "ocean3d"])
+def test_oracle_mass_positive_and_symmetric(kw, phase):
+    """SolidPoint::test / FluidPoint::test (SolidPoint.cpp:98-161, FluidPoint.cpp:104-155) on
+    the oracle, point by point: unit stiffness impulses (2 for order 0) through one Newmark
+    update give the inverse-mass matrix, with positive diagonal and self-adjoint -- for a
+    phi-dependent (Mass3D) fluid mass and both ocean-load forms."""
+    spec = synth.annulus_domain(seed=5, n_theta=2, n_r=2, nu=3, nu_random=True, nu_max=6, source=False,
+                                n_receivers=0, **kw)
+    so, fo = spec.point_offsets()
+    ofs, nc = (so, 3) if phase == "solid" else (fo, 1)
+    if phase == "solid":
+        special = sorted(p for p in spec.oc_pt.tolist() if spec.p_kind[p] == 0)
+    else:
+        special = [int(p) for p in np.flatnonzero((spec.p_mflen > 1) & (spec.p_kind == 1))]
+    assert special
+    for p in special[:10]:
+        d = _oracle()(spec, double=True)
+        n = d.nsolid if phase == "solid" else d.nfluid
+        nr = int(spec.p_nr[p])
+        na = nr // 2 + 1
+        rows = []
+        for a in range(na):
+            if nr % 2 == 0 and a == na - 1:
+                continue
+            for c in range(nc):
+                if spec.p_axial[p] and ((nc == 3 and ((a == 0 and c != 2) or (a == 1 and c == 2) or a >= 2))
+                                        or (nc == 1 and a > 0)):
+                    continue
+                rows.append((a, c))
+        M = np.zeros((len(rows), len(rows)))
+        for j, (a, c) in enumerate(rows):
+            st = np.zeros(n, complex)
+            st[ofs[p] + nc * a + c] = 2.0 if a == 0 else 1.0
+            for which in ("displ", "veloc", "accel"):
+                d.set(which, phase, np.zeros(n, complex))
+            d.set("stiff", phase, st)
+            d.update_newmark()
+            acc = d.get("accel", phase)
+            M[:, j] = [acc[ofs[p] + nc * a1 + c1].real for a1, c1 in rows]
+        assert (np.diag(M) > 0).all(), p
+        assert np.abs(M - M.T).max() <= 1e-9 * np.abs(M).max(), p
