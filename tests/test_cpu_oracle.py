@@ -618,3 +618,45 @@ def test_oracle_mass_positive_and_symmetric(kw, phase):
             M[:, j] = [acc[ofs[p] + nc * a1 + c1].real for a1, c1 in rows]
         assert (np.diag(M) > 0).all(), p
         assert np.abs(M - M.T).max() <= 1e-9 * np.abs(M).max(), p
+
+
+def test_cpp_host_interface_compiles(tmp_path):
+    """include/ax3d.hpp (the C++ mirror of the reference's Domain over the C-ABI) compiles as
+    C++17 with warnings as errors, and a program using every loop body links against
+    libax3d.so (no GPU needed to compile and link)."""
+    import shutil
+    if not shutil.which("g++"):
+        pytest.skip("g++ not available")
+    lib = ROOT / "axisem3d_gb300/libax3d.so"
+    if not lib.exists():
+        from axisem3d_gb300 import build
+        build.build()
+    src = tmp_path / "host.cpp"
+    src.write_text("""#include "ax3d.hpp"
+#include <cstdio>
+int main(int argc, char **) {
+    if (argc < 2) return 0;  // compiled and linked only
+    ax3d_config cfg{};
+    cfg.npol = 4;
+    try {
+        ax3d::Domain dom(cfg);
+        dom.finalize();
+        dom.updateNewmark();
+        dom.applySource(0);
+        dom.computeStiff();
+        dom.coupleSolidFluid();
+        dom.record(0);
+        dom.solve(1);
+        std::printf("%d\\n", dom.currentStep());
+    } catch (const ax3d::Error &e) {
+        std::printf("%d %s\\n", e.code(), e.what());
+    }
+    return 0;
+}
+""")
+    res = subprocess.run(["g++", "-std=c++17", "-Wall", "-Wextra", "-Werror", str(src), "-I", str(ROOT / "include"),
+                          "-L", str(lib.parent), "-lax3d", f"-Wl,-rpath,{lib.parent}", "-o", str(tmp_path / "host")],
+                         capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr
+    run = subprocess.run([str(tmp_path / "host")], capture_output=True, text=True)
+    assert run.returncode == 0
