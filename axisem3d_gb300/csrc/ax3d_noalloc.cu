@@ -12,7 +12,9 @@
 // points, one Fourier order count Nu for all points (nr = 2 Nu + 1).  Arithmetic as
 // SolidElement::displToStiff + gatherStiffFromElement (SolidElement.cpp:43-65, 404-443;
 // SolidPoint.cpp:197-209), with the same per-point operators as the domain path.
+#include <cstdint>
 #include <cstring>
+#include <mutex>
 #include <string>
 
 #include "../../include/ax3d.h"
@@ -28,10 +30,17 @@ using namespace ax3d;
 constexpr size_t NOALLOC_SCRATCH_BYTES = (size_t)AX3D_NOALLOC_SCRATCH_MIB << 20;
 static __device__ __align__(256) float2 g_noalloc_scratch[NOALLOC_SCRATCH_BYTES / sizeof(float2)];
 
-// Device address of g_noalloc_scratch, looked up once per device (host code only holds
-// a host-side stand-in for the symbol, which no kernel may be given).
+// Per-device set-up, done once with that device current: the device address of
+// g_noalloc_scratch (host code only holds a host-side stand-in for the symbol, which no
+// kernel may be given), the SM count, and the two kernels loaded.  Guarded by a mutex, so
+// two host threads making their first call on one device do not race on the slot.
 constexpr int MAX_DEVICES = 64;
-float2 *g_scratch_ptr[MAX_DEVICES] = {nullptr};
+struct DevSetup {
+    float2 *scratch = nullptr;
+    int sms = 0;
+};
+DevSetup g_dev[MAX_DEVICES];
+std::mutex g_dev_mu;
 
 struct GMats {
     float g[2][25];  // [0] GLL, [1] GLJ(0,1); passed by value, so no copy to the device is needed
@@ -108,6 +117,38 @@ int fail(int code, const std::string &m) {
     return code;
 }
 
+// Resolves the scratch address and SM count of the current device and forces the module
+// (the scratch array and both kernels) onto it, under lazy module loading too: after this
+// the entry point touches no allocator of its own.
+int device_setup(DevSetup &out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return fail(AX3D_ERR_CUDA, std::string("cudaGetDevice || ") + cudaGetErrorString(e));
+    if (dev < 0 || dev >= MAX_DEVICES)
+        return fail(AX3D_ERR_UNSUPPORTED, "ax3d_compute_stiff_iso1d_noalloc || device index");
+    std::lock_guard<std::mutex> lk(g_dev_mu);
+    DevSetup &d = g_dev[dev];
+    if (!d.scratch) {
+        cudaFuncAttributes fa;
+        e = cudaFuncGetAttributes(&fa, k_noalloc_elem);
+        if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_noalloc_gather);
+        if (e != cudaSuccess)
+            return fail(AX3D_ERR_CUDA, std::string("cudaFuncGetAttributes || ") + cudaGetErrorString(e));
+        int sms = 0;
+        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess)
+            return fail(AX3D_ERR_CUDA, std::string("cudaDeviceGetAttribute || ") + cudaGetErrorString(e));
+        void *ptr = nullptr;
+        e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess)
+            return fail(AX3D_ERR_CUDA, std::string("cudaGetSymbolAddress || ") + cudaGetErrorString(e));
+        d.sms = sms > 0 ? sms : 1;
+        d.scratch = static_cast<float2 *>(ptr);
+    }
+    out = d;
+    return AX3D_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -120,26 +161,22 @@ int ax3d_compute_stiff_iso1d_noalloc(int32_t nelem, int32_t nu, const int32_t *d
                                      const double *g_glj, void *stream) {
     if (nelem < 0 || nu < 0 || npoints < 0)
         return fail(AX3D_ERR_ARG, "ax3d_compute_stiff_iso1d_noalloc || negative size");
+    // set-up first, so that a call with nelem = 0 at start-up loads everything
+    DevSetup d;
+    int rc = device_setup(d);
+    if (rc != AX3D_OK) return rc;
     if (nelem == 0 || npoints == 0) return AX3D_OK;
     if (!d_points || !d_axial || !d_geometry || !d_lambda_mu || !d_gather_ptr || !d_gather_ref || !d_displ ||
         !d_stiff || !g_gll || !g_glj)
         return fail(AX3D_ERR_ARG, "ax3d_compute_stiff_iso1d_noalloc || null argument");
+    if (((uintptr_t)d_displ | (uintptr_t)d_stiff) & 7)
+        return fail(AX3D_ERR_ARG, "ax3d_compute_stiff_iso1d_noalloc || d_displ and d_stiff must be 8-byte aligned "
+                                  "(complex float pairs)");
     const size_t need = (size_t)nelem * NPE * ((size_t)nu + 1) * 3 * sizeof(float2);
     if (need > NOALLOC_SCRATCH_BYTES)
         return fail(AX3D_ERR_ARG, "ax3d_compute_stiff_iso1d_noalloc || element forces need " + std::to_string(need) +
                                       " bytes, more than the " + std::to_string(NOALLOC_SCRATCH_BYTES) +
                                       "-byte static scratch (nelem * 25 * (nu + 1) * 24 bytes)");
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return fail(AX3D_ERR_CUDA, std::string("cudaGetDevice || ") + cudaGetErrorString(e));
-    if (dev < 0 || dev >= MAX_DEVICES) return fail(AX3D_ERR_UNSUPPORTED, "ax3d_compute_stiff_iso1d_noalloc || device index");
-    if (!g_scratch_ptr[dev]) {  // first call on this device: resolve the scratch's device address
-        void *ptr = nullptr;
-        e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-        if (e != cudaSuccess)
-            return fail(AX3D_ERR_CUDA, std::string("cudaGetSymbolAddress || ") + cudaGetErrorString(e));
-        g_scratch_ptr[dev] = static_cast<float2 *>(ptr);
-    }
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     GMats G;
     for (int i = 0; i < 25; i++) {
@@ -147,14 +184,14 @@ int ax3d_compute_stiff_iso1d_noalloc(int32_t nelem, int32_t nu, const int32_t *d
         G.g[1][i] = (float)g_glj[i];
     }
     const int64_t items = (int64_t)nelem * (nu + 1);
-    int blocks = (int)std::min<int64_t>((items + 7) / 8, 152 * 16);
+    int blocks = (int)std::min<int64_t>((items + 7) / 8, (int64_t)d.sms * 16);
     k_noalloc_elem<<<blocks, 256, 0, s>>>(G, nelem, nu, d_points, d_axial, d_geometry, d_lambda_mu,
-                                           reinterpret_cast<const float2 *>(d_displ), g_scratch_ptr[dev]);
+                                           reinterpret_cast<const float2 *>(d_displ), d.scratch);
     const int64_t rows = (int64_t)npoints * (nu + 1);
-    blocks = (int)std::min<int64_t>((rows + 255) / 256, 152 * 32);
-    k_noalloc_gather<<<blocks, 256, 0, s>>>(npoints, nu, d_gather_ptr, d_gather_ref, g_scratch_ptr[dev],
+    blocks = (int)std::min<int64_t>((rows + 255) / 256, (int64_t)d.sms * 32);
+    k_noalloc_gather<<<blocks, 256, 0, s>>>(npoints, nu, d_gather_ptr, d_gather_ref, d.scratch,
                                              reinterpret_cast<float2 *>(d_stiff));
-    e = cudaGetLastError();
+    const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(AX3D_ERR_CUDA, std::string("launch || ") + cudaGetErrorString(e));
     return AX3D_OK;
 }

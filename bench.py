@@ -14,8 +14,9 @@ e2e    = the same through the C-ABI with host buffers: each step copies the
          displacement in from pinned host memory, steps, and copies it back, the copies
          streamed (ax3d_set_field_async / ax3d_get_field_async) so that they overlap the
          steps; the synchronous form is reported beside it.
-Reference arm (--impl reference): the CPU oracle port of the same loop, one process
-per host core over a static element partition, on a bounded sample.
+Reference arm (--impl reference): the CPU port of the same loop (the oracle's arithmetic
+with O(nr log nr) FP32 transforms, as the reference uses FFTW), one process per host
+core over a static element partition, on a bounded sample.
 """
 from __future__ import annotations
 
@@ -147,17 +148,13 @@ def allmax(world, x):
     return x
 
 
-def traffic_ratio():
-    """DRAM bytes per algorithmic byte of the element pass, from the committed ncu summary
-    (dram__bytes_read.sum + dram__bytes_write.sum of every element launch of one step of
-    the 20,000-element case, which has the benchmark's distributions): the full workload's
-    traffic is this ratio times its algorithmic bytes."""
-    p = ROOT / "profiles" / "k_elem_phys_dram_20k.md"
-    if p.exists():
-        for line in p.read_text().splitlines():
-            if line.startswith("dram bytes per algorithmic byte:"):
-                return float(line.split(":")[1].split()[0])
-    return None
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per algorithmic byte of the
+# element pass, measured by ncu over every element launch of one step of the
+# 20,000-element case of this workload (same distributions, ~5.5 GB of element data, far
+# above L2).  The 200,000-element workload is too large to capture with more than one ncu
+# pass; its traffic grows in proportion to the elements processed, so it is this ratio
+# times its algorithmic bytes.  Re-measured whenever the element kernel changes.
+TRAFFIC_PER_ALGO_BYTE = 0.889
 
 
 def peaks():
@@ -169,24 +166,34 @@ def peaks():
 
 
 # ------------------------------------------------------------------ CPU (oracle) arm
+# The CPU baseline is the oracle's loop (the reference's per-element arithmetic) built with
+# O(nr log nr) FP32 transforms in place of the checker's exact DFT, as the reference runs
+# FFTW plans (oracle/ax3d_fft.hpp): kind "port", variant "port-fft".  One process per host core, each on its
+# own partition of elements drawn from the workload's distributions (one MPI rank per core
+# in the reference).
 def _cpu_worker(a):
-    """Build one partition sample and time the oracle's loop body on it."""
+    """Build one partition sample and time the CPU baseline's loop body on it."""
     seed, n_elem, att, steps = a
-    import numpy as _np  # noqa
     sys.path.insert(0, str(ROOT))
     from axisem3d_gb300 import workloads as W
     from oracle.oracle_py import OracleDomain
     spec = W.element_benchmark(n_elem=n_elem, seed=seed, att=att_kind(att))
-    d = OracleDomain(spec)
+    d = OracleDomain(spec, fft=True)
     d.set("displ", "solid", W.benchmark_displacement(spec, seed=seed + 1).astype(np.complex128))
-    d.step(1)  # first touch
+    d.step(1)  # first touch, transform plans
     t0 = time.perf_counter()
     d.step(steps)
     dt = time.perf_counter() - t0
-    return W.updates_per_step(spec) * steps, dt
+    return W.updates_per_step(spec) * steps, dt, spec.element_nr().tolist()
 
 
-def cpu_baseline(att, cores, sample, steps=1, seed=1000):
+def nr_histogram(nr):
+    """Quartiles and mean of the sample's ring sizes, for the record."""
+    q = np.percentile(np.asarray(nr), [0, 25, 50, 75, 100])
+    return f"nr mean {float(np.mean(nr)):.1f}, quartiles {'/'.join(str(int(x)) for x in q)}"
+
+
+def cpu_baseline(att, cores, sample, steps=2, seed=1000):
     import multiprocessing as mp
     from oracle.oracle_py import build_oracle
     build_oracle()
@@ -195,18 +202,21 @@ def cpu_baseline(att, cores, sample, steps=1, seed=1000):
         res = pool.map(_cpu_worker, [(seed + 7 * i, sample, att, steps) for i in range(cores)])
     upd = sum(r[0] for r in res)
     wall = max(r[1] for r in res)
-    return upd / wall, dict(cores=cores, sample=f"{cores} partitions x {sample} elements x {steps} step(s), "
-                            f"same Nu/material distribution, seeds {seed}..", wall_s=wall)
+    nrs = [x for r in res for x in r[2]]
+    return upd / wall, dict(cores=cores, sample=f"FFT port: {cores} partitions x {sample} elements x {steps} step(s) of the "
+                            f"same Nu / material distributions (seeds {seed}..; {nr_histogram(nrs)}; the 200,000-"
+                            f"element workload: nr mean ~144)", wall_s=wall)
+
+
+CPU_SAMPLE = 160  # elements per core: ~10-30 s of CPU work per call
 
 
 def run_reference(args, world, rank):
     if rank != 0:
         return
     cores = os.cpu_count() or 1
-    sample = args.cpu_sample or 24
+    sample = args.cpu_sample or CPU_SAMPLE
     vals = []
-    for _ in range(args.warmup):
-        pass  # each oracle partition does its own first-touch step
     for _ in range(max(1, min(args.steps, 3))):
         v, info = cpu_baseline(args.att, cores, sample)
         vals.append(v)
@@ -217,10 +227,10 @@ def run_reference(args, world, rank):
             "config": {"workload": f"element stiffness batching, {args.elements} TI elements, Nu 8-256 "
                                    f"log-uniform, 3 SLS {args.att}, 3-D (physical-space) material"},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": info["cores"], "kind": "port",
-                             "sample": info["sample"]},
+                             "variant": "port-fft", "sample": info["sample"]},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "note": "the reference (C++/Eigen/FFTW/MPI) does not build here; the CPU oracle port of the "
-                    "same loop is timed, one process per core"}
+            "note": "the reference (C++/Eigen/FFTW/MPI) does not build here; the CPU port of the same loop "
+                    "with O(nr log nr) FP32 transforms is timed, one process per core"}
     print(json.dumps(line), flush=True)
 
 
@@ -299,10 +309,12 @@ def run_gb300(args, world, rank, local):
     cpu = None
     if not args.no_cpu_baseline:
         try:
-            v, info = cpu_baseline(args.att, os.cpu_count() or 1, args.cpu_sample or 24)
-            cpu = {"value": v, "unit": UNIT, "cores": info["cores"], "kind": "port", "sample": info["sample"]}
+            v, info = cpu_baseline(args.att, os.cpu_count() or 1, args.cpu_sample or CPU_SAMPLE)
+            cpu = {"value": v, "unit": UNIT, "cores": info["cores"], "kind": "port", "variant": "port-fft",
+                   "sample": info["sample"]}
         except Exception as e:  # the CPU leg must not hide the GPU number
-            cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"failed: {e}"}
+            cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "variant": "port-fft",
+                   "sample": f"failed: {e}"}
     line = {
         "metric": METRIC, "value": upd * args.steps * world / dev_s_max, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_s_max * 1e3 / args.steps,
@@ -314,7 +326,7 @@ def run_gb300(args, world, rank, local):
                    "updates_per_step": upd, "parallelism": f"replicas x{world}",
                    "l2": "working set > L2 (no flush needed)"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": (tr * abytes if (tr := traffic_ratio()) else None),
+                     "frac": achieved / peak, "traffic": (tr * abytes if (tr := TRAFFIC_PER_ALGO_BYTE) else None),
                      "traffic_unit": "bytes per step (ncu DRAM bytes per algorithmic byte x algorithmic bytes)",
                      "peak_source": src,
                      "kernel": "element stiffness (k_elem_phys, all buckets)",

@@ -299,13 +299,17 @@ int ax3d_destroy(ax3d_domain *d);
                  ascending element order (the order the reference's element loop sums in)
      d_displ, d_stiff [npoints][nu + 1][3] complex
      g_gll, g_glj host [25] G matrices (as ax3d_config).
+   d_displ and d_stiff must be 8-byte aligned (AX3D_ERR_ARG otherwise).
    Runs asynchronously on `stream` (a cudaStream_t, NULL = default stream).  Returns
    AX3D_ERR_ARG without launching when nelem * 25 * (nu + 1) * 24 bytes exceeds the
-   scratch.  The first call on a device resolves the scratch's device address
-   (cudaGetSymbolAddress) with that device current; make it before any stream capture.
-   All calls share the one scratch: calls that overlap on the GPU (two streams, two
-   threads) race and must be serialised by the caller.  The scratch keeps the last
-   call's contents; every entry a call reads is written by the same call first. */
+   scratch.  Set-up: the first call on a device, with that device current, loads the
+   scratch array and the two kernels onto it (even under lazy module loading) and looks up
+   the scratch's device address (cudaGetSymbolAddress) and the SM count; a call with
+   nelem = 0 does only this.  Make one such call per device at start-up, before the
+   caller's pool takes the device memory and before any stream capture; later calls then
+   allocate nothing.  All calls share the one scratch: calls that overlap on the GPU (two
+   streams, two threads) race and must be serialised by the caller.  The scratch keeps the
+   last call's contents; every entry a call reads is written by the same call first. */
 int ax3d_compute_stiff_iso1d_noalloc(int32_t nelem, int32_t nu, const int32_t *d_points,
                                      const uint8_t *d_axial, const float *d_geometry,
                                      const float *d_lambda_mu, int32_t npoints,

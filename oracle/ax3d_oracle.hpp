@@ -27,7 +27,12 @@
 #include <stdexcept>
 #include <string>
 #include <deque>
+#include <type_traits>
 #include <vector>
+
+#ifdef AX3D_ORACLE_FFT
+#include "ax3d_fft.hpp"
+#endif
 
 namespace axo {
 
@@ -267,17 +272,38 @@ struct Oracle {
     }
 
     // ================= FFT (FFTW conventions) =================
+    // cos / sin (2 pi m / nr), m = 0..nr-1, in double: the same values the sums below would
+    // compute term by term (their angle is 2 pi ((k a) mod nr) / nr), looked up instead.
+    struct Twiddles {
+        int nr = 0;
+        std::vector<double> c, s;
+    };
+    static const Twiddles &twiddles(int nr) {
+        thread_local Twiddles t;
+        if (t.nr != nr) {
+            t.nr = nr;
+            t.c.resize(nr);
+            t.s.resize(nr);
+            for (int m = 0; m < nr; m++) {
+                const double th = 2. * M_PI * (double)m / nr;
+                t.c[m] = std::cos(th);
+                t.s[m] = std::sin(th);
+            }
+        }
+        return t;
+    }
     // C2R: x_k = Re X_0 + 2 sum_{a=1}^{Nu'} Re(X_a e^{+2 pi i k a / nr}), Nu' = Nu - nyquist;
     // the Nyquist order enters with weight 1 (zero wherever the reference uses it).
     static void c2r(const C *X, int nr, Real *x, int stride_in = 1) {
         int nu = nr / 2;
+        const Twiddles &T = twiddles(nr);
         for (int k = 0; k < nr; k++) {
             double acc = (double)X[0].real();
             for (int a = 1; a <= nu; a++) {
-                double th = 2. * M_PI * (double)((int64_t)k * a % nr) / nr;
+                const int m = (int)((int64_t)k * a % nr);
                 double w = (nr % 2 == 0 && a == nu) ? 1. : 2.;
                 const C &v = X[(size_t)a * stride_in];
-                acc += w * ((double)v.real() * std::cos(th) - (double)v.imag() * std::sin(th));
+                acc += w * ((double)v.real() * T.c[m] - (double)v.imag() * T.s[m]);
             }
             x[k] = (Real)acc;
         }
@@ -285,15 +311,40 @@ struct Oracle {
     // R2C scaled by 1/nr: X_a = (1/nr) sum_k x_k e^{-2 pi i k a / nr}, a = 0..Nu.
     static void r2c(const Real *x, int nr, C *X, int stride_out = 1) {
         int nu = nr / 2;
+        const Twiddles &T = twiddles(nr);
         for (int a = 0; a <= nu; a++) {
             double re = 0., im = 0.;
             for (int k = 0; k < nr; k++) {
-                double th = 2. * M_PI * (double)((int64_t)k * a % nr) / nr;
-                re += (double)x[k] * std::cos(th);
-                im -= (double)x[k] * std::sin(th);
+                const int m = (int)((int64_t)k * a % nr);
+                re += (double)x[k] * T.c[m];
+                im -= (double)x[k] * T.s[m];
             }
             X[(size_t)a * stride_out] = C((Real)(re / nr), (Real)(im / nr));
         }
+    }
+
+    // Two columns at once.  The checker transforms each by the exact DFT above; the timed
+    // CPU baseline (built with AX3D_ORACLE_FFT, Real = float) by one O(nr log nr) complex
+    // FFT of the pair (ax3d_fft.hpp), as FFTW's many-column plans serve FieldFFT.
+    static void c2r_pair(const C *X1, const C *X2, int nr, Real *x1, Real *x2) {
+#ifdef AX3D_ORACLE_FFT
+        if constexpr (std::is_same_v<Real, float>) {
+            axfft::c2r_pair(X1, X2, 1, nr, x1, x2);
+            return;
+        }
+#endif
+        c2r(X1, nr, x1);
+        c2r(X2, nr, x2);
+    }
+    static void r2c_pair(const Real *x1, const Real *x2, int nr, C *X1, C *X2) {
+#ifdef AX3D_ORACLE_FFT
+        if constexpr (std::is_same_v<Real, float>) {
+            axfft::r2c_pair(x1, x2, nr, X1, X2, 1);
+            return;
+        }
+#endif
+        r2c(x1, nr, X1);
+        r2c(x2, nr, X2);
     }
 
     // ================= Gradient (SOLVER/src/core/element/grad/Gradient.cpp) =================
@@ -836,12 +887,16 @@ struct Oracle {
             // physical space (3D material): FieldFFT::transformF2P -> stress -> transformP2F
             const int nr = e.nr;
             std::vector<Real> sR((size_t)6 * nPE * nr), tR((size_t)6 * nPE * nr);
-            std::vector<C> col(n);
-            for (int c = 0; c < 6; c++)
-                for (int p = 0; p < nPE; p++) {
-                    for (int a = 0; a < n; a++) col[a] = strain[a][c][p];
-                    c2r(col.data(), nr, &sR[((size_t)c * nPE + p) * nr]);
+            std::vector<C> col(n), col2(n);
+            // columns i = c * 25 + p, two at a time (150 columns, 75 pairs)
+            for (int i = 0; i < 6 * nPE; i += 2) {
+                const int c1 = i / nPE, p1 = i % nPE, c2 = (i + 1) / nPE, p2 = (i + 1) % nPE;
+                for (int a = 0; a < n; a++) {
+                    col[a] = strain[a][c1][p1];
+                    col2[a] = strain[a][c2][p2];
                 }
+                c2r_pair(col.data(), col2.data(), nr, &sR[(size_t)i * nr], &sR[(size_t)(i + 1) * nr]);
+            }
             const Real *md = e.mod.data();
             for (int k = 0; k < nr; k++)
                 for (int p = 0; p < nPE; p++) {
@@ -864,11 +919,14 @@ struct Oracle {
                     }
                     for (int c = 0; c < 6; c++) tR[((size_t)c * nPE + p) * nr + k] = sig[c];
                 }
-            for (int c = 0; c < 6; c++)
-                for (int p = 0; p < nPE; p++) {
-                    r2c(&tR[((size_t)c * nPE + p) * nr], nr, col.data());
-                    for (int a = 0; a < n; a++) stress[a][c][p] = col[a];
+            for (int i = 0; i < 6 * nPE; i += 2) {
+                const int c1 = i / nPE, p1 = i % nPE, c2 = (i + 1) / nPE, p2 = (i + 1) % nPE;
+                r2c_pair(&tR[(size_t)i * nr], &tR[(size_t)(i + 1) * nr], nr, col.data(), col2.data());
+                for (int a = 0; a < n; a++) {
+                    stress[a][c1][p1] = col[a];
+                    stress[a][c2][p2] = col2[a];
                 }
+            }
         }
         force.assign((size_t)n * 3 * nPE, C(0));
         for (int a = 0; a < n; a++) {

@@ -273,3 +273,17 @@ extern "C" size_t axo_last_error(char *buf, size_t len) {
     }
     return g_err.size();
 }
+
+#ifdef AX3D_ORACLE_FFT
+// The CPU baseline's transforms alone, for the test that checks them against the exact
+// DFT: two Hermitian columns (orders 0..nr/2, interleaved complex float) to two real
+// columns of nr samples, and back (x 1/nr).
+extern "C" int axf_c2r_pair(int32_t nr, const float *X1, const float *X2, float *x1, float *x2) {
+    axfft::c2r_pair(reinterpret_cast<const axfft::cf *>(X1), reinterpret_cast<const axfft::cf *>(X2), 1, nr, x1, x2);
+    return 0;
+}
+extern "C" int axf_r2c_pair(int32_t nr, const float *x1, const float *x2, float *X1, float *X2) {
+    axfft::r2c_pair(x1, x2, nr, reinterpret_cast<axfft::cf *>(X1), reinterpret_cast<axfft::cf *>(X2), 1);
+    return 0;
+}
+#endif

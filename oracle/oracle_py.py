@@ -1,8 +1,10 @@
 """Python binding of the CPU oracle (TEST INFRASTRUCTURE ONLY).
 
-Loaded only by tests/, __graft_entry__.smoke() and the cpu_baseline leg of bench.py.
-OracleDomain drives oracle/_build/libax3d_oracle.so through the same Domain API as
-axisem3d_gb300.capi.Ax3dDomain, in FP32 (the reference's default Real) or FP64.
+Loaded only by tests/, __graft_entry__.smoke() and the CPU legs of bench.py.
+OracleDomain drives oracle/_build/libax3d_oracle.so (the checker: exact DFT) through the
+same Domain API as axisem3d_gb300.capi.Ax3dDomain, in FP32 (the reference's default Real)
+or FP64; with fft=True it drives oracle/_build/libax3d_cpufft.so instead, the same loop
+with O(nr log nr) FP32 transforms, which bench.py times as the CPU baseline.
 """
 from __future__ import annotations
 
@@ -16,27 +18,54 @@ from axisem3d_gb300.capi import _DomainBase, bind
 
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "libax3d_oracle.so"
-_lib = None
+LIB_FFT = HERE / "_build" / "libax3d_cpufft.so"
+_libs = {}
 
 
 def build_oracle() -> Path:
-    subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+    subprocess.run(["make", "-s", "-j2", "-C", str(HERE)], check=True)
     return LIB
 
 
-def load_oracle() -> C.CDLL:
-    global _lib
-    if _lib is None:
-        srcs = [HERE / "ax3d_oracle.hpp", HERE / "ax3d_oracle_capi.cpp"]
-        if not LIB.exists() or any(s.stat().st_mtime > LIB.stat().st_mtime for s in srcs):
+def load_oracle(fft: bool = False) -> C.CDLL:
+    if fft not in _libs:
+        path = LIB_FFT if fft else LIB
+        srcs = [HERE / "ax3d_oracle.hpp", HERE / "ax3d_oracle_capi.cpp", HERE / "ax3d_fft.hpp"]
+        if not path.exists() or any(s.stat().st_mtime > path.stat().st_mtime for s in srcs):
             build_oracle()
-        lib = C.CDLL(str(LIB))
+        lib = C.CDLL(str(path))
         bind(lib, "axo_", C.POINTER(C.c_double), extra_double_io=True)
         bind(lib, "axod_", C.POINTER(C.c_double), extra_double_io=True)
         lib.axo_last_error.argtypes = [C.c_char_p, C.c_size_t]
         lib.axo_last_error.restype = C.c_size_t
-        _lib = lib
-    return _lib
+        if fft:
+            for n in ("axf_c2r_pair", "axf_r2c_pair"):
+                getattr(lib, n).argtypes = [C.c_int32] + [C.POINTER(C.c_float)] * 4
+        _libs[fft] = lib
+    return _libs[fft]
+
+
+def fft_pair(nr: int, X1: np.ndarray, X2: np.ndarray):
+    """The CPU baseline's C2R of two Hermitian columns (orders 0..nr/2) -> two real columns."""
+    lib = load_oracle(fft=True)
+    a = np.ascontiguousarray(X1, np.complex64)
+    b = np.ascontiguousarray(X2, np.complex64)
+    x1, x2 = np.zeros(nr, np.float32), np.zeros(nr, np.float32)
+    f = lambda v: v.ctypes.data_as(C.POINTER(C.c_float))
+    lib.axf_c2r_pair(nr, f(a.view(np.float32)), f(b.view(np.float32)), f(x1), f(x2))
+    return x1, x2
+
+
+def ifft_pair(x1: np.ndarray, x2: np.ndarray):
+    """The CPU baseline's R2C (x 1/nr) of two real columns -> orders 0..nr/2 of each."""
+    lib = load_oracle(fft=True)
+    nr = len(x1)
+    a = np.ascontiguousarray(x1, np.float32)
+    b = np.ascontiguousarray(x2, np.float32)
+    X1, X2 = np.zeros(nr // 2 + 1, np.complex64), np.zeros(nr // 2 + 1, np.complex64)
+    f = lambda v: v.ctypes.data_as(C.POINTER(C.c_float))
+    lib.axf_r2c_pair(nr, f(a), f(b), f(X1.view(np.float32)), f(X2.view(np.float32)))
+    return X1, X2
 
 
 class OracleDomain(_DomainBase):
@@ -46,7 +75,20 @@ class OracleDomain(_DomainBase):
     field_dtype = np.float64
     field_ctype = C.c_double
 
-    def __init__(self, spec, double: bool = False):
+    def __init__(self, spec, double: bool = False, fft: bool = False):
+        if double and fft:
+            raise ValueError("the FFT CPU baseline is FP32 only")
         self.prefix = "axod_" if double else "axo_"
-        self.lib = load_oracle()
+        self.lib = load_oracle(fft=fft)
         self._build(spec, 0, with_first=False)
+
+
+def seismograms_of_inputs(input_dir, nsteps: int, double: bool = False, kahan: bool = False) -> np.ndarray:
+    """Build the domain of a parfile directory and run the oracle for nsteps; returns the
+    seismograms [step][receiver][component].  A module-level function, so that tests can
+    run it in spawned worker processes beside the GPU run."""
+    from axisem3d_gb300 import solver
+    spec = solver.Simulation(input_dir).build(kahan=kahan)
+    o = OracleDomain(spec, double=double)
+    o.step(nsteps)
+    return o.seismograms(0, nsteps)

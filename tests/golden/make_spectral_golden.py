@@ -11,7 +11,9 @@ import re
 import sys
 from pathlib import Path
 
-ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+if len(sys.argv) != 2:
+    sys.exit("usage: make_spectral_golden.py <path of the AxiSEM3D checkout>")
+ref = Path(sys.argv[1])
 src = (ref / "SOLVER/src/preloop/spectral/SpectralConstants.cpp").read_text()
 out = {}
 for name in ("pgll_4", "pglj_4", "wgll_4", "wglj_4", "Ggll_4", "Gglj_4"):

@@ -660,3 +660,49 @@ int main(int argc, char **) {
     assert res.returncode == 0, res.stderr
     run = subprocess.run([str(tmp_path / "host")], capture_output=True, text=True)
     assert run.returncode == 0
+
+
+# ring sizes nr = 2 Nu + 1 of the GPU ring-size sweep, plus every length the benchmark's
+# Nu range 8-256 can produce and a few even ones
+RING_NR = sorted({2 * nu + 1 for nu in (8, 11, 18, 35, 65, 70, 100, 128, 150, 195, 254)}
+                 | set(range(17, 514, 2)) | {16, 50, 64, 144, 260, 512})
+
+
+def test_cpu_fft_baseline_transforms_match_exact_dft():
+    """The CPU baseline's O(nr log nr) FP32 transforms (mixed-radix Stockham, Bluestein for
+    large prime factors, two real columns per complex transform) against the exact DFT in
+    double with FFTW's conventions, relative L2 <= 1e-6 per column, both directions."""
+    from oracle.oracle_py import fft_pair, ifft_pair
+    rng = np.random.default_rng(5)
+    for nr in RING_NR:
+        n = nr // 2 + 1
+        X = (rng.standard_normal((2, n)) + 1j * rng.standard_normal((2, n))).astype(np.complex64)
+        x1, x2 = fft_pair(nr, X[0], X[1])
+        for got, spec in ((x1, X[0]), (x2, X[1])):
+            want = np.fft.irfft(spec.astype(np.complex128), nr) * nr  # reads Re of orders 0 and nr/2 only
+            assert np.linalg.norm(got - want) <= 1e-6 * np.linalg.norm(want), nr
+        r = rng.standard_normal((2, nr)).astype(np.float32)
+        Y1, Y2 = ifft_pair(r[0], r[1])
+        for got, x in ((Y1, r[0]), (Y2, r[1])):
+            want = np.fft.rfft(x.astype(np.float64)) / nr
+            assert np.linalg.norm(got - want) <= 1e-6 * np.linalg.norm(want), nr
+
+
+@pytest.mark.parametrize("att", [ATT_CG4, ATT_FULL])
+def test_cpu_fft_baseline_loop_matches_oracle(att):
+    """The timed CPU baseline (the oracle's loop with the FFT transforms) against the
+    checker on the element benchmark's domain, Nu 8-256: element stiffness and two steps."""
+    from oracle.oracle_py import OracleDomain
+    from axisem3d_gb300 import workloads as W
+    spec = W.element_benchmark(n_elem=20, seed=9, att=att)
+    u0 = W.benchmark_displacement(spec, seed=8)
+    out = []
+    for fft in (False, True):
+        d = OracleDomain(spec, fft=fft)
+        d.set("displ", "solid", u0)
+        d.compute_stiff()
+        s = d.get("stiff", "solid")
+        d.step(2)
+        out.append((s, d.get("accel", "solid")))
+    for a, b in zip(out[0], out[1]):
+        assert np.linalg.norm(a - b) <= 1e-6 * np.linalg.norm(a)

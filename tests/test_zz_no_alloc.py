@@ -2,9 +2,11 @@
 
 Callers that cannot allocate device memory (their own pre-sized pool, or no allocation
 once a run has started) call ax3d_compute_stiff_iso1d_noalloc with their own buffers.
-This test gives it buffers made by torch, runs it twice in a row on different
-displacements and compares each result with ax3d_compute_stiff on the same mesh, at the
-tolerance of the other parity tests (relative L2 <= 1e-5).
+This test gives it buffers made by torch, makes the start-up call (nelem = 0) that loads
+the scratch and the kernels, runs it twice in a row on different displacements and
+compares each result with ax3d_compute_stiff on the same mesh and with the CPU oracle, at
+the tolerance of the other parity tests (relative L2 <= 1e-5); the device's free memory
+and torch's allocated bytes must not move across the second call.
 """
 import ctypes as C
 
@@ -56,20 +58,36 @@ def test_noalloc_stiffness_matches_domain_path():
     pg = gll.ctypes.data_as(C.POINTER(C.c_double))
     pj = glj.ctypes.data_as(C.POINTER(C.c_double))
 
-    for seed in (21, 22):  # two calls in a row share (and overwrite) the static scratch
+    from oracle.oracle_py import OracleDomain
+    orc = OracleDomain(spec)
+
+    # start-up call: loads the scratch and the kernels on this device, launches nothing
+    assert fn(0, nu, None, None, None, None, 0, None, None, None, None, pg, pj, None) == 0
+
+    for k, seed in enumerate((21, 22)):  # two calls in a row share (and overwrite) the static scratch
         u, _ = synth.random_fields(spec, seed=seed)
         dom.set("displ", "solid", u)
         dom.set("stiff", "solid", np.zeros_like(u))
         dom.compute_stiff()
         ref = dom.get("stiff")
+        orc.set("displ", "solid", u)
+        orc.set("stiff", "solid", np.zeros_like(u))
+        orc.compute_stiff()
         du = t(u.astype(np.complex64).view(np.float32), torch.float32)
         st = torch.zeros(2 * u.size, dtype=torch.float32, device=dev)
+        torch.cuda.synchronize()
+        free0, alloc0 = torch.cuda.mem_get_info(dev)[0], torch.cuda.memory_allocated(dev)
         rc = fn(ne, nu, pts.data_ptr(), axial.data_ptr(), geo.data_ptr(), lm.data_ptr(), npt, gptr.data_ptr(),
                 gref.data_ptr(), du.data_ptr(), st.data_ptr(), pg, pj, None)
         assert rc == 0, rc
         torch.cuda.synchronize()
+        if k == 1:  # after the first real call nothing on the device may grow
+            assert torch.cuda.mem_get_info(dev)[0] == free0
+            assert torch.cuda.memory_allocated(dev) == alloc0
         got = st.cpu().numpy().view(np.complex64)
         assert _rel(got, ref) <= TOL, _rel(got, ref)
+        want = orc.get("stiff", "solid")
+        assert _rel(got, want) <= TOL, _rel(got, want)
 
 
 def test_noalloc_rejects_oversized_batch():
@@ -86,3 +104,9 @@ def test_noalloc_rejects_oversized_batch():
     buf = C.create_string_buffer(512)
     lib.ax3d_last_error(buf, 512)
     assert b"static scratch" in buf.value
+    odd = C.c_void_p(20)  # not 8-byte aligned: refused before any launch
+    rc = fn(1, 1, dummy, dummy, dummy, dummy, 10, dummy, dummy, odd, dummy,
+            gll.ctypes.data_as(C.POINTER(C.c_double)), glj.ctypes.data_as(C.POINTER(C.c_double)), None)
+    assert rc == 1
+    lib.ax3d_last_error(buf, 512)
+    assert b"aligned" in buf.value
