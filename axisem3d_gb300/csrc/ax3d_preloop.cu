@@ -1,5 +1,13 @@
-// ax3d_preloop.cu -- pre-loop on the GPU in FP64: the elastic moduli of many elements at
-// once, Material::createElastic (SOLVER/src/preloop/physics/material/Material.cpp:280-379)
+// ax3d_preloop.cu -- pre-loop on the GPU in FP64.
+//
+// Geometry and mass: Quad::createGraident and Quad::formIntegralFactor
+// (SOLVER/src/preloop/mesh/Quad.cpp:509-547) over the spherical, linear and semi-spherical
+// mappings (SOLVER/src/preloop/spectral/mapping/SphericalMapping.cpp:9-78,
+// LinearMapping.cpp:8-44, SemiSphericalMapping.cpp:9-70, rotated by Mapping::sOrthogQ2,
+// Mapping.cpp:48-53), and Material::computeElementalMass (Material.cpp:233-255); one thread
+// per (element, GLL point) or (element, row, GLL point).
+//
+// Moduli: the elastic moduli of many elements at once, Material::createElastic (SOLVER/src/preloop/physics/material/Material.cpp:280-379)
 // with the attenuation split of AttBuilder::createAttenuation1D/3D
 // (SOLVER/src/preloop/physics/attenuation/AttBuilder.cpp:17-129), the per-sample factors of
 // AttAxiSEM::computeAttFactors (AttAxiSEM.cpp:14-57) and the CG4 weights of
@@ -125,6 +133,134 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// (s, z) and d(s, z)/d(xi, eta) of one GLL point; etype 0 spherical, 1 linear, 2 semi-spherical
+__device__ void map_jac(const double *nd, double xi, double eta, int etype, int co, double sz[2], double J[2][2]) {
+    // nd: (s0..s3, z0..z3) of the corners
+    if (etype == 1) {
+        const double xp = 1.0 + xi, xm = 1.0 - xi, ep = 1.0 + eta, em = 1.0 - eta;
+        const double shp[4] = {0.25 * xm * em, 0.25 * xp * em, 0.25 * xp * ep, 0.25 * xm * ep};
+        const double dx[4] = {-0.25 * em, 0.25 * em, 0.25 * ep, -0.25 * ep};
+        const double de[4] = {-0.25 * xm, -0.25 * xp, 0.25 * xp, 0.25 * xm};
+        for (int c = 0; c < 2; c++) {
+            double a = 0.0, b = 0.0, d = 0.0;
+            for (int k = 0; k < 4; k++) {
+                a += nd[4 * c + k] * shp[k];
+                b += nd[4 * c + k] * dx[k];
+                d += nd[4 * c + k] * de[k];
+            }
+            sz[c] = a;
+            J[c][0] = b;
+            J[c][1] = d;
+        }
+        return;
+    }
+    // rotation bringing the curved side to position 2: rows (q00, q01), (q10, q11)
+    const double Q[4][4] = {{-1, 0, 0, -1}, {0, -1, 1, 0}, {1, 0, 0, 1}, {0, 1, -1, 0}};
+    const double q00 = Q[co][0], q01 = Q[co][1], q10 = Q[co][2], q11 = Q[co][3];
+    const int i0 = (co + 2) & 3, i1 = (co + 3) & 3, i2 = co & 3, i3 = (co + 1) & 3;
+    auto rot = [&](int k, double &a, double &b) {
+        a = q00 * nd[k] + q01 * nd[4 + k];
+        b = q10 * nd[k] + q11 * nd[4 + k];
+    };
+    double s2n, z2n, s3n, z3n;
+    rot(i2, s2n, z2n);
+    rot(i3, s3n, z3n);
+    const double pi = 3.14159265358979323846;
+    double t2 = atan2(s2n, z2n), t3 = atan2(s3n, z3n);
+    if (t2 - t3 > pi) t3 += 2.0 * pi;  // XMath::makeClose
+    if (t3 - t2 > pi) t2 += 2.0 * pi;
+    const double r3 = sqrt(s3n * s3n + z3n * z3n);
+    const double x = q00 * xi + q01 * eta, y = q10 * xi + q11 * eta;
+    const double ao = ((1.0 - x) * t3 + (1.0 + x) * t2) / 2.0;
+    const double so = sin(ao), coo = cos(ao);
+    double s2, z2, K00, K01, K10, K11;
+    double s0n, z0n, s1n, z1n;
+    rot(i0, s0n, z0n);
+    rot(i1, s1n, z1n);
+    if (etype == 0) {
+        double t0 = atan2(s0n, z0n), t1 = atan2(s1n, z1n);
+        if (t0 - t1 > pi) t1 += 2.0 * pi;
+        if (t1 - t0 > pi) t0 += 2.0 * pi;
+        const double r0 = sqrt(s0n * s0n + z0n * z0n);
+        const double ai = ((1.0 - x) * t0 + (1.0 + x) * t1) / 2.0;
+        const double si = sin(ai), ci = cos(ai);
+        s2 = (1.0 + y) * r3 / 2.0 * so + (1.0 - y) * r0 / 2.0 * si;
+        z2 = (1.0 + y) * r3 / 2.0 * coo + (1.0 - y) * r0 / 2.0 * ci;
+        K00 = (1.0 + y) * r3 * (t2 - t3) / 4.0 * coo + (1.0 - y) * r0 * (t1 - t0) / 4.0 * ci;
+        K01 = 0.5 * (r3 * so - r0 * si);
+        K10 = -(1.0 + y) * r3 * (t2 - t3) / 4.0 * so - (1.0 - y) * r0 * (t1 - t0) / 4.0 * si;
+        K11 = 0.5 * (r3 * coo - r0 * ci);
+    } else {
+        s2 = (1.0 + y) * r3 / 2.0 * so + (1.0 - y) / 2.0 * (((1.0 - x) * s0n + (1.0 + x) * s1n) / 2.0);
+        z2 = (1.0 + y) * r3 / 2.0 * coo + (1.0 - y) / 2.0 * (((1.0 - x) * z0n + (1.0 + x) * z1n) / 2.0);
+        K00 = ((1.0 - y) * (s1n - s0n)) / 4.0 + ((1.0 + y) * r3 * (t2 - t3) * coo) / 4.0;
+        K01 = -((1.0 - x) * s0n + (1.0 + x) * s1n) / 4.0 + r3 / 2.0 * so;
+        K10 = ((1.0 - y) * (z1n - z0n)) / 4.0 - ((1.0 + y) * r3 * (t2 - t3) * so) / 4.0;
+        K11 = -((1.0 - x) * z0n + (1.0 + x) * z1n) / 4.0 + r3 / 2.0 * coo;
+    }
+    sz[0] = q00 * s2 + q10 * z2;  // Q^T (s2, z2)
+    sz[1] = q01 * s2 + q11 * z2;
+    // J = Q^T K Q
+    const double KQ00 = K00 * q00 + K01 * q10, KQ01 = K00 * q01 + K01 * q11;
+    const double KQ10 = K10 * q00 + K11 * q10, KQ11 = K10 * q01 + K11 * q11;
+    J[0][0] = q00 * KQ00 + q10 * KQ10;
+    J[0][1] = q00 * KQ01 + q10 * KQ11;
+    J[1][0] = q01 * KQ00 + q11 * KQ10;
+    J[1][1] = q01 * KQ01 + q11 * KQ11;
+}
+
+struct SpecNodes {
+    double xg[5], wg[5], xj[5], wj[5];
+};
+
+// nodes [n][2][4]; out geo [n][5][25], ifact [n][25], crds [n][25][2]
+__global__ void __launch_bounds__(256)
+    k_pre_geometry(int n, const double *__restrict__ nodes, const int8_t *__restrict__ etype,
+                   const int8_t *__restrict__ curved, const uint8_t *__restrict__ axial, SpecNodes S,
+                   double *__restrict__ geo, double *__restrict__ ifact, double *__restrict__ crds) {
+    const int64_t total = (int64_t)n * 25;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int e = (int)(t / 25), k = (int)(t - (int64_t)e * 25);
+        const int ip = k / 5, jp = k - 5 * (k / 5);
+        const bool ax = axial[e] != 0;
+        const double xi = ax ? S.xj[ip] : S.xg[ip], eta = S.xg[jp];
+        const double wxw = (ax ? S.wj[ip] : S.wg[ip]) * S.wg[jp];
+        double sz[2], J[2][2];
+        map_jac(nodes + (int64_t)e * 8, xi, eta, etype[e], curved[e], sz, J);
+        const double det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+        double *g = geo + (int64_t)e * 125;
+        g[k] = J[0][0] / det;
+        g[25 + k] = -J[0][1] / det;
+        g[50 + k] = -J[1][0] / det;
+        g[75 + k] = J[1][1] / det;
+        g[100 + k] = (ax && ip == 0) ? 0.0 : 1.0 / sz[0];
+        double f;
+        if (ax)
+            f = ip == 0 ? wxw * J[0][0] * det : wxw * sz[0] / (1.0 + xi) * det;
+        else
+            f = wxw * sz[0] * det;
+        ifact[t] = f;
+        crds[2 * t] = sz[0];
+        crds[2 * t + 1] = sz[1];
+    }
+}
+
+// Material::computeElementalMass: per (element, row, point) rho iFact, fluid iFact / (rho vp^2)
+__global__ void k_pre_mass(int n, const int32_t *__restrict__ rows, const int64_t *__restrict__ rofs,
+                           const double *__restrict__ ifact, const float *__restrict__ rho,
+                           const float *__restrict__ vp, const uint8_t *__restrict__ fluid,
+                           double *__restrict__ mass) {
+    for (int e = blockIdx.x; e < n; e += gridDim.x) {
+        const bool fl = fluid[e] != 0;
+        for (int t = threadIdx.x; t < rows[e] * 25; t += blockDim.x) {
+            const int64_t i = rofs[e] + t;
+            const double r = rho[i];
+            const double m = fl ? 1.0 / (r * ((double)vp[i] * (double)vp[i])) : r;
+            mass[i] = m * ifact[(int64_t)e * 25 + t % 25];
+        }
+    }
+}
+
 template <typename T>
 struct Dev {
     T *p = nullptr;
@@ -219,6 +355,130 @@ extern "C" int ax3d_precompute_elastic(int32_t device, int32_t n_elem, const int
     cudaSetDevice(prev_device);
     if (err != cudaSuccess) {
         g_pre_err = std::string("ax3d_precompute_elastic || CUDA: ") + cudaGetErrorString(err);
+        return AX3D_ERR_CUDA;
+    }
+    return AX3D_OK;
+}
+
+extern "C" int ax3d_precompute_geometry(int32_t device, int32_t n_elem, const double *nodes, const int8_t *etype,
+                                        const int8_t *curved_outer, const uint8_t *axial, const double *spectral,
+                                        double *geometry, double *ifact, double *crds) {
+    using namespace ax3d;
+    if (n_elem < 0 || (n_elem && (!nodes || !etype || !curved_outer || !axial || !spectral || !geometry || !ifact ||
+                                  !crds))) {
+        g_pre_err = "ax3d_precompute_geometry || bad argument";
+        return AX3D_ERR_ARG;
+    }
+    for (int e = 0; e < n_elem; e++)
+        if (etype[e] < 0 || etype[e] > 2 || curved_outer[e] < 0 || curved_outer[e] > 3) {
+            g_pre_err = "ax3d_precompute_geometry || mapping type must be 0..2 and curved side 0..3";
+            return AX3D_ERR_ARG;
+        }
+    if (n_elem == 0) return AX3D_OK;
+    SpecNodes S;
+    for (int i = 0; i < 5; i++) {
+        S.xg[i] = spectral[i];
+        S.wg[i] = spectral[5 + i];
+        S.xj[i] = spectral[10 + i];
+        S.wj[i] = spectral[15 + i];
+    }
+    int prev_device = 0;
+    cudaGetDevice(&prev_device);
+    cudaError_t err = cudaSetDevice(device);
+    Dev<double> d_nodes, d_geo, d_if, d_crds;
+    Dev<int8_t> d_et, d_co;
+    Dev<uint8_t> d_ax;
+    const size_t ne = (size_t)n_elem;
+    if (err == cudaSuccess) err = d_nodes.up(nodes, ne * 8);
+    if (err == cudaSuccess) err = d_et.up(etype, ne);
+    if (err == cudaSuccess) err = d_co.up(curved_outer, ne);
+    if (err == cudaSuccess) err = d_ax.up(axial, ne);
+    if (err == cudaSuccess) err = d_geo.up(nullptr, ne * 125);
+    if (err == cudaSuccess) err = d_if.up(nullptr, ne * 25);
+    if (err == cudaSuccess) err = d_crds.up(nullptr, ne * 50);
+    if (err == cudaSuccess) {
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+        const int grid = (int)std::min<int64_t>(((int64_t)ne * 25 + 255) / 256, (int64_t)std::max(sms, 1) * 8);
+        k_pre_geometry<<<grid, 256>>>(n_elem, d_nodes.p, d_et.p, d_co.p, d_ax.p, S, d_geo.p, d_if.p, d_crds.p);
+        err = cudaGetLastError();
+        if (err == cudaSuccess) err = cudaMemcpy(geometry, d_geo.p, ne * 125 * sizeof(double), cudaMemcpyDeviceToHost);
+        if (err == cudaSuccess) err = cudaMemcpy(ifact, d_if.p, ne * 25 * sizeof(double), cudaMemcpyDeviceToHost);
+        if (err == cudaSuccess) err = cudaMemcpy(crds, d_crds.p, ne * 50 * sizeof(double), cudaMemcpyDeviceToHost);
+    }
+    d_nodes.release();
+    d_et.release();
+    d_co.release();
+    d_ax.release();
+    d_geo.release();
+    d_if.release();
+    d_crds.release();
+    cudaSetDevice(prev_device);
+    if (err != cudaSuccess) {
+        g_pre_err = std::string("ax3d_precompute_geometry || CUDA: ") + cudaGetErrorString(err);
+        return AX3D_ERR_CUDA;
+    }
+    return AX3D_OK;
+}
+
+extern "C" int ax3d_precompute_mass(int32_t device, int32_t n_elem, const int32_t *rows, const double *ifact,
+                                    const float *rho, const float *vp, const uint8_t *fluid, double *mass) {
+    using namespace ax3d;
+    if (n_elem < 0 || (n_elem && (!rows || !ifact || !rho || !fluid || !mass))) {
+        g_pre_err = "ax3d_precompute_mass || bad argument";
+        return AX3D_ERR_ARG;
+    }
+    std::vector<int64_t> rofs(n_elem);
+    int64_t nrow = 0;
+    bool any_fluid = false;
+    for (int e = 0; e < n_elem; e++) {
+        if (rows[e] < 1) {
+            g_pre_err = "ax3d_precompute_mass || rows must be >= 1";
+            return AX3D_ERR_ARG;
+        }
+        rofs[e] = nrow * 25;
+        nrow += rows[e];
+        any_fluid |= fluid[e] != 0;
+    }
+    if (any_fluid && !vp) {
+        g_pre_err = "ax3d_precompute_mass || fluid elements need vp";
+        return AX3D_ERR_ARG;
+    }
+    if (n_elem == 0) return AX3D_OK;
+    const size_t nv = (size_t)nrow * 25;
+    int prev_device = 0;
+    cudaGetDevice(&prev_device);
+    cudaError_t err = cudaSetDevice(device);
+    Dev<int32_t> d_rows;
+    Dev<int64_t> d_rofs;
+    Dev<double> d_if, d_mass;
+    Dev<float> d_rho, d_vp;
+    Dev<uint8_t> d_fl;
+    if (err == cudaSuccess) err = d_rows.up(rows, n_elem);
+    if (err == cudaSuccess) err = d_rofs.up(rofs.data(), n_elem);
+    if (err == cudaSuccess) err = d_if.up(ifact, (size_t)n_elem * 25);
+    if (err == cudaSuccess) err = d_rho.up(rho, nv);
+    if (err == cudaSuccess) err = d_vp.up(any_fluid ? vp : nullptr, any_fluid ? nv : 1);
+    if (err == cudaSuccess) err = d_fl.up(fluid, n_elem);
+    if (err == cudaSuccess) err = d_mass.up(nullptr, nv);
+    if (err == cudaSuccess) {
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+        const int grid = std::min(n_elem, std::max(sms, 1) * 16);
+        k_pre_mass<<<grid, 256>>>(n_elem, d_rows.p, d_rofs.p, d_if.p, d_rho.p, d_vp.p, d_fl.p, d_mass.p);
+        err = cudaGetLastError();
+        if (err == cudaSuccess) err = cudaMemcpy(mass, d_mass.p, nv * sizeof(double), cudaMemcpyDeviceToHost);
+    }
+    d_rows.release();
+    d_rofs.release();
+    d_if.release();
+    d_rho.release();
+    d_vp.release();
+    d_fl.release();
+    d_mass.release();
+    cudaSetDevice(prev_device);
+    if (err != cudaSuccess) {
+        g_pre_err = std::string("ax3d_precompute_mass || CUDA: ") + cudaGetErrorString(err);
         return AX3D_ERR_CUDA;
     }
     return AX3D_OK;

@@ -1,4 +1,9 @@
-"""Pre-loop material precompute: elastic and attenuation moduli of many elements at once.
+"""Pre-loop precompute of many elements at once: geometry, elemental mass, elastic and
+attenuation moduli.
+
+geometry_gpu runs ax3d_precompute_geometry (Quad::createGraident + formIntegralFactor,
+Quad.cpp:509-547, FP64 on the GPU) and mass_gpu ax3d_precompute_mass
+(Material::computeElementalMass, Material.cpp:233-255).
 
 moduli_gpu runs ax3d_precompute_elastic (FP64 on the GPU); moduli_host is the same
 computation in numpy (FP64) with the functions the solver uses one element at a time
@@ -90,3 +95,66 @@ def moduli_host(rows, ifact, model: dict, isotropic=False, att=ATT_NONE, sls: SL
         mods.append((np.stack([F, L]) if isotropic else np.stack([A, Cc, F, L, N])).ravel())
     return (np.concatenate(mods).astype(np.float32),
             np.concatenate(atts).astype(np.float32) if atts else np.zeros(0, np.float32))
+
+
+def _check(lib, rc):
+    if rc != 0:
+        buf = C.create_string_buffer(512)
+        lib.ax3d_precompute_last_error(buf, 512)
+        raise RuntimeError(buf.value.decode())
+
+
+def spectral_table():
+    """GLL nodes, GLL weights, GLJ(0,1) nodes, GLJ weights (nPol = 4) as one [20] FP64 array."""
+    from . import spectral as S
+    return np.ascontiguousarray(np.concatenate([S.gll()[0], S.gll()[1], S.glj()[0], S.glj()[1]]), np.float64)
+
+
+def geometry_gpu(nodes, etype, co, axial, device=0):
+    """ax3d_precompute_geometry: nodes [E,2,4] -> geo [E,5,25], ifact [E,25], crds [E,25,2] (FP64)."""
+    from .capi import load_library
+    lib = load_library()
+    f = lib.ax3d_precompute_geometry
+    P_D = C.POINTER(C.c_double)
+    f.argtypes = [C.c_int32, C.c_int32, P_D, C.c_void_p, C.c_void_p, C.c_void_p, P_D, P_D, P_D, P_D]
+    nodes = np.ascontiguousarray(nodes, np.float64)
+    E = nodes.shape[0]
+    et = np.ascontiguousarray(etype, np.int8)
+    cc = np.ascontiguousarray(co, np.int8)
+    ax = np.ascontiguousarray(axial, np.uint8)
+    sp = spectral_table()
+    geo, ifact, crds = np.zeros((E, 5, 25)), np.zeros((E, 25)), np.zeros((E, 25, 2))
+    d = lambda a: a.ctypes.data_as(P_D)
+    _check(lib, f(int(device), E, d(nodes), et.ctypes.data_as(C.c_void_p), cc.ctypes.data_as(C.c_void_p),
+                  ax.ctypes.data_as(C.c_void_p), d(sp), d(geo), d(ifact), d(crds)))
+    return geo, ifact, crds
+
+
+def mass_gpu(rows, ifact, rho, vp, fluid, device=0):
+    """ax3d_precompute_mass: element masses [sum rows * 25] (FP64) from rho (and vp for fluids)
+    given per element as [rows][25] back to back."""
+    from .capi import load_library
+    lib = load_library()
+    f = lib.ax3d_precompute_mass
+    P_D = C.POINTER(C.c_double)
+    f.argtypes = [C.c_int32, C.c_int32, C.c_void_p, P_D, C.c_void_p, C.c_void_p, C.c_void_p, P_D]
+    rows = np.ascontiguousarray(rows, np.int32)
+    ifact = np.ascontiguousarray(ifact, np.float64)
+    rho = np.ascontiguousarray(rho, np.float32)
+    vp = np.ascontiguousarray(vp, np.float32) if vp is not None else None
+    fl = np.ascontiguousarray(fluid, np.uint8)
+    mass = np.zeros(int(rows.sum()) * 25)
+    _check(lib, f(int(device), len(rows), rows.ctypes.data_as(C.c_void_p), ifact.ctypes.data_as(P_D),
+                  rho.ctypes.data_as(C.c_void_p), vp.ctypes.data_as(C.c_void_p) if vp is not None else None,
+                  fl.ctypes.data_as(C.c_void_p), mass.ctypes.data_as(P_D)))
+    return mass
+
+
+def jacobian_from_geometry(geo):
+    """(J00, J01, J10, J11, det) [E,5,5] from the createGraident operators: dsdxii dzdeta -
+    dsdeta dzdxii = 1 / detJ, then J00 = dsdxii detJ, J01 = -dsdeta detJ, J10 = -dzdxii detJ,
+    J11 = dzdeta detJ."""
+    E = geo.shape[0]
+    g = geo.reshape(E, 5, 5, 5)
+    det = 1.0 / (g[:, 0] * g[:, 3] - g[:, 1] * g[:, 2])
+    return g[:, 0] * det, -g[:, 1] * det, -g[:, 2] * det, g[:, 3] * det, det

@@ -245,8 +245,9 @@ class Simulation:
     def build(self, kahan=False, nu_elem=None, preloop="host") -> DomainSpec:
         """Pack the domain.  nu_elem: optional per-element Fourier order (a learned or user
         Nu field) replacing NU_CONST; each point takes the maximum over its elements.
-        preloop = "gpu" computes the solid elements' moduli with ax3d_precompute_elastic
-        (FP64 on the GPU) instead of numpy."""
+        preloop = "gpu" computes the element geometry (ax3d_precompute_geometry), the 1-D
+        elemental masses (ax3d_precompute_mass) and the solid elements' moduli
+        (ax3d_precompute_elastic) in FP64 on the GPU instead of numpy."""
         par = self.par
         ex = Exodus.read(self.input_dir / par.get("MODEL_1D_EXODUS_MESH_FILE"))
         self.ex = ex
@@ -262,7 +263,15 @@ class Simulation:
         semi = ex.etype == 2
         co[semi] = np.where(np.abs(r[semi, 2] - r[semi, 3]) < 1e-3 * self.R, 2, 0)
         nodes = np.transpose(ex.nodes[ex.conn], (0, 2, 1))
-        geo, ifact, crds, theta, jac = GEO.batch_geometry(nodes, ex.etype, co, axial_e)
+        if preloop == "gpu":
+            # Quad::createGraident + formIntegralFactor on the GPU (FP64)
+            from . import preloop as PL
+            geo, ifact, crds = PL.geometry_gpu(nodes, ex.etype, co, axial_e)
+            rr = np.hypot(crds[..., 0], crds[..., 1])
+            theta = np.where(rr < 1e-10, 0.0, np.arccos(np.clip(crds[..., 1] / np.where(rr < 1e-10, 1.0, rr), -1, 1)))
+            jac = PL.jacobian_from_geometry(geo)
+        else:
+            geo, ifact, crds, theta, jac = GEO.batch_geometry(nodes, ex.etype, co, axial_e)
         self.nodes4, self.co, self.axial_e = nodes, co, axial_e
         # unique GLL points by coordinates (Connectivity::formElemToGLL)
         tol = 1e-3
@@ -356,8 +365,15 @@ class Simulation:
         rho0 = np.array([props3[e]["RHO"][0] if e3d[e] else rho[e] for e in range(E)])
         vp0 = np.array([props3[e]["VP"][0] if e3d[e] else vp[e] for e in range(E)])
         sm, fm = m1 & ~fl, m1 & fl
-        np.add.at(ms, e_pts[sm].ravel(), (rho0[sm] * ifact[sm]).ravel())
-        np.add.at(mf, e_pts[fm].ravel(), (ifact[fm] / (rho0[fm] * vp0[fm] ** 2)).ravel())
+        if preloop == "gpu":  # Material::computeElementalMass on the GPU (FP64), then assembled
+            from . import preloop as PL
+            em = PL.mass_gpu(np.ones(int(m1.sum())), ifact[m1], rho0[m1], vp0[m1], fl[m1]).reshape(-1, 25)
+            sel = np.nonzero(m1)[0]
+            np.add.at(ms, e_pts[sel[~fl[sel]]].ravel(), em[~fl[sel]].ravel())
+            np.add.at(mf, e_pts[sel[fl[sel]]].ravel(), em[fl[sel]].ravel())
+        else:
+            np.add.at(ms, e_pts[sm].ravel(), (rho0[sm] * ifact[sm]).ravel())
+            np.add.at(mf, e_pts[fm].ravel(), (ifact[fm] / (rho0[fm] * vp0[fm] ** 2)).ravel())
         ms3, mf3 = {}, {}
         for e in m3e:
             for k in range(25):

@@ -209,6 +209,21 @@ int ax3d_precompute_elastic(int32_t device, int32_t n_elem, const int32_t *rows,
                             int32_t isotropic, int32_t att, int32_t nsls, const double *w, const double *y,
                             double f_min, double f_max, double f_ref, int32_t do_kappa, float *moduli,
                             float *att_moduli);
+/* Quad::createGraident + Quad::formIntegralFactor (Quad.cpp:509-547) for many elements on
+   `device`, FP64: nodes [n][2][4] ((s0..s3), (z0..z3) of the corners in the reference's node
+   order), etype [n] (0 spherical, 1 linear, 2 semi-spherical mapping), curved_outer [n]
+   (0..3, the curved side), axial [n]; spectral [20] = GLL nodes, GLL weights, GLJ(0,1) nodes,
+   GLJ weights (SpectralConstants, nPol = 4).  Out: geometry [n][5][25] (dsdxii, dsdeta,
+   dzdxii, dzdeta, inv_s), ifact [n][25], crds [n][25][2] (s, z of every GLL point). */
+int ax3d_precompute_geometry(int32_t device, int32_t n_elem, const double *nodes, const int8_t *etype,
+                             const int8_t *curved_outer, const uint8_t *axial, const double *spectral,
+                             double *geometry, double *ifact, double *crds);
+/* Material::computeElementalMass (Material.cpp:233-255) without relabelling for many
+   elements on `device`, FP64: rows [n] (1 or nr), ifact [n][25], rho and (fluid elements) vp
+   as [rows][25] per element back to back, fluid [n].  Out: mass [rows][25] per element,
+   rho iFact for solids and iFact / (rho vp^2) for fluids. */
+int ax3d_precompute_mass(int32_t device, int32_t n_elem, const int32_t *rows, const double *ifact,
+                         const float *rho, const float *vp, const uint8_t *fluid, double *mass);
 size_t ax3d_precompute_last_error(char *buf, size_t n);
 
 /* Strain and curl at receivers (PointwiseRecorder::record, PointwiseRecorder.cpp:96-130;

@@ -8,6 +8,7 @@
 
 #include "../include/ax3d.h"
 #include "ax3d_oracle.hpp"
+#include "ax3d_oracle_preloop.hpp"
 
 namespace {
 thread_local std::string g_err;
@@ -272,6 +273,62 @@ extern "C" size_t axo_last_error(char *buf, size_t len) {
         buf[n] = 0;
     }
     return g_err.size();
+}
+
+// ---- FP64 pre-loop (ax3d_oracle_preloop.hpp), the checker of ax3d_precompute_* ----
+extern "C" int axo_pre_geometry(int32_t n, const double *nodes, const int8_t *etype, const int8_t *co,
+                                const uint8_t *axial, const double *spectral, double *geo, double *ifact,
+                                double *crds) {
+    axo_pre::Spectral S;
+    for (int i = 0; i < 5; i++) {
+        S.xg[i] = spectral[i];
+        S.wg[i] = spectral[5 + i];
+        S.xj[i] = spectral[10 + i];
+        S.wj[i] = spectral[15 + i];
+    }
+    for (int e = 0; e < n; e++) {
+        double nd[2][4];
+        for (int r = 0; r < 2; r++)
+            for (int k = 0; k < 4; k++) nd[r][k] = nodes[(int64_t)e * 8 + r * 4 + k];
+        axo_pre::quad_geometry(nd, etype[e], co[e], axial[e] != 0, S,
+                               reinterpret_cast<double(*)[25]>(geo + (int64_t)e * 125), ifact + (int64_t)e * 25,
+                               reinterpret_cast<double(*)[2]>(crds + (int64_t)e * 50));
+    }
+    return 0;
+}
+
+extern "C" int axo_pre_mass(int32_t n, const int32_t *rows, const double *ifact, const double *rho,
+                            const double *vp, const uint8_t *fluid, double *mass) {
+    int64_t o = 0;
+    for (int e = 0; e < n; e++) {
+        axo_pre::elemental_mass(rows[e], ifact + (int64_t)e * 25, rho + o, vp ? vp + o : nullptr, fluid[e] != 0,
+                                mass + o);
+        o += (int64_t)rows[e] * 25;
+    }
+    return 0;
+}
+
+// model values [8][rows][25] per element back to back (vpv, vph, vsv, vsh, eta, rho, qkappa,
+// qmu); out moduli [k][rows][25] and att [2][rows][npa] per element back to back
+extern "C" int axo_pre_elastic(int32_t n, const int32_t *rows, const double *ifact, const double *model,
+                               int32_t iso, int32_t att, int32_t nsls, const double *w, const double *y,
+                               double f_min, double f_max, double f_ref, int32_t do_kappa, double *mod,
+                               double *attm) {
+    axo_pre::AttFit fit{nsls, std::vector<double>(w, w + (att ? nsls : 0)),
+                        std::vector<double>(y, y + (att ? nsls : 0)), f_min, f_max, f_ref, do_kappa != 0};
+    int64_t mi = 0, mo = 0, ao = 0;
+    const int km = iso ? 2 : 5, npa = att == 2 ? 4 : 25;
+    for (int e = 0; e < n; e++) {
+        const int64_t nv = (int64_t)rows[e] * 25;
+        const double *m = model + mi;
+        axo_pre::create_elastic(rows[e], ifact + (int64_t)e * 25, m, m + nv, m + 2 * nv, m + 3 * nv, m + 4 * nv,
+                                m + 5 * nv, m + 6 * nv, m + 7 * nv, iso != 0, att, &fit, mod + mo,
+                                att ? attm + ao : nullptr);
+        mi += 8 * nv;
+        mo += km * nv;
+        ao += att ? 2 * (int64_t)rows[e] * npa : 0;
+    }
+    return 0;
 }
 
 #ifdef AX3D_ORACLE_FFT

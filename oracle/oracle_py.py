@@ -30,7 +30,7 @@ def build_oracle() -> Path:
 def load_oracle(fft: bool = False) -> C.CDLL:
     if fft not in _libs:
         path = LIB_FFT if fft else LIB
-        srcs = [HERE / "ax3d_oracle.hpp", HERE / "ax3d_oracle_capi.cpp", HERE / "ax3d_fft.hpp"]
+        srcs = [HERE / n for n in ("ax3d_oracle.hpp", "ax3d_oracle_capi.cpp", "ax3d_fft.hpp", "ax3d_oracle_preloop.hpp")]
         if not path.exists() or any(s.stat().st_mtime > path.stat().st_mtime for s in srcs):
             build_oracle()
         lib = C.CDLL(str(path))
@@ -92,3 +92,56 @@ def seismograms_of_inputs(input_dir, nsteps: int, double: bool = False, kahan: b
     o = OracleDomain(spec, double=double)
     o.step(nsteps)
     return o.seismograms(0, nsteps)
+
+
+def _pd(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def pre_geometry(nodes, etype, co, axial, spectral):
+    """FP64 Quad::createGraident + formIntegralFactor: geo [n,5,25], ifact [n,25], crds [n,25,2]."""
+    lib = load_oracle()
+    n = len(etype)
+    nodes = np.ascontiguousarray(nodes, np.float64)
+    et = np.ascontiguousarray(etype, np.int8)
+    cc = np.ascontiguousarray(co, np.int8)
+    ax = np.ascontiguousarray(axial, np.uint8)
+    sp = np.ascontiguousarray(spectral, np.float64)
+    geo, ifact, crds = np.zeros((n, 5, 25)), np.zeros((n, 25)), np.zeros((n, 25, 2))
+    lib.axo_pre_geometry(C.c_int32(n), _pd(nodes), et.ctypes.data_as(C.c_void_p), cc.ctypes.data_as(C.c_void_p),
+                         ax.ctypes.data_as(C.c_void_p), _pd(sp), _pd(geo), _pd(ifact), _pd(crds))
+    return geo, ifact, crds
+
+
+def pre_mass(rows, ifact, rho, vp, fluid):
+    """FP64 Material::computeElementalMass; rho, vp flat [sum rows * 25]."""
+    lib = load_oracle()
+    rows = np.ascontiguousarray(rows, np.int32)
+    ifact = np.ascontiguousarray(ifact, np.float64)
+    rho = np.ascontiguousarray(rho, np.float64)
+    vp = np.ascontiguousarray(vp if vp is not None else np.ones_like(rho), np.float64)
+    fl = np.ascontiguousarray(fluid, np.uint8)
+    mass = np.zeros(int(rows.sum()) * 25)
+    lib.axo_pre_mass(C.c_int32(len(rows)), rows.ctypes.data_as(C.c_void_p), _pd(ifact), _pd(rho), _pd(vp),
+                     fl.ctypes.data_as(C.c_void_p), _pd(mass))
+    return mass
+
+
+def pre_elastic(rows, ifact, model, iso, att, fit=None):
+    """FP64 Material::createElastic (+ AttBuilder, AttAxiSEM).  model: list over elements of
+    [8][rows][25] arrays (vpv, vph, vsv, vsh, eta, rho, qkappa, qmu).  fit: (w, y, f_min,
+    f_max, f_ref, do_kappa).  Returns flat moduli and attenuation moduli."""
+    lib = load_oracle()
+    rows = np.ascontiguousarray(rows, np.int32)
+    ifact = np.ascontiguousarray(ifact, np.float64)
+    flat = np.ascontiguousarray(np.concatenate([np.asarray(m, np.float64).reshape(-1) for m in model]))
+    km, npa = (2 if iso else 5), (4 if att == 2 else 25)
+    mod = np.zeros(int(rows.sum()) * 25 * km)
+    attm = np.zeros(max(1, int(rows.sum()) * 2 * npa if att else 1))
+    w, y, fmin, fmax, fref, dk = fit if fit is not None else (np.zeros(1), np.zeros(1), 1.0, 1.0, 1.0, True)
+    w = np.ascontiguousarray(w, np.float64)
+    y = np.ascontiguousarray(y, np.float64)
+    lib.axo_pre_elastic(C.c_int32(len(rows)), rows.ctypes.data_as(C.c_void_p), _pd(ifact), _pd(flat),
+                        C.c_int32(int(iso)), C.c_int32(att), C.c_int32(len(w)), _pd(w), _pd(y), C.c_double(fmin),
+                        C.c_double(fmax), C.c_double(fref), C.c_int32(int(dk)), _pd(mod), _pd(attm))
+    return mod, attm[: int(rows.sum()) * 2 * npa] if att else np.zeros(0)

@@ -471,27 +471,114 @@ def test_gpu_preloop_moduli_match_host(tmp_path_factory, ax3d_lib, attenuation):
     np.testing.assert_allclose(b.e_attm, a.e_attm, rtol=2e-6, atol=1e-30)
 
 
+def _ti_model(seed=2):
+    rng = np.random.default_rng(seed)
+    rows = np.array([1, 7, 1, 13, 5])
+    ifact = rng.uniform(1e9, 5e9, (len(rows), 25))
+    model = {k: [rng.uniform(lo, hi, (r, 25)).astype(np.float32) for r in rows] for k, lo, hi in
+             (("vpv", 8e3, 9e3), ("vph", 8e3, 9.5e3), ("vsv", 4e3, 5e3), ("vsh", 4e3, 5.2e3), ("eta", 0.9, 1.0),
+              ("rho", 3e3, 4e3), ("qkappa", 1e4, 6e4), ("qmu", 80, 600))}
+    return rows, ifact, model
+
+
+NAMES8 = ("vpv", "vph", "vsv", "vsh", "eta", "rho", "qkappa", "qmu")
+
+
+def test_oracle_preloop_elastic_matches_numpy():
+    """The oracle's FP64 Material::createElastic + AttBuilder + AttAxiSEM restatement and the
+    numpy pre-loop agree (TI and isotropic, no / full / CG4 attenuation)."""
+    from axisem3d_gb300 import attenuation as ATT
+    from axisem3d_gb300 import preloop as PL
+    from axisem3d_gb300.spec import ATT_CG4, ATT_FULL, ATT_NONE
+    from oracle.oracle_py import pre_elastic
+    rows, ifact, model = _ti_model()
+    w, y = ATT.fit_sls(3, 1 / 200, 1 / 10)
+    sls = PL.SLSFit(w, y, 1 / 200, 1 / 10, 1.0)
+    per_elem = [np.stack([model[k][e] for k in NAMES8]) for e in range(len(rows))]
+    for att in (ATT_NONE, ATT_FULL, ATT_CG4):
+        for iso in (False, True):
+            m = dict(model) if att != ATT_NONE else {k: v for k, v in model.items() if k not in ("qkappa", "qmu")}
+            h_mod, h_att = PL.moduli_host(rows, ifact, m, isotropic=iso, att=att, sls=sls)
+            o_mod, o_att = pre_elastic(rows, ifact, per_elem, iso, att, (w, y, 1 / 200, 1 / 10, 1.0, True))
+            np.testing.assert_allclose(o_mod.astype(np.float32), h_mod, rtol=1e-6)
+            np.testing.assert_allclose(o_att.astype(np.float32), h_att, rtol=1e-6, atol=1e-30)
+
+
+def _mesh_elements(tmp_path_factory, name, **kw):
+    d = tmp_path_factory.mktemp(name) / "input"
+    solver.write_inputs(d, steps=10, n_stations=2, seed=3, **kw)
+    sim = solver.Simulation(d)
+    spec = sim.build()
+    return sim, spec
+
+
+def test_oracle_preloop_geometry_matches_numpy(tmp_path_factory):
+    """The oracle's FP64 Quad::createGraident / formIntegralFactor restatement and the numpy
+    pre-loop agree on every element of the default half disk (spherical, linear and
+    semi-spherical mappings, axial elements)."""
+    from axisem3d_gb300 import geometry as GEO
+    from axisem3d_gb300 import preloop as PL
+    from oracle.oracle_py import pre_geometry
+    sim, _ = _mesh_elements(tmp_path_factory, "geo")
+    et = sim.ex.etype
+    assert len(np.unique(et)) >= 2 and sim.axial_e.any()
+    geo, ifact, crds, _, _ = GEO.batch_geometry(sim.nodes4, et, sim.co, sim.axial_e)
+    og, oi, oc = pre_geometry(sim.nodes4, et, sim.co, sim.axial_e, PL.spectral_table())
+    for a, b in ((og, geo), (oi, ifact), (oc, crds)):
+        scale = np.abs(b).max(axis=tuple(range(1, b.ndim)), keepdims=True)
+        assert (np.abs(a - b) <= 1e-11 * scale).all()
+
+
+@pytest.mark.gpu
+def test_gpu_preloop_geometry_and_mass_match_oracle(tmp_path_factory, ax3d_lib):
+    """ax3d_precompute_geometry and ax3d_precompute_mass (FP64 on the GPU) against the oracle's
+    FP64 restatement on every element of the default half disk (fluid core included), and the
+    domain built with the GPU pre-loop against the host pre-loop."""
+    from axisem3d_gb300 import preloop as PL
+    from oracle.oracle_py import pre_geometry, pre_mass
+    sim, spec_h = _mesh_elements(tmp_path_factory, "geog")
+    et = sim.ex.etype
+    og, oi, oc = pre_geometry(sim.nodes4, et, sim.co, sim.axial_e, PL.spectral_table())
+    gg, gi, gc = PL.geometry_gpu(sim.nodes4, et, sim.co, sim.axial_e)
+    for a, b in ((gg, og), (gi, oi), (gc, oc)):
+        scale = np.abs(b).max(axis=tuple(range(1, b.ndim)), keepdims=True)
+        assert (np.abs(a - b) <= 1e-12 * scale).all()
+    E = len(et)
+    rng = np.random.default_rng(4)
+    rows = rng.integers(1, 6, E)
+    rho = rng.uniform(2.6e3, 13e3, int(rows.sum()) * 25).astype(np.float32)
+    vp = rng.uniform(5.8e3, 13.7e3, int(rows.sum()) * 25).astype(np.float32)
+    fl = sim.fluid.astype(np.uint8)
+    assert fl.any() and (fl == 0).any()
+    gm = PL.mass_gpu(rows, oi, rho, vp, fl)
+    om = pre_mass(rows, oi, rho.astype(np.float64), vp.astype(np.float64), fl)
+    np.testing.assert_allclose(gm, om, rtol=1e-14)
+    spec_g = solver.Simulation(sim.input_dir).build(preloop="gpu")
+    np.testing.assert_allclose(spec_g.e_geo, spec_h.e_geo, rtol=1e-6, atol=1e-12)
+    np.testing.assert_allclose(spec_g.p_ms, spec_h.p_ms, rtol=1e-6)
+    np.testing.assert_allclose(spec_g.p_mf, spec_h.p_mf, rtol=1e-6)
+
+
 @pytest.mark.gpu
 def test_gpu_preloop_transversely_isotropic(ax3d_lib):
-    """TI moduli with full and CG4 attenuation, random model values, GPU vs numpy."""
+    """ax3d_precompute_elastic: TI and isotropic moduli with no, full and CG4 attenuation,
+    random model values, GPU (FP64, rounded to FP32) against the oracle's FP64 restatement of
+    Material::createElastic + AttBuilder + AttAxiSEM."""
     from axisem3d_gb300 import preloop as PL
     from axisem3d_gb300 import attenuation as ATT
     from axisem3d_gb300.spec import ATT_CG4, ATT_FULL, ATT_NONE
-    rng = np.random.default_rng(2)
-    rows = np.array([1, 7, 1, 13, 5])
-    ifact = rng.uniform(1e9, 5e9, (len(rows), 25))
-    model = {k: [rng.uniform(lo, hi, (r, 25)) for r in rows] for k, lo, hi in
-             (("vpv", 8e3, 9e3), ("vph", 8e3, 9.5e3), ("vsv", 4e3, 5e3), ("vsh", 4e3, 5.2e3), ("eta", 0.9, 1.0),
-              ("rho", 3e3, 4e3), ("qkappa", 1e4, 6e4), ("qmu", 80, 600))}
+    from oracle.oracle_py import pre_elastic
+    rows, ifact, model = _ti_model()
     w, y = ATT.fit_sls(3, 1 / 200, 1 / 10)
     sls = PL.SLSFit(w, y, 1 / 200, 1 / 10, 1.0)
+    per_elem = [np.stack([model[k][e] for k in NAMES8]) for e in range(len(rows))]
     for att in (ATT_NONE, ATT_FULL, ATT_CG4):
         for iso in (False, True):
             m = dict(model) if att != ATT_NONE else {k: v for k, v in model.items() if k not in ("qkappa", "qmu")}
             g_mod, g_att = PL.moduli_gpu(rows, ifact, m, isotropic=iso, att=att, sls=sls)
-            h_mod, h_att = PL.moduli_host(rows, ifact, m, isotropic=iso, att=att, sls=sls)
-            np.testing.assert_allclose(g_mod, h_mod, rtol=2e-6)
-            np.testing.assert_allclose(g_att, h_att, rtol=2e-6, atol=1e-30)
+            o_mod, o_att = pre_elastic(rows, ifact, per_elem, iso, att, (w, y, 1 / 200, 1 / 10, 1.0, True))
+            np.testing.assert_allclose(g_mod, o_mod.astype(np.float32), rtol=1e-6)
+            np.testing.assert_allclose(g_att, o_att.astype(np.float32), rtol=1e-6, atol=1e-30)
 
 
 def test_point_force_source(tmp_path_factory):
