@@ -105,6 +105,7 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.ax3d_last_error.argtypes = [C.c_char_p, C.c_size_t]
     lib.ax3d_last_error.restype = C.c_size_t
     lib.ax3d_enable_timers.argtypes = [C.c_void_p, C.c_int32]
+    lib.ax3d_autotune.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, C.c_size_t]
     lib.ax3d_read_timers.argtypes = [C.c_void_p, P_F64, P_I64]
     if path is None:
         _LIB = lib
@@ -324,6 +325,13 @@ class Ax3dDomain(_DomainBase):
     def __init__(self, spec: DomainSpec, device: int = 0, lib: C.CDLL | None = None):
         self.lib = lib or load_library()
         self._build(spec, device, with_first=True)
+
+    def autotune(self, trials: int = 2) -> str:
+        """ax3d_autotune: the physical-space bucket schedule from timed element passes on this
+        domain (cached per process by shape); returns the library's report."""
+        buf = C.create_string_buffer(4096)
+        self._ck(self.lib.ax3d_autotune(self.h, int(trials), buf, 4096))
+        return buf.value.decode()
 
     def enable_timers(self, on: bool = True):
         self._ck(self.lib.ax3d_enable_timers(self.h, int(on)))

@@ -138,6 +138,16 @@ struct ax3d_domain {
     int nitems_p1s = 0, nitems_p1f = 0, nitems_p3s = 0, nitems_p3f = 0, n_p3s = 0, n_p3f = 0, nr_p3 = 1;
     std::vector<ax3d::PhysBucket> buckets_s, buckets_f;
     std::vector<DevBuf<int32_t>> bucket_lists;
+    // the bucket schedule: geometric step of the transform length between buckets, shared
+    // memory policy (0: two CTAs per SM where they fit; 1: one CTA per SM, fewer clusters)
+    // and side streams used; set at ax3d_finalize, changed by ax3d_autotune
+    struct Schedule {
+        double ratio = 1.12;
+        int policy = 0, nside = NSIDE;
+    } sched;
+    std::vector<int32_t> phys3_s_list, phys3_f_list;  // physical-space elements
+    std::vector<int32_t> lbuf_of_nr;                   // buffer length of each ring size's plan
+    int num_sms = 0;
     DevBuf<int32_t> d_pts3d, d_sf3d;
     int n_pts3d = 0, n_sf3d = 0, n_sf1d = 0;
     DevBuf<int32_t> d_selem, d_snord;
@@ -510,7 +520,6 @@ struct ax3d_domain {
         int64_t efsize = 0, memsize = 0;
         std::vector<std::vector<int64_t>> sref(np), fref(np);
         std::vector<int2> items_s, items_f;
-        std::map<int, std::vector<int32_t>> phys_s, phys_f;  // keyed by bucket id
         std::vector<int32_t> phys3_s, phys3_f;
         std::vector<int2> items_p1s, items_p1f, items_p3s, items_p3f;
         std::vector<int32_t> p3s, p3f;
@@ -582,11 +591,10 @@ struct ax3d_domain {
         for (int e = 0; e < ne; e++)
             if (e_flags[e] & ax3d::EF_IN3D) used[e_nr[e]] = 1;
         ax3d::FftTables ft = ax3d::build_fft_tables(used);
-        for (int fl = 0; fl < 2; fl++)
-            for (int e : fl ? phys3_f : phys3_s) {
-                const int b = (int)std::floor(std::log((double)ft.plans[e_nr[e]].Lbuf) / std::log(1.12));
-                (fl ? phys_f : phys_s)[b].push_back(e);
-            }
+        phys3_s_list = phys3_s;
+        phys3_f_list = phys3_f;
+        lbuf_of_nr.assign(ft.plans.size(), 1);
+        for (size_t k = 0; k < ft.plans.size(); k++) lbuf_of_nr[k] = ft.plans[k].Lbuf;
         // ocean load per point (GLLPoint.cpp:57-72 picks MassOcean1D / MassOcean3D)
         std::vector<int32_t> p_oclen(np, 0);
         std::vector<int64_t> p_ocofs(np, 0);
@@ -691,32 +699,8 @@ struct ax3d_domain {
         d_items_f.upload(items_f, st);
         nitems_s = (int)items_s.size();
         nitems_f = (int)items_f.size();
-        bucket_lists.resize(phys_s.size() + phys_f.size());
-        buckets_s.clear();
-        buckets_f.clear();
-        int num_sms = 0;
         CK(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, device));
-        size_t bi = 0;
-        for (int fl = 0; fl < 2; fl++) {
-            auto &src = fl ? phys_f : phys_s;
-            auto &dst = fl ? buckets_f : buckets_s;
-            for (auto &kv : src) {
-                ax3d::PhysBucket b;
-                b.count = (int)kv.second.size();
-                for (int e : kv.second) {
-                    b.L_max = std::max(b.L_max, ft.plans[e_nr[e]].Lbuf);
-                    b.n_max = std::max(b.n_max, e_nr[e] / 2 + 1);
-                }
-                ax3d::size_phys_bucket(b, !fl);
-                if (b.npts_chunk <= 0)
-                    throw Error(AX3D_ERR_UNSUPPORTED, "ax3d_finalize || nr too large for the physical-space kernel");
-                b.grid = ax3d::phys_grid(b, !fl, num_sms);
-                bucket_lists[bi].upload(kv.second, st);
-                b.elems = bucket_lists[bi].p;
-                bi++;
-                dst.push_back(b);
-            }
-        }
+        build_buckets(sched, st);
         n_pts3d = (int)pts3d.size();
         n_sf3d = (int)sf3d.size();
         d_pts3d.upload(pts3d.empty() ? std::vector<int32_t>{0} : pts3d, st);
@@ -858,6 +842,134 @@ struct ax3d_domain {
         ax3d::launch_source(P, T, F, d_selem.p, d_snord.p, d_sofs_src.p, d_sforce.p, (int)s_elem.size(),
                             d_stf.p, (int)stf.size(), d_targ.p, 0, stream);
     }
+    // Physical-space buckets of a schedule: elements grouped by the geometric step of their
+    // transform buffer length, each bucket with its own shared-memory size, points per CTA,
+    // cluster size and persistent grid.
+    void build_buckets(const Schedule &sc, cudaStream_t st) {
+        std::map<int, std::vector<int32_t>> phys[2];  // keyed by bucket id
+        for (int fl = 0; fl < 2; fl++)
+            for (int e : fl ? phys3_f_list : phys3_s_list) {
+                const int b = (int)std::floor(std::log((double)lbuf_of_nr[e_nr[e]]) / std::log(sc.ratio));
+                phys[fl][b].push_back(e);
+            }
+        bucket_lists.clear();
+        bucket_lists.resize(phys[0].size() + phys[1].size());
+        buckets_s.clear();
+        buckets_f.clear();
+        size_t bi = 0;
+        for (int fl = 0; fl < 2; fl++) {
+            auto &dst = fl ? buckets_f : buckets_s;
+            for (auto &kv : phys[fl]) {
+                ax3d::PhysBucket b;
+                b.count = (int)kv.second.size();
+                for (int e : kv.second) {
+                    b.L_max = std::max(b.L_max, lbuf_of_nr[e_nr[e]]);
+                    b.n_max = std::max(b.n_max, e_nr[e] / 2 + 1);
+                }
+                ax3d::size_phys_bucket(b, !fl, sc.policy);
+                if (b.npts_chunk <= 0)
+                    throw Error(AX3D_ERR_UNSUPPORTED, "ax3d_finalize || nr too large for the physical-space kernel");
+                b.grid = ax3d::phys_grid(b, !fl, num_sms);
+                bucket_lists[bi].upload(kv.second, st);
+                b.elems = bucket_lists[bi].p;
+                bi++;
+                dst.push_back(b);
+            }
+        }
+        sched = sc;
+    }
+    // ---- autotuner: the bucket schedule from timed trials on this domain's own elements ----
+    // Candidates: transform-length steps between buckets {1.06, 1.12, 1.25, 1.5} x shared-
+    // memory policy {two CTAs per SM, one CTA per SM} x side streams {1, NSIDE}.  Each trial
+    // times `trials` element passes (after one untimed pass) with CUDA events on the domain's
+    // stream; the point stiffness and the memory variables the passes change are saved
+    // before and put back after every trial.  The choice is cached per process under the
+    // device name and the histogram of transform buffer lengths, so a second domain of the
+    // same shape takes it without trials.
+    static std::map<std::string, Schedule> &tune_cache() {
+        static std::map<std::string, Schedule> c;
+        return c;
+    }
+    std::string tune_key() const {
+        cudaDeviceProp prop;
+        CK(cudaGetDeviceProperties(&prop, device));
+        std::map<int, int64_t> hist;
+        for (int fl = 0; fl < 2; fl++)
+            for (int e : fl ? phys3_f_list : phys3_s_list) hist[lbuf_of_nr[e_nr[e]] * 2 + fl]++;
+        std::string k = prop.name;
+        for (auto &kv : hist) k += " " + std::to_string(kv.first) + ":" + std::to_string(kv.second);
+        return k;
+    }
+    std::string autotune(int trials) {
+        need_final();
+        if (phys3_s_list.empty() && phys3_f_list.empty()) return "no physical-space elements: nothing to tune";
+        const std::string key = tune_key();
+        auto hit = tune_cache().find(key);
+        char buf[256];
+        if (hit != tune_cache().end()) {
+            build_buckets(hit->second, stream);
+            drop_graph();
+            snprintf(buf, sizeof buf, "cached: ratio %.2f, policy %d, side streams %d", hit->second.ratio,
+                     hit->second.policy, hit->second.nside);
+            return buf;
+        }
+        trials = std::max(1, trials);
+        // save what an element pass changes
+        DevBuf<float2> save_ss, save_fs;
+        DevBuf<float> save_mem;
+        save_ss.alloc(std::max<int64_t>(nsolid, 1));
+        save_fs.alloc(std::max<int64_t>(nfluid, 1));
+        save_mem.alloc(std::max<int64_t>(d_mem.n, 1));
+        auto copy = [&](void *dst, const void *src, size_t bytes) {
+            if (bytes) CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, stream));
+        };
+        copy(save_ss.p, d_ss.p, (size_t)nsolid * sizeof(float2));
+        copy(save_fs.p, d_fs.p, (size_t)nfluid * sizeof(float2));
+        copy(save_mem.p, d_mem.p, (size_t)d_mem.n * sizeof(float));
+        cudaEvent_t a = get_event(), b = get_event();
+        const bool was_timers = timers;
+        timers = false;
+        const Schedule start = sched;
+        Schedule best = start;
+        float best_ms = 1e30f;
+        std::string log;
+        for (double ratio : {1.06, 1.12, 1.25, 1.5})
+            for (int policy : {0, 1})
+                for (int nside : {1, (int)NSIDE}) {
+                    Schedule sc;
+                    sc.ratio = ratio;
+                    sc.policy = policy;
+                    sc.nside = nside;
+                    build_buckets(sc, stream);
+                    launch_elements(false);  // untimed: first launch of this shape
+                    CK(cudaEventRecord(a, stream));
+                    for (int t = 0; t < trials; t++) launch_elements(false);
+                    CK(cudaEventRecord(b, stream));
+                    CK(cudaEventSynchronize(b));
+                    float ms = 0.f;
+                    CK(cudaEventElapsedTime(&ms, a, b));
+                    ms /= trials;
+                    snprintf(buf, sizeof buf, " %.2f/%d/%d:%.2f", ratio, policy, nside, ms);
+                    log += buf;
+                    if (ms < best_ms) {
+                        best_ms = ms;
+                        best = sc;
+                    }
+                    copy(d_ss.p, save_ss.p, (size_t)nsolid * sizeof(float2));
+                    copy(d_fs.p, save_fs.p, (size_t)nfluid * sizeof(float2));
+                    copy(d_mem.p, save_mem.p, (size_t)d_mem.n * sizeof(float));
+                }
+        build_buckets(best, stream);
+        drop_graph();
+        CK(cudaStreamSynchronize(stream));
+        pool.push_back(a);
+        pool.push_back(b);
+        timers = was_timers;
+        tune_cache()[key] = best;
+        snprintf(buf, sizeof buf, "chose ratio %.2f, policy %d, side streams %d (%.2f ms per element pass); trials ms:",
+                 best.ratio, best.policy, best.nside, best_ms);
+        return std::string(buf) + log;
+    }
     // Element stiffness (Domain::computeStiff's element loop).  The physical-space buckets
     // go round-robin, longest transforms first, over side streams forked from and joined
     // back into the main stream, so one bucket's tail overlaps the next bucket's start;
@@ -876,14 +988,15 @@ struct ax3d_domain {
             for (auto &b : buckets_f) ax3d::launch_elem_phys(false, T, P, F.fu, b, X, sls, overwrite, stream);
             return;
         }
+        const int ns = std::max(1, std::min(sched.nside, NSIDE));
         CK(cudaEventRecord(ev_fork, stream));
-        for (int k = 0; k < NSIDE; k++) CK(cudaStreamWaitEvent(side[k], ev_fork, 0));
+        for (int k = 0; k < ns; k++) CK(cudaStreamWaitEvent(side[k], ev_fork, 0));
         int i = 0;
         for (auto it = buckets_s.rbegin(); it != buckets_s.rend(); ++it)
-            ax3d::launch_elem_phys(true, T, P, F.su, *it, X, sls, overwrite, side[i++ % NSIDE]);
+            ax3d::launch_elem_phys(true, T, P, F.su, *it, X, sls, overwrite, side[i++ % ns]);
         for (auto it = buckets_f.rbegin(); it != buckets_f.rend(); ++it)
-            ax3d::launch_elem_phys(false, T, P, F.fu, *it, X, sls, overwrite, side[i++ % NSIDE]);
-        for (int k = 0; k < NSIDE; k++) {
+            ax3d::launch_elem_phys(false, T, P, F.fu, *it, X, sls, overwrite, side[i++ % ns]);
+        for (int k = 0; k < ns; k++) {
             CK(cudaEventRecord(ev_join[k], side[k]));
             CK(cudaStreamWaitEvent(stream, ev_join[k], 0));
         }
@@ -1481,6 +1594,19 @@ int ax3d_enable_timers(ax3d_domain *d, int32_t enable) {
     return guard([&] {
         if (!d) throw Error(AX3D_ERR_ARG, "ax3d_enable_timers || null domain");
         d->timers = enable != 0;
+    });
+}
+
+int ax3d_autotune(ax3d_domain *d, int32_t trials, char *report, size_t len) {
+    return guard([&] {
+        if (!d) throw Error(AX3D_ERR_ARG, "ax3d_autotune || null domain");
+        CK(cudaSetDevice(d->device));
+        const std::string r = d->autotune(trials);
+        if (report && len) {
+            const size_t n = std::min(len - 1, r.size());
+            std::memcpy(report, r.data(), n);
+            report[n] = 0;
+        }
     });
 }
 

@@ -57,7 +57,7 @@ void set_g_matrices_phys(const float *g_gll, const float *g_glj, cudaStream_t s)
 // FP64 plans, twiddles, chirps and kernel spectra for every used ring size (used[nr] != 0)
 FftTables build_fft_tables(const std::vector<char> &used);
 size_t phys_smem_bytes(int Lmax, int nsq, int npts_chunk);
-void size_phys_bucket(PhysBucket &b, bool solid);
+void size_phys_bucket(PhysBucket &b, bool solid, int policy = 0);
 int phys_grid(const PhysBucket &b, bool solid, int num_sms);
 
 void launch_elem_fourier_solid(const ElemTable &T, const PointTable &P, const float2 *su,

@@ -371,6 +371,35 @@ __device__ __noinline__ void direct_pass(float2 *buf, int S, int ns, int L, int 
     }
 }
 
+// A direct pass of prime R: GS lanes x KL outputs cover its (R - 1) / 2 output pairs; SG
+// (sequences per group) trades twiddle reuse against the number of groups that keep the
+// CTA's threads busy: the cheapest of SG = 1, 2, 4 by rounds x steps x instructions per step.
+template <int GS, int KL>
+__device__ void direct_sg(float2 *buf, int S, int ns, int L, int Ls, int R, const float2 *tw, int sg, bool dit,
+                          const Grp g) {
+    const int groups = L / R;  // butterflies of the pass per sequence
+    int best = 4;
+    int64_t bcost = INT64_MAX;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        const int SGc = 1 << c;
+        const int64_t lanes = (int64_t)groups * ((ns + SGc - 1) / SGc) * GS;
+        const int64_t rounds = (lanes + g.n - 1) / g.n;
+        const int64_t cost = rounds * (4 * SGc + 4 * KL * SGc + 4 * KL);
+        if (cost < bcost) {
+            bcost = cost;
+            best = SGc;
+        }
+    }
+    if constexpr (KL >= 4) best = best > 2 ? 2 : best;  // four sequences x four outputs spill
+    if (best == 1)
+        direct_pass<GS, KL, 1>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
+    else if (best == 2 || KL >= 4)
+        direct_pass<GS, KL, 2>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
+    else
+        direct_pass<GS, KL, 4>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
+}
+
 __device__ void run_pass(int R, float2 *buf, int S, int ns, int L, int Ls, const float2 *tw, int sg, bool dit,
                          const Grp g) {
     switch (R) {
@@ -381,17 +410,29 @@ __device__ void run_pass(int R, float2 *buf, int S, int ns, int L, int Ls, const
         case 7: rad_pass<7>(buf, S, ns, L, Ls, tw, sg, dit, g); break;
         case 11: rad_pass<11>(buf, S, ns, L, Ls, tw, sg, dit, g); break;
         case 13: rad_pass<13>(buf, S, ns, L, Ls, tw, sg, dit, g); break;
-        default:
-            if (R <= 17)
-                direct_pass<8, 1, 4>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
-            else if (R <= 33)
-                direct_pass<16, 1, 4>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
-            else if (R <= 65)
-                direct_pass<32, 1, 4>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
-            else if (R <= 129)
-                direct_pass<32, 2, 2>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
+        default: {
+            // the narrowest group whose lanes cover the H = (R - 1) / 2 output pairs with at
+            // most three outputs each (four for R above 193)
+            const int H = (R - 1) / 2;
+            if (H <= 8)
+                direct_sg<4, 2>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
+            else if (H <= 12)
+                direct_sg<4, 3>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
+            else if (H <= 16)
+                direct_sg<8, 2>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
+            else if (H <= 24)
+                direct_sg<8, 3>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
+            else if (H <= 32)
+                direct_sg<16, 2>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
+            else if (H <= 48)
+                direct_sg<16, 3>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
+            else if (H <= 64)
+                direct_sg<32, 2>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
+            else if (H <= 96)
+                direct_sg<32, 3>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
             else
-                direct_pass<32, 4, 1>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
+                direct_sg<32, 4>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
+        }
     }
 }
 
@@ -1134,11 +1175,12 @@ std::vector<int> radices(int L) {
     return out;
 }
 
-// modelled cost of one length-L transform of one sequence (FP32 operations plus shared
-// traffic per pass)
+// modelled cost of one length-L transform of one sequence: issued instructions per point
+// and pass (a radix-R butterfly in registers, or for a prime above 13 the direct pass's
+// (R - 1) / 2 multiply-accumulate steps of about 3.3 instructions per point each)
 double pass_cost(int L) {
     double c = 0;
-    for (int r : radices(L)) c += (double)L * (r == 2 ? 12 : r == 4 ? 15 : r <= 13 ? r + 8 : r + 10);
+    for (int r : radices(L)) c += (double)L * (r == 2 ? 12 : r == 4 ? 15 : r <= 13 ? r + 8 : 1.65 * r + 12);
     return c;
 }
 bool smooth13(int n) {
@@ -1312,13 +1354,15 @@ FftTables build_fft_tables(const std::vector<char> &used) {
     return T;
 }
 
-// Points per CTA, cluster size and shared memory of a bucket: all 25 points in one CTA
-// when two CTAs per SM fit, else the smallest cluster whose CTAs fit (two per SM if
-// possible).
-void size_phys_bucket(PhysBucket &b, bool solid) {
+// Points per CTA, cluster size and shared memory of a bucket.  Policy 0: all 25 points in
+// one CTA when two CTAs per SM fit, else the smallest cluster whose CTAs fit (two per SM if
+// possible).  Policy 1: the smallest cluster whose CTAs fit the whole shared memory of an SM
+// (one CTA per SM for rings up to ~360 samples, fewer clusters above).
+void size_phys_bucket(PhysBucket &b, bool solid, int policy) {
     const int nsq = solid ? 3 : 2;
     b.npts_chunk = 0;
-    for (size_t cap : {SMEM_TWO, SMEM_CAP}) {
+    const std::vector<size_t> caps = policy == 1 ? std::vector<size_t>{SMEM_CAP} : std::vector<size_t>{SMEM_TWO, SMEM_CAP};
+    for (size_t cap : caps) {
         for (int pc = NPE; pc >= 1; pc--) {
             const size_t sm = phys_smem_bytes(b.L_max, nsq, pc);
             const int C = (NPE + pc - 1) / pc;

@@ -103,7 +103,8 @@ def calibrate_margin(y_pred, labels, nu_full, quantile=0.99):
 
 
 def run(spec, steps, learn=None):
-    """Time-to-seismogram of one GPU run (first step to seismograms on the host).
+    """Loop time of one GPU run (first step to seismograms on the host; the pre-loop and
+    any network inference are timed by the caller and added for time-to-seismogram).
     learn = (interval, epsilon) turns the wisdom learner on.  Returns (seis, seconds,
     wisdom or None, unique-point updates per step)."""
     import torch
@@ -159,17 +160,29 @@ def experiment(work, n_train=64, n_test=16, nu_full=64, steps=600, epochs=200, b
     margin = calibrate_margin(ytr, labels_tr, nu_full)
     log(f"fit {t_fit:.1f} s, loss {hist[0]:.4g} -> {hist[-1]:.4g}, margin {margin:.3f}")
     tests = []
-    seis_l_all, specs_l = [], []
+    seis_l_all, specs_l, pre_l_all = [], [], []
     for i in range(n_test):
         d = write_case(work / f"test{i}", 5000 + i, nu_full, steps, mesh_kw)
+        # plain full-Nu route: pre-loop, then the loop
+        t0 = time.perf_counter()
         sim = solver.Simulation(d)
         spec_f = sim.build()
+        pre_f = time.perf_counter() - t0
         seis_f, t_f, _, upd_f = run(spec_f, steps)
         _, t_fl, wis, _ = run(spec_f, steps, learn=(interval, eps))
+        # learned route: features, network inference, pre-loop at the predicted Nu, the loop
+        t0 = time.perf_counter()
         x = element_features(sim)
+        t_feat = time.perf_counter() - t0
+        import torch
+        t0 = time.perf_counter()
         y = net.forward(x).cpu().numpy()
+        torch.cuda.synchronize()
+        t_inf = time.perf_counter() - t0
         nu_e = decode(y, nu_full, margin)
+        t0 = time.perf_counter()
         spec_l = sim.build(nu_elem=nu_e)
+        pre_l = time.perf_counter() - t0
         seis_l, t_l, _, upd_l = run(spec_l, steps)
         mis = float(np.linalg.norm(seis_l - seis_f) / np.linalg.norm(seis_f))
         # the reference's route without a network: reuse the wisdom of this model's own
@@ -177,13 +190,19 @@ def experiment(work, n_train=64, n_test=16, nu_full=64, steps=600, epochs=200, b
         spec_w = sim.build(nu_elem=np.maximum(element_labels(spec_f, wis), 1))
         seis_w, t_w, _, upd_w = run(spec_w, steps)
         mis_w = float(np.linalg.norm(seis_w - seis_f) / np.linalg.norm(seis_f))
+        tts_f = pre_f + t_f
+        tts_l = t_feat + t_inf + pre_l + t_l
         tests.append(dict(seed=5000 + i, misfit=mis, t_full=t_f, t_full_learning=t_fl, t_learned=t_l,
-                          speedup=t_f / t_l, upd_full=upd_f, upd_learned=upd_l, misfit_wisdom=mis_w, t_wisdom=t_w,
+                          speedup=t_f / t_l, preloop_full=pre_f, preloop_learned=pre_l, features=t_feat,
+                          inference=t_inf, tts_full=tts_f, tts_learned=tts_l, tts_speedup=tts_f / tts_l,
+                          upd_full=upd_f, upd_learned=upd_l, misfit_wisdom=mis_w, t_wisdom=t_w,
                           mean_nu_pred=float(nu_e.mean()), mean_nu_label=float(element_labels(spec_f, wis).mean())))
         del spec_f, spec_w
         specs_l.append(spec_l)
         seis_l_all.append(seis_l)
-        log(f"test {i}: misfit {mis:.4f} (wisdom {mis_w:.4f}), full {t_f:.2f} s, learned {t_l:.2f} s")
+        pre_l_all.append(t_feat + t_inf + pre_l)
+        log(f"test {i}: misfit {mis:.4f} (wisdom {mis_w:.4f}), full {tts_f:.2f} s (loop {t_f:.2f}), "
+            f"learned {tts_l:.2f} s (loop {t_l:.2f}), updates {upd_f} -> {upd_l}")
         if out:
             (Path(out) / "tests_partial.json").write_text(json.dumps(tests, indent=1))
     # all held-out learned-Nu runs batched into one domain
@@ -193,6 +212,8 @@ def experiment(work, n_train=64, n_test=16, nu_full=64, steps=600, epochs=200, b
     parts = ensemble.split_seismograms(seis_b, info)
     mis_b = max(float(np.linalg.norm(p - s) / np.linalg.norm(s)) for p, s in zip(parts, seis_l_all))
     t_full_sum = sum(t["t_full"] for t in tests)
+    tts_full_sum = sum(t["tts_full"] for t in tests)
+    tts_batched = sum(pre_l_all) + t_b  # every learned model's features, inference, pre-loop + one batched loop
     summary = dict(
         n_train=n_train, n_test=n_test, nu_full=nu_full, steps=steps, elements=int(len(specs_l[0].e_pts)),
         epochs=epochs, batch=batch, fit_seconds=t_fit, train_runs_seconds=t_train_runs,
@@ -200,7 +221,10 @@ def experiment(work, n_train=64, n_test=16, nu_full=64, steps=600, epochs=200, b
         margin=margin, tests=tests,
         misfit_max=max(t["misfit"] for t in tests), misfit_mean=float(np.mean([t["misfit"] for t in tests])),
         speedup_mean=float(np.mean([t["speedup"] for t in tests])),
+        tts_speedup_mean=float(np.mean([t["tts_speedup"] for t in tests])),
         batched_seconds=t_b, batched_vs_sequential_full=t_full_sum / t_b,
+        tts_batched_learned_seconds=tts_batched, tts_sequential_full_seconds=tts_full_sum,
+        tts_learned_batched_vs_sequential_full=tts_full_sum / tts_batched,
         batched_vs_sequential_learned=sum(t["t_learned"] for t in tests) / t_b,
         batched_split_misfit_max=mis_b)
     if out:

@@ -292,6 +292,16 @@ enum {
     AX3D_NTIMERS = 8
 };
 int ax3d_enable_timers(ax3d_domain *d, int32_t enable);
+/* No counterpart in the reference, whose element cost table (Domain.cpp:349-382) weights
+   the METIS partition instead (Mesh.cpp:412-588).  After ax3d_finalize: chooses the
+   schedule of the physical-space element buckets -- the step of transform length between
+   buckets, the shared-memory policy (two CTAs per SM, or one CTA per SM with fewer
+   clusters) and the side streams -- from timed element passes on this domain's own
+   elements (`trials` timed passes per candidate; the fields are left as they were), then
+   recaptures the step.  The choice is cached for the process under the device name and the
+   domain's histogram of transform lengths; a later domain of the same shape takes it
+   without trials.  `report` (len bytes, may be NULL) receives the choice and the times. */
+int ax3d_autotune(ax3d_domain *d, int32_t trials, char *report, size_t len);
 int ax3d_read_timers(ax3d_domain *d, double *ms, int64_t *launches);
 
 int ax3d_destroy(ax3d_domain *d);

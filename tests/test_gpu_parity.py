@@ -316,3 +316,29 @@ def test_streamed_field_transfers_match_synchronous(ax3d_lib):
     b.get_async("veloc", "solid", got)
     b.sync_fields()
     np.testing.assert_array_equal(got, a.get("veloc", "solid"))
+
+
+def test_autotuned_schedule_keeps_results(ax3d_lib):
+    """ax3d_autotune times bucket schedules on the domain's own elements, leaves the fields as
+    they were, and the chosen schedule gives the oracle's results; a second domain of the
+    same shape takes the cached choice."""
+    from oracle.oracle_py import OracleDomain
+    from axisem3d_gb300 import workloads as W
+    from axisem3d_gb300.capi import Ax3dDomain
+    spec = W.element_benchmark(n_elem=20, seed=9, att=ATT_CG4)
+    u0 = W.benchmark_displacement(spec, seed=8)
+    g, o = Ax3dDomain(spec), OracleDomain(spec)
+    for d in (g, o):
+        d.set("displ", "solid", u0)
+        d.compute_stiff()
+    before = {w: g.get(w, "solid").copy() for w in ("displ", "stiff")}
+    rep = g.autotune(1)
+    assert rep.startswith("chose ratio"), rep
+    for w in ("displ", "stiff"):
+        np.testing.assert_array_equal(g.get(w, "solid"), before[w])
+    for d in (g, o):
+        d.step(3)
+    for which in ("displ", "veloc", "accel"):
+        assert rel(g.get(which, "solid"), o.get(which, "solid")) <= TOL, which
+    g2 = Ax3dDomain(spec)
+    assert g2.autotune(1).startswith("cached")
