@@ -4,11 +4,14 @@
 // 64-sample tile's whole forward and backward pass in shared memory: the activations
 // (BF16), the pre-activations (FP32, for GELU'), one weight matrix at a time (BF16) and
 // the back-propagated errors (BF16).  Products of two BF16 values are exact in FP32 and
-// are accumulated with FP32 FMAs.  Each tile writes its parameter gradient to its own
-// slot; one pass then sums the slots in tile order and applies Adam, so results do not
-// depend on scheduling.  The GEMMs are 64 x 128 x 128 per tile: CUDA-core FMAs from
-// shared memory keep every SM busy for the sizes used here (tens of thousands of
-// samples per batch), with no tensor-core staging to amortise.
+// are accumulated in FP32.  Each tile writes its parameter gradient to its own slot; one
+// pass then sums the slots in tile order and applies Adam, so results do not depend on
+// scheduling.  The per-tile GEMMs -- the three forward layers (64 x 128 x K), the two
+// hidden backward products (64 x 128 x 128) and the two hidden weight gradients
+// (128 x 128 x 64) -- run on the tensor cores as warp-level BF16 mma.sync (m16n8k16, FP32
+// accumulators), their operands read from shared memory with ldmatrix (transposed where
+// the stored layout is k-major); the small first-layer weight gradient and the output
+// layer stay on the CUDA cores.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -84,26 +87,54 @@ __device__ __forceinline__ void load_w(uint16_t *sW, const uint16_t *g, int rows
     }
 }
 
-// acc[bb][c] = sum_r in[b][r] * sW[r][c] for the thread's 4 samples b = tb*4 + bb and
-// 8 columns c = tc*8 + cc (K rows, input pitch IP)
+// ---- tensor-core tiles: mma.sync m16n8k16, BF16 inputs, FP32 accumulators ----
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+// four 8x8 BF16 matrices; lane l gives the address of row l % 8 of matrix l / 8
+__device__ __forceinline__ void ldsm4(uint32_t (&r)[4], const void *p) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(smem_addr(p)));
+}
+__device__ __forceinline__ void ldsm4t(uint32_t (&r)[4], const void *p) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(smem_addr(p)));
+}
+// d += a (16x16, row) * b (16x8, col)
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// Warp w of 8 computes rows m0 = (w % 4) 16 .. +16 and columns n0 = (w / 4) 64 .. +64 of
+// out[b][c] = sum_r in[b][r] sW[r][c] (in: [64][K] pitch IP; sW: [K][128] pitch HP).
+// acc[nt][i]: column n0 + 8 nt + 2 (lane % 4) + (i & 1), row m0 + lane / 4 + 8 (i >> 1).
 template <int K, int IP>
-__device__ __forceinline__ void mm_tile(const uint16_t *in, const uint16_t *sW, int tb, int tc,
-                                        float (&acc)[4][8]) {
+__device__ __forceinline__ void mma_rows(const uint16_t *in, const uint16_t *sW, float (&acc)[8][4]) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int m0 = (w & 3) * 16, n0 = (w >> 2) * 64;
+    const int q = lane >> 3, i = lane & 7;
 #pragma unroll
-    for (int bb = 0; bb < 4; bb++)
+    for (int nt = 0; nt < 8; nt++)
 #pragma unroll
-        for (int c = 0; c < 8; c++) acc[bb][c] = 0.f;
-#pragma unroll 4
-    for (int r = 0; r < K; r += 2) {
-        float w0[8], w1[8];
-        unpack8(*reinterpret_cast<const uint4 *>(sW + r * HP + tc * 8), w0);
-        unpack8(*reinterpret_cast<const uint4 *>(sW + (r + 1) * HP + tc * 8), w1);
+        for (int c = 0; c < 4; c++) acc[nt][c] = 0.f;
 #pragma unroll
-        for (int bb = 0; bb < 4; bb++) {
-            const uint32_t hv = *reinterpret_cast<const uint32_t *>(in + (tb * 4 + bb) * IP + r);
-            const float h0 = bf_lo(hv), h1 = bf_hi(hv);
+    for (int k0 = 0; k0 < K; k0 += 16) {
+        uint32_t a[4];
+        // matrices: (rows 0-7, k 0-7), (rows 8-15, k 0-7), (rows 0-7, k 8-15), (rows 8-15, k 8-15)
+        ldsm4(a, in + (m0 + i + 8 * (q & 1)) * IP + k0 + 8 * (q >> 1));
 #pragma unroll
-            for (int c = 0; c < 8; c++) acc[bb][c] = fmaf(h1, w1[c], fmaf(h0, w0[c], acc[bb][c]));
+        for (int np = 0; np < 4; np++) {
+            // B of two n-tiles from the k-major sW: (k 0-7, n), (k 8-15, n), (k 0-7, n+8), (k 8-15, n+8)
+            uint32_t b[4];
+            ldsm4t(b, sW + (k0 + i + 8 * (q & 1)) * HP + n0 + 16 * np + 8 * (q >> 1));
+            mma_bf16(acc[2 * np], a, b[0], b[1]);
+            mma_bf16(acc[2 * np + 1], a, b[2], b[3]);
         }
     }
 }
@@ -112,76 +143,90 @@ __device__ __forceinline__ void mm_tile(const uint16_t *in, const uint16_t *sW, 
 template <int K, int IP, bool KEEPZ>
 __device__ __forceinline__ void dense_fwd(const uint16_t *in, const uint16_t *sW, const float *bias,
                                           float *sZ, uint16_t *out, int tid) {
-    const int tc = tid & 15, tb = tid >> 4;
-    float acc[4][8];
-    mm_tile<K, IP>(in, sW, tb, tc, acc);
-    float bv[8];
+    float acc[8][4];
+    mma_rows<K, IP>(in, sW, acc);
+    const int lane = tid & 31, w = tid >> 5;
+    const int r0 = (w & 3) * 16 + (lane >> 2), c0 = (w >> 2) * 64 + 2 * (lane & 3);
 #pragma unroll
-    for (int c = 0; c < 8; c++) bv[c] = __ldg(bias + tc * 8 + c);
+    for (int nt = 0; nt < 8; nt++) {
+        const int c = c0 + 8 * nt;
+        const float b0 = __ldg(bias + c), b1 = __ldg(bias + c + 1);
 #pragma unroll
-    for (int bb = 0; bb < 4; bb++) {
-        const int b = tb * 4 + bb;
-        float z[8], h[8];
-#pragma unroll
-        for (int c = 0; c < 8; c++) {
-            z[c] = acc[bb][c] + bv[c];
-            h[c] = gelu(z[c]);
+        for (int h = 0; h < 2; h++) {
+            const int b = r0 + 8 * h;
+            const float z0 = acc[nt][2 * h] + b0, z1 = acc[nt][2 * h + 1] + b1;
+            if (KEEPZ) *reinterpret_cast<float2 *>(sZ + b * NH + c) = make_float2(z0, z1);
+            *reinterpret_cast<uint32_t *>(out + b * HP + c) =
+                (uint32_t)to_bf(gelu(z0)) | ((uint32_t)to_bf(gelu(z1)) << 16);
         }
-        if (KEEPZ) {
-            float4 *zp = reinterpret_cast<float4 *>(sZ + b * NH + tc * 8);
-            zp[0] = make_float4(z[0], z[1], z[2], z[3]);
-            zp[1] = make_float4(z[4], z[5], z[6], z[7]);
-        }
-        *reinterpret_cast<uint4 *>(out + b * HP + tc * 8) = pack8(h);
     }
 }
 
-// backward through one hidden layer: dh = W^T dz (sW holds W as [out][in]),
+// backward through one hidden layer: dh = W^T dz (sW holds W as [out][in], which is the
+// k-major [k][n] operand of dh[b][in] = sum_out dz[b][out] W[out][in]),
 // dz_prev = bf16(dh * gelu'(z_prev))
 __device__ __forceinline__ void dense_bwd(const uint16_t *dz, const uint16_t *sW, const float *zprev,
                                           uint16_t *dzprev, int tid) {
-    const int tc = tid & 15, tb = tid >> 4;
-    float acc[4][8];
-    mm_tile<NH, HP>(dz, sW, tb, tc, acc);
+    float acc[8][4];
+    mma_rows<NH, HP>(dz, sW, acc);
+    const int lane = tid & 31, w = tid >> 5;
+    const int r0 = (w & 3) * 16 + (lane >> 2), c0 = (w >> 2) * 64 + 2 * (lane & 3);
 #pragma unroll
-    for (int bb = 0; bb < 4; bb++) {
-        const int b = tb * 4 + bb;
-        const float4 *zp = reinterpret_cast<const float4 *>(zprev + b * NH + tc * 8);
-        const float4 za = zp[0], zb = zp[1];
-        const float z[8] = {za.x, za.y, za.z, za.w, zb.x, zb.y, zb.z, zb.w};
-        float d[8];
+    for (int nt = 0; nt < 8; nt++) {
+        const int c = c0 + 8 * nt;
 #pragma unroll
-        for (int c = 0; c < 8; c++) d[c] = acc[bb][c] * dgelu(z[c]);
-        *reinterpret_cast<uint4 *>(dzprev + b * HP + tc * 8) = pack8(d);
+        for (int h = 0; h < 2; h++) {
+            const int b = r0 + 8 * h;
+            const float2 z = *reinterpret_cast<const float2 *>(zprev + b * NH + c);
+            *reinterpret_cast<uint32_t *>(dzprev + b * HP + c) =
+                (uint32_t)to_bf(acc[nt][2 * h] * dgelu(z.x)) | ((uint32_t)to_bf(acc[nt][2 * h + 1] * dgelu(z.y)) << 16);
+        }
     }
 }
 
 // weight gradient of a 128 x 128 layer over the tile: P[j][k] = sum_b dz[b][j] h[b][k];
-// bias gradient P_b[j] = sum_b dz[b][j]
+// bias gradient P_b[j] = sum_b dz[b][j].  Warp w computes rows j0 = (w % 4) 32 .. +32 and
+// columns k0 = (w / 4) 64 .. +64; both operands are stored [b][.], so A = dz^T comes in
+// through transposed ldmatrix and B = h as in the forward layers.
 __device__ __forceinline__ void wgrad(const uint16_t *dz, const uint16_t *h, float *P, float *Pb,
                                       int tid) {
-    const int jb = tid >> 4, kb = tid & 15;
-    float acc[8][8];
+    const int lane = tid & 31, w = tid >> 5;
+    const int j0 = (w & 3) * 32, n0 = (w >> 2) * 64;
+    const int q = lane >> 3, i = lane & 7;
+    float acc[2][8][4];
 #pragma unroll
-    for (int a = 0; a < 8; a++)
+    for (int mt = 0; mt < 2; mt++)
 #pragma unroll
-        for (int c = 0; c < 8; c++) acc[a][c] = 0.f;
-#pragma unroll 2
-    for (int b = 0; b < TB; b++) {
-        float d[8], x[8];
-        unpack8(*reinterpret_cast<const uint4 *>(dz + b * HP + jb * 8), d);
-        unpack8(*reinterpret_cast<const uint4 *>(h + b * HP + kb * 8), x);
+        for (int nt = 0; nt < 8; nt++)
 #pragma unroll
-        for (int a = 0; a < 8; a++)
+            for (int c = 0; c < 4; c++) acc[mt][nt][c] = 0.f;
 #pragma unroll
-            for (int c = 0; c < 8; c++) acc[a][c] = fmaf(d[a], x[c], acc[a][c]);
+    for (int b0 = 0; b0 < TB; b0 += 16) {
+        uint32_t a[2][4];
+#pragma unroll
+        for (int mt = 0; mt < 2; mt++)
+            // (j 0-7, b 0-7), (j 8-15, b 0-7), (j 0-7, b 8-15), (j 8-15, b 8-15) of the [b][j] store
+            ldsm4t(a[mt], dz + (b0 + i + 8 * (q >> 1)) * HP + j0 + 16 * mt + 8 * (q & 1));
+#pragma unroll
+        for (int np = 0; np < 4; np++) {
+            uint32_t bb[4];
+            ldsm4t(bb, h + (b0 + i + 8 * (q & 1)) * HP + n0 + 16 * np + 8 * (q >> 1));
+#pragma unroll
+            for (int mt = 0; mt < 2; mt++) {
+                mma_bf16(acc[mt][2 * np], a[mt], bb[0], bb[1]);
+                mma_bf16(acc[mt][2 * np + 1], a[mt], bb[2], bb[3]);
+            }
+        }
     }
 #pragma unroll
-    for (int a = 0; a < 8; a++) {
-        float4 *p = reinterpret_cast<float4 *>(P + (jb * 8 + a) * NH + kb * 8);
-        p[0] = make_float4(acc[a][0], acc[a][1], acc[a][2], acc[a][3]);
-        p[1] = make_float4(acc[a][4], acc[a][5], acc[a][6], acc[a][7]);
-    }
+    for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+        for (int nt = 0; nt < 8; nt++)
+#pragma unroll
+            for (int hh = 0; hh < 2; hh++) {
+                const int j = j0 + 16 * mt + (lane >> 2) + 8 * hh, k = n0 + 8 * nt + 2 * (lane & 3);
+                *reinterpret_cast<float2 *>(P + j * NH + k) = make_float2(acc[mt][nt][2 * hh], acc[mt][nt][2 * hh + 1]);
+            }
     if (tid < NH) {
         float s = 0.f;
         for (int b = 0; b < TB; b++) s += __uint_as_float((uint32_t)dz[b * HP + tid] << 16);

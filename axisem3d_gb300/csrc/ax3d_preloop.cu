@@ -370,8 +370,9 @@ extern "C" int ax3d_precompute_geometry(int32_t device, int32_t n_elem, const do
         return AX3D_ERR_ARG;
     }
     for (int e = 0; e < n_elem; e++)
-        if (etype[e] < 0 || etype[e] > 2 || curved_outer[e] < 0 || curved_outer[e] > 3) {
-            g_pre_err = "ax3d_precompute_geometry || mapping type must be 0..2 and curved side 0..3";
+        if (etype[e] < 0 || etype[e] > 2 || (etype[e] != 1 && (curved_outer[e] < 0 || curved_outer[e] > 3))) {
+            g_pre_err = "ax3d_precompute_geometry || mapping type must be 0..2 and, for a curved mapping, curved "
+                        "side 0..3";
             return AX3D_ERR_ARG;
         }
     if (n_elem == 0) return AX3D_OK;

@@ -212,7 +212,7 @@ int ax3d_precompute_elastic(int32_t device, int32_t n_elem, const int32_t *rows,
 /* Quad::createGraident + Quad::formIntegralFactor (Quad.cpp:509-547) for many elements on
    `device`, FP64: nodes [n][2][4] ((s0..s3), (z0..z3) of the corners in the reference's node
    order), etype [n] (0 spherical, 1 linear, 2 semi-spherical mapping), curved_outer [n]
-   (0..3, the curved side), axial [n]; spectral [20] = GLL nodes, GLL weights, GLJ(0,1) nodes,
+   (0..3, the curved side; ignored for linear), axial [n]; spectral [20] = GLL nodes, GLL weights, GLJ(0,1) nodes,
    GLJ weights (SpectralConstants, nPol = 4).  Out: geometry [n][5][25] (dsdxii, dsdeta,
    dzdxii, dzdeta, inv_s), ifact [n][25], crds [n][25][2] (s, z of every GLL point). */
 int ax3d_precompute_geometry(int32_t device, int32_t n_elem, const double *nodes, const int8_t *etype,

@@ -145,7 +145,8 @@ def test_learned_nu_gain_on_held_out_model(tmp_path, ax3d_lib, capsys):
     the Fourier order of every element of a model it has not seen.  Without the network the
     method runs that model at the full Nu (or pays a full-Nu run first to learn its wisdom);
     with it, the run at the predicted orders costs fewer GLL-point x azimuth updates per step
-    and its seismograms stay within 1 % relative L2 of the full-Nu run's."""
+    and its seismograms stay within 1 % relative L2 of the full-Nu run's.  (The network is
+    fitted on two of the three models; the third calibrates the shift of its predictions.)"""
     from axisem3d_gb300 import nu_learn
     mesh = dict(n_theta=16, h_mantle=600e3, h_core=700e3, r_c=1500e3)
     s = nu_learn.experiment(tmp_path, n_train=3, n_test=1, nu_full=32, steps=300, epochs=200, batch=512,
@@ -154,7 +155,7 @@ def test_learned_nu_gain_on_held_out_model(tmp_path, ax3d_lib, capsys):
     with capsys.disabled():
         print(f"\nlearned Nu: misfit {t['misfit']:.4f}, updates/step {t['upd_full']} -> {t['upd_learned']}, "
               f"mean Nu {t['mean_nu_pred']:.1f} (labels {t['mean_nu_label']:.1f}), loss {s['loss_first']:.4g} -> "
-              f"{s['loss_last']:.4g}")
+              f"{s['loss_last']:.4g}, calibrated shift {s['shift']}")
     assert s["loss_last"] < 0.5 * s["loss_first"]
     assert t["misfit"] <= 0.01
     assert t["upd_learned"] < t["upd_full"]
