@@ -19,6 +19,7 @@ from . import attenuation as ATT
 from . import model3d as M3D
 from . import geometry as GEO
 from . import netcdf as NC
+from . import relabelling as RL
 from . import spectral as S
 from .spec import (ATT_CG4, ATT_FULL, ATT_NONE, MAT_ACOUSTIC, MAT_ISO, POINT_FLUID, POINT_SOLID,
                    POINT_SOLID_FLUID, DomainSpec)
@@ -317,9 +318,6 @@ class Simulation:
         self.phi2d = self._phi2d()
         # options that would change the physics but are not built here: refuse them rather
         # than run without them (Geometric3D::buildInparam, ExodusModel.cpp:557-572)
-        if _int_or(par, "MODEL_3D_GEOMETRIC_NUM", 0) > 0:
-            raise ValueError("Geometric3D::buildInparam || 3-D geometric models (particle relabelling from "
-                             "undulations) are not derived by this pre-loop; pass X through ax3d_set_prt.")
         emode = (par.values.get("MODEL_3D_ELLIPTICITY_MODE") or ["off"])[0].lower()
         if emode != "off":
             raise ValueError("ExodusModel::buildInparam || MODEL_3D_ELLIPTICITY_MODE: only 'off' (a spherical "
@@ -345,6 +343,32 @@ class Simulation:
                         continue
                     e3d[sel[j]] = True
                     props3[sel[j]] = {k: v[j] for k, v in cur.items()}
+        # particle relabelling from the geometric models (Quad::addGeometric3D, Quad.cpp:249-255;
+        # Relabelling::addUndulation): the elements with a nonzero undulation
+        gmodels = RL.geometric_models(par, self._cmt_latlon(), self.R)
+        relab = {}
+        if gmodels:
+            # element centre radius (Quad::computeCenterRadius: mapping at xi = eta = 0)
+            rcen = np.zeros(E)
+            zero = np.zeros((1, 1))
+            for e in range(E):
+                sc, zc, *_ = GEO._batch_map_jac(nodes[e:e + 1], zero, zero, int(ex.etype[e]), int(max(co[e], 0)))
+                rcen[e] = float(np.hypot(sc[0, 0], zc[0, 0]))
+            for e in range(E):
+                r_ = RL.Relabelled(gmodels, geo[e], crds[e], int(e_nr[e]), p_nr[e_pts[e]], bool(axial_e[e]),
+                                   rcen[e], phi2d=self.phi2d)
+                if not r_.zero:
+                    relab[e] = r_
+            for e, r_ in relab.items():
+                if not r_.par1d() and not e3d[e]:
+                    # elem1D = elem1D && isPar1D (Quad.cpp:388-389, 406-407): the element turns 3-D
+                    n = int(e_nr[e])
+                    e3d[e] = True
+                    props3[e] = {"VP": np.repeat(vp[e][None, :], n, 0), "VS": np.repeat(vs[e][None, :], n, 0),
+                                 "RHO": np.repeat(rho[e][None, :], n, 0)}
+        self.relab = relab
+        # stiffness Jacobian of each relabelled element, on its rows (1 for a 1-D element)
+        jstiff = {e: (r_.stiff_jacobian() if e3d[e] else r_.stiff_jacobian()[:1]) for e, r_ in relab.items()}
         self.e3d, self.models = e3d, models
         self.vp_e, self.vs_e = vp.mean(1), vs.mean(1)
         # point phases, masses (Material::computeElementalMass), coupling normals
@@ -356,10 +380,11 @@ class Simulation:
         # elements whose mass varies with phi (3-D rho, or 3-D vp in a fluid); the others
         # add a constant; 3-D masses are resampled onto each point's own Nr
         # (Material.cpp:215-224, XMath::linearResampling)
-        m3e = [e for e in np.nonzero(e3d)[0] if np.ptp(props3[e]["RHO"], 0).any()
-               or (fl[e] and np.ptp(props3[e]["VP"], 0).any())]
+        m3e = [e for e in np.nonzero(e3d)[0] if e not in relab and (np.ptp(props3[e]["RHO"], 0).any()
+               or (fl[e] and np.ptp(props3[e]["VP"], 0).any()))]
         m1 = np.ones(E, bool)
         m1[m3e] = False
+        m1[list(relab)] = False
         ms = np.zeros(P)
         mf = np.zeros(P)
         rho0 = np.array([props3[e]["RHO"][0] if e3d[e] else rho[e] for e in range(E)])
@@ -384,7 +409,20 @@ class Simulation:
                     mf3[p] = mf3.get(p, 0.0) + ifact[e, k] / (rr * vv ** 2)
                 else:
                     ms3[p] = ms3.get(p, 0.0) + rr * ifact[e, k]
+        for e, r_ in relab.items():
+            # Material::computeElementalMass with the relabelling's mass Jacobian (Material.cpp:233-255)
+            for k in range(25):
+                p = int(e_pts[e, k])
+                n = int(p_nr[p])
+                rr = (M3D.linear_resampling(n, props3[e]["RHO"][:, k]) if e3d[e] else np.full(n, rho[e, k]))
+                jm = r_.mass_jacobian(k)
+                if fl[e]:
+                    vv = (M3D.linear_resampling(n, props3[e]["VP"][:, k]) if e3d[e] else np.full(n, vp[e, k]))
+                    mf3[p] = mf3.get(p, 0.0) + ifact[e, k] / (rr * vv ** 2) * jm
+                else:
+                    ms3[p] = ms3.get(p, 0.0) + rr * ifact[e, k] * jm
         sfn = np.zeros((P, 3))
+        sfn3 = {}  # undulated boundary: normals per slice (Quad::computeNormal with getSFNormalRTZ)
         sfside = ex.side.get("solid_fluid_boundary", np.full(E, -1))
         wg, wjw = S.gll()[1], S.glj()[1]
         def side_normal(e, side):
@@ -423,14 +461,26 @@ class Simulation:
 
         for e in np.nonzero(sfside >= 0)[0]:
             for k, nvec in side_normal(e, sfside[e]):
-                sfn[e_pts[e, k]] += 0.5 * (nvec if fl[e] else -nvec)  # GLLPoint::addSFNormal
+                pk = e_pts[e, k]
+                if e in relab:
+                    # normal_RTZ per slice rotated to (s, phi, z), times the same area factor
+                    sint, cost = crds[e, k, 0] / np.hypot(*crds[e, k]), crds[e, k, 1] / np.hypot(*crds[e, k])
+                    Q = np.array([[cost, 0.0, sint], [0.0, 1.0, 0.0], [-sint, 0.0, cost]])
+                    nv = relab[e].sf_normal_rtz(k) @ Q.T * float(nvec @ np.array([sint, 0.0, cost]))
+                    sfn3[pk] = sfn3.get(pk, 0.0) + 0.5 * (nv if fl[e] else -nv)
+                else:
+                    sfn[pk] += 0.5 * (nvec if fl[e] else -nvec)  # GLLPoint::addSFNormal
         # moduli (Material::createElastic / createAcoustic, isotropic)
         att_on = par.get("ATTENUATION", bool)
         cg4 = par.get("ATTENUATION_CG4", bool)
         dokappa = par.get("ATTENUATION_QKAPPA", bool)
         # time step (Mesh::getDeltaT x TIME_DELTA_T_FACTOR, or TIME_DELTA_T)
         dt_user = par.get("TIME_DELTA_T", float)
-        dt = dt_user if dt_user > 0 else float(ex.dt.min()) * par.get("TIME_DELTA_T_FACTOR", float)
+        # Quad::getDeltaT (Quad.cpp:291-305): dt on slices scales with the deformed hmin
+        dt_e = ex.dt.astype(float).copy()
+        for e, r_ in relab.items():
+            dt_e[e] *= r_.hmin_slices().min() / r_.hmin_ref()
+        dt = dt_user if dt_user > 0 else float(dt_e.min()) * par.get("TIME_DELTA_T_FACTOR", float)
         self.dt = dt
         attk = ATT_NONE
         alpha = beta = gamma = np.zeros(0)
@@ -445,14 +495,14 @@ class Simulation:
         e_mod, e_attm, e_mat, e_att = [], [], [], []
         gpu_mod = self._moduli_gpu(E, fl, e3d, props3, vp, vs, rho, ifact, mat, attk,
                                    (w, y, fmin, fmax, fref) if attk != ATT_NONE else None,
-                                   dokappa) if preloop == "gpu" else None
+                                   dokappa, jstiff) if preloop == "gpu" else None
         for e in range(E):
             f = ifact[e]
             # (nr, 25) for 3-D elements, (1, 25) for 1-D ones
             vp_e, vs_e, rho_e = ((props3[e]["VP"], props3[e]["VS"], props3[e]["RHO"]) if e3d[e]
                                  else (vp[e][None, :], vs[e][None, :], rho[e][None, :]))
-            if fl[e]:
-                e_mod.append((f / rho_e).ravel())
+            if fl[e]:  # Material::createAcoustic: K = iFact / rho, times the stiffness Jacobian
+                e_mod.append((f / rho_e * jstiff.get(e, 1.0)).ravel())
                 e_attm.append(np.zeros(0))
                 e_mat.append(MAT_ACOUSTIC)
                 e_att.append(ATT_NONE)
@@ -463,8 +513,9 @@ class Simulation:
                 e_mat.append(MAT_ISO)
                 e_att.append(attk)
                 continue
-            lam = rho_e * (vp_e ** 2 - 2 * vs_e ** 2) * f
-            mu = rho_e * vs_e ** 2 * f
+            # relabelling multiplies the moduli by the stiffness Jacobian before the attenuation split
+            lam = rho_e * (vp_e ** 2 - 2 * vs_e ** 2) * f * jstiff.get(e, 1.0)
+            mu = rho_e * vs_e ** 2 * f * jstiff.get(e, 1.0)
             attm = np.zeros(0)
             if attk != ATT_NONE:
                 A = C = lam + 2 * mu
@@ -516,7 +567,14 @@ class Simulation:
         sfrows, sfirows = [], []
         for p in np.nonzero(kind == POINT_SOLID_FLUID)[0]:
             mfp = mf[p] + mf3.get(p, 0.0)
-            if np.ndim(mfp) and np.ptp(mfp) > 0:
+            if p in sfn3:  # undulated boundary: SFCoupling3D with per-slice normals
+                n = int(p_nr[p])
+                rows = sfn[p][None, :] + sfn3[p]
+                mfr = np.broadcast_to(np.ravel(mfp), (n,)) if np.size(mfp) in (1, n) else mfp
+                sflen[p] = n
+                sfrows.append(rows)
+                sfirows.append(rows / np.asarray(mfr, float)[:, None])
+            elif np.ndim(mfp) and np.ptp(mfp) > 0:
                 sflen[p] = len(mfp)
                 rows = np.repeat(sfn[p][None, :], len(mfp), 0)
                 sfrows.append(rows)
@@ -539,6 +597,21 @@ class Simulation:
             nsls=nsls, att_alpha=alpha, att_beta=beta, att_gamma=gamma, att_do_kappa=dokappa,
             kahan=kahan, stability_interval=par.get("OPTION_STABILITY_INTERVAL", int),
             oc_pt=oc_pt, oc_len=oc_len, oc_vals=oc_vals, p_crds=pcrd)
+        if relab:
+            # the PRT of each relabelled element (Relabelling::createPRT): X [4][25] on a 1-D
+            # element (PRT_1D), [4][Nr][25] on a 3-D one (PRT_3D)
+            pe, pl, px = [], [], []
+            for e in sorted(relab):
+                X = relab[e].stiff_x()
+                pe.append(e)
+                pl.append(X.shape[1] if e3d[e] else 1)
+                px.append((X if e3d[e] else X[:, :1, :]).ravel())
+            spec.prt_elem = np.array(pe, np.int32)
+            spec.prt_len = np.array(pl, np.int32)
+            spec.prt_x = np.concatenate(px).astype(np.float32)
+            if len(oc_pt) and any(e in relab for e in np.nonzero(fl == 0)[0] if (ex.side.get("r1", np.full(E, -1))[e] >= 0)):
+                raise ValueError("Quad::setOceanLoad3D || ocean load on an undulated surface is not built; "
+                                 "use MODEL_3D_OCEAN_LOAD none with geometric models there.")
         self.e_pts, self.crds, self.jac, self.fluid = e_pts, crds, jac, fl
         self._source(spec)
         self._stf(spec)
@@ -548,9 +621,10 @@ class Simulation:
         return spec
 
     # ------------------------------------------------------------------ source
-    def _moduli_gpu(self, E, fl, e3d, props3, vp, vs, rho, ifact, mat, attk, fit, dokappa):
+    def _moduli_gpu(self, E, fl, e3d, props3, vp, vs, rho, ifact, mat, attk, fit, dokappa, jstiff=None):
         """Isotropic solid moduli of every solid element in one ax3d_precompute_elastic call;
-        returns {element: (moduli [2][rows][25], attenuation moduli)}."""
+        returns {element: (moduli [2][rows][25], attenuation moduli)}.  jstiff: relabelled
+        elements' stiffness Jacobians, applied through rho (every modulus is linear in it)."""
         from . import preloop as PL
         solid = [e for e in range(E) if not fl[e]]
         rows, model = [], {k: [] for k in ("vpv", "vph", "vsv", "vsh", "eta", "rho", "qkappa", "qmu")}
@@ -564,7 +638,7 @@ class Simulation:
             model["vsv"].append(vs_e)
             model["vsh"].append(vs_e)
             model["eta"].append(np.ones((nr, 25)))
-            model["rho"].append(rho_e)
+            model["rho"].append(rho_e * (jstiff or {}).get(e, 1.0))
             if attk != ATT_NONE:
                 model["qkappa"].append(np.broadcast_to(mat["QKAPPA"][e][None, :], (nr, 25)))
                 model["qmu"].append(np.broadcast_to(mat["QMU"][e][None, :], (nr, 25)))

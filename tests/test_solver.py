@@ -715,7 +715,7 @@ def test_record_interval_subsamples_station_output(tmp_path_factory):
 
 def test_user_nr_field_and_refused_options(tmp_path_factory):
     """NU_TYPE user-defined (UserNrField as shipped: Nu linear in depth through the
-    (depth, nu) pairs); geometric models and ellipticity, not built, are refused."""
+    (depth, nu) pairs); data-driven geometric models and ellipticity, not built, are refused."""
     from axisem3d_gb300 import wisdom as W
     nr = W.user_nr(["0", "8", "1000e3", "2", "3000e3", "2"], [0.0, 0.0, 0.0, 0.0],
                    [6371e3, 6371e3 - 500e3, 6371e3 - 1000e3, 100.0], 6371e3)
@@ -729,7 +729,7 @@ def test_user_nr_field_and_refused_options(tmp_path_factory):
     assert spec.p_nr.max() <= 13 and spec.p_nr.min() >= 1 and len(np.unique(spec.p_nr)) > 2
     m = (d / "inparam.model").read_text()
     (d / "inparam.model").write_text(m.replace("MODEL_3D_GEOMETRIC_NUM 0", "MODEL_3D_GEOMETRIC_NUM 1\nMODEL_3D_GEOMETRIC_LIST crust1"))
-    with pytest.raises(ValueError, match="ax3d_set_prt"):
+    with pytest.raises(NotImplementedError, match="not shipped"):
         solver.Simulation(d).build()
     (d / "inparam.model").write_text(m + "MODEL_3D_ELLIPTICITY_MODE full\nMODEL_3D_ELLIPTICITY_INVF 298.3\n")
     with pytest.raises(ValueError, match="ELLIPTICITY"):
@@ -812,3 +812,105 @@ def test_reference_template_parfiles_parse(tmp_path):
     assert par.get("NU_WISDOM_LEARN_EPSILON", float) == 1e-3
     assert par.get("ATTENUATION_CG4", bool) is True
     assert par.get("MODEL_3D_VOLUMETRIC_LIST", str, 1) == "crust1"
+
+
+def _bump_inputs(tmp_path_factory, name, latlon, **kw):
+    from pathlib import Path
+    d = tmp_path_factory.mktemp(name) / "input"
+    solver.write_inputs(d, mesh_kw=SMALL_MESH, steps=60, hdur=20.0, n_stations=3, seed=3, nu=4, **kw)
+    pm = Path(d) / "inparam.model"
+    pm.write_text(pm.read_text().replace(
+        "MODEL_3D_GEOMETRIC_NUM 0", f"MODEL_3D_GEOMETRIC_NUM 1\nMODEL_3D_GEOMETRIC_LIST bump$6371${latlon}$20$15$400"))
+    return d
+
+
+class _Const:
+    """A geometric model with a constant radial shift."""
+
+    def __init__(self, c):
+        self.c = c
+
+    def delta_r(self, xyz, r_center):
+        return np.full(xyz.shape[:-1], self.c)
+
+
+class _Linear:
+    """deltaR = k (r - r0)."""
+
+    def __init__(self, k, r0):
+        self.k, self.r0 = k, r0
+
+    def delta_r(self, xyz, r_center):
+        return self.k * (np.linalg.norm(xyz, axis=-1) - self.r0)
+
+
+def test_relabelling_of_analytic_undulations(small_inputs):
+    """Relabelling.cpp restated on fields with known answers: no undulation is no relabelling; a
+    constant radial shift c has no gradient, so X = (1 / (1 + c/Z), 0, 0, 1) and the Jacobian is
+    (1 + c/Z)^2; deltaR = k (r - r0) is linear in eta on a spherical element, so its radial
+    derivative is k to rounding, its other derivatives vanish, X3 = 1 / (1 + k)."""
+    from axisem3d_gb300 import relabelling as RL
+    sim = solver.Simulation(small_inputs)
+    spec = sim.build()
+    E = spec.n_elements
+    e = next(i for i in range(E) if not sim.axial_e[i] and not sim.fluid[i] and sim.ex.etype[i] == 0)
+    pn = spec.p_nr[spec.e_pts[e]]
+    nr = int(pn.max())
+    args = (spec.e_geo[e].astype(np.float64), sim.crds[e], nr, pn, False, 0.0)
+    assert RL.Relabelled([_Const(0.0)], *args).zero
+    geo = None
+    from axisem3d_gb300 import geometry as GEO
+    geo, _, _, _, _ = GEO.batch_geometry(sim.nodes4[e:e + 1], sim.ex.etype[e:e + 1], sim.co[e:e + 1], sim.axial_e[e:e + 1])
+    args = (geo[0], sim.crds[e], nr, pn, False, 0.0)
+    Z = np.hypot(sim.crds[e, :, 0], sim.crds[e, :, 1])
+    r_ = RL.Relabelled([_Const(1500.0)], *args)
+    assert not r_.zero and r_.par1d()
+    X = r_.stiff_x()
+    np.testing.assert_allclose(X[0], np.broadcast_to(1 / (1 + 1500.0 / Z), X[0].shape), rtol=1e-9)
+    assert np.abs(X[1]).max() < 1e-9 and np.abs(X[2]).max() < 1e-9
+    np.testing.assert_allclose(X[3], 1.0, atol=1e-9)
+    np.testing.assert_allclose(r_.stiff_jacobian(), np.broadcast_to((1 + 1500.0 / Z) ** 2, (nr, 25)), rtol=1e-9)
+    r_ = RL.Relabelled([_Linear(0.01, 3.0e6)], *args)
+    np.testing.assert_allclose(r_.dZdZ, 0.01, atol=1e-9)
+    assert np.abs(r_.dZdR).max() < 1e-9 and np.abs(r_.dZdT).max() < 1e-9
+    np.testing.assert_allclose(r_.stiff_x()[3], 1 / 1.01, rtol=1e-9)
+
+
+def test_geometric_bump_builds_relabelled_elements(tmp_path_factory):
+    """MODEL_3D_GEOMETRIC_LIST bump: an undulation centred on the source axis keeps the
+    relabelled elements 1-D (PRT_1D), one off the axis makes them 3-D (PRT_3D) with per-slice
+    moduli; the time loop runs on the oracle; an unknown model is refused."""
+    from oracle.oracle_py import OracleDomain
+    s1 = solver.Simulation(_bump_inputs(tmp_path_factory, "bump1", "0$0"))
+    a = s1.build()
+    assert len(s1.relab) > 0 and set(a.prt_len.tolist()) == {1} and not s1.e3d.any()
+    s2 = solver.Simulation(_bump_inputs(tmp_path_factory, "bump2", "30$40"))
+    b = s2.build()
+    assert len(s2.relab) > 0 and (b.prt_len > 1).all() and s2.e3d[b.prt_elem].all()
+    o = OracleDomain(b)
+    o.step(60)
+    seis = o.seismograms(0, 60)
+    assert np.isfinite(seis).all() and np.abs(seis).max() > 0
+    d = _bump_inputs(tmp_path_factory, "bump3", "0$0")
+    from pathlib import Path
+    pm = Path(d) / "inparam.model"
+    pm.write_text(pm.read_text().replace("bump$", "crust1$"))
+    with pytest.raises(NotImplementedError, match="crust1"):
+        solver.Simulation(d).build()
+
+
+@pytest.mark.gpu
+def test_geometric_bump_gpu_matches_oracle(tmp_path_factory, ax3d_lib):
+    """The full solver on a mesh relabelled by an off-axis bump of the surface (PRT_3D
+    elements, per-slice moduli and masses from the relabelling Jacobians), GPU vs oracle."""
+    from oracle.oracle_py import OracleDomain
+    from axisem3d_gb300.capi import Ax3dDomain
+    spec = solver.Simulation(_bump_inputs(tmp_path_factory, "bumpg", "30$40")).build()
+    g, o = Ax3dDomain(spec), OracleDomain(spec)
+    g.step(60)
+    o.step(60)
+    a, b = g.seismograms(0, 60), o.seismograms(0, 60)
+    assert np.linalg.norm(a - b) <= 1e-5 * np.linalg.norm(b)
+    for which in ("displ", "veloc"):
+        x, y = g.get(which, "solid"), o.get(which, "solid")
+        assert np.linalg.norm(x - y) <= 1e-5 * np.linalg.norm(y)
