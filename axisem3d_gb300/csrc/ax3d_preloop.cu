@@ -261,6 +261,46 @@ __global__ void k_pre_mass(int n, const int32_t *__restrict__ rows, const int64_
     }
 }
 
+// 3-D model sampling (Material::addVolumetric3D, Material.cpp:96-231, for the project's
+// Gaussian-random model): the field rms sqrt(2 / M) sum_j cos(kr_j r + klR_j . n + phase_j) at
+// every GLL point of every element on its nr slices phi_k = 2 pi k / nr (or one phi in 2-D
+// mode), x = (s cos phi, s sin phi, z), r = |x|, n = x / r.  One thread per sample, FP64.
+__global__ void __launch_bounds__(256)
+    k_pre_gaussian_random(int n, const int32_t *__restrict__ rows, const int64_t *__restrict__ rofs,
+                          const double *__restrict__ crds, int modes, const double *__restrict__ kr,
+                          const double *__restrict__ klR, const double *__restrict__ ph, double amp,
+                          double phi2d, int use_phi2d, double *__restrict__ out) {
+    extern __shared__ double sm_modes[];  // kr, klR (3 x modes), phase
+    for (int i = threadIdx.x; i < modes; i += blockDim.x) {
+        sm_modes[i] = kr[i];
+        sm_modes[modes + i] = klR[i];
+        sm_modes[2 * modes + i] = klR[modes + i];
+        sm_modes[3 * modes + i] = klR[2 * modes + i];
+        sm_modes[4 * modes + i] = ph[i];
+    }
+    __syncthreads();
+    const double two_pi = 6.28318530717958647692;
+    for (int e = blockIdx.x; e < n; e += gridDim.x) {
+        const int nr = rows[e];
+        for (int t = threadIdx.x; t < nr * 25; t += blockDim.x) {
+            const int k = t / 25, p = t - k * 25;
+            const double s = crds[((int64_t)e * 25 + p) * 2], z = crds[((int64_t)e * 25 + p) * 2 + 1];
+            const double phi = use_phi2d ? phi2d : two_pi * (double)k / (double)nr;
+            double sp, cp;
+            sincos(phi, &sp, &cp);
+            const double x = s * cp, y = s * sp;
+            const double r = sqrt(x * x + y * y + z * z);
+            const double inv = 1.0 / fmax(r, 1e-9);
+            const double nx = x * inv, ny = y * inv, nz = z * inv;
+            double acc = 0.0;
+            for (int j = 0; j < modes; j++)
+                acc += cos(sm_modes[j] * r + nx * sm_modes[modes + j] + ny * sm_modes[2 * modes + j] +
+                           nz * sm_modes[3 * modes + j] + sm_modes[4 * modes + j]);
+            out[rofs[e] + t] = amp * acc;
+        }
+    }
+}
+
 template <typename T>
 struct Dev {
     T *p = nullptr;
@@ -480,6 +520,65 @@ extern "C" int ax3d_precompute_mass(int32_t device, int32_t n_elem, const int32_
     cudaSetDevice(prev_device);
     if (err != cudaSuccess) {
         g_pre_err = std::string("ax3d_precompute_mass || CUDA: ") + cudaGetErrorString(err);
+        return AX3D_ERR_CUDA;
+    }
+    return AX3D_OK;
+}
+
+extern "C" int ax3d_sample_gaussian_random(int32_t device, int32_t n_elem, const int32_t *rows, const double *crds,
+                                           int32_t modes, const double *kr, const double *klR, const double *phase,
+                                           double rms, int32_t use_phi2d, double phi2d, double *out) {
+    using namespace ax3d;
+    if (n_elem < 0 || modes < 1 || modes > 4096 ||
+        (n_elem && (!rows || !crds || !kr || !klR || !phase || !out))) {
+        g_pre_err = "ax3d_sample_gaussian_random || bad argument";
+        return AX3D_ERR_ARG;
+    }
+    std::vector<int64_t> rofs(n_elem);
+    int64_t nrow = 0;
+    for (int e = 0; e < n_elem; e++) {
+        if (rows[e] < 1) {
+            g_pre_err = "ax3d_sample_gaussian_random || rows must be >= 1";
+            return AX3D_ERR_ARG;
+        }
+        rofs[e] = nrow * 25;
+        nrow += rows[e];
+    }
+    if (n_elem == 0) return AX3D_OK;
+    const size_t nv = (size_t)nrow * 25;
+    int prev_device = 0;
+    cudaGetDevice(&prev_device);
+    cudaError_t err = cudaSetDevice(device);
+    Dev<int32_t> d_rows;
+    Dev<int64_t> d_rofs;
+    Dev<double> d_crds, d_kr, d_kl, d_ph, d_out;
+    if (err == cudaSuccess) err = d_rows.up(rows, n_elem);
+    if (err == cudaSuccess) err = d_rofs.up(rofs.data(), n_elem);
+    if (err == cudaSuccess) err = d_crds.up(crds, (size_t)n_elem * 50);
+    if (err == cudaSuccess) err = d_kr.up(kr, modes);
+    if (err == cudaSuccess) err = d_kl.up(klR, (size_t)3 * modes);
+    if (err == cudaSuccess) err = d_ph.up(phase, modes);
+    if (err == cudaSuccess) err = d_out.up(nullptr, nv);
+    if (err == cudaSuccess) {
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+        const int grid = std::min(n_elem, std::max(sms, 1) * 16);
+        const double amp = rms * std::sqrt(2.0 / (double)modes);
+        k_pre_gaussian_random<<<grid, 256, (size_t)5 * modes * sizeof(double)>>>(
+            n_elem, d_rows.p, d_rofs.p, d_crds.p, modes, d_kr.p, d_kl.p, d_ph.p, amp, phi2d, use_phi2d != 0, d_out.p);
+        err = cudaGetLastError();
+        if (err == cudaSuccess) err = cudaMemcpy(out, d_out.p, nv * sizeof(double), cudaMemcpyDeviceToHost);
+    }
+    d_rows.release();
+    d_rofs.release();
+    d_crds.release();
+    d_kr.release();
+    d_kl.release();
+    d_ph.release();
+    d_out.release();
+    cudaSetDevice(prev_device);
+    if (err != cudaSuccess) {
+        g_pre_err = std::string("ax3d_sample_gaussian_random || CUDA: ") + cudaGetErrorString(err);
         return AX3D_ERR_CUDA;
     }
     return AX3D_OK;

@@ -246,9 +246,10 @@ class Simulation:
     def build(self, kahan=False, nu_elem=None, preloop="host") -> DomainSpec:
         """Pack the domain.  nu_elem: optional per-element Fourier order (a learned or user
         Nu field) replacing NU_CONST; each point takes the maximum over its elements.
-        preloop = "gpu" computes the element geometry (ax3d_precompute_geometry), the 1-D
-        elemental masses (ax3d_precompute_mass) and the solid elements' moduli
-        (ax3d_precompute_elastic) in FP64 on the GPU instead of numpy."""
+        preloop = "gpu" computes the element geometry (ax3d_precompute_geometry), the
+        Gaussian-random 3-D model samples (ax3d_sample_gaussian_random), the 1-D elemental
+        masses (ax3d_precompute_mass) and the solid elements' moduli (ax3d_precompute_elastic)
+        in FP64 on the GPU instead of numpy."""
         par = self.par
         ex = Exodus.read(self.input_dir / par.get("MODEL_1D_EXODUS_MESH_FILE"))
         self.ex = ex
@@ -334,7 +335,8 @@ class Simulation:
             for nr in np.unique(e_nr):
                 sel = np.nonzero(e_nr == nr)[0]
                 cur, touched = M3D.apply_models(models, {"VP": vp[sel], "VS": vs[sel], "RHO": rho[sel]},
-                                                crds[sel], int(nr), fl[sel], phi2d=self.phi2d)
+                                                crds[sel], int(nr), fl[sel], phi2d=self.phi2d,
+                                                gpu=preloop == "gpu")
                 for j in np.nonzero(touched)[0]:
                     if self.phi2d is not None:
                         # 2-D mode: every slice sees the model at phi2D, so the element stays

@@ -224,6 +224,16 @@ int ax3d_precompute_geometry(int32_t device, int32_t n_elem, const double *nodes
    rho iFact for solids and iFact / (rho vp^2) for fluids. */
 int ax3d_precompute_mass(int32_t device, int32_t n_elem, const int32_t *rows, const double *ifact,
                          const float *rho, const float *vp, const uint8_t *fluid, double *mass);
+/* 3-D model sampling of the project's Gaussian-random volumetric model (no counterpart in
+   the reference, whose tomography models are data tables; the step is
+   Material::addVolumetric3D, Material.cpp:96-231) on `device`, FP64: for every element (rows
+   [n] slices, GLL coordinates crds [n][25][2] = (s, z)) and slice phi_k = 2 pi k / rows (or
+   phi2d for every slice when use_phi2d), the value rms sqrt(2 / modes) sum_j cos(kr_j r +
+   klR_j . n + phase_j) with x = (s cos phi, s sin phi, z), r = |x|, n = x / r; klR is
+   [3][modes].  out: [rows][25] per element back to back. */
+int ax3d_sample_gaussian_random(int32_t device, int32_t n_elem, const int32_t *rows, const double *crds,
+                                int32_t modes, const double *kr, const double *klR, const double *phase,
+                                double rms, int32_t use_phi2d, double phi2d, double *out);
 size_t ax3d_precompute_last_error(char *buf, size_t n);
 
 /* Strain and curl at receivers (PointwiseRecorder::record, PointwiseRecorder.cpp:96-130;

@@ -914,3 +914,25 @@ def test_geometric_bump_gpu_matches_oracle(tmp_path_factory, ax3d_lib):
     for which in ("displ", "veloc"):
         x, y = g.get(which, "solid"), o.get(which, "solid")
         assert np.linalg.norm(x - y) <= 1e-5 * np.linalg.norm(y)
+
+
+@pytest.mark.gpu
+def test_gpu_gaussian_random_sampling_matches_host(ax3d_lib):
+    """ax3d_sample_gaussian_random (FP64 on the GPU) against the host evaluation of the same
+    Gaussian-random model (FP32 phases, FP64 sum) on the rings of random GLL points, full 3-D
+    and 2-D mode."""
+    from axisem3d_gb300 import model3d as M3D
+    m = M3D.GaussianRandom(["VS", "ref1d", "0.04", "500", "200", "7"], 6371e3)
+    rng = np.random.default_rng(3)
+    n, nr = 40, 37
+    r = rng.uniform(3500e3, 6371e3, (n, 25))
+    t = rng.uniform(0.0, np.pi, (n, 25))
+    crds = np.stack([r * np.sin(t), r * np.cos(t)], -1)
+    for phi2d in (None, 0.7):
+        g = m.evaluate_rings_gpu(crds, nr, phi2d)
+        phi = 2 * np.pi * np.arange(nr) / nr if phi2d is None else np.full(nr, phi2d)
+        s, z = crds[..., 0], crds[..., 1]
+        xyz = np.stack([s[:, None, :] * np.cos(phi)[None, :, None], s[:, None, :] * np.sin(phi)[None, :, None],
+                        np.broadcast_to(z[:, None, :], (n, nr, 25))], -1)
+        h, _ = m.evaluate(xyz)
+        assert np.abs(g - h).max() <= 1e-5 * np.abs(h).max()
