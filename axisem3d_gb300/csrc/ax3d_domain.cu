@@ -879,8 +879,9 @@ struct ax3d_domain {
         sched = sc;
     }
     // ---- autotuner: the bucket schedule from timed trials on this domain's own elements ----
-    // Candidates: transform-length steps between buckets {1.06, 1.12, 1.25, 1.5} x shared-
-    // memory policy {two CTAs per SM, one CTA per SM} x side streams {1, NSIDE}.  Each trial
+    // Candidates: transform-length steps between buckets {1.06, 1.12, 1.25} x shared-memory
+    // policy {two CTAs per SM; one CTA per SM; two per SM for small rings and one 512-thread
+    // CTA per SM above} x side streams {1, NSIDE}.  Each trial
     // times `trials` element passes (after one untimed pass) with CUDA events on the domain's
     // stream; the point stiffness and the memory variables the passes change are saved
     // before and put back after every trial.  The choice is cached per process under the
@@ -933,8 +934,8 @@ struct ax3d_domain {
         Schedule best = start;
         float best_ms = 1e30f;
         std::string log;
-        for (double ratio : {1.06, 1.12, 1.25, 1.5})
-            for (int policy : {0, 1})
+        for (double ratio : {1.06, 1.12, 1.25})
+            for (int policy : {0, 1, 2})
                 for (int nside : {1, (int)NSIDE}) {
                     Schedule sc;
                     sc.ratio = ratio;
@@ -1594,6 +1595,23 @@ int ax3d_enable_timers(ax3d_domain *d, int32_t enable) {
     return guard([&] {
         if (!d) throw Error(AX3D_ERR_ARG, "ax3d_enable_timers || null domain");
         d->timers = enable != 0;
+    });
+}
+
+int ax3d_set_schedule(ax3d_domain *d, double ratio, int32_t policy, int32_t nside) {
+    return guard([&] {
+        if (!d) throw Error(AX3D_ERR_ARG, "ax3d_set_schedule || null domain");
+        if (!(ratio > 1.0 && ratio < 4.0) || policy < 0 || policy > 2 || nside < 1)
+            throw Error(AX3D_ERR_ARG, "ax3d_set_schedule || ratio in (1, 4), policy 0..2, nside >= 1");
+        d->need_final();
+        CK(cudaSetDevice(d->device));
+        ax3d_domain::Schedule sc;
+        sc.ratio = ratio;
+        sc.policy = policy;
+        sc.nside = nside;
+        d->build_buckets(sc, d->stream);
+        d->drop_graph();
+        CK(cudaStreamSynchronize(d->stream));
     });
 }
 

@@ -42,6 +42,7 @@ struct PhysBucket {
     int n_max = 0;             // most Fourier orders in the bucket
     int npts_chunk = 25;       // GLL points per CTA (shared-memory budget)
     int csize = 1;             // CTAs per cluster sharing one element
+    int nt = 256;              // threads per CTA (256, or 512 with a whole SM's shared memory)
     size_t smem = 0;
     int grid = 0;              // persistent CTAs (a multiple of csize)
 };
@@ -56,7 +57,7 @@ void init_phys_attributes();
 void set_g_matrices_phys(const float *g_gll, const float *g_glj, cudaStream_t s);
 // FP64 plans, twiddles, chirps and kernel spectra for every used ring size (used[nr] != 0)
 FftTables build_fft_tables(const std::vector<char> &used);
-size_t phys_smem_bytes(int Lmax, int nsq, int npts_chunk);
+size_t phys_smem_bytes(int Lmax, int nsq, int npts_chunk, int nthreads = 256);
 void size_phys_bucket(PhysBucket &b, bool solid, int policy = 0);
 int phys_grid(const PhysBucket &b, bool solid, int num_sms);
 

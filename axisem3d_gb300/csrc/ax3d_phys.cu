@@ -46,8 +46,7 @@ namespace ax3d {
 
 namespace {
 
-constexpr int NT = 256;      // threads per CTA
-constexpr int NW = NT / 32;  // warps per CTA
+constexpr int NT = 256;      // threads per CTA (512 for buckets of policy 2)
 constexpr int WSCR = 125;    // per-warp grad / divergence scratch (float2)
 constexpr int RESEED = 8;    // direct DFT: exact twiddle reload interval
 constexpr int DIRECT_MAX = 257;  // largest prime handled by a direct pass
@@ -686,9 +685,9 @@ struct PhysSmem {
 
 }  // namespace
 
-size_t phys_smem_bytes(int Lmax, int nsq, int npts_chunk) {
+size_t phys_smem_bytes(int Lmax, int nsq, int npts_chunk, int nthreads) {
     return (size_t)PLAN_BYTES + (size_t)8 * Lmax + (size_t)8 * ((Lmax + 1) & ~1) + 4 * 64 + (size_t)8 * Lmax * nsq * npts_chunk +
-           (size_t)8 * NW * WSCR;
+           (size_t)8 * (nthreads / 32) * WSCR;
 }
 
 // ------------------------------------------------------------------------------------
@@ -727,9 +726,10 @@ __device__ __noinline__ void phase_grad(const ElemTable &T, const PointTable &P,
     }
     USrc us;
     us.init(P, u, SOLID, T.pts[e * NPE + p]);
-    // this CTA's orders: a = crank NW + warp + k C NW; the displacement of the next two
-    // of them is in flight while one is differentiated
-    const int a0 = crank * NW + warp, da = C * NW;
+    // this CTA's orders: a = crank nw + warp + k C nw (nw warps per CTA); the displacement
+    // of the next two of them is in flight while one is differentiated
+    const int nwc = (int)(blockDim.x >> 5);
+    const int a0 = crank * nwc + warp, da = C * nwc;
     float2 un[3], un2[3];
     if (active) {
         us.load(SOLID, a0, un);
@@ -927,7 +927,8 @@ __device__ __noinline__ void phase_quad(const ElemTable &T, const PointTable &P,
         plim = pnu - (pnr % 2 == 0);
         st = T.stiff + P.sofs[pt];
     }
-    for (int a = crank * NW + warp; a < n; a += C * NW) {
+    const int nwc = (int)(blockDim.x >> 5);
+    for (int a = crank * nwc + warp; a < n; a += C * nwc) {
         float2 old[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
         const bool row = SOLID && direct && active && a <= pnu;
         if (rmw && row && a <= plim) {  // issued before the divergence so the loads overlap it
@@ -980,8 +981,8 @@ __device__ __noinline__ void phase_quad(const ElemTable &T, const PointTable &P,
 // The kernel: SOLID = 6 strain components (3 sequences per point), else the fluid's 3
 // potential-gradient components (2 sequences per point).
 // ------------------------------------------------------------------------------------
-template <bool SOLID>
-__global__ void __launch_bounds__(NT, 2)
+template <bool SOLID, int NTT>
+__global__ void __launch_bounds__(NTT, NTT <= 256 ? 2 : 1)
     k_elem_phys(const __grid_constant__ ElemTable T, const __grid_constant__ PointTable P,
                 const float2 *__restrict__ u, const int32_t *__restrict__ elems, int count, int Pc, int Lmax,
                 const __grid_constant__ PhysTables X, const __grid_constant__ SLS sls, int overwrite) {
@@ -1027,17 +1028,17 @@ __global__ void __launch_bounds__(NT, 2)
         pk.inv_nr = 1.f / (float)nr;
         const float hsc = pl.kind == 0 ? 0.5f / (float)nr : 0.5f;
         const float *md = T.moduli + T.mofs[e];
-        for (int m = threadIdx.x; m < L; m += NT) tw[m] = X.f2[pl.tw + m];
+        for (int m = threadIdx.x; m < L; m += blockDim.x) tw[m] = X.f2[pl.tw + m];
         if (!blue)
-            for (int m = threadIdx.x; m < nr; m += NT) sm.rev[m] = X.i32[pl.rev + m];
+            for (int m = threadIdx.x; m < nr; m += blockDim.x) sm.rev[m] = X.i32[pl.rev + m];
         if (pl.kind == 2)
-            for (int m = threadIdx.x; m < nr; m += NT) sm.ord[m] = X.i32[pl.ord + m];
+            for (int m = threadIdx.x; m < nr; m += blockDim.x) sm.ord[m] = X.i32[pl.ord + m];
         // positions the packing does not write: the Nyquist order (even nr) and the
         // Bluestein padding [nr, Lb)
         if (nr % 2 == 0)
-            for (int s = threadIdx.x; s < ns; s += NT) buf[(int64_t)(nr / 2) * S + s] = make_float2(0.f, 0.f);
+            for (int s = threadIdx.x; s < ns; s += blockDim.x) buf[(int64_t)(nr / 2) * S + s] = make_float2(0.f, 0.f);
         if (blue)
-            for (int t = threadIdx.x; t < (Lb - nr) * ns; t += NT)
+            for (int t = threadIdx.x; t < (Lb - nr) * ns; t += blockDim.x)
                 buf[(int64_t)(nr + t / ns) * S + t % ns] = make_float2(0.f, 0.f);
         __syncthreads();  // the order table is read by the packing in phase 1
         // ---- phase 1: Hermitian-packed strain spectra (this CTA's orders, all points) ----
@@ -1138,8 +1139,10 @@ void set_g_matrices_phys(const float *g_gll, const float *g_glj, cudaStream_t s)
 }
 
 void init_phys_attributes() {
-    cudaFuncSetAttribute(k_elem_phys<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_CAP);
-    cudaFuncSetAttribute(k_elem_phys<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_CAP);
+    cudaFuncSetAttribute(k_elem_phys<true, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_CAP);
+    cudaFuncSetAttribute(k_elem_phys<false, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_CAP);
+    cudaFuncSetAttribute(k_elem_phys<true, 2 * NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_CAP);
+    cudaFuncSetAttribute(k_elem_phys<false, 2 * NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_CAP);
 }
 
 namespace {
@@ -1354,17 +1357,35 @@ FftTables build_fft_tables(const std::vector<char> &used) {
     return T;
 }
 
-// Points per CTA, cluster size and shared memory of a bucket.  Policy 0: all 25 points in
-// one CTA when two CTAs per SM fit, else the smallest cluster whose CTAs fit (two per SM if
-// possible).  Policy 1: the smallest cluster whose CTAs fit the whole shared memory of an SM
-// (one CTA per SM for rings up to ~360 samples, fewer clusters above).
+// Points per CTA, cluster size, threads per CTA and shared memory of a bucket.
+//   Policy 0: 256-thread CTAs; all 25 points in one CTA when two CTAs per SM fit, else the
+//             smallest cluster whose CTAs fit (two per SM if possible).
+//   Policy 1: 256-thread CTAs; the smallest cluster whose CTAs fit the whole shared memory
+//             of an SM (one CTA per SM for rings up to ~360 samples, fewer clusters above).
+//   Policy 2: as policy 0 while all points fit two CTAs per SM; larger rings take 512-thread
+//             CTAs with the whole shared memory of an SM (16 warps per SM as two 256-thread
+//             CTAs give), in the smallest cluster that fits: no cluster up to ~360 samples.
 void size_phys_bucket(PhysBucket &b, bool solid, int policy) {
     const int nsq = solid ? 3 : 2;
     b.npts_chunk = 0;
+    b.nt = NT;
+    if (policy == 2 && phys_smem_bytes(b.L_max, nsq, NPE, NT) > SMEM_TWO) {
+        for (int pc = NPE; pc >= 1; pc--) {
+            const size_t sm = phys_smem_bytes(b.L_max, nsq, pc, 2 * NT);
+            const int C = (NPE + pc - 1) / pc;
+            if (sm <= SMEM_CAP && C <= CLUSTER_MAX) {
+                b.npts_chunk = pc;
+                b.csize = C;
+                b.smem = sm;
+                b.nt = 2 * NT;
+                return;
+            }
+        }
+    }
     const std::vector<size_t> caps = policy == 1 ? std::vector<size_t>{SMEM_CAP} : std::vector<size_t>{SMEM_TWO, SMEM_CAP};
     for (size_t cap : caps) {
         for (int pc = NPE; pc >= 1; pc--) {
-            const size_t sm = phys_smem_bytes(b.L_max, nsq, pc);
+            const size_t sm = phys_smem_bytes(b.L_max, nsq, pc, NT);
             const int C = (NPE + pc - 1) / pc;
             if (sm <= cap && C <= CLUSTER_MAX) {
                 b.npts_chunk = pc;
@@ -1377,11 +1398,10 @@ void size_phys_bucket(PhysBucket &b, bool solid, int policy) {
 }
 
 namespace {
-template <bool SOLID>
 cudaLaunchConfig_t phys_config(const PhysBucket &b, cudaLaunchAttribute *at, cudaStream_t s) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)std::max(b.grid, b.csize));
-    cfg.blockDim = dim3(NT);
+    cfg.blockDim = dim3((unsigned)b.nt);
     cfg.dynamicSmemBytes = b.smem;
     cfg.stream = s;
     at[0].id = cudaLaunchAttributeClusterDimension;
@@ -1392,18 +1412,21 @@ cudaLaunchConfig_t phys_config(const PhysBucket &b, cudaLaunchAttribute *at, cud
     cfg.numAttrs = 1;
     return cfg;
 }
+// the instantiation of a bucket: solid or fluid, 256 or 512 threads
+template <typename F>
+void with_kernel(bool solid, int nt, F f) {
+    if (solid)
+        nt > NT ? f(k_elem_phys<true, 2 * NT>) : f(k_elem_phys<true, NT>);
+    else
+        nt > NT ? f(k_elem_phys<false, 2 * NT>) : f(k_elem_phys<false, NT>);
+}
 }  // namespace
 
 int phys_grid(const PhysBucket &b, bool solid, int num_sms) {
     cudaLaunchAttribute at[1];
     int ncl = 0;
-    if (solid) {
-        cudaLaunchConfig_t cfg = phys_config<true>(b, at, nullptr);
-        cudaOccupancyMaxActiveClusters(&ncl, k_elem_phys<true>, &cfg);
-    } else {
-        cudaLaunchConfig_t cfg = phys_config<false>(b, at, nullptr);
-        cudaOccupancyMaxActiveClusters(&ncl, k_elem_phys<false>, &cfg);
-    }
+    cudaLaunchConfig_t cfg = phys_config(b, at, nullptr);
+    with_kernel(solid, b.nt, [&](auto k) { cudaOccupancyMaxActiveClusters(&ncl, k, &cfg); });
     if (ncl <= 0) ncl = std::max(1, num_sms / b.csize);
     return b.csize * std::max(1, std::min(b.count, ncl));
 }
@@ -1412,15 +1435,11 @@ void launch_elem_phys(bool solid, const ElemTable &T, const PointTable &P, const
                       const PhysTables &X, const SLS &sls, bool overwrite, cudaStream_t s) {
     if (b.count <= 0) return;
     cudaLaunchAttribute at[1];
-    if (solid) {
-        cudaLaunchConfig_t cfg = phys_config<true>(b, at, s);
-        cudaLaunchKernelEx(&cfg, k_elem_phys<true>, T, P, u, (const int32_t *)b.elems, b.count, b.npts_chunk,
-                           b.L_max, X, sls, (int)overwrite);
-    } else {
-        cudaLaunchConfig_t cfg = phys_config<false>(b, at, s);
-        cudaLaunchKernelEx(&cfg, k_elem_phys<false>, T, P, u, (const int32_t *)b.elems, b.count, b.npts_chunk,
-                           b.L_max, X, sls, (int)overwrite);
-    }
+    cudaLaunchConfig_t cfg = phys_config(b, at, s);
+    with_kernel(solid, b.nt, [&](auto k) {
+        cudaLaunchKernelEx(&cfg, k, T, P, u, (const int32_t *)b.elems, b.count, b.npts_chunk, b.L_max, X, sls,
+                           (int)overwrite);
+    });
 }
 
 }  // namespace ax3d

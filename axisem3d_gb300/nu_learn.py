@@ -99,12 +99,12 @@ def decode(y, nu_full, shift=0.0):
 SHIFTS = (0.0, 0.05, 0.1, 0.15, 0.2, 0.3, 0.45, 0.7)
 
 
-def calibrate_shift(sim, y, seis_full, nu_full, steps, target, log=print):
+def calibrate_shift(sim, y, seis_full, nu_full, steps, target, log=print, preloop="gpu"):
     """The smallest encoded-space shift of the predictions whose run reproduces a validation
     model's full-Nu seismograms within `target` relative L2 (calibration by simulation on a
     model the network was not fitted on); 1.0 (full Nu) if none does."""
     for sh in SHIFTS:
-        spec = sim.build(nu_elem=decode(y, nu_full, sh))
+        spec = sim.build(nu_elem=decode(y, nu_full, sh), preloop=preloop)
         seis, _, _, upd = run(spec, steps)
         mis = float(np.linalg.norm(seis - seis_full) / np.linalg.norm(seis_full))
         log(f"calibration shift {sh:.2f}: misfit {mis:.4g}, updates/step {upd}")
@@ -134,11 +134,11 @@ def run(spec, steps, learn=None):
 
 
 def experiment(work, n_train=64, n_test=16, nu_full=64, steps=600, epochs=200, batch=4096, lr=2e-3,
-               eps=1e-3, interval=5, mesh_kw=None, out=None, log=print, target=0.005):
+               eps=1e-3, interval=5, mesh_kw=None, out=None, log=print, target=0.005, preloop="gpu"):
     """Train on the wisdom of n_train - 1 full-Nu runs, calibrate the prediction shift on the
     last training model by simulation (misfit <= target, half the 1 % bar), evaluate on
-    n_test held-out models.  Returns the summary dict (also written to out/summary.json with
-    the parameters in out/nu_mlp.npz)."""
+    n_test held-out models.  Every pre-loop runs on the GPU unless preloop = "host".  Returns the
+    summary dict (also written to out/summary.json with the parameters in out/nu_mlp.npz)."""
     from .nu_mlp import NuMLP
     work = Path(work)
     X, Y, pre = [], [], []
@@ -148,7 +148,7 @@ def experiment(work, n_train=64, n_test=16, nu_full=64, steps=600, epochs=200, b
         d = write_case(work / f"train{i}", 1000 + i, nu_full, steps, mesh_kw)
         t0 = time.perf_counter()
         sim = solver.Simulation(d)
-        spec = sim.build()
+        spec = sim.build(preloop=preloop)
         pre.append(time.perf_counter() - t0)
         seis, t, wis, _ = run(spec, steps, learn=(interval, eps))
         t_train_runs += t
@@ -174,7 +174,8 @@ def experiment(work, n_train=64, n_test=16, nu_full=64, steps=600, epochs=200, b
     shift, val_misfit = 0.0, None
     if val is not None:
         shift, val_misfit = calibrate_shift(val[0], net.forward(val[1]).cpu().numpy(), nu_full=nu_full,
-                                            seis_full=val[2], steps=steps, target=target, log=log)
+                                            seis_full=val[2], steps=steps, target=target, log=log,
+                                            preloop=preloop)
     tests = []
     seis_l_all, specs_l, pre_l_all = [], [], []
     for i in range(n_test):
@@ -182,7 +183,7 @@ def experiment(work, n_train=64, n_test=16, nu_full=64, steps=600, epochs=200, b
         # plain full-Nu route: pre-loop, then the loop
         t0 = time.perf_counter()
         sim = solver.Simulation(d)
-        spec_f = sim.build()
+        spec_f = sim.build(preloop=preloop)
         pre_f = time.perf_counter() - t0
         seis_f, t_f, _, upd_f = run(spec_f, steps)
         _, t_fl, wis, _ = run(spec_f, steps, learn=(interval, eps))
@@ -197,13 +198,13 @@ def experiment(work, n_train=64, n_test=16, nu_full=64, steps=600, epochs=200, b
         t_inf = time.perf_counter() - t0
         nu_e = decode(y, nu_full, shift)
         t0 = time.perf_counter()
-        spec_l = sim.build(nu_elem=nu_e)
+        spec_l = sim.build(nu_elem=nu_e, preloop=preloop)
         pre_l = time.perf_counter() - t0
         seis_l, t_l, _, upd_l = run(spec_l, steps)
         mis = float(np.linalg.norm(seis_l - seis_f) / np.linalg.norm(seis_f))
         # the reference's route without a network: reuse the wisdom of this model's own
         # full run (which must be paid first)
-        spec_w = sim.build(nu_elem=np.maximum(element_labels(spec_f, wis), 1))
+        spec_w = sim.build(nu_elem=np.maximum(element_labels(spec_f, wis), 1), preloop=preloop)
         seis_w, t_w, _, upd_w = run(spec_w, steps)
         mis_w = float(np.linalg.norm(seis_w - seis_f) / np.linalg.norm(seis_f))
         tts_f = pre_f + t_f

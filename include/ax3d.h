@@ -312,6 +312,12 @@ int ax3d_enable_timers(ax3d_domain *d, int32_t enable);
    domain's histogram of transform lengths; a later domain of the same shape takes it
    without trials.  `report` (len bytes, may be NULL) receives the choice and the times. */
 int ax3d_autotune(ax3d_domain *d, int32_t trials, char *report, size_t len);
+/* No counterpart in the reference.  After ax3d_finalize: sets the bucket schedule by hand --
+   ratio (> 1) between the transform lengths of neighbouring buckets, shared-memory policy
+   (0: 256-thread CTAs, two per SM where they fit; 1: 256-thread CTAs with an SM's whole
+   shared memory; 2: as 0 for rings that fit two per SM, 512-thread CTAs with an SM's whole
+   shared memory above) and side streams (1..3) -- and recaptures the step. */
+int ax3d_set_schedule(ax3d_domain *d, double ratio, int32_t policy, int32_t nside);
 int ax3d_read_timers(ax3d_domain *d, double *ms, int64_t *launches);
 
 int ax3d_destroy(ax3d_domain *d);
