@@ -106,7 +106,7 @@ def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
     lib.ax3d_last_error.restype = C.c_size_t
     lib.ax3d_enable_timers.argtypes = [C.c_void_p, C.c_int32]
     lib.ax3d_autotune.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, C.c_size_t]
-    lib.ax3d_set_schedule.argtypes = [C.c_void_p, C.c_double, C.c_int32, C.c_int32]
+    lib.ax3d_set_schedule.argtypes = [C.c_void_p, C.c_double, C.c_int32, C.c_int32, C.c_int32]
     lib.ax3d_read_timers.argtypes = [C.c_void_p, P_F64, P_I64]
     if path is None:
         _LIB = lib
@@ -334,9 +334,9 @@ class Ax3dDomain(_DomainBase):
         self._ck(self.lib.ax3d_autotune(self.h, int(trials), buf, 4096))
         return buf.value.decode()
 
-    def set_schedule(self, ratio: float = 1.12, policy: int = 0, nside: int = 3):
+    def set_schedule(self, ratio: float = 1.12, policy: int = 0, nside: int = 3, merge: bool = False):
         """ax3d_set_schedule: the physical-space bucket schedule, by hand."""
-        self._ck(self.lib.ax3d_set_schedule(self.h, float(ratio), int(policy), int(nside)))
+        self._ck(self.lib.ax3d_set_schedule(self.h, float(ratio), int(policy), int(nside), int(merge)))
 
     def enable_timers(self, on: bool = True):
         self._ck(self.lib.ax3d_enable_timers(self.h, int(on)))

@@ -143,7 +143,7 @@ struct ax3d_domain {
     // and side streams used; set at ax3d_finalize, changed by ax3d_autotune
     struct Schedule {
         double ratio = 1.12;
-        int policy = 0, nside = NSIDE;
+        int policy = 0, nside = NSIDE, merge = 0;
     } sched;
     std::vector<int32_t> phys3_s_list, phys3_f_list;  // physical-space elements
     std::vector<int32_t> lbuf_of_nr;                   // buffer length of each ring size's plan
@@ -852,28 +852,70 @@ struct ax3d_domain {
                 const int b = (int)std::floor(std::log((double)lbuf_of_nr[e_nr[e]]) / std::log(sc.ratio));
                 phys[fl][b].push_back(e);
             }
+        // size every bucket; with `merge`, buckets of one launch shape (CTAs per cluster,
+        // threads per CTA) then become one persistent launch over their elements, longest
+        // transforms first, its shared memory laid out for the longest and its points per CTA
+        // the fewest of the merged buckets
+        struct Sized {
+            ax3d::PhysBucket b;
+            std::vector<int32_t> elems;
+        };
+        std::vector<Sized> sized[2];
+        for (int fl = 0; fl < 2; fl++)
+            for (auto &kv : phys[fl]) {
+                Sized z;
+                z.b.count = (int)kv.second.size();
+                for (int e : kv.second) {
+                    z.b.L_max = std::max(z.b.L_max, lbuf_of_nr[e_nr[e]]);
+                    z.b.n_max = std::max(z.b.n_max, e_nr[e] / 2 + 1);
+                }
+                ax3d::size_phys_bucket(z.b, !fl, sc.policy);
+                if (z.b.npts_chunk <= 0)
+                    throw Error(AX3D_ERR_UNSUPPORTED, "ax3d_finalize || nr too large for the physical-space kernel");
+                z.elems = kv.second;
+                sized[fl].push_back(z);
+            }
+        if (sc.merge)
+            for (int fl = 0; fl < 2; fl++) {
+                std::map<std::pair<int, int>, Sized> byshape;
+                for (auto &z : sized[fl]) {
+                    auto key = std::make_pair(z.b.csize, z.b.nt);
+                    auto it = byshape.find(key);
+                    if (it == byshape.end()) {
+                        byshape[key] = z;
+                        continue;
+                    }
+                    Sized &m = it->second;
+                    m.elems.insert(m.elems.end(), z.elems.begin(), z.elems.end());
+                    m.b.count += z.b.count;
+                    m.b.L_max = std::max(m.b.L_max, z.b.L_max);
+                    m.b.n_max = std::max(m.b.n_max, z.b.n_max);
+                    m.b.npts_chunk = std::min(m.b.npts_chunk, z.b.npts_chunk);
+                    m.b.smem = std::max(m.b.smem, z.b.smem);
+                }
+                sized[fl].clear();
+                for (auto &kv : byshape) {
+                    Sized z = kv.second;
+                    std::stable_sort(z.elems.begin(), z.elems.end(), [&](int32_t a, int32_t b) {
+                        return lbuf_of_nr[e_nr[a]] > lbuf_of_nr[e_nr[b]];
+                    });
+                    z.b.smem = ax3d::phys_smem_bytes(z.b.L_max, fl ? 2 : 3, z.b.npts_chunk, z.b.nt);
+                    sized[fl].push_back(z);
+                }
+            }
         bucket_lists.clear();
-        bucket_lists.resize(phys[0].size() + phys[1].size());
+        bucket_lists.resize(sized[0].size() + sized[1].size());
         buckets_s.clear();
         buckets_f.clear();
         size_t bi = 0;
         for (int fl = 0; fl < 2; fl++) {
             auto &dst = fl ? buckets_f : buckets_s;
-            for (auto &kv : phys[fl]) {
-                ax3d::PhysBucket b;
-                b.count = (int)kv.second.size();
-                for (int e : kv.second) {
-                    b.L_max = std::max(b.L_max, lbuf_of_nr[e_nr[e]]);
-                    b.n_max = std::max(b.n_max, e_nr[e] / 2 + 1);
-                }
-                ax3d::size_phys_bucket(b, !fl, sc.policy);
-                if (b.npts_chunk <= 0)
-                    throw Error(AX3D_ERR_UNSUPPORTED, "ax3d_finalize || nr too large for the physical-space kernel");
-                b.grid = ax3d::phys_grid(b, !fl, num_sms);
-                bucket_lists[bi].upload(kv.second, st);
-                b.elems = bucket_lists[bi].p;
+            for (auto &z : sized[fl]) {
+                z.b.grid = ax3d::phys_grid(z.b, !fl, num_sms);
+                bucket_lists[bi].upload(z.elems, st);
+                z.b.elems = bucket_lists[bi].p;
                 bi++;
-                dst.push_back(b);
+                dst.push_back(z.b);
             }
         }
         sched = sc;
@@ -910,8 +952,8 @@ struct ax3d_domain {
         if (hit != tune_cache().end()) {
             build_buckets(hit->second, stream);
             drop_graph();
-            snprintf(buf, sizeof buf, "cached: ratio %.2f, policy %d, side streams %d", hit->second.ratio,
-                     hit->second.policy, hit->second.nside);
+            snprintf(buf, sizeof buf, "cached: ratio %.2f, policy %d, side streams %d, merged %d", hit->second.ratio,
+                     hit->second.policy, hit->second.nside, hit->second.merge);
             return buf;
         }
         trials = std::max(1, trials);
@@ -934,13 +976,14 @@ struct ax3d_domain {
         Schedule best = start;
         float best_ms = 1e30f;
         std::string log;
+        std::vector<Schedule> cands;
         for (double ratio : {1.06, 1.12, 1.25})
             for (int policy : {0, 1, 2})
-                for (int nside : {1, (int)NSIDE}) {
-                    Schedule sc;
-                    sc.ratio = ratio;
-                    sc.policy = policy;
-                    sc.nside = nside;
+                for (int nside : {1, (int)NSIDE}) cands.push_back(Schedule{ratio, policy, nside, 0});
+        for (int policy : {0, 2})
+            for (int nside : {1, (int)NSIDE}) cands.push_back(Schedule{1.12, policy, nside, 1});
+        for (const Schedule &sc : cands) {
+                {
                     build_buckets(sc, stream);
                     launch_elements(false);  // untimed: first launch of this shape
                     CK(cudaEventRecord(a, stream));
@@ -950,7 +993,7 @@ struct ax3d_domain {
                     float ms = 0.f;
                     CK(cudaEventElapsedTime(&ms, a, b));
                     ms /= trials;
-                    snprintf(buf, sizeof buf, " %.2f/%d/%d:%.2f", ratio, policy, nside, ms);
+                    snprintf(buf, sizeof buf, " %.2f/%d/%d%s:%.2f", sc.ratio, sc.policy, sc.nside, sc.merge ? "m" : "", ms);
                     log += buf;
                     if (ms < best_ms) {
                         best_ms = ms;
@@ -960,6 +1003,7 @@ struct ax3d_domain {
                     copy(d_fs.p, save_fs.p, (size_t)nfluid * sizeof(float2));
                     copy(d_mem.p, save_mem.p, (size_t)d_mem.n * sizeof(float));
                 }
+        }
         build_buckets(best, stream);
         drop_graph();
         CK(cudaStreamSynchronize(stream));
@@ -967,8 +1011,9 @@ struct ax3d_domain {
         pool.push_back(b);
         timers = was_timers;
         tune_cache()[key] = best;
-        snprintf(buf, sizeof buf, "chose ratio %.2f, policy %d, side streams %d (%.2f ms per element pass); trials ms:",
-                 best.ratio, best.policy, best.nside, best_ms);
+        snprintf(buf, sizeof buf,
+                 "chose ratio %.2f, policy %d, side streams %d, merged %d (%.2f ms per element pass); trials ms:",
+                 best.ratio, best.policy, best.nside, best.merge, best_ms);
         return std::string(buf) + log;
     }
     // Element stiffness (Domain::computeStiff's element loop).  The physical-space buckets
@@ -1598,7 +1643,7 @@ int ax3d_enable_timers(ax3d_domain *d, int32_t enable) {
     });
 }
 
-int ax3d_set_schedule(ax3d_domain *d, double ratio, int32_t policy, int32_t nside) {
+int ax3d_set_schedule(ax3d_domain *d, double ratio, int32_t policy, int32_t nside, int32_t merge) {
     return guard([&] {
         if (!d) throw Error(AX3D_ERR_ARG, "ax3d_set_schedule || null domain");
         if (!(ratio > 1.0 && ratio < 4.0) || policy < 0 || policy > 2 || nside < 1)
@@ -1609,6 +1654,7 @@ int ax3d_set_schedule(ax3d_domain *d, double ratio, int32_t policy, int32_t nsid
         sc.ratio = ratio;
         sc.policy = policy;
         sc.nside = nside;
+        sc.merge = merge != 0;
         d->build_buckets(sc, d->stream);
         d->drop_graph();
         CK(cudaStreamSynchronize(d->stream));

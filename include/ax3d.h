@@ -305,8 +305,8 @@ int ax3d_enable_timers(ax3d_domain *d, int32_t enable);
 /* No counterpart in the reference, whose element cost table (Domain.cpp:349-382) weights
    the METIS partition instead (Mesh.cpp:412-588).  After ax3d_finalize: chooses the
    schedule of the physical-space element buckets -- the step of transform length between
-   buckets, the shared-memory policy (two CTAs per SM, or one CTA per SM with fewer
-   clusters) and the side streams -- from timed element passes on this domain's own
+   buckets, the shared-memory policy (see ax3d_set_schedule), the side streams and whether
+   buckets of one launch shape merge into one launch -- from timed element passes on this domain's own
    elements (`trials` timed passes per candidate; the fields are left as they were), then
    recaptures the step.  The choice is cached for the process under the device name and the
    domain's histogram of transform lengths; a later domain of the same shape takes it
@@ -316,8 +316,10 @@ int ax3d_autotune(ax3d_domain *d, int32_t trials, char *report, size_t len);
    ratio (> 1) between the transform lengths of neighbouring buckets, shared-memory policy
    (0: 256-thread CTAs, two per SM where they fit; 1: 256-thread CTAs with an SM's whole
    shared memory; 2: as 0 for rings that fit two per SM, 512-thread CTAs with an SM's whole
-   shared memory above) and side streams (1..3) -- and recaptures the step. */
-int ax3d_set_schedule(ax3d_domain *d, double ratio, int32_t policy, int32_t nside);
+   shared memory above), side streams (1..3) and merge (nonzero: the buckets of one launch
+   shape -- CTAs per cluster, threads per CTA -- run as one persistent launch over their
+   elements, longest transforms first) -- and recaptures the step. */
+int ax3d_set_schedule(ax3d_domain *d, double ratio, int32_t policy, int32_t nside, int32_t merge);
 int ax3d_read_timers(ax3d_domain *d, double *ms, int64_t *launches);
 
 int ax3d_destroy(ax3d_domain *d);

@@ -344,19 +344,20 @@ def test_autotuned_schedule_keeps_results(ax3d_lib):
     assert g2.autotune(1).startswith("cached")
 
 
-@pytest.mark.parametrize("policy", [1, 2])
-def test_schedule_policies_match_oracle(ax3d_lib, policy):
+@pytest.mark.parametrize("policy,merge", [(1, False), (2, False), (0, True), (2, True)])
+def test_schedule_policies_match_oracle(ax3d_lib, policy, merge):
     """The benchmark's domain (Nu 8-256) under the other bucket schedules: policy 1 (256-thread
     CTAs with an SM's whole shared memory) and policy 2 (512-thread CTAs above the rings that
-    fit two CTAs per SM, clusters of 512-thread CTAs for the largest), compute_stiff and three
-    steps against the oracle."""
+    fit two CTAs per SM, clusters of 512-thread CTAs for the largest), each also with the
+    buckets of one launch shape merged into one launch; compute_stiff and three steps against
+    the oracle."""
     from oracle.oracle_py import OracleDomain
     from axisem3d_gb300 import workloads as W
     from axisem3d_gb300.capi import Ax3dDomain
     spec = W.element_benchmark(n_elem=20, seed=9, att=ATT_CG4)
     u0 = W.benchmark_displacement(spec, seed=8)
     g, o = Ax3dDomain(spec), OracleDomain(spec)
-    g.set_schedule(1.12, policy, 2)
+    g.set_schedule(1.12, policy, 2, merge)
     for d in (g, o):
         d.set("displ", "solid", u0)
         d.compute_stiff()
