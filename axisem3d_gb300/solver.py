@@ -478,10 +478,18 @@ class Simulation:
         dokappa = par.get("ATTENUATION_QKAPPA", bool)
         # time step (Mesh::getDeltaT x TIME_DELTA_T_FACTOR, or TIME_DELTA_T)
         dt_user = par.get("TIME_DELTA_T", float)
-        # Quad::getDeltaT (Quad.cpp:291-305): dt on slices scales with the deformed hmin
+        # Quad::getDeltaT (Quad.cpp:291-305): dt on slices = courant hmin / vmax with the mesh's
+        # courant = dt_ref vmax_ref / hmin_ref, hmin from the deformed element (relabelling)
+        # and vmax = the largest P velocity of each slice after the 3-D models
+        # (Material::getVMax, Material.cpp:521-537); the element's dt is the smallest
         dt_e = ex.dt.astype(float).copy()
-        for e, r_ in relab.items():
-            dt_e[e] *= r_.hmin_slices().min() / r_.hmin_ref()
+        for e in set(np.nonzero(e3d)[0].tolist()) | set(relab):
+            ratio = np.ones(int(e_nr[e]))
+            if e3d[e]:
+                ratio = ratio * (vp[e].max() / props3[e]["VP"].max(1))
+            if e in relab:
+                ratio = ratio * (relab[e].hmin_slices() / relab[e].hmin_ref())
+            dt_e[e] *= float(ratio.min())
         dt = dt_user if dt_user > 0 else float(dt_e.min()) * par.get("TIME_DELTA_T_FACTOR", float)
         self.dt = dt
         attk = ATT_NONE
