@@ -873,6 +873,9 @@ struct ax3d_domain {
                 if (z.b.npts_chunk <= 0)
                     throw Error(AX3D_ERR_UNSUPPORTED, "ax3d_finalize || nr too large for the physical-space kernel");
                 z.elems = kv.second;
+                // ring sizes together (the kernel keeps one ring's plan and tables loaded)
+                std::stable_sort(z.elems.begin(), z.elems.end(),
+                                 [&](int32_t a, int32_t b) { return e_nr[a] > e_nr[b]; });
                 sized[fl].push_back(z);
             }
         if (sc.merge)
@@ -897,7 +900,8 @@ struct ax3d_domain {
                 for (auto &kv : byshape) {
                     Sized z = kv.second;
                     std::stable_sort(z.elems.begin(), z.elems.end(), [&](int32_t a, int32_t b) {
-                        return lbuf_of_nr[e_nr[a]] > lbuf_of_nr[e_nr[b]];
+                        const int la = lbuf_of_nr[e_nr[a]], lb = lbuf_of_nr[e_nr[b]];
+                        return la != lb ? la > lb : e_nr[a] > e_nr[b];
                     });
                     z.b.smem = ax3d::phys_smem_bytes(z.b.L_max, fl ? 2 : 3, z.b.npts_chunk, z.b.nt);
                     sized[fl].push_back(z);

@@ -1004,6 +1004,7 @@ __global__ void __launch_bounds__(NTT, NTT <= 256 ? 2 : 1)
     // this CTA's GLL points
     const int p0 = crank * Pc, pc = min(Pc, NPE - p0), ns = NSQ * pc;
 
+    int have_nr = -1;  // ring size whose plan and tables the shared memory holds
     for (int ei = blockIdx.x / C; ei < count; ei += gridDim.x / C) {
         const int e = elems[ei];
         const int flags = T.flags[e];
@@ -1012,11 +1013,16 @@ __global__ void __launch_bounds__(NTT, NTT <= 256 ? 2 : 1)
         const int mat = ef_mat(flags), att = SOLID ? ef_att(flags) : 0;
         const bool tiso = SOLID && (mat == 1 || mat == 2);
         csync();  // the whole cluster is done with the previous element's sequences
-        // the plan in shared memory: the transform passes read it once per pass
-        if (threadIdx.x < (int)(sizeof(FftPlan) / 4))
-            reinterpret_cast<int32_t *>(sm.pl)[threadIdx.x] =
-                reinterpret_cast<const int32_t *>(X.plans + nr)[threadIdx.x];
-        __syncthreads();
+        // the plan and its tables in shared memory (the transform passes read them once per
+        // pass), loaded only when the ring size changes: bucket lists are sorted by it
+        const bool reload = nr != have_nr;
+        if (reload) {
+            if (threadIdx.x < (int)(sizeof(FftPlan) / 4))
+                reinterpret_cast<int32_t *>(sm.pl)[threadIdx.x] =
+                    reinterpret_cast<const int32_t *>(X.plans + nr)[threadIdx.x];
+            __syncthreads();
+        }
+        have_nr = nr;
         const FftPlan &pl = *sm.pl;
         const int L = pl.L, Lb = pl.Lbuf;
         const bool blue = pl.kind == 1;
@@ -1028,11 +1034,13 @@ __global__ void __launch_bounds__(NTT, NTT <= 256 ? 2 : 1)
         pk.inv_nr = 1.f / (float)nr;
         const float hsc = pl.kind == 0 ? 0.5f / (float)nr : 0.5f;
         const float *md = T.moduli + T.mofs[e];
-        for (int m = threadIdx.x; m < L; m += blockDim.x) tw[m] = X.f2[pl.tw + m];
-        if (!blue)
-            for (int m = threadIdx.x; m < nr; m += blockDim.x) sm.rev[m] = X.i32[pl.rev + m];
-        if (pl.kind == 2)
-            for (int m = threadIdx.x; m < nr; m += blockDim.x) sm.ord[m] = X.i32[pl.ord + m];
+        if (reload) {
+            for (int m = threadIdx.x; m < L; m += blockDim.x) tw[m] = X.f2[pl.tw + m];
+            if (!blue)
+                for (int m = threadIdx.x; m < nr; m += blockDim.x) sm.rev[m] = X.i32[pl.rev + m];
+            if (pl.kind == 2)
+                for (int m = threadIdx.x; m < nr; m += blockDim.x) sm.ord[m] = X.i32[pl.ord + m];
+        }
         // positions the packing does not write: the Nyquist order (even nr) and the
         // Bluestein padding [nr, Lb)
         if (nr % 2 == 0)

@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--elements", type=int, default=200_000)
     ap.add_argument("--att", default="cg4", choices=["cg4", "full", "none"])
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--schedule", default="",
+                    help="ratio,policy,nside,merge: pin the element bucket schedule instead of autotuning it")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=0, help="elements per CPU worker (0 = auto)")
@@ -245,7 +247,12 @@ def run_gb300(args, world, rank, local):
     u0 = W.benchmark_displacement(spec, seed=args.seed + 100 + rank)
     dom = Ax3dDomain(spec, device=local)
     dom.set("displ", "solid", u0)
-    tune = dom.autotune(2)  # the bucket schedule from timed element passes on this domain
+    if args.schedule:
+        r, pol, ns, mg = args.schedule.split(",")
+        dom.set_schedule(float(r), int(pol), int(ns), bool(int(mg)))
+        tune = f"pinned {args.schedule}"
+    else:
+        tune = dom.autotune(2)  # the bucket schedule from timed element passes on this domain
     t_build = time.perf_counter() - t_build
     upd = W.updates_per_step(spec)
 
