@@ -35,9 +35,19 @@ def model_strings(seed: int, rms: float = 0.04, lat_km: float = 500.0, rad_km: f
             f"gaussian_random$VP$Ref1D${rms}${lat_km}${rad_km}${seed + 7919}")
 
 
-def write_case(d, seed, nu_full, steps, mesh_kw=None, n_stations=20):
-    return solver.write_inputs(d, mesh_kw=mesh_kw, nu=nu_full, steps=steps, n_stations=n_stations, seed=0,
-                               models3d=model_strings(seed), lucky=True)
+# TIME_DELTA_T_FACTOR of the experiment's runs: with the 3-D models, runs on the default half
+# disk at the mesh's CFL step grow unstable once the P wave reaches the core-mantle boundary
+# beneath the source; 0.8 of it is stable (full-Nu and learned-Nu runs use the same step)
+DT_FACTOR = 0.8
+
+
+def write_case(d, seed, nu_full, steps, mesh_kw=None, n_stations=20, dt_factor=DT_FACTOR):
+    d = solver.write_inputs(d, mesh_kw=mesh_kw, nu=nu_full, steps=steps, n_stations=n_stations, seed=0,
+                            models3d=model_strings(seed), lucky=True)
+    if dt_factor != 1.0:
+        p = Path(d) / "inparam.time_src_recv"
+        p.write_text(p.read_text().replace("TIME_DELTA_T_FACTOR 1.0", f"TIME_DELTA_T_FACTOR {dt_factor}"))
+    return d
 
 
 def ring_bands(models, s, z, nphi=512):
