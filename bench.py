@@ -155,8 +155,9 @@ def allmax(world, x):
 # 20,000-element case of this workload (same distributions, ~5.5 GB of element data, far
 # above L2).  The 200,000-element workload is too large to capture with more than one ncu
 # pass; its traffic grows in proportion to the elements processed, so it is this ratio
-# times its algorithmic bytes.  Re-measured whenever the element kernel changes.
-TRAFFIC_PER_ALGO_BYTE = 0.889
+# times its algorithmic bytes.  Re-measured whenever the element kernel or the schedule
+# changes (this figure: the merged 512-thread schedule the autotuner picks).
+TRAFFIC_PER_ALGO_BYTE = 1.028
 
 
 def peaks():
