@@ -132,6 +132,12 @@ class GaussianRandom(Model3D):
     def evaluate_rings_gpu(self, crds, nr, phi2d=None, device=0):
         """The field on the nr slices of every GLL point, crds (n, 25, 2) = (s, z), computed by
         ax3d_sample_gaussian_random (FP64 on the GPU); (n, nr, 25)."""
+        return self.evaluate_rows_gpu(crds, np.full(len(crds), int(nr), np.int32), phi2d, device).reshape(
+            len(crds), int(nr), 25)
+
+    def evaluate_rows_gpu(self, crds, rows, phi2d=None, device=0):
+        """The field on rows[e] slices of every GLL point of element e, crds (n, 25, 2), in
+        one sampler call; flat, element e's (rows[e], 25) block after those of elements < e."""
         import ctypes as C
         from .capi import load_library
         lib = load_library()
@@ -140,12 +146,12 @@ class GaussianRandom(Model3D):
         f.argtypes = [C.c_int32, C.c_int32, C.c_void_p, P_D, C.c_int32, P_D, P_D, P_D, C.c_double, C.c_int32,
                       C.c_double, P_D]
         n = len(crds)
-        rows = np.full(n, int(nr), np.int32)
+        rows = np.ascontiguousarray(rows, np.int32)
         c = np.ascontiguousarray(crds, np.float64)
         kr = np.ascontiguousarray(self.kr, np.float64)
         klR = np.ascontiguousarray(self.R * self.kl.T, np.float64)
         ph = np.ascontiguousarray(self.ph, np.float64)
-        out = np.empty((n, int(nr), 25))
+        out = np.empty(int(rows.astype(np.int64).sum()) * 25)
         d = lambda a: a.ctypes.data_as(P_D)
         rc = f(int(device), n, rows.ctypes.data_as(C.c_void_p), d(c), self.modes, d(kr), d(klR), d(ph), self.rms,
                int(phi2d is not None), float(phi2d or 0.0), d(out))
@@ -197,26 +203,30 @@ def volumetric_models(par, src_latlon, R):
     return out
 
 
-def apply_models(models, props1d, crds, nr, fluid, phi2d=None, gpu=False):
+def apply_models(models, props1d, crds, nr, fluid, phi2d=None, gpu=False, presampled=None):
     """3-D properties of a group of elements sharing one Nr.
 
     props1d: {"VP","VS","RHO": (n, 25)} 1-D values at the GLL points; crds (n, 25, 2) = (s, z);
     fluid (n,) bool.  Slice alpha sits at phi = 2 pi alpha / nr, or every slice at phi2d in
     2-D mode (Quad::computeGeocentricGlobal with phi2D).  Returns ({prop: (n, nr, 25)},
     touched (n,) bool): elements with any point inside any model's range.  gpu: sample the
-    Gaussian-random models on the GPU (ax3d_sample_gaussian_random)."""
+    Gaussian-random models on the GPU (ax3d_sample_gaussian_random); presampled: {model
+    index: (n, nr, 25)} values already sampled for this group."""
     phi = 2 * math.pi * np.arange(nr) / nr if phi2d is None else np.full(nr, float(phi2d))
     n = len(crds)
     out = {k: np.empty((n, nr, 25), np.float32) for k in props1d}
     touched = np.zeros(n, bool)
-    on_gpu = {i: m.evaluate_rings_gpu(crds, nr, phi2d) for i, m in enumerate(models)
-              if gpu and isinstance(m, GaussianRandom)}
+    on_gpu = dict(presampled or {})
+    on_gpu.update({i: m.evaluate_rings_gpu(crds, nr, phi2d) for i, m in enumerate(models)
+                   if gpu and isinstance(m, GaussianRandom) and i not in on_gpu})
+    host = len(on_gpu) < len(models)
     step = max(1, (1 << 21) // (nr * 25))   # ~2M samples per chunk
     for a in range(0, n, step):
         b = min(n, a + step)
-        s, z = crds[a:b, :, 0], crds[a:b, :, 1]
-        xyz = np.stack([s[:, None, :] * np.cos(phi)[None, :, None], s[:, None, :] * np.sin(phi)[None, :, None],
-                        np.broadcast_to(z[:, None, :], (b - a, nr, 25))], -1)
+        if host:
+            s, z = crds[a:b, :, 0], crds[a:b, :, 1]
+            xyz = np.stack([s[:, None, :] * np.cos(phi)[None, :, None], s[:, None, :] * np.sin(phi)[None, :, None],
+                            np.broadcast_to(z[:, None, :], (b - a, nr, 25))], -1)
         cur = {k: np.repeat(v[a:b, None, :], nr, 1).astype(float) for k, v in props1d.items()}
         for i, m in enumerate(models):
             if i in on_gpu:

@@ -68,13 +68,37 @@ def ring_bands(models, s, z, nphi=512):
         for m in vs_models:
             val, inr = m.evaluate(xyz)
             d += np.where(inr, val, 0.0)
-        P = np.abs(np.fft.rfft(d, axis=1) / nphi) ** 2
-        for i in range(8):
-            out[a:b, i] = P[:, 2 ** i:2 ** (i + 1)].sum(1)
+        out[a:b] = _band_powers(d)
     return out
 
 
-def element_features(sim, period: float = 50.0) -> np.ndarray:
+def _band_powers(d):
+    """Band powers (8 octaves of orders 1..255) of rows of azimuthal samples d (E, nphi)."""
+    P = np.abs(np.fft.rfft(d, axis=1) / d.shape[1]) ** 2
+    return np.stack([P[:, 2 ** i:2 ** (i + 1)].sum(1) for i in range(8)], 1)
+
+
+def ring_bands_gpu(models, s, z, nphi=512, device=0):
+    """ring_bands with the rings sampled on the GPU (GaussianRandom.evaluate_rings_gpu,
+    FP64): the element centres are packed 25 to a row of the sampler's (n, 25) layout."""
+    E = len(s)
+    vs_models = [m for m in models if m.prop == "VS" and m.ref != 0]
+    if not vs_models or E == 0:
+        return np.zeros((E, 8))
+    n = (E + 24) // 25
+    crd = np.zeros((n * 25, 2))
+    crd[:E, 0], crd[:E, 1] = s, z
+    crd = crd.reshape(n, 25, 2)
+    d = np.zeros((E, nphi))
+    for m in vs_models:
+        if not hasattr(m, "evaluate_rings_gpu"):
+            return ring_bands(models, s, z, nphi)
+        d += m.evaluate_rings_gpu(crd, nphi, device=device).transpose(0, 2, 1).reshape(n * 25, nphi)[:E]
+    return _band_powers(d)
+
+
+def element_features(sim, period: float = 50.0, gpu: bool = False) -> np.ndarray:
+    """The 16 features of every element; gpu samples the rings of the 3-D model on the GPU."""
     c = sim.crds[:, 12]
     s, z = c[:, 0], c[:, 1]
     r = np.hypot(s, z)
@@ -88,7 +112,8 @@ def element_features(sim, period: float = 50.0) -> np.ndarray:
     f[:, 5] = sim.vp_e / 1e4
     f[:, 6] = sim.vs_e / 1e4
     f[:, 7] = sim.src_dep / 1e6
-    f[:, 8:] = (np.log10(ring_bands(sim.models, s, z) + 1e-12) + 12.0) / 12.0
+    bands = ring_bands_gpu(sim.models, s, z) if gpu else ring_bands(sim.models, s, z)
+    f[:, 8:] = (np.log10(bands + 1e-12) + 12.0) / 12.0
     return f
 
 
@@ -162,7 +187,7 @@ def experiment(work, n_train=64, n_test=16, nu_full=64, steps=600, epochs=200, b
         pre.append(time.perf_counter() - t0)
         seis, t, wis, _ = run(spec, steps, learn=(interval, eps))
         t_train_runs += t
-        x = element_features(sim)
+        x = element_features(sim, gpu=preloop == "gpu")
         y = encode(np.minimum(element_labels(spec, wis), nu_full), nu_full)
         log(f"train {i}: {t:.2f} s, mean label Nu {np.mean(element_labels(spec, wis)):.1f}")
         if i == n_train - 1 and n_train > 1:
@@ -199,7 +224,7 @@ def experiment(work, n_train=64, n_test=16, nu_full=64, steps=600, epochs=200, b
         _, t_fl, wis, _ = run(spec_f, steps, learn=(interval, eps))
         # learned route: features, network inference, pre-loop at the predicted Nu, the loop
         t0 = time.perf_counter()
-        x = element_features(sim)
+        x = element_features(sim, gpu=preloop == "gpu")
         t_feat = time.perf_counter() - t0
         import torch
         t0 = time.perf_counter()

@@ -312,7 +312,9 @@ class Simulation:
         force_odd = (p_nr % 2 == 0) & near_axis
         p_nr = np.where(force_odd, p_nr + 1, p_nr)
         if _flag(par, "FFTW_LUCKY_NUMBER"):
-            p_nr = np.array([next_lucky(int(n), bool(f)) for n, f in zip(p_nr, force_odd)])
+            key = 2 * p_nr.astype(np.int64) + force_odd
+            uk, inv = np.unique(key, return_inverse=True)
+            p_nr = np.array([next_lucky(int(k // 2), bool(k % 2)) for k in uk])[inv.ravel()]
         # volumetric 3-D models (Material::addVolumetric3D) on each element's Nr slices
         e_nr = p_nr[e_pts].max(1)
         models = M3D.volumetric_models(par, self._cmt_latlon(), self.R)
@@ -332,11 +334,23 @@ class Simulation:
         e3d = np.zeros(E, bool)
         props3 = {}
         if models:
-            for nr in np.unique(e_nr):
+            # GPU: each Gaussian-random model sampled on every element's slices in one call,
+            # elements ordered by Nr so that each group's block is contiguous
+            groups = np.unique(e_nr)
+            pre = {}
+            if preloop == "gpu":
+                order = np.argsort(e_nr, kind="stable")
+                bounds = np.concatenate([[0], np.cumsum([int(nr) * 25 * int((e_nr == nr).sum()) for nr in groups])])
+                for i, m in enumerate(models):
+                    if isinstance(m, M3D.GaussianRandom):
+                        pre[i] = m.evaluate_rows_gpu(crds[order], e_nr[order], self.phi2d)
+            for gi, nr in enumerate(groups):
                 sel = np.nonzero(e_nr == nr)[0]
                 cur, touched = M3D.apply_models(models, {"VP": vp[sel], "VS": vs[sel], "RHO": rho[sel]},
                                                 crds[sel], int(nr), fl[sel], phi2d=self.phi2d,
-                                                gpu=preloop == "gpu")
+                                                gpu=preloop == "gpu",
+                                                presampled={i: v[bounds[gi]:bounds[gi + 1]].reshape(len(sel), int(nr), 25)
+                                                            for i, v in pre.items()})
                 for j in np.nonzero(touched)[0]:
                     if self.phi2d is not None:
                         # 2-D mode: every slice sees the model at phi2D, so the element stays

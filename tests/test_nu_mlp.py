@@ -159,3 +159,23 @@ def test_learned_nu_gain_on_held_out_model(tmp_path, ax3d_lib, capsys):
     assert s["loss_last"] < 0.5 * s["loss_first"]
     assert t["misfit"] <= 0.01
     assert t["upd_learned"] < t["upd_full"]
+
+
+@pytest.mark.gpu
+def test_ring_features_gpu_match_host(ax3d_lib):
+    """The band-power features sampled on the GPU (FP64 sampler) equal the host sampling
+    (FP32 phases, FP64 sums) on the rings through the element centres of a seeded model."""
+    from axisem3d_gb300 import model3d as M3D, nu_learn
+    vs, vp = nu_learn.model_strings(1234)
+    R = 6371e3
+    models = [M3D.GaussianRandom(vs.split("$")[1:], R), M3D.GaussianRandom(vp.split("$")[1:], R)]
+    rng = np.random.default_rng(3)
+    E = 203  # not a multiple of the sampler's 25-point rows
+    r = rng.uniform(3.5e6, R, E)
+    th = rng.uniform(0.0, np.pi, E)
+    s, z = r * np.sin(th), r * np.cos(th)
+    host = nu_learn.ring_bands(models, s, z)
+    gpu = nu_learn.ring_bands_gpu(models, s, z)
+    fh = (np.log10(host + 1e-12) + 12.0) / 12.0
+    fg = (np.log10(gpu + 1e-12) + 12.0) / 12.0
+    assert np.abs(fg - fh).max() < 1e-4

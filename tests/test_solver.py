@@ -936,3 +936,11 @@ def test_gpu_gaussian_random_sampling_matches_host(ax3d_lib):
                         np.broadcast_to(z[:, None, :], (n, nr, 25))], -1)
         h, _ = m.evaluate(xyz)
         assert np.abs(g - h).max() <= 1e-5 * np.abs(h).max()
+    # one call over elements of different slice counts (the solver's batched sampling)
+    rows = rng.integers(1, 9, n)
+    flat = m.evaluate_rows_gpu(crds, rows)
+    ofs = np.concatenate([[0], np.cumsum(rows * 25)])
+    assert len(flat) == ofs[-1]
+    for e in range(n):
+        np.testing.assert_array_equal(flat[ofs[e]:ofs[e + 1]].reshape(rows[e], 25),
+                                      m.evaluate_rings_gpu(crds[e:e + 1], int(rows[e]))[0])
