@@ -135,7 +135,8 @@ struct ax3d_domain {
     DevBuf<int64_t> d_prtofs, d_wofs;
     DevBuf<float> d_prtx;
     DevBuf<float2> d_w;
-    int nitems_p1s = 0, nitems_p1f = 0, nitems_p3s = 0, nitems_p3f = 0, n_p3s = 0, n_p3f = 0, nr_p3 = 1;
+    int nitems_p1s = 0, nitems_p1f = 0, nitems_p3s = 0, nitems_p3f = 0, n_p3s = 0, n_p3f = 0;
+    int lbuf_p3s = 1, lbuf_p3f = 1;  // longest transform buffer of the PRT_3D elements
     std::vector<ax3d::PhysBucket> buckets_s, buckets_f;
     std::vector<DevBuf<int32_t>> bucket_lists;
     // the bucket schedule: geometric step of the transform length between buckets, shared
@@ -543,12 +544,10 @@ struct ax3d_domain {
             memofs[e] = memsize;
             if (a) memsize += (int64_t)(sls.nsls + 1) * 6 * npa * (e3d ? nr : 2 * n);
             if (e_prtlen[e] && e3d) {
-                if (nr > 4096) throw Error(AX3D_ERR_ARG, "ax3d_set_prt || PRT_3D elements need nr <= 4096");
                 (fluid ? p3f : p3s).push_back(e);
                 for (int al = 0; al < n; al++) (fluid ? items_p3f : items_p3s).push_back(make_int2(e, al));
                 wofs[e] = wsize;
                 wsize += (int64_t)n * (fluid ? 3 : 9) * 25;
-                nr_p3 = std::max(nr_p3, nr);
             } else if (e_prtlen[e]) {
                 for (int al = 0; al < n; al++) (fluid ? items_p1f : items_p1s).push_back(make_int2(e, al));
             } else if (e3d) {
@@ -595,6 +594,11 @@ struct ax3d_domain {
         phys3_f_list = phys3_f;
         lbuf_of_nr.assign(ft.plans.size(), 1);
         for (size_t k = 0; k < ft.plans.size(); k++) lbuf_of_nr[k] = ft.plans[k].Lbuf;
+        for (int e : p3s) lbuf_p3s = std::max(lbuf_p3s, lbuf_of_nr[e_nr[e]]);
+        for (int e : p3f) lbuf_p3f = std::max(lbuf_p3f, lbuf_of_nr[e_nr[e]]);
+        if ((!p3s.empty() && ax3d::prt3_points_per_cta(true, lbuf_p3s) == 0) ||
+            (!p3f.empty() && ax3d::prt3_points_per_cta(false, lbuf_p3f) == 0))
+            throw Error(AX3D_ERR_ARG, "ax3d_set_prt || a PRT_3D element's ring is too long for one CTA's shared memory");
         // ocean load per point (GLLPoint.cpp:57-72 picks MassOcean1D / MassOcean3D)
         std::vector<int32_t> p_oclen(np, 0);
         std::vector<int64_t> p_ocofs(np, 0);
@@ -1029,8 +1033,8 @@ struct ax3d_domain {
         ax3d::launch_elem_fourier_fluid(T, P, F.fu, d_items_f.p, nitems_f, stream);
         ax3d::launch_elem_prt1(true, T, P, F.su, d_items_p1s.p, nitems_p1s, sls, stream);
         ax3d::launch_elem_prt1(false, T, P, F.fu, d_items_p1f.p, nitems_p1f, sls, stream);
-        ax3d::launch_elem_prt3(true, T, P, F.su, d_items_p3s.p, nitems_p3s, d_p3s.p, n_p3s, nr_p3, sls, stream);
-        ax3d::launch_elem_prt3(false, T, P, F.fu, d_items_p3f.p, nitems_p3f, d_p3f.p, n_p3f, nr_p3, sls, stream);
+        ax3d::launch_elem_prt3(true, T, P, F.su, d_items_p3s.p, nitems_p3s, d_p3s.p, n_p3s, lbuf_p3s, X, sls, stream);
+        ax3d::launch_elem_prt3(false, T, P, F.fu, d_items_p3f.p, nitems_p3f, d_p3f.p, n_p3f, lbuf_p3f, X, sls, stream);
         const int nb = (int)(buckets_s.size() + buckets_f.size());
         if (nb == 0) return;
         if (nb == 1) {

@@ -364,11 +364,11 @@ __global__ void __launch_bounds__(FW_WARPS * 32)
 }
 
 // PRT_3D elements (3-D material, X per sample): the gradient of every order, rotated to
-// RTZ, goes to a Fourier-space scratch w [alpha][nc][25] (k_prt3_grad); one CTA per
-// (element, point) transforms its nc columns to the nr samples by a direct DFT, relabels,
+// RTZ, goes to a Fourier-space scratch w [alpha][nc][25] (k_prt3_grad); k_prt3_fft
+// (ax3d_phys.cu, on the element pass's transforms) takes it to the nr samples, relabels,
 // computes the stress (+ SLS) and the relabelled-back stress per sample and transforms
-// back into w (k_prt3_phys, PRT_3D.cpp with FieldFFT's C2R / R2C x 1/nr); the divergence
-// of every order follows (k_prt3_quad).
+// back into w (PRT_3D.cpp with FieldFFT's C2R / R2C x 1/nr); the divergence of every
+// order follows (k_prt3_quad).
 template <bool SOLID>
 __global__ void __launch_bounds__(FW_WARPS * 32)
     k_prt3_grad(ElemTable T, PointTable P, const float2 *__restrict__ u, const int2 *__restrict__ items, int nitems) {
@@ -417,95 +417,6 @@ __global__ void __launch_bounds__(FW_WARPS * 32)
 #pragma unroll
             for (int c = 0; c < NC; c++) w[c * NPE] = v[c];
         }
-    }
-}
-
-template <bool SOLID>
-__global__ void __launch_bounds__(128) k_prt3_phys(ElemTable T, const int32_t *__restrict__ elems, SLS sls) {
-    constexpr int NC = SOLID ? 9 : 3;
-    extern __shared__ float sm_prt[];
-    const int e = elems[blockIdx.x / NPE], p = blockIdx.x % NPE;
-    const int flags = T.flags[e];
-    const int nr = T.nr[e], n = nr / 2 + 1, lim = nr / 2 - (nr % 2 == 0);
-    float2 *tw = reinterpret_cast<float2 *>(sm_prt);  // (cos, sin)(2 pi m / nr)
-    float *x = sm_prt + 2 * nr;                        // [NC][nr]
-    for (int m = threadIdx.x; m < nr; m += blockDim.x) {
-        float sn, cs;
-        sincospif(2.f * (float)m / (float)nr, &sn, &cs);
-        tw[m] = make_float2(cs, sn);
-    }
-    __syncthreads();
-    float2 *w = T.w + T.wofs[e] + p;
-    // C2R (FFTW convention: unnormalised, Im of order 0 ignored); the Nyquist order is zero
-    for (int t = threadIdx.x; t < NC * nr; t += blockDim.x) {
-        const int c = t / nr, k = t - c * nr;
-        float acc = w[c * NPE].x;
-        int m = 0;
-        for (int a = 1; a <= lim; a++) {
-            m += k;
-            if (m >= nr) m -= nr;
-            const float2 v = w[((int64_t)a * NC + c) * NPE];
-            acc += 2.f * (v.x * tw[m].x - v.y * tw[m].y);
-        }
-        x[c * nr + k] = acc;
-    }
-    __syncthreads();
-    const float *xp = T.prtx + T.prtofs[e];
-    const float *md = T.moduli + T.mofs[e];
-    for (int k = threadIdx.x; k < nr; k += blockDim.x) {
-        auto xf = [&](int m) { return xp[((int64_t)m * nr + k) * NPE + p]; };
-        if constexpr (SOLID) {
-            float s9[9], und[6], sig[6];
-#pragma unroll
-            for (int c = 0; c < 9; c++) s9[c] = x[c * nr + k];
-            prt_s2u(s9, und, xf);
-            elastic(ef_mat(flags), und, sig, [&](int m) { return md[((int64_t)m * nr + k) * NPE + p]; });
-            const int att = ef_att(flags);
-            if (att) {
-                const int npa = att == 2 ? 4 : NPE;
-                const int qq = att == 2 ? cg4_index(p) : p;
-                if (qq >= 0) {
-                    float *mem = T.mem + T.memofs[e];
-                    const int64_t sl = (int64_t)nr * 6 * npa;
-                    float *R = mem + (int64_t)k * 6 * npa + qq;
-                    float *SR = R + sls.nsls * sl;
-                    for (int l = 0; l < sls.nsls; l++)
-#pragma unroll
-                        for (int c = 0; c < 6; c++) sig[c] -= R[l * sl + c * npa];
-                    const float *am = T.attm + T.aofs[e];
-                    sls_update(sls, R, SR, sl, (int64_t)npa, und, am[(int64_t)k * npa + qq],
-                               am[(int64_t)nr * npa + (int64_t)k * npa + qq]);
-                }
-            }
-            prt_u2s(sig, s9, xf);
-#pragma unroll
-            for (int c = 0; c < 9; c++) x[c * nr + k] = s9[c];
-        } else {
-            float v[3] = {x[k], x[nr + k], x[2 * nr + k]};
-            prt_s2u_fluid(v, xf);
-            const float K = md[(int64_t)k * NPE + p];
-#pragma unroll
-            for (int c = 0; c < 3; c++) v[c] *= K;
-            prt_u2s_fluid(v, xf);
-#pragma unroll
-            for (int c = 0; c < 3; c++) x[c * nr + k] = v[c];
-        }
-    }
-    __syncthreads();
-    // R2C x 1/nr, orders 0..nr/2 (the divergence drops the Nyquist order)
-    const float inv = 1.f / (float)nr;
-    for (int t = threadIdx.x; t < NC * n; t += blockDim.x) {
-        const int c = t / n, a = t - c * n;
-        float re = 0.f, im = 0.f;
-        int m = 0;
-        for (int k = 0; k < nr; k++) {
-            const float v = x[c * nr + k];
-            re += v * tw[m].x;
-            im -= v * tw[m].y;
-            m += a;
-            if (m >= nr) m -= nr;
-        }
-        w[((int64_t)a * NC + c) * NPE] = make_float2(re * inv, im * inv);
     }
 }
 
@@ -568,16 +479,16 @@ void launch_elem_prt1(bool solid, const ElemTable &T, const PointTable &P, const
 }
 
 void launch_elem_prt3(bool solid, const ElemTable &T, const PointTable &P, const float2 *u, const int2 *items,
-                      int nitems, const int32_t *elems, int nelem, int nr_max, const SLS &sls, cudaStream_t s) {
+                      int nitems, const int32_t *elems, int nelem, int lbuf_max, const PhysTables &X, const SLS &sls,
+                      cudaStream_t s) {
     if (nitems <= 0 || nelem <= 0) return;
-    const size_t smem = (size_t)(2 + (solid ? 9 : 3)) * nr_max * sizeof(float);
     if (solid) {
         k_prt3_grad<true><<<fw_blocks(nitems), FW_WARPS * 32, 0, s>>>(T, P, u, items, nitems);
-        k_prt3_phys<true><<<nelem * NPE, 128, smem, s>>>(T, elems, sls);
+        launch_prt3_fft(true, T, elems, nelem, lbuf_max, X, sls, s);
         k_prt3_quad<true><<<fw_blocks(nitems), FW_WARPS * 32, 0, s>>>(T, items, nitems);
     } else {
         k_prt3_grad<false><<<fw_blocks(nitems), FW_WARPS * 32, 0, s>>>(T, P, u, items, nitems);
-        k_prt3_phys<false><<<nelem * NPE, 128, smem, s>>>(T, elems, sls);
+        launch_prt3_fft(false, T, elems, nelem, lbuf_max, X, sls, s);
         k_prt3_quad<false><<<fw_blocks(nitems), FW_WARPS * 32, 0, s>>>(T, items, nitems);
     }
 }
@@ -599,8 +510,6 @@ void launch_elem_fourier_fluid(const ElemTable &T, const PointTable &P, const fl
 
 void init_kernel_attributes() {
     init_phys_attributes();
-    cudaFuncSetAttribute(k_prt3_phys<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, PRT3_SMEM_MAX);
-    cudaFuncSetAttribute(k_prt3_phys<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, PRT3_SMEM_MAX);
 }
 
 }  // namespace ax3d

@@ -81,13 +81,19 @@ void launch_source(const PointTable &P, const ElemTable &T, const Fields &F,
                    const int32_t *src_elem, const int32_t *src_nord, const int64_t *src_ofs,
                    const float2 *src_force, int nsrc, const float *stf, int nstf,
                    const int32_t *tptr, int tofs, cudaStream_t s);
-constexpr int PRT3_SMEM_MAX = 200 * 1024;  // k_prt3_phys: (2 + 9) nr floats, so nr <= 4654
 // particle relabelling: PRT_1D elements in Fourier space, PRT_3D elements through the
-// Fourier scratch T.w (nr_max = largest nr among them, for the per-CTA sample buffer)
+// Fourier scratch T.w (lbuf_max = longest transform buffer among them, sizing k_prt3_fft's
+// shared memory)
 void launch_elem_prt1(bool solid, const ElemTable &T, const PointTable &P, const float2 *u, const int2 *items,
                       int nitems, const SLS &sls, cudaStream_t s);
 void launch_elem_prt3(bool solid, const ElemTable &T, const PointTable &P, const float2 *u, const int2 *items,
-                      int nitems, const int32_t *elems, int nelem, int nr_max, const SLS &sls, cudaStream_t s);
+                      int nitems, const int32_t *elems, int nelem, int lbuf_max, const PhysTables &X, const SLS &sls,
+                      cudaStream_t s);
+// PRT_3D transform pass (k_prt3_fft) and the points per CTA it takes for sequences of Lmax
+// buffer positions (0: not even one fits in shared memory)
+void launch_prt3_fft(bool solid, const ElemTable &T, const int32_t *elems, int nelem, int Lmax, const PhysTables &X,
+                     const SLS &sls, cudaStream_t s);
+int prt3_points_per_cta(bool solid, int Lmax);
 void launch_record_strain_curl(const PointTable &P, const ElemTable &T, const float2 *su, const int32_t *rec_elem,
                                const float *rec_phi, const float *rec_w, const int32_t *list, int n,
                                float *strain_out, int nst, float *curl_out, int ncu, int cap, const int32_t *tptr,

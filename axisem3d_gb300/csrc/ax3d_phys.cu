@@ -1138,6 +1138,129 @@ __global__ void __launch_bounds__(NTT, NTT <= 256 ? 2 : 1)
     csync();  // no CTA leaves while a peer may still read its shared memory
 }
 
+// PRT_3D elements (PRT_3D.cpp, with FieldFFT's C2R / R2C x 1/nr) on the element pass's
+// transforms.  k_prt3_grad leaves the relabelled-frame gradient spectra of every order in the
+// Fourier-space scratch w [alpha][nc][25]; here one CTA per (element, chunk of Pc points)
+// packs each point's nc columns in pairs into complex sequences, transforms them to the nr
+// samples, relabels (X), computes the stress (+ SLS) and relabels back at every sample, and
+// transforms back into w, orders 0..nr/2; k_prt3_quad takes the divergence.
+template <bool SOLID>
+__global__ void __launch_bounds__(NT, 2)
+    k_prt3_fft(const __grid_constant__ ElemTable T, const int32_t *__restrict__ elems, int nchunk, int Pc, int Lmax,
+               const __grid_constant__ PhysTables X, const __grid_constant__ SLS sls) {
+    constexpr int NC = SOLID ? 9 : 3;
+    constexpr int NSQ = (NC + 1) / 2;
+    extern __shared__ __align__(16) char smem[];
+    const int S = NSQ * Pc;
+    PhysSmem sm(smem, Lmax, S);
+    float2 *buf = sm.buf;
+    const int e = elems[blockIdx.x / nchunk], p0 = (blockIdx.x % nchunk) * Pc;
+    const int pc = min(Pc, NPE - p0), ns = NSQ * pc;
+    const int flags = T.flags[e];
+    const int nr = T.nr[e], nu = nr / 2, lim = nu - (nr % 2 == 0);
+    const Grp g = grp_cta();
+    if (threadIdx.x < (int)(sizeof(FftPlan) / 4))
+        reinterpret_cast<int32_t *>(sm.pl)[threadIdx.x] = reinterpret_cast<const int32_t *>(X.plans + nr)[threadIdx.x];
+    __syncthreads();
+    const FftPlan &pl = *sm.pl;
+    const int L = pl.L, Lb = pl.Lbuf;
+    const bool blue = pl.kind == 1;
+    for (int m = threadIdx.x; m < L; m += blockDim.x) sm.tw[m] = X.f2[pl.tw + m];
+    if (!blue)
+        for (int m = threadIdx.x; m < nr; m += blockDim.x) sm.rev[m] = X.i32[pl.rev + m];
+    if (pl.kind == 2)
+        for (int m = threadIdx.x; m < nr; m += blockDim.x) sm.ord[m] = X.i32[pl.ord + m];
+    Pk pk;
+    pk.kind = pl.kind;
+    pk.nr = nr;
+    pk.chirp = X.f2 + pl.chirp;
+    pk.ord = sm.ord;
+    pk.inv_nr = 1.f / (float)nr;
+    const float hsc = pl.kind == 0 ? 0.5f / (float)nr : 0.5f;
+    // positions the packing does not write: the Nyquist order (even nr), the Bluestein padding
+    if (nr % 2 == 0)
+        for (int t = threadIdx.x; t < ns; t += blockDim.x) buf[(int64_t)nu * S + t] = make_float2(0.f, 0.f);
+    if (blue)
+        for (int t = threadIdx.x; t < (Lb - nr) * ns; t += blockDim.x)
+            buf[(int64_t)(nr + t / ns) * S + t % ns] = make_float2(0.f, 0.f);
+    __syncthreads();  // the order table is read by the packing
+    float2 *w = T.w + T.wofs[e] + p0;
+    // orders 0..lim of column pair (2s, 2s + 1) of point pp -> sequence NSQ pp + s
+    for (int t = threadIdx.x; t < (lim + 1) * ns; t += blockDim.x) {
+        const int a = t / ns, col = t - a * ns, pp = col / NSQ, sq = col - pp * NSQ;
+        const float2 *wa = w + (int64_t)a * NC * NPE + pp;
+        const float2 A = wa[2 * sq * NPE];
+        const float2 B = 2 * sq + 1 < NC ? wa[(2 * sq + 1) * NPE] : make_float2(0.f, 0.f);
+        zput(buf, S, col, a, pk, A, B);
+    }
+    __syncthreads();
+    transform_c2r(buf, S, ns, nr, pl, sm.tw, X.f2, g);
+    const float *xp = T.prtx + T.prtofs[e];
+    const float *md = T.moduli + T.mofs[e];
+    for (int t = threadIdx.x; t < nr * pc; t += blockDim.x) {
+        const int pos = t / pc, pp = t - pos * pc, p = p0 + pp;
+        const SampleAt sa(pos, pk, sm.rev);
+        const int k = sa.k;
+        float v[2 * NSQ];
+#pragma unroll
+        for (int sq = 0; sq < NSQ; sq++) {
+            const float2 z = sample_in(buf, S, NSQ * pp + sq, sa, pk);
+            v[2 * sq] = z.x;
+            v[2 * sq + 1] = z.y;
+        }
+        auto xf = [&](int m) { return xp[((int64_t)m * nr + k) * NPE + p]; };
+        if constexpr (SOLID) {
+            float und[6], sig[6];
+            prt_s2u(v, und, xf);
+            elastic(ef_mat(flags), und, sig, [&](int m) { return md[((int64_t)m * nr + k) * NPE + p]; });
+            const int att = ef_att(flags);
+            if (att) {
+                const int npa = att == 2 ? 4 : NPE;
+                const int qq = att == 2 ? cg4_index(p) : p;
+                if (qq >= 0) {
+                    float *mem = T.mem + T.memofs[e];
+                    const int64_t sl = (int64_t)nr * 6 * npa;
+                    float *R = mem + (int64_t)k * 6 * npa + qq;
+                    float *SR = R + sls.nsls * sl;
+                    for (int l = 0; l < sls.nsls; l++)
+#pragma unroll
+                        for (int c = 0; c < 6; c++) sig[c] -= R[l * sl + c * npa];
+                    const float *am = T.attm + T.aofs[e];
+                    sls_update(sls, R, SR, sl, (int64_t)npa, und, am[(int64_t)k * npa + qq],
+                               am[(int64_t)nr * npa + (int64_t)k * npa + qq]);
+                }
+            }
+            prt_u2s(sig, v, xf);
+            v[9] = 0.f;
+        } else {
+            prt_s2u_fluid(v, xf);
+            const float K = md[(int64_t)k * NPE + p];
+#pragma unroll
+            for (int c = 0; c < 3; c++) v[c] *= K;
+            prt_u2s_fluid(v, xf);
+            v[3] = 0.f;
+        }
+#pragma unroll
+        for (int sq = 0; sq < NSQ; sq++) sample_out(buf, S, NSQ * pp + sq, sa, pk, make_float2(v[2 * sq], v[2 * sq + 1]));
+    }
+    if (blue) {
+        __syncthreads();
+        for (int t = threadIdx.x; t < (Lb - nr) * ns; t += blockDim.x)
+            buf[(int64_t)(nr + t / ns) * S + t % ns] = make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    transform_r2c(buf, S, ns, nr, pl, sm.tw, X.f2, g);
+    // orders 0..nr/2 (x 1/nr) back into w (the divergence drops the Nyquist order)
+    for (int t = threadIdx.x; t < (nu + 1) * ns; t += blockDim.x) {
+        const int a = t / ns, col = t - a * ns, pp = col / NSQ, sq = col - pp * NSQ;
+        float2 A, B;
+        zget(buf, S, col, a, pk, hsc, A, B);
+        float2 *wa = w + (int64_t)a * NC * NPE + pp;
+        wa[2 * sq * NPE] = A;
+        if (2 * sq + 1 < NC) wa[(2 * sq + 1) * NPE] = B;
+    }
+}
+
 // ------------------------------------------------------------------------------------
 // host side
 // ------------------------------------------------------------------------------------
@@ -1151,6 +1274,31 @@ void init_phys_attributes() {
     cudaFuncSetAttribute(k_elem_phys<false, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_CAP);
     cudaFuncSetAttribute(k_elem_phys<true, 2 * NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_CAP);
     cudaFuncSetAttribute(k_elem_phys<false, 2 * NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_CAP);
+    cudaFuncSetAttribute(k_prt3_fft<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_CAP);
+    cudaFuncSetAttribute(k_prt3_fft<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_CAP);
+}
+
+// Points per CTA of the PRT_3D transform pass for sequences of Lmax buffer positions: all 25
+// if they fit two CTAs per SM, else the most that do, else the most that fit one CTA per SM;
+// 0 if not even one point fits.
+int prt3_points_per_cta(bool solid, int Lmax) {
+    const int nsq = solid ? 5 : 2;
+    for (size_t cap : {SMEM_TWO, SMEM_CAP})
+        for (int pc = NPE; pc >= 1; pc--)
+            if (phys_smem_bytes(Lmax, nsq, pc, NT) <= cap) return pc;
+    return 0;
+}
+
+void launch_prt3_fft(bool solid, const ElemTable &T, const int32_t *elems, int nelem, int Lmax, const PhysTables &X,
+                     const SLS &sls, cudaStream_t s) {
+    const int pc = prt3_points_per_cta(solid, Lmax);
+    if (nelem <= 0 || pc <= 0) return;
+    const int nchunk = (NPE + pc - 1) / pc;
+    const size_t smem = phys_smem_bytes(Lmax, solid ? 5 : 2, pc, NT);
+    if (solid)
+        k_prt3_fft<true><<<nelem * nchunk, NT, smem, s>>>(T, elems, nchunk, pc, Lmax, X, sls);
+    else
+        k_prt3_fft<false><<<nelem * nchunk, NT, smem, s>>>(T, elems, nchunk, pc, Lmax, X, sls);
 }
 
 namespace {

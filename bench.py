@@ -401,30 +401,37 @@ def run_halfdisk(args, world, rank, local):
 def run_ensemble(args, world, rank, local, members=32, steps=200):
     """Batched ensemble in the form of the ensemble configuration, scaled to this mesher: 32
     independent 3-D Earths (seeded Gaussian-random dlnVs / dlnVp, 4 % RMS), meshes of 48 to 96
-    elements in colatitude (about 2,700 to 5,900 quads), per-element Nu log-uniform in 4-256,
-    moment-tensor sources at 10-600 km depth, compensated Newmark.  All members run in one
-    domain whose step is one captured CUDA graph with an autotuned bucket schedule, against the
-    same members run one after another, each in its own domain.  A fixed window of `steps`
-    steps (the configuration's 10,000 scale linearly); pre-loops on the GPU, timed apart."""
+    elements in colatitude (about 2,700 to 5,900 quads), per-element Nu log-uniform in 4-256
+    (the range a learned Nu field spans), moment-tensor sources at 10-600 km depth,
+    compensated Newmark, 0.8 of the mesh's CFL step (the step the 3-D runs are stable at).
+    All members run in one domain whose step is one captured CUDA graph with an autotuned
+    bucket schedule, against (1) the same members run one after another, each in its own
+    domain, and (2) the plain full-Nu solver (Nu = 256 everywhere) on the same members one
+    after another.  A fixed window of `steps` steps (the configuration's 10,000 scale
+    linearly); pre-loops on the GPU, timed apart and added for time-to-seismogram."""
     import tempfile
     import torch
     from axisem3d_gb300 import build, ensemble, solver
     from axisem3d_gb300.capi import Ax3dDomain
-    from axisem3d_gb300.nu_learn import model_strings
+    from axisem3d_gb300.nu_learn import DT_FACTOR, model_strings
     build.build()
     rng = np.random.default_rng(args.seed)
-    specs = []
-    t_pre = time.perf_counter()
+    specs, sims = [], []
+    pre_var = []
     for i in range(members):
         d = Path(tempfile.mkdtemp()) / "input"
         nt = int(rng.choice([48, 64, 96]))
         solver.write_inputs(d, mesh_kw=dict(n_theta=nt), steps=steps, hdur=50.0, n_stations=10, seed=args.seed + i,
                             depth_km=float(rng.uniform(10, 600)), nu=256, models3d=model_strings(100 + i))
+        p = d / "inparam.time_src_recv"
+        p.write_text(p.read_text().replace("TIME_DELTA_T_FACTOR 1.0", f"TIME_DELTA_T_FACTOR {DT_FACTOR}"))
         sim = solver.Simulation(d)
         sim.build(preloop="gpu")  # mesh and element count
         nu_e = np.round(np.exp(rng.uniform(np.log(4), np.log(256), len(sim.e_pts)))).astype(np.int64)
+        t0 = time.perf_counter()
         specs.append(sim.build(kahan=True, nu_elem=nu_e, preloop="gpu"))
-    t_pre = time.perf_counter() - t_pre
+        pre_var.append(time.perf_counter() - t0)
+        sims.append(sim)
     dt = min(s.dt for s in specs)
     for s in specs:
         s.dt = dt
@@ -440,19 +447,38 @@ def run_ensemble(args, world, rank, local, members=32, steps=200):
     seis = dom.seismograms(0, args.warmup + steps)
     t_batch = time.perf_counter() - t0
     dom.close()
-    t_seq = 0.0
-    for s in specs:
-        d1 = Ax3dDomain(s, device=local)
-        d1.autotune(2)
-        d1.step(args.warmup)
-        torch.cuda.synchronize()
+
+    def sequential(member_specs):
+        t = 0.0
+        ok = True
+        for s in member_specs:
+            d1 = Ax3dDomain(s, device=local)
+            d1.autotune(2)
+            d1.step(args.warmup)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            d1.step(steps)
+            ok &= bool(np.isfinite(d1.seismograms(0, args.warmup + steps)).all())
+            t += time.perf_counter() - t0
+            d1.close()
+        return t, ok
+
+    t_seq, _ = sequential(specs)
+    # the plain full-Nu solver on the same members (pre-loop timed, then the loop)
+    pre_full, full_specs = [], []
+    for sim in sims:
         t0 = time.perf_counter()
-        d1.step(steps)
-        d1.seismograms(0, args.warmup + steps)
-        t_seq += time.perf_counter() - t0
-        d1.close()
+        fs = sim.build(kahan=True, preloop="gpu")
+        pre_full.append(time.perf_counter() - t0)
+        fs.dt = dt
+        fs.stf = specs[0].stf
+        full_specs.append(fs)
+    upd_full = int(sum(int(fs.p_nr.astype(np.int64).sum()) for fs in full_specs))
+    t_full, ok_full = sequential(full_specs)
     if rank != 0:
         return
+    tts_batched = sum(pre_var) + t_batch
+    tts_full = sum(pre_full) + t_full
     line = {"metric": "GLL-pt*azimuth updates/s (unique-point count), batched ensemble", "value": upd * steps / t_batch,
             "unit": UNIT, "n_gpus": world, "steps": steps, "warmup": args.warmup,
             "ms_per_step": t_batch * 1e3 / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -461,7 +487,11 @@ def run_ensemble(args, world, rank, local, members=32, steps=200):
                                    "autotuned buckets), per-element Nu 4-256, compensated Newmark",
                        "elements": spec.n_elements, "points": spec.n_points, "autotune": tune[:200]},
             "sequential_value": upd * steps / t_seq, "batched_over_sequential": t_seq / t_batch,
-            "preloop_s_all_members": t_pre, "finite": bool(np.isfinite(seis).all())}
+            "full_nu": {"updates_per_step": upd_full, "loop_s": t_full, "preloop_s": sum(pre_full),
+                        "loop_over_batched": t_full / t_batch, "finite": ok_full},
+            "time_to_seismogram": {"batched_s": tts_batched, "sequential_full_nu_s": tts_full,
+                                   "ratio": tts_full / tts_batched, "preloop_batched_s": sum(pre_var)},
+            "finite": bool(np.isfinite(seis).all())}
     print(json.dumps(line), flush=True)
 
 

@@ -48,10 +48,17 @@ CASES = {
     "ti3d_cg4_prt3d": dict(in3d=True, mat=MAT_TISO, att=ATT_CG4, nu=6, prt=0.05),
     "aniso3d_full_prt3d_mixednu": dict(in3d=True, mat=MAT_ANISO, att=ATT_FULL, nu_random=True, nu_max=7, prt=0.05),
     "fluid3d_prt3d": dict(fluid_layers=(1,), in3d=True, fluid3d=True, nu=5, prt=0.05),
+    # PRT_3D on every transform kind: mixed radix (lucky sizes), a direct prime pass, Bluestein
+    "aniso3d_full_prt3d_fft_lucky": dict(in3d=True, mat=MAT_ANISO, att=ATT_FULL, nu_random=True, nu_max=40,
+                                         lucky=True, prt=0.05),
+    "fluid3d_prt3d_direct131": dict(fluid_layers=(1,), in3d=True, fluid3d=True, nu=65, mat=MAT_TISO, n_theta=2,
+                                    n_r=2, prt=0.05),
+    "ti3d_cg4_prt3d_bluestein509": dict(in3d=True, mat=MAT_TISO, att=ATT_CG4, nu=254, n_theta=2, n_r=2, prt=0.05),
 }
 # time-loop steps for the cases whose O(nr^2) FP64 oracle transform is slow
 STEPS = {"ti3d_fft260_chunked": 6, "ti3d_cg4_direct131": 10, "iso3d_full_direct391": 4,
-         "ti3d_cg4_bluestein509": 4, "fluid3d_bluestein257": 6}
+         "ti3d_cg4_bluestein509": 4, "fluid3d_bluestein257": 6, "fluid3d_prt3d_direct131": 10,
+         "ti3d_cg4_prt3d_bluestein509": 4}
 
 # Every transform path of the physical-space kernel: each direct-pass shape (prime
 # factors 17, 23, 37, 71, 131 and 47 x 3, 43 x 7, 17 x 23), Bluestein (257, 509) and
