@@ -63,7 +63,7 @@ def spherical_batch(r0, r1, t0, t1, axial):
 
 
 def element_benchmark(n_elem=200_000, seed=0, att=ATT_CG4, nsls=3, dt=0.05, axial_frac=0.01,
-                      nu_min=8, nu_max=256, kahan=False, dtype=np.float32):
+                      nu_min=8, nu_max=256, kahan=False, dtype=np.float32, in3d=True):
     rng = np.random.default_rng(seed)
     nu = np.round(np.exp(rng.uniform(np.log(nu_min), np.log(nu_max), n_elem))).astype(np.int32)
     nr = 2 * nu + 1
@@ -85,8 +85,11 @@ def element_benchmark(n_elem=200_000, seed=0, att=ATT_CG4, nsls=3, dt=0.05, axia
         alpha, beta, gamma, _, _ = ATT.att_factors(w, y, f_min, f_max, f_ref, dt, np.ones(1), np.ones(1), True)
         qmu_e = rng.uniform(80, 600, n_elem)
     npa = 4 if att == ATT_CG4 else 25
-    mod_len = 5 * nr.astype(np.int64) * 25
-    att_len = (2 * nr.astype(np.int64) * npa) if att != ATT_NONE else np.zeros(n_elem, np.int64)
+    # material rows per element: every azimuth sample (3-D, physical-space path) or one
+    # (1-D, Fourier-space path)
+    rows_e = nr.astype(np.int64) if in3d else np.ones(n_elem, np.int64)
+    mod_len = 5 * rows_e * 25
+    att_len = (2 * rows_e * npa) if att != ATT_NONE else np.zeros(n_elem, np.int64)
     mofs = np.concatenate([[0], np.cumsum(mod_len)[:-1]]).astype(np.int64)
     aofs = np.concatenate([[0], np.cumsum(att_len)[:-1]]).astype(np.int64)
     moduli = np.empty(int(mod_len.sum()), dtype)
@@ -96,7 +99,7 @@ def element_benchmark(n_elem=200_000, seed=0, att=ATT_CG4, nsls=3, dt=0.05, axia
     for r_val in np.unique(nr):
         idx = np.nonzero(nr == r_val)[0]
         m = len(idx)
-        shape = (m, int(r_val), 25)
+        shape = (m, int(r_val) if in3d else 1, 25)
         vp = MANTLE_VP * (1 + 0.05 * rng.uniform(-1, 1, shape))
         vs = MANTLE_VS * (1 + 0.05 * rng.uniform(-1, 1, shape))
         rho = MANTLE_RHO * (1 + 0.05 * rng.uniform(-1, 1, shape))
@@ -157,7 +160,7 @@ def element_benchmark(n_elem=200_000, seed=0, att=ATT_CG4, nsls=3, dt=0.05, axia
         p_mflen=np.zeros(P, np.int32), p_mf=np.zeros(0, np.float32), p_sflen=np.zeros(P, np.int32),
         p_sfn=np.zeros((0, 3), np.float32), p_sfni=np.zeros((0, 3), np.float32),
         e_pts=e_pts, e_mat=np.full(n_elem, MAT_TISO, np.int8), e_axial=axial.astype(np.uint8),
-        e_in3d=np.ones(n_elem, np.uint8), e_geo=geo.astype(np.float32), e_trig=trig.astype(np.float32),
+        e_in3d=np.full(n_elem, int(in3d), np.uint8), e_geo=geo.astype(np.float32), e_trig=trig.astype(np.float32),
         e_mofs=mofs, e_mod=moduli, e_att=np.full(n_elem, att, np.int8), e_aofs=aofs, e_attm=attm,
         nsls=nsls if att != ATT_NONE else 0, att_alpha=alpha, att_beta=beta, att_gamma=gamma,
         att_do_kappa=True, kahan=kahan, stability_interval=0)

@@ -37,6 +37,62 @@ METRIC = "GLL-pt*azimuth updates/s (element-local count), fused stiffness+Newmar
 UNIT = "updates/s"
 
 
+def run_earth3d(args, world, rank, local, full_steps=20000):
+    """3-D Earth full solver: the layered half disk refined to ~63,000 quads (about 10 s
+    shortest period), seeded Gaussian-random dlnVs / dlnVp (4 % RMS, 500 km lateral, 200 km
+    radial correlation) forcing physical-space stiffness everywhere in the solid, Nu fixed
+    at 256, fluid outer core with solid-fluid coupling, compensated Newmark, 200 stations.
+    The run covers 20,000 steps; here a window of max(steps, 50) steps is timed and the
+    time-to-seismogram of the whole run is the pre-loop plus 20,000 times the step time.
+    0.8 of the mesh's CFL step (the step 3-D runs at the top orders are stable at)."""
+    import tempfile
+    import torch
+    from axisem3d_gb300 import build, solver
+    from axisem3d_gb300.capi import Ax3dDomain
+    from axisem3d_gb300.nu_learn import DT_FACTOR, model_strings
+    build.build()
+    window = max(args.steps, 50)
+    d = Path(tempfile.mkdtemp()) / "input"
+    mesh = dict(n_theta=320, h_mantle=30e3, h_core=33e3)
+    solver.write_inputs(d, mesh_kw=mesh, steps=full_steps, hdur=10.0, n_stations=200, seed=args.seed, nu=256,
+                        models3d=model_strings(1000 + args.seed))
+    p = d / "inparam.time_src_recv"
+    p.write_text(p.read_text().replace("TIME_DELTA_T_FACTOR 1.0", f"TIME_DELTA_T_FACTOR {DT_FACTOR}"))
+    t0 = time.perf_counter()
+    sim = solver.Simulation(d)
+    spec = sim.build(kahan=True, preloop="gpu")
+    t_pre = time.perf_counter() - t0
+    upd = int(spec.p_nr.astype(np.int64).sum())
+    dom = Ax3dDomain(spec, device=local)
+    tune = dom.autotune(2)
+    dom.enable_timers(True)
+    dom.step(args.warmup)
+    dom.read_timers()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    dom.step(window)
+    seis = dom.seismograms(0, args.warmup + window)
+    wall = time.perf_counter() - t0
+    tm = dom.read_timers()
+    dom.close()
+    dev_s = tm["step"][0] / 1e3
+    if rank != 0:
+        return
+    line = {"metric": "GLL-pt*azimuth updates/s (unique-point count), 3-D full solver", "value": upd * window / dev_s,
+            "unit": UNIT, "n_gpus": world, "steps": window, "warmup": args.warmup,
+            "ms_per_step": dev_s * 1e3 / window, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": f"3-D Earth full solver, {spec.n_elements} quads, Nu=256, Gaussian-random 3-D "
+                                   f"model, fluid core, compensated Newmark, {len(spec.r_elem)} stations",
+                       "points": spec.n_points, "dt": spec.dt, "schedule": tune[:120]},
+            "phases_ms_per_step": {k: v[0] / window for k, v in tm.items()},
+            "gpu_launches": sum(v[1] for k, v in tm.items() if k != "step"),
+            "preloop_s": t_pre, "wall_ms_per_step": wall * 1e3 / window,
+            "time_to_seismogram_s": {"run_steps": full_steps, "estimate": t_pre + full_steps * dev_s / window},
+            "finite": bool(np.isfinite(seis).all())}
+    print(json.dumps(line), flush=True)
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -45,15 +101,22 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--elements", type=int, default=200_000)
     ap.add_argument("--att", default="cg4", choices=["cg4", "full", "none"])
+    ap.add_argument("--material", default="3d", choices=["3d", "1d"],
+                    help="3d: moduli per azimuth sample (physical-space path, default); 1d: per GLL point "
+                         "(Fourier-space path)")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--schedule", default="",
                     help="ratio,policy,nside,merge: pin the element bucket schedule instead of autotuning it")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=0, help="elements per CPU worker (0 = auto)")
-    ap.add_argument("--workload", default="elements", choices=["elements", "halfdisk", "ensemble"],
-                    help="elements: the element-level benchmark (default); halfdisk: the full solver")
+    ap.add_argument("--workload", default="elements", choices=["elements", "halfdisk", "earth3d", "ensemble"],
+                    help="elements: the element-level benchmark (default); halfdisk: the full solver; earth3d: "
+                         "the 3-D full solver at Nu 256; ensemble: the batched ensemble")
     return ap.parse_args()
+
+
+MATERIAL = {"3d": "3-D (physical-space) material", "1d": "1-D (Fourier-space) material"}
 
 
 def att_kind(name):
@@ -61,18 +124,22 @@ def att_kind(name):
     return {"cg4": ATT_CG4, "full": ATT_FULL, "none": ATT_NONE}[name]
 
 
-def algorithmic_bytes(spec, att):
+def algorithmic_bytes(spec, att, in3d=True):
     """Compulsory HBM bytes of one element-stiffness pass (each array read/written once).
 
     Per element with n = Nu+1 orders and nr samples: displacement in 600 n, element force
-    out 600 n, geometry 500 B, theta tables 400 B, TI moduli 5*25*4*nr, SLS state
-    (nsls+1)*nr*6*npa*4 read + write, attenuation moduli 2*nr*npa*4 (npa = 4 CG4 / 25)."""
+    out 600 n, geometry 500 B, theta tables 400 B; 3-D (physical space): TI moduli
+    5*25*4*nr, SLS state (nsls+1)*nr*6*npa*4 read + write, attenuation moduli 2*nr*npa*4
+    (npa = 4 CG4 / 25); 1-D (Fourier space): TI moduli 5*25*4, complex SLS state
+    (nsls+1)*n*6*npa*8 read + write, attenuation moduli 2*npa*4."""
     nr = spec.element_nr().astype(np.int64)
     n = nr // 2 + 1
-    b = 600 * n + 600 * n + 500 + 400 + 5 * 25 * 4 * nr
+    rows = nr if in3d else 1
+    b = 600 * n + 600 * n + 500 + 400 + 5 * 25 * 4 * rows
     if att != "none":
         npa = 4 if att == "cg4" else 25
-        b = b + 2 * (spec.nsls + 1) * nr * 6 * npa * 4 + 2 * nr * npa * 4
+        state = nr * 6 * npa * 4 if in3d else n * 6 * npa * 8
+        b = b + 2 * (spec.nsls + 1) * state + 2 * rows * npa * 4
     return int(b.sum())
 
 
@@ -176,11 +243,11 @@ def peaks():
 # in the reference).
 def _cpu_worker(a):
     """Build one partition sample and time the CPU baseline's loop body on it."""
-    seed, n_elem, att, steps = a
+    seed, n_elem, att, steps, in3d = a
     sys.path.insert(0, str(ROOT))
     from axisem3d_gb300 import workloads as W
     from oracle.oracle_py import OracleDomain
-    spec = W.element_benchmark(n_elem=n_elem, seed=seed, att=att_kind(att))
+    spec = W.element_benchmark(n_elem=n_elem, seed=seed, att=att_kind(att), in3d=in3d)
     d = OracleDomain(spec, fft=True)
     d.set("displ", "solid", W.benchmark_displacement(spec, seed=seed + 1).astype(np.complex128))
     d.step(1)  # first touch, transform plans
@@ -196,13 +263,13 @@ def nr_histogram(nr):
     return f"nr mean {float(np.mean(nr)):.1f}, quartiles {'/'.join(str(int(x)) for x in q)}"
 
 
-def cpu_baseline(att, cores, sample, steps=2, seed=1000):
+def cpu_baseline(att, cores, sample, steps=2, seed=1000, in3d=True):
     import multiprocessing as mp
     from oracle.oracle_py import build_oracle
     build_oracle()
     ctx = mp.get_context("spawn")
     with ctx.Pool(cores) as pool:
-        res = pool.map(_cpu_worker, [(seed + 7 * i, sample, att, steps) for i in range(cores)])
+        res = pool.map(_cpu_worker, [(seed + 7 * i, sample, att, steps, in3d) for i in range(cores)])
     upd = sum(r[0] for r in res)
     wall = max(r[1] for r in res)
     nrs = [x for r in res for x in r[2]]
@@ -221,14 +288,14 @@ def run_reference(args, world, rank):
     sample = args.cpu_sample or CPU_SAMPLE
     vals = []
     for _ in range(max(1, min(args.steps, 3))):
-        v, info = cpu_baseline(args.att, cores, sample)
+        v, info = cpu_baseline(args.att, cores, sample, in3d=args.material == "3d")
         vals.append(v)
     v = float(np.median(vals))
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
             "config": {"workload": f"element stiffness batching, {args.elements} TI elements, Nu 8-256 "
-                                   f"log-uniform, 3 SLS {args.att}, 3-D (physical-space) material"},
+                                   f"log-uniform, 3 SLS {args.att}, {MATERIAL[args.material]}"},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": info["cores"], "kind": "port",
                              "variant": "port-fft", "sample": info["sample"]},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -244,7 +311,8 @@ def run_gb300(args, world, rank, local):
     from axisem3d_gb300.capi import Ax3dDomain
     build.build()
     t_build = time.perf_counter()
-    spec = W.element_benchmark(n_elem=args.elements, seed=args.seed + rank, att=att_kind(args.att))
+    in3d = args.material == "3d"
+    spec = W.element_benchmark(n_elem=args.elements, seed=args.seed + rank, att=att_kind(args.att), in3d=in3d)
     u0 = W.benchmark_displacement(spec, seed=args.seed + 100 + rank)
     dom = Ax3dDomain(spec, device=local)
     dom.set("displ", "solid", u0)
@@ -311,14 +379,14 @@ def run_gb300(args, world, rank, local):
     if rank != 0:
         return
     elem_ms = tm["elements"][0] / args.steps
-    abytes = algorithmic_bytes(spec, args.att)
+    abytes = algorithmic_bytes(spec, args.att, in3d)
     peak, src = peaks()
     achieved = abytes / (elem_ms / 1e3) / 1e9
     launches = sum(v[1] for k, v in tm.items() if k != "step")
     cpu = None
     if not args.no_cpu_baseline:
         try:
-            v, info = cpu_baseline(args.att, os.cpu_count() or 1, args.cpu_sample or CPU_SAMPLE)
+            v, info = cpu_baseline(args.att, os.cpu_count() or 1, args.cpu_sample or CPU_SAMPLE, in3d=in3d)
             cpu = {"value": v, "unit": UNIT, "cores": info["cores"], "kind": "port", "variant": "port-fft",
                    "sample": info["sample"]}
         except Exception as e:  # the CPU leg must not hide the GPU number
@@ -330,15 +398,17 @@ def run_gb300(args, world, rank, local):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded)",
         "config": {"workload": f"element stiffness batching, {args.elements} TI elements, Nu 8-256 "
-                               f"log-uniform (nr = 2Nu+1), 3 SLS {args.att}, 3-D (physical-space) material, "
+                               f"log-uniform (nr = 2Nu+1), 3 SLS {args.att}, {MATERIAL[args.material]}, "
                                f"fused stiffness+Newmark step", "elements": args.elements,
                    "updates_per_step": upd, "parallelism": f"replicas x{world}", "schedule": tune[:80],
                    "l2": "working set > L2 (no flush needed)"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": (tr * abytes if (tr := TRAFFIC_PER_ALGO_BYTE) else None),
+                     "frac": achieved / peak,
+                     "traffic": (TRAFFIC_PER_ALGO_BYTE * abytes if in3d and args.att == "cg4" else None),
                      "traffic_unit": "bytes per step (ncu DRAM bytes per algorithmic byte x algorithmic bytes)",
                      "peak_source": src,
-                     "kernel": "element stiffness (k_elem_phys, all buckets)",
+                     "kernel": ("element stiffness (k_elem_phys, all buckets)" if in3d
+                                else "element stiffness (k_elem_fourier_solid)"),
                      "algorithmic_bytes_per_step": abytes, "kernel_ms_per_step": elem_ms},
         "phases_ms_per_step": {k: v[0] / args.steps for k, v in tm.items()},
         "gpu_launches": launches,
@@ -502,6 +572,8 @@ def main():
         run_reference(args, world, rank)
     elif args.workload == "halfdisk":
         run_halfdisk(args, world, rank, local)
+    elif args.workload == "earth3d":
+        run_earth3d(args, world, rank, local)
     elif args.workload == "ensemble":
         run_ensemble(args, world, rank, local)
     else:

@@ -193,17 +193,18 @@ def test_wisdom_learning_matches_oracle(ax3d_lib):
     assert (np.abs(wg - wo) <= 1).all() and (wg != wo).mean() <= 0.01
 
 
-@pytest.mark.parametrize("att", [ATT_CG4, ATT_FULL])
-def test_element_benchmark_matches_oracle(ax3d_lib, att):
+@pytest.mark.parametrize("att,in3d", [(ATT_CG4, True), (ATT_FULL, True), (ATT_CG4, False), (ATT_FULL, False)])
+def test_element_benchmark_matches_oracle(ax3d_lib, att, in3d):
     """The element-stiffness benchmark's domain over its whole Nu range 8-256 (elements that
     own their points, so they assemble directly into the point stiffness): ten of the 20
     elements have rings above nr 186, which run on thread-block clusters, the rest on single
     CTAs.  compute_stiff (read-modify-write of the point stiffness), then three steps (the
-    write-only stiffness rows of ax3d_step), TI moduli, CG4 or full-grid SLS."""
+    write-only stiffness rows of ax3d_step), TI moduli, CG4 or full-grid SLS; with 3-D
+    material (physical-space path) and with 1-D material (Fourier-space path)."""
     from oracle.oracle_py import OracleDomain
     from axisem3d_gb300 import workloads as W
     from axisem3d_gb300.capi import Ax3dDomain
-    spec = W.element_benchmark(n_elem=20, seed=9, att=att, nu_min=8, nu_max=256)
+    spec = W.element_benchmark(n_elem=20, seed=9, att=att, nu_min=8, nu_max=256, in3d=in3d)
     nr = spec.element_nr()
     assert (nr > 186).sum() >= 6 and nr.max() > 450 and nr.min() < 32
     u0 = W.benchmark_displacement(spec, seed=8)
