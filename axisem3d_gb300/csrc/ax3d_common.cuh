@@ -8,6 +8,10 @@ namespace ax3d {
 
 constexpr int NP = 5;    // GLL points per edge (nPol = 4)
 constexpr int NPE = 25;  // GLL points per element
+// Fourier orders per work item of the Fourier-space element kernels: a warp keeps the
+// element's operators, geometry and moduli in registers over FW_OB consecutive orders
+// and loads the next order's displacement while it works on the current one
+constexpr int FW_OB = 8;
 
 // element flag bits
 constexpr int EF_AXIAL = 1;

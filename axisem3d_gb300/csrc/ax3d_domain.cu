@@ -553,7 +553,7 @@ struct ax3d_domain {
             } else if (e3d) {
                 (fluid ? phys3_f : phys3_s).push_back(e);
             } else {
-                for (int al = 0; al < n; al++) (fluid ? items_f : items_s).push_back(make_int2(e, al));
+                for (int al = 0; al < n; al += ax3d::FW_OB) (fluid ? items_f : items_s).push_back(make_int2(e, al));
             }
         }
         // physical-space solid elements that own all their points (solid points of no other

@@ -135,8 +135,19 @@ __device__ __forceinline__ float2 load_fluid_u(const PointTable &P, const float2
 }
 
 // ------------------------------------------------------------------------------------
-// Fourier-space solid elements: warp per (element, order)
+// Fourier-space solid elements: warp per (element, block of FW_OB orders)
 // ------------------------------------------------------------------------------------
+// A point's displacement block and order limit, read once per work item.
+struct UPoint {
+    const float2 *base;
+    int plim;
+    __device__ __forceinline__ void init(const PointTable &P, const float2 *u, int64_t ofs, int pt) {
+        const int pnr = P.nr[pt];
+        plim = pnr / 2 - (pnr % 2 == 0);
+        base = u + ofs;
+    }
+};
+
 __global__ void __launch_bounds__(FW_WARPS * 32)
     k_elem_fourier_solid(ElemTable T, PointTable P, const float2 *__restrict__ su,
                          const int2 *__restrict__ items, int nitems, SLS sls) {
@@ -146,45 +157,70 @@ __global__ void __launch_bounds__(FW_WARPS * 32)
     const bool active = lane < NPE;
     const int p = active ? lane : 0;
     for (int it = blockIdx.x * FW_WARPS + warp; it < nitems; it += gridDim.x * FW_WARPS) {
-        const int e = items[it].x, a = items[it].y;
+        const int e = items[it].x, a0 = items[it].y;
         const int flags = T.flags[e];
         const bool axial = flags & EF_AXIAL;
         const int nr = T.nr[e], nu = nr / 2, n = nu + 1, lim = nu - (nr % 2 == 0);
+        const int a1 = min(a0 + FW_OB, n);
         const int mat = ef_mat(flags), att = ef_att(flags);
         const bool tiso = (mat == 1 || mat == 2);
+        // the element's per-lane constants, kept over the item's orders
         LaneOps L;
         L.init(p, axial);
         Geo g;
         g.load(T.geo + (int64_t)e * 125, p);
-        if (active) {
-            float2 u[3];
-            load_solid_u(P, su, T.pts[e * NPE + p], a, u);
-            q[p] = u[0];
-            q[25 + p] = u[1];
-            q[50 + p] = u[2];
-        }
-        __syncwarp();
-        float2 eps[6], sig[6];
-#pragma unroll
-        for (int c = 0; c < 6; c++) eps[c] = make_float2(0.f, 0.f);
-        if (active && a <= lim) grad6_lane(L, g, axial, a, q, eps);
-        __syncwarp();
-        if (active) {
+        float s1 = 0.f, c1 = 0.f, s2 = 0.f, c2 = 0.f;
+        if (tiso) {
             const float *tr = T.trig + (int64_t)e * 100;
-            float s1 = 0.f, c1 = 0.f, s2 = 0.f, c2 = 0.f;
-            if (tiso) {
-                s1 = tr[p];
-                c1 = tr[25 + p];
-                s2 = tr[50 + p];
-                c2 = tr[75 + p];
-                spz_rtz(eps, s1, c1, s2, c2);
+            s1 = tr[p];
+            c1 = tr[25 + p];
+            s2 = tr[50 + p];
+            c2 = tr[75 + p];
+        }
+        const float *md = T.moduli + T.mofs[e];
+        const int npa = att == 2 ? 4 : NPE;
+        const int qq = att == 2 ? cg4_index(p) : p;
+        float dk = 0.f, dm = 0.f;
+        if (att && qq >= 0) {
+            const float *am = T.attm + T.aofs[e];
+            dk = am[qq];
+            dm = am[npa + qq];
+        }
+        const int pt = T.pts[e * NPE + p];
+        UPoint up;
+        up.init(P, su, P.sofs[pt], pt);
+        float2 un[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+        if (active && a0 <= up.plim) {
+            const float2 *s = up.base + (int64_t)a0 * 3;
+            un[0] = s[0];
+            un[1] = s[1];
+            un[2] = s[2];
+        }
+        float2 *ef = T.ef + T.efofs[e] + (int64_t)p * n * 3;
+        for (int a = a0; a < a1; a++) {
+            if (active) {
+                q[p] = un[0];
+                q[25 + p] = un[1];
+                q[50 + p] = un[2];
+                // the next order's displacement is in flight while this one is worked on
+                un[0] = un[1] = un[2] = make_float2(0.f, 0.f);
+                if (a + 1 < a1 && a + 1 <= up.plim) {
+                    const float2 *s = up.base + (int64_t)(a + 1) * 3;
+                    un[0] = s[0];
+                    un[1] = s[1];
+                    un[2] = s[2];
+                }
             }
-            const float *md = T.moduli + T.mofs[e];
-            elastic(mat, eps, sig, [&](int k) { return md[k * NPE + p]; });
-            if (att) {
-                const int npa = att == 2 ? 4 : NPE;
-                const int qq = att == 2 ? cg4_index(p) : p;
-                if (qq >= 0) {
+            __syncwarp();
+            float2 eps[6], sig[6];
+#pragma unroll
+            for (int c = 0; c < 6; c++) eps[c] = make_float2(0.f, 0.f);
+            if (active && a <= lim) grad6_lane(L, g, axial, a, q, eps);
+            __syncwarp();
+            if (active) {
+                if (tiso) spz_rtz(eps, s1, c1, s2, c2);
+                elastic(mat, eps, sig, [&](int k) { return md[k * NPE + p]; });
+                if (att && qq >= 0) {
                     float2 *mem = reinterpret_cast<float2 *>(T.mem + T.memofs[e]);
                     const int64_t sl = (int64_t)n * 6 * npa;
                     float2 *R = mem + (int64_t)a * 6 * npa + qq;
@@ -192,28 +228,29 @@ __global__ void __launch_bounds__(FW_WARPS * 32)
                     for (int l = 0; l < sls.nsls; l++)
 #pragma unroll
                         for (int c = 0; c < 6; c++) sig[c] = csub(sig[c], R[l * sl + c * npa]);
-                    const float *am = T.attm + T.aofs[e];
-                    sls_update(sls, R, SR, sl, (int64_t)npa, eps, am[qq], am[npa + qq]);
+                    sls_update(sls, R, SR, sl, (int64_t)npa, eps, dk, dm);
+                }
+                if (tiso) rtz_spz(sig, s1, c1, s2, c2);
+            }
+            float2 f[3];
+            quad6_lane(L, g, axial, a, sig, q, active && a <= lim, f);
+            if (active) {
+                float2 *o = ef + (int64_t)a * 3;
+                if (a <= lim) {
+                    o[0] = f[0];
+                    o[1] = f[1];
+                    o[2] = f[2];
+                } else {
+                    o[0] = o[1] = o[2] = make_float2(0.f, 0.f);
                 }
             }
-            if (tiso) rtz_spz(sig, s1, c1, s2, c2);
-        }
-        float2 f[3];
-        quad6_lane(L, g, axial, a, sig, q, active && a <= lim, f);
-        if (active) {
-            float2 *ef = T.ef + T.efofs[e] + ((int64_t)p * n + a) * 3;
-            if (a <= lim) {
-                ef[0] = f[0];
-                ef[1] = f[1];
-                ef[2] = f[2];
-            } else {
-                ef[0] = ef[1] = ef[2] = make_float2(0.f, 0.f);
-            }
+            __syncwarp();  // the scratch is rewritten by the next order
         }
     }
 }
 
-// Fourier-space fluid elements (FluidElement.cpp:333-355 with Acoustic1D.cpp:8-16)
+// Fourier-space fluid elements (FluidElement.cpp:333-355 with Acoustic1D.cpp:8-16): warp
+// per (element, block of FW_OB orders), as the solid kernel
 __global__ void __launch_bounds__(FW_WARPS * 32)
     k_elem_fourier_fluid(ElemTable T, PointTable P, const float2 *__restrict__ fu,
                          const int2 *__restrict__ items, int nitems) {
@@ -223,25 +260,37 @@ __global__ void __launch_bounds__(FW_WARPS * 32)
     const bool active = lane < NPE;
     const int p = active ? lane : 0;
     for (int it = blockIdx.x * FW_WARPS + warp; it < nitems; it += gridDim.x * FW_WARPS) {
-        const int e = items[it].x, a = items[it].y;
+        const int e = items[it].x, a0 = items[it].y;
         const bool axial = T.flags[e] & EF_AXIAL;
         const int nr = T.nr[e], nu = nr / 2, n = nu + 1, lim = nu - (nr % 2 == 0);
+        const int a1 = min(a0 + FW_OB, n);
         LaneOps L;
         L.init(p, axial);
         Geo g;
         g.load(T.geo + (int64_t)e * 125, p);
-        if (active) q[p] = load_fluid_u(P, fu, T.pts[e * NPE + p], a);
-        __syncwarp();
-        float2 eps[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
-        if (active && a <= lim) grad1_lane(L, g, axial, a, q, eps);
-        __syncwarp();
-        float2 sig[3];
         const float K = active ? T.moduli[T.mofs[e] + p] : 0.f;
+        const int pt = T.pts[e * NPE + p];
+        UPoint up;
+        up.init(P, fu, P.fofs[pt], pt);
+        float2 un = (active && a0 <= up.plim) ? up.base[a0] : make_float2(0.f, 0.f);
+        float2 *ef = T.ef + T.efofs[e] + (int64_t)p * n;
+        for (int a = a0; a < a1; a++) {
+            if (active) {
+                q[p] = un;
+                un = (a + 1 < a1 && a + 1 <= up.plim) ? up.base[a + 1] : make_float2(0.f, 0.f);
+            }
+            __syncwarp();
+            float2 eps[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+            if (active && a <= lim) grad1_lane(L, g, axial, a, q, eps);
+            __syncwarp();
+            float2 sig[3];
 #pragma unroll
-        for (int c = 0; c < 3; c++) sig[c] = cscale(K, eps[c]);
-        float2 f;
-        quad1_lane(L, g, axial, a, sig, q, active && a <= lim, f);
-        if (active) T.ef[T.efofs[e] + (int64_t)p * n + a] = a <= lim ? f : make_float2(0.f, 0.f);
+            for (int c = 0; c < 3; c++) sig[c] = cscale(K, eps[c]);
+            float2 f;
+            quad1_lane(L, g, axial, a, sig, q, active && a <= lim, f);
+            if (active) ef[a] = a <= lim ? f : make_float2(0.f, 0.f);
+            __syncwarp();
+        }
     }
 }
 

@@ -141,16 +141,16 @@ def test_batch_above_max_is_rejected(ax3d_lib):
 @pytest.mark.gpu
 def test_learned_nu_gain_on_held_out_model(tmp_path, ax3d_lib, capsys):
     """What the trained network gains over the method without it.  The network is trained on
-    the Nu wisdom labels of three full-Nu runs (seeded Gaussian-random 3-D models) and predicts
-    the Fourier order of every element of a model it has not seen.  Without the network the
+    the Nu wisdom labels of full-Nu runs (seeded Gaussian-random 3-D models) and predicts the
+    Fourier order of every element of a model it has not seen.  Without the network the
     method runs that model at the full Nu (or pays a full-Nu run first to learn its wisdom);
     with it, the run at the predicted orders costs fewer GLL-point x azimuth updates per step
     and its seismograms stay within 1 % relative L2 of the full-Nu run's.  (The network is
-    fitted on two of the three models; the third calibrates the shift of its predictions.)"""
+    fitted on four models; two more calibrate the shift of its predictions.)"""
     from axisem3d_gb300 import nu_learn
     mesh = dict(n_theta=16, h_mantle=600e3, h_core=700e3, r_c=1500e3)
-    s = nu_learn.experiment(tmp_path, n_train=3, n_test=1, nu_full=32, steps=300, epochs=200, batch=512,
-                            mesh_kw=mesh, log=lambda m: None)
+    s = nu_learn.experiment(tmp_path, n_train=6, n_val=2, n_test=1, nu_full=32, steps=375, epochs=200,
+                            batch=512, mesh_kw=mesh, log=lambda m: None)
     t = s["tests"][0]
     with capsys.disabled():
         print(f"\nlearned Nu: misfit {t['misfit']:.4f}, updates/step {t['upd_full']} -> {t['upd_learned']}, "
