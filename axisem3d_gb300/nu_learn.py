@@ -230,9 +230,12 @@ def experiment(work, n_train=64, n_test=16, nu_full=64, steps=600, epochs=200, b
         pre_f = time.perf_counter() - t0
         seis_f, t_f, _, upd_f = run(spec_f, steps)
         _, t_fl, wis, _ = run(spec_f, steps, learn=(interval, eps))
-        # learned route: features, network inference, pre-loop at the predicted Nu, the loop
+        # learned route, from the input files alone: the feature pass (mesh, geometry, 1-D
+        # material), the features, network inference, the pre-loop at the predicted Nu, the loop
         t0 = time.perf_counter()
-        x = element_features(sim, gpu=preloop == "gpu")
+        sim_l = solver.Simulation(d)
+        sim_l.feature_pass(preloop=preloop)
+        x = element_features(sim_l, gpu=preloop == "gpu")
         t_feat = time.perf_counter() - t0
         import torch
         t0 = time.perf_counter()
@@ -241,7 +244,7 @@ def experiment(work, n_train=64, n_test=16, nu_full=64, steps=600, epochs=200, b
         t_inf = time.perf_counter() - t0
         nu_e = decode(y, nu_full, shift)
         t0 = time.perf_counter()
-        spec_l = sim.build(nu_elem=nu_e, preloop=preloop)
+        spec_l = sim_l.build(nu_elem=nu_e, preloop=preloop)
         pre_l = time.perf_counter() - t0
         seis_l, t_l, _, upd_l = run(spec_l, steps)
         mis = float(np.linalg.norm(seis_l - seis_f) / np.linalg.norm(seis_f))

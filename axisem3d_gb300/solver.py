@@ -242,14 +242,9 @@ class Simulation:
         self.output_dir = Path(output_dir or self.input_dir.parent / "output")
         self.par = Parameters(self.input_dir)
 
-    # ------------------------------------------------------------------ build
-    def build(self, kahan=False, nu_elem=None, preloop="host") -> DomainSpec:
-        """Pack the domain.  nu_elem: optional per-element Fourier order (a learned or user
-        Nu field) replacing NU_CONST; each point takes the maximum over its elements.
-        preloop = "gpu" computes the element geometry (ax3d_precompute_geometry), the
-        Gaussian-random 3-D model samples (ax3d_sample_gaussian_random), the 1-D elemental
-        masses (ax3d_precompute_mass) and the solid elements' moduli (ax3d_precompute_elastic)
-        in FP64 on the GPU instead of numpy."""
+    def _mesh_geometry(self, preloop):
+        """The Exodus mesh and every element's GLL geometry (Quad::createGraident +
+        formIntegralFactor; FP64 on the GPU when preloop = "gpu")."""
         par = self.par
         ex = Exodus.read(self.input_dir / par.get("MODEL_1D_EXODUS_MESH_FILE"))
         self.ex = ex
@@ -274,6 +269,52 @@ class Simulation:
             jac = PL.jacobian_from_geometry(geo)
         else:
             geo, ifact, crds, theta, jac = GEO.batch_geometry(nodes, ex.etype, co, axial_e)
+        return ex, E, axial_e, co, nodes, geo, ifact, crds, theta, jac
+
+    @staticmethod
+    def _gll_material(ex, axial_e):
+        """1-D material at the GLL points: bilinear in (xi, eta) of the element's nodal values."""
+        E = len(ex.conn)
+        xg = S.gll()[0]
+        xj = S.glj()[0]
+        XI = np.where(axial_e[:, None, None], xj[None, :, None], xg[None, :, None]) * np.ones((1, 1, 5))
+        ETA = np.broadcast_to(xg[None, None, :], (E, 5, 5))
+        shp = np.stack([(1 - XI) * (1 - ETA), (1 + XI) * (1 - ETA), (1 + XI) * (1 + ETA), (1 - XI) * (1 + ETA)], -1) / 4
+        return {k: np.einsum("epqk,ek->epq", shp, v).reshape(E, 25) for k, v in ex.nodal.items()}
+
+    def feature_pass(self, preloop="host"):
+        """What the learned-Nu element features need before any Nr is chosen, without the
+        rest of the pre-loop: the element GLL coordinates, the 1-D Vp and Vs per element, the
+        3-D models and the source depth."""
+        ex, E, axial_e, co, nodes, geo, ifact, crds, theta, jac = self._mesh_geometry(preloop)
+        mat = self._gll_material(ex, axial_e)
+        self.crds = crds
+        self.vp_e, self.vs_e = mat["VP"].mean(1), mat["VS"].mean(1)
+        self.models = M3D.volumetric_models(self.par, self._cmt_latlon(), self.R)
+        self.src_dep = self._source_depth()
+
+    def _source_depth(self):
+        """Source depth in m from SOURCE_FILE (0 in non-source mode)."""
+        if _flag(self.par, "DEVELOP_NON_SOURCE_MODE"):
+            return 0.0
+        text = (self.input_dir / self.par.get("SOURCE_FILE")).read_text()
+        if self.par.get("SOURCE_TYPE").lower() == "point_force":
+            return _parse_keys(text, ("depth",))["depth"] * 1e3
+        for line in text.splitlines()[1:]:
+            if ":" in line and line.split(":", 1)[0].strip() == "depth":
+                return float(line.split(":", 1)[1]) * 1e3
+        raise ValueError("Source::buildInparam || no depth in SOURCE_FILE")
+
+    # ------------------------------------------------------------------ build
+    def build(self, kahan=False, nu_elem=None, preloop="host") -> DomainSpec:
+        """Pack the domain.  nu_elem: optional per-element Fourier order (a learned or user
+        Nu field) replacing NU_CONST; each point takes the maximum over its elements.
+        preloop = "gpu" computes the element geometry (ax3d_precompute_geometry), the
+        Gaussian-random 3-D model samples (ax3d_sample_gaussian_random), the 1-D elemental
+        masses (ax3d_precompute_mass) and the solid elements' moduli (ax3d_precompute_elastic)
+        in FP64 on the GPU instead of numpy."""
+        par = self.par
+        ex, E, axial_e, co, nodes, geo, ifact, crds, theta, jac = self._mesh_geometry(preloop)
         self.nodes4, self.co, self.axial_e = nodes, co, axial_e
         # unique GLL points by coordinates (Connectivity::formElemToGLL)
         tol = 1e-3
@@ -284,14 +325,9 @@ class Simulation:
         pcrd = np.zeros((P, 2))
         pcrd[e_pts.ravel()] = crds.reshape(-1, 2)
         pcrd[np.abs(pcrd[:, 0]) < 1e-6, 0] = 0.0
-        # materials at GLL points: bilinear in (xi, eta) of the element's nodal values
-        xg = S.gll()[0]
-        xj = S.glj()[0]
-        XI = np.where(axial_e[:, None, None], xj[None, :, None], xg[None, :, None]) * np.ones((1, 1, 5))
-        ETA = np.broadcast_to(xg[None, None, :], (E, 5, 5))
-        shp = np.stack([(1 - XI) * (1 - ETA), (1 + XI) * (1 - ETA), (1 + XI) * (1 + ETA), (1 - XI) * (1 + ETA)], -1) / 4
-        mat = {k: np.einsum("epqk,ek->epq", shp, v).reshape(E, 25) for k, v in ex.nodal.items()}
+        mat = self._gll_material(ex, axial_e)
         vp, vs, rho = mat["VP"], mat["VS"], mat["RHO"]
+        xj = S.glj()[0]
         fl = ex.fluid
         # Nr field (NrField::buildInparam, NrField.cpp:20-64) with Quad::formNrField's limits;
         # point coordinates rounded as formNrField does (offset = min(1e-5, distTol / 1e3))

@@ -179,3 +179,16 @@ def test_ring_features_gpu_match_host(ax3d_lib):
     fh = (np.log10(host + 1e-12) + 12.0) / 12.0
     fg = (np.log10(gpu + 1e-12) + 12.0) / 12.0
     assert np.abs(fg - fh).max() < 1e-4
+
+
+def test_feature_pass_matches_build(tmp_path):
+    """The learned route's feature pass (mesh, geometry, 1-D material only) gives the element
+    features the full pre-loop gives, so the features need no pre-loop at any Nu."""
+    from axisem3d_gb300 import nu_learn, solver
+    d = nu_learn.write_case(tmp_path / "c", 5000, 16, 10, dict(n_theta=16, h_mantle=600e3, h_core=700e3,
+                                                                r_c=1500e3))
+    a = solver.Simulation(d)
+    a.build()
+    b = solver.Simulation(d)
+    b.feature_pass()
+    np.testing.assert_array_equal(nu_learn.element_features(b), nu_learn.element_features(a))
