@@ -176,6 +176,86 @@ def run(spec, steps, learn=None):
     return seis, t, wis, int(np.asarray(spec.p_nr, np.int64).sum())
 
 
+def held_out(net, shift, work, n_test=16, nu_full=64, steps=600, eps=1e-3, interval=5, mesh_kw=None, out=None,
+             log=print, preloop="gpu", seed0=5000):
+    """The network against the plain full-Nu solver on n_test held-out seeded models (seeds
+    seed0, seed0 + 1, ...): per model the full-Nu route (pre-loop, loop), the learned route
+    from the input files alone (feature pass, features, inference, pre-loop at the predicted
+    Nu, loop) and the wisdom route (the model's own full-Nu wisdom reused); then all learned
+    models batched into one domain.  Returns the per-model records and the batched figures."""
+    work = Path(work)
+    if out:
+        Path(out).mkdir(parents=True, exist_ok=True)
+    tests = []
+    seis_l_all, specs_l, pre_l_all = [], [], []
+    for i in range(n_test):
+        d = write_case(work / f"test{i}", seed0 + i, nu_full, steps, mesh_kw)
+        # plain full-Nu route: pre-loop, then the loop
+        t0 = time.perf_counter()
+        sim = solver.Simulation(d)
+        spec_f = sim.build(preloop=preloop)
+        pre_f = time.perf_counter() - t0
+        seis_f, t_f, _, upd_f = run(spec_f, steps)
+        _, t_fl, wis, _ = run(spec_f, steps, learn=(interval, eps))
+        # learned route, from the input files alone: the feature pass (mesh, geometry, 1-D
+        # material), the features, network inference, the pre-loop at the predicted Nu, the loop
+        t0 = time.perf_counter()
+        sim_l = solver.Simulation(d)
+        sim_l.feature_pass(preloop=preloop)
+        x = element_features(sim_l, gpu=preloop == "gpu")
+        t_feat = time.perf_counter() - t0
+        import torch
+        t0 = time.perf_counter()
+        y = net.forward(x).cpu().numpy()
+        torch.cuda.synchronize()
+        t_inf = time.perf_counter() - t0
+        nu_e = decode(y, nu_full, shift)
+        t0 = time.perf_counter()
+        spec_l = sim_l.build(nu_elem=nu_e, preloop=preloop)
+        pre_l = time.perf_counter() - t0
+        seis_l, t_l, _, upd_l = run(spec_l, steps)
+        mis = float(np.linalg.norm(seis_l - seis_f) / np.linalg.norm(seis_f))
+        # the reference's route without a network: reuse the wisdom of this model's own
+        # full run (which must be paid first)
+        spec_w = sim.build(nu_elem=np.maximum(element_labels(spec_f, wis), 1), preloop=preloop)
+        seis_w, t_w, _, upd_w = run(spec_w, steps)
+        mis_w = float(np.linalg.norm(seis_w - seis_f) / np.linalg.norm(seis_f))
+        tts_f = pre_f + t_f
+        tts_l = t_feat + t_inf + pre_l + t_l
+        tests.append(dict(seed=seed0 + i, misfit=mis, t_full=t_f, t_full_learning=t_fl, t_learned=t_l,
+                          speedup=t_f / t_l, preloop_full=pre_f, preloop_learned=pre_l, features=t_feat,
+                          inference=t_inf, tts_full=tts_f, tts_learned=tts_l, tts_speedup=tts_f / tts_l,
+                          upd_full=upd_f, upd_learned=upd_l, misfit_wisdom=mis_w, t_wisdom=t_w,
+                          mean_nu_pred=float(nu_e.mean()), mean_nu_label=float(element_labels(spec_f, wis).mean())))
+        del spec_f, spec_w
+        specs_l.append(spec_l)
+        seis_l_all.append(seis_l)
+        pre_l_all.append(t_feat + t_inf + pre_l)
+        log(f"test {i}: misfit {mis:.4f} (wisdom {mis_w:.4f}), full {tts_f:.2f} s (loop {t_f:.2f}), "
+            f"learned {tts_l:.2f} s (loop {t_l:.2f}), updates {upd_f} -> {upd_l}")
+        if out:
+            (Path(out) / "tests_partial.json").write_text(json.dumps(tests, indent=1))
+    # all held-out learned-Nu runs batched into one domain
+    from . import ensemble
+    big, info = ensemble.concat(specs_l)
+    seis_b, t_b, _, upd_b = run(big, steps)
+    parts = ensemble.split_seismograms(seis_b, info)
+    mis_b = max(float(np.linalg.norm(p - s) / np.linalg.norm(s)) for p, s in zip(parts, seis_l_all))
+    t_full_sum = sum(t["t_full"] for t in tests)
+    tts_full_sum = sum(t["tts_full"] for t in tests)
+    tts_batched = sum(pre_l_all) + t_b  # every learned model's features, inference, pre-loop + one batched loop
+    return tests, dict(
+        elements=int(len(specs_l[0].e_pts)), misfit_max=max(t["misfit"] for t in tests),
+        misfit_mean=float(np.mean([t["misfit"] for t in tests])),
+        speedup_mean=float(np.mean([t["speedup"] for t in tests])),
+        tts_speedup_mean=float(np.mean([t["tts_speedup"] for t in tests])),
+        batched_seconds=t_b, batched_vs_sequential_full=t_full_sum / t_b,
+        tts_batched_learned_seconds=tts_batched, tts_sequential_full_seconds=tts_full_sum,
+        tts_learned_batched_vs_sequential_full=tts_full_sum / tts_batched,
+        batched_vs_sequential_learned=sum(t["t_learned"] for t in tests) / t_b,
+        batched_split_misfit_max=mis_b)
+
+
 def experiment(work, n_train=64, n_test=16, nu_full=64, steps=600, epochs=200, batch=4096, lr=2e-3,
                eps=1e-3, interval=5, mesh_kw=None, out=None, log=print, target=0.005, preloop="gpu", n_val=1):
     """Train on the wisdom of n_train - n_val full-Nu runs, calibrate the prediction shift on
@@ -219,83 +299,38 @@ def experiment(work, n_train=64, n_test=16, nu_full=64, steps=600, epochs=200, b
     if vals:
         shift, val_misfit = calibrate_shift(vals, net, nu_full=nu_full, steps=steps, target=target, log=log,
                                             preloop=preloop)
-    tests = []
-    seis_l_all, specs_l, pre_l_all = [], [], []
-    for i in range(n_test):
-        d = write_case(work / f"test{i}", 5000 + i, nu_full, steps, mesh_kw)
-        # plain full-Nu route: pre-loop, then the loop
-        t0 = time.perf_counter()
-        sim = solver.Simulation(d)
-        spec_f = sim.build(preloop=preloop)
-        pre_f = time.perf_counter() - t0
-        seis_f, t_f, _, upd_f = run(spec_f, steps)
-        _, t_fl, wis, _ = run(spec_f, steps, learn=(interval, eps))
-        # learned route, from the input files alone: the feature pass (mesh, geometry, 1-D
-        # material), the features, network inference, the pre-loop at the predicted Nu, the loop
-        t0 = time.perf_counter()
-        sim_l = solver.Simulation(d)
-        sim_l.feature_pass(preloop=preloop)
-        x = element_features(sim_l, gpu=preloop == "gpu")
-        t_feat = time.perf_counter() - t0
-        import torch
-        t0 = time.perf_counter()
-        y = net.forward(x).cpu().numpy()
-        torch.cuda.synchronize()
-        t_inf = time.perf_counter() - t0
-        nu_e = decode(y, nu_full, shift)
-        t0 = time.perf_counter()
-        spec_l = sim_l.build(nu_elem=nu_e, preloop=preloop)
-        pre_l = time.perf_counter() - t0
-        seis_l, t_l, _, upd_l = run(spec_l, steps)
-        mis = float(np.linalg.norm(seis_l - seis_f) / np.linalg.norm(seis_f))
-        # the reference's route without a network: reuse the wisdom of this model's own
-        # full run (which must be paid first)
-        spec_w = sim.build(nu_elem=np.maximum(element_labels(spec_f, wis), 1), preloop=preloop)
-        seis_w, t_w, _, upd_w = run(spec_w, steps)
-        mis_w = float(np.linalg.norm(seis_w - seis_f) / np.linalg.norm(seis_f))
-        tts_f = pre_f + t_f
-        tts_l = t_feat + t_inf + pre_l + t_l
-        tests.append(dict(seed=5000 + i, misfit=mis, t_full=t_f, t_full_learning=t_fl, t_learned=t_l,
-                          speedup=t_f / t_l, preloop_full=pre_f, preloop_learned=pre_l, features=t_feat,
-                          inference=t_inf, tts_full=tts_f, tts_learned=tts_l, tts_speedup=tts_f / tts_l,
-                          upd_full=upd_f, upd_learned=upd_l, misfit_wisdom=mis_w, t_wisdom=t_w,
-                          mean_nu_pred=float(nu_e.mean()), mean_nu_label=float(element_labels(spec_f, wis).mean())))
-        del spec_f, spec_w
-        specs_l.append(spec_l)
-        seis_l_all.append(seis_l)
-        pre_l_all.append(t_feat + t_inf + pre_l)
-        log(f"test {i}: misfit {mis:.4f} (wisdom {mis_w:.4f}), full {tts_f:.2f} s (loop {t_f:.2f}), "
-            f"learned {tts_l:.2f} s (loop {t_l:.2f}), updates {upd_f} -> {upd_l}")
-        if out:
-            (Path(out) / "tests_partial.json").write_text(json.dumps(tests, indent=1))
-    # all held-out learned-Nu runs batched into one domain
-    from . import ensemble
-    big, info = ensemble.concat(specs_l)
-    seis_b, t_b, _, upd_b = run(big, steps)
-    parts = ensemble.split_seismograms(seis_b, info)
-    mis_b = max(float(np.linalg.norm(p - s) / np.linalg.norm(s)) for p, s in zip(parts, seis_l_all))
-    t_full_sum = sum(t["t_full"] for t in tests)
-    tts_full_sum = sum(t["tts_full"] for t in tests)
-    tts_batched = sum(pre_l_all) + t_b  # every learned model's features, inference, pre-loop + one batched loop
+    tests, res = held_out(net, shift, work, n_test=n_test, nu_full=nu_full, steps=steps, eps=eps, interval=interval,
+                          mesh_kw=mesh_kw, out=out, log=log, preloop=preloop)
     summary = dict(
-        n_train=n_train, n_test=n_test, nu_full=nu_full, steps=steps, elements=int(len(specs_l[0].e_pts)),
+        n_train=n_train, n_test=n_test, nu_full=nu_full, steps=steps,
         epochs=epochs, batch=batch, fit_seconds=t_fit, train_runs_seconds=t_train_runs,
         preloop_seconds_mean=float(np.mean(pre)) if pre else None, loss_first=float(hist[0]), loss_last=float(hist[-1]),
-        shift=shift, validation_misfit=val_misfit, target=target, tests=tests,
-        misfit_max=max(t["misfit"] for t in tests), misfit_mean=float(np.mean([t["misfit"] for t in tests])),
-        speedup_mean=float(np.mean([t["speedup"] for t in tests])),
-        tts_speedup_mean=float(np.mean([t["tts_speedup"] for t in tests])),
-        batched_seconds=t_b, batched_vs_sequential_full=t_full_sum / t_b,
-        tts_batched_learned_seconds=tts_batched, tts_sequential_full_seconds=tts_full_sum,
-        tts_learned_batched_vs_sequential_full=tts_full_sum / tts_batched,
-        batched_vs_sequential_learned=sum(t["t_learned"] for t in tests) / t_b,
-        batched_split_misfit_max=mis_b)
+        shift=shift, validation_misfit=val_misfit, target=target, tests=tests, **res)
     if out:
         out = Path(out)
         out.mkdir(parents=True, exist_ok=True)
         (out / "summary.json").write_text(json.dumps(summary, indent=1))
         np.savez(out / "nu_mlp.npz", params=net.get_params(), nu_full=nu_full, shift=shift)
     net.close()
+    return summary
+
+
+def evaluate(params_file, work, n_test=16, steps=600, mesh_kw=None, out=None, log=print, preloop="gpu"):
+    """The held-out comparison of a trained network saved by `experiment` (out/nu_mlp.npz:
+    parameters, Nu_full, calibrated shift), without training again."""
+    from .nu_mlp import NuMLP
+    d = np.load(params_file)
+    nu_full, shift = int(d["nu_full"]), float(d["shift"])
+    net = NuMLP(max_batch=4096, params=d["params"])
+    tests, res = held_out(net, shift, work, n_test=n_test, nu_full=nu_full, steps=steps, mesh_kw=mesh_kw,
+                          out=out, log=log, preloop=preloop)
+    net.close()
+    summary = dict(params=str(params_file), n_test=n_test, nu_full=nu_full, steps=steps, shift=shift,
+                   tests=tests, **res)
+    if out:
+        out = Path(out)
+        out.mkdir(parents=True, exist_ok=True)
+        (out / "summary_eval.json").write_text(json.dumps(summary, indent=1))
     return summary
 
 
@@ -311,7 +346,11 @@ if __name__ == "__main__":
     ap.add_argument("--epochs", type=int, default=200)
     ap.add_argument("--eps", type=float, default=1e-3)
     ap.add_argument("--val", type=int, default=1, help="training models that calibrate instead of fitting")
+    ap.add_argument("--params", default="", help="evaluate this saved network on the held-out models, no training")
     a = ap.parse_args()
-    s = experiment(a.work, a.train, a.test, a.nu, a.steps, a.epochs, eps=a.eps, out=a.out,
-                   log=lambda m: print(m, flush=True), n_val=a.val)
+    if a.params:
+        s = evaluate(a.params, a.work, a.test, a.steps, out=a.out, log=lambda m: print(m, flush=True))
+    else:
+        s = experiment(a.work, a.train, a.test, a.nu, a.steps, a.epochs, eps=a.eps, out=a.out,
+                       log=lambda m: print(m, flush=True), n_val=a.val)
     print(json.dumps({k: v for k, v in s.items() if k != "tests"}))
