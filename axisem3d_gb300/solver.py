@@ -244,7 +244,22 @@ class Simulation:
 
     def _mesh_geometry(self, preloop):
         """The Exodus mesh and every element's GLL geometry (Quad::createGraident +
-        formIntegralFactor; FP64 on the GPU when preloop = "gpu")."""
+        formIntegralFactor; FP64 on the GPU when preloop = "gpu").  Nothing here depends on
+        Nr, so a later build of the same simulation (another Nu field) reuses it (copies of
+        the arrays)."""
+        cache = getattr(self, "_geometry_cache", {})
+        if preloop in cache:
+            ex, E, axial_e, co, nodes, geo, ifact, crds, theta, jac = cache[preloop]
+            self.ex, self.R = ex, float(ex.glob.get("radius", 6371e3))
+            return (ex, E, axial_e.copy(), co.copy(), nodes.copy(), geo.copy(), ifact.copy(), crds.copy(),
+                    theta.copy(), tuple(a.copy() for a in jac))
+        res = self._mesh_geometry_compute(preloop)
+        ex, E, axial_e, co, nodes, geo, ifact, crds, theta, jac = res
+        self._geometry_cache = {preloop: (ex, E, axial_e.copy(), co.copy(), nodes.copy(), geo.copy(), ifact.copy(),
+                                          crds.copy(), theta.copy(), tuple(a.copy() for a in jac))}
+        return res
+
+    def _mesh_geometry_compute(self, preloop):
         par = self.par
         ex = Exodus.read(self.input_dir / par.get("MODEL_1D_EXODUS_MESH_FILE"))
         self.ex = ex
