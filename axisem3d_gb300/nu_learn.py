@@ -138,14 +138,15 @@ def calibrate_shift(vals, net, nu_full, steps, target, log=print, preloop="gpu")
     """The smallest encoded-space shift of the predictions whose runs reproduce every
     validation model's full-Nu seismograms within `target` relative L2 (calibration by
     simulation on models the network was not fitted on); vals = [(sim, features, full-Nu
-    seismograms)].  Returns (shift, largest validation misfit); (1.0, 0.0), i.e. full Nu,
+    seismograms, clock of the full-Nu run)].  Returns (shift, largest validation misfit);
+    (1.0, 0.0), i.e. full Nu,
     if no shift qualifies."""
-    ys = [net.forward(x).cpu().numpy() for _, x, _ in vals]
+    ys = [net.forward(x).cpu().numpy() for _, x, _, _ in vals]
     for sh in SHIFTS:
         worst = 0.0
-        for (sim, _, seis_full), y in zip(vals, ys):
+        for (sim, _, seis_full, clk), y in zip(vals, ys):
             spec = sim.build(nu_elem=decode(y, nu_full, sh), preloop=preloop)
-            seis, _, _, upd = run(spec, steps)
+            seis, _, _, upd = run(spec, steps, clk=clk)
             mis = float(np.linalg.norm(seis - seis_full) / np.linalg.norm(seis_full))
             log(f"calibration shift {sh:.2f}: misfit {mis:.4g}, updates/step {upd}")
             worst = max(worst, mis)
@@ -156,13 +157,23 @@ def calibrate_shift(vals, net, nu_full, steps, target, log=print, preloop="gpu")
     return 1.0, 0.0
 
 
-def run(spec, steps, learn=None):
+def clock(spec):
+    """A run's time step and source time function, to impose on another run of the same model."""
+    return float(spec.dt), np.array(spec.stf, copy=True)
+
+
+def run(spec, steps, learn=None, clk=None):
     """Loop time of one GPU run (first step to seismograms on the host; the pre-loop and
     any network inference are timed by the caller and added for time-to-seismogram).
-    learn = (interval, epsilon) turns the wisdom learner on.  Returns (seis, seconds,
-    wisdom or None, unique-point updates per step)."""
+    learn = (interval, epsilon) turns the wisdom learner on.  clk = clock(other spec) runs
+    on that run's time step: the step of Quad::getDeltaT follows the largest velocity on
+    each element's Nr slices, so runs of one model at different Nu fields differ in dt by
+    up to ~1 %, and seismograms are compared sample by sample on one time axis (the
+    full-Nu run's).  Returns (seis, seconds, wisdom or None, unique-point updates per step)."""
     import torch
     from .capi import Ax3dDomain
+    if clk is not None:
+        spec.dt, spec.stf = clk[0], clk[1].copy()
     dom = Ax3dDomain(spec)
     if learn:
         dom.set_wisdom_learning(int(learn[0]), float(learn[1]))
@@ -213,12 +224,12 @@ def held_out(net, shift, work, n_test=16, nu_full=64, steps=600, eps=1e-3, inter
         t0 = time.perf_counter()
         spec_l = sim_l.build(nu_elem=nu_e, preloop=preloop)
         pre_l = time.perf_counter() - t0
-        seis_l, t_l, _, upd_l = run(spec_l, steps)
+        seis_l, t_l, _, upd_l = run(spec_l, steps, clk=clock(spec_f))
         mis = float(np.linalg.norm(seis_l - seis_f) / np.linalg.norm(seis_f))
         # the reference's route without a network: reuse the wisdom of this model's own
         # full run (which must be paid first)
         spec_w = sim.build(nu_elem=np.maximum(element_labels(spec_f, wis), 1), preloop=preloop)
-        seis_w, t_w, _, upd_w = run(spec_w, steps)
+        seis_w, t_w, _, upd_w = run(spec_w, steps, clk=clock(spec_f))
         mis_w = float(np.linalg.norm(seis_w - seis_f) / np.linalg.norm(seis_f))
         tts_f = pre_f + t_f
         tts_l = t_feat + t_inf + pre_l + t_l
@@ -237,6 +248,11 @@ def held_out(net, shift, work, n_test=16, nu_full=64, steps=600, eps=1e-3, inter
             (Path(out) / "tests_partial.json").write_text(json.dumps(tests, indent=1))
     # all held-out learned-Nu runs batched into one domain
     from . import ensemble
+    # one time axis for the batch (the members share it when their full-Nu runs do)
+    clk_b = min((clock(sp) for sp in specs_l), key=lambda c: c[0])
+    pinned = any(abs(sp.dt - clk_b[0]) > 1e-12 * clk_b[0] for sp in specs_l)
+    for sp in specs_l:
+        sp.dt, sp.stf = clk_b[0], clk_b[1].copy()
     big, info = ensemble.concat(specs_l)
     seis_b, t_b, _, upd_b = run(big, steps)
     parts = ensemble.split_seismograms(seis_b, info)
@@ -253,7 +269,7 @@ def held_out(net, shift, work, n_test=16, nu_full=64, steps=600, eps=1e-3, inter
         tts_batched_learned_seconds=tts_batched, tts_sequential_full_seconds=tts_full_sum,
         tts_learned_batched_vs_sequential_full=tts_full_sum / tts_batched,
         batched_vs_sequential_learned=sum(t["t_learned"] for t in tests) / t_b,
-        batched_split_misfit_max=mis_b)
+        batched_split_misfit_max=mis_b, batched_dt_pinned=pinned)
 
 
 def experiment(work, n_train=64, n_test=16, nu_full=64, steps=600, epochs=200, batch=4096, lr=2e-3,
@@ -280,7 +296,7 @@ def experiment(work, n_train=64, n_test=16, nu_full=64, steps=600, epochs=200, b
         y = encode(np.minimum(element_labels(spec, wis), nu_full), nu_full)
         log(f"train {i}: {t:.2f} s, mean label Nu {np.mean(element_labels(spec, wis)):.1f}")
         if i >= n_train - n_val and n_train > n_val:
-            vals.append((sim, x, seis))  # held out of the fit: calibrates the shift
+            vals.append((sim, x, seis, clock(spec)))  # held out of the fit: calibrates the shift
         else:
             X.append(x)
             Y.append(y)
