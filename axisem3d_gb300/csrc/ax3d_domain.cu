@@ -988,8 +988,9 @@ struct ax3d_domain {
         for (double ratio : {1.06, 1.12, 1.25})
             for (int policy : {0, 1, 2})
                 for (int nside : {1, (int)NSIDE}) cands.push_back(Schedule{ratio, policy, nside, 0});
-        for (int policy : {0, 2})
+        for (int policy : {0, 2, 3})
             for (int nside : {1, (int)NSIDE}) cands.push_back(Schedule{1.12, policy, nside, 1});
+        for (int nside : {1, (int)NSIDE}) cands.push_back(Schedule{1.12, 3, nside, 0});
         for (const Schedule &sc : cands) {
                 {
                     build_buckets(sc, stream);
@@ -1654,8 +1655,8 @@ int ax3d_enable_timers(ax3d_domain *d, int32_t enable) {
 int ax3d_set_schedule(ax3d_domain *d, double ratio, int32_t policy, int32_t nside, int32_t merge) {
     return guard([&] {
         if (!d) throw Error(AX3D_ERR_ARG, "ax3d_set_schedule || null domain");
-        if (!(ratio > 1.0 && ratio < 4.0) || policy < 0 || policy > 2 || nside < 1)
-            throw Error(AX3D_ERR_ARG, "ax3d_set_schedule || ratio in (1, 4), policy 0..2, nside >= 1");
+        if (!(ratio > 1.0 && ratio < 4.0) || policy < 0 || policy > 3 || nside < 1)
+            throw Error(AX3D_ERR_ARG, "ax3d_set_schedule || ratio in (1, 4), policy 0..3, nside >= 1");
         d->need_final();
         CK(cudaSetDevice(d->device));
         ax3d_domain::Schedule sc;

@@ -52,6 +52,7 @@ constexpr int RESEED = 8;    // direct DFT: exact twiddle reload interval
 constexpr int DIRECT_MAX = 257;  // largest prime handled by a direct pass
 constexpr size_t SMEM_CAP = 227 * 1024;
 constexpr size_t SMEM_TWO = 112 * 1024;  // two CTAs per SM
+constexpr size_t SMEM_FOUR = 56 * 1024;  // four CTAs per SM
 constexpr int64_t PREFETCH_MAX = 1024 * 1024;  // largest per-element block asked of L2 ahead
 constexpr int CLUSTER_MAX = 8;
 constexpr int PLAN_BYTES = (sizeof(FftPlan) + 15) / 16 * 16;
@@ -982,7 +983,7 @@ __device__ __noinline__ void phase_quad(const ElemTable &T, const PointTable &P,
 // potential-gradient components (2 sequences per point).
 // ------------------------------------------------------------------------------------
 template <bool SOLID, int NTT>
-__global__ void __launch_bounds__(NTT, NTT <= 256 ? 2 : 1)
+__global__ void __launch_bounds__(NTT, NTT == 128 ? 4 : NTT == 256 ? 2 : 1)
     k_elem_phys(const __grid_constant__ ElemTable T, const __grid_constant__ PointTable P,
                 const float2 *__restrict__ u, const int32_t *__restrict__ elems, int count, int Pc, int Lmax,
                 const __grid_constant__ PhysTables X, const __grid_constant__ SLS sls, int overwrite) {
@@ -1274,6 +1275,8 @@ void init_phys_attributes() {
     cudaFuncSetAttribute(k_elem_phys<false, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_CAP);
     cudaFuncSetAttribute(k_elem_phys<true, 2 * NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_CAP);
     cudaFuncSetAttribute(k_elem_phys<false, 2 * NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_CAP);
+    cudaFuncSetAttribute(k_elem_phys<true, NT / 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_CAP);
+    cudaFuncSetAttribute(k_elem_phys<false, NT / 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_CAP);
     cudaFuncSetAttribute(k_prt3_fft<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_CAP);
     cudaFuncSetAttribute(k_prt3_fft<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_CAP);
 }
@@ -1521,10 +1524,24 @@ FftTables build_fft_tables(const std::vector<char> &used) {
 //   Policy 2: as policy 0 while all points fit two CTAs per SM; larger rings take 512-thread
 //             CTAs with the whole shared memory of an SM (16 warps per SM as two 256-thread
 //             CTAs give), in the smallest cluster that fits: no cluster up to ~360 samples.
+//   Policy 3: as policy 2, except that rings whose 25 points fit a quarter of an SM's shared
+//             memory take 128-thread CTAs, four per SM (16 warps per SM over four elements
+//             in flight instead of two: short rings spend most of their time in barriers).
 void size_phys_bucket(PhysBucket &b, bool solid, int policy) {
     const int nsq = solid ? 3 : 2;
     b.npts_chunk = 0;
     b.nt = NT;
+    if (policy == 3) {
+        const size_t sm = phys_smem_bytes(b.L_max, nsq, NPE, NT / 2);
+        if (sm <= SMEM_FOUR) {
+            b.npts_chunk = NPE;
+            b.csize = 1;
+            b.smem = sm;
+            b.nt = NT / 2;
+            return;
+        }
+        policy = 2;
+    }
     if (policy == 2 && phys_smem_bytes(b.L_max, nsq, NPE, NT) > SMEM_TWO) {
         for (int pc = NPE; pc >= 1; pc--) {
             const size_t sm = phys_smem_bytes(b.L_max, nsq, pc, 2 * NT);
@@ -1568,13 +1585,13 @@ cudaLaunchConfig_t phys_config(const PhysBucket &b, cudaLaunchAttribute *at, cud
     cfg.numAttrs = 1;
     return cfg;
 }
-// the instantiation of a bucket: solid or fluid, 256 or 512 threads
+// the instantiation of a bucket: solid or fluid, 128, 256 or 512 threads
 template <typename F>
 void with_kernel(bool solid, int nt, F f) {
     if (solid)
-        nt > NT ? f(k_elem_phys<true, 2 * NT>) : f(k_elem_phys<true, NT>);
+        nt > NT ? f(k_elem_phys<true, 2 * NT>) : nt < NT ? f(k_elem_phys<true, NT / 2>) : f(k_elem_phys<true, NT>);
     else
-        nt > NT ? f(k_elem_phys<false, 2 * NT>) : f(k_elem_phys<false, NT>);
+        nt > NT ? f(k_elem_phys<false, 2 * NT>) : nt < NT ? f(k_elem_phys<false, NT / 2>) : f(k_elem_phys<false, NT>);
 }
 }  // namespace
 
