@@ -142,9 +142,11 @@ struct ax3d_domain {
     // the bucket schedule: geometric step of the transform length between buckets, shared
     // memory policy (0: two CTAs per SM where they fit; 1: one CTA per SM, fewer clusters)
     // and side streams used; set at ax3d_finalize, changed by ax3d_autotune
+    // the bucket schedule without ax3d_autotune / ax3d_set_schedule: policy 3 with merged
+    // launches (the autotuner's choice on the short-ring domains of learned Nu fields)
     struct Schedule {
         double ratio = 1.12;
-        int policy = 0, nside = NSIDE, merge = 0;
+        int policy = 3, nside = NSIDE, merge = 1;
     } sched;
     std::vector<int32_t> phys3_s_list, phys3_f_list;  // physical-space elements
     std::vector<int32_t> lbuf_of_nr;                   // buffer length of each ring size's plan

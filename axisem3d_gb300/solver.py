@@ -384,6 +384,8 @@ class Simulation:
             warnings.warn("MODEL_PLOT_SLICES_NUM > 0: slice plots (SlicePlot) are not written by this solver")
         e3d = np.zeros(E, bool)
         props3 = {}
+        rho_var, vp_var = np.zeros(E, bool), np.zeros(E, bool)
+        rho_first, vp_first, vp_max3 = rho.copy(), vp.copy(), vp.max(1)
         if models:
             # GPU: each Gaussian-random model sampled on every element's slices in one call,
             # elements ordered by Nr so that each group's block is contiguous
@@ -402,14 +404,22 @@ class Simulation:
                                                 gpu=preloop == "gpu",
                                                 presampled={i: v[bounds[gi]:bounds[gi + 1]].reshape(len(sel), int(nr), 25)
                                                             for i, v in pre.items()})
-                for j in np.nonzero(touched)[0]:
-                    if self.phi2d is not None:
-                        # 2-D mode: every slice sees the model at phi2D, so the element stays
-                        # 1-D with the first row (isSolidPar1D, XMath::structuredUseFirstRow)
-                        vp[sel[j]], vs[sel[j]], rho[sel[j]] = cur["VP"][j, 0], cur["VS"][j, 0], cur["RHO"][j, 0]
-                        continue
-                    e3d[sel[j]] = True
-                    props3[sel[j]] = {k: v[j] for k, v in cur.items()}
+                tj = np.nonzero(touched)[0]
+                if self.phi2d is not None:
+                    # 2-D mode: every slice sees the model at phi2D, so the element stays
+                    # 1-D with the first row (isSolidPar1D, XMath::structuredUseFirstRow)
+                    vp[sel[tj]], vs[sel[tj]], rho[sel[tj]] = cur["VP"][tj, 0], cur["VS"][tj, 0], cur["RHO"][tj, 0]
+                    continue
+                e3d[sel[tj]] = True
+                # per element, for the mass and the time step below: whether rho (vp) varies
+                # over the slices, the first slice, and the largest Vp of the element
+                g3 = {k: v[tj] for k, v in cur.items()}
+                rho_var[sel[tj]] = (g3["RHO"].max(1) != g3["RHO"].min(1)).any(1)
+                vp_var[sel[tj]] = (g3["VP"].max(1) != g3["VP"].min(1)).any(1)
+                rho_first[sel[tj]], vp_first[sel[tj]] = g3["RHO"][:, 0], g3["VP"][:, 0]
+                vp_max3[sel[tj]] = g3["VP"].max((1, 2))
+                for jj, j in enumerate(tj):
+                    props3[sel[j]] = {k: v[jj] for k, v in g3.items()}
         # particle relabelling from the geometric models (Quad::addGeometric3D, Quad.cpp:249-255;
         # Relabelling::addUndulation): the elements with a nonzero undulation
         gmodels = RL.geometric_models(par, self._cmt_latlon(), self.R)
@@ -447,15 +457,16 @@ class Simulation:
         # elements whose mass varies with phi (3-D rho, or 3-D vp in a fluid); the others
         # add a constant; 3-D masses are resampled onto each point's own Nr
         # (Material.cpp:215-224, XMath::linearResampling)
-        m3e = [e for e in np.nonzero(e3d)[0] if e not in relab and (np.ptp(props3[e]["RHO"], 0).any()
-               or (fl[e] and np.ptp(props3[e]["VP"], 0).any()))]
+        not_relab = np.ones(E, bool)
+        not_relab[list(relab)] = False
+        rho_first[~e3d], vp_first[~e3d] = rho[~e3d], vp[~e3d]  # 1-D elements (2-D mode: the model at phi2D)
+        m3e = np.nonzero(e3d & not_relab & (rho_var | (fl & vp_var)))[0].tolist()
         m1 = np.ones(E, bool)
         m1[m3e] = False
         m1[list(relab)] = False
         ms = np.zeros(P)
         mf = np.zeros(P)
-        rho0 = np.array([props3[e]["RHO"][0] if e3d[e] else rho[e] for e in range(E)])
-        vp0 = np.array([props3[e]["VP"][0] if e3d[e] else vp[e] for e in range(E)])
+        rho0, vp0 = rho_first, vp_first
         sm, fm = m1 & ~fl, m1 & fl
         if preloop == "gpu":  # Material::computeElementalMass on the GPU (FP64), then assembled
             from . import preloop as PL
@@ -548,12 +559,13 @@ class Simulation:
         # and vmax = the largest P velocity of each slice after the 3-D models
         # (Material::getVMax, Material.cpp:521-537); the element's dt is the smallest
         dt_e = ex.dt.astype(float).copy()
-        for e in set(np.nonzero(e3d)[0].tolist()) | set(relab):
+        plain3 = e3d & not_relab  # the smallest ratio over the slices: 1-D vmax / the slice's largest vmax
+        dt_e[plain3] *= vp.max(1)[plain3] / vp_max3[plain3]
+        for e in relab:
             ratio = np.ones(int(e_nr[e]))
             if e3d[e]:
                 ratio = ratio * (vp[e].max() / props3[e]["VP"].max(1))
-            if e in relab:
-                ratio = ratio * (relab[e].hmin_slices() / relab[e].hmin_ref())
+            ratio = ratio * (relab[e].hmin_slices() / relab[e].hmin_ref())
             dt_e[e] *= float(ratio.min())
         dt = dt_user if dt_user > 0 else float(dt_e.min()) * par.get("TIME_DELTA_T_FACTOR", float)
         self.dt = dt
