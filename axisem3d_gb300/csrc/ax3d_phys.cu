@@ -371,35 +371,6 @@ __device__ __noinline__ void direct_pass(float2 *buf, int S, int ns, int L, int 
     }
 }
 
-// A direct pass of prime R: GS lanes x KL outputs cover its (R - 1) / 2 output pairs; SG
-// (sequences per group) trades twiddle reuse against the number of groups that keep the
-// CTA's threads busy: the cheapest of SG = 1, 2, 4 by rounds x steps x instructions per step.
-template <int GS, int KL>
-__device__ void direct_sg(float2 *buf, int S, int ns, int L, int Ls, int R, const float2 *tw, int sg, bool dit,
-                          const Grp g) {
-    const int groups = L / R;  // butterflies of the pass per sequence
-    int best = 4;
-    int64_t bcost = INT64_MAX;
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-        const int SGc = 1 << c;
-        const int64_t lanes = (int64_t)groups * ((ns + SGc - 1) / SGc) * GS;
-        const int64_t rounds = (lanes + g.n - 1) / g.n;
-        const int64_t cost = rounds * (4 * SGc + 4 * KL * SGc + 4 * KL);
-        if (cost < bcost) {
-            bcost = cost;
-            best = SGc;
-        }
-    }
-    if constexpr (KL >= 4) best = best > 2 ? 2 : best;  // four sequences x four outputs spill
-    if (best == 1)
-        direct_pass<GS, KL, 1>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
-    else if (best == 2 || KL >= 4)
-        direct_pass<GS, KL, 2>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
-    else
-        direct_pass<GS, KL, 4>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
-}
-
 __device__ void run_pass(int R, float2 *buf, int S, int ns, int L, int Ls, const float2 *tw, int sg, bool dit,
                          const Grp g) {
     switch (R) {
@@ -412,26 +383,21 @@ __device__ void run_pass(int R, float2 *buf, int S, int ns, int L, int Ls, const
         case 13: rad_pass<13>(buf, S, ns, L, Ls, tw, sg, dit, g); break;
         default: {
             // the narrowest group whose lanes cover the H = (R - 1) / 2 output pairs with at
-            // most three outputs each (four for R above 193)
+            // most three outputs each (four for R above 193), two sequences per group: five
+            // instantiations in all, so that CTAs of different rings on one SM share little
+            // instruction cache (measured: 4.9 % faster on rings up to 91 samples than a
+            // cost-model choice among 26 instantiations, 0.8 % on the full Nu 8-256 mix)
             const int H = (R - 1) / 2;
-            if (H <= 8)
-                direct_sg<4, 2>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
-            else if (H <= 12)
-                direct_sg<4, 3>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
-            else if (H <= 16)
-                direct_sg<8, 2>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
+            if (H <= 12)
+                direct_pass<4, 3, 2>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
             else if (H <= 24)
-                direct_sg<8, 3>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
-            else if (H <= 32)
-                direct_sg<16, 2>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
+                direct_pass<8, 3, 2>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
             else if (H <= 48)
-                direct_sg<16, 3>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
-            else if (H <= 64)
-                direct_sg<32, 2>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
+                direct_pass<16, 3, 2>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
             else if (H <= 96)
-                direct_sg<32, 3>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
+                direct_pass<32, 3, 2>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
             else
-                direct_sg<32, 4>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
+                direct_pass<32, 4, 2>(buf, S, ns, L, Ls, R, tw, sg, dit, g);
         }
     }
 }
