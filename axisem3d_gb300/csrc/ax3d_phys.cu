@@ -163,8 +163,9 @@ __device__ __noinline__ void rad_pass(float2 *buf, int S, int ns, int L, int Ls,
             sq[qk] = w.y;
         }
     }
-    // U butterflies per iteration, their shared-memory loads issued together
-    constexpr int U = R <= 4 ? 4 : R <= 5 ? 2 : 1;
+    // U butterflies per iteration, their shared-memory loads issued together (two for the
+    // radices up to 5: four measured 0.4-3 % slower, the larger body costing instruction cache)
+    constexpr int U = R <= 5 ? 2 : 1;
     const int64_t rs = (int64_t)m * S;
     for (int t0 = g.tid; t0 < total; t0 += g.n * U) {
         float2 v[U][R];
