@@ -6,7 +6,8 @@ library exists here, so this module implements the classic file format from its 
 specification: header (magic, numrecs, dimension list, global attributes, variable list
 with begin offsets) followed by big-endian, 4-byte-padded data.  Only fixed-size (non
 record) variables are written; the reader also accepts record variables of one record.
-NetCDF-4/HDF5 files (magic "\\x89HDF") are rejected with a clear error.
+NetCDF-4 / HDF5 files (magic "\\x89HDF", the format of AxiSEM3D's own meshes) go to the
+HDF5 reader of `hdf5.py`.
 """
 from __future__ import annotations
 
@@ -192,7 +193,8 @@ def read(path) -> Dataset:
     with open(path, "rb") as f:
         buf = f.read()
     if buf[:4] == b"\x89HDF":
-        raise ValueError(f"{path}: NetCDF-4/HDF5 file; only NetCDF classic (CDF-1/2) is supported")
+        from . import hdf5
+        return hdf5.read(path)
     if buf[:3] != b"CDF" or buf[3] not in (1, 2):
         raise ValueError(f"{path}: not a NetCDF classic file")
     version = buf[3]

@@ -21,7 +21,7 @@ from . import geometry as GEO
 from . import netcdf as NC
 from . import relabelling as RL
 from . import spectral as S
-from .spec import (ATT_CG4, ATT_FULL, ATT_NONE, MAT_ACOUSTIC, MAT_ISO, POINT_FLUID, POINT_SOLID,
+from .spec import (ATT_CG4, ATT_FULL, ATT_NONE, MAT_ACOUSTIC, MAT_ISO, MAT_TISO, POINT_FLUID, POINT_SOLID,
                    POINT_SOLID_FLUID, DomainSpec)
 
 # the parameter registry (Parameters::registerAll, Parameters.cpp:23-100)
@@ -84,6 +84,7 @@ class Exodus:
     nodal: dict             # name -> [E, 4]
     side: dict              # side-set name -> [E] side (-1 none)
     glob: dict              # global variables
+    isotropic: bool = True  # VP_0 / VS_0 (isotropic) or VPV_0 ... ETA_0 (TI) variables
 
     @staticmethod
     def read(path):
@@ -101,14 +102,40 @@ class Exodus:
         enames = d.strings("name_elem_var")
         ev = {nm: np.asarray(d[f"vals_elem_var{i + 1}eb1"], float).ravel() for i, nm in enumerate(enames)}
         nodal = {}
-        for base in ("VP", "VS", "RHO", "QMU", "QKAPPA"):
+        for base in ("VP", "VS", "VPV", "VPH", "VSV", "VSH", "ETA", "RHO", "QMU", "QKAPPA"):
             if f"{base}_0" in ev:
                 nodal[base] = np.stack([ev[f"{base}_{k}"] for k in range(4)], 1)
+        # ExodusModel::isIsotropic (ExodusModel.cpp:575-578) and Material::Material
+        # (Material.cpp:36-50): isotropic meshes give vpv = vph = VP, vsv = vsh = VS, eta = 1;
+        # "vp" / "vs" of a TI mesh are vpv / vsv (Material::getProperty)
+        iso = "VP" in nodal
+        if iso:
+            nodal["VPV"] = nodal["VPH"] = nodal["VP"]
+            nodal["VSV"] = nodal["VSH"] = nodal["VS"]
+            nodal["ETA"] = np.ones_like(nodal["VP"])
+        else:
+            nodal["VP"], nodal["VS"] = nodal["VPV"], nodal["VSV"]
+        # ExodusModel::formAuxiliary (ExodusModel.cpp:378-404): the nodes of an axial element
+        # are rotated so that side 3 lies on the axis (side set "t1" names the axis when present)
+        axis = side.get("t1", side.get("t0"))
+        if axis is not None:
+            for e in np.nonzero((axis >= 0) & (axis != 3))[0]:
+                a = int(axis[e])
+                perm = [(j + a - 3) % 4 for j in range(4)]
+                conn[e] = conn[e][perm]
+                for v in {id(v): v for v in nodal.values()}.values():  # aliases rotate once
+                    v[e] = v[e][perm]
+                for v in side.values():
+                    if v[e] != -1:
+                        v[e] = (v[e] - a + 3) % 4
+            if "t1" in side:
+                side["t0"] = side["t1"]
         info = d.strings("info_records")
         if not any("spherical" in s for s in info):
             raise ValueError("Exodus || only crdsys = spherical meshes are supported")
         return Exodus(np.stack([d["coordx"], d["coordy"]], 1).astype(float), conn,
-                      ev["element_type"].astype(int), ev["fluid"] > 0.5, ev.get("dt", np.zeros(E)), nodal, side, glob)
+                      ev["element_type"].astype(int), ev["fluid"] > 0.5, ev.get("dt", np.zeros(E)), nodal, side, glob,
+                      iso)
 
 
 def _int_or(par, key, default):
@@ -268,12 +295,27 @@ class Simulation:
         axial_e = ex.side.get("t0", np.full(E, -1)) >= 0
         if (ex.side["t0"][axial_e] != 3).any():
             raise ValueError("Quad::Quad || Axial side must be 3.")
+        # the curved side of each spherical / semi-spherical element (Quad::Quad, Quad.cpp:51-87)
+        # with the mesh's distance tolerance (shortest element side / 1000, ExodusModel.cpp:70-86)
         r = np.hypot(ex.nodes[ex.conn][..., 0], ex.nodes[ex.conn][..., 1])
+        xy = ex.nodes[ex.conn]
+        tol = float(np.hypot(*(xy - np.roll(xy, -1, axis=1)).transpose(2, 0, 1)).min()) / 1000.0
+        r0, r1, r2, r3 = r[:, 0], r[:, 1], r[:, 2], r[:, 3]
         co = np.full(E, -1)
-        sph = ex.etype == 0
-        co[sph] = np.where(r[sph, 2] > r[sph, 0] + 1e-6, 2, 0)
-        semi = ex.etype == 2
-        co[semi] = np.where(np.abs(r[semi, 2] - r[semi, 3]) < 1e-3 * self.R, 2, 0)
+        sph, semi = ex.etype == 0, ex.etype == 2
+        a02 = (np.abs(r0 - r1) < tol) & (np.abs(r2 - r3) < tol)
+        a13 = (np.abs(r1 - r2) < tol) & (np.abs(r3 - r0) < tol)
+        co = np.where(sph & a02, np.where(r2 > r0, 2, 0), co)
+        co = np.where(sph & ~a02 & a13, np.where(r3 > r1, 3, 1), co)
+        if (sph & ~a02 & ~a13).any():
+            raise ValueError("Quad::Quad || Invalid spherical element shape.")
+        c_semi = np.select([(np.abs(r0 - r1) < tol) & (r0 > r2), (np.abs(r1 - r2) < tol) & (r1 > r3),
+                            (np.abs(r2 - r3) < tol) & (r2 > r0), (np.abs(r3 - r0) < tol) & (r3 > r1)], [0, 1, 2, 3], -1)
+        co = np.where(semi, c_semi, co)
+        if (semi & (c_semi < 0)).any():
+            raise ValueError("Quad::Quad || Invalid semi-spherical element shape.")
+        if (axial_e & (ex.etype != 1) & ((3 + co) % 2 == 0)).any():
+            raise ValueError("Quad::Quad || Conflict in axial setting.")
         nodes = np.transpose(ex.nodes[ex.conn], (0, 2, 1))
         if preloop == "gpu":
             # Quad::createGraident + formIntegralFactor on the GPU (FP64)
@@ -423,6 +465,10 @@ class Simulation:
         # particle relabelling from the geometric models (Quad::addGeometric3D, Quad.cpp:249-255;
         # Relabelling::addUndulation): the elements with a nonzero undulation
         gmodels = RL.geometric_models(par, self._cmt_latlon(), self.R)
+        ti_mesh = not ex.isotropic
+        if ti_mesh and (models or gmodels):
+            raise NotImplementedError("Material::addVolumetric3D / Relabelling || 3-D models on a transversely "
+                                      "isotropic mesh are not built here; use no 3-D models or an isotropic mesh")
         relab = {}
         if gmodels:
             # element centre radius (Quad::computeCenterRadius: mapping at xi = eta = 0)
@@ -580,9 +626,10 @@ class Simulation:
             alpha, beta, gamma, _, _ = ATT.att_factors(w, y, fmin, fmax, fref, dt, np.ones(1), np.ones(1), dokappa)
             attk = ATT_CG4 if cg4 else ATT_FULL
         e_mod, e_attm, e_mat, e_att = [], [], [], []
-        gpu_mod = self._moduli_gpu(E, fl, e3d, props3, vp, vs, rho, ifact, mat, attk,
-                                   (w, y, fmin, fmax, fref) if attk != ATT_NONE else None,
-                                   dokappa, jstiff) if preloop == "gpu" else None
+        fit = (w, y, fmin, fmax, fref) if attk != ATT_NONE else None
+        ti_mod = self._moduli_ti(fl, mat, ifact, attk, fit, dokappa, cg4, dt, preloop) if ti_mesh else None
+        gpu_mod = self._moduli_gpu(E, fl, e3d, props3, vp, vs, rho, ifact, mat, attk, fit,
+                                   dokappa, jstiff) if preloop == "gpu" and not ti_mesh else None
         for e in range(E):
             f = ifact[e]
             # (nr, 25) for 3-D elements, (1, 25) for 1-D ones
@@ -593,6 +640,13 @@ class Simulation:
                 e_attm.append(np.zeros(0))
                 e_mat.append(MAT_ACOUSTIC)
                 e_att.append(ATT_NONE)
+                continue
+            if ti_mod is not None:
+                mod_e, attm_e, iso_e = ti_mod[e]
+                e_mod.append(mod_e)
+                e_attm.append(attm_e)
+                e_mat.append(MAT_ISO if iso_e else MAT_TISO)
+                e_att.append(attk)
                 continue
             if gpu_mod is not None:
                 e_mod.append(gpu_mod[e][0])
@@ -708,6 +762,60 @@ class Simulation:
         return spec
 
     # ------------------------------------------------------------------ source
+    @staticmethod
+    def _moduli_ti(fl, mat, ifact, attk, fit, dokappa, cg4, dt, preloop):
+        """Material::createElastic (Material.cpp:280-379) for the 1-D solid elements of a
+        transversely isotropic mesh: A = rho vph^2, C = rho vpv^2, L = rho vsv^2, N = rho vsh^2
+        (times iFact), F = eta (A - 2 L), the attenuation split on their Voigt average; an
+        element with vpv = vph, vsv = vsh and eta = 1 (Material::isIsotropic, tolerance
+        tinyDouble = 1e-10) keeps F, L as Isotropic1D.  FP64 on the GPU (preloop = "gpu",
+        ax3d_precompute_elastic) or numpy.  {element: (moduli, attenuation moduli, isotropic)}."""
+        solid = np.nonzero(~fl)[0]
+        g = {k: mat[k][solid] for k in ("VPV", "VPH", "VSV", "VSH", "ETA", "RHO")}
+        nrm = lambda a: np.sqrt((a * a).sum(1))
+        iso = ((nrm(g["VPV"] - g["VPH"]) < 1e-10 * nrm(g["VPV"])) & (nrm(g["VSV"] - g["VSH"]) < 1e-10 * nrm(g["VSV"]))
+               & (nrm(g["ETA"] - 1.0) < 1e-10))
+        npa = 4 if attk == ATT_CG4 else 25
+        f = ifact[solid]
+        if preloop == "gpu":
+            from . import preloop as PL
+            model = {k.lower(): [v[i][None, :] for i in range(len(solid))] for k, v in g.items()}
+            if attk != ATT_NONE:
+                model["qkappa"] = [mat["QKAPPA"][e][None, :] for e in solid]
+                model["qmu"] = [mat["QMU"][e][None, :] for e in solid]
+            sls = PL.SLSFit(*fit, do_kappa=dokappa) if fit else None
+            mod, att = PL.moduli_gpu(np.ones(len(solid), np.int32), f, model, isotropic=False, att=attk, sls=sls)
+            mod = mod.reshape(len(solid), 5, 25)
+            att = att.reshape(len(solid), -1) if attk != ATT_NONE else np.zeros((len(solid), 0), np.float32)
+        else:
+            A = g["RHO"] * g["VPH"] ** 2 * f
+            C = g["RHO"] * g["VPV"] ** 2 * f
+            L = g["RHO"] * g["VSV"] ** 2 * f
+            N = g["RHO"] * g["VSH"] ** 2 * f
+            F = g["ETA"] * (A - 2 * L)
+            att = np.zeros((len(solid), 2 * npa if attk != ATT_NONE else 0))
+            if attk != ATT_NONE:
+                w, y, fmin, fmax, fref = fit
+                kappa, mu = ATT.voigt_ti(A, C, F, L, N)
+                for i, e in enumerate(solid):
+                    qk, qm = mat["QKAPPA"][e][None, :], mat["QMU"][e][None, :]
+                    fac = ATT.att_factors(w, y, fmin, fmax, fref, dt, qk, qm, dokappa)
+                    k2, m2, dk, dm = ATT.apply_attenuation(kappa[i][None, :], mu[i][None, :], qk, qm, f[i], cg4,
+                                                           (fac[3], fac[4]))
+                    dkap, dmu = k2[0] - kappa[i], m2[0] - mu[i]
+                    A[i] += dkap + 4.0 / 3.0 * dmu
+                    C[i] += dkap + 4.0 / 3.0 * dmu
+                    F[i] += dkap - 2.0 / 3.0 * dmu
+                    L[i] += dmu
+                    N[i] += dmu
+                    att[i] = np.concatenate([dk.ravel(), dm.ravel()])
+            mod = np.stack([A, C, F, L, N], 1).astype(np.float32)
+            att = att.astype(np.float32)
+        out = {}
+        for i, e in enumerate(solid):
+            out[e] = ((mod[i, 2:4] if iso[i] else mod[i]).ravel(), att[i], bool(iso[i]))
+        return out
+
     def _moduli_gpu(self, E, fl, e3d, props3, vp, vs, rho, ifact, mat, attk, fit, dokappa, jstiff=None):
         """Isotropic solid moduli of every solid element in one ax3d_precompute_elastic call;
         returns {element: (moduli [2][rows][25], attenuation moduli)}.  jstiff: relabelled

@@ -32,10 +32,98 @@ def test_netcdf_roundtrip(tmp_path):
     assert (tmp_path / "x.nc").read_bytes()[:4] == b"CDF\x02"
 
 
-def test_netcdf_rejects_hdf5(tmp_path):
+def test_netcdf_bad_hdf5_raises(tmp_path):
+    """NetCDF-4 / HDF5 files go to the HDF5 reader, which names what it cannot read."""
     (tmp_path / "h.e").write_bytes(b"\x89HDF\r\n\x1a\n" + b"\0" * 64)
     with pytest.raises(ValueError, match="HDF5"):
         NC.read(tmp_path / "h.e")
+    (tmp_path / "g.e").write_bytes(b"\x89HDF\r\n\x1a\n\x02" + b"\0" * 64)
+    with pytest.raises(ValueError, match="superblock version 2"):
+        NC.read(tmp_path / "g.e")
+
+
+def _spec_arrays_equal(a, b):
+    return [k for k, v in vars(a).items() if isinstance(v, np.ndarray)
+            and (v.shape != getattr(b, k).shape or not np.array_equal(v, getattr(b, k)))]
+
+
+def test_rotated_axial_elements_read_back(tmp_path):
+    """A mesh whose axial elements store the axis on side 0, 1 or 2 (ExodusModel::
+    formAuxiliary rotates them to side 3, with their side sets and nodal values) gives the
+    same domain as the mesh written with the axis on side 3."""
+    specs = []
+    for i, rot in enumerate((False, True)):
+        d = solver.write_inputs(tmp_path / f"r{i}", mesh_kw=dict(SMALL_MESH, rotate_axis=rot), steps=10, nu=3,
+                                attenuation=True)
+        specs.append(solver.Simulation(d).build())
+    ds = NC.read(tmp_path / "r1" / "mesh.e")
+    axis = np.asarray(ds["side_ss1"]) - 1
+    assert set(axis.tolist()) == {0, 1, 2}
+    assert _spec_arrays_equal(specs[0], specs[1]) == []
+
+
+def test_transversely_isotropic_mesh(tmp_path):
+    """A mesh with VPV / VPH / VSV / VSH / ETA (Material::Material, Material::createElastic):
+    TransverselyIsotropic1D moduli A = rho vph^2, C = rho vpv^2, L = rho vsv^2, N = rho vsh^2
+    (times iFact), F = eta (A - 2 L) where the mesh is anisotropic, Isotropic1D elsewhere with
+    the moduli of the isotropic mesh; 3-D models on it are refused."""
+    from axisem3d_gb300.spec import MAT_ISO, MAT_TISO
+    specs, sims = [], []
+    for i, ti in enumerate((False, True)):
+        d = solver.write_inputs(tmp_path / f"t{i}", mesh_kw=dict(SMALL_MESH, ti=ti), steps=10, nu=3)
+        sims.append(solver.Simulation(d))
+        specs.append(sims[-1].build())
+    a, b = specs
+    assert (b.e_mat == MAT_TISO).sum() > 0 and (a.e_mat == MAT_TISO).sum() == 0
+    ends = lambda sp: np.append(sp.e_mofs[1:], len(sp.e_mod))
+    m = sims[1]._gll_material(sims[1].ex, sims[1].axial_e)
+    for e in range(b.n_elements):
+        mb = b.e_mod[b.e_mofs[e]:ends(b)[e]]
+        if b.e_mat[e] == MAT_TISO:
+            rho, vpv, vph, vsv, vsh, eta = (m[k][e] for k in ("RHO", "VPV", "VPH", "VSV", "VSH", "ETA"))
+            A, C, L, N = rho * vph ** 2, rho * vpv ** 2, rho * vsv ** 2, rho * vsh ** 2
+            ratio = mb.reshape(5, 25) / np.stack([A, C, eta * (A - 2 * L), L, N])  # = iFact at every point
+            np.testing.assert_allclose(ratio, np.broadcast_to(ratio[3], (5, 25)), rtol=1e-5)
+            assert (eta < 1).any() and not np.allclose(vph, vpv)
+        else:
+            np.testing.assert_array_equal(mb, a.e_mod[a.e_mofs[e]:ends(a)[e]])
+    d = solver.write_inputs(tmp_path / "t3", mesh_kw=dict(SMALL_MESH, ti=True), steps=10, nu=3,
+                            models3d=("gaussian_random$VS$Ref1D$0.04$500$200$7",))
+    with pytest.raises(NotImplementedError, match="transversely"):
+        solver.Simulation(d).build()
+
+
+def test_hdf5_mesh_of_the_reference():
+    """The reference's own template mesh (NetCDF-4 / HDF5, PREM anisotropic with one crust,
+    50 s) and template inputs, when AX3D_REFERENCE_INPUT names a copy of that input folder:
+    the mesh reads (chunked, compressed datasets), and the case builds with its TI upper
+    mantle, attenuation and rotated axial elements (ellipticity switched off, not built)."""
+    import os
+    import shutil
+    src = os.environ.get("AX3D_REFERENCE_INPUT")
+    if not src:
+        pytest.skip("AX3D_REFERENCE_INPUT is not set")
+    from pathlib import Path
+    from axisem3d_gb300.spec import MAT_TISO
+    ds = NC.read(Path(src) / "AxiSEM_prem_ani_one_crust_50.e")
+    assert ds["connect1"].shape == (2016, 4) and ds["coordx"].shape == (2115,)
+    assert ds.strings("name_glo_var")[6] == "radius" and float(ds["vals_glo_var"][0, 6]) == 6371e3
+    assert "crdsys = spherical" in ds.strings("info_records")
+    names = ds.strings("name_elem_var")
+    vpv = ds[f"vals_elem_var{names.index('VPV_0') + 1}eb1"]
+    assert abs(float(vpv.max()) - 13716.622269026377) < 1e-6
+    import tempfile
+    d = Path(tempfile.mkdtemp()) / "input"
+    shutil.copytree(src, d)
+    for f in d.iterdir():
+        f.chmod(0o644)
+    p = d / "inparam.model"
+    p.write_text("\n".join("MODEL_3D_ELLIPTICITY_MODE off" if ln.startswith("MODEL_3D_ELLIPTICITY_MODE") else ln
+                           for ln in p.read_text().splitlines()) + "\n")
+    sim = solver.Simulation(d)
+    spec = sim.build()
+    assert spec.n_elements == 2016 and (spec.e_mat == MAT_TISO).sum() == 256
+    assert np.isfinite(spec.e_geo).all() and set(np.unique(sim.co).tolist()) == {-1, 0, 2, 3}
 
 
 def test_parameters_parsing(small_inputs):
@@ -86,6 +174,33 @@ def test_full_solver_gpu_matches_oracle(small_inputs, ax3d_lib):
     from axisem3d_gb300.capi import Ax3dDomain
     sim = solver.Simulation(small_inputs)
     spec = sim.build()
+    g, o = Ax3dDomain(spec), OracleDomain(spec)
+    g.step(200)
+    o.step(200)
+    a, b = g.seismograms(0, 200), o.seismograms(0, 200)
+    assert np.linalg.norm(a - b) <= 1e-5 * np.linalg.norm(b)
+    for which in ("displ", "veloc"):
+        x, y = g.get(which, "solid"), o.get(which, "solid")
+        assert np.linalg.norm(x - y) <= 1e-5 * np.linalg.norm(y)
+
+
+@pytest.mark.gpu
+def test_transversely_isotropic_mesh_gpu_matches_oracle(tmp_path_factory, ax3d_lib):
+    """A transversely isotropic mesh (TI top 220 km of the mantle) with its axial elements
+    stored rotated, attenuation (CG4) on and Nu = 3: the GPU pre-loop's moduli equal the
+    numpy pre-loop's, and 200 steps of GPU seismograms and fields match the oracle."""
+    from oracle.oracle_py import OracleDomain
+    from axisem3d_gb300.capi import Ax3dDomain
+    from axisem3d_gb300.spec import MAT_TISO
+    d = tmp_path_factory.mktemp("ti") / "input"
+    solver.write_inputs(d, mesh_kw=dict(SMALL_MESH, ti=True, rotate_axis=True), steps=200, hdur=20.0,
+                        n_stations=6, seed=3, nu=3, attenuation=True)
+    host = solver.Simulation(d).build(preloop="host")
+    spec = solver.Simulation(d).build(preloop="gpu")
+    assert (spec.e_mat == MAT_TISO).sum() > 0
+    np.testing.assert_array_equal(spec.e_mofs, host.e_mofs)
+    np.testing.assert_allclose(spec.e_mod, host.e_mod, rtol=2e-6, atol=0)
+    np.testing.assert_allclose(spec.e_attm, host.e_attm, rtol=2e-6, atol=1e-30)
     g, o = Ax3dDomain(spec), OracleDomain(spec)
     g.step(200)
     o.step(200)
