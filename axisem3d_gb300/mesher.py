@@ -23,7 +23,6 @@ from __future__ import annotations
 import numpy as np
 
 from . import attenuation as ATT
-from . import geometry as GEO
 from . import netcdf as NC
 
 R_EARTH = 6371e3
@@ -144,13 +143,11 @@ def half_disk(n_theta=96, h_mantle=100e3, h_core=110e3, r_c=1500e3, seed=0, cour
             if abs(r0 - R_CMB) < 1.0 and abs(r1 - R_CMB) < 1.0:
                 sf_e.append(e)
                 sf_s.append(side)
-    # CFL time step per element: courant * (min GLL spacing) / vmax
-    geo, ifact, crds, theta, _ = GEO.batch_geometry(np.transpose(xy[conn], (0, 2, 1)), etype,
-                                                    _curved_side(xy, conn, etype), np.isin(np.arange(E), ax_e))
-    c = crds.reshape(E, 5, 5, 2)
-    d1 = np.hypot(*(c[:, 1:, :] - c[:, :-1, :]).transpose(3, 0, 1, 2)).reshape(E, -1).min(1)
-    d2 = np.hypot(*(c[:, :, 1:] - c[:, :, :-1]).transpose(3, 0, 1, 2)).reshape(E, -1).min(1)
-    dt_e = courant * np.minimum(d1, d2) / vp.max(1)
+    # the element's time step as AxiSEM's mesher writes it: courant * (shortest element side) /
+    # vmax; the solver scales it by the closest GLL distance over that side (Quad::getDeltaT)
+    xy4 = xy[conn]
+    side = np.hypot(*(xy4 - np.roll(xy4, -1, axis=1)).transpose(2, 0, 1)).min(1)
+    dt_e = courant * side / vp.max(1)
     # attenuation: SLS fit and Q per layer
     w, y = ATT.fit_sls(nsls, f_min, f_max)
     qm = np.where(fluid, 1e5, np.where(rcen > R_MOHO, qmu[1], qmu[0]))
@@ -218,17 +215,6 @@ def _rotate_rows(v, rot):
     for e, a in rot.items():
         v[e] = v[e][[(k - a + 3) % 4 for k in range(4)]]
     return v
-
-
-def _curved_side(xy, conn, etype):
-    """Quad's curved-outer side of every element (Quad.cpp:51-88): 2 or 0 here."""
-    r = np.hypot(xy[conn][..., 0], xy[conn][..., 1])
-    co = np.full(len(conn), -1)
-    sph = etype == 0
-    co[sph] = np.where(r[sph, 2] > r[sph, 0], 2, 0)
-    semi = etype == 2
-    co[semi] = np.where(np.abs(r[semi, 2] - r[semi, 3]) < 1.0, 2, 0)
-    return co
 
 
 def write_half_disk(path, **kw):

@@ -604,15 +604,22 @@ class Simulation:
         # courant = dt_ref vmax_ref / hmin_ref, hmin from the deformed element (relabelling)
         # and vmax = the largest P velocity of each slice after the 3-D models
         # (Material::getVMax, Material.cpp:521-537); the element's dt is the smallest
-        dt_e = ex.dt.astype(float).copy()
-        plain3 = e3d & not_relab  # the smallest ratio over the slices: 1-D vmax / the slice's largest vmax
-        dt_e[plain3] *= vp.max(1)[plain3] / vp_max3[plain3]
+        # Quad::getCourant (Quad.cpp:617-628): courant = the mesh's dt x vmax_ref / the shortest
+        # element side, vmax_ref = max(vpv, vph) over the element's nodes (Material::getVMaxRef);
+        # hmin = the closest two GLL points (XMath::findClosestDist), per slice when relabelled
+        xy4 = ex.nodes[ex.conn]
+        hmin_edge = np.hypot(*(xy4 - np.roll(xy4, -1, axis=1)).transpose(2, 0, 1)).min(1)
+        vmax_ref = np.maximum(ex.nodal["VPV"], ex.nodal["VPH"]).max(1)
+        courant = ex.dt.astype(float) * vmax_ref / hmin_edge
+        dd = crds[:, :, None, :] - crds[:, None, :, :]
+        dd = np.hypot(dd[..., 0], dd[..., 1])
+        hmin_gll = np.where(np.eye(25, dtype=bool)[None], np.inf, dd).min((1, 2))
+        vmax_1d = np.maximum(mat["VPV"], mat["VPH"]).max(1)
+        vmax_e = np.where(e3d, vp_max3, vmax_1d)  # the slice maximum: 3-D elements' largest slice
+        dt_e = courant * hmin_gll / vmax_e
         for e in relab:
-            ratio = np.ones(int(e_nr[e]))
-            if e3d[e]:
-                ratio = ratio * (vp[e].max() / props3[e]["VP"].max(1))
-            ratio = ratio * (relab[e].hmin_slices() / relab[e].hmin_ref())
-            dt_e[e] *= float(ratio.min())
+            vm = props3[e]["VP"].max(1) if e3d[e] else np.full(int(e_nr[e]), vmax_1d[e])
+            dt_e[e] = float((courant[e] * relab[e].hmin_slices() / vm).min())
         dt = dt_user if dt_user > 0 else float(dt_e.min()) * par.get("TIME_DELTA_T_FACTOR", float)
         self.dt = dt
         attk = ATT_NONE

@@ -124,6 +124,14 @@ def test_hdf5_mesh_of_the_reference():
     spec = sim.build()
     assert spec.n_elements == 2016 and (spec.e_mat == MAT_TISO).sum() == 256
     assert np.isfinite(spec.e_geo).all() and set(np.unique(sim.co).tolist()) == {-1, 0, 2, 3}
+    # Quad::getDeltaT: the mesh's dt (courant x shortest side / vp, 2.524 s in the crust)
+    # scaled by the closest GLL distance over the shortest side
+    assert abs(spec.dt - 0.43585) < 1e-4 and abs(float(sim.ex.dt.min()) - 2.52414) < 1e-4
+    from oracle.oracle_py import OracleDomain
+    o = OracleDomain(spec)
+    o.step(40)
+    u = o.get("displ", "solid")
+    assert np.isfinite(u).all() and 1e-4 < np.abs(u).max() < 1.0
 
 
 def test_parameters_parsing(small_inputs):
