@@ -224,7 +224,7 @@ def allmax(world, x):
 # pass; its traffic grows in proportion to the elements processed, so it is this ratio
 # times its algorithmic bytes.  Re-measured whenever the element kernel or the schedule
 # changes (this figure: schedule policy 3 with merged launches, the autotuner's pick).
-TRAFFIC_PER_ALGO_BYTE = 1.025
+TRAFFIC_PER_ALGO_BYTE = 1.034
 
 
 def peaks():
