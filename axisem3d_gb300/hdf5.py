@@ -7,8 +7,9 @@ that such files use: object headers of version 1, groups held in symbol tables (
 B-trees of type 0, symbol-table nodes, local heaps), datasets with compact, contiguous or
 chunked layout (version 1 B-trees of type 1), the deflate, shuffle and Fletcher-32 filters,
 and fixed-point, floating-point and fixed-length string datatypes.  Every dataset of the
-root group becomes a variable of a `netcdf.Dataset`; attributes are not read.  Anything
-outside that subset raises ValueError.
+root group becomes a variable of a `netcdf.Dataset`; attributes are not read.  A file
+outside that subset raises ValueError; a dataset outside it (variable-length strings, shared
+messages) is left out and named in the dataset's attrs["unread_datasets"].
 """
 from __future__ import annotations
 
@@ -65,8 +66,10 @@ class _File:
             p, n = blocks.pop(0)
             end = p + n
             while p + 8 <= end and len(out) < nmsg:
-                mt, ms = self.u(p, 2), self.u(p + 2, 2)
+                mt, ms, flags = self.u(p, 2), self.u(p + 2, 2), b[p + 4]
                 data = b[p + 8:p + 8 + ms]
+                if flags & 0x02 and mt in (0x01, 0x03, 0x05, 0x08, 0x0B):
+                    raise ValueError(f"HDF5 || shared header message (type {mt}) is not supported")
                 p += 8 + ms
                 if mt == 0x10:  # continuation
                     blocks.append((int.from_bytes(data[0:8], "little"), int.from_bytes(data[8:16], "little")))
@@ -251,8 +254,13 @@ def read(path) -> Dataset:
     if bt is None:
         raise ValueError("HDF5 || the root group has no symbol table (newer group format)")
     ds = Dataset()
+    unread = []
     for name, addr in h.group(bt, hp).items():
-        data = h.dataset(addr)
+        try:
+            data = h.dataset(addr)
+        except ValueError:  # a dataset outside the subset (e.g. variable-length strings)
+            unread.append(name)
+            continue
         if data is None:
             continue
         if data.dtype.kind == "S" and data.dtype.itemsize == 1:
@@ -261,4 +269,5 @@ def read(path) -> Dataset:
         for dn, n in zip(dims, data.shape):
             ds.dims[dn] = n
         ds.variables[name] = Variable(name, dims, data, {})
+    ds.attrs["unread_datasets"] = unread
     return ds
