@@ -13,7 +13,6 @@ messages) is left out and named in the dataset's attrs["unread_datasets"].
 """
 from __future__ import annotations
 
-import struct
 import zlib
 
 import numpy as np
