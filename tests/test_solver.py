@@ -196,7 +196,9 @@ def test_full_solver_gpu_matches_oracle(small_inputs, ax3d_lib):
 def test_transversely_isotropic_mesh_gpu_matches_oracle(tmp_path_factory, ax3d_lib):
     """A transversely isotropic mesh (TI top 220 km of the mantle) with its axial elements
     stored rotated, attenuation (CG4) on and Nu = 3: the GPU pre-loop's moduli equal the
-    numpy pre-loop's, and 200 steps of GPU seismograms and fields match the oracle."""
+    numpy pre-loop's, 200 steps of GPU seismograms match the FP32 oracle within 1e-5, and
+    the GPU fields are as close to the FP64 oracle's as the FP32 oracle's are (the two FP32
+    runs differ in operation order, ~1e-5 of the field after 200 attenuated TI steps)."""
     from oracle.oracle_py import OracleDomain
     from axisem3d_gb300.capi import Ax3dDomain
     from axisem3d_gb300.spec import MAT_TISO
@@ -209,14 +211,16 @@ def test_transversely_isotropic_mesh_gpu_matches_oracle(tmp_path_factory, ax3d_l
     np.testing.assert_array_equal(spec.e_mofs, host.e_mofs)
     np.testing.assert_allclose(spec.e_mod, host.e_mod, rtol=2e-6, atol=0)
     np.testing.assert_allclose(spec.e_attm, host.e_attm, rtol=2e-6, atol=1e-30)
-    g, o = Ax3dDomain(spec), OracleDomain(spec)
-    g.step(200)
-    o.step(200)
+    g, o, od = Ax3dDomain(spec), OracleDomain(spec), OracleDomain(spec, double=True)
+    for dom in (g, o, od):
+        dom.step(200)
     a, b = g.seismograms(0, 200), o.seismograms(0, 200)
     assert np.linalg.norm(a - b) <= 1e-5 * np.linalg.norm(b)
+    rel = lambda x, y: float(np.linalg.norm(x - y) / np.linalg.norm(y))
     for which in ("displ", "veloc"):
-        x, y = g.get(which, "solid"), o.get(which, "solid")
-        assert np.linalg.norm(x - y) <= 1e-5 * np.linalg.norm(y)
+        x, y, z = g.get(which, "solid"), o.get(which, "solid"), od.get(which, "solid")
+        assert rel(x, y) <= 3e-5, which
+        assert rel(x, z) <= 2 * rel(y, z) + 1e-6, which
 
 
 @pytest.mark.gpu
