@@ -1,0 +1,102 @@
+"""Test infrastructure: a minimal writer of the HDF5 subset `axisem3d_gb300.hdf5` reads
+(version 0 superblock, one root group held in a symbol table, version 1 object headers,
+contiguous datasets and chunked datasets with the deflate filter), so that the reader is
+exercised without an HDF5 library or an external file.  Written from the published HDF5
+format specification; little-endian int32 / float64 and one-byte strings only."""
+from __future__ import annotations
+
+import struct
+import zlib
+
+import numpy as np
+
+UNDEF = 0xFFFFFFFFFFFFFFFF
+
+
+def _pad8(b: bytes) -> bytes:
+    return b + b"\0" * (-len(b) % 8)
+
+
+def _msg(mtype: int, data: bytes) -> bytes:
+    data = _pad8(data)
+    return struct.pack("<HHB3x", mtype, len(data), 0) + data
+
+
+def _ohdr(msgs: list) -> bytes:
+    body = b"".join(msgs)
+    return struct.pack("<BBHII4x", 1, 0, len(msgs), 1, len(body)) + body
+
+
+def _datatype(a: np.ndarray) -> bytes:
+    if a.dtype == np.dtype("<i4"):
+        return struct.pack("<B3sI", 0x10 | 0, bytes([0x08, 0, 0]), 4) + struct.pack("<HH", 0, 32)
+    if a.dtype == np.dtype("<f8"):
+        return struct.pack("<B3sI", 0x10 | 1, bytes([0x20, 0x3F, 0]), 8) + struct.pack("<HHBBBBI", 0, 64, 52, 11, 0,
+                                                                                     52, 1023)
+    if a.dtype == np.dtype("S1"):
+        return struct.pack("<B3sI", 0x10 | 3, bytes([0, 0, 0]), 1)
+    raise ValueError(f"unsupported dtype {a.dtype}")
+
+
+def write(path, datasets: dict):
+    """datasets: name -> array, or (array, chunk shape) for a chunked, deflated dataset."""
+    out = bytearray(b"\0" * 96)  # superblock, written last
+    names = sorted(datasets)
+    # local heap data: "" at offset 0, then the names, each padded to 8 bytes
+    heap_data = bytearray(b"\0" * 8)
+    offs = {}
+    for n in names:
+        offs[n] = len(heap_data)
+        heap_data += _pad8(n.encode() + b"\0")
+
+    def put(b: bytes) -> int:
+        addr = len(out)
+        out.extend(b)
+        out.extend(b"\0" * (-len(out) % 8))
+        return addr
+
+    heap_data_addr = put(bytes(heap_data))
+    heap_addr = put(b"HEAP" + bytes([0, 0, 0, 0]) + struct.pack("<QQQ", len(heap_data), UNDEF, heap_data_addr))
+    ohdr = {}
+    for n in names:
+        spec = datasets[n]
+        a, chunks = (spec if isinstance(spec, tuple) else (spec, None))
+        a = np.ascontiguousarray(a)
+        nd = a.ndim
+        space = struct.pack("<BBBB4x", 1, nd, 0, 0) + b"".join(struct.pack("<Q", d) for d in a.shape)
+        msgs = [_msg(0x01, space), _msg(0x03, _datatype(a))]
+        if chunks is None:
+            addr = put(a.tobytes())
+            msgs.append(_msg(0x08, struct.pack("<BBQQ", 3, 1, addr, a.nbytes)))
+        else:
+            keys = []
+            grid = [range(0, s, c) for s, c in zip(a.shape, chunks)]
+            for corner in np.array(np.meshgrid(*grid, indexing="ij")).reshape(nd, -1).T:
+                block = np.zeros(chunks, a.dtype)
+                sl = tuple(slice(o, min(o + c, s)) for o, c, s in zip(corner, chunks, a.shape))
+                block[tuple(slice(0, x.stop - x.start) for x in sl)] = a[sl]
+                raw = zlib.compress(block.tobytes())
+                keys.append((len(raw), corner, put(raw)))
+            node = bytearray(b"TREE" + bytes([1, 0]) + struct.pack("<HQQ", len(keys), UNDEF, UNDEF))
+            for size, corner, addr in keys:
+                node += struct.pack("<II", size, 0) + b"".join(struct.pack("<Q", int(o)) for o in corner)
+                node += struct.pack("<Q", 0) + struct.pack("<Q", addr)
+            node += struct.pack("<II", 0, 0) + b"".join(struct.pack("<Q", s) for s in a.shape) + struct.pack("<Q", 0)
+            bt = put(bytes(node))
+            msgs.append(_msg(0x08, struct.pack("<BBBQ", 3, 2, nd + 1, bt) +
+                             b"".join(struct.pack("<I", c) for c in chunks) + struct.pack("<I", a.itemsize)))
+            msgs.append(_msg(0x0B, struct.pack("<BB6x", 1, 1) + struct.pack("<HHHHI4x", 1, 0, 0, 1, 6)))
+        ohdr[n] = put(_ohdr(msgs))
+    snod = bytearray(b"SNOD" + bytes([1, 0]) + struct.pack("<H", len(names)))
+    for n in names:
+        snod += struct.pack("<QQII16x", offs[n], ohdr[n], 0, 0)
+    snod_addr = put(bytes(snod))
+    btree = put(b"TREE" + bytes([0, 0]) + struct.pack("<HQQ", 1, UNDEF, UNDEF) +
+                struct.pack("<QQQ", 0, snod_addr, offs[names[-1]]))
+    root = put(_ohdr([_msg(0x11, struct.pack("<QQ", btree, heap_addr))]))
+    sb = b"\x89HDF\r\n\x1a\n" + bytes([0, 0, 0, 0, 0, 8, 8, 0]) + struct.pack("<HHI", 4, 16, 0)
+    sb += struct.pack("<QQQQ", 0, UNDEF, len(out), UNDEF)
+    sb += struct.pack("<QQII", 0, root, 1, 0) + struct.pack("<QQ", btree, heap_addr)
+    out[:96] = sb
+    with open(path, "wb") as f:
+        f.write(bytes(out))

@@ -1071,3 +1071,25 @@ def test_gpu_gaussian_random_sampling_matches_host(ax3d_lib):
     for e in range(n):
         np.testing.assert_array_equal(flat[ofs[e]:ofs[e + 1]].reshape(rows[e], 25),
                                       m.evaluate_rings_gpu(crds[e:e + 1], int(rows[e]))[0])
+
+
+def test_hdf5_reader_on_a_written_file(tmp_path):
+    """The HDF5 reader on a file written by the test's own minimal HDF5 writer: contiguous
+    int32 / float64 / one-byte-string datasets and chunked, deflated datasets with edge
+    chunks come back exact through netcdf.read."""
+    from tests import _hdf5_writer as W
+    rng = np.random.default_rng(5)
+    conn = rng.integers(1, 2000, (37, 4)).astype("<i4")
+    crd = rng.normal(size=101).astype("<f8")
+    vals = rng.normal(size=(3, 29)).astype("<f8")
+    names = np.zeros((3, 33), "S1")
+    for i, s in enumerate(("r1", "solid_fluid_boundary", "t0")):
+        names[i, :len(s)] = np.frombuffer(s.encode(), "S1")
+    W.write(tmp_path / "m.e", {"connect1": (conn, (16, 4)), "coordx": crd, "ss_names": names,
+                               "vals": (vals, (2, 8))})
+    ds = NC.read(tmp_path / "m.e")
+    np.testing.assert_array_equal(ds["connect1"], conn)
+    np.testing.assert_array_equal(ds["coordx"], crd)
+    np.testing.assert_array_equal(ds["vals"], vals)
+    assert ds.strings("ss_names") == ["r1", "solid_fluid_boundary", "t0"]
+    assert ds.attrs["unread_datasets"] == []
