@@ -737,7 +737,7 @@ template <int MAT>
 __device__ __noinline__ void phase_stress(float2 *buf, int S, int nr, int ne_, const int32_t *lst, const int32_t *rev,
                                           const float *md, const Pk pk, int p0, const Grp g) {
     constexpr int NM = MAT == 0 ? 2 : MAT == 1 ? 5 : 21;
-    constexpr int IT = MAT == 2 ? 1 : MAT == 1 ? 4 : 8;
+    constexpr int IT = MAT == 2 ? 1 : MAT == 1 ? 2 : 8;
     const int total = nr * ne_;
     const FDiv fe = make_fdiv((uint32_t)ne_);
     for (int t0 = g.tid; t0 < total; t0 += g.n * IT) {
