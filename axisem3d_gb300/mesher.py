@@ -175,7 +175,9 @@ def half_disk(n_theta=96, h_mantle=100e3, h_core=110e3, r_c=1500e3, seed=0, cour
         ds.add_var(f"side_ss{i + 1}", (f"num_side_ss{i + 1}",), np.array(ss) + 1, dtype=np.int32)
     ds.add_dim("two", 2)
     ds.add_dim("num_ellip", 2)
-    ds.add_var("ellipticity", ("two", "num_ellip"), np.array([[0.0, R_EARTH], [0.0, 0.0]]))
+    # ellipticity profile as AxiSEM's mesher writes it: knots r / R and the flattening relative
+    # to the surface's (a linear stand-in for the Clairaut profile, 0.7227 at the centre)
+    ds.add_var("ellipticity", ("two", "num_ellip"), np.array([[0.0, 1.0], [0.7227, 1.0]]))
     enames, evals = ["element_type", "fluid", "dt"], [etype.astype(float), fluid.astype(float), dt_e]
     if ti:
         aniso = (rin > R_EARTH - 220e3) & ~fluid[:, None]

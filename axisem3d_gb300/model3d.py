@@ -62,8 +62,14 @@ class Model3D:
         raise NotImplementedError
 
 
+def _spherical_colat(lat_deg, depth):
+    return math.radians(90.0 - lat_deg)
+
+
 class Bubble(Model3D):
-    def __init__(self, params, src, R):
+    def __init__(self, params, src, R, lat2theta=None):
+        """src = (latitude, longitude[, depth m]); lat2theta(lat, depth) the geodesy's
+        geographic latitude -> geocentric colatitude (spherical when None)."""
         self._head(params, "bubble", 7)
         value, radius, depth, lat, lon = (float(p) for p in params[2:7])
         self.value, self.radius = value, radius * 1e3
@@ -75,10 +81,12 @@ class Bubble(Model3D):
             t, p = math.radians(lat), math.radians(lon)
             self.center = r * np.array([math.sin(t) * math.cos(p), math.sin(t) * math.sin(p), math.cos(t)])
         else:
-            t, p = math.radians(90.0 - lat), math.radians(lon)
+            l2t = lat2theta or _spherical_colat
+            t, p = l2t(lat, depth * 1e3), math.radians(lon % 360)
             xg = r * np.array([math.sin(t) * math.cos(p), math.sin(t) * math.sin(p), math.cos(t)])
-            slat, slon = src
-            self.center = _rotation(math.radians(90.0 - slat), math.radians(slon)).T @ xg
+            slat, slon = src[0], src[1]
+            sdep = src[2] if len(src) > 2 else 0.0
+            self.center = _rotation(l2t(slat, sdep), math.radians(slon % 360)).T @ xg
         self.hwhm = self.radius * 0.2 if hwhm < 0 else hwhm
         if self.ref == 0:
             self.hwhm = 0.0
@@ -181,7 +189,7 @@ class GaussianRandom(Model3D):
         return out.reshape(shape), np.ones(shape, bool)
 
 
-def volumetric_models(par, src_latlon, R):
+def volumetric_models(par, src_latlon, R, lat2theta=None):
     """Volumetric3D::buildInparam: the MODEL_3D_VOLUMETRIC_NUM models of the list."""
     n = par.get("MODEL_3D_VOLUMETRIC_NUM", int)
     out = []
@@ -194,7 +202,7 @@ def volumetric_models(par, src_latlon, R):
         strs = entry.split("$")
         name, params = strs[0].lower(), strs[1:]
         if name == "bubble":
-            out.append(Bubble(params, src_latlon, R))
+            out.append(Bubble(params, src_latlon, R, lat2theta))
         elif name == "gaussian_random":
             out.append(GaussianRandom(params, R))
         else:

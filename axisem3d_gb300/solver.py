@@ -85,6 +85,7 @@ class Exodus:
     side: dict              # side-set name -> [E] side (-1 none)
     glob: dict              # global variables
     isotropic: bool = True  # VP_0 / VS_0 (isotropic) or VPV_0 ... ETA_0 (TI) variables
+    ellip: np.ndarray = None  # [2, n] ellipticity knots (r / R) and coefficients
 
     @staticmethod
     def read(path):
@@ -135,7 +136,7 @@ class Exodus:
             raise ValueError("Exodus || only crdsys = spherical meshes are supported")
         return Exodus(np.stack([d["coordx"], d["coordy"]], 1).astype(float), conn,
                       ev["element_type"].astype(int), ev["fluid"] > 0.5, ev.get("dt", np.zeros(E)), nodal, side, glob,
-                      iso)
+                      iso, np.asarray(d["ellipticity"], float) if "ellipticity" in d else None)
 
 
 def _int_or(par, key, default):
@@ -254,6 +255,49 @@ def back_azimuth(src_theta, src_phi, rec_theta, rec_phi):
     return t
 
 
+class Geodesy:
+    """Geodesy::setup / getFlattening / lat2Theta_r / theta2Lat_r (Geodesy.cpp:64-117,
+    176-199): the flattening at radius r is the global flattening 1 / MODEL_3D_ELLIPTICITY_INVF
+    times the mesh's ellipticity profile (linear between knots of r / R, 1 beyond the last),
+    zero with MODEL_3D_ELLIPTICITY_MODE off; geographic latitudes become geocentric
+    colatitudes through tan(lat_c) = (1 - f)^2 tan(lat)."""
+
+    def __init__(self, r_outer=6371e3, flattening=0.0, knots=(), coeffs=()):
+        self.R, self.f0 = float(r_outer), float(flattening)
+        self.knots, self.coeffs = np.asarray(knots, float), np.asarray(coeffs, float)
+
+    def flattening(self, r):
+        f, rr = 1.0, r / self.R
+        for i in range(1, len(self.knots)):
+            if rr <= self.knots[i]:
+                k0, k1, c0, c1 = self.knots[i - 1], self.knots[i], self.coeffs[i - 1], self.coeffs[i]
+                f = (c1 - c0) / (k1 - k0) * (rr - k0) + c0
+                break
+        return f * self.f0
+
+    @staticmethod
+    def _clamp(lat, limit_round, limit_bound, what):
+        if abs(lat) > limit_bound:
+            raise ValueError(f"Geodesy::{what} || Latitude out of range [-90, 90]")
+        return max(-limit_round, min(limit_round, lat))
+
+    def lat2theta(self, lat_deg, depth):
+        """Geocentric colatitude (rad) of a geographic latitude (deg) at the given depth (m)."""
+        f = self.flattening(self.R - depth)
+        lat = self._clamp(lat_deg, 90.0 - 1e-10, 90.1, "lat2Theta")
+        if f == 0.0:
+            return math.pi / 2 - math.radians(lat)
+        return math.pi / 2 - math.atan((1 - f) ** 2 * math.tan(math.radians(lat)))
+
+    def theta2lat(self, theta, depth):
+        """Geographic latitude (deg) of a geocentric colatitude (rad) at the given depth (m)."""
+        f = self.flattening(self.R - depth)
+        lat = self._clamp(math.pi / 2 - theta, math.radians(90.0 - 1e-10), math.radians(90.1), "theta2Lat")
+        if f == 0.0:
+            return math.degrees(lat)
+        return math.degrees(math.atan(math.tan(lat) / (1 - f) ** 2))
+
+
 def glob_to_src(theta_g, phi_g, src_theta, src_phi):
     """Geodesy::rotateGlob2Src on the unit sphere (no ellipticity)."""
     x = np.array([math.sin(theta_g) * math.cos(phi_g), math.sin(theta_g) * math.sin(phi_g), math.cos(theta_g)])
@@ -347,8 +391,29 @@ class Simulation:
         mat = self._gll_material(ex, axial_e)
         self.crds = crds
         self.vp_e, self.vs_e = mat["VP"].mean(1), mat["VS"].mean(1)
-        self.models = M3D.volumetric_models(self.par, self._cmt_latlon(), self.R)
+        self.geo_ = self.geodesy()
+        self.models = M3D.volumetric_models(self.par, self._src_llz(), self.R, self.geo_.lat2theta)
         self.src_dep = self._source_depth()
+
+    def ellipticity_mode(self):
+        return (self.par.values.get("MODEL_3D_ELLIPTICITY_MODE") or ["off"])[0].lower()
+
+    def geodesy(self):
+        """Geodesy::setup as ExodusModel::buildInparam calls it (ExodusModel.cpp:557-572): no
+        flattening with MODEL_3D_ELLIPTICITY_MODE off, else 1 / MODEL_3D_ELLIPTICITY_INVF
+        with the mesh's ellipticity profile (the mesh read first)."""
+        if self.ellipticity_mode() == "off":
+            return Geodesy(self.R)
+        inv_f = self.par.get("MODEL_3D_ELLIPTICITY_INVF", float)
+        if inv_f <= 0.0:
+            raise ValueError("ExodusModel::buildInparam || Invalid flattening.")
+        ell = self.ex.ellip
+        return Geodesy(self.R, 1.0 / inv_f, *((ell[0], ell[1]) if ell is not None else ((), ())))
+
+    def _src_llz(self):
+        """(latitude, longitude, depth m) of the source for the geodesy's rotations."""
+        lat, lon = self._cmt_latlon()
+        return lat, lon, self._source_depth()
 
     def _source_depth(self):
         """Source depth in m from SOURCE_FILE (0 in non-source mode)."""
@@ -410,14 +475,14 @@ class Simulation:
             p_nr = np.array([next_lucky(int(k // 2), bool(k % 2)) for k in uk])[inv.ravel()]
         # volumetric 3-D models (Material::addVolumetric3D) on each element's Nr slices
         e_nr = p_nr[e_pts].max(1)
-        models = M3D.volumetric_models(par, self._cmt_latlon(), self.R)
+        self.geo_ = self.geodesy()
+        models = M3D.volumetric_models(par, self._src_llz(), self.R, self.geo_.lat2theta)
         self.phi2d = self._phi2d()
         # options that would change the physics but are not built here: refuse them rather
         # than run without them (Geometric3D::buildInparam, ExodusModel.cpp:557-572)
-        emode = (par.values.get("MODEL_3D_ELLIPTICITY_MODE") or ["off"])[0].lower()
-        if emode != "off":
-            raise ValueError("ExodusModel::buildInparam || MODEL_3D_ELLIPTICITY_MODE: only 'off' (a spherical "
-                             "Earth) is built.")
+        if self.ellipticity_mode() == "full":
+            raise ValueError("Geometric3D::buildInparam || MODEL_3D_ELLIPTICITY_MODE full (the ellipsoidal "
+                             "deformation of the mesh) is not built; use off or geographic.")
         if _flag(par, "ATTENUATION") and _flag(par, "ATTENUATION_SPECFEM_LEGACY"):
             raise ValueError("AttBuilder::buildInparam || ATTENUATION_SPECFEM_LEGACY: the SPECFEM SLS fit is "
                              "not built; set it false.")
@@ -869,10 +934,10 @@ class Simulation:
         if mode == "source-centered":
             return math.radians(par.get("MODEL_2D_AZIMUTH", float)) % (2 * math.pi)
         if mode == "geographic":
-            lat, lon = self._cmt_latlon()
-            _, ph = glob_to_src(math.pi / 2 - math.radians(par.get("MODEL_2D_LATITUDE", float)),
+            lat, lon, dep = self._src_llz()
+            _, ph = glob_to_src(self.geo_.lat2theta(par.get("MODEL_2D_LATITUDE", float), 0.0),
                                 math.radians(par.get("MODEL_2D_LONGITUDE", float) % 360),
-                                math.pi / 2 - math.radians(lat), math.radians(lon % 360))
+                                self.geo_.lat2theta(lat, dep), math.radians(lon % 360))
             return ph
         raise ValueError("Mesh::Mesh || Invalid input for MODEL_2D_MODE.")
 
@@ -1103,7 +1168,7 @@ class Simulation:
         system = par.get("OUT_STATIONS_SYSTEM").lower()
         self.components = par.get("OUT_STATIONS_COMPONENTS").upper()
         lines = [l.split() for l in (self.input_dir / par.get("OUT_STATIONS_FILE")).read_text().splitlines() if l.strip()]
-        src_t = math.pi / 2 - math.radians(self.src_lat)
+        src_t = self.geo_.lat2theta(self.src_lat, self.src_dep)  # Geodesy::lat2Theta_d
         src_p = math.radians(self.src_lon % 360)
         dup = par.get("OUT_STATIONS_DUPLICATED").lower()
         if dup not in ("ignore", "rename", "error"):
@@ -1132,7 +1197,7 @@ class Simulation:
             extra = {t.lower() for t in toks[6:]}
             dumps.append((1 if "dump_strain" in extra else 0) | (2 if "dump_curl" in extra else 0))
             if system == "geographic":
-                th_g, ph_g = math.pi / 2 - math.radians(la), math.radians(lo % 360)
+                th_g, ph_g = self.geo_.lat2theta(la, bur), math.radians(lo % 360)  # Receiver.cpp:27
                 th, ph = glob_to_src(th_g, ph_g, src_t, src_p)
             else:
                 th, ph = math.radians(la), math.radians(lo)

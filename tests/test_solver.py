@@ -96,8 +96,9 @@ def test_transversely_isotropic_mesh(tmp_path):
 def test_hdf5_mesh_of_the_reference():
     """The reference's own template mesh (NetCDF-4 / HDF5, PREM anisotropic with one crust,
     50 s) and template inputs, when AX3D_REFERENCE_INPUT names a copy of that input folder:
-    the mesh reads (chunked, compressed datasets), and the case builds with its TI upper
-    mantle, attenuation and rotated axial elements (ellipticity switched off, not built)."""
+    the mesh reads (chunked, compressed datasets), and the case builds as it is: TI upper
+    mantle, attenuation, rotated axial elements, geographic ellipticity (flattened station
+    and source latitudes), the reference's time step, and 40 stable oracle steps."""
     import os
     import shutil
     src = os.environ.get("AX3D_REFERENCE_INPUT")
@@ -117,13 +118,11 @@ def test_hdf5_mesh_of_the_reference():
     shutil.copytree(src, d)
     for f in d.iterdir():
         f.chmod(0o644)
-    p = d / "inparam.model"
-    p.write_text("\n".join("MODEL_3D_ELLIPTICITY_MODE off" if ln.startswith("MODEL_3D_ELLIPTICITY_MODE") else ln
-                           for ln in p.read_text().splitlines()) + "\n")
     sim = solver.Simulation(d)
     spec = sim.build()
     assert spec.n_elements == 2016 and (spec.e_mat == MAT_TISO).sum() == 256
     assert np.isfinite(spec.e_geo).all() and set(np.unique(sim.co).tolist()) == {-1, 0, 2, 3}
+    assert sim.ellipticity_mode() == "geographic" and sim.geo_.flattening(6371e3) == 1 / 299.8
     # Quad::getDeltaT: the mesh's dt (courant x shortest side / vp, 2.524 s in the crust)
     # scaled by the closest GLL distance over the shortest side
     assert abs(spec.dt - 0.43585) < 1e-4 and abs(float(sim.ex.dt.min()) - 2.52414) < 1e-4
@@ -1093,3 +1092,37 @@ def test_hdf5_reader_on_a_written_file(tmp_path):
     np.testing.assert_array_equal(ds["vals"], vals)
     assert ds.strings("ss_names") == ["r1", "solid_fluid_boundary", "t0"]
     assert ds.attrs["unread_datasets"] == []
+
+
+def test_geographic_ellipticity_mode(tmp_path):
+    """MODEL_3D_ELLIPTICITY_MODE geographic (ExodusModel.cpp:557-572, Geodesy.cpp:64-117,
+    176-199): station and source latitudes become geocentric colatitudes with the flattening
+    1 / MODEL_3D_ELLIPTICITY_INVF scaled by the mesh's ellipticity profile; off leaves them
+    spherical; full (the ellipsoidal deformation of the mesh) is refused."""
+    import math
+    g = solver.Geodesy(6371e3, 1 / 299.8, [0.0, 0.5, 1.0], [0.7, 0.8, 1.0])
+    assert g.flattening(6371e3) == pytest.approx(1 / 299.8)
+    assert g.flattening(0.75 * 6371e3) == pytest.approx(0.9 / 299.8)
+    t = g.lat2theta(45.0, 0.0)
+    assert t == pytest.approx(math.pi / 2 - math.atan((1 - 1 / 299.8) ** 2))
+    for lat in (-89.0, -30.0, 0.0, 12.5, 60.0):
+        assert g.theta2lat(g.lat2theta(lat, 2e5), 2e5) == pytest.approx(lat, abs=1e-12)
+    assert solver.Geodesy(6371e3).lat2theta(30.0, 0.0) == pytest.approx(math.radians(60.0))
+    thetas = {}
+    for mode in ("off", "geographic"):
+        d = solver.write_inputs(tmp_path / mode, mesh_kw=SMALL_MESH, steps=10, nu=2, n_stations=6,
+                                system="geographic")
+        (d / "STATIONS").write_text("".join(f"S{i} XX {la:.3f} {lo:.3f} 0.0 0.0\n" for i, (la, lo) in
+                                            enumerate([(45.0, 10.0), (-30.0, 60.0), (60.0, -120.0), (10.0, 170.0)])))
+        p = d / "inparam.model"
+        p.write_text(p.read_text() + f"MODEL_3D_ELLIPTICITY_MODE {mode}\nMODEL_3D_ELLIPTICITY_INVF 299.8\n")
+        sim = solver.Simulation(d)
+        sim.build()
+        thetas[mode] = np.array([r[5] for r in sim.receivers])
+    diff = np.abs(thetas["geographic"] - thetas["off"])
+    assert diff.max() > 1e-4 and diff.max() < 0.01  # at most ~1/300 rad of latitude shift
+    d = solver.write_inputs(tmp_path / "full", mesh_kw=SMALL_MESH, steps=10, nu=2)
+    p = d / "inparam.model"
+    p.write_text(p.read_text() + "MODEL_3D_ELLIPTICITY_MODE full\nMODEL_3D_ELLIPTICITY_INVF 299.8\n")
+    with pytest.raises(ValueError, match="full"):
+        solver.Simulation(d).build()
