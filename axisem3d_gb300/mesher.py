@@ -58,12 +58,14 @@ def _radii(r0, r1, h):
 
 def half_disk(n_theta=96, h_mantle=100e3, h_core=110e3, r_c=1500e3, seed=0, courant=0.6,
               nsls=3, f_min=1 / 200.0, f_max=1 / 10.0, f_ref=1.0, qmu=(600.0, 80.0), qkappa=57823.0,
-              ti=False, rotate_axis=False):
+              ti=False, rotate_axis=False, rotate_all=False):
     """Return a NetCDF Dataset with the Exodus schema.  n_theta must be a multiple of 4.
     ti: write the transversely isotropic variables (VPV, VPH, VSV, VSH, ETA) with radial
     anisotropy in the top 220 km of the mantle (vph = 1.03 vpv, vsh = 1.04 vsv, eta = 0.95),
     as PREM-like meshes do.  rotate_axis: store the axial elements with their nodes rotated so
-    that the axis is side 0, 1 or 2 (in turn), as meshers may write them."""
+    that the axis is side 0, 1 or 2 (in turn), as meshers may write them.  rotate_all: store
+    every other element with its nodes rotated by e % 4 (its curved side then 0, 1, 2 or 3):
+    the same Earth in other local orientations."""
     if n_theta % 4:
         raise ValueError("n_theta must be a multiple of 4")
     rng = np.random.default_rng(seed)
@@ -185,22 +187,26 @@ def half_disk(n_theta=96, h_mantle=100e3, h_core=110e3, r_c=1500e3, seed=0, cour
                 ("VSH", np.where(aniso, 1.04 * vs, vs)), ("ETA", np.where(aniso, 0.95, 1.0)))
     else:
         mats = (("VP", vp), ("VS", vs))
-    conn_w, sides_w = conn, {}
-    if rotate_axis:
-        # the reader's rotation (axis side a -> 3) undone: conn_old[k] = conn[(k - a + 3) % 4]
-        conn_w = conn.copy()
-        rot = {}
+    # stored node order: element e's node k is node (k + shift[e]) % 4 of the built element
+    shift = {}
+    if rotate_axis:  # the axis on side 0, 1 or 2; the reader rotates it back to side 3
         for i, e in enumerate(ax_e):
-            a = i % 3
-            rot[e] = a
-            conn_w[e] = conn[e][[(k - a + 3) % 4 for k in range(4)]]
+            shift[e] = (3 - i % 3) % 4
+    if rotate_all:  # every other element's nodes rotated as well (curved sides 1 / 3 occur)
+        axial_set = set(ax_e)
+        for e in range(E):
+            if e not in axial_set:
+                shift[e] = e % 4
     mats = mats + (("RHO", rho), ("QMU", np.repeat(qm[:, None], 4, 1)), ("QKAPPA", np.full((E, 4), qkappa)))
-    if rotate_axis:
-        mats = tuple((nm, _rotate_rows(np.asarray(v, float), rot)) for nm, v in mats)
+    if shift:
+        conn_w = conn.copy()
+        for e, t in shift.items():
+            conn_w[e] = conn[e][[(k + t) % 4 for k in range(4)]]
+        mats = tuple((nm, _rotate_rows(np.asarray(v, float), shift)) for nm, v in mats)
         ds.variables["connect1"].data[...] = (conn_w + 1).astype(">i4")
         for i, (_, ee, ss) in enumerate(sets):
             ds.variables[f"side_ss{i + 1}"].data[...] = np.array(
-                [(sd + rot[e] - 3) % 4 if e in rot else sd for e, sd in zip(ee, ss)], np.int64) + 1
+                [(sd - shift.get(e, 0)) % 4 for e, sd in zip(ee, ss)], np.int64) + 1
     for nm, v in mats:
         for k in range(4):
             enames.append(f"{nm}_{k}")
@@ -211,11 +217,11 @@ def half_disk(n_theta=96, h_mantle=100e3, h_core=110e3, r_c=1500e3, seed=0, cour
     return ds
 
 
-def _rotate_rows(v, rot):
-    """Nodal values [E, 4] of the elements in rot stored in their rotated node order."""
+def _rotate_rows(v, shift):
+    """Nodal values [E, 4] of the elements in shift stored in their rotated node order."""
     v = v.copy()
-    for e, a in rot.items():
-        v[e] = v[e][[(k - a + 3) % 4 for k in range(4)]]
+    for e, t in shift.items():
+        v[e] = v[e][[(k + t) % 4 for k in range(4)]]
     return v
 
 
