@@ -1203,11 +1203,14 @@ class Simulation:
                 th, ph = math.radians(la), math.radians(lo)
                 th_g, ph_g = src_to_glob(th, ph, src_t, src_p)
             self.baz.append(back_azimuth(src_t, src_p, th_g, ph_g))
+            # the station's geographic coordinates as the outputs name them (Receiver.cpp:38-39)
+            lat_g = self.geo_.theta2lat(th_g, bur)
+            lon_g = math.degrees(ph_g - 2 * math.pi if ph_g > math.pi else ph_g)
             r = self.R - bur
             e, xi, eta = self._locate(r * math.sin(th), r * math.cos(th))
             wxi = _lagrange(xi, S.glj()[0] if self.axial_e[e] else S.gll()[0])
             weta = _lagrange(eta, S.gll()[0])
-            rec.append((name, net, la, lo, bur, th, ph, e, np.outer(wxi, weta).ravel()))
+            rec.append((name, net, lat_g, lon_g, bur, th, ph, e, np.outer(wxi, weta).ravel()))
         self.receivers = rec
         spec.r_dump = np.array(dumps, np.int32)
         spec.r_elem = np.array([r[7] for r in rec], np.int32)

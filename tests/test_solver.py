@@ -1161,6 +1161,9 @@ def test_geographic_ellipticity_mode(tmp_path):
         sim = solver.Simulation(d)
         sim.build()
         thetas[mode] = np.array([r[5] for r in sim.receivers])
+        # the outputs name the geographic coordinates back (Receiver.cpp:38-39)
+        np.testing.assert_allclose([r[2] for r in sim.receivers], [45.0, -30.0, 60.0, 10.0], atol=1e-9)
+        np.testing.assert_allclose([r[3] for r in sim.receivers], [10.0, 60.0, -120.0, 170.0], atol=1e-9)
     diff = np.abs(thetas["geographic"] - thetas["off"])
     assert diff.max() > 1e-4 and diff.max() < 0.01  # at most ~1/300 rad of latitude shift
     d = solver.write_inputs(tmp_path / "full", mesh_kw=SMALL_MESH, steps=10, nu=2)
