@@ -216,13 +216,14 @@ def apply_models(models, props1d, crds, nr, fluid, phi2d=None, gpu=False, presam
 
     props1d: {"VP","VS","RHO": (n, 25)} 1-D values at the GLL points; crds (n, 25, 2) = (s, z);
     fluid (n,) bool.  Slice alpha sits at phi = 2 pi alpha / nr, or every slice at phi2d in
-    2-D mode (Quad::computeGeocentricGlobal with phi2D).  Returns ({prop: (n, nr, 25)},
-    touched (n,) bool): elements with any point inside any model's range.  gpu: sample the
+    2-D mode (Quad::computeGeocentricGlobal with phi2D).  Returns ({prop: (n, nr, 25)
+    float32}, touched (n,) bool): elements with any point inside any model's range; a property
+    no model changes is its 1-D row broadcast over the slices (a read-only view).  gpu: sample the
     Gaussian-random models on the GPU (ax3d_sample_gaussian_random); presampled: {model
     index: (n, nr, 25)} values already sampled for this group."""
     phi = 2 * math.pi * np.arange(nr) / nr if phi2d is None else np.full(nr, float(phi2d))
     n = len(crds)
-    out = {k: np.empty((n, nr, 25), np.float32) for k in props1d}
+    out = {}
     touched = np.zeros(n, bool)
     on_gpu = dict(presampled or {})
     on_gpu.update({i: m.evaluate_rings_gpu(crds, nr, phi2d) for i, m in enumerate(models)
@@ -235,11 +236,13 @@ def apply_models(models, props1d, crds, nr, fluid, phi2d=None, gpu=False, presam
             s, z = crds[a:b, :, 0], crds[a:b, :, 1]
             xyz = np.stack([s[:, None, :] * np.cos(phi)[None, :, None], s[:, None, :] * np.sin(phi)[None, :, None],
                             np.broadcast_to(z[:, None, :], (b - a, nr, 25))], -1)
-        cur = {k: np.repeat(v[a:b, None, :], nr, 1).astype(float) for k, v in props1d.items()}
+        # the properties a model has changed, (n, nr, 25); the others stay the 1-D row, which
+        # broadcasts over the slices
+        cur = {}
         for i, m in enumerate(models):
             if i in on_gpu:
                 val = on_gpu[i][a:b]
-                inr = np.ones(val.shape, bool)
+                inr = np.ones((b - a, 1, 1), bool)  # the sampler covers every point
             else:
                 val, inr = m.evaluate(xyz)
             if not m.fluid:
@@ -247,20 +250,32 @@ def apply_models(models, props1d, crds, nr, fluid, phi2d=None, gpu=False, presam
             if not inr.any():
                 continue
             touched[a:b] |= inr.any((1, 2))
-            x1 = props1d[m.prop][a:b, None, :]
-            x = cur[m.prop]
+            x1 = props1d[m.prop][a:b, None, :].astype(float)
+            x = cur.get(m.prop, x1)
             if m.ref == 0:
-                new = np.broadcast_to(val, x.shape)
-            elif m.ref == 1:
-                new = x1 * (1.0 + val)
+                cur[m.prop] = np.where(inr, val, x)
+                continue
+            new = 1.0 + val  # a new array: the perturbation applied in place
+            if m.ref == 1:
+                new *= x1
             elif m.ref == 2:
-                new = x * (1.0 + val)
+                new *= x
             else:
-                new = (x - x1) * (1.0 + val) + x1
-            cur[m.prop] = np.where(inr, new, x)
+                new *= x - x1
+                new += x1
+            if not inr.all():
+                np.copyto(new, x, where=~inr)
+            cur[m.prop] = new
+        for k in cur:
+            if k not in out:  # first change of k: the chunks before hold its 1-D row
+                out[k] = np.empty((n, nr, 25), np.float32)
+                out[k][:a] = props1d[k][:a, None, :]
         for k in out:
-            out[k][a:b] = cur[k]
-    return out, touched
+            out[k][a:b] = cur[k] if k in cur else props1d[k][a:b, None, :]
+    for k, v in props1d.items():
+        if k not in out:  # no model changes k: its 1-D row, broadcast over the slices (read-only)
+            out[k] = np.broadcast_to(v.astype(np.float32)[:, None, :], (n, nr, 25))
+    return {k: out[k] for k in props1d}, touched
 
 
 def linear_resampling(new_size, original):

@@ -36,12 +36,15 @@ class SLSFit:
 
 
 def _flat(a):
+    """One contiguous float32 vector of an array, or of a list of per-element arrays."""
+    if isinstance(a, np.ndarray):
+        return np.ascontiguousarray(a, np.float32).reshape(-1)
     return np.ascontiguousarray(np.concatenate([np.asarray(x, np.float32).reshape(-1) for x in a]))
 
 
 def moduli_gpu(rows, ifact, model: dict, isotropic=False, att=ATT_NONE, sls: SLSFit | None = None, device=0):
-    """ax3d_precompute_elastic.  model: name -> list over elements of [rows][25] arrays
-    (vpv, vph, vsv, vsh, eta, rho[, qkappa, qmu])."""
+    """ax3d_precompute_elastic.  model: name -> list over elements of [rows][25] arrays, or
+    their concatenation (vpv, vph, vsv, vsh, eta, rho[, qkappa, qmu])."""
     from .capi import load_library
     lib = load_library()
     f = lib.ax3d_precompute_elastic

@@ -221,6 +221,20 @@ def _parse_keys(text, keys):
     return out
 
 
+def _varies(a):
+    """Per element of a (n, nr, 25) property: whether any point's value changes over the
+    slices (none for a 1-D row broadcast over them)."""
+    if a.strides[1] == 0:
+        return np.zeros(len(a), bool)
+    return (a.max(1) != a.min(1)).any(1)
+
+
+# the five points of each element side in GLL index order: (ip, jp) with jp = 0 (side 0),
+# ip = 4 (side 1), jp = 4 (side 2) and ip = 0 (side 3), local index ip * 5 + jp
+_SIDE_IP = np.array([[0, 1, 2, 3, 4], [4] * 5, [0, 1, 2, 3, 4], [0] * 5])
+_SIDE_JP = np.array([[0] * 5, [0, 1, 2, 3, 4], [4] * 5, [0, 1, 2, 3, 4]])
+
+
 def _colat(s, z):
     """Geodesy::rtheta (Geodesy.cpp:13-16): colatitude of (s, z), 0 at the centre."""
     r = math.hypot(s, z)
@@ -441,7 +455,14 @@ class Simulation:
         # unique GLL points by coordinates (Connectivity::formElemToGLL)
         tol = 1e-3
         key = np.round(crds.reshape(-1, 2) / tol).astype(np.int64)
-        _, pid, inv = np.unique(key, axis=0, return_index=True, return_inverse=True)
+        # rows numbered in lexicographic (s, z) key order, as np.unique(axis=0) would, by one
+        # lexsort instead of a sort of structured rows
+        order = np.lexsort((key[:, 1], key[:, 0]))
+        ks = key[order]
+        first = np.ones(len(ks), bool)
+        first[1:] = (ks[1:] != ks[:-1]).any(1)
+        inv = np.empty(len(ks), np.int64)
+        inv[order] = np.cumsum(first) - 1
         e_pts = inv.reshape(E, 25).astype(np.int32)
         P = int(e_pts.max()) + 1
         pcrd = np.zeros((P, 2))
@@ -520,9 +541,9 @@ class Simulation:
                 e3d[sel[tj]] = True
                 # per element, for the mass and the time step below: whether rho (vp) varies
                 # over the slices, the first slice, and the largest Vp of the element
-                g3 = {k: v[tj] for k, v in cur.items()}
-                rho_var[sel[tj]] = (g3["RHO"].max(1) != g3["RHO"].min(1)).any(1)
-                vp_var[sel[tj]] = (g3["VP"].max(1) != g3["VP"].min(1)).any(1)
+                g3 = cur if len(tj) == len(sel) else {k: v[tj] for k, v in cur.items()}
+                rho_var[sel[tj]] = _varies(g3["RHO"])
+                vp_var[sel[tj]] = _varies(g3["VP"])
                 rho_first[sel[tj]], vp_first[sel[tj]] = g3["RHO"][:, 0], g3["VP"][:, 0]
                 vp_max3[sel[tj]] = g3["VP"].max((1, 2))
                 for jj, j in enumerate(tj):
@@ -614,51 +635,44 @@ class Simulation:
         sfn3 = {}  # undulated boundary: normals per slice (Quad::computeNormal with getSFNormalRTZ)
         sfside = ex.side.get("solid_fluid_boundary", np.full(E, -1))
         wg, wjw = S.gll()[1], S.glj()[1]
-        def side_normal(e, side):
-            """Quad::computeNormal (Quad.cpp:661-715) without relabelling, for the five
-            points (local index, normal) of one side."""
-            n0, n1 = nodes[e][:, side], nodes[e][:, (side + 1) % 4]
-            r0, t0 = np.hypot(*n0), _colat(*n0)
-            r1, t1 = np.hypot(*n1), _colat(*n1)
+        def side_normals(es, sides):
+            """Quad::computeNormal (Quad.cpp:661-715) without relabelling, for the five points
+            of side sides[i] of element es[i]: local indices (n, 5) and normals (n, 5, 3)."""
+            es, sides = np.asarray(es, np.int64), np.asarray(sides, np.int64)
+            n0, n1 = nodes[es, :, sides], nodes[es, :, (sides + 1) % 4]
+            r0, r1 = np.hypot(n0[:, 0], n0[:, 1]), np.hypot(n1[:, 0], n1[:, 1])
+            dth = np.abs(np.array([_colat(*b) - _colat(*a) for a, b in zip(n0, n1)]))
             rsf = 0.5 * (r0 + r1)
-            h_r_dt, h_r2_dt = 0.5 * rsf * abs(t1 - t0), 0.5 * rsf * rsf * abs(t1 - t0)
-            out = []
-            for ip in range(5):
-                for jp in range(5):
-                    on = (side == 0 and jp == 0) or (side == 1 and ip == 4) or (side == 2 and jp == 4) or \
-                         (side == 3 and ip == 0)
-                    if not on:
-                        continue
-                    k = ip * 5 + jp
-                    sz = crds[e, k]
-                    rr = np.hypot(*sz)
-                    sint, cost = sz[0] / rr, sz[1] / rr
-                    nvec = np.array([sint, 0.0, cost])
-                    wsf = (wjw if axial_e[e] else wg)[ip] if side in (0, 2) else wg[jp]
-                    if axial_e[e]:
-                        if ip == 0:
-                            nvec *= wsf * jac[0][e, ip, jp] * h_r_dt
-                        else:
-                            xi = xj[ip]
-                            nvec *= wsf / (1 + xi) * sint * h_r2_dt
-                    else:
-                        nvec *= wsf * sint * h_r2_dt
-                    if side != co[e]:
-                        nvec = -nvec
-                    out.append((k, nvec))
-            return out
+            h_r_dt, h_r2_dt = (0.5 * rsf * dth)[:, None], (0.5 * rsf * rsf * dth)[:, None]
+            ip, jp = _SIDE_IP[sides], _SIDE_JP[sides]
+            k = ip * 5 + jp
+            sz = crds[es[:, None], k]
+            rr = np.hypot(sz[..., 0], sz[..., 1])
+            sint, cost = sz[..., 0] / rr, sz[..., 1] / rr
+            ax = axial_e[es][:, None]
+            wsf = np.where(np.isin(sides, (0, 2))[:, None], np.where(ax, wjw[ip], wg[ip]), wg[jp])
+            with np.errstate(divide="ignore", invalid="ignore"):
+                fac = np.where(~ax, wsf * sint * h_r2_dt,
+                               np.where(ip == 0, wsf * jac[0][es[:, None], ip, jp] * h_r_dt,
+                                        wsf / (1 + xj[ip]) * sint * h_r2_dt))
+            nv = np.stack([sint, np.zeros_like(sint), cost], -1) * fac[..., None]
+            return k, np.where((sides != co[es])[:, None, None], -nv, nv)
 
-        for e in np.nonzero(sfside >= 0)[0]:
-            for k, nvec in side_normal(e, sfside[e]):
+        sf_e = np.nonzero(sfside >= 0)[0]
+        sf_k, sf_nv = side_normals(sf_e, sfside[sf_e])
+        plain = ~np.isin(sf_e, list(relab))
+        # GLLPoint::addSFNormal, element by element
+        np.add.at(sfn, e_pts[sf_e[plain, None], sf_k[plain]].ravel(),
+                  (0.5 * np.where(fl[sf_e[plain]][:, None, None], sf_nv[plain], -sf_nv[plain])).reshape(-1, 3))
+        for i in np.nonzero(~plain)[0]:
+            e = sf_e[i]
+            for k, nvec in zip(sf_k[i], sf_nv[i]):
                 pk = e_pts[e, k]
-                if e in relab:
-                    # normal_RTZ per slice rotated to (s, phi, z), times the same area factor
-                    sint, cost = crds[e, k, 0] / np.hypot(*crds[e, k]), crds[e, k, 1] / np.hypot(*crds[e, k])
-                    Q = np.array([[cost, 0.0, sint], [0.0, 1.0, 0.0], [-sint, 0.0, cost]])
-                    nv = relab[e].sf_normal_rtz(k) @ Q.T * float(nvec @ np.array([sint, 0.0, cost]))
-                    sfn3[pk] = sfn3.get(pk, 0.0) + 0.5 * (nv if fl[e] else -nv)
-                else:
-                    sfn[pk] += 0.5 * (nvec if fl[e] else -nvec)  # GLLPoint::addSFNormal
+                # normal_RTZ per slice rotated to (s, phi, z), times the same area factor
+                sint, cost = crds[e, k, 0] / np.hypot(*crds[e, k]), crds[e, k, 1] / np.hypot(*crds[e, k])
+                Q = np.array([[cost, 0.0, sint], [0.0, 1.0, 0.0], [-sint, 0.0, cost]])
+                nv = relab[e].sf_normal_rtz(k) @ Q.T * float(nvec @ np.array([sint, 0.0, cost]))
+                sfn3[pk] = sfn3.get(pk, 0.0) + 0.5 * (nv if fl[e] else -nv)
         # moduli (Material::createElastic / createAcoustic, isotropic)
         att_on = par.get("ATTENUATION", bool)
         cg4 = par.get("ATTENUATION_CG4", bool)
@@ -676,9 +690,16 @@ class Simulation:
         hmin_edge = np.hypot(*(xy4 - np.roll(xy4, -1, axis=1)).transpose(2, 0, 1)).min(1)
         vmax_ref = np.maximum(ex.nodal["VPV"], ex.nodal["VPH"]).max(1)
         courant = ex.dt.astype(float) * vmax_ref / hmin_edge
-        dd = crds[:, :, None, :] - crds[:, None, :, :]
-        dd = np.hypot(dd[..., 0], dd[..., 1])
-        hmin_gll = np.where(np.eye(25, dtype=bool)[None], np.inf, dd).min((1, 2))
+        # every pair of an element's GLL points once, point-major for contiguous gathers; the
+        # distance (hypot) is taken only for the pairs whose squared distance is within 1e-9 of
+        # the element's smallest, which always holds the closest pair
+        pa, pb = np.triu_indices(25, 1)
+        T = np.ascontiguousarray(crds.transpose(1, 2, 0))
+        D = T[pa] - T[pb]
+        d2 = D[:, 0] * D[:, 0] + D[:, 1] * D[:, 1]
+        pr, pe = np.nonzero(d2 <= d2.min(0) * (1 + 1e-9))
+        hmin_gll = np.full(E, np.inf)
+        np.minimum.at(hmin_gll, pe, np.hypot(D[pr, 0, pe], D[pr, 1, pe]))
         vmax_1d = np.maximum(mat["VPV"], mat["VPH"]).max(1)
         vmax_e = np.where(e3d, vp_max3, vmax_1d)  # the slice maximum: 3-D elements' largest slice
         dt_e = courant * hmin_gll / vmax_e
@@ -708,8 +729,10 @@ class Simulation:
             vp_e, vs_e, rho_e = ((props3[e]["VP"], props3[e]["VS"], props3[e]["RHO"]) if e3d[e]
                                  else (vp[e][None, :], vs[e][None, :], rho[e][None, :]))
             if fl[e]:  # Material::createAcoustic: K = iFact / rho, times the stiffness Jacobian
-                e_mod.append((f / rho_e * jstiff.get(e, 1.0)).ravel())
-                e_attm.append(np.zeros(0))
+                # stored as float32 here, so that with the GPU's float32 solid moduli the
+                # concatenation below needs no float64 copy
+                e_mod.append((f / rho_e * jstiff.get(e, 1.0)).ravel().astype(np.float32))
+                e_attm.append(np.zeros(0, np.float32))
                 e_mat.append(MAT_ACOUSTIC)
                 e_att.append(ATT_NONE)
                 continue
@@ -773,7 +796,7 @@ class Simulation:
                 vals[ofs[p]:ofs[p] + lens[p]] = 1.0 / v
             return lens.astype(np.int32), vals.astype(np.float32)
         p_mslen, p_ms = pack_mass(has_s, ms, ms3)
-        oc_pt, oc_len, oc_vals = self._ocean_load(ex, fl, e_pts, crds, side_normal, ms, ms3, p_nr)
+        oc_pt, oc_len, oc_vals = self._ocean_load(ex, fl, e_pts, crds, side_normals, ms, ms3, p_nr)
         p_mflen, p_mf = pack_mass(has_f, mf, mf3)
         # coupling rows (SolidFluidCoupling1D / 3D when the fluid mass varies with phi)
         sflen = np.where(kind == POINT_SOLID_FLUID, 1, 0).astype(np.int32)
@@ -805,8 +828,8 @@ class Simulation:
             e_pts=e_pts, e_mat=np.array(e_mat, np.int8), e_axial=axial_e.astype(np.uint8),
             e_in3d=e3d.astype(np.uint8), e_geo=geo.astype(np.float32),
             e_trig=GEO.trig_tables(theta).transpose(1, 0, 2).astype(np.float32),
-            e_mofs=mofs, e_mod=np.concatenate(e_mod).astype(np.float32), e_att=np.array(e_att, np.int8),
-            e_aofs=aofs, e_attm=(np.concatenate(e_attm) if e_attm else np.zeros(0)).astype(np.float32),
+            e_mofs=mofs, e_mod=np.concatenate(e_mod).astype(np.float32, copy=False), e_att=np.array(e_att, np.int8),
+            e_aofs=aofs, e_attm=(np.concatenate(e_attm) if e_attm else np.zeros(0)).astype(np.float32, copy=False),
             nsls=nsls, att_alpha=alpha, att_beta=beta, att_gamma=gamma, att_do_kappa=dokappa,
             kahan=kahan, stability_interval=par.get("OPTION_STABILITY_INTERVAL", int),
             oc_pt=oc_pt, oc_len=oc_len, oc_vals=oc_vals, p_crds=pcrd)
@@ -893,30 +916,27 @@ class Simulation:
         returns {element: (moduli [2][rows][25], attenuation moduli)}.  jstiff: relabelled
         elements' stiffness Jacobians, applied through rho (every modulus is linear in it)."""
         from . import preloop as PL
-        solid = [e for e in range(E) if not fl[e]]
-        rows, model = [], {k: [] for k in ("vpv", "vph", "vsv", "vsh", "eta", "rho", "qkappa", "qmu")}
-        for e in solid:
-            vp_e, vs_e, rho_e = ((props3[e]["VP"], props3[e]["VS"], props3[e]["RHO"]) if e3d[e]
-                                 else (vp[e][None, :], vs[e][None, :], rho[e][None, :]))
-            nr = vp_e.shape[0]
-            rows.append(nr)
-            model["vpv"].append(vp_e)
-            model["vph"].append(vp_e)
-            model["vsv"].append(vs_e)
-            model["vsh"].append(vs_e)
-            model["eta"].append(np.ones((nr, 25)))
-            model["rho"].append(rho_e * (jstiff or {}).get(e, 1.0))
-            if attk != ATT_NONE:
-                model["qkappa"].append(np.broadcast_to(mat["QKAPPA"][e][None, :], (nr, 25)))
-                model["qmu"].append(np.broadcast_to(mat["QMU"][e][None, :], (nr, 25)))
-        if attk == ATT_NONE:
-            model.pop("qkappa")
-            model.pop("qmu")
+        solid = np.nonzero(~fl)[0]
+        jstiff = jstiff or {}
+        rows = np.array([props3[e]["VP"].shape[0] if e3d[e] else 1 for e in solid], np.int64)
+
+        def stacked(key, base, scale):
+            """[rows][25] of every solid element (3-D rows, or the 1-D row) times its scale,
+            concatenated."""
+            return np.concatenate([(props3[e][key] if e3d[e] else base[e][None, :]) *
+                                   (scale[e] if e in scale else 1) for e in solid] if scale else
+                                  [props3[e][key] if e3d[e] else base[e][None, :] for e in solid])
+        vp_s, vs_s = stacked("VP", vp, {}), stacked("VS", vs, {})
+        model = {"vpv": vp_s, "vph": vp_s, "vsv": vs_s, "vsh": vs_s,
+                 "eta": np.ones((int(rows.sum()), 25), np.float32), "rho": stacked("RHO", rho, jstiff)}
+        if attk != ATT_NONE:
+            model["qkappa"] = np.repeat(mat["QKAPPA"][solid], rows, axis=0)
+            model["qmu"] = np.repeat(mat["QMU"][solid], rows, axis=0)
         sls = PL.SLSFit(*fit, do_kappa=dokappa) if fit else None
         mod, att = PL.moduli_gpu(np.array(rows), ifact[solid], model, isotropic=True, att=attk, sls=sls)
         npa = 4 if attk == ATT_CG4 else 25
         out, mo, ao = {}, 0, 0
-        for e, nr in zip(solid, rows):
+        for e, nr in zip(solid.tolist(), rows.tolist()):
             na = 2 * nr * npa if attk != ATT_NONE else 0
             out[e] = (mod[mo:mo + 2 * nr * 25], att[ao:ao + na])
             mo += 2 * nr * 25
@@ -985,7 +1005,7 @@ class Simulation:
         nu = dom.get_wisdom()
         return W.write_wisdom(path, self.spec.p_crds[:, 0], self.spec.p_crds[:, 1], nu, self.spec.p_nr // 2)
 
-    def _ocean_load(self, ex, fl, e_pts, crds, side_normal, ms, ms3, p_nr):
+    def _ocean_load(self, ex, fl, e_pts, crds, side_normals, ms, ms3, p_nr):
         """MODEL_3D_OCEAN_LOAD (OceanLoad3D::buildInparam, OceanLoad3D.cpp:20-52): 'none' or
         'constant$<depth km>' (OceanLoad3D_const, 3 km by default).  Solid elements on the
         surface side set give their outer points the summed side normal and the ocean depth
@@ -1006,10 +1026,10 @@ class Simulation:
         self.ocean_depth = depth
         surf = ex.side.get("r1", np.full(len(fl), -1))
         normal = {}
-        for e in np.nonzero((surf >= 0) & ~fl)[0]:
-            for k, nvec in side_normal(e, surf[e]):
-                p = int(e_pts[e, k])
-                normal[p] = normal.get(p, 0.0) + nvec  # GLLPoint::addSurfNormal
+        es = np.nonzero((surf >= 0) & ~fl)[0]
+        ks, nvs = side_normals(es, surf[es])
+        for p, nvec in zip(e_pts[es[:, None], ks].ravel().tolist(), nvs.reshape(-1, 3)):
+            normal[p] = normal.get(p, 0.0) + nvec  # GLLPoint::addSurfNormal
         pts = sorted(normal)
         if depth == 0.0 or not pts:
             return none
@@ -1299,7 +1319,9 @@ class Simulation:
 
     def _locate(self, s, z):
         """Quad::invMapping by Newton iterations (Mapping.cpp:17-28) over candidate elements."""
-        cen = self.crds.mean(1)
+        if getattr(self, "_cen_of", None) is not self.crds:  # element centres, once per mesh
+            self._cen, self._cen_of = self.crds.mean(1), self.crds
+        cen = self._cen
         order = np.argsort(np.hypot(cen[:, 0] - s, cen[:, 1] - z))
         for e in order[:64]:
             if self.fluid[e]:
