@@ -143,7 +143,10 @@ struct ax3d_domain {
     // memory policy (0: two CTAs per SM where they fit; 1: one CTA per SM, fewer clusters)
     // and side streams used; set at ax3d_finalize, changed by ax3d_autotune
     // the bucket schedule without ax3d_autotune / ax3d_set_schedule: policy 3 with merged
-    // launches (the autotuner's choice on the short-ring domains of learned Nu fields)
+    // launches.  Policy 4 (64-thread CTAs for the shortest rings) gains on learned-Nu
+    // domains with three side streams but loses on others there (concurrent persistent
+    // launches of different CTA sizes contend for the SMs: element pass of 100,000 elements
+    // at Nu 4-40 11.9 ms against 9.6 ms for this default), so it is left to the autotuner
     struct Schedule {
         double ratio = 1.12;
         int policy = 3, nside = NSIDE, merge = 1;
@@ -933,7 +936,8 @@ struct ax3d_domain {
     // ---- autotuner: the bucket schedule from timed trials on this domain's own elements ----
     // Candidates: transform-length steps between buckets {1.06, 1.12, 1.25} x shared-memory
     // policy {two CTAs per SM; one CTA per SM; two per SM for small rings and one 512-thread
-    // CTA per SM above} x side streams {1, NSIDE}.  Each trial
+    // CTA per SM above; as the last with four 128-thread CTAs per SM for short rings, and
+    // with eight 64-thread CTAs per SM for the shortest} x side streams {1, NSIDE}.  Each trial
     // times `trials` element passes (after one untimed pass) with CUDA events on the domain's
     // stream; the point stiffness and the memory variables the passes change are saved
     // before and put back after every trial.  The choice is cached per process under the
@@ -990,7 +994,7 @@ struct ax3d_domain {
         for (double ratio : {1.06, 1.12, 1.25})
             for (int policy : {0, 1, 2})
                 for (int nside : {1, (int)NSIDE}) cands.push_back(Schedule{ratio, policy, nside, 0});
-        for (int policy : {0, 2, 3})
+        for (int policy : {0, 2, 3, 4})
             for (int nside : {1, (int)NSIDE}) cands.push_back(Schedule{1.12, policy, nside, 1});
         for (int nside : {1, (int)NSIDE}) cands.push_back(Schedule{1.12, 3, nside, 0});
         for (const Schedule &sc : cands) {
@@ -1657,8 +1661,8 @@ int ax3d_enable_timers(ax3d_domain *d, int32_t enable) {
 int ax3d_set_schedule(ax3d_domain *d, double ratio, int32_t policy, int32_t nside, int32_t merge) {
     return guard([&] {
         if (!d) throw Error(AX3D_ERR_ARG, "ax3d_set_schedule || null domain");
-        if (!(ratio > 1.0 && ratio < 4.0) || policy < 0 || policy > 3 || nside < 1)
-            throw Error(AX3D_ERR_ARG, "ax3d_set_schedule || ratio in (1, 4), policy 0..3, nside >= 1");
+        if (!(ratio > 1.0 && ratio < 4.0) || policy < 0 || policy > 4 || nside < 1)
+            throw Error(AX3D_ERR_ARG, "ax3d_set_schedule || ratio in (1, 4), policy 0..4, nside >= 1");
         d->need_final();
         CK(cudaSetDevice(d->device));
         ax3d_domain::Schedule sc;

@@ -53,6 +53,7 @@ constexpr int DIRECT_MAX = 257;  // largest prime handled by a direct pass
 constexpr size_t SMEM_CAP = 227 * 1024;
 constexpr size_t SMEM_TWO = 112 * 1024;  // two CTAs per SM
 constexpr size_t SMEM_FOUR = 56 * 1024;  // four CTAs per SM
+constexpr size_t SMEM_EIGHT = 27 * 1024; // eight CTAs per SM
 constexpr int64_t PREFETCH_MAX = 1024 * 1024;  // largest per-element block asked of L2 ahead
 constexpr int CLUSTER_MAX = 8;
 constexpr int PLAN_BYTES = (sizeof(FftPlan) + 15) / 16 * 16;
@@ -950,7 +951,7 @@ __device__ __noinline__ void phase_quad(const ElemTable &T, const PointTable &P,
 // potential-gradient components (2 sequences per point).
 // ------------------------------------------------------------------------------------
 template <bool SOLID, int NTT>
-__global__ void __launch_bounds__(NTT, NTT == 128 ? 4 : NTT == 256 ? 2 : 1)
+__global__ void __launch_bounds__(NTT, NTT == 64 ? 8 : NTT == 128 ? 4 : NTT == 256 ? 2 : 1)
     k_elem_phys(const __grid_constant__ ElemTable T, const __grid_constant__ PointTable P,
                 const float2 *__restrict__ u, const int32_t *__restrict__ elems, int count, int Pc, int Lmax,
                 const __grid_constant__ PhysTables X, const __grid_constant__ SLS sls, int overwrite) {
@@ -1244,6 +1245,8 @@ void init_phys_attributes() {
     cudaFuncSetAttribute(k_elem_phys<false, 2 * NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_CAP);
     cudaFuncSetAttribute(k_elem_phys<true, NT / 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_CAP);
     cudaFuncSetAttribute(k_elem_phys<false, NT / 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_CAP);
+    cudaFuncSetAttribute(k_elem_phys<true, NT / 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_CAP);
+    cudaFuncSetAttribute(k_elem_phys<false, NT / 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_CAP);
     cudaFuncSetAttribute(k_prt3_fft<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_CAP);
     cudaFuncSetAttribute(k_prt3_fft<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_CAP);
 }
@@ -1494,10 +1497,24 @@ FftTables build_fft_tables(const std::vector<char> &used) {
 //   Policy 3: as policy 2, except that rings whose 25 points fit a quarter of an SM's shared
 //             memory take 128-thread CTAs, four per SM (16 warps per SM over four elements
 //             in flight instead of two: short rings spend most of their time in barriers).
+//   Policy 4: as policy 3, except that rings whose 25 points fit an eighth of an SM's shared
+//             memory (up to ~41 samples for a solid, ~60 for a fluid) take 64-thread CTAs,
+//             eight per SM (the same 16 warps over eight elements in flight).
 void size_phys_bucket(PhysBucket &b, bool solid, int policy) {
     const int nsq = solid ? 3 : 2;
     b.npts_chunk = 0;
     b.nt = NT;
+    if (policy == 4) {
+        const size_t sm = phys_smem_bytes(b.L_max, nsq, NPE, NT / 4);
+        if (sm <= SMEM_EIGHT) {
+            b.npts_chunk = NPE;
+            b.csize = 1;
+            b.smem = sm;
+            b.nt = NT / 4;
+            return;
+        }
+        policy = 3;
+    }
     if (policy == 3) {
         const size_t sm = phys_smem_bytes(b.L_max, nsq, NPE, NT / 2);
         if (sm <= SMEM_FOUR) {
@@ -1552,13 +1569,19 @@ cudaLaunchConfig_t phys_config(const PhysBucket &b, cudaLaunchAttribute *at, cud
     cfg.numAttrs = 1;
     return cfg;
 }
-// the instantiation of a bucket: solid or fluid, 128, 256 or 512 threads
+// the instantiation of a bucket: solid or fluid, 64, 128, 256 or 512 threads
 template <typename F>
 void with_kernel(bool solid, int nt, F f) {
     if (solid)
-        nt > NT ? f(k_elem_phys<true, 2 * NT>) : nt < NT ? f(k_elem_phys<true, NT / 2>) : f(k_elem_phys<true, NT>);
+        nt > NT        ? f(k_elem_phys<true, 2 * NT>)
+        : nt == NT / 4 ? f(k_elem_phys<true, NT / 4>)
+        : nt < NT      ? f(k_elem_phys<true, NT / 2>)
+                       : f(k_elem_phys<true, NT>);
     else
-        nt > NT ? f(k_elem_phys<false, 2 * NT>) : nt < NT ? f(k_elem_phys<false, NT / 2>) : f(k_elem_phys<false, NT>);
+        nt > NT        ? f(k_elem_phys<false, 2 * NT>)
+        : nt == NT / 4 ? f(k_elem_phys<false, NT / 4>)
+        : nt < NT      ? f(k_elem_phys<false, NT / 2>)
+                       : f(k_elem_phys<false, NT>);
 }
 }  // namespace
 

@@ -317,7 +317,8 @@ int ax3d_autotune(ax3d_domain *d, int32_t trials, char *report, size_t len);
    (0: 256-thread CTAs, two per SM where they fit; 1: 256-thread CTAs with an SM's whole
    shared memory; 2: as 0 for rings that fit two per SM, 512-thread CTAs with an SM's whole
    shared memory above; 3: as 2, with 128-thread CTAs four per SM for the rings that fit a
-   quarter of an SM's shared memory), side streams (1..3) and merge (nonzero: the buckets of one launch
+   quarter of an SM's shared memory; 4: as 3, with 64-thread CTAs eight per SM for the rings
+   that fit an eighth), side streams (1..3) and merge (nonzero: the buckets of one launch
    shape -- CTAs per cluster, threads per CTA -- run as one persistent launch over their
    elements, longest transforms first) -- and recaptures the step. */
 int ax3d_set_schedule(ax3d_domain *d, double ratio, int32_t policy, int32_t nside, int32_t merge);

@@ -352,13 +352,15 @@ def test_autotuned_schedule_keeps_results(ax3d_lib):
     assert g2.autotune(1).startswith("cached")
 
 
-@pytest.mark.parametrize("policy,merge", [(1, False), (2, False), (0, True), (2, True), (3, False), (3, True)])
+@pytest.mark.parametrize("policy,merge", [(1, False), (2, False), (0, True), (2, True), (3, False), (3, True),
+                                          (4, False), (4, True)])
 def test_schedule_policies_match_oracle(ax3d_lib, policy, merge):
     """The benchmark's domain (Nu 8-256) under the other bucket schedules: policy 1 (256-thread
     CTAs with an SM's whole shared memory), policy 2 (512-thread CTAs above the rings that
-    fit two CTAs per SM, clusters of 512-thread CTAs for the largest) and policy 3 (as 2, with
-    128-thread CTAs four per SM for the short rings), each also with the buckets of one launch
-    shape merged into one launch; compute_stiff and three steps against the oracle."""
+    fit two CTAs per SM, clusters of 512-thread CTAs for the largest), policy 3 (as 2, with
+    128-thread CTAs four per SM for the short rings) and policy 4 (as 3, with 64-thread CTAs
+    eight per SM for the shortest), each also with the buckets of one launch shape merged
+    into one launch; compute_stiff and three steps against the oracle."""
     from oracle.oracle_py import OracleDomain
     from axisem3d_gb300 import workloads as W
     from axisem3d_gb300.capi import Ax3dDomain
