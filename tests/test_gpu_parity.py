@@ -1,7 +1,7 @@
 """GPU parity: the CUDA path through the C-ABI against the CPU oracle.
 
 Tolerance: relative L2 <= 1e-5 against the FP32 oracle (the reference's default Real),
-the spec bar for floating-point parity; the FP64 oracle error is reported too.
+the parity bar for the floating-point path; the FP64 oracle error is reported too.
 """
 import numpy as np
 import pytest
