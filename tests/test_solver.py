@@ -403,6 +403,77 @@ def test_volumetric_3d_models_unit():
     np.testing.assert_allclose(M3D.linear_resampling(6, ring), [1.0, 1.5, 2.0, 2.5, 3.0, 2.0])
 
 
+class _FieldModel:
+    """A volumetric model for apply_models: a perturbation and a range that are functions of
+    the point (so any chunking of the points sees the same values)."""
+
+    def __init__(self, prop, ref, fluid, frac, seed):
+        self.prop, self.ref, self.fluid, self.frac, self.seed = prop, ref, fluid, frac, seed
+
+    def evaluate(self, xyz):
+        x, y, z = xyz[..., 0], xyz[..., 1], xyz[..., 2]
+        val = 0.05 * np.sin(1e-6 * (x + 2 * y + 3 * z) + self.seed) + (3000.0 if self.ref == 0 else 0.0)
+        inr = 0.5 * (np.sin(1e-5 * (1.3 * x + 0.7 * y - z) + 2 * self.seed) + 1) < self.frac
+        return val, inr
+
+
+def _apply_models_dense(models, props1d, crds, nr, fluid):
+    """Material::addVolumetric3D on dense (n, nr, 25) float64 copies of every property, model
+    after model (Volumetric3D reference kinds: absolute, Ref1D, Ref3D, reference difference)."""
+    n = len(crds)
+    phi = 2 * np.pi * np.arange(nr) / nr
+    s, z = crds[..., 0], crds[..., 1]
+    xyz = np.stack([s[:, None, :] * np.cos(phi)[None, :, None], s[:, None, :] * np.sin(phi)[None, :, None],
+                    np.broadcast_to(z[:, None, :], (n, nr, 25))], -1)
+    cur = {k: np.repeat(v[:, None, :], nr, 1).astype(float) for k, v in props1d.items()}
+    touched = np.zeros(n, bool)
+    for m in models:
+        val, inr = m.evaluate(xyz)
+        if not m.fluid:
+            inr = inr & ~fluid[:, None, None]
+        touched |= inr.any((1, 2))
+        x1, x = props1d[m.prop][:, None, :], cur[m.prop]
+        new = {0: np.broadcast_to(val, x.shape), 1: x1 * (1.0 + val), 2: x * (1.0 + val),
+               3: (x - x1) * (1.0 + val) + x1}[m.ref]
+        cur[m.prop] = np.where(inr, new, x)
+    return {k: v.astype(np.float32) for k, v in cur.items()}, touched
+
+
+@pytest.mark.parametrize("n,nr", [(7, 5), (31, 13), (4000, 30)])
+def test_apply_models_matches_dense_restatement(n, nr):
+    """model3d.apply_models keeps a property no model changes as its 1-D row (a read-only
+    broadcast view), applies perturbations in place and works in chunks of ~2M samples; its
+    values equal, bit for bit, the dense restatement above for every reference kind, models
+    with and without fluid, partial ranges and (at n = 4000, nr = 30) chunks."""
+    from axisem3d_gb300 import model3d as M3D
+    rng = np.random.default_rng(n)
+    props = {k: rng.uniform(1000.0, 9000.0, (n, 25)) for k in ("VP", "VS", "RHO")}
+    crds = rng.uniform(0.0, 6e6, (n, 25, 2))
+    fluid = rng.random(n) < 0.3
+    for trial in range(8):
+        models = [_FieldModel(str(rng.choice(["VP", "VS", "RHO"])), int(rng.integers(0, 4)), bool(rng.random() < 0.5),
+                              float(rng.choice([0.0, 0.3, 1.0])), 10 * trial + i) for i in range(int(rng.integers(1, 4)))]
+        got, t_got = M3D.apply_models(models, props, crds, nr, fluid)
+        want, t_want = _apply_models_dense(models, props, crds, nr, fluid)
+        np.testing.assert_array_equal(t_got, t_want)
+        for k in want:
+            assert got[k].shape == want[k].shape and got[k].dtype == np.float32
+            np.testing.assert_array_equal(got[k], want[k])
+            if not any(m.prop == k for m in models):
+                assert got[k].strides[1] == 0  # left as the broadcast 1-D row
+        assert solver._varies(got["RHO"]).tolist() == (want["RHO"].max(1) != want["RHO"].min(1)).any(1).tolist()
+
+
+def test_point_numbering_matches_unique_rows(small_inputs):
+    """The unique-point numbering of the build (one lexsort of the rounded coordinates)
+    equals np.unique's row order, so the points keep their numbers."""
+    sim = solver.Simulation(small_inputs)
+    sim.build()
+    key = np.round(sim.crds.reshape(-1, 2) / 1e-3).astype(np.int64)
+    _, inv = np.unique(key, axis=0, return_inverse=True)
+    np.testing.assert_array_equal(sim.e_pts.ravel(), inv.ravel())
+
+
 def test_unknown_volumetric_model_raises(tmp_path):
     d = solver.write_inputs(tmp_path / "input", mesh_kw=SMALL_MESH, steps=10, models3d=("s20rts",))
     with pytest.raises(NotImplementedError):
