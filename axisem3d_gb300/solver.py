@@ -9,6 +9,7 @@ Pre-computation is FP64 (geometry, materials, masses, normals, source, receivers
 """
 from __future__ import annotations
 
+import functools
 import math
 from dataclasses import dataclass
 from pathlib import Path
@@ -227,6 +228,46 @@ def _varies(a):
     if a.strides[1] == 0:
         return np.zeros(len(a), bool)
     return (a.max(1) != a.min(1)).any(1)
+
+
+def closest_gll_distance(crds):
+    """XMath::findClosestDist over each element's 25 GLL points, crds (E, 25, 2): the
+    smallest distance between two of them.  Every pair once, point-major for contiguous
+    gathers; the distance (hypot) is taken only for the pairs whose squared distance is within
+    1e-9 of the element's smallest, which always holds the closest pair."""
+    pa, pb = np.triu_indices(25, 1)
+    T = np.ascontiguousarray(np.asarray(crds, float).transpose(1, 2, 0))
+    D = T[pa] - T[pb]
+    d2 = D[:, 0] * D[:, 0] + D[:, 1] * D[:, 1]
+    pr, pe = np.nonzero(d2 <= d2.min(0) * (1 + 1e-9))
+    out = np.full(T.shape[2], np.inf)
+    np.minimum.at(out, pe, np.hypot(D[pr, 0, pe], D[pr, 1, pe]))
+    return out
+
+
+def boundary_normals(nodes, crds, jac0, axial_e, co, es, sides):
+    """Quad::computeNormal (Quad.cpp:661-715) without relabelling, for the five points of side
+    sides[i] of element es[i]: local indices (n, 5) and normals (n, 5, 3).  nodes (E, 2, 4),
+    crds (E, 25, 2), jac0 the (E, 5, 5) first Jacobian entry, co the curved side per element."""
+    wg, wjw, xj = S.gll()[1], S.glj()[1], S.glj()[0]
+    es, sides = np.asarray(es, np.int64), np.asarray(sides, np.int64)
+    n0, n1 = nodes[es, :, sides], nodes[es, :, (sides + 1) % 4]
+    r0, r1 = np.hypot(n0[:, 0], n0[:, 1]), np.hypot(n1[:, 0], n1[:, 1])
+    dth = np.abs(np.array([_colat(*b) - _colat(*a) for a, b in zip(n0, n1)]))
+    rsf = 0.5 * (r0 + r1)
+    h_r_dt, h_r2_dt = (0.5 * rsf * dth)[:, None], (0.5 * rsf * rsf * dth)[:, None]
+    ip, jp = _SIDE_IP[sides], _SIDE_JP[sides]
+    k = ip * 5 + jp
+    sz = crds[es[:, None], k]
+    rr = np.hypot(sz[..., 0], sz[..., 1])
+    sint, cost = sz[..., 0] / rr, sz[..., 1] / rr
+    ax = np.asarray(axial_e, bool)[es][:, None]
+    wsf = np.where(np.isin(sides, (0, 2))[:, None], np.where(ax, wjw[ip], wg[ip]), wg[jp])
+    with np.errstate(divide="ignore", invalid="ignore"):
+        fac = np.where(~ax, wsf * sint * h_r2_dt,
+                       np.where(ip == 0, wsf * jac0[es[:, None], ip, jp] * h_r_dt, wsf / (1 + xj[ip]) * sint * h_r2_dt))
+    nv = np.stack([sint, np.zeros_like(sint), cost], -1) * fac[..., None]
+    return k, np.where((sides != np.asarray(co)[es])[:, None, None], -nv, nv)
 
 
 # the five points of each element side in GLL index order: (ip, jp) with jp = 0 (side 0),
@@ -634,29 +675,7 @@ class Simulation:
         sfn = np.zeros((P, 3))
         sfn3 = {}  # undulated boundary: normals per slice (Quad::computeNormal with getSFNormalRTZ)
         sfside = ex.side.get("solid_fluid_boundary", np.full(E, -1))
-        wg, wjw = S.gll()[1], S.glj()[1]
-        def side_normals(es, sides):
-            """Quad::computeNormal (Quad.cpp:661-715) without relabelling, for the five points
-            of side sides[i] of element es[i]: local indices (n, 5) and normals (n, 5, 3)."""
-            es, sides = np.asarray(es, np.int64), np.asarray(sides, np.int64)
-            n0, n1 = nodes[es, :, sides], nodes[es, :, (sides + 1) % 4]
-            r0, r1 = np.hypot(n0[:, 0], n0[:, 1]), np.hypot(n1[:, 0], n1[:, 1])
-            dth = np.abs(np.array([_colat(*b) - _colat(*a) for a, b in zip(n0, n1)]))
-            rsf = 0.5 * (r0 + r1)
-            h_r_dt, h_r2_dt = (0.5 * rsf * dth)[:, None], (0.5 * rsf * rsf * dth)[:, None]
-            ip, jp = _SIDE_IP[sides], _SIDE_JP[sides]
-            k = ip * 5 + jp
-            sz = crds[es[:, None], k]
-            rr = np.hypot(sz[..., 0], sz[..., 1])
-            sint, cost = sz[..., 0] / rr, sz[..., 1] / rr
-            ax = axial_e[es][:, None]
-            wsf = np.where(np.isin(sides, (0, 2))[:, None], np.where(ax, wjw[ip], wg[ip]), wg[jp])
-            with np.errstate(divide="ignore", invalid="ignore"):
-                fac = np.where(~ax, wsf * sint * h_r2_dt,
-                               np.where(ip == 0, wsf * jac[0][es[:, None], ip, jp] * h_r_dt,
-                                        wsf / (1 + xj[ip]) * sint * h_r2_dt))
-            nv = np.stack([sint, np.zeros_like(sint), cost], -1) * fac[..., None]
-            return k, np.where((sides != co[es])[:, None, None], -nv, nv)
+        side_normals = functools.partial(boundary_normals, nodes, crds, jac[0], axial_e, co)
 
         sf_e = np.nonzero(sfside >= 0)[0]
         sf_k, sf_nv = side_normals(sf_e, sfside[sf_e])
@@ -690,16 +709,7 @@ class Simulation:
         hmin_edge = np.hypot(*(xy4 - np.roll(xy4, -1, axis=1)).transpose(2, 0, 1)).min(1)
         vmax_ref = np.maximum(ex.nodal["VPV"], ex.nodal["VPH"]).max(1)
         courant = ex.dt.astype(float) * vmax_ref / hmin_edge
-        # every pair of an element's GLL points once, point-major for contiguous gathers; the
-        # distance (hypot) is taken only for the pairs whose squared distance is within 1e-9 of
-        # the element's smallest, which always holds the closest pair
-        pa, pb = np.triu_indices(25, 1)
-        T = np.ascontiguousarray(crds.transpose(1, 2, 0))
-        D = T[pa] - T[pb]
-        d2 = D[:, 0] * D[:, 0] + D[:, 1] * D[:, 1]
-        pr, pe = np.nonzero(d2 <= d2.min(0) * (1 + 1e-9))
-        hmin_gll = np.full(E, np.inf)
-        np.minimum.at(hmin_gll, pe, np.hypot(D[pr, 0, pe], D[pr, 1, pe]))
+        hmin_gll = closest_gll_distance(crds)
         vmax_1d = np.maximum(mat["VPV"], mat["VPH"]).max(1)
         vmax_e = np.where(e3d, vp_max3, vmax_1d)  # the slice maximum: 3-D elements' largest slice
         dt_e = courant * hmin_gll / vmax_e

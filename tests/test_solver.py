@@ -474,6 +474,70 @@ def test_point_numbering_matches_unique_rows(small_inputs):
     np.testing.assert_array_equal(sim.e_pts.ravel(), inv.ravel())
 
 
+def _normal_pointwise(nodes, crds, jac0, axial, co, e, side):
+    """Quad::computeNormal (Quad.cpp:661-715) point by point: (local index, normal) of the
+    five points on side `side` of element e."""
+    from axisem3d_gb300 import spectral as S
+    wg, wjw, xj = S.gll()[1], S.glj()[1], S.glj()[0]
+    n0, n1 = nodes[e][:, side], nodes[e][:, (side + 1) % 4]
+    r0, t0 = np.hypot(*n0), solver._colat(*n0)
+    r1, t1 = np.hypot(*n1), solver._colat(*n1)
+    rsf = 0.5 * (r0 + r1)
+    h_r_dt, h_r2_dt = 0.5 * rsf * abs(t1 - t0), 0.5 * rsf * rsf * abs(t1 - t0)
+    out = []
+    for ip in range(5):
+        for jp in range(5):
+            if not ((side == 0 and jp == 0) or (side == 1 and ip == 4) or (side == 2 and jp == 4) or
+                    (side == 3 and ip == 0)):
+                continue
+            k = ip * 5 + jp
+            rr = np.hypot(*crds[e, k])
+            sint, cost = crds[e, k, 0] / rr, crds[e, k, 1] / rr
+            nvec = np.array([sint, 0.0, cost])
+            wsf = (wjw if axial[e] else wg)[ip] if side in (0, 2) else wg[jp]
+            if axial[e]:
+                nvec *= wsf * jac0[e, ip, jp] * h_r_dt if ip == 0 else wsf / (1 + xj[ip]) * sint * h_r2_dt
+            else:
+                nvec *= wsf * sint * h_r2_dt
+            out.append((k, -nvec if side != co[e] else nvec))
+    return out
+
+
+def test_boundary_normals_match_pointwise(small_inputs):
+    """solver.boundary_normals (all boundary sides at once) equals the point-by-point
+    Quad::computeNormal on the solid-fluid and the surface sides of the coarse mesh, bit for
+    bit, axial elements included."""
+    sim = solver.Simulation(small_inputs)
+    sim.build()
+    ex = sim.ex
+    checked = 0
+    for name in ("solid_fluid_boundary", "r1"):
+        sides = ex.side.get(name)
+        if sides is None:
+            continue
+        es = np.nonzero(sides >= 0)[0]
+        ks, nvs = solver.boundary_normals(sim.nodes4, sim.crds, sim.jac[0], sim.axial_e, sim.co, es, sides[es])
+        for i, e in enumerate(es):
+            want = _normal_pointwise(sim.nodes4, sim.crds, sim.jac[0], sim.axial_e, sim.co, e, sides[e])
+            assert ks[i].tolist() == [k for k, _ in want]
+            np.testing.assert_array_equal(nvs[i], np.array([v for _, v in want]))
+            checked += 1
+    assert checked > 0 and sim.axial_e[np.nonzero(ex.side["r1"] >= 0)[0]].any()
+
+
+def test_closest_gll_distance_is_the_smallest_pair():
+    """solver.closest_gll_distance (squared distances, hypot on the near-minimal pairs only)
+    equals the smallest hypot over all 300 pairs of each element's GLL points."""
+    rng = np.random.default_rng(4)
+    base = np.stack(np.meshgrid(np.linspace(0, 1, 5), np.linspace(0, 1, 5), indexing="ij"), -1).reshape(25, 2)
+    crds = base[None] * rng.uniform(1e4, 1e5, (200, 1, 1)) + rng.normal(0, 3e3, (200, 25, 2)) + rng.uniform(0, 6e6, (200, 1, 2))
+    crds[:5] = crds[:5, :1]  # coincident points: distance 0
+    crds[5:10, 7] = crds[5:10, 3]
+    pa, pb = np.triu_indices(25, 1)
+    want = np.hypot(crds[:, pa, 0] - crds[:, pb, 0], crds[:, pa, 1] - crds[:, pb, 1]).min(1)
+    np.testing.assert_array_equal(solver.closest_gll_distance(crds), want)
+
+
 def test_unknown_volumetric_model_raises(tmp_path):
     d = solver.write_inputs(tmp_path / "input", mesh_kw=SMALL_MESH, steps=10, models3d=("s20rts",))
     with pytest.raises(NotImplementedError):
