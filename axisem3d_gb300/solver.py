@@ -511,7 +511,6 @@ class Simulation:
         pcrd[np.abs(pcrd[:, 0]) < 1e-6, 0] = 0.0
         mat = self._gll_material(ex, axial_e)
         vp, vs, rho = mat["VP"], mat["VS"], mat["RHO"]
-        xj = S.glj()[0]
         fl = ex.fluid
         # Nr field (NrField::buildInparam, NrField.cpp:20-64) with Quad::formNrField's limits;
         # point coordinates rounded as formNrField does (offset = min(1e-5, distTol / 1e3))
