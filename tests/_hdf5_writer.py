@@ -1,8 +1,9 @@
 """Test infrastructure: a minimal writer of the HDF5 subset `axisem3d_gb300.hdf5` reads
 (version 0 superblock, one root group held in a symbol table, version 1 object headers,
-contiguous datasets and chunked datasets with the deflate filter), so that the reader is
-exercised without an HDF5 library or an external file.  Written from the published HDF5
-format specification; little-endian int32 / float64 and one-byte strings only."""
+compact and contiguous datasets, chunked datasets through the shuffle, deflate and
+Fletcher-32 filters), so that the reader is exercised without an HDF5 library or an
+external file.  Written from the published HDF5 format specification; little-endian int32 /
+float64 and one-byte strings only."""
 from __future__ import annotations
 
 import struct
@@ -38,8 +39,43 @@ def _datatype(a: np.ndarray) -> bytes:
     raise ValueError(f"unsupported dtype {a.dtype}")
 
 
+def _fletcher32(b: bytes) -> int:
+    """Fletcher-32 over little-endian 16-bit words (an odd last byte padded with zero)."""
+    if len(b) % 2:
+        b += b"\0"
+    s1 = s2 = 0
+    for (w,) in struct.iter_unpack("<H", b):
+        s1 = (s1 + w) % 65535
+        s2 = (s2 + s1) % 65535
+    return (s2 << 16) | s1
+
+
+def _filter_message(filters, itemsize) -> bytes:
+    """Filter pipeline message, version 1: (id, name length 0, flags 0, client values)."""
+    ids = {"shuffle": (2, [itemsize]), "deflate": (1, [6]), "fletcher32": (3, [])}
+    body = b""
+    for f in filters:
+        fid, vals = ids[f]
+        body += struct.pack("<HHHH", fid, 0, 0, len(vals)) + b"".join(struct.pack("<I", v) for v in vals)
+        body += b"\0" * (4 * (len(vals) % 2))
+    return struct.pack("<BB6x", 1, len(filters)) + body
+
+
+def _apply_filters(raw: bytes, filters, itemsize) -> bytes:
+    for f in filters:
+        if f == "shuffle":
+            raw = np.frombuffer(raw, np.uint8).reshape(-1, itemsize).T.tobytes()
+        elif f == "deflate":
+            raw = zlib.compress(raw)
+        else:
+            raw = raw + struct.pack("<I", _fletcher32(raw))
+    return raw
+
+
 def write(path, datasets: dict):
-    """datasets: name -> array, or (array, chunk shape) for a chunked, deflated dataset."""
+    """datasets: name -> array (contiguous), (array, "compact"), (array, chunk shape) for a
+    chunked, deflated dataset, or (array, chunk shape, filters) with filters a sequence of
+    "shuffle", "deflate" and "fletcher32" in the order they are applied."""
     out = bytearray(b"\0" * 96)  # superblock, written last
     names = sorted(datasets)
     # local heap data: "" at offset 0, then the names, each padded to 8 bytes
@@ -59,13 +95,16 @@ def write(path, datasets: dict):
     heap_addr = put(b"HEAP" + bytes([0, 0, 0, 0]) + struct.pack("<QQQ", len(heap_data), UNDEF, heap_data_addr))
     ohdr = {}
     for n in names:
-        spec = datasets[n]
-        a, chunks = (spec if isinstance(spec, tuple) else (spec, None))
+        spec = datasets[n] if isinstance(datasets[n], tuple) else (datasets[n],)
+        a, chunks = spec[0], (spec[1] if len(spec) > 1 else None)
+        filters = spec[2] if len(spec) > 2 else ("deflate",)
         a = np.ascontiguousarray(a)
         nd = a.ndim
         space = struct.pack("<BBBB4x", 1, nd, 0, 0) + b"".join(struct.pack("<Q", d) for d in a.shape)
         msgs = [_msg(0x01, space), _msg(0x03, _datatype(a))]
-        if chunks is None:
+        if chunks == "compact":
+            msgs.append(_msg(0x08, struct.pack("<BBH", 3, 0, a.nbytes) + a.tobytes()))
+        elif chunks is None:
             addr = put(a.tobytes())
             msgs.append(_msg(0x08, struct.pack("<BBQQ", 3, 1, addr, a.nbytes)))
         else:
@@ -75,7 +114,7 @@ def write(path, datasets: dict):
                 block = np.zeros(chunks, a.dtype)
                 sl = tuple(slice(o, min(o + c, s)) for o, c, s in zip(corner, chunks, a.shape))
                 block[tuple(slice(0, x.stop - x.start) for x in sl)] = a[sl]
-                raw = zlib.compress(block.tobytes())
+                raw = _apply_filters(block.tobytes(), filters, a.itemsize)
                 keys.append((len(raw), corner, put(raw)))
             node = bytearray(b"TREE" + bytes([1, 0]) + struct.pack("<HQQ", len(keys), UNDEF, UNDEF))
             for size, corner, addr in keys:
@@ -85,7 +124,7 @@ def write(path, datasets: dict):
             bt = put(bytes(node))
             msgs.append(_msg(0x08, struct.pack("<BBBQ", 3, 2, nd + 1, bt) +
                              b"".join(struct.pack("<I", c) for c in chunks) + struct.pack("<I", a.itemsize)))
-            msgs.append(_msg(0x0B, struct.pack("<BB6x", 1, 1) + struct.pack("<HHHHI4x", 1, 0, 0, 1, 6)))
+            msgs.append(_msg(0x0B, _filter_message(filters, a.itemsize)))
         ohdr[n] = put(_ohdr(msgs))
     snod = bytearray(b"SNOD" + bytes([1, 0]) + struct.pack("<H", len(names)))
     for n in names:

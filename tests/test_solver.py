@@ -1251,8 +1251,9 @@ def test_gpu_gaussian_random_sampling_matches_host(ax3d_lib):
 
 def test_hdf5_reader_on_a_written_file(tmp_path):
     """The HDF5 reader on a file written by the test's own minimal HDF5 writer: contiguous
-    int32 / float64 / one-byte-string datasets and chunked, deflated datasets with edge
-    chunks come back exact through netcdf.read."""
+    int32 / float64 / one-byte-string datasets, a compact dataset and chunked datasets with
+    edge chunks through deflate, shuffle + deflate and shuffle + deflate + Fletcher-32 come
+    back exact through netcdf.read."""
     from tests import _hdf5_writer as W
     rng = np.random.default_rng(5)
     conn = rng.integers(1, 2000, (37, 4)).astype("<i4")
@@ -1261,11 +1262,17 @@ def test_hdf5_reader_on_a_written_file(tmp_path):
     names = np.zeros((3, 33), "S1")
     for i, s in enumerate(("r1", "solid_fluid_boundary", "t0")):
         names[i, :len(s)] = np.frombuffer(s.encode(), "S1")
+    small = rng.integers(-5, 5, 7).astype("<i4")
     W.write(tmp_path / "m.e", {"connect1": (conn, (16, 4)), "coordx": crd, "ss_names": names,
-                               "vals": (vals, (2, 8))})
+                               "vals": (vals, (2, 8)), "coordy": (crd[::-1].copy(), (32,), ("shuffle", "deflate")),
+                               "coordz": (crd * 2, (40,), ("shuffle", "deflate", "fletcher32")),
+                               "eb_prop1": (small, "compact")})
     ds = NC.read(tmp_path / "m.e")
     np.testing.assert_array_equal(ds["connect1"], conn)
     np.testing.assert_array_equal(ds["coordx"], crd)
+    np.testing.assert_array_equal(ds["coordy"], crd[::-1])
+    np.testing.assert_array_equal(ds["coordz"], crd * 2)
+    np.testing.assert_array_equal(ds["eb_prop1"], small)
     np.testing.assert_array_equal(ds["vals"], vals)
     assert ds.strings("ss_names") == ["r1", "solid_fluid_boundary", "t0"]
     assert ds.attrs["unread_datasets"] == []
