@@ -72,10 +72,33 @@ def _apply_filters(raw: bytes, filters, itemsize) -> bytes:
     return raw
 
 
-def write(path, datasets: dict):
+def _chunk_key(size, corner) -> bytes:
+    return struct.pack("<II", size, 0) + b"".join(struct.pack("<Q", int(o)) for o in corner) + struct.pack("<Q", 0)
+
+
+def _chunk_tree(keys, shape, put, fanout) -> int:
+    """Version 1 B-tree of chunks: one leaf node, or (fanout > 0) leaves of at most fanout
+    chunks under a level-1 root; returns the root's address."""
+    end = _chunk_key(0, shape)
+
+    def node(level, entries):
+        b = bytearray(b"TREE" + bytes([1, level]) + struct.pack("<HQQ", len(entries), UNDEF, UNDEF))
+        for key, addr in entries:
+            b += key + struct.pack("<Q", addr)
+        return bytes(b + end)
+    leaf_entries = [(_chunk_key(size, corner), addr) for size, corner, addr in keys]
+    if not fanout or len(leaf_entries) <= fanout:
+        return put(node(0, leaf_entries))
+    leaves = [leaf_entries[i:i + fanout] for i in range(0, len(leaf_entries), fanout)]
+    return put(node(1, [(lf[0][0], put(node(0, lf))) for lf in leaves]))
+
+
+def write(path, datasets: dict, fanout: int = 0, continuation: bool = False):
     """datasets: name -> array (contiguous), (array, "compact"), (array, chunk shape) for a
     chunked, deflated dataset, or (array, chunk shape, filters) with filters a sequence of
-    "shuffle", "deflate" and "fletcher32" in the order they are applied."""
+    "shuffle", "deflate" and "fletcher32" in the order they are applied.  fanout > 0: chunk
+    B-trees of two levels, at most fanout chunks per leaf; continuation: every dataset's
+    object header keeps its first two messages and continues in a second block."""
     out = bytearray(b"\0" * 96)  # superblock, written last
     names = sorted(datasets)
     # local heap data: "" at offset 0, then the names, each padded to 8 bytes
@@ -116,16 +139,18 @@ def write(path, datasets: dict):
                 block[tuple(slice(0, x.stop - x.start) for x in sl)] = a[sl]
                 raw = _apply_filters(block.tobytes(), filters, a.itemsize)
                 keys.append((len(raw), corner, put(raw)))
-            node = bytearray(b"TREE" + bytes([1, 0]) + struct.pack("<HQQ", len(keys), UNDEF, UNDEF))
-            for size, corner, addr in keys:
-                node += struct.pack("<II", size, 0) + b"".join(struct.pack("<Q", int(o)) for o in corner)
-                node += struct.pack("<Q", 0) + struct.pack("<Q", addr)
-            node += struct.pack("<II", 0, 0) + b"".join(struct.pack("<Q", s) for s in a.shape) + struct.pack("<Q", 0)
-            bt = put(bytes(node))
+            bt = _chunk_tree(keys, a.shape, put, fanout)
             msgs.append(_msg(0x08, struct.pack("<BBBQ", 3, 2, nd + 1, bt) +
                              b"".join(struct.pack("<I", c) for c in chunks) + struct.pack("<I", a.itemsize)))
             msgs.append(_msg(0x0B, _filter_message(filters, a.itemsize)))
-        ohdr[n] = put(_ohdr(msgs))
+        if continuation and len(msgs) > 2:
+            rest = b"".join(msgs[2:])
+            caddr = put(rest)
+            cont = _msg(0x10, struct.pack("<QQ", caddr, len(rest)))
+            body = b"".join(msgs[:2]) + cont
+            ohdr[n] = put(struct.pack("<BBHII4x", 1, 0, len(msgs) + 1, 1, len(body)) + body)
+        else:
+            ohdr[n] = put(_ohdr(msgs))
     snod = bytearray(b"SNOD" + bytes([1, 0]) + struct.pack("<H", len(names)))
     for n in names:
         snod += struct.pack("<QQII16x", offs[n], ohdr[n], 0, 0)

@@ -1276,6 +1276,14 @@ def test_hdf5_reader_on_a_written_file(tmp_path):
     np.testing.assert_array_equal(ds["vals"], vals)
     assert ds.strings("ss_names") == ["r1", "solid_fluid_boundary", "t0"]
     assert ds.attrs["unread_datasets"] == []
+    # two-level chunk B-trees (3 chunks per leaf) and object headers in two blocks
+    big = rng.normal(size=(50, 7)).astype("<f8")
+    W.write(tmp_path / "m2.e", {"vals": (big, (4, 3), ("shuffle", "deflate")), "connect1": (conn, (5, 4)),
+                                "coordx": crd}, fanout=3, continuation=True)
+    ds = NC.read(tmp_path / "m2.e")
+    np.testing.assert_array_equal(ds["vals"], big)
+    np.testing.assert_array_equal(ds["connect1"], conn)
+    np.testing.assert_array_equal(ds["coordx"], crd)
 
 
 def test_geographic_ellipticity_mode(tmp_path):
